@@ -1,0 +1,587 @@
+// capi.cu -- the C ABI of libenkfg (declared in include/enkfg.h).
+#include "internal.cuh"
+#include <stdarg.h>
+#include <stdlib.h>
+#include <math.h>
+
+enkfg_status upload_obs_coords(enkfg_ctx* ctx, const float* lon, const float* lat, cudaStream_t st);
+enkfg_status upload_query_coords(enkfg_ctx* ctx, const enkfg_grid* g, cudaStream_t st);
+
+void set_err(enkfg_ctx* c, const char* fmt, ...)
+{
+    if (!c) return;
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(c->err, sizeof(c->err), fmt, ap);
+    va_end(ap);
+}
+
+enkfg_status cuda_fail(enkfg_ctx* c, cudaError_t e, const char* what, int line)
+{
+    set_err(c, "CUDA error in %s (line %d): %s", what, line, cudaGetErrorString(e));
+    if (e == cudaErrorMemoryAllocation) return ENKFG_ENOMEM;
+    return ENKFG_ECUDA;
+}
+
+#define NEED(cond, code, ...)                \
+    do {                                     \
+        if (!(cond)) {                       \
+            set_err(ctx, __VA_ARGS__);       \
+            return code;                     \
+        }                                    \
+    } while (0)
+
+#define SETDEV() CK(cudaSetDevice(ctx->device))
+
+static cudaStream_t pick(enkfg_ctx* ctx, void* stream)
+{
+    return stream ? (cudaStream_t)stream : ctx->stream;
+}
+
+extern "C" {
+
+ENKFG_API int enkfg_version(void)
+{
+    return ENKFG_VERSION;
+}
+
+ENKFG_API const char* enkfg_status_string(enkfg_status st)
+{
+    switch (st) {
+    case ENKFG_OK: return "ok";
+    case ENKFG_EINVAL: return "invalid argument";
+    case ENKFG_ECUDA: return "CUDA error";
+    case ENKFG_ENOMEM: return "out of device memory";
+    case ENKFG_ETIMEOUT: return "device wait timed out";
+    case ENKFG_ENUMERIC: return "numerical failure";
+    case ENKFG_ECAPACITY: return "capacity exceeded";
+    case ENKFG_ESTATE: return "required inputs not set";
+    case ENKFG_EUNSUPPORTED: return "unsupported option";
+    }
+    return "unknown status";
+}
+
+ENKFG_API const char* enkfg_last_error(const enkfg_ctx* ctx)
+{
+    return ctx ? ctx->err : "no context";
+}
+
+ENKFG_API enkfg_status enkfg_create(int device, enkfg_ctx** out)
+{
+    if (!out) return ENKFG_EINVAL;
+    *out = nullptr;
+    int n = 0;
+    cudaError_t e = cudaGetDeviceCount(&n);
+    if (e != cudaSuccess || device < 0 || device >= n) {
+        cudaGetLastError();
+        return e != cudaSuccess ? ENKFG_ECUDA : ENKFG_EINVAL;
+    }
+    if (cudaSetDevice(device) != cudaSuccess) return ENKFG_ECUDA;
+    enkfg_ctx* ctx = (enkfg_ctx*)calloc(1, sizeof(enkfg_ctx));
+    if (!ctx) return ENKFG_ENOMEM;
+    ctx->device = device;
+    if (cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess) {
+        free(ctx);
+        return ENKFG_ECUDA;
+    }
+    for (int k = 0; k < 8; ++k) cudaEventCreate(&ctx->ev[k]);
+    if (cudaMalloc(&ctx->d_qhead, 1024 * sizeof(int)) != cudaSuccess ||
+        cudaMalloc(&ctx->d_rfac, ENKFG_MAXTYPES * sizeof(double)) != cudaSuccess) {
+        enkfg_destroy(ctx);
+        return ENKFG_ENOMEM;
+    }
+    *out = ctx;
+    return ENKFG_OK;
+}
+
+ENKFG_API void enkfg_destroy(enkfg_ctx* ctx)
+{
+    if (!ctx) return;
+    cudaSetDevice(ctx->device);
+    cudaStreamSynchronize(ctx->stream);
+    void* ptrs[] = { ctx->d_lon, ctx->d_lat, ctx->d_type, ctx->d_status, ctx->d_estd, ctx->d_value, ctx->d_rfac,
+                     ctx->d_S, ctx->d_s, ctx->d_std, ctx->d_types, ctx->d_bstart, ctx->d_bfill, ctx->d_key,
+                     ctx->d_sid, ctx->d_sx, ctx->d_sy, ctx->d_sz, ctx->d_stype, ctx->d_St, ctx->d_ss, ctx->d_ox,
+                     ctx->d_oy, ctx->d_oz, ctx->d_qx, ctx->d_qy, ctx->d_qz, ctx->d_T, ctx->d_w, ctx->d_T64,
+                     ctx->d_w64, ctx->d_nlobs, ctx->d_dfs, ctx->d_srf, ctx->d_pnlobs, ctx->d_pdfs, ctx->d_psrf,
+                     ctx->d_counts, ctx->d_order, ctx->d_qhead, ctx->d_status_pt, ctx->d_scratch,
+                     ctx->d_numlevels, ctx->d_fields, ctx->d_infl };
+    for (size_t k = 0; k < sizeof(ptrs) / sizeof(ptrs[0]); ++k)
+        if (ptrs[k]) cudaFree(ptrs[k]);
+    for (int k = 0; k < 8; ++k)
+        if (ctx->ev[k]) cudaEventDestroy(ctx->ev[k]);
+    if (ctx->stream) cudaStreamDestroy(ctx->stream);
+    free(ctx);
+}
+
+ENKFG_API long long enkfg_kernel_launches(const enkfg_ctx* ctx)
+{
+    return ctx ? ctx->launches : 0;
+}
+
+ENKFG_API enkfg_status enkfg_stage_times(const enkfg_ctx* ctx, float* ms4)
+{
+    if (!ctx || !ms4) return ENKFG_EINVAL;
+    for (int k = 0; k < 4; ++k) ms4[k] = ctx->stage_ms[k];
+    return ENKFG_OK;
+}
+
+ENKFG_API enkfg_status enkfg_set_obstypes(enkfg_ctx* ctx, int ntypes, const int* nlocrad, const double* locrad,
+                                          const double* locweight, const double* rfactor, int geographic)
+{
+    if (!ctx) return ENKFG_EINVAL;
+    NEED(ntypes >= 1 && ntypes <= ENKFG_MAXTYPES, ENKFG_EINVAL, "ntypes = %d out of range 1..%d", ntypes,
+         ENKFG_MAXTYPES);
+    NEED(nlocrad && locrad, ENKFG_EINVAL, "nlocrad/locrad are required");
+    for (int t = 0; t < ntypes; ++t) {
+        NEED(nlocrad[t] >= 1 && nlocrad[t] <= ENKFG_MAXLOCRAD, ENKFG_EINVAL, "type %d: nlocrad = %d", t, nlocrad[t]);
+        ctx->nlocrad[t] = nlocrad[t];
+        for (int k = 0; k < ENKFG_MAXLOCRAD; ++k) {
+            double r = locrad[t * ENKFG_MAXLOCRAD + k];
+            double w = locweight ? locweight[t * ENKFG_MAXLOCRAD + k] : 1.0;
+            if (k < nlocrad[t]) NEED(r > 0.0 && isfinite(r), ENKFG_EINVAL, "type %d: locrad[%d] = %g", t, k, r);
+            ctx->locrad[t][k] = k < nlocrad[t] ? r : 0.0;
+            ctx->locweight[t][k] = k < nlocrad[t] ? w : 0.0;
+        }
+        ctx->rfactor[t] = rfactor ? rfactor[t] : 1.0;
+    }
+    if (ctx->types_set && (ctx->ntypes != ntypes || ctx->geographic != (geographic ? 1 : 0))) ctx->obs_set = false;
+    ctx->ntypes = ntypes;
+    ctx->geographic = geographic ? 1 : 0;
+    ctx->types_set = true;
+    ctx->index_valid = false;
+    ctx->gather_valid = false;
+    return ENKFG_OK;
+}
+
+ENKFG_API enkfg_status enkfg_set_obs(enkfg_ctx* ctx, int nobs, const float* lon, const float* lat, const short* type,
+                                     const short* status, const float* estd, const float* value)
+{
+    if (!ctx) return ENKFG_EINVAL;
+    NEED(ctx->types_set, ENKFG_ESTATE, "enkfg_set_obstypes must come first");
+    NEED(nobs >= 0 && lon && lat && type && status, ENKFG_EINVAL, "bad observation arrays");
+    for (int o = 0; o < nobs; ++o)
+        NEED(type[o] >= 0 && type[o] < ctx->ntypes, ENKFG_EINVAL, "obs %d: type %d out of range", o, (int)type[o]);
+    SETDEV();
+    enkfg_status s;
+    size_t n = nobs > 0 ? nobs : 1, cap;
+    void** bufs[] = { (void**)&ctx->d_lon, (void**)&ctx->d_lat, (void**)&ctx->d_type, (void**)&ctx->d_status,
+                      (void**)&ctx->d_estd, (void**)&ctx->d_value, (void**)&ctx->d_ox, (void**)&ctx->d_oy,
+                      (void**)&ctx->d_oz };
+    for (size_t k = 0; k < sizeof(bufs) / sizeof(bufs[0]); ++k) {
+        if (*bufs[k]) cudaFree(*bufs[k]);
+        *bufs[k] = nullptr;
+    }
+    (void)cap;
+    (void)s;
+    CK(cudaMalloc(&ctx->d_lon, n * sizeof(float)));
+    CK(cudaMalloc(&ctx->d_lat, n * sizeof(float)));
+    CK(cudaMalloc(&ctx->d_type, n * sizeof(short)));
+    CK(cudaMalloc(&ctx->d_status, n * sizeof(short)));
+    CK(cudaMalloc(&ctx->d_estd, n * sizeof(float)));
+    CK(cudaMalloc(&ctx->d_value, n * sizeof(float)));
+    CK(cudaMalloc(&ctx->d_ox, n * sizeof(double)));
+    CK(cudaMalloc(&ctx->d_oy, n * sizeof(double)));
+    if (ctx->geographic) CK(cudaMalloc(&ctx->d_oz, n * sizeof(double)));
+    ctx->nobs = nobs;
+    if (nobs > 0) {
+        CK(cudaMemcpyAsync(ctx->d_lon, lon, nobs * sizeof(float), cudaMemcpyHostToDevice, ctx->stream));
+        CK(cudaMemcpyAsync(ctx->d_lat, lat, nobs * sizeof(float), cudaMemcpyHostToDevice, ctx->stream));
+        CK(cudaMemcpyAsync(ctx->d_type, type, nobs * sizeof(short), cudaMemcpyHostToDevice, ctx->stream));
+        CK(cudaMemcpyAsync(ctx->d_status, status, nobs * sizeof(short), cudaMemcpyHostToDevice, ctx->stream));
+        if (estd) CK(cudaMemcpyAsync(ctx->d_estd, estd, nobs * sizeof(float), cudaMemcpyHostToDevice, ctx->stream));
+        if (value) CK(cudaMemcpyAsync(ctx->d_value, value, nobs * sizeof(float), cudaMemcpyHostToDevice, ctx->stream));
+        if ((s = upload_obs_coords(ctx, lon, lat, ctx->stream))) return s;
+    }
+    CK(cudaStreamSynchronize(ctx->stream));
+    ctx->obs_set = true;
+    ctx->index_valid = false;
+    ctx->gather_valid = false;
+    ctx->s_mode = 0;
+    return ENKFG_OK;
+}
+
+static enkfg_status alloc_S(enkfg_ctx* ctx, int nmem, int nmem_dynamic)
+{
+    if (ctx->d_S) cudaFree(ctx->d_S);
+    if (ctx->d_s) cudaFree(ctx->d_s);
+    if (ctx->d_std) cudaFree(ctx->d_std);
+    ctx->d_S = nullptr;
+    ctx->d_s = ctx->d_std = nullptr;
+    size_t n = ctx->nobs > 0 ? ctx->nobs : 1;
+    CK(cudaMalloc(&ctx->d_S, (size_t)nmem * n * sizeof(float)));
+    CK(cudaMalloc(&ctx->d_s, n * sizeof(double)));
+    CK(cudaMalloc(&ctx->d_std, n * sizeof(double)));
+    CK(cudaMemsetAsync(ctx->d_s, 0, n * sizeof(double), ctx->stream));
+    ctx->nmem = nmem;
+    ctx->nmem_dyn = nmem_dynamic;
+    ctx->gather_valid = false;
+    return ENKFG_OK;
+}
+
+ENKFG_API enkfg_status enkfg_set_HE(enkfg_ctx* ctx, int nmem, int nmem_dynamic, const float* HE)
+{
+    if (!ctx) return ENKFG_EINVAL;
+    NEED(ctx->obs_set, ENKFG_ESTATE, "enkfg_set_obs must come first");
+    NEED(nmem >= 2 && nmem <= 144 && nmem_dynamic >= 1 && nmem_dynamic <= nmem && HE, ENKFG_EINVAL,
+         "bad ensemble size %d/%d", nmem, nmem_dynamic);
+    SETDEV();
+    enkfg_status s = alloc_S(ctx, nmem, nmem_dynamic);
+    if (s) return s;
+    if (ctx->nobs > 0)
+        CK(cudaMemcpyAsync(ctx->d_S, HE, (size_t)nmem * ctx->nobs * sizeof(float), cudaMemcpyHostToDevice,
+                           ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    ctx->s_mode = 1;
+    return ENKFG_OK;
+}
+
+ENKFG_API enkfg_status enkfg_calc_innovations(enkfg_ctx* ctx, double* s_f, double* std_f)
+{
+    if (!ctx) return ENKFG_EINVAL;
+    NEED(ctx->s_mode == 1, ENKFG_ESTATE, "innovations need HE (enkfg_set_HE) and are computed once");
+    SETDEV();
+    enkfg_status s;
+    if (ctx->nobs > 0 && (s = run_innovations(ctx, ctx->stream))) return s;
+    if (s_f && ctx->nobs > 0)
+        CK(cudaMemcpyAsync(s_f, ctx->d_s, ctx->nobs * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+    if (std_f && ctx->nobs > 0)
+        CK(cudaMemcpyAsync(std_f, ctx->d_std, ctx->nobs * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    ctx->s_mode = 2;
+    ctx->gather_valid = false;
+    return ENKFG_OK;
+}
+
+ENKFG_API enkfg_status enkfg_standardise(enkfg_ctx* ctx)
+{
+    if (!ctx) return ENKFG_EINVAL;
+    NEED(ctx->s_mode == 2, ENKFG_ESTATE, "standardisation needs innovations (enkfg_calc_innovations)");
+    SETDEV();
+    enkfg_status s;
+    if (ctx->nobs > 0 && (s = run_standardise(ctx, ctx->stream))) return s;
+    ctx->s_mode = 3;
+    ctx->gather_valid = false;
+    return ENKFG_OK;
+}
+
+ENKFG_API enkfg_status enkfg_set_S(enkfg_ctx* ctx, int nmem, int nmem_dynamic, const float* S, const double* sv)
+{
+    if (!ctx) return ENKFG_EINVAL;
+    NEED(ctx->obs_set, ENKFG_ESTATE, "enkfg_set_obs must come first");
+    NEED(nmem >= 2 && nmem <= 144 && nmem_dynamic >= 1 && nmem_dynamic <= nmem && S && sv, ENKFG_EINVAL,
+         "bad ensemble size %d/%d", nmem, nmem_dynamic);
+    SETDEV();
+    enkfg_status s = alloc_S(ctx, nmem, nmem_dynamic);
+    if (s) return s;
+    if (ctx->nobs > 0) {
+        CK(cudaMemcpyAsync(ctx->d_S, S, (size_t)nmem * ctx->nobs * sizeof(float), cudaMemcpyHostToDevice,
+                           ctx->stream));
+        CK(cudaMemcpyAsync(ctx->d_s, sv, ctx->nobs * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+    }
+    CK(cudaStreamSynchronize(ctx->stream));
+    ctx->s_mode = 3;
+    return ENKFG_OK;
+}
+
+ENKFG_API enkfg_status enkfg_get_S(enkfg_ctx* ctx, float* S, double* sv)
+{
+    if (!ctx) return ENKFG_EINVAL;
+    NEED(ctx->s_mode >= 1, ENKFG_ESTATE, "no ensemble observations set");
+    SETDEV();
+    if (S && ctx->nobs > 0)
+        CK(cudaMemcpyAsync(S, ctx->d_S, (size_t)ctx->nmem * ctx->nobs * sizeof(float), cudaMemcpyDeviceToHost,
+                           ctx->stream));
+    if (sv && ctx->nobs > 0)
+        CK(cudaMemcpyAsync(sv, ctx->d_s, ctx->nobs * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    return ENKFG_OK;
+}
+
+ENKFG_API enkfg_status enkfg_set_grid(enkfg_ctx* ctx, const enkfg_grid* g)
+{
+    if (!ctx || !g) return ENKFG_EINVAL;
+    NEED(ctx->types_set, ENKFG_ESTATE, "enkfg_set_obstypes must come first (geographic flag)");
+    NEED(g->mni >= 1 && g->mnj >= 1 && g->stride >= 1, ENKFG_EINVAL, "bad grid %d x %d stride %d", g->mni, g->mnj,
+         g->stride);
+    NEED((g->x && g->y) || (g->x2d && g->y2d), ENKFG_EINVAL, "grid coordinates are required");
+    SETDEV();
+    ctx->mni = g->mni;
+    ctx->mnj = g->mnj;
+    ctx->stride = g->stride;
+    ctx->periodic_i = g->periodic_i ? 1 : 0;
+    ctx->nj = (g->mnj - 1) / g->stride + 1;
+    ctx->ni = (g->mni - 1) / g->stride + 1;
+    int npts = ctx->nj * ctx->ni;
+    if (ctx->d_qx) cudaFree(ctx->d_qx);
+    if (ctx->d_qy) cudaFree(ctx->d_qy);
+    if (ctx->d_qz) cudaFree(ctx->d_qz);
+    ctx->d_qx = ctx->d_qy = ctx->d_qz = nullptr;
+    CK(cudaMalloc(&ctx->d_qx, npts * sizeof(double)));
+    CK(cudaMalloc(&ctx->d_qy, npts * sizeof(double)));
+    if (ctx->geographic) CK(cudaMalloc(&ctx->d_qz, npts * sizeof(double)));
+    enkfg_status s = upload_query_coords(ctx, g, ctx->stream);
+    if (s) return s;
+    ctx->grid_set = true;
+    ctx->t_valid = false;
+    return ENKFG_OK;
+}
+
+ENKFG_API enkfg_status enkfg_transform_dims(const enkfg_ctx* ctx, int* nj, int* ni)
+{
+    if (!ctx || !ctx->grid_set) return ENKFG_ESTATE;
+    if (nj) *nj = ctx->nj;
+    if (ni) *ni = ctx->ni;
+    return ENKFG_OK;
+}
+
+ENKFG_API enkfg_status enkfg_local_obs(enkfg_ctx* ctx, int* counts, long long* offsets, int* ids, double* coeffs,
+                                      long long capacity)
+{
+    if (!ctx) return ENKFG_EINVAL;
+    NEED(ctx->obs_set && ctx->grid_set, ENKFG_ESTATE, "observations and grid must be set");
+    NEED(counts, ENKFG_EINVAL, "counts is required");
+    NEED(!ids || (offsets && coeffs), ENKFG_EINVAL, "ids needs offsets and coeffs");
+    SETDEV();
+    enkfg_status s;
+    cudaStream_t st = ctx->stream;
+    if (!ctx->index_valid && (s = build_index(ctx, st))) return s;
+    int npts = ctx->nj * ctx->ni;
+    if ((s = ensure(ctx, &ctx->d_counts, &ctx->counts_cap, (size_t)npts))) return s;
+    if ((s = count_local(ctx, ctx->d_counts, nullptr, st))) return s;
+    CK(cudaMemcpyAsync(counts, ctx->d_counts, npts * sizeof(int), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    if (!ids) return ENKFG_OK;
+    long long* d_off;
+    CK(cudaMalloc(&d_off, (npts + 1) * sizeof(long long)));
+    if ((s = scan_counts(ctx, ctx->d_counts, d_off, npts, st))) {
+        cudaFree(d_off);
+        return s;
+    }
+    long long total = 0;
+    cudaMemcpyAsync(&total, d_off + npts, sizeof(long long), cudaMemcpyDeviceToHost, st);
+    cudaStreamSynchronize(st);
+    if (total > capacity) {
+        cudaFree(d_off);
+        set_err(ctx, "%lld local observations exceed the capacity %lld", total, capacity);
+        return ENKFG_ECAPACITY;
+    }
+    int* d_ids = nullptr;
+    double* d_c = nullptr;
+    cudaError_t e1 = cudaMalloc(&d_ids, (total > 0 ? total : 1) * sizeof(int));
+    cudaError_t e2 = cudaMalloc(&d_c, (total > 0 ? total : 1) * sizeof(double));
+    if (e1 != cudaSuccess || e2 != cudaSuccess) {
+        cudaGetLastError();
+        cudaFree(d_off);
+        cudaFree(d_ids);
+        cudaFree(d_c);
+        set_err(ctx, "cannot allocate %lld list entries", total);
+        return ENKFG_ENOMEM;
+    }
+    s = list_local(ctx, d_off, d_ids, d_c, st);
+    if (!s) {
+        cudaMemcpyAsync(offsets, d_off, (npts + 1) * sizeof(long long), cudaMemcpyDeviceToHost, st);
+        cudaMemcpyAsync(ids, d_ids, total * sizeof(int), cudaMemcpyDeviceToHost, st);
+        cudaMemcpyAsync(coeffs, d_c, total * sizeof(double), cudaMemcpyDeviceToHost, st);
+        cudaError_t e = cudaStreamSynchronize(st);
+        if (e != cudaSuccess) s = cuda_fail(ctx, e, "list copy", __LINE__);
+    }
+    cudaFree(d_off);
+    cudaFree(d_ids);
+    cudaFree(d_c);
+    return s;
+}
+
+static enkfg_status check_calc(enkfg_ctx* ctx, const enkfg_calc_params* p)
+{
+    NEED(p, ENKFG_EINVAL, "params are required");
+    NEED(ctx->obs_set && ctx->grid_set, ENKFG_ESTATE, "observations and grid must be set");
+    NEED(ctx->s_mode == 3, ENKFG_ESTATE, "S must be standardised (enkfg_standardise or enkfg_set_S)");
+    NEED(p->mode == ENKFG_MODE_ENKF || p->mode == ENKFG_MODE_ENOI || p->mode == ENKFG_MODE_HYBRID, ENKFG_EINVAL,
+         "bad mode %d", p->mode);
+    NEED(p->scheme == ENKFG_SCHEME_DENKF || p->scheme == ENKFG_SCHEME_ETKF, ENKFG_EINVAL, "bad scheme %d", p->scheme);
+    NEED(p->path == ENKFG_PATH_PLAIN || p->path == ENKFG_PATH_BATCHED, ENKFG_EINVAL, "bad path %d", p->path);
+    NEED(isfinite(p->alpha), ENKFG_EINVAL, "alpha must be finite");
+    return ENKFG_OK;
+}
+
+static enkfg_status finish_calc(enkfg_ctx* ctx, cudaStream_t st)
+{
+    int npts = ctx->nj * ctx->ni;
+    CK(cudaStreamSynchronize(st));
+    // first failing point, if any
+    int* h = (int*)malloc(npts * sizeof(int));
+    if (!h) return ENKFG_ENOMEM;
+    CK(cudaMemcpy(h, ctx->d_status_pt, npts * sizeof(int), cudaMemcpyDeviceToHost));
+    for (int k = 0; k < npts; ++k)
+        if (h[k]) {
+            set_err(ctx, "local analysis (j=%d, i=%d): factorisation failed (code %d)", k / ctx->ni, k % ctx->ni, h[k]);
+            free(h);
+            return ENKFG_ENUMERIC;
+        }
+    free(h);
+    float ms = 0.0f;
+    cudaEventElapsedTime(&ms, ctx->ev[0], ctx->ev[1]);
+    ctx->stage_ms[0] = ms;
+    cudaEventElapsedTime(&ms, ctx->ev[1], ctx->ev[2]);
+    ctx->stage_ms[1] = ms;
+    cudaEventElapsedTime(&ms, ctx->ev[2], ctx->ev[3]);
+    ctx->stage_ms[2] = ms;
+    return ENKFG_OK;
+}
+
+ENKFG_API enkfg_status enkfg_calc_transforms_dev(enkfg_ctx* ctx, const enkfg_calc_params* p, void* stream)
+{
+    if (!ctx) return ENKFG_EINVAL;
+    enkfg_status s = check_calc(ctx, p);
+    if (s) return s;
+    SETDEV();
+    return run_transforms(ctx, p, pick(ctx, stream));
+}
+
+ENKFG_API enkfg_status enkfg_calc_transforms(enkfg_ctx* ctx, const enkfg_calc_params* p, float* T, float* w,
+                                             double* T64, double* w64, const enkfg_diag* diag)
+{
+    if (!ctx) return ENKFG_EINVAL;
+    enkfg_status s = check_calc(ctx, p);
+    if (s) return s;
+    NEED(w, ENKFG_EINVAL, "w is required");
+    bool enkf = (p->mode != ENKFG_MODE_ENOI);
+    NEED(!enkf || T, ENKFG_EINVAL, "T is required for EnKF/hybrid");
+    SETDEV();
+    cudaStream_t st = ctx->stream;
+    enkfg_calc_params q = *p;
+    if (diag && diag->nlobs) q.want_diag = 1;
+    if ((s = run_transforms(ctx, &q, st))) return s;
+    if ((s = finish_calc(ctx, st))) return s;
+    size_t npts = (size_t)ctx->nj * ctx->ni, m = ctx->nmem, md = ctx->nmem_dyn;
+    if (enkf) CK(cudaMemcpyAsync(T, ctx->d_T, npts * md * m * sizeof(float), cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(w, ctx->d_w, npts * m * sizeof(float), cudaMemcpyDeviceToHost, st));
+    if (enkf && T64) CK(cudaMemcpyAsync(T64, ctx->d_T64, npts * md * m * sizeof(double), cudaMemcpyDeviceToHost, st));
+    if (w64) CK(cudaMemcpyAsync(w64, ctx->d_w64, npts * m * sizeof(double), cudaMemcpyDeviceToHost, st));
+    if (diag && q.want_diag) {
+        size_t pn = npts * ctx->ntypes;
+        if (diag->nlobs) CK(cudaMemcpyAsync(diag->nlobs, ctx->d_nlobs, npts * sizeof(int), cudaMemcpyDeviceToHost, st));
+        if (diag->dfs) CK(cudaMemcpyAsync(diag->dfs, ctx->d_dfs, npts * sizeof(float), cudaMemcpyDeviceToHost, st));
+        if (diag->srf) CK(cudaMemcpyAsync(diag->srf, ctx->d_srf, npts * sizeof(float), cudaMemcpyDeviceToHost, st));
+        if (diag->pnlobs) CK(cudaMemcpyAsync(diag->pnlobs, ctx->d_pnlobs, pn * sizeof(int), cudaMemcpyDeviceToHost, st));
+        if (diag->pdfs) CK(cudaMemcpyAsync(diag->pdfs, ctx->d_pdfs, pn * sizeof(float), cudaMemcpyDeviceToHost, st));
+        if (diag->psrf) CK(cudaMemcpyAsync(diag->psrf, ctx->d_psrf, pn * sizeof(float), cudaMemcpyDeviceToHost, st));
+    }
+    CK(cudaStreamSynchronize(st));
+    return ENKFG_OK;
+}
+
+ENKFG_API enkfg_status enkfg_transforms_dev_ptr(enkfg_ctx* ctx, float** T, float** w)
+{
+    if (!ctx) return ENKFG_EINVAL;
+    NEED(ctx->t_valid, ENKFG_ESTATE, "no transforms computed");
+    if (T) *T = ctx->d_T;
+    if (w) *w = ctx->d_w;
+    return ENKFG_OK;
+}
+
+ENKFG_API enkfg_status enkfg_set_transforms(enkfg_ctx* ctx, int mode, int nmem, int nmem_dynamic, const float* T,
+                                            const float* w)
+{
+    if (!ctx) return ENKFG_EINVAL;
+    NEED(ctx->grid_set, ENKFG_ESTATE, "the grid must be set");
+    NEED(w && (mode == ENKFG_MODE_ENOI || T), ENKFG_EINVAL, "T/w are required");
+    NEED(nmem >= 2 && nmem_dynamic >= 1 && nmem_dynamic <= nmem, ENKFG_EINVAL, "bad ensemble size");
+    SETDEV();
+    enkfg_status s;
+    size_t npts = (size_t)ctx->nj * ctx->ni;
+    size_t nT = mode == ENKFG_MODE_ENOI ? 1 : npts * nmem_dynamic * nmem;
+    if ((s = ensure(ctx, &ctx->d_T, &ctx->T_cap, nT))) return s;
+    if ((s = ensure(ctx, &ctx->d_w, &ctx->w_cap, npts * nmem))) return s;
+    if (mode != ENKFG_MODE_ENOI)
+        CK(cudaMemcpyAsync(ctx->d_T, T, nT * sizeof(float), cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaMemcpyAsync(ctx->d_w, w, npts * nmem * sizeof(float), cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    ctx->t_mode = mode;
+    ctx->t_nmem = nmem;
+    ctx->t_ndyn = nmem_dynamic;
+    ctx->t_valid = true;
+    return ENKFG_OK;
+}
+
+static enkfg_status check_update(enkfg_ctx* ctx, const enkfg_update_params* p, int nfield, const int* levels)
+{
+    NEED(p && levels && nfield >= 1, ENKFG_EINVAL, "params, levels and nfield >= 1 are required");
+    NEED(ctx->grid_set, ENKFG_ESTATE, "the grid must be set");
+    NEED(p->mode == ENKFG_MODE_ENKF || p->mode == ENKFG_MODE_HYBRID || p->mode == ENKFG_MODE_ENOI, ENKFG_EINVAL,
+         "bad mode");
+    NEED(p->nmem >= 2 && p->nmem_dynamic >= 0 && p->nmem_dynamic <= p->nmem, ENKFG_EINVAL, "bad ensemble size");
+    return ENKFG_OK;
+}
+
+ENKFG_API enkfg_status enkfg_update_fields_dev(enkfg_ctx* ctx, const enkfg_update_params* p, const int* numlevels_dev,
+                                               int nfield, const int* levels, float* fields_dev, float* infl_dev,
+                                               void* stream)
+{
+    if (!ctx) return ENKFG_EINVAL;
+    enkfg_status s = check_update(ctx, p, nfield, levels);
+    if (s) return s;
+    NEED(numlevels_dev && fields_dev, ENKFG_EINVAL, "device buffers are required");
+    SETDEV();
+    return run_update(ctx, p, numlevels_dev, nfield, levels, fields_dev, infl_dev, pick(ctx, stream));
+}
+
+ENKFG_API enkfg_status enkfg_update_fields(enkfg_ctx* ctx, const enkfg_update_params* p, const int* numlevels,
+                                          int nfield, const int* levels, float* fields, float* infl)
+{
+    if (!ctx) return ENKFG_EINVAL;
+    enkfg_status s = check_update(ctx, p, nfield, levels);
+    if (s) return s;
+    NEED(numlevels && fields, ENKFG_EINVAL, "numlevels and fields are required");
+    SETDEV();
+    cudaStream_t st = ctx->stream;
+    int j2 = p->j2 < 0 ? ctx->mnj - 1 : p->j2;
+    size_t jsize = (size_t)(j2 - p->j1 + 1);
+    size_t plane = jsize * ctx->mni;
+    size_t per = (size_t)(p->mode == ENKFG_MODE_ENOI ? p->nmem + 1 : p->nmem) * plane;
+    size_t nf = (size_t)nfield * per;
+    if ((s = ensure(ctx, &ctx->d_numlevels, &ctx->numlevels_cap, (size_t)ctx->mnj * ctx->mni))) return s;
+    if ((s = ensure(ctx, &ctx->d_fields, &ctx->fields_cap, nf))) return s;
+    if (infl && (s = ensure(ctx, &ctx->d_infl, &ctx->infl_cap, (size_t)nfield * plane))) return s;
+    CK(cudaMemcpyAsync(ctx->d_numlevels, numlevels, (size_t)ctx->mnj * ctx->mni * sizeof(int), cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(ctx->d_fields, fields, nf * sizeof(float), cudaMemcpyHostToDevice, st));
+    if ((s = run_update(ctx, p, ctx->d_numlevels, nfield, levels, ctx->d_fields, infl ? ctx->d_infl : nullptr, st)))
+        return s;
+    CK(cudaMemcpyAsync(fields, ctx->d_fields, nf * sizeof(float), cudaMemcpyDeviceToHost, st));
+    if (infl) CK(cudaMemcpyAsync(infl, ctx->d_infl, (size_t)nfield * plane * sizeof(float), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    float ms = 0.0f;
+    cudaEventElapsedTime(&ms, ctx->ev[4], ctx->ev[5]);
+    ctx->stage_ms[3] = ms;
+    return ENKFG_OK;
+}
+
+ENKFG_API enkfg_status enkfg_set_hybrid_ensemble_dev(enkfg_ctx* ctx, int nmem, int nmem_dynamic, double gamma, int nij,
+                                                     float* v_dev, void* stream)
+{
+    if (!ctx) return ENKFG_EINVAL;
+    NEED(nmem > nmem_dynamic + 1 && nmem_dynamic >= 1 && nij >= 0 && v_dev, ENKFG_EINVAL,
+         "hybrid needs at least 2 static members");
+    SETDEV();
+    return run_hybrid(ctx, nmem, nmem_dynamic, gamma, nij, v_dev, pick(ctx, stream));
+}
+
+ENKFG_API enkfg_status enkfg_set_hybrid_ensemble(enkfg_ctx* ctx, int nmem, int nmem_dynamic, double gamma, int nij,
+                                                 float* v)
+{
+    if (!ctx) return ENKFG_EINVAL;
+    NEED(nmem > nmem_dynamic + 1 && nmem_dynamic >= 1 && nij >= 0 && v, ENKFG_EINVAL,
+         "hybrid needs at least 2 static members");
+    SETDEV();
+    enkfg_status s;
+    size_t n = (size_t)nmem * nij;
+    if ((s = ensure(ctx, &ctx->d_fields, &ctx->fields_cap, n))) return s;
+    CK(cudaMemcpyAsync(ctx->d_fields, v, n * sizeof(float), cudaMemcpyHostToDevice, ctx->stream));
+    if ((s = run_hybrid(ctx, nmem, nmem_dynamic, gamma, nij, ctx->d_fields, ctx->stream))) return s;
+    CK(cudaMemcpyAsync(v, ctx->d_fields, n * sizeof(float), cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    return ENKFG_OK;
+}
+
+}  // extern "C"

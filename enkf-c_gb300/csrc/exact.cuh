@@ -1,0 +1,57 @@
+// exact.cuh -- FP64 arithmetic that reproduces the reference's host results
+// bit for bit.  Every operation is an explicitly rounded intrinsic, so the
+// compiler cannot contract a multiply and an add into an FMA (the reference
+// is built with -std=c99 -O2, which does not contract either).
+#pragma once
+
+namespace exact {
+
+// squared distance, summed in axis order from 0.0 (kdtree.c:530-531)
+__device__ __forceinline__ double dist2(double ox, double oy, double qx, double qy)
+{
+    double d0 = __dsub_rn(ox, qx), d1 = __dsub_rn(oy, qy);
+    return __dadd_rn(__dmul_rn(d0, d0), __dmul_rn(d1, d1));
+}
+
+__device__ __forceinline__ double dist3(double ox, double oy, double oz, double qx, double qy, double qz)
+{
+    double d0 = __dsub_rn(ox, qx), d1 = __dsub_rn(oy, qy), d2 = __dsub_rn(oz, qz);
+    return __dadd_rn(__dadd_rn(__dmul_rn(d0, d0), __dmul_rn(d1, d1)), __dmul_rn(d2, d2));
+}
+
+// Gaspari-Cohn taper with support at x = 1 (utils.c:1425-1443): the same
+// polynomial pieces, evaluated in the same order.
+__device__ __forceinline__ double taper_gc(double x)
+{
+    if (x >= 1.0) return 0.0;
+    x = __dmul_rn(x, 2.0);
+    double x2 = __dmul_rn(x, x);
+    double x3 = __dmul_rn(x2, x);
+    double f;
+    if (x < 1.0) {
+        double a = __dadd_rn(__ddiv_rn(-x3, 4.0), __ddiv_rn(x2, 2.0));
+        f = __dadd_rn(1.0, __dmul_rn(x2, a));
+        f = __dadd_rn(f, __dmul_rn(x3, 5.0 / 8.0));
+        f = __dsub_rn(f, __dmul_rn(x2, 5.0 / 3.0));
+    } else {
+        double a = __dsub_rn(__ddiv_rn(x3, 12.0), __ddiv_rn(x2, 2.0));
+        f = __dmul_rn(x2, a);
+        f = __dadd_rn(f, __dmul_rn(x3, 5.0 / 8.0));
+        f = __dadd_rn(f, __dmul_rn(x2, 5.0 / 3.0));
+        f = __dsub_rn(f, __dmul_rn(x, 5.0));
+        f = __dadd_rn(f, 4.0);
+        f = __dsub_rn(f, __ddiv_rn(2.0 / 3.0, x));
+    }
+    return (f >= 0.0) ? f : 0.0;
+}
+
+// multi-radius taper coefficient (obstypes.c:800-809)
+__device__ __forceinline__ double calclcoeff(int nlocrad, const double* locrad, const double* locweight, double dist)
+{
+    double sum = 0.0;
+    for (int i = 0; i < nlocrad; ++i)
+        if (dist <= locrad[i]) sum = __dadd_rn(sum, __dmul_rn(locweight[i], taper_gc(__ddiv_rn(dist, locrad[i]))));
+    return sum;
+}
+
+}  // namespace exact

@@ -1,0 +1,667 @@
+// index.cu -- device spatial index of the observations and the local
+// observation search (obs_findlocal, reference common/observations.c:
+// 1837-1927; kd-tree range search common/kdtree.c:516-574).
+//
+// The reference walks one kd-tree per observation type for every local
+// analysis.  Here the observations of each type are bucketed on a uniform
+// cell grid (cell edge >= the type's largest radius), buckets numbered in
+// Morton order, so the observations within range of a point are found by
+// scanning the 3x3 (3x3x3 on the sphere) cells around it.  Membership uses
+// the reference's predicate bit for bit: distsq = sum of squared coordinate
+// differences in FP64, accumulated in axis order, compared `<= r*r`; all of
+// it with round-to-nearest intrinsics so that no multiply-add is fused.
+#include "internal.cuh"
+#include "exact.cuh"
+
+// ---------------------------------------------------------------------------
+// Morton codes
+// ---------------------------------------------------------------------------
+__host__ __device__ static inline unsigned int spread2(unsigned int v)
+{
+    v &= 0x0000ffffu;
+    v = (v | (v << 8)) & 0x00ff00ffu;
+    v = (v | (v << 4)) & 0x0f0f0f0fu;
+    v = (v | (v << 2)) & 0x33333333u;
+    v = (v | (v << 1)) & 0x55555555u;
+    return v;
+}
+
+__host__ __device__ static inline unsigned int spread3(unsigned int v)
+{
+    v &= 0x000003ffu;
+    v = (v | (v << 16)) & 0x030000ffu;
+    v = (v | (v << 8)) & 0x0300f00fu;
+    v = (v | (v << 4)) & 0x030c30c3u;
+    v = (v | (v << 2)) & 0x09249249u;
+    return v;
+}
+
+__device__ __forceinline__ long long bucket_of(const TypeIndex& t, int ndim, int cx, int cy, int cz)
+{
+    unsigned int code = (ndim == 2) ? (spread2(cx) | (spread2(cy) << 1))
+                                    : (spread3(cx) | (spread3(cy) << 1) | (spread3(cz) << 2));
+    return t.bucket_base + (long long)code;
+}
+
+__device__ __forceinline__ int cell_coord(double v, double v0, double inv_cell)
+{
+    return (int)floor((v - v0) * inv_cell);
+}
+
+// ---------------------------------------------------------------------------
+// bounding boxes per type (order-preserving integer encoding of doubles)
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ unsigned long long dkey(double d)
+{
+    long long b = __double_as_longlong(d);
+    return b >= 0 ? ((unsigned long long)b ^ 0x8000000000000000ull) : ~(unsigned long long)b;
+}
+
+static double dkey_inv(unsigned long long k)
+{
+    long long b = (k & 0x8000000000000000ull) ? (long long)(k ^ 0x8000000000000000ull) : (long long)~k;
+    double d;
+    memcpy(&d, &b, 8);
+    return d;
+}
+
+__global__ void k_bbox(int nobs, int ndim, const double* __restrict__ ox, const double* __restrict__ oy,
+                       const double* __restrict__ oz, const short* __restrict__ type,
+                       const short* __restrict__ status, unsigned long long* __restrict__ box)
+{
+    // box[t*6 + 2*axis + 0] = min key, + 1 = max key (as max of keys)
+    int o = blockIdx.x * blockDim.x + threadIdx.x;
+    if (o >= nobs || status[o] != 0) return;
+    int t = type[o];
+    double v[3] = { ox[o], oy[o], ndim == 3 ? oz[o] : 0.0 };
+    for (int a = 0; a < ndim; ++a) {
+        unsigned long long k = dkey(v[a]);
+        atomicMin(&box[t * 6 + 2 * a], k);
+        atomicMax(&box[t * 6 + 2 * a + 1], k);
+    }
+}
+
+__global__ void k_keys(int nobs, int ndim, const double* __restrict__ ox, const double* __restrict__ oy,
+                       const double* __restrict__ oz, const short* __restrict__ type,
+                       const short* __restrict__ status, const TypeIndex* __restrict__ types,
+                       int* __restrict__ key, int* __restrict__ bcount)
+{
+    int o = blockIdx.x * blockDim.x + threadIdx.x;
+    if (o >= nobs) return;
+    if (status[o] != 0) {
+        key[o] = -1;
+        return;
+    }
+    const TypeIndex& t = types[type[o]];
+    int cx = min(max(cell_coord(ox[o], t.x0, t.inv_cell), 0), t.ncx - 1);
+    int cy = min(max(cell_coord(oy[o], t.y0, t.inv_cell), 0), t.ncy - 1);
+    int cz = 0;
+    if (ndim == 3) cz = min(max(cell_coord(oz[o], t.z0, t.inv_cell), 0), t.ncz - 1);
+    long long b = bucket_of(t, ndim, cx, cy, cz);
+    key[o] = (int)b;
+    atomicAdd(&bcount[b], 1);
+}
+
+__global__ void k_scatter(int nobs, const int* __restrict__ key, const long long* __restrict__ bstart,
+                          int* __restrict__ bfill, int* __restrict__ sid)
+{
+    int o = blockIdx.x * blockDim.x + threadIdx.x;
+    if (o >= nobs) return;
+    int b = key[o];
+    if (b < 0) return;
+    long long pos = bstart[b] + atomicAdd(&bfill[b], 1);
+    sid[pos] = o;
+}
+
+// sort the ids inside each bucket (deterministic order): bitonic in shared
+// memory for buckets up to 8192 entries, rank sort for larger ones.
+#define BSORT_CAP 8192
+__global__ void k_bucket_sort(long long nbuckets, const long long* __restrict__ bstart, int* __restrict__ sid,
+                              int* __restrict__ tmp)
+{
+    __shared__ int s[BSORT_CAP];
+    for (long long b = blockIdx.x; b < nbuckets; b += gridDim.x) {
+        long long b0 = bstart[b], b1 = bstart[b + 1];
+        int n = (int)(b1 - b0);
+        if (n <= 1) continue;
+        if (n <= BSORT_CAP) {
+            int np2 = 1;
+            while (np2 < n) np2 <<= 1;
+            for (int i = threadIdx.x; i < np2; i += blockDim.x) s[i] = i < n ? sid[b0 + i] : 0x7fffffff;
+            __syncthreads();
+            for (int k = 2; k <= np2; k <<= 1) {
+                for (int j = k >> 1; j > 0; j >>= 1) {
+                    for (int i = threadIdx.x; i < np2; i += blockDim.x) {
+                        int l = i ^ j;
+                        if (l > i) {
+                            int a = s[i], c = s[l];
+                            bool up = ((i & k) == 0);
+                            if ((a > c) == up) {
+                                s[i] = c;
+                                s[l] = a;
+                            }
+                        }
+                    }
+                    __syncthreads();
+                }
+            }
+            for (int i = threadIdx.x; i < n; i += blockDim.x) sid[b0 + i] = s[i];
+            __syncthreads();
+        } else {
+            for (int i = threadIdx.x; i < n; i += blockDim.x) {
+                int v = sid[b0 + i], r = 0;
+                for (int k = 0; k < n; ++k) r += sid[b0 + k] < v;
+                tmp[b0 + r] = v;
+            }
+            __syncthreads();
+            for (int i = threadIdx.x; i < n; i += blockDim.x) sid[b0 + i] = tmp[b0 + i];
+            __syncthreads();
+        }
+    }
+}
+
+__global__ void k_sorted_coords(int nsorted, const int* __restrict__ sid, const double* __restrict__ ox,
+                                const double* __restrict__ oy, const double* __restrict__ oz,
+                                const short* __restrict__ type, double* __restrict__ sx, double* __restrict__ sy,
+                                double* __restrict__ sz, short* __restrict__ stype)
+{
+    int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= nsorted) return;
+    int o = sid[p];
+    sx[p] = ox[o];
+    sy[p] = oy[o];
+    if (sz) sz[p] = oz[o];
+    stype[p] = type[o];
+}
+
+// S [nmem][nobs] -> St [nsorted][mpad] (sorted order, member-contiguous):
+// tiled transpose into T1 [nobs][mpad] then a row gather.
+__global__ void k_transpose_S(int nmem, int nobs, int mpad, const float* __restrict__ S, float* __restrict__ St)
+{
+    __shared__ float tile[32][33];
+    int o0 = blockIdx.x * 32, e0 = blockIdx.y * 32;
+    for (int k = threadIdx.y; k < 32; k += blockDim.y) {
+        int e = e0 + k, o = o0 + threadIdx.x;
+        tile[k][threadIdx.x] = (e < nmem && o < nobs) ? S[(size_t)e * nobs + o] : 0.0f;
+    }
+    __syncthreads();
+    for (int k = threadIdx.y; k < 32; k += blockDim.y) {
+        int o = o0 + k, e = e0 + threadIdx.x;
+        if (o < nobs && e < mpad) St[(size_t)o * mpad + e] = (e < nmem) ? tile[threadIdx.x][k] : 0.0f;
+    }
+}
+
+__global__ void k_gather_rows(int nsorted, int mpad, const int* __restrict__ sid, const float* __restrict__ src,
+                              const double* __restrict__ s, float* __restrict__ St, double* __restrict__ ss)
+{
+    // one warp per sorted row, float4 copies
+    int p = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    int lane = threadIdx.x & 31;
+    if (p >= nsorted) return;
+    int o = sid[p];
+    const float4* a = (const float4*)(src + (size_t)o * mpad);
+    float4* b = (float4*)(St + (size_t)p * mpad);
+    for (int k = lane; k < mpad / 4; k += 32) b[k] = a[k];
+    if (lane == 0) ss[p] = s[o];
+}
+
+// ---------------------------------------------------------------------------
+// exclusive scan (int -> long long)
+// ---------------------------------------------------------------------------
+#define SCAN_T 1024
+#define SCAN_IPT 4
+__global__ void k_scan_block(const int* __restrict__ in, long long n, long long* __restrict__ out,
+                             long long* __restrict__ bsum)
+{
+    __shared__ long long ws[32];
+    long long base = (long long)blockIdx.x * SCAN_T * SCAN_IPT + (long long)threadIdx.x * SCAN_IPT;
+    long long v[SCAN_IPT];
+    long long acc = 0;
+    for (int k = 0; k < SCAN_IPT; ++k) {
+        long long i = base + k;
+        v[k] = (i < n) ? in[i] : 0;
+        acc += v[k];
+    }
+    int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    long long x = acc;
+    for (int d = 1; d < 32; d <<= 1) {
+        long long y = __shfl_up_sync(0xffffffffu, x, d);
+        if (lane >= d) x += y;
+    }
+    if (lane == 31) ws[wid] = x;
+    __syncthreads();
+    if (wid == 0) {
+        long long w = (lane < (SCAN_T >> 5)) ? ws[lane] : 0;
+        for (int d = 1; d < 32; d <<= 1) {
+            long long y = __shfl_up_sync(0xffffffffu, w, d);
+            if (lane >= d) w += y;
+        }
+        ws[lane] = w;
+    }
+    __syncthreads();
+    long long excl = x - acc + (wid > 0 ? ws[wid - 1] : 0);
+    for (int k = 0; k < SCAN_IPT; ++k) {
+        long long i = base + k;
+        if (i < n) out[i] = excl;
+        excl += v[k];
+    }
+    if (threadIdx.x == SCAN_T - 1) bsum[blockIdx.x] = excl;
+}
+
+__global__ void k_scan_add(long long* __restrict__ out, long long n, const long long* __restrict__ boff)
+{
+    long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    long long per = SCAN_T * SCAN_IPT;
+    if (i < n) out[i] += boff[i / per];
+}
+
+// scan of long long block sums, serial in one thread per chunk (few blocks)
+__global__ void k_scan_ll_small(const long long* __restrict__ in, long long n, long long* __restrict__ out)
+{
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    long long acc = 0;
+    for (long long i = 0; i < n; ++i) {
+        long long v = in[i];
+        out[i] = acc;
+        acc += v;
+    }
+    out[n] = acc;
+}
+
+enkfg_status scan_counts(enkfg_ctx* ctx, const int* d_in, long long* d_out, long long n, cudaStream_t st)
+{
+    long long per = SCAN_T * SCAN_IPT;
+    long long nb = (n + per - 1) / per;
+    if (nb < 1) nb = 1;
+    size_t need = (size_t)(2 * nb + 2) * sizeof(long long);
+    enkfg_status s = ensure(ctx, (char**)&ctx->d_scratch, &ctx->scratch_cap, need);
+    if (s) return s;
+    long long* bsum = (long long*)ctx->d_scratch;
+    long long* boff = bsum + nb;
+    k_scan_block<<<(unsigned)nb, SCAN_T, 0, st>>>(d_in, n, d_out, bsum);
+    CKL();
+    k_scan_ll_small<<<1, 32, 0, st>>>(bsum, nb, boff);
+    CKL();
+    k_scan_add<<<div_up(n + 1, 256), 256, 0, st>>>(d_out, n, boff);
+    CKL();
+    // total
+    CK(cudaMemcpyAsync(d_out + n, boff + nb, sizeof(long long), cudaMemcpyDeviceToDevice, st));
+    return ENKFG_OK;
+}
+
+// ---------------------------------------------------------------------------
+// build the index
+// ---------------------------------------------------------------------------
+enkfg_status build_index(enkfg_ctx* ctx, cudaStream_t st)
+{
+    int nobs = ctx->nobs, ntypes = ctx->ntypes, ndim = ctx->geographic ? 3 : 2;
+    size_t cap;
+    enkfg_status s;
+
+    // bounding boxes
+    unsigned long long* d_box;
+    CK(cudaMalloc(&d_box, (size_t)ntypes * 6 * sizeof(unsigned long long)));
+    {
+        unsigned long long* h = (unsigned long long*)malloc(ntypes * 6 * sizeof(unsigned long long));
+        for (int t = 0; t < ntypes; ++t)
+            for (int a = 0; a < 3; ++a) {
+                h[t * 6 + 2 * a] = ~0ull;
+                h[t * 6 + 2 * a + 1] = 0ull;
+            }
+        cudaMemcpyAsync(d_box, h, ntypes * 6 * sizeof(unsigned long long), cudaMemcpyHostToDevice, st);
+        if (nobs > 0) {
+            k_bbox<<<div_up(nobs, 256), 256, 0, st>>>(nobs, ndim, ctx->d_ox, ctx->d_oy, ctx->d_oz, ctx->d_type,
+                                                     ctx->d_status, d_box);
+            ctx->launches++;
+        }
+        cudaMemcpyAsync(h, d_box, ntypes * 6 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, st);
+        cudaError_t e = cudaStreamSynchronize(st);
+        cudaFree(d_box);
+        if (e != cudaSuccess) {
+            free(h);
+            return cuda_fail(ctx, e, "bbox", __LINE__);
+        }
+        long long base = 0;
+        for (int t = 0; t < ntypes; ++t) {
+            TypeIndex& ti = ctx->h_types[t];
+            memset(&ti, 0, sizeof(ti));
+            ti.nlocrad = ctx->nlocrad[t];
+            double rmax = 0.0;
+            for (int k = 0; k < ti.nlocrad; ++k) {
+                ti.locrad[k] = ctx->locrad[t][k];
+                ti.locweight[k] = ctx->locweight[t][k];
+                if (ti.locrad[k] > rmax) rmax = ti.locrad[k];
+            }
+            ti.rmax = rmax;
+            ti.rmax2 = rmax * rmax;
+            bool empty = (h[t * 6] == ~0ull);
+            double lo[3] = { 0, 0, 0 }, hi[3] = { 0, 0, 0 };
+            if (!empty)
+                for (int a = 0; a < ndim; ++a) {
+                    lo[a] = dkey_inv(h[t * 6 + 2 * a]);
+                    hi[a] = dkey_inv(h[t * 6 + 2 * a + 1]);
+                }
+            // cell edge: at least the radius (slightly enlarged so that
+            // rounding in the cell arithmetic cannot skip a neighbour cell),
+            // and at most 4096 cells per axis
+            double ext = 0.0;
+            for (int a = 0; a < ndim; ++a) ext = fmax(ext, hi[a] - lo[a]);
+            double cell = fmax(rmax * (1.0 + 1e-9), ext / (ndim == 2 ? 4000.0 : 1000.0));
+            if (!(cell > 0.0)) cell = 1.0;
+            ti.inv_cell = 1.0 / cell;
+            ti.x0 = lo[0];
+            ti.y0 = lo[1];
+            ti.z0 = lo[2];
+            ti.ncx = empty ? 1 : (int)floor((hi[0] - lo[0]) * ti.inv_cell) + 1;
+            ti.ncy = empty ? 1 : (int)floor((hi[1] - lo[1]) * ti.inv_cell) + 1;
+            ti.ncz = (ndim == 3 && !empty) ? (int)floor((hi[2] - lo[2]) * ti.inv_cell) + 1 : 1;
+            int nmax = ti.ncx > ti.ncy ? ti.ncx : ti.ncy;
+            if (ti.ncz > nmax) nmax = ti.ncz;
+            int mb = 0;
+            while ((1 << mb) < nmax) mb++;
+            ti.mbits = mb;
+            ti.nbuckets = 1ll << (ndim * mb);
+            ti.bucket_base = base;
+            base += ti.nbuckets;
+        }
+        free(h);
+        ctx->nbuckets = base;
+    }
+    if (ctx->nbuckets > (1ll << 30)) {
+        set_err(ctx, "spatial index too large (%lld buckets)", ctx->nbuckets);
+        return ENKFG_ECAPACITY;
+    }
+    cap = 0;
+    if (ctx->d_types == nullptr) CK(cudaMalloc(&ctx->d_types, sizeof(TypeIndex) * ENKFG_MAXTYPES));
+    CK(cudaMemcpyAsync(ctx->d_types, ctx->h_types, sizeof(TypeIndex) * ntypes, cudaMemcpyHostToDevice, st));
+
+    // bucket counts, scan, scatter, sort
+    cudaFree(ctx->d_bstart);
+    cudaFree(ctx->d_bfill);
+    cudaFree(ctx->d_key);
+    ctx->d_bstart = nullptr;
+    ctx->d_bfill = nullptr;
+    ctx->d_key = nullptr;
+    CK(cudaMalloc(&ctx->d_bstart, (ctx->nbuckets + 1) * sizeof(long long)));
+    CK(cudaMalloc(&ctx->d_bfill, ctx->nbuckets * sizeof(int)));
+    CK(cudaMalloc(&ctx->d_key, (size_t)(nobs > 0 ? nobs : 1) * sizeof(int)));
+    CK(cudaMemsetAsync(ctx->d_bfill, 0, ctx->nbuckets * sizeof(int), st));
+    if (nobs > 0) {
+        k_keys<<<div_up(nobs, 256), 256, 0, st>>>(nobs, ndim, ctx->d_ox, ctx->d_oy, ctx->d_oz, ctx->d_type,
+                                                 ctx->d_status, ctx->d_types, ctx->d_key, ctx->d_bfill);
+        CKL();
+    }
+    if ((s = scan_counts(ctx, ctx->d_bfill, ctx->d_bstart, ctx->nbuckets, st))) return s;
+    long long total = 0;
+    CK(cudaMemcpyAsync(&total, ctx->d_bstart + ctx->nbuckets, sizeof(long long), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    ctx->nsorted = (int)total;
+    int ns = ctx->nsorted > 0 ? ctx->nsorted : 1;
+    cudaFree(ctx->d_sid);
+    cudaFree(ctx->d_sx);
+    cudaFree(ctx->d_sy);
+    cudaFree(ctx->d_sz);
+    cudaFree(ctx->d_stype);
+    ctx->d_sid = nullptr;
+    ctx->d_sx = ctx->d_sy = ctx->d_sz = nullptr;
+    ctx->d_stype = nullptr;
+    CK(cudaMalloc(&ctx->d_sid, ns * sizeof(int)));
+    CK(cudaMalloc(&ctx->d_sx, ns * sizeof(double)));
+    CK(cudaMalloc(&ctx->d_sy, ns * sizeof(double)));
+    if (ndim == 3) CK(cudaMalloc(&ctx->d_sz, ns * sizeof(double)));
+    CK(cudaMalloc(&ctx->d_stype, ns * sizeof(short)));
+    CK(cudaMemsetAsync(ctx->d_bfill, 0, ctx->nbuckets * sizeof(int), st));
+    if (nobs > 0) {
+        k_scatter<<<div_up(nobs, 256), 256, 0, st>>>(nobs, ctx->d_key, ctx->d_bstart, ctx->d_bfill, ctx->d_sid);
+        CKL();
+        int grid = (int)(ctx->nbuckets < 65536 ? ctx->nbuckets : 65536);
+        k_bucket_sort<<<grid, 512, 0, st>>>(ctx->nbuckets, ctx->d_bstart, ctx->d_sid, ctx->d_key);
+        CKL();
+    }
+    if (ctx->nsorted > 0) {
+        k_sorted_coords<<<div_up(ctx->nsorted, 256), 256, 0, st>>>(ctx->nsorted, ctx->d_sid, ctx->d_ox, ctx->d_oy,
+                                                                  ctx->d_oz, ctx->d_type, ctx->d_sx, ctx->d_sy,
+                                                                  ctx->d_sz, ctx->d_stype);
+        CKL();
+    }
+    // per-type sorted ranges (bucket_base ranges are contiguous by type)
+    for (int t = 0; t < ntypes; ++t) {
+        long long r[2];
+        CK(cudaMemcpyAsync(&r[0], ctx->d_bstart + ctx->h_types[t].bucket_base, sizeof(long long),
+                           cudaMemcpyDeviceToHost, st));
+        CK(cudaMemcpyAsync(&r[1], ctx->d_bstart + ctx->h_types[t].bucket_base + ctx->h_types[t].nbuckets,
+                           sizeof(long long), cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
+        ctx->h_types[t].pos_begin = (int)r[0];
+        ctx->h_types[t].pos_end = (int)r[1];
+    }
+    CK(cudaMemcpyAsync(ctx->d_types, ctx->h_types, sizeof(TypeIndex) * ntypes, cudaMemcpyHostToDevice, st));
+    ctx->index_valid = true;
+    ctx->gather_valid = false;
+    return ENKFG_OK;
+}
+
+enkfg_status build_gather(enkfg_ctx* ctx, cudaStream_t st)
+{
+    int m = ctx->nmem, nobs = ctx->nobs;
+    int mpad = (m + 3) & ~3;
+    ctx->mpad = mpad;
+    int ns = ctx->nsorted > 0 ? ctx->nsorted : 1;
+    cudaFree(ctx->d_St);
+    cudaFree(ctx->d_ss);
+    ctx->d_St = nullptr;
+    ctx->d_ss = nullptr;
+    CK(cudaMalloc(&ctx->d_St, (size_t)ns * mpad * sizeof(float)));
+    CK(cudaMalloc(&ctx->d_ss, (size_t)ns * sizeof(double)));
+    if (nobs > 0 && ctx->nsorted > 0) {
+        float* tmp;
+        CK(cudaMalloc(&tmp, (size_t)nobs * mpad * sizeof(float)));
+        dim3 g(div_up(nobs, 32), div_up(mpad, 32));
+        k_transpose_S<<<g, dim3(32, 8), 0, st>>>(m, nobs, mpad, ctx->d_S, tmp);
+        ctx->launches++;
+        k_gather_rows<<<div_up((long long)ctx->nsorted * 32, 256), 256, 0, st>>>(ctx->nsorted, mpad, ctx->d_sid, tmp,
+                                                                               ctx->d_s, ctx->d_St, ctx->d_ss);
+        ctx->launches++;
+        cudaError_t e = cudaGetLastError();
+        cudaStreamSynchronize(st);
+        cudaFree(tmp);
+        if (e != cudaSuccess) return cuda_fail(ctx, e, "gather", __LINE__);
+    }
+    ctx->gather_valid = true;
+    return ENKFG_OK;
+}
+
+// ---------------------------------------------------------------------------
+// local observation count / list
+// ---------------------------------------------------------------------------
+
+// Neighbour cells of a query point for type t: returns the number of cells
+// and fills the bucket ids (at most 27).
+__device__ __forceinline__ int neighbour_buckets(const TypeIndex& t, int ndim, double qx, double qy, double qz,
+                                                 long long* b)
+{
+    // query cell (as a double first: the query can be far outside the grid)
+    double fx = floor((qx - t.x0) * t.inv_cell), fy = floor((qy - t.y0) * t.inv_cell);
+    double fz = ndim == 3 ? floor((qz - t.z0) * t.inv_cell) : 0.0;
+    int n = 0;
+    if (fx < -1.0 || fx > (double)t.ncx || fy < -1.0 || fy > (double)t.ncy) return 0;
+    if (ndim == 3 && (fz < -1.0 || fz > (double)t.ncz)) return 0;
+    int cx = (int)fx, cy = (int)fy, cz = (int)fz;
+    int zlo = ndim == 3 ? cz - 1 : 0, zhi = ndim == 3 ? cz + 1 : 0;
+    for (int z = zlo; z <= zhi; ++z) {
+        if (z < 0 || z >= t.ncz) continue;
+        for (int y = cy - 1; y <= cy + 1; ++y) {
+            if (y < 0 || y >= t.ncy) continue;
+            for (int x = cx - 1; x <= cx + 1; ++x) {
+                if (x < 0 || x >= t.ncx) continue;
+                b[n++] = bucket_of(t, ndim, x, y, z);
+            }
+        }
+    }
+    return n;
+}
+
+// one warp per strided point
+__global__ void k_count_local(int npts, int ntypes, int ndim, const TypeIndex* __restrict__ types,
+                              const long long* __restrict__ bstart, const double* __restrict__ sx,
+                              const double* __restrict__ sy, const double* __restrict__ sz,
+                              const double* __restrict__ qx, const double* __restrict__ qy,
+                              const double* __restrict__ qz, int* __restrict__ counts, int* __restrict__ pcounts)
+{
+    int pt = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    int lane = threadIdx.x & 31;
+    if (pt >= npts) return;
+    double x = qx[pt], y = qy[pt], z = ndim == 3 ? qz[pt] : 0.0;
+    int total = 0;
+    for (int t = 0; t < ntypes; ++t) {
+        const TypeIndex& ti = types[t];
+        int nt = 0;
+        if (ti.pos_end > ti.pos_begin) {
+            long long bk[27];
+            int nb = neighbour_buckets(ti, ndim, x, y, z, bk);
+            for (int k = 0; k < nb; ++k) {
+                long long b0 = bstart[bk[k]], b1 = bstart[bk[k] + 1];
+                for (long long base = b0; base < b1; base += 32) {
+                    long long p = base + lane;
+                    bool in = false;
+                    if (p < b1) {
+                        double d2 = ndim == 2 ? exact::dist2(sx[p], sy[p], x, y)
+                                              : exact::dist3(sx[p], sy[p], sz[p], x, y, z);
+                        in = d2 <= ti.rmax2;
+                    }
+                    nt += __popc(__ballot_sync(0xffffffffu, in));
+                }
+            }
+        }
+        if (pcounts != nullptr && lane == 0) pcounts[(size_t)t * npts + pt] = nt;
+        total += nt;
+    }
+    if (lane == 0) counts[pt] = total;
+}
+
+enkfg_status count_local(enkfg_ctx* ctx, int* d_counts, int* d_pcounts, cudaStream_t st)
+{
+    int npts = ctx->nj * ctx->ni;
+    int ndim = ctx->geographic ? 3 : 2;
+    k_count_local<<<div_up((long long)npts * 32, 256), 256, 0, st>>>(
+        npts, ctx->ntypes, ndim, ctx->d_types, ctx->d_bstart, ctx->d_sx, ctx->d_sy, ctx->d_sz, ctx->d_qx, ctx->d_qy,
+        ctx->d_qz, d_counts, d_pcounts);
+    CKL();
+    return ENKFG_OK;
+}
+
+// One CTA per point: collect (id, taper) of every local obs, sort by id and
+// write the CSR row.  Capacity LIST_CAP entries per point (a power of two,
+// so that the bitonic network never leaves the arrays).
+#define LIST_CAP 8192
+#define LIST_T 256
+__global__ void __launch_bounds__(LIST_T) k_list_local(int npts, int ntypes, int ndim,
+                                                       const TypeIndex* __restrict__ types,
+                                                       const long long* __restrict__ bstart,
+                                                       const double* __restrict__ sx, const double* __restrict__ sy,
+                                                       const double* __restrict__ sz, const int* __restrict__ sid,
+                                                       const double* __restrict__ qx, const double* __restrict__ qy,
+                                                       const double* __restrict__ qz,
+                                                       const long long* __restrict__ offsets, int* __restrict__ ids,
+                                                       double* __restrict__ coeffs, int* __restrict__ err)
+{
+    extern __shared__ unsigned char smem[];
+    int* kid = (int*)smem;
+    double* kc = (double*)(smem + LIST_CAP * sizeof(int));
+    __shared__ int wsum[LIST_T / 32];
+    __shared__ int n_sh;
+    int pt = blockIdx.x;
+    if (pt >= npts) return;
+    double x = qx[pt], y = qy[pt], z = ndim == 3 ? qz[pt] : 0.0;
+    int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    if (threadIdx.x == 0) n_sh = 0;
+    __syncthreads();
+    for (int t = 0; t < ntypes; ++t) {
+        const TypeIndex& ti = types[t];
+        if (ti.pos_end <= ti.pos_begin) continue;
+        long long bk[27];
+        int nb = neighbour_buckets(ti, ndim, x, y, z, bk);
+        for (int k = 0; k < nb; ++k) {
+            long long b0 = bstart[bk[k]], b1 = bstart[bk[k] + 1];
+            for (long long base = b0; base < b1; base += LIST_T) {
+                long long p = base + threadIdx.x;
+                bool in = false;
+                double d2 = 0.0;
+                if (p < b1) {
+                    d2 = ndim == 2 ? exact::dist2(sx[p], sy[p], x, y) : exact::dist3(sx[p], sy[p], sz[p], x, y, z);
+                    in = d2 <= ti.rmax2;
+                }
+                unsigned bal = __ballot_sync(0xffffffffu, in);
+                if (lane == 0) wsum[wid] = __popc(bal);
+                __syncthreads();
+                int before = 0, tot = 0;
+                for (int w = 0; w < LIST_T / 32; ++w) {
+                    if (w < wid) before += wsum[w];
+                    tot += wsum[w];
+                }
+                int pos = n_sh + before + __popc(bal & ((1u << lane) - 1));
+                if (in && pos < LIST_CAP) {
+                    kid[pos] = sid[p];
+                    kc[pos] = exact::calclcoeff(ti.nlocrad, ti.locrad, ti.locweight, __dsqrt_rn(d2));
+                }
+                __syncthreads();
+                if (threadIdx.x == 0) n_sh += tot;
+                __syncthreads();
+            }
+        }
+    }
+    int n = n_sh;
+    if (n > LIST_CAP) {
+        if (threadIdx.x == 0) atomicMax(err, n);
+        return;
+    }
+    int np2 = 1;
+    while (np2 < n) np2 <<= 1;
+    for (int i = n + threadIdx.x; i < np2; i += LIST_T) kid[i] = 0x7fffffff;
+    __syncthreads();
+    for (int k = 2; k <= np2; k <<= 1) {
+        for (int j = k >> 1; j > 0; j >>= 1) {
+            for (int i = threadIdx.x; i < np2; i += LIST_T) {
+                int l = i ^ j;
+                if (l > i) {
+                    int a = kid[i], c = kid[l];
+                    bool up = ((i & k) == 0);
+                    if ((a > c) == up) {
+                        double tmp = kc[i];
+                        kid[i] = c;
+                        kid[l] = a;
+                        kc[i] = kc[l];
+                        kc[l] = tmp;
+                    }
+                }
+            }
+            __syncthreads();
+        }
+    }
+    long long o0 = offsets[pt];
+    for (int i = threadIdx.x; i < n; i += LIST_T) {
+        ids[o0 + i] = kid[i];
+        coeffs[o0 + i] = kc[i];
+    }
+}
+
+enkfg_status list_local(enkfg_ctx* ctx, const long long* d_offsets, int* d_ids, double* d_coeffs, cudaStream_t st)
+{
+    int npts = ctx->nj * ctx->ni;
+    int ndim = ctx->geographic ? 3 : 2;
+    size_t smem = LIST_CAP * (sizeof(int) + sizeof(double));
+    CK(cudaFuncSetAttribute(k_list_local, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    CK(cudaMemsetAsync(ctx->d_qhead, 0, 2 * sizeof(int), st));
+    k_list_local<<<npts, LIST_T, smem, st>>>(npts, ctx->ntypes, ndim, ctx->d_types, ctx->d_bstart, ctx->d_sx,
+                                             ctx->d_sy, ctx->d_sz, ctx->d_sid, ctx->d_qx, ctx->d_qy, ctx->d_qz,
+                                             d_offsets, d_ids, d_coeffs, ctx->d_qhead + 1);
+    CKL();
+    int over = 0;
+    CK(cudaMemcpyAsync(&over, ctx->d_qhead + 1, sizeof(int), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    if (over > 0) {
+        set_err(ctx, "a point has %d local observations, above the list capacity %d", over, LIST_CAP);
+        return ENKFG_ECAPACITY;
+    }
+    return ENKFG_OK;
+}

@@ -1,0 +1,185 @@
+// internal.cuh -- shared definitions of libenkfg (GB300 EnKF-C hot path).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <stdio.h>
+#include <string.h>
+#include "../../include/enkfg.h"
+
+#define ENKFG_VERSION 1
+
+// ---------------------------------------------------------------------------
+// Per-type spatial index description (device copy lives in ctx->d_types).
+// The observations of one type are bucketed on a uniform grid of cells of
+// edge >= the type's maximum localisation radius; buckets are numbered in
+// Morton (Z) order of their cell coordinates, so a query point visits the
+// 3x3 (2-D) or 3x3x3 (3-D) cells around it.
+// ---------------------------------------------------------------------------
+struct TypeIndex {
+    double x0, y0, z0;          // origin of the cell grid
+    double inv_cell;            // 1 / cell edge
+    int ncx, ncy, ncz;          // cells per axis (ncz = 1 in 2-D)
+    int mbits;                  // Morton bits per axis
+    long long bucket_base;      // first bucket of this type in the global bucket array
+    long long nbuckets;         // 2^(ndim*mbits)
+    int pos_begin, pos_end;     // range of this type in the sorted obs arrays
+    int nlocrad;
+    double locrad[ENKFG_MAXLOCRAD];
+    double locweight[ENKFG_MAXLOCRAD];
+    double rmax;                // max(locrad)
+    double rmax2;               // rmax * rmax (rounded as the reference rounds range*range)
+};
+
+struct enkfg_ctx {
+    int device;
+    cudaStream_t stream;
+    char err[1024];
+    long long launches;
+    float stage_ms[4];
+    cudaEvent_t ev[8];
+
+    // observation types
+    int ntypes;
+    int geographic;
+    int nlocrad[ENKFG_MAXTYPES];
+    double locrad[ENKFG_MAXTYPES][ENKFG_MAXLOCRAD];
+    double locweight[ENKFG_MAXTYPES][ENKFG_MAXLOCRAD];
+    double rfactor[ENKFG_MAXTYPES];
+    bool types_set;
+
+    // observations (original order)
+    int nobs;
+    float* d_lon;
+    float* d_lat;
+    short* d_type;
+    short* d_status;
+    float* d_estd;
+    float* d_value;
+    double* d_rfac;             // [ntypes]
+    bool obs_set;
+
+    // ensemble observations
+    int nmem, nmem_dyn;
+    float* d_S;                 // [nmem][nobs]
+    double* d_s;                // [nobs]
+    double* d_std;              // [nobs]
+    int s_mode;                 // 0 none, 1 HE, 2 HA (innovations done), 3 S (standardised)
+
+    // spatial index (rebuilt when obs or S change)
+    bool index_valid;
+    bool gather_valid;
+    int nsorted;                // obs with status OK
+    TypeIndex h_types[ENKFG_MAXTYPES];
+    TypeIndex* d_types;
+    long long nbuckets;
+    long long* d_bstart;        // [nbuckets + 1]
+    int* d_bfill;               // [nbuckets] scratch
+    int* d_key;                 // [nobs] scratch
+    int* d_sid;                 // [nsorted] obs id at sorted position
+    double* d_sx;               // [nsorted] kd coordinates in sorted order
+    double* d_sy;
+    double* d_sz;
+    short* d_stype;             // [nsorted]
+    int mpad;                   // member stride of d_St (multiple of 4)
+    float* d_St;                // [nsorted][mpad] standardised S, sorted, member-contiguous
+    double* d_ss;               // [nsorted] standardised innovation, sorted
+    double* d_ox;               // [nobs] kd coordinates (original order)
+    double* d_oy;
+    double* d_oz;
+
+    // grid
+    bool grid_set;
+    int mni, mnj, stride, periodic_i, ni, nj;
+    double* d_qx;               // [nj*ni] query coordinates of the strided points
+    double* d_qy;
+    double* d_qz;
+
+    // transforms (resident)
+    int t_mode, t_nmem, t_ndyn;
+    bool t_valid;
+    float* d_T;                 // [nj*ni][ndyn][nmem]
+    float* d_w;                 // [nj*ni][nmem]
+    double* d_T64;
+    double* d_w64;
+    size_t T_cap, w_cap, T64_cap, w64_cap;
+    int* d_nlobs;
+    float* d_dfs;
+    float* d_srf;
+    int* d_pnlobs;
+    float* d_pdfs;
+    float* d_psrf;
+    size_t nlobs_cap, dfs_cap, srf_cap, pnlobs_cap, pdfs_cap, psrf_cap;
+
+    // work queue / scratch
+    int* d_counts;              // [npoints]
+    int* d_order;               // [npoints]
+    int* d_qhead;               // queue head + error flag
+    int* d_status_pt;           // [npoints] per-point status
+    void* d_scratch;
+    size_t scratch_cap;
+    size_t counts_cap, order_cap, status_cap;
+
+    // update scratch
+    int* d_numlevels;
+    size_t numlevels_cap;
+    float* d_fields;
+    size_t fields_cap;
+    float* d_infl;
+    size_t infl_cap;
+};
+
+// ---------------------------------------------------------------------------
+// helpers
+// ---------------------------------------------------------------------------
+void set_err(enkfg_ctx* c, const char* fmt, ...);
+enkfg_status cuda_fail(enkfg_ctx* c, cudaError_t e, const char* what, int line);
+
+#define CK(call)                                                        \
+    do {                                                                \
+        cudaError_t e_ = (call);                                        \
+        if (e_ != cudaSuccess) return cuda_fail(ctx, e_, #call, __LINE__); \
+    } while (0)
+
+#define CKL()                                                           \
+    do {                                                                \
+        ctx->launches++;                                                \
+        cudaError_t e_ = cudaGetLastError();                            \
+        if (e_ != cudaSuccess) return cuda_fail(ctx, e_, "kernel launch", __LINE__); \
+    } while (0)
+
+template <typename T>
+static inline enkfg_status ensure(enkfg_ctx* ctx, T** p, size_t* cap, size_t n)
+{
+    if (n == 0) n = 1;
+    if (*p != nullptr && *cap >= n) return ENKFG_OK;
+    if (*p) cudaFree(*p);
+    *p = nullptr;
+    *cap = 0;
+    cudaError_t e = cudaMalloc((void**)p, n * sizeof(T));
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        set_err(ctx, "cudaMalloc of %zu bytes failed: %s", n * sizeof(T), cudaGetErrorString(e));
+        return ENKFG_ENOMEM;
+    }
+    *cap = n;
+    return ENKFG_OK;
+}
+
+static inline int div_up(long long a, long long b) { return (int)((a + b - 1) / b); }
+
+// exclusive scan of int counts into long long offsets (device), n entries;
+// offsets[n] = total.  Uses ctx scratch.
+enkfg_status scan_counts(enkfg_ctx* ctx, const int* d_in, long long* d_out, long long n, cudaStream_t st);
+
+// stages implemented in the .cu files
+enkfg_status build_index(enkfg_ctx* ctx, cudaStream_t st);
+enkfg_status build_gather(enkfg_ctx* ctx, cudaStream_t st);
+enkfg_status count_local(enkfg_ctx* ctx, int* d_counts, int* d_pcounts, cudaStream_t st);
+enkfg_status list_local(enkfg_ctx* ctx, const long long* d_offsets, int* d_ids, double* d_coeffs, cudaStream_t st);
+enkfg_status run_transforms(enkfg_ctx* ctx, const enkfg_calc_params* p, cudaStream_t st);
+enkfg_status run_update(enkfg_ctx* ctx, const enkfg_update_params* p, const int* d_numlevels, int nfield,
+                        const int* levels, float* d_fields, float* d_infl, cudaStream_t st);
+enkfg_status run_innovations(enkfg_ctx* ctx, cudaStream_t st);
+enkfg_status run_standardise(enkfg_ctx* ctx, cudaStream_t st);
+enkfg_status run_hybrid(enkfg_ctx* ctx, int nmem, int nmem_d, double gamma, int nij, float* d_v, cudaStream_t st);

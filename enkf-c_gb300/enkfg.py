@@ -1,0 +1,315 @@
+"""Python binding of libenkfg (the C ABI in include/enkfg.h).
+
+The class `Enkfg` exposes the device path under the names of the EnKF-C
+routines it replaces (reference enkf/ tree):
+
+  set_obstypes / set_obs        obstypes.c:170-560, observations.c:452 (obs_read)
+  set_HE                        das->S in S_MODE_HE_f (dasystem.h:95)
+  calcinnandspread              das_calcinnandspread (calc/ensobs.c:541)
+  standardise                   das_standardise (calc/ensobs.c:849)
+  findlocal                     obs_findlocal (common/observations.c:1837), all points
+  calctransforms                das_calctransforms (calc/transforms.c:991)
+  updatefields / updatebg       das_updatefields / das_updatebg (update/update.c:92, 568)
+  sethybridensemble             das_sethybridensemble (common/dasystem.c:775)
+
+The reference stops the program on any error (enkf_quit); here every failing
+call raises `EnkfgError` carrying the status code and the library's message.
+There is no CPU fallback: if libenkfg.so cannot be loaded, or no GPU is
+present, construction fails.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from typing import Optional
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIBPATH = os.path.join(_HERE, "_lib", "libenkfg.so")
+
+MODE_ENKF, MODE_ENOI, MODE_HYBRID = 0, 1, 2
+SCHEME_DENKF, SCHEME_ETKF = 0, 1
+PATH_PLAIN, PATH_BATCHED = 0, 1
+PREC_FP64, PREC_MIXED = 0, 1
+MAXLOCRAD = 8
+
+STATUS = {0: "OK", 1: "EINVAL", 2: "ECUDA", 3: "ENOMEM", 4: "ETIMEOUT", 5: "ENUMERIC", 6: "ECAPACITY",
+          7: "ESTATE", 8: "EUNSUPPORTED"}
+
+# every symbol include/enkfg.h declares
+EXPORTS = ["enkfg_create", "enkfg_destroy", "enkfg_last_error", "enkfg_status_string", "enkfg_version",
+           "enkfg_set_obstypes", "enkfg_set_obs", "enkfg_set_HE", "enkfg_calc_innovations", "enkfg_standardise",
+           "enkfg_set_S", "enkfg_get_S", "enkfg_set_grid", "enkfg_transform_dims", "enkfg_local_obs",
+           "enkfg_calc_transforms", "enkfg_calc_transforms_dev", "enkfg_transforms_dev_ptr",
+           "enkfg_set_transforms", "enkfg_update_fields", "enkfg_update_fields_dev", "enkfg_set_hybrid_ensemble",
+           "enkfg_set_hybrid_ensemble_dev", "enkfg_kernel_launches", "enkfg_stage_times"]
+
+
+class EnkfgError(RuntimeError):
+    def __init__(self, status: int, msg: str):
+        super().__init__(f"{STATUS.get(status, status)}: {msg}")
+        self.status = status
+
+
+class Grid(C.Structure):
+    _fields_ = [("mni", C.c_int), ("mnj", C.c_int), ("x", C.POINTER(C.c_double)), ("y", C.POINTER(C.c_double)),
+                ("x2d", C.POINTER(C.c_double)), ("y2d", C.POINTER(C.c_double)), ("stride", C.c_int),
+                ("periodic_i", C.c_int)]
+
+
+class CalcParams(C.Structure):
+    _fields_ = [("mode", C.c_int), ("scheme", C.c_int), ("alpha", C.c_double), ("path", C.c_int),
+                ("precision", C.c_int), ("want_diag", C.c_int)]
+
+
+class Diag(C.Structure):
+    _fields_ = [("nlobs", C.POINTER(C.c_int)), ("dfs", C.POINTER(C.c_float)), ("srf", C.POINTER(C.c_float)),
+                ("pnlobs", C.POINTER(C.c_int)), ("pdfs", C.POINTER(C.c_float)), ("psrf", C.POINTER(C.c_float))]
+
+
+class UpdateParams(C.Structure):
+    _fields_ = [("mode", C.c_int), ("nmem", C.c_int), ("nmem_dynamic", C.c_int), ("surfk", C.c_int),
+                ("issurfacevar", C.c_int), ("inflation", C.c_float), ("inf_ratio", C.c_double),
+                ("output_increment", C.c_int), ("applylog", C.c_int), ("j1", C.c_int), ("j2", C.c_int),
+                ("precision", C.c_int)]
+
+
+_lib = None
+
+
+def load(path: str = LIBPATH):
+    """Load libenkfg.so (raises if it is missing: there is no fallback)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(path):
+            raise FileNotFoundError(f"{path} is missing; build it with enkf-c_gb300/build.py")
+        L = C.CDLL(path)
+        L.enkfg_last_error.restype = C.c_char_p
+        L.enkfg_status_string.restype = C.c_char_p
+        L.enkfg_kernel_launches.restype = C.c_longlong
+        L.enkfg_create.argtypes = [C.c_int, C.POINTER(C.c_void_p)]
+        L.enkfg_destroy.argtypes = [C.c_void_p]
+        L.enkfg_last_error.argtypes = [C.c_void_p]
+        L.enkfg_kernel_launches.argtypes = [C.c_void_p]
+        _lib = L
+    return _lib
+
+
+def _p(a, t):
+    return None if a is None else a.ctypes.data_as(C.POINTER(t))
+
+
+class Enkfg:
+    """One device context (one GPU, one host thread)."""
+
+    def __init__(self, device: int = 0):
+        L = load()
+        h = C.c_void_p()
+        st = L.enkfg_create(device, C.byref(h))
+        if st != 0:
+            raise EnkfgError(st, "enkfg_create failed (no CUDA device?)")
+        self.h = h
+        self.L = L
+        self.nobs = 0
+        self.nmem = self.nmem_dynamic = 0
+        self.ntypes = 0
+        self.grid = None
+        self.nj = self.ni = 0
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.enkfg_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _ck(self, st):
+        if st != 0:
+            raise EnkfgError(st, self.L.enkfg_last_error(self.h).decode())
+
+    @property
+    def launches(self) -> int:
+        return int(self.L.enkfg_kernel_launches(self.h))
+
+    def stage_times(self):
+        ms = (C.c_float * 4)()
+        self._ck(self.L.enkfg_stage_times(self.h, ms))
+        return list(ms)
+
+    # ---- inputs ----------------------------------------------------------
+    def set_obstypes(self, nlocrad, locrad, locweight=None, rfactor=None, geographic=False):
+        nlocrad = np.ascontiguousarray(nlocrad, np.int32)
+        self.ntypes = nlocrad.size
+        lr = np.ascontiguousarray(locrad, np.float64).reshape(self.ntypes, MAXLOCRAD)
+        lw = None if locweight is None else np.ascontiguousarray(locweight, np.float64).reshape(self.ntypes, MAXLOCRAD)
+        rf = None if rfactor is None else np.ascontiguousarray(rfactor, np.float64)
+        self._keep_types = (nlocrad, lr, lw, rf)
+        self._ck(self.L.enkfg_set_obstypes(self.h, C.c_int(self.ntypes), _p(nlocrad, C.c_int), _p(lr, C.c_double),
+                                           _p(lw, C.c_double), _p(rf, C.c_double), C.c_int(int(geographic))))
+
+    def set_obs(self, lon, lat, otype, status, estd=None, value=None):
+        lon = np.ascontiguousarray(lon, np.float32)
+        lat = np.ascontiguousarray(lat, np.float32)
+        otype = np.ascontiguousarray(otype, np.int16)
+        status = np.ascontiguousarray(status, np.int16)
+        estd = None if estd is None else np.ascontiguousarray(estd, np.float32)
+        value = None if value is None else np.ascontiguousarray(value, np.float32)
+        self.nobs = lon.size
+        self._ck(self.L.enkfg_set_obs(self.h, C.c_int(self.nobs), _p(lon, C.c_float), _p(lat, C.c_float),
+                                      _p(otype, C.c_short), _p(status, C.c_short), _p(estd, C.c_float),
+                                      _p(value, C.c_float)))
+
+    def set_HE(self, HE, nmem_dynamic=None):
+        HE = np.ascontiguousarray(HE, np.float32)
+        m = HE.shape[0]
+        md = m if nmem_dynamic is None else int(nmem_dynamic)
+        self.nmem, self.nmem_dynamic = m, md
+        self._ck(self.L.enkfg_set_HE(self.h, C.c_int(m), C.c_int(md), _p(HE, C.c_float)))
+
+    def calcinnandspread(self):
+        s_f = np.zeros(self.nobs)
+        std_f = np.zeros(self.nobs)
+        self._ck(self.L.enkfg_calc_innovations(self.h, _p(s_f, C.c_double), _p(std_f, C.c_double)))
+        return s_f, std_f
+
+    def standardise(self):
+        self._ck(self.L.enkfg_standardise(self.h))
+
+    def set_S(self, S, s, nmem_dynamic=None):
+        S = np.ascontiguousarray(S, np.float32)
+        s = np.ascontiguousarray(s, np.float64)
+        m = S.shape[0]
+        md = m if nmem_dynamic is None else int(nmem_dynamic)
+        self.nmem, self.nmem_dynamic = m, md
+        self._ck(self.L.enkfg_set_S(self.h, C.c_int(m), C.c_int(md), _p(S, C.c_float), _p(s, C.c_double)))
+
+    def get_S(self):
+        S = np.zeros((self.nmem, self.nobs), np.float32)
+        s = np.zeros(self.nobs)
+        self._ck(self.L.enkfg_get_S(self.h, _p(S, C.c_float), _p(s, C.c_double)))
+        return S, s
+
+    def set_grid(self, x=None, y=None, stride=1, periodic_i=False, x2d=None, y2d=None):
+        if x2d is not None:
+            x2d = np.ascontiguousarray(x2d, np.float64)
+            y2d = np.ascontiguousarray(y2d, np.float64)
+            mnj, mni = x2d.shape
+            g = Grid(mni, mnj, None, None, _p(x2d, C.c_double), _p(y2d, C.c_double), stride, int(periodic_i))
+            keep = (x2d, y2d)
+        else:
+            x = np.ascontiguousarray(x, np.float64)
+            y = np.ascontiguousarray(y, np.float64)
+            mni, mnj = x.size, y.size
+            g = Grid(mni, mnj, _p(x, C.c_double), _p(y, C.c_double), None, None, stride, int(periodic_i))
+            keep = (x, y)
+        self._ck(self.L.enkfg_set_grid(self.h, C.byref(g)))
+        self._keep_grid = keep
+        self.mni, self.mnj, self.stride = mni, mnj, stride
+        nj, ni = C.c_int(), C.c_int()
+        self._ck(self.L.enkfg_transform_dims(self.h, C.byref(nj), C.byref(ni)))
+        self.nj, self.ni = nj.value, ni.value
+
+    # ---- calc ------------------------------------------------------------
+    def findlocal(self, lists: bool = True, capacity: Optional[int] = None):
+        """Local obs of every strided point: counts [nj][ni] and, if lists,
+        (offsets [nj*ni+1], ids, coeffs) with each row sorted by obs id."""
+        npts = self.nj * self.ni
+        counts = np.zeros(npts, np.int32)
+        if not lists:
+            self._ck(self.L.enkfg_local_obs(self.h, _p(counts, C.c_int), None, None, None, C.c_longlong(0)))
+            return counts.reshape(self.nj, self.ni)
+        self._ck(self.L.enkfg_local_obs(self.h, _p(counts, C.c_int), None, None, None, C.c_longlong(0)))
+        total = int(counts.astype(np.int64).sum()) if capacity is None else int(capacity)
+        offsets = np.zeros(npts + 1, np.int64)
+        ids = np.zeros(max(total, 1), np.int32)
+        coeffs = np.zeros(max(total, 1), np.float64)
+        self._ck(self.L.enkfg_local_obs(self.h, _p(counts, C.c_int), _p(offsets, C.c_longlong), _p(ids, C.c_int),
+                                        _p(coeffs, C.c_double), C.c_longlong(total)))
+        return counts.reshape(self.nj, self.ni), offsets, ids[:total], coeffs[:total]
+
+    def calctransforms(self, mode=MODE_ENKF, scheme=SCHEME_ETKF, alpha=1.0, path=PATH_PLAIN, precision=PREC_FP64,
+                       want64=False, want_diag=True):
+        npts = self.nj * self.ni
+        m, md = self.nmem, self.nmem_dynamic
+        enkf = mode != MODE_ENOI
+        T = np.zeros((self.nj, self.ni, md, m), np.float32) if enkf else None
+        w = np.zeros((self.nj, self.ni, m), np.float32)
+        T64 = np.zeros((self.nj, self.ni, md, m)) if (want64 and enkf) else None
+        w64 = np.zeros((self.nj, self.ni, m)) if want64 else None
+        out = dict(T=T, w=w, T64=T64, w64=w64)
+        dg = None
+        if want_diag:
+            nt = self.ntypes
+            out.update(nlobs=np.zeros((self.nj, self.ni), np.int32), dfs=np.zeros((self.nj, self.ni), np.float32),
+                       srf=np.zeros((self.nj, self.ni), np.float32),
+                       pnlobs=np.zeros((nt, self.nj, self.ni), np.int32),
+                       pdfs=np.zeros((nt, self.nj, self.ni), np.float32),
+                       psrf=np.zeros((nt, self.nj, self.ni), np.float32))
+            dg = Diag(_p(out["nlobs"], C.c_int), _p(out["dfs"], C.c_float), _p(out["srf"], C.c_float),
+                      _p(out["pnlobs"], C.c_int), _p(out["pdfs"], C.c_float), _p(out["psrf"], C.c_float))
+        prm = CalcParams(mode, scheme, float(alpha), path, precision, int(want_diag))
+        self._ck(self.L.enkfg_calc_transforms(self.h, C.byref(prm), _p(T, C.c_float), _p(w, C.c_float),
+                                              _p(T64, C.c_double), _p(w64, C.c_double),
+                                              C.byref(dg) if dg is not None else None))
+        return out
+
+    def calctransforms_dev(self, mode=MODE_ENKF, scheme=SCHEME_ETKF, alpha=1.0, path=PATH_PLAIN,
+                           precision=PREC_FP64, want_diag=False, stream=None):
+        prm = CalcParams(mode, scheme, float(alpha), path, precision, int(want_diag))
+        self._ck(self.L.enkfg_calc_transforms_dev(self.h, C.byref(prm), C.c_void_p(stream)))
+
+    def set_transforms(self, T, w, mode=MODE_ENKF, nmem=None, nmem_dynamic=None):
+        w = np.ascontiguousarray(w, np.float32)
+        m = w.shape[-1] if nmem is None else nmem
+        md = (T.shape[-2] if T is not None else m) if nmem_dynamic is None else nmem_dynamic
+        T = None if T is None else np.ascontiguousarray(T, np.float32)
+        self._ck(self.L.enkfg_set_transforms(self.h, C.c_int(mode), C.c_int(m), C.c_int(md), _p(T, C.c_float),
+                                             _p(w, C.c_float)))
+
+    # ---- update ----------------------------------------------------------
+    def updatefields(self, fields, numlevels, levels, *, mode=MODE_ENKF, nmem=None, nmem_dynamic=None, surfk=0,
+                     issurfacevar=0, inflation=1.0, inf_ratio=float("nan"), output_increment=0, applylog=0, j1=0,
+                     j2=-1, precision=PREC_FP64, want_infl=False):
+        """fields [nfield][nmem(+1 for EnOI)][jsize][mni] float32, updated
+        and returned (a copy); levels [nfield]."""
+        f = np.ascontiguousarray(fields, np.float32).copy()
+        nl = np.ascontiguousarray(numlevels, np.int32)
+        lv = np.ascontiguousarray(levels, np.int32)
+        nfield = f.shape[0]
+        m = self.nmem if nmem is None else nmem
+        md = self.nmem_dynamic if nmem_dynamic is None else nmem_dynamic
+        infl = np.zeros((nfield,) + f.shape[2:], np.float32) if want_infl else None
+        prm = UpdateParams(mode, m, md, surfk, issurfacevar, C.c_float(inflation), float(inf_ratio),
+                           int(output_increment), int(applylog), j1, j2, precision)
+        self._ck(self.L.enkfg_update_fields(self.h, C.byref(prm), _p(nl, C.c_int), C.c_int(nfield), _p(lv, C.c_int),
+                                            _p(f, C.c_float), _p(infl, C.c_float)))
+        return (f, infl) if want_infl else f
+
+    def updatebg(self, fields, numlevels, levels, **kw):
+        kw["mode"] = MODE_ENOI
+        return self.updatefields(fields, numlevels, levels, **kw)
+
+    def updatefields_dev(self, fields_ptr, numlevels_ptr, nfield, levels, *, mode=MODE_ENKF, nmem=None,
+                         nmem_dynamic=None, surfk=0, issurfacevar=0, inflation=1.0, inf_ratio=float("nan"),
+                         output_increment=0, applylog=0, j1=0, j2=-1, precision=PREC_FP64, infl_ptr=None,
+                         stream=None):
+        lv = np.ascontiguousarray(levels, np.int32)
+        m = self.nmem if nmem is None else nmem
+        md = self.nmem_dynamic if nmem_dynamic is None else nmem_dynamic
+        prm = UpdateParams(mode, m, md, surfk, issurfacevar, C.c_float(inflation), float(inf_ratio),
+                           int(output_increment), int(applylog), j1, j2, precision)
+        self._ck(self.L.enkfg_update_fields_dev(self.h, C.byref(prm), C.c_void_p(numlevels_ptr), C.c_int(nfield),
+                                                _p(lv, C.c_int), C.c_void_p(fields_ptr), C.c_void_p(infl_ptr),
+                                                C.c_void_p(stream)))
+
+    def sethybridensemble(self, v, nmem_dynamic, gamma):
+        v = np.ascontiguousarray(v, np.float32).copy()
+        m, nij = v.shape[0], int(np.prod(v.shape[1:]))
+        self._ck(self.L.enkfg_set_hybrid_ensemble(self.h, C.c_int(m), C.c_int(nmem_dynamic), C.c_double(gamma),
+                                                  C.c_int(nij), _p(v, C.c_float)))
+        return v

@@ -1,0 +1,198 @@
+/*
+ * enkfg.h -- C ABI of the GB300 EnKF-C analysis hot path (libenkfg.so).
+ *
+ * The library replaces two host stages of EnKF-C with sm_103a CUDA kernels:
+ *   enkf_calc   : das_calctransforms  (reference calc/transforms.c:991-1637)
+ *   enkf_update : das_updatefields / das_updatebg  (update/update.c:92-814)
+ * together with the routines they call (obs_findlocal, calc_wT_etkf,
+ * calc_wT_denkf, calc_G/calc_w, das_calcinnandspread, das_standardise,
+ * das_sethybridensemble).  Each entry point below names the reference
+ * interface it stands in for.
+ *
+ * Conventions (unlike the reference, nothing aborts):
+ *   - every call returns an enkfg_status; enkfg_last_error() explains it;
+ *   - host buffers are owned by the caller, device buffers by the context;
+ *   - a context is bound to one GPU and is used from one host thread;
+ *   - array layouts are the reference's: S [nmem][nobs], transforms
+ *     T [nj][ni][m_dyn][m] and w [nj][ni][m] (transforms.nc, transforms.c:
+ *     54-94), fields [nmem][jsize][mni] per field-layer (update.c:92).
+ *   - device-pointer entry points (suffix _dev) take and return plain device
+ *     addresses and a cudaStream_t passed as void*; nothing is synchronised
+ *     on the host by them.
+ */
+#ifndef ENKFG_H
+#define ENKFG_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#if defined(__GNUC__)
+#define ENKFG_API __attribute__((visibility("default")))
+#else
+#define ENKFG_API
+#endif
+
+typedef enum {
+    ENKFG_OK = 0,
+    ENKFG_EINVAL = 1,           /* bad argument or inconsistent sizes */
+    ENKFG_ECUDA = 2,            /* a CUDA runtime call failed */
+    ENKFG_ENOMEM = 3,           /* device allocation failed */
+    ENKFG_ETIMEOUT = 4,         /* a bounded device wait gave up */
+    ENKFG_ENUMERIC = 5,         /* a per-point factorisation failed (info in last_error) */
+    ENKFG_ECAPACITY = 6,        /* an output or scratch capacity is too small */
+    ENKFG_ESTATE = 7,           /* call order: required inputs not set */
+    ENKFG_EUNSUPPORTED = 8      /* option not implemented on the device path */
+} enkfg_status;
+
+enum { ENKFG_MODE_ENKF = 0, ENKFG_MODE_ENOI = 1, ENKFG_MODE_HYBRID = 2 };        /* dasystem.h MODE_* */
+enum { ENKFG_SCHEME_DENKF = 0, ENKFG_SCHEME_ETKF = 1 };                          /* dasystem.h SCHEME_* */
+enum { ENKFG_PATH_PLAIN = 0, ENKFG_PATH_BATCHED = 1 };
+enum { ENKFG_PREC_FP64 = 0, ENKFG_PREC_MIXED = 1 };
+
+#define ENKFG_MAXLOCRAD 8
+#define ENKFG_MAXTYPES 32
+#define ENKFG_MAXMEM 160
+
+typedef struct enkfg_ctx enkfg_ctx;
+
+/* Context on CUDA device `device`.  Replaces the per-rank state EnKF-C keeps
+ * in dasystem/observations (dasystem.h:60-128) for the hot path. */
+ENKFG_API enkfg_status enkfg_create(int device, enkfg_ctx** ctx);
+ENKFG_API void enkfg_destroy(enkfg_ctx* ctx);
+ENKFG_API const char* enkfg_last_error(const enkfg_ctx* ctx);
+ENKFG_API const char* enkfg_status_string(enkfg_status st);
+ENKFG_API int enkfg_version(void);
+
+/* Observation types: LOCRAD/LOCWEIGHT/RFACTOR per type (obstypes.c:170-560,
+ * used by obstype_calclcoeff obstypes.c:800 and das_standardise ensobs.c:849).
+ * locrad/locweight are [ntypes][ENKFG_MAXLOCRAD]; geographic selects 3-D
+ * distances on the sphere (ll2xyz, utils.c:1449). */
+ENKFG_API enkfg_status enkfg_set_obstypes(enkfg_ctx* ctx, int ntypes, const int* nlocrad, const double* locrad, const double* locweight, const double* rfactor, int geographic);
+
+/* Observations (observation fields used on the path, observations.h:47-100):
+ * float lon/lat, type, status (0 = STATUS_OK), float estd and value. */
+ENKFG_API enkfg_status enkfg_set_obs(enkfg_ctx* ctx, int nobs, const float* lon, const float* lat, const short* type, const short* status, const float* estd, const float* value);
+
+/* Forecast ensemble observations HE [nmem][nobs] (das->S in S_MODE_HE_f,
+ * dasystem.h:95).  nmem_dynamic < nmem for hybrid ensembles. */
+ENKFG_API enkfg_status enkfg_set_HE(enkfg_ctx* ctx, int nmem, int nmem_dynamic, const float* HE);
+
+/* das_calcinnandspread (ensobs.c:541-690): HE -> HA in place on the device,
+ * innovations s_f = y - Hx and spread std_f; either output may be NULL. */
+ENKFG_API enkfg_status enkfg_calc_innovations(enkfg_ctx* ctx, double* s_f, double* std_f);
+
+/* das_standardise (ensobs.c:849-898): S and s_f divided by
+ * estd * sqrt(rfactor) * sqrt(nmem - 1), on the device. */
+ENKFG_API enkfg_status enkfg_standardise(enkfg_ctx* ctx);
+
+/* Set standardised S [nmem][nobs] and s [nobs] directly (the state
+ * das_calctransforms works on after das_standardise, S_MODE_S_f). */
+ENKFG_API enkfg_status enkfg_set_S(enkfg_ctx* ctx, int nmem, int nmem_dynamic, const float* S, const double* s);
+/* Copy the device S / s back (either may be NULL). */
+ENKFG_API enkfg_status enkfg_get_S(enkfg_ctx* ctx, float* S, double* s);
+
+/* Model grid of the analysed variables (rectangular: x[mni], y[mnj];
+ * curvilinear: x2d/y2d [mnj][mni], x/y NULL) with the transform stride and
+ * the periodic-i flag (grid_getstride, grid_isperiodic_i; hgrid_ij2xy,
+ * hgrid.c:457-472). */
+typedef struct {
+    int mni, mnj;
+    const double* x;
+    const double* y;
+    const double* x2d;
+    const double* y2d;
+    int stride;
+    int periodic_i;
+} enkfg_grid;
+ENKFG_API enkfg_status enkfg_set_grid(enkfg_ctx* ctx, const enkfg_grid* grid);
+
+/* Strided transform grid size: nj = (mnj-1)/stride+1, ni = (mni-1)/stride+1
+ * (transforms.c:1065-1072). */
+ENKFG_API enkfg_status enkfg_transform_dims(const enkfg_ctx* ctx, int* nj, int* ni);
+
+/* obs_findlocal (observations.c:1837-1927) for every strided grid point.
+ * counts [nj*ni] receives the local obs count per point.  If ids is not
+ * NULL, offsets [nj*ni+1] receives the CSR offsets and ids/coeffs the local
+ * observation ids (sorted by id) and their taper coefficients, up to
+ * `capacity` entries (ENKFG_ECAPACITY if the total exceeds it). */
+ENKFG_API enkfg_status enkfg_local_obs(enkfg_ctx* ctx, int* counts, long long* offsets, int* ids, double* coeffs, long long capacity);
+
+typedef struct {
+    int mode;                   /* ENKFG_MODE_* */
+    int scheme;                 /* ENKFG_SCHEME_* */
+    double alpha;               /* relaxation to prior, transforms.c:1270-1286 */
+    int path;                   /* ENKFG_PATH_PLAIN or ENKFG_PATH_BATCHED */
+    int precision;              /* ENKFG_PREC_FP64 or ENKFG_PREC_MIXED */
+    int want_diag;              /* fill the enkf_diag.nc outputs */
+} enkfg_calc_params;
+
+typedef struct {
+    int* nlobs;                 /* [nj][ni] */
+    float* dfs;                 /* [nj][ni] */
+    float* srf;                 /* [nj][ni] */
+    int* pnlobs;                /* [ntypes][nj][ni] */
+    float* pdfs;                /* [ntypes][nj][ni] */
+    float* psrf;                /* [ntypes][nj][ni] */
+} enkfg_diag;
+
+/* das_calctransforms (transforms.c:991-1637): for every strided point find
+ * the local obs, taper, form I + S'S, solve (ETKF eigen / DEnKF Cholesky /
+ * EnOI), relax to prior and write T [nj][ni][m_dyn][m] (NULL for EnOI) and
+ * w [nj][ni][m] as float, plus, if not NULL, the same in double before the
+ * float cast (T64, w64) and the diagnostics (enkf_diag.nc, transforms.c:
+ * 1298-1345).  Results stay resident on the device for enkfg_update_*. */
+ENKFG_API enkfg_status enkfg_calc_transforms(enkfg_ctx* ctx, const enkfg_calc_params* p, float* T, float* w, double* T64, double* w64, const enkfg_diag* diag);
+
+/* Device-resident form: computes into the context's device buffers on
+ * `stream` (NULL = the context stream) without host copies. */
+ENKFG_API enkfg_status enkfg_calc_transforms_dev(enkfg_ctx* ctx, const enkfg_calc_params* p, void* stream);
+/* Device addresses of the resident transforms (valid until the next calc). */
+ENKFG_API enkfg_status enkfg_transforms_dev_ptr(enkfg_ctx* ctx, float** T, float** w);
+/* Load transforms (e.g. read back from transforms.nc) into the context. */
+ENKFG_API enkfg_status enkfg_set_transforms(enkfg_ctx* ctx, int mode, int nmem, int nmem_dynamic, const float* T, const float* w);
+
+typedef struct {
+    int mode;                   /* ENKF / HYBRID: das_updatefields; ENOI: das_updatebg */
+    int nmem, nmem_dynamic;
+    int surfk;                  /* grid_getsurflayerid */
+    int issurfacevar;
+    float inflation;            /* INFLATION (model_getvarinflation) */
+    double inf_ratio;           /* NaN: plain multiplicative inflation */
+    int output_increment;       /* --output-increment */
+    int applylog;               /* variable stored as log10 */
+    int j1, j2;                 /* field tile rows (FIELDSPLIT), j1 % stride == 0; j2 < 0: all */
+    int precision;              /* ENKFG_PREC_FP64 (float CUDA cores) or ENKFG_PREC_MIXED */
+} enkfg_update_params;
+
+/* das_updatefields (update.c:92-564) for nfield field-layers sharing the
+ * grid: fields [nfield][nmem][jsize][mni] updated in place (host), levels
+ * [nfield] their layer index, numlevels [mnj][mni] the grid's wet-level
+ * count.  infl (or NULL) receives [nfield][jsize][mni] inflation
+ * (--write-inflation).  For ENKFG_MODE_ENOI the call is das_updatebg
+ * (update.c:568-814) and fields are [nfield][nmem+1][jsize][mni] with the
+ * background in slot nmem.  Uses the transforms resident in the context. */
+ENKFG_API enkfg_status enkfg_update_fields(enkfg_ctx* ctx, const enkfg_update_params* p, const int* numlevels, int nfield, const int* levels, float* fields, float* infl);
+
+/* Device-resident form: fields/infl are device addresses. */
+ENKFG_API enkfg_status enkfg_update_fields_dev(enkfg_ctx* ctx, const enkfg_update_params* p, const int* numlevels_dev, int nfield, const int* levels, float* fields_dev, float* infl_dev, void* stream);
+
+/* das_sethybridensemble (dasystem.c:775-819) on v [nmem][nij] (host, in
+ * place): dynamic anomalies scaled by k_d, static by k_s, both recentred on
+ * the dynamic mean. */
+ENKFG_API enkfg_status enkfg_set_hybrid_ensemble(enkfg_ctx* ctx, int nmem, int nmem_dynamic, double gamma, int nij, float* v);
+ENKFG_API enkfg_status enkfg_set_hybrid_ensemble_dev(enkfg_ctx* ctx, int nmem, int nmem_dynamic, double gamma, int nij, float* v_dev, void* stream);
+
+/* Number of kernels this context has launched (for launch accounting). */
+ENKFG_API long long enkfg_kernel_launches(const enkfg_ctx* ctx);
+/* Last stage timings in milliseconds, measured with CUDA events on the
+ * launching stream: [0] index build, [1] count/queue, [2] transforms,
+ * [3] update. */
+ENKFG_API enkfg_status enkfg_stage_times(const enkfg_ctx* ctx, float* ms4);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

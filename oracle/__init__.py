@@ -1,0 +1,353 @@
+"""CPU oracle for the EnKF-C analysis hot path -- TEST INFRASTRUCTURE ONLY.
+
+This package is the checker the GPU library is compared against (and the CPU
+baseline timed beside it).  Only tests, the smoke check and the CPU-baseline
+leg of the benchmark import it; the product never does.
+
+  liboracle.so       C restatement of the reference loops (enkf_oracle.c),
+                     built by oracle/Makefile on whichever machine runs it.
+  _ref/libenkf_ref.so the reference's own calc/calcs.c + common/kdtree.c,
+                     compiled unmodified by oracle/ref/Makefile where the
+                     reference sources exist; used to pin the restatement.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import glob
+import os
+import subprocess
+import threading
+from typing import Optional
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB = os.path.join(HERE, "liboracle.so")
+REFLIB = os.path.join(HERE, "_ref", "libenkf_ref.so")
+REFDIR = "/root/reference/enkf"
+MAXLOCRAD = 8
+
+_lock = threading.Lock()
+_lib = None
+_ref = None
+
+
+def blas_path() -> str:
+    """The OpenBLAS shipped inside the scipy (or numpy) wheel."""
+    import scipy
+    cands = []
+    for pkg in (scipy,):
+        d = os.path.join(os.path.dirname(pkg.__file__), "..", "scipy.libs")
+        cands += sorted(glob.glob(os.path.join(d, "libscipy_openblas*.so*")))
+    try:
+        import numpy
+        d = os.path.join(os.path.dirname(numpy.__file__), "..", "numpy.libs")
+        cands += sorted(glob.glob(os.path.join(d, "libscipy_openblas*.so*")))
+    except Exception:
+        pass
+    if not cands:
+        raise RuntimeError("no OpenBLAS found inside the scipy/numpy wheels")
+    return os.path.realpath(cands[0])
+
+
+def build(force: bool = False) -> str:
+    """Compile liboracle.so in place (and _ref when the reference is present)."""
+    if force or not os.path.exists(LIB) or os.path.getmtime(LIB) < max(
+            os.path.getmtime(os.path.join(HERE, f)) for f in ("enkf_oracle.c", "or_blas.c", "enkf_oracle.h")):
+        subprocess.run(["make", "-s", "-B" if force else "all"], cwd=HERE, check=True)
+    if os.path.isdir(REFDIR):
+        subprocess.run(["make", "-s", "REFDIR=" + REFDIR], cwd=os.path.join(HERE, "ref"), check=True)
+    return LIB
+
+
+def _p(a, t):
+    return a.ctypes.data_as(C.POINTER(t)) if a is not None else None
+
+
+def lib():
+    global _lib
+    with _lock:
+        if _lib is None:
+            build()
+            L = C.CDLL(LIB)
+            rc = L.or_blas_load(blas_path().encode())
+            if rc != 0:
+                raise RuntimeError(f"or_blas_load failed ({rc})")
+            L.or_obs_create.restype = C.c_void_p
+            L.or_findlocal.restype = C.c_int
+            L.or_taper_gc.restype = C.c_double
+            L.or_taper_gc.argtypes = [C.c_double]
+            L.or_calclcoeff.restype = C.c_double
+            L.or_calctransforms.restype = C.c_int
+            _lib = L
+    return _lib
+
+
+def reflib():
+    """The reference's own compiled numerics + kd-tree, or None if not built."""
+    global _ref
+    with _lock:
+        if _ref is None and os.path.exists(REFLIB):
+            L = C.CDLL(REFLIB)
+            if L.or_blas_load(blas_path().encode()) != 0:
+                return None
+            L.ref_kd_build.restype = C.c_void_p
+            L.ref_kd_build.argtypes = [C.c_int, C.c_int, C.c_void_p]
+            L.ref_kd_free.argtypes = [C.c_void_p]
+            L.ref_kd_range.argtypes = [C.c_void_p, C.c_void_p, C.c_double, C.c_int, C.c_void_p, C.c_void_p, C.c_int]
+            _ref = L
+    return _ref
+
+
+class CalcParams(C.Structure):
+    _fields_ = [("mode", C.c_int), ("scheme", C.c_int), ("nmem", C.c_int), ("nmem_dynamic", C.c_int),
+                ("alpha", C.c_double), ("stride", C.c_int), ("mni", C.c_int), ("mnj", C.c_int),
+                ("x", C.POINTER(C.c_double)), ("y", C.POINTER(C.c_double)),
+                ("x2d", C.POINTER(C.c_double)), ("y2d", C.POINTER(C.c_double))]
+
+
+class UpdateParams(C.Structure):
+    _fields_ = [("mode", C.c_int), ("nmem", C.c_int), ("nmem_dynamic", C.c_int), ("stride", C.c_int),
+                ("periodic_i", C.c_int), ("mni", C.c_int), ("mnj", C.c_int), ("ni", C.c_int), ("nj", C.c_int),
+                ("j1", C.c_int), ("j2", C.c_int), ("level", C.c_int), ("surfk", C.c_int),
+                ("issurfacevar", C.c_int), ("inflation0", C.c_float), ("inf_ratio", C.c_double),
+                ("output_increment", C.c_int), ("applylog", C.c_int)]
+
+
+def locrad_table(ntypes: int, locrad, locweight=None):
+    """[ntypes][MAXLOCRAD] radius / weight tables.  `locrad` is a scalar (one
+    radius for every type) or a per-type list of radius lists."""
+    nl = np.zeros(ntypes, np.int32)
+    lr = np.zeros((ntypes, MAXLOCRAD), np.float64)
+    lw = np.zeros((ntypes, MAXLOCRAD), np.float64)
+    for t in range(ntypes):
+        r = np.atleast_1d(np.asarray(locrad if np.isscalar(locrad) else locrad[t], np.float64))
+        wt = np.ones_like(r) if locweight is None else np.atleast_1d(np.asarray(locweight[t], np.float64))
+        nl[t] = r.size
+        lr[t, :r.size] = r
+        lw[t, :r.size] = wt
+    return nl, lr, lw
+
+
+class ObsSet:
+    """Observation set with per-type kd-trees (or_obs_create)."""
+
+    def __init__(self, lon, lat, otype, status, ntypes, nlocrad, locrad, locweight, nlobsmax=None,
+                 geographic=False):
+        L = lib()
+        self.lon = np.ascontiguousarray(lon, np.float32)
+        self.lat = np.ascontiguousarray(lat, np.float32)
+        self.otype = np.ascontiguousarray(otype, np.int16)
+        self.status = np.ascontiguousarray(status, np.int16)
+        self.ntypes = int(ntypes)
+        self.nlocrad = np.ascontiguousarray(nlocrad, np.int32)
+        self.locrad = np.ascontiguousarray(locrad, np.float64)
+        self.locweight = np.ascontiguousarray(locweight, np.float64)
+        nlm = None if nlobsmax is None else np.ascontiguousarray(nlobsmax, np.int32)
+        self.h = L.or_obs_create(C.c_int(self.lon.size), _p(self.lon, C.c_float), _p(self.lat, C.c_float),
+                                 _p(self.otype, C.c_short), _p(self.status, C.c_short), C.c_int(self.ntypes),
+                                 _p(self.nlocrad, C.c_int), _p(self.locrad, C.c_double),
+                                 _p(self.locweight, C.c_double), _p(nlm, C.c_int), C.c_int(int(geographic)))
+        self.nobs = self.lon.size
+
+    def __del__(self):
+        try:
+            lib().or_obs_destroy(C.c_void_p(self.h))
+        except Exception:
+            pass
+
+    def findlocal(self, x: float, y: float):
+        cap = max(self.nobs, 1)
+        ids = np.empty(cap, np.int32)
+        lc = np.empty(cap, np.float64)
+        n = lib().or_findlocal(C.c_void_p(self.h), C.c_double(x), C.c_double(y), _p(ids, C.c_int),
+                               _p(lc, C.c_double), C.c_int(cap))
+        assert n >= 0
+        return ids[:n].copy(), lc[:n].copy()
+
+
+def taper_gc(x: float) -> float:
+    return lib().or_taper_gc(float(x))
+
+
+def calc_wT(mode, scheme, m, mout, s, S):
+    """Per-point numerics; S is [m][p].  Returns (w, T [m][m], G [p][m])."""
+    S = np.ascontiguousarray(S, np.float64).copy()
+    s = np.ascontiguousarray(s, np.float64)
+    p = S.shape[1]
+    w = np.zeros(m)
+    T = np.zeros((m, m))
+    G = np.zeros((p, m))
+    rc = lib().or_calc_wT(C.c_int(mode), C.c_int(scheme), C.c_int(m), C.c_int(mout), C.c_int(p),
+                          _p(s, C.c_double), _p(S, C.c_double), _p(w, C.c_double), _p(T, C.c_double),
+                          _p(G, C.c_double))
+    if rc != 0:
+        raise RuntimeError(f"LAPACK info {rc}")
+    return w, T, G
+
+
+def ref_calc_wT(mode, scheme, m, mout, s, S):
+    """The same through the reference's own calcs.c (needs oracle/_ref)."""
+    L = reflib()
+    if L is None:
+        raise RuntimeError("reference library not built")
+    S = np.ascontiguousarray(S, np.float64).copy()
+    s = np.ascontiguousarray(s, np.float64).copy()
+    p = S.shape[1]
+    w = np.zeros(m)
+    T = np.zeros((m, m))
+    G = np.zeros((p, m))
+    L.ref_calc_wT(C.c_int(mode), C.c_int(scheme), C.c_int(m), C.c_int(mout), C.c_int(p), _p(s, C.c_double),
+                  _p(S, C.c_double), _p(w, C.c_double), _p(T, C.c_double), _p(G, C.c_double))
+    return w, T, G
+
+
+class RefKdTree:
+    """A reference kd-tree (common/kdtree.c) built as obs_createkdtrees does."""
+
+    def __init__(self, coords: np.ndarray):
+        L = reflib()
+        self.coords = np.ascontiguousarray(coords, np.float64)
+        self.ndim = self.coords.shape[1]
+        self.n = self.coords.shape[0]
+        self.h = L.ref_kd_build(self.ndim, self.n, self.coords.ctypes.data)
+
+    def __del__(self):
+        try:
+            reflib().ref_kd_free(self.h)
+        except Exception:
+            pass
+
+    def range(self, q, r, ordered=False):
+        q = np.ascontiguousarray(q, np.float64)
+        cap = max(self.n, 1)
+        data = np.empty(cap, np.int32)
+        d2 = np.empty(cap, np.float64)
+        n = reflib().ref_kd_range(self.h, q.ctypes.data, float(r), int(ordered), data.ctypes.data,
+                                  d2.ctypes.data, cap)
+        assert n >= 0
+        return data[:n].copy(), d2[:n].copy()
+
+
+def calcinnandspread(HE, value, status):
+    S = np.ascontiguousarray(HE, np.float32).copy()
+    m, n = S.shape
+    s_f = np.zeros(n)
+    std_f = np.zeros(n)
+    lib().or_calcinnandspread(C.c_int(m), C.c_int(n), _p(S, C.c_float), _p(np.ascontiguousarray(value, np.float32), C.c_float),
+                              _p(np.ascontiguousarray(status, np.int16), C.c_short), _p(s_f, C.c_double),
+                              _p(std_f, C.c_double))
+    return S, s_f, std_f
+
+
+def standardise(S, s_f, estd, otype, rfactor):
+    S = np.ascontiguousarray(S, np.float32).copy()
+    s_f = np.ascontiguousarray(s_f, np.float64).copy()
+    m, n = S.shape
+    lib().or_standardise(C.c_int(m), C.c_int(n), _p(S, C.c_float), _p(s_f, C.c_double),
+                         _p(np.ascontiguousarray(estd, np.float32), C.c_float),
+                         _p(np.ascontiguousarray(otype, np.int16), C.c_short),
+                         _p(np.ascontiguousarray(rfactor, np.float64), C.c_double))
+    return S, s_f
+
+
+def calctransforms(obs: ObsSet, *, mode, scheme, nmem, nmem_dynamic, alpha, stride, x, y, S, s,
+                   rows=None, threads: int = 1, want64=False, want_diag=True, x2d=None, y2d=None):
+    """das_calctransforms over strided rows `rows` (default all), run on
+    `threads` host threads (contiguous row blocks, as distribute_iterations
+    assigns them).  Returns a dict of full-size outputs."""
+    x = np.ascontiguousarray(x, np.float64)
+    y = np.ascontiguousarray(y, np.float64)
+    mni = x.size if x2d is None else x2d.shape[1]
+    mnj = y.size if y2d is None else y2d.shape[0]
+    nj = (mnj - 1) // stride + 1
+    ni = (mni - 1) // stride + 1
+    m, md = nmem, nmem_dynamic
+    enkf = mode in (0, 2)
+    S = np.ascontiguousarray(S, np.float32)
+    s = np.ascontiguousarray(s, np.float64)
+    T = np.zeros((nj, ni, md, m), np.float32) if enkf else None
+    w = np.zeros((nj, ni, m), np.float32)
+    T64 = np.zeros((nj, ni, md, m)) if (want64 and enkf) else None
+    w64 = np.zeros((nj, ni, m)) if want64 else None
+    nt = obs.ntypes
+    nlobs = np.zeros((nj, ni), np.int32) if want_diag else None
+    dfs = np.zeros((nj, ni), np.float32) if want_diag else None
+    srf = np.zeros((nj, ni), np.float32) if want_diag else None
+    pn = np.zeros((nt, nj, ni), np.int32) if want_diag else None
+    pd = np.zeros((nt, nj, ni), np.float32) if want_diag else None
+    ps = np.zeros((nt, nj, ni), np.float32) if want_diag else None
+    x2 = None if x2d is None else np.ascontiguousarray(x2d, np.float64)
+    y2 = None if y2d is None else np.ascontiguousarray(y2d, np.float64)
+    P = CalcParams(mode, scheme, m, md, float(alpha), stride, mni, mnj, _p(x, C.c_double), _p(y, C.c_double),
+                   _p(x2, C.c_double), _p(y2, C.c_double))
+    r0, r1 = (0, nj) if rows is None else rows
+    L = lib()
+    rcs = []
+
+    def run(a, b):
+        rc = L.or_calctransforms(C.c_void_p(obs.h), C.byref(P), _p(S, C.c_float), _p(s, C.c_double),
+                                 _p(obs.otype, C.c_short), C.c_int(a), C.c_int(b), _p(T, C.c_float),
+                                 _p(w, C.c_float), _p(T64, C.c_double), _p(w64, C.c_double), _p(nlobs, C.c_int),
+                                 _p(dfs, C.c_float), _p(srf, C.c_float), _p(pn, C.c_int), _p(pd, C.c_float),
+                                 _p(ps, C.c_float))
+        rcs.append(rc)
+
+    threads = max(1, min(threads, r1 - r0))
+    if threads == 1:
+        run(r0, r1)
+    else:
+        bounds = np.linspace(r0, r1, threads + 1).astype(int)
+        ts = [threading.Thread(target=run, args=(int(bounds[k]), int(bounds[k + 1]))) for k in range(threads)]
+        for t in ts:
+            t.start()
+        for t in ts:
+            t.join()
+    if any(rcs):
+        raise RuntimeError(f"LAPACK failure {rcs}")
+    return dict(T=T, w=w, T64=T64, w64=w64, nlobs=nlobs, dfs=dfs, srf=srf, pnlobs=pn, pdfs=pd, psrf=ps)
+
+
+def updatefields(v, T, w, numlevels, *, mode, nmem, nmem_dynamic, stride, periodic_i=0, level=0, surfk=0,
+                 issurfacevar=0, inflation=1.0, inf_ratio=float("nan"), output_increment=0, applylog=0,
+                 j1=0, j2=None, want_infl=False):
+    """das_updatefields for one field-layer. v is [nmem][jsize][mni] (copied)."""
+    v = np.ascontiguousarray(v, np.float32).copy()
+    nl = np.ascontiguousarray(numlevels, np.int32)
+    mnj, mni = nl.shape
+    nj, ni = w.shape[:2]
+    if j2 is None:
+        j2 = mnj - 1
+    infl = np.zeros((j2 - j1 + 1, mni), np.float32) if want_infl else None
+    P = UpdateParams(mode, nmem, nmem_dynamic, stride, periodic_i, mni, mnj, ni, nj, j1, j2, level, surfk,
+                     issurfacevar, C.c_float(inflation), float(inf_ratio), output_increment, applylog)
+    Tc = np.ascontiguousarray(T, np.float32)
+    wc = np.ascontiguousarray(w, np.float32)
+    lib().or_updatefields(C.byref(P), _p(Tc, C.c_float), _p(wc, C.c_float), _p(nl, C.c_int), _p(v, C.c_float),
+                          _p(infl, C.c_float))
+    return (v, infl) if want_infl else v
+
+
+def updatebg(v, w, numlevels, *, nmem, stride, periodic_i=0, level=0, surfk=0, issurfacevar=0, j1=0, j2=None):
+    """das_updatebg for one field-layer. v is [nmem + 1][jsize][mni] (copied)."""
+    v = np.ascontiguousarray(v, np.float32).copy()
+    nl = np.ascontiguousarray(numlevels, np.int32)
+    mnj, mni = nl.shape
+    nj, ni = w.shape[:2]
+    if j2 is None:
+        j2 = mnj - 1
+    P = UpdateParams(1, nmem, nmem, stride, periodic_i, mni, mnj, ni, nj, j1, j2, level, surfk, issurfacevar,
+                     C.c_float(1.0), float("nan"), 0, 0)
+    wc = np.ascontiguousarray(w, np.float32)
+    lib().or_updatebg(C.byref(P), _p(wc, C.c_float), _p(nl, C.c_int), _p(v, C.c_float))
+    return v
+
+
+def sethybridensemble(v, nmem_d, gamma):
+    """das_sethybridensemble. v is [nmem][nij] (copied). Returns (v, vmean)."""
+    v = np.ascontiguousarray(v, np.float32).copy()
+    m, nij = v.shape
+    vmean = np.zeros(nij)
+    lib().or_sethybridensemble(C.c_int(m), C.c_int(nmem_d), C.c_int(m - nmem_d), C.c_double(gamma),
+                               C.c_int(nij), _p(v, C.c_float), _p(vmean, C.c_double))
+    return v, vmean

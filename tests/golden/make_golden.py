@@ -1,0 +1,122 @@
+"""Generate the golden fixtures under tests/golden/ from the REFERENCE itself.
+
+Run in a container that holds the reference sources (it builds
+oracle/_ref/libenkf_ref.so from the reference's calc/calcs.c and
+common/kdtree.c, unmodified).  The fixtures pin the oracle restatement and the
+GPU library without needing the reference at test time:
+
+  numerics.npz    calc_wT_etkf / calc_wT_denkf / calc_G+calc_w (calcs.c) on
+                  seeded S, s for p < m and p >= m: outputs w, T, G.
+  kdtree.npz      kd_findnodeswithinrange (kdtree.c) results, in the tree's
+                  own order, for trees built as obs_createkdtrees does
+                  (sequential insertion by obs index), several query points,
+                  two observation types.
+  transforms.npz  das_calctransforms on a sample of workload-1 points: local
+                  obs from the reference kd-tree, taper and gather as
+                  transforms.c:1250-1258 (restated here), numerics from the
+                  reference's calcs.c: double T and w before the float cast.
+                  The inputs (obs, S, s) are stored alongside.
+
+Usage:  python tests/golden/make_golden.py
+"""
+from __future__ import annotations
+
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+sys.path.insert(0, os.path.join(ROOT, "enkf-c_gb300"))
+
+import oracle  # noqa: E402
+import synth  # noqa: E402
+
+
+def numerics():
+    rng = np.random.default_rng(20240)
+    cases = []
+    for (m, mout, p) in [(24, 24, 60), (24, 24, 7), (24, 16, 40), (48, 48, 48), (48, 48, 300), (96, 96, 150),
+                         (96, 64, 20)]:
+        S = rng.standard_normal((m, p)) * (0.5 / np.sqrt(m - 1)) * rng.uniform(0.2, 3.0)
+        S -= S.mean(axis=0, keepdims=True)   # anomalies: columns of HA sum to zero
+        s = rng.standard_normal(p)
+        for mode, scheme in [(0, 1), (0, 0), (1, 0)]:
+            w, T, G = oracle.ref_calc_wT(mode, scheme, m, mout, s, S)
+            cases.append(dict(m=m, mout=mout, p=p, mode=mode, scheme=scheme, S=S, s=s, w=w, T=T[:mout] if mode != 1 else T[:0], G=G))
+    out = {}
+    for k, c in enumerate(cases):
+        for key, v in c.items():
+            out[f"c{k}_{key}"] = np.asarray(v)
+    out["ncases"] = np.array(len(cases))
+    np.savez_compressed(os.path.join(HERE, "numerics.npz"), **out)
+    print("numerics:", len(cases), "cases")
+
+
+def kdtree():
+    w = synth.make(2, scale=0.12, with_fields=False)
+    coords = np.stack([w.lon.astype(np.float64), w.lat.astype(np.float64)], 1)
+    rng = np.random.default_rng(7)
+    qs = np.stack([rng.uniform(0, w.ni - 1, 40), rng.uniform(0, w.nj - 1, 40)], 1)
+    qs[:8] = np.floor(qs[:8])           # grid points (integer coordinates)
+    out = dict(lon=w.lon, lat=w.lat, otype=w.otype, q=qs, r=np.array([6.0, 9.0]))
+    for t in range(w.ntypes):
+        ids = np.nonzero(w.otype == t)[0]
+        tree = oracle.RefKdTree(coords[ids])
+        for k, q in enumerate(qs):
+            d, d2 = tree.range(q, out["r"][t])
+            out[f"t{t}_q{k}_ids"] = ids[d].astype(np.int32)
+            out[f"t{t}_q{k}_d2"] = d2
+    np.savez_compressed(os.path.join(HERE, "kdtree.npz"), **out)
+    print("kdtree:", w.nobs, "obs,", len(qs), "queries")
+
+
+def transforms():
+    w = synth.make(1, with_fields=False)
+    S, s_f, _ = oracle.calcinnandspread(w.HE, w.value, w.status)
+    S, s = oracle.standardise(S, s_f, w.estd, w.otype, np.ones(w.ntypes))
+    m = w.nmem
+    coords = np.stack([w.lon.astype(np.float64), w.lat.astype(np.float64)], 1)
+    tree = oracle.RefKdTree(coords)      # one type, all status OK
+    rng = np.random.default_rng(11)
+    npts = w.nanalyses
+    pts = np.sort(rng.choice(npts, 160, replace=False))
+    T64 = np.zeros((pts.size, m, m))
+    w64 = np.zeros((pts.size, m))
+    nl = np.zeros(pts.size, np.int32)
+    for k, pt in enumerate(pts):
+        jj, ii = divmod(int(pt), w.ni_s)
+        q = np.array([w.x[ii * w.stride], w.y[jj * w.stride]])
+        d, d2 = tree.range(q, w.locrad)
+        lobs = d
+        lc = np.array([oracle.taper_gc(np.sqrt(v) / w.locrad) for v in d2])
+        nl[k] = lobs.size
+        if lobs.size == 0:
+            T64[k] = np.eye(m)
+            continue
+        Sloc = S[:, lobs].astype(np.float64) * lc[None, :]
+        sloc = s[lobs] * lc
+        ww, T, G = oracle.ref_calc_wT(w.mode, w.scheme, m, m, sloc, Sloc)
+        # relaxation to prior with alpha = 1 (transforms.c:1276-1286)
+        for e1 in range(m):
+            T[e1, e1] -= 1.0
+            T[e1, :] *= w.alpha
+            T[e1, e1] += 1.0
+        T64[k] = T
+        w64[k] = ww
+    np.savez_compressed(os.path.join(HERE, "transforms.npz"), lon=w.lon, lat=w.lat, otype=w.otype,
+                        status=w.status, S=S, s=s, x=w.x, y=w.y, locrad=np.array(w.locrad), pts=pts, T64=T64,
+                        w64=w64, nlobs=nl, mode=np.array(w.mode), scheme=np.array(w.scheme),
+                        stride=np.array(w.stride))
+    print("transforms:", pts.size, "points, mean p", nl.mean())
+
+
+if __name__ == "__main__":
+    oracle.build()
+    if oracle.reflib() is None:
+        sys.exit("the reference library oracle/_ref/libenkf_ref.so could not be built")
+    numerics()
+    kdtree()
+    transforms()

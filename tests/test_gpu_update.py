@@ -1,0 +1,139 @@
+"""Parity of the GPU update stage (das_updatefields / das_updatebg /
+das_sethybridensemble) with the CPU oracle, through the C ABI.
+
+Tolerances: the reference applies X5 with a float sgemv whose summation order
+is the BLAS's; the device sums in its own order, so analysis fields agree to
+float rounding: |a - b| <= 2e-5 * max(1, |b|) (fields here are O(15)).
+Masked cells, missing values and the EnOI/hybrid kernels, which follow the
+reference's operation order exactly, are compared bit for bit.
+"""
+import numpy as np
+import pytest
+
+import oracle
+import synth
+from helpers import gpu_setup, obsset, prepare
+
+pytestmark = pytest.mark.gpu
+
+
+def close(a, b, tol=2e-5):
+    a = np.asarray(a, np.float64)
+    b = np.asarray(b, np.float64)
+    return float((np.abs(a - b) / np.maximum(1.0, np.abs(b))).max())
+
+
+def transforms(ctx, w, mode=0, scheme=1):
+    S, s = prepare(w)
+    obs, tabs = obsset(w)
+    gpu_setup(ctx, w, S, s, tabs)
+    return ctx.calctransforms(mode=mode, scheme=scheme, alpha=1.0, want_diag=False)
+
+
+def run_both(ctx, w, out, fields, levels, **kw):
+    nfield = fields.shape[0]
+    got = ctx.updatefields(fields, w.numlevels, levels, **kw)
+    ref = np.empty_like(fields)
+    okw = dict(kw)
+    okw.pop("precision", None)
+    mode = okw.pop("mode", 0)
+    nmem = okw.pop("nmem", w.nmem)
+    nmd = okw.pop("nmem_dynamic", w.nmem_dynamic)
+    j2 = okw.pop("j2", -1)
+    j1 = okw.get("j1", 0)
+    for f in range(nfield):
+        ref[f] = oracle.updatefields(fields[f], out["T"], out["w"], w.numlevels, mode=mode, nmem=nmem,
+                                     nmem_dynamic=nmd, stride=w.stride, level=int(levels[f]),
+                                     j2=None if j2 < 0 else j2, **okw)
+    return got, ref
+
+
+def test_update_stride1_inflation(ctx):
+    w = synth.make(1)
+    out = transforms(ctx, w)
+    fields = w.fields[0]                       # [1 layer][m][nj][ni]
+    got, ref = run_both(ctx, w, out, fields, np.array([0]), inflation=1.05)
+    assert close(got, ref) < 2e-5
+    assert not np.array_equal(got, fields)
+
+
+def test_update_stride3_mask_layers(ctx):
+    w = synth.make(2, scale=0.1, nobs=5000, nmem=24)
+    w.locrad = 10.0
+    out = transforms(ctx, w, mode=0, scheme=0)
+    fl = w.fields.reshape(-1, *w.fields.shape[2:])          # [nf*nl][m][nj][ni]
+    levels = np.tile(np.arange(w.nlayers), w.nfields)
+    nl = w.numlevels.copy()
+    nl[nl > 0] = np.random.default_rng(0).integers(1, w.nlayers + 1, (nl > 0).sum())
+    w.numlevels = nl
+    got, ref = run_both(ctx, w, out, fl, levels, inflation=1.1, inf_ratio=0.5)
+    assert close(got, ref) < 2e-5
+    masked = nl[None, :, :] <= levels[:, None, None]
+    assert np.all(got.transpose(1, 0, 2, 3)[:, masked] == 0.0)
+
+
+def test_update_missing_values_increment_log_periodic(ctx):
+    w = synth.make(1, scale=0.5)
+    w.stride = 2
+    out = transforms(ctx, w)
+    fields = w.fields[0].copy()
+    fields[0, 3, 5, 7] = np.nan                 # dynamic member missing -> cell zeroed
+    fields[0, 0, 9, 9] = 2.0e6                  # |v| > MAXOBSVAL
+    got, ref = run_both(ctx, w, out, fields, np.array([0]), output_increment=1)
+    assert close(got, ref) < 2e-5
+    assert np.all(got[0, :, 5, 7] == 0) and np.all(got[0, :, 9, 9] == 0)
+    lg = np.log10(np.abs(w.fields[0]) + 1).astype(np.float32)
+    got, ref = run_both(ctx, w, out, lg, np.array([0]), output_increment=1, applylog=1)
+    assert close(got, ref, 1e-4) < 1e-4
+
+
+def test_update_periodic_and_tile(ctx):
+    w = synth.make(1, scale=0.5)
+    w.stride = 3
+    S, s = prepare(w)
+    obs, tabs = obsset(w)
+    nl, lr, lw = tabs
+    ctx.set_obstypes(nl, lr, lw, np.ones(1))
+    ctx.set_obs(w.lon, w.lat, w.otype, w.status, w.estd, w.value)
+    ctx.set_S(S, s)
+    ctx.set_grid(w.x, w.y, stride=3, periodic_i=True)
+    out = ctx.calctransforms(mode=0, scheme=1, want_diag=False)
+    fields = w.fields[0]
+    got = ctx.updatefields(fields, w.numlevels, [0])
+    ref = oracle.updatefields(fields[0], out["T"], out["w"], w.numlevels, mode=0, nmem=w.nmem,
+                              nmem_dynamic=w.nmem, stride=3, periodic_i=1)
+    assert close(got[0], ref) < 2e-5
+    # a field tile (FIELDSPLIT) of rows 6..20
+    sub = fields[:, :, 6:21, :]
+    got = ctx.updatefields(sub, w.numlevels, [0], j1=6, j2=20)
+    ref = oracle.updatefields(sub[0], out["T"], out["w"], w.numlevels, mode=0, nmem=w.nmem, nmem_dynamic=w.nmem,
+                              stride=3, periodic_i=1, j1=6, j2=20)
+    assert close(got[0], ref) < 2e-5
+
+
+def test_update_hybrid(ctx):
+    w = synth.make(1, scale=0.5, nmem=24)
+    w.nmem_dynamic = 16
+    out = transforms(ctx, w, mode=2)
+    v = w.fields[0, 0].reshape(w.nmem, -1)
+    hv = ctx.sethybridensemble(v, 16, 0.5)
+    rv, _ = oracle.sethybridensemble(v, 16, 0.5)
+    assert np.array_equal(hv, rv)
+    fields = hv.reshape(1, w.nmem, w.nj, w.ni)
+    got, ref = run_both(ctx, w, out, fields, np.array([0]), mode=2, nmem=24, nmem_dynamic=16, inflation=1.02,
+                        inf_ratio=0.3)
+    assert close(got, ref) < 2e-5
+
+
+def test_update_enoi_bg_bitexact(ctx):
+    w = synth.make(1, scale=0.5)
+    w.stride = 2
+    out = transforms(ctx, w, mode=1, scheme=0)
+    m = w.nmem
+    fields = np.concatenate([w.fields[0, 0], w.fields[0, 0].mean(0, keepdims=True)], 0)[None]
+    nl = w.numlevels.copy()
+    nl[::5, ::7] = 0
+    w.numlevels = nl
+    got = ctx.updatebg(fields, nl, [0], nmem=m, nmem_dynamic=m)
+    ref = oracle.updatebg(fields[0], out["w"], nl, nmem=m, stride=2)
+    assert np.array_equal(got[0], ref)
