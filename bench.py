@@ -1,0 +1,405 @@
+"""Benchmark of the EnKF-C analysis cycle (calc + update) on GB300.
+
+Workload (default): the 600x900 batched DEnKF workload -- 30% land, 4 layers,
+2 fields, 48 members, 400k observations on swaths and over the ocean, radius
+30 cells, stride 3 (60,000 local analyses per cycle).  Synthetic, seeded
+inputs (enkf-c_gb300/synth.py).
+
+One step = one full cycle on the device with every input resident in HBM:
+spatial index build, innovations (das_calcinnandspread), standardisation,
+local-analysis transforms for all 60,000 points, and the X5 update of all
+8 field-layers.  `value` = local analyses per second of that cycle.
+
+`e2e` = the same cycle through the host-buffer C ABI (HE, fields in pinned
+host memory; T, w and the updated fields copied back), timed on the host.
+
+Multi-GPU: the cycle does not exchange data between GPUs, so --gpus N runs N
+independent replicas (one process per GPU); value = all analyses / max time.
+
+--impl reference times the CPU restatement of the reference (oracle/) on the
+host cores over a bounded sample of the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(ROOT, "enkf-c_gb300")
+for _p in (ROOT, PKG):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+import numpy as np  # noqa: E402
+
+METRIC = "local analyses/s (calc + update cycle)"
+UNIT = "analyses/s"
+
+
+def load_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return json.load(f), "measured"
+    except Exception:
+        return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons during the timed region."""
+
+    def __init__(self, index: int):
+        self.index = index
+        self.samples = []
+        self.proc = None
+
+    def __enter__(self):
+        q = ("clocks.sm,clocks.max.sm,clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={q}",
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) >= 6:
+                self.samples.append(parts)
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(s[0]) for s in self.samples if s[0].replace(".", "").isdigit()]
+        mx = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for s in self.samples for k in range(4) if s[2 + k].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.samples)}
+
+
+def workload(cfg: int, scale: float):
+    import synth
+    return synth.make(cfg, scale=scale)
+
+
+def obs_tables(w):
+    nl = np.ones(w.ntypes, np.int32)
+    lr = np.zeros((w.ntypes, 8))
+    lr[:, 0] = w.locrad
+    lw = np.zeros((w.ntypes, 8))
+    lw[:, 0] = 1.0
+    return nl, lr, lw
+
+
+def update_bytes(w, nfl):
+    m = w.nmem
+    cells = w.nj * w.ni
+    fields = 2 * nfl * m * cells * 4
+    x5 = w.nanalyses * (w.nmem_dynamic * m + m) * 4
+    return fields + x5, fields, x5
+
+
+# ---------------------------------------------------------------------------
+# GPU arm
+# ---------------------------------------------------------------------------
+def run_gpu(args, rank, world, local_rank):
+    import torch
+
+    import build as _b
+    _b.build()
+    import enkfg
+
+    torch.cuda.set_device(local_rank)
+    dev = torch.device("cuda", local_rank)
+    w = workload(args.config, args.scale)
+    nfl = w.nfields * w.nlayers
+    m = w.nmem
+    path = enkfg.PATH_BATCHED if args.path == "batched" else enkfg.PATH_PLAIN
+    prec = enkfg.PREC_MIXED if args.precision == "mixed" else enkfg.PREC_FP64
+
+    ctx = enkfg.Enkfg(local_rank)
+    nl, lr, lw = obs_tables(w)
+    ctx.set_obstypes(nl, lr, lw, np.ones(w.ntypes))
+    ctx.set_obs(w.lon, w.lat, w.otype, w.status, w.estd, w.value)
+    ctx.set_grid(w.x, w.y, stride=w.stride)
+
+    stream = torch.cuda.Stream(device=dev)
+    ctx.set_stream(stream.cuda_stream)
+    HE_d = torch.from_numpy(w.HE).to(dev)
+    fields_h = np.ascontiguousarray(w.fields.reshape(nfl, m, w.nj, w.ni))
+    fields_d = torch.from_numpy(fields_h).to(dev)
+    numlev_d = torch.from_numpy(w.numlevels.astype(np.int32)).to(dev)
+    levels = np.tile(np.arange(w.nlayers, dtype=np.int32), w.nfields)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)   # 256 MB > L2 (129 MB)
+    torch.cuda.synchronize()
+
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+
+    def step(timed_parts=None):
+        with torch.cuda.stream(stream):
+            flush.zero_()
+            if timed_parts is not None:
+                timed_parts[0].record(stream)
+            ctx.rebuild_index()
+            ctx.set_HE_dev(HE_d.data_ptr(), m, w.nmem_dynamic)
+            ctx.calcinnandspread(want=False)
+            ctx.standardise()
+            ctx.calctransforms_dev(mode=w.mode, scheme=w.scheme, alpha=w.alpha, path=path, precision=prec)
+            if timed_parts is not None:
+                timed_parts[1].record(stream)
+            ctx.updatefields_dev(fields_d.data_ptr(), numlev_d.data_ptr(), nfl, levels, mode=w.mode, nmem=m,
+                                 nmem_dynamic=w.nmem_dynamic, inflation=w.inflation, inf_ratio=w.inf_ratio,
+                                 precision=prec)
+            if timed_parts is not None:
+                timed_parts[2].record(stream)
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+    torch.cuda.synchronize()
+    calc_ms, upd_ms = [], []
+    l0 = ctx.launches
+    with ClockSampler(local_rank) as clk:
+        ev[0].record(stream)
+        for k in range(args.steps):
+            parts = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+            step(parts)
+            stream.synchronize()
+            calc_ms.append(parts[0].elapsed_time(parts[1]))
+            upd_ms.append(parts[1].elapsed_time(parts[2]))
+        ev[1].record(stream)
+        torch.cuda.synchronize()
+    launches = ctx.launches - l0
+    total_ms = ev[0].elapsed_time(ev[1])
+    if world > 1:
+        t = torch.tensor([total_ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t.item())
+        dist.barrier()
+    ms_per_step = total_ms / args.steps
+    value = world * w.nanalyses * args.steps / (total_ms / 1e3)
+
+    # dominant-kernel roofline: the transform kernel's FP64 contraction or
+    # the update kernel's HBM traffic, whichever takes longer
+    peaks, peak_src = load_peaks()
+    calc_t = statistics.median(calc_ms) / 1e3
+    upd_t = statistics.median(upd_ms) / 1e3
+    ub, _, _ = update_bytes(w, nfl)
+    counts = ctx.findlocal(lists=False).astype(np.float64)
+    flops = float((2.0 * m * m * counts + 2.0 * m * counts).sum())
+    if upd_t >= calc_t:
+        roof = {"kernel": "k_update_fields", "bound": "hbm", "achieved": ub / upd_t / 1e9,
+                "peak": peaks["hbm_gbs"], "unit": "GB/s", "peak_source": peak_src}
+    else:
+        fp64_peak = 1250.0
+        roof = {"kernel": "k_transforms (calc stage)", "bound": "fp64", "achieved": flops / calc_t / 1e9,
+                "peak": fp64_peak, "unit": "GFLOP/s",
+                "peak_source": "GB300 nominal FP64 (not in MEASURED_PEAKS.json)"}
+    roof["frac"] = roof["achieved"] / roof["peak"]
+    roof["traffic"] = None
+
+    # end to end through the host-buffer C ABI (pinned host memory)
+    e2e = None
+    if rank == 0 or world > 1:
+        HE_pin = torch.from_numpy(w.HE).pin_memory().numpy()
+        f_pin = torch.from_numpy(fields_h).pin_memory().numpy()
+        ctx.set_stream(None)
+        T_h = torch.empty((w.nj_s, w.ni_s, w.nmem_dynamic, m), dtype=torch.float32).pin_memory().numpy()
+
+        def e2e_step():
+            ctx.rebuild_index()
+            ctx.set_HE(HE_pin, w.nmem_dynamic)
+            ctx.calcinnandspread(want=False)
+            ctx.standardise()
+            out = ctx.calctransforms(mode=w.mode, scheme=w.scheme, alpha=w.alpha, path=path, precision=prec,
+                                     want_diag=False)
+            res = ctx.updatefields(f_pin, w.numlevels, levels, mode=w.mode, nmem=m, nmem_dynamic=w.nmem_dynamic,
+                                   inflation=w.inflation, inf_ratio=w.inf_ratio, precision=prec)
+            return out, res
+
+        for _ in range(max(1, min(args.warmup, 2))):
+            e2e_step()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        ne = max(1, min(args.steps, 3))
+        for _ in range(ne):
+            out, res = e2e_step()
+        torch.cuda.synchronize()
+        te = (time.perf_counter() - t0) / ne
+        h2d = w.HE.nbytes + fields_h.nbytes + w.numlevels.size * 4
+        d2h = out["w"].nbytes + (out["T"].nbytes if out["T"] is not None else 0) + res.nbytes
+        e2e = {"value": w.nanalyses / te, "unit": UNIT, "ms_per_step": te * 1e3, "h2d_bytes_per_step": int(h2d),
+               "d2h_bytes_per_step": int(d2h)}
+        del T_h
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        cpu = cpu_baseline(w, args.cpu_rows)
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64" if prec == enkfg.PREC_FP64 else "f32/tf32-split",
+            "data": "synthetic (seeded, enkf-c_gb300/synth.py)",
+            "config": {"workload": f"workload {w.cfg}: {w.ni}x{w.nj} grid, {w.nlayers} layers x {w.nfields} fields, "
+                                   f"m={m}, {w.nobs} obs, {'DEnKF' if w.scheme == 0 else 'ETKF'}, radius "
+                                   f"{w.locrad:g}, stride {w.stride}",
+                       "local_analyses": w.nanalyses, "path": args.path, "precision": args.precision,
+                       "parallelism": f"replicas x{world}", "l2": "256 MB flush before every step; "
+                                                             "fields (830 MB) exceed L2"},
+            "stages_ms": {"calc": statistics.median(calc_ms), "update": statistics.median(upd_ms)},
+            "update_gbs": ub / upd_t / 1e9,
+            "calc_gflops_fp64": flops / calc_t / 1e9,
+            "roofline": roof, "e2e": e2e, "cpu_baseline": cpu, "gpu_launches": int(launches),
+            "clocks": clk.summary(),
+        }
+        print(json.dumps(line))
+    ctx.close()
+
+
+# ---------------------------------------------------------------------------
+# CPU (oracle) side
+# ---------------------------------------------------------------------------
+def cpu_sample(w, rows, threads):
+    """The calc + update cycle of the CPU restatement: per-cycle set-up (kd-trees,
+    innovations, standardisation) on the whole domain, the transforms of `rows`
+    strided rows spread over the domain, and the update of the model rows they
+    cover.  Returns (analyses in the sample, set-up s, calc s, update s,
+    sampled rows)."""
+    import concurrent.futures as cf
+
+    import oracle
+    t0 = time.perf_counter()
+    nl, lr, lw = oracle.locrad_table(w.ntypes, w.locrad)
+    obs = oracle.ObsSet(w.lon, w.lat, w.otype, w.status, w.ntypes, nl, lr, lw)
+    S, s = oracle.prepare(w.HE, w.value, w.status, w.estd, w.otype, np.ones(w.ntypes))
+    t_setup = time.perf_counter() - t0
+    sel = [int(r) for r in np.unique(np.linspace(0, w.nj_s - 1, rows).astype(int))]
+    t0 = time.perf_counter()
+    out = oracle.calctransforms(obs, mode=w.mode, scheme=w.scheme, nmem=w.nmem, nmem_dynamic=w.nmem_dynamic,
+                                alpha=w.alpha, stride=w.stride, x=w.x, y=w.y, S=S, s=s, rows=sel, threads=threads,
+                                want_diag=False)
+    t_calc = time.perf_counter() - t0
+    nfl = w.nfields * w.nlayers
+    fl = w.fields.reshape(nfl, w.nmem, w.nj, w.ni)
+    T = out["T"] if out["T"] is not None else np.zeros((w.nj_s, w.ni_s, 1, w.nmem), np.float32)
+
+    def upd(args_):
+        jj, f = args_
+        j1 = jj * w.stride
+        j2 = min(w.nj - 1, j1 + w.stride - 1)
+        return oracle.updatefields(fl[f][:, j1:j2 + 1], T, out["w"], w.numlevels, mode=w.mode, nmem=w.nmem,
+                                   nmem_dynamic=w.nmem_dynamic, stride=w.stride, level=f % w.nlayers,
+                                   inflation=w.inflation, inf_ratio=w.inf_ratio, j1=j1, j2=j2)
+
+    t0 = time.perf_counter()
+    with cf.ThreadPoolExecutor(max_workers=threads) as ex:
+        list(ex.map(upd, [(jj, f) for jj in sel for f in range(nfl)]))
+    t_upd = time.perf_counter() - t0
+    return len(sel) * w.ni_s, t_setup, t_calc, t_upd, len(sel)
+
+
+def cpu_rate(w, n, ts, tc, tu, nrows):
+    """Analyses/s of a full cycle extrapolated from the row sample."""
+    full = ts + (tc + tu) * (w.nj_s / nrows)
+    return w.nanalyses / full, full
+
+
+def cpu_baseline(w, rows):
+    threads = os.cpu_count() or 1
+    n, ts, tc, tu, nrows = cpu_sample(w, rows, threads)
+    v, full = cpu_rate(w, n, ts, tc, tu, nrows)
+    return {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"{nrows} of {w.nj_s} strided rows ({n} local analyses) and their model rows x "
+                      f"{w.nfields * w.nlayers} field-layers, extrapolated to the full cycle ({full:.1f} s): "
+                      f"set-up {ts:.2f} s, calc {tc:.2f} s, update {tu:.2f} s; C restatement of the reference "
+                      f"(oracle/) + OpenBLAS, {threads} threads"}
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return
+    import oracle
+    oracle.build()
+    w = workload(args.config, args.scale)
+    threads = os.cpu_count() or 1
+    kind = "port"
+    for _ in range(args.warmup):
+        cpu_sample(w, max(1, args.cpu_rows // 4), threads)
+    times = []
+    for _ in range(args.steps):
+        n, ts, tc, tu, nrows = cpu_sample(w, args.cpu_rows, threads)
+        times.append(cpu_rate(w, n, ts, tc, tu, nrows)[1])
+    value = w.nanalyses * len(times) / sum(times)
+    ts = sum(times)
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ts / args.steps * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
+            "impl": "reference",
+            "config": {"workload": f"workload {w.cfg}: {w.ni}x{w.nj}, m={w.nmem}, {w.nobs} obs", "path": "cpu",
+                       "parallelism": f"{threads} host threads"},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": kind,
+                             "sample": f"{args.cpu_rows} strided rows per step of {w.nj_s}, extrapolated to the full "
+                                       f"cycle; CPU restatement of the "
+                                       f"reference (oracle/, C + OpenBLAS); the reference's own build needs MPI and "
+                                       f"NetCDF, absent here"},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--config", type=int, default=2)
+    ap.add_argument("--scale", type=float, default=1.0)
+    ap.add_argument("--path", default="batched", choices=["plain", "batched"])
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
+    ap.add_argument("--cpu-rows", type=int, default=24)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+        return
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        torch.cuda.set_device(local_rank)
+        dist.init_process_group("nccl")
+    run_gpu(args, rank, world, local_rank)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -110,8 +110,25 @@ ENKFG_API void enkfg_destroy(enkfg_ctx* ctx)
         if (ptrs[k]) cudaFree(ptrs[k]);
     for (int k = 0; k < 8; ++k)
         if (ctx->ev[k]) cudaEventDestroy(ctx->ev[k]);
+    if (ctx->own_stream) ctx->stream = ctx->own_stream;
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
     free(ctx);
+}
+
+ENKFG_API enkfg_status enkfg_set_stream(enkfg_ctx* ctx, void* stream)
+{
+    if (!ctx) return ENKFG_EINVAL;
+    if (ctx->own_stream == nullptr) ctx->own_stream = ctx->stream;
+    ctx->stream = stream ? (cudaStream_t)stream : ctx->own_stream;
+    return ENKFG_OK;
+}
+
+ENKFG_API enkfg_status enkfg_rebuild_index(enkfg_ctx* ctx)
+{
+    if (!ctx) return ENKFG_EINVAL;
+    ctx->index_valid = false;
+    ctx->gather_valid = false;
+    return ENKFG_OK;
 }
 
 ENKFG_API long long enkfg_kernel_launches(const enkfg_ctx* ctx)
@@ -233,6 +250,26 @@ ENKFG_API enkfg_status enkfg_set_HE(enkfg_ctx* ctx, int nmem, int nmem_dynamic, 
                            ctx->stream));
     CK(cudaStreamSynchronize(ctx->stream));
     ctx->s_mode = 1;
+    return ENKFG_OK;
+}
+
+ENKFG_API enkfg_status enkfg_set_HE_dev(enkfg_ctx* ctx, int nmem, int nmem_dynamic, const float* HE_dev)
+{
+    if (!ctx) return ENKFG_EINVAL;
+    NEED(ctx->obs_set, ENKFG_ESTATE, "enkfg_set_obs must come first");
+    NEED(nmem >= 2 && nmem <= 144 && nmem_dynamic >= 1 && nmem_dynamic <= nmem && HE_dev, ENKFG_EINVAL,
+         "bad ensemble size %d/%d", nmem, nmem_dynamic);
+    SETDEV();
+    if (ctx->d_S == nullptr || ctx->nmem != nmem) {
+        enkfg_status s = alloc_S(ctx, nmem, nmem_dynamic);
+        if (s) return s;
+    }
+    ctx->nmem_dyn = nmem_dynamic;
+    if (ctx->nobs > 0)
+        CK(cudaMemcpyAsync(ctx->d_S, HE_dev, (size_t)nmem * ctx->nobs * sizeof(float), cudaMemcpyDeviceToDevice,
+                           ctx->stream));
+    ctx->s_mode = 1;
+    ctx->gather_valid = false;
     return ENKFG_OK;
 }
 

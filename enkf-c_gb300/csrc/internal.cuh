@@ -33,7 +33,8 @@ struct TypeIndex {
 
 struct enkfg_ctx {
     int device;
-    cudaStream_t stream;
+    cudaStream_t stream;        // stream all work goes to
+    cudaStream_t own_stream;    // the context's own stream while a caller stream is bound
     char err[1024];
     long long launches;
     float stage_ms[4];

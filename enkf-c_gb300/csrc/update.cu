@@ -215,7 +215,15 @@ __global__ void __launch_bounds__(UPD_NT) k_update_fields(UpdArgs a)
                     float out;
                     if (!a.output_increment) out = va;
                     else if (!a.applylog) out = __fsub_rn(va, vf);
-                    else out = (!isnormal(vf)) ? 0.0f : (float)(exp10((double)va) - exp10((double)vf));
+                    else {
+                        // --output-increment of a log10 variable: difference
+                        // in physical space, 0 where the forecast is not a
+                        // normal number (update.c:484-497)
+                        float avf = fabsf(vf);
+                        bool normal = (avf >= 1.17549435e-38f) && (avf <= 3.40282347e+38f);
+                        double ea = pow(10.0, (double)va), ef = pow(10.0, (double)vf);
+                        out = normal ? (float)(ea - ef) : 0.0f;
+                    }
                     v[e1 * nk + c] = out;
                 }
             }

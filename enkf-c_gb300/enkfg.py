@@ -43,7 +43,8 @@ EXPORTS = ["enkfg_create", "enkfg_destroy", "enkfg_last_error", "enkfg_status_st
            "enkfg_set_S", "enkfg_get_S", "enkfg_set_grid", "enkfg_transform_dims", "enkfg_local_obs",
            "enkfg_calc_transforms", "enkfg_calc_transforms_dev", "enkfg_transforms_dev_ptr",
            "enkfg_set_transforms", "enkfg_update_fields", "enkfg_update_fields_dev", "enkfg_set_hybrid_ensemble",
-           "enkfg_set_hybrid_ensemble_dev", "enkfg_kernel_launches", "enkfg_stage_times"]
+           "enkfg_set_hybrid_ensemble_dev", "enkfg_kernel_launches", "enkfg_stage_times", "enkfg_set_stream",
+           "enkfg_set_HE_dev", "enkfg_rebuild_index"]
 
 
 class EnkfgError(RuntimeError):
@@ -171,7 +172,23 @@ class Enkfg:
         self.nmem, self.nmem_dynamic = m, md
         self._ck(self.L.enkfg_set_HE(self.h, C.c_int(m), C.c_int(md), _p(HE, C.c_float)))
 
-    def calcinnandspread(self):
+    def set_stream(self, stream):
+        """Bind a cudaStream_t (int address, e.g. torch.cuda.Stream().cuda_stream)."""
+        self._ck(self.L.enkfg_set_stream(self.h, C.c_void_p(stream)))
+
+    def set_HE_dev(self, HE_ptr, nmem, nmem_dynamic=None):
+        md = nmem if nmem_dynamic is None else int(nmem_dynamic)
+        self.nmem, self.nmem_dynamic = nmem, md
+        self._ck(self.L.enkfg_set_HE_dev(self.h, C.c_int(nmem), C.c_int(md), C.c_void_p(HE_ptr)))
+
+    def rebuild_index(self):
+        self._ck(self.L.enkfg_rebuild_index(self.h))
+
+    def calcinnandspread(self, want=True):
+        if not want:
+            self._ck(self.L.enkfg_calc_innovations(self.h, None, None))
+            return None
+
         s_f = np.zeros(self.nobs)
         std_f = np.zeros(self.nobs)
         self._ck(self.L.enkfg_calc_innovations(self.h, _p(s_f, C.c_double), _p(std_f, C.c_double)))

@@ -185,6 +185,18 @@ ENKFG_API enkfg_status enkfg_update_fields_dev(enkfg_ctx* ctx, const enkfg_updat
 ENKFG_API enkfg_status enkfg_set_hybrid_ensemble(enkfg_ctx* ctx, int nmem, int nmem_dynamic, double gamma, int nij, float* v);
 ENKFG_API enkfg_status enkfg_set_hybrid_ensemble_dev(enkfg_ctx* ctx, int nmem, int nmem_dynamic, double gamma, int nij, float* v_dev, void* stream);
 
+/* Run all later work of this context on `stream` (a cudaStream_t; NULL
+ * restores the context's own stream). */
+ENKFG_API enkfg_status enkfg_set_stream(enkfg_ctx* ctx, void* stream);
+
+/* Device-resident HE [nmem][nobs] (a device address): copied on the device
+ * into the context, as enkfg_set_HE does from the host. */
+ENKFG_API enkfg_status enkfg_set_HE_dev(enkfg_ctx* ctx, int nmem, int nmem_dynamic, const float* HE_dev);
+
+/* Drop the spatial index so that the next transforms call rebuilds it
+ * (obs_createkdtrees is part of every enkf_calc run, observations.c:1616). */
+ENKFG_API enkfg_status enkfg_rebuild_index(enkfg_ctx* ctx);
+
 /* Number of kernels this context has launched (for launch accounting). */
 ENKFG_API long long enkfg_kernel_launches(const enkfg_ctx* ctx);
 /* Last stage timings in milliseconds, measured with CUDA events on the

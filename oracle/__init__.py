@@ -253,9 +253,10 @@ def standardise(S, s_f, estd, otype, rfactor):
 
 def calctransforms(obs: ObsSet, *, mode, scheme, nmem, nmem_dynamic, alpha, stride, x, y, S, s,
                    rows=None, threads: int = 1, want64=False, want_diag=True, x2d=None, y2d=None):
-    """das_calctransforms over strided rows `rows` (default all), run on
-    `threads` host threads (contiguous row blocks, as distribute_iterations
-    assigns them).  Returns a dict of full-size outputs."""
+    """das_calctransforms over strided rows `rows` (default all; a (first,
+    last+1) tuple or a list of rows), run on `threads` host threads
+    (contiguous row blocks, as distribute_iterations assigns them).  Returns a
+    dict of full-size outputs (rows not computed stay zero)."""
     x = np.ascontiguousarray(x, np.float64)
     y = np.ascontiguousarray(y, np.float64)
     mni = x.size if x2d is None else x2d.shape[1]
@@ -281,7 +282,12 @@ def calctransforms(obs: ObsSet, *, mode, scheme, nmem, nmem_dynamic, alpha, stri
     y2 = None if y2d is None else np.ascontiguousarray(y2d, np.float64)
     P = CalcParams(mode, scheme, m, md, float(alpha), stride, mni, mnj, _p(x, C.c_double), _p(y, C.c_double),
                    _p(x2, C.c_double), _p(y2, C.c_double))
-    r0, r1 = (0, nj) if rows is None else rows
+    if rows is None:
+        rowlist = list(range(nj))
+    elif isinstance(rows, tuple) and len(rows) == 2:
+        rowlist = list(range(int(rows[0]), int(rows[1])))
+    else:
+        rowlist = [int(r) for r in rows]
     L = lib()
     rcs = []
 
@@ -293,12 +299,23 @@ def calctransforms(obs: ObsSet, *, mode, scheme, nmem, nmem_dynamic, alpha, stri
                                  _p(ps, C.c_float))
         rcs.append(rc)
 
-    threads = max(1, min(threads, r1 - r0))
+    def run_list(lst):
+        # contiguous runs of rows in one call each
+        k = 0
+        while k < len(lst):
+            e = k
+            while e + 1 < len(lst) and lst[e + 1] == lst[e] + 1:
+                e += 1
+            run(lst[k], lst[e] + 1)
+            k = e + 1
+
+    threads = max(1, min(threads, len(rowlist)))
     if threads == 1:
-        run(r0, r1)
+        run_list(rowlist)
     else:
-        bounds = np.linspace(r0, r1, threads + 1).astype(int)
-        ts = [threading.Thread(target=run, args=(int(bounds[k]), int(bounds[k + 1]))) for k in range(threads)]
+        # contiguous blocks of rows per thread, as distribute_iterations assigns them
+        bounds = np.linspace(0, len(rowlist), threads + 1).astype(int)
+        ts = [threading.Thread(target=run_list, args=(rowlist[bounds[k]:bounds[k + 1]],)) for k in range(threads)]
         for t in ts:
             t.start()
         for t in ts:
@@ -341,6 +358,12 @@ def updatebg(v, w, numlevels, *, nmem, stride, periodic_i=0, level=0, surfk=0, i
     wc = np.ascontiguousarray(w, np.float32)
     lib().or_updatebg(C.byref(P), _p(wc, C.c_float), _p(nl, C.c_int), _p(v, C.c_float))
     return v
+
+
+def prepare(HE, value, status, estd, otype, rfactor):
+    """das_calcinnandspread then das_standardise: standardised (S, s)."""
+    S, s_f, _ = calcinnandspread(HE, value, status)
+    return standardise(S, s_f, estd, otype, rfactor)
 
 
 def sethybridensemble(v, nmem_d, gamma):
