@@ -44,7 +44,7 @@ EXPORTS = ["enkfg_create", "enkfg_destroy", "enkfg_last_error", "enkfg_status_st
            "enkfg_calc_transforms", "enkfg_calc_transforms_dev", "enkfg_transforms_dev_ptr",
            "enkfg_set_transforms", "enkfg_update_fields", "enkfg_update_fields_dev", "enkfg_set_hybrid_ensemble",
            "enkfg_set_hybrid_ensemble_dev", "enkfg_kernel_launches", "enkfg_stage_times", "enkfg_set_stream",
-           "enkfg_set_HE_dev", "enkfg_rebuild_index"]
+           "enkfg_set_HE_dev", "enkfg_rebuild_index", "enkfg_local_offsets_noalloc"]
 
 
 class EnkfgError(RuntimeError):

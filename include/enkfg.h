@@ -204,6 +204,24 @@ ENKFG_API long long enkfg_kernel_launches(const enkfg_ctx* ctx);
  * [3] update. */
 ENKFG_API enkfg_status enkfg_stage_times(const enkfg_ctx* ctx, float* ms4);
 
+/* No counterpart in the reference.  CSR offsets of local-observation
+ * counts (offsets[k] = counts[0] + ... + counts[k-1], offsets[n] = total; the
+ * same offsets enkfg_local_obs returns) for callers that cannot allocate
+ * device memory: code whose device memory is owned by a pool or another
+ * framework, hosts that forbid allocation after start-up, or callers that
+ * must avoid the implicit synchronisation of cudaMalloc/cudaFree.  It needs
+ * no context and allocates nothing: counts_dev [n] and offsets_dev [n+1] are
+ * the caller's device buffers, and the scan's block sums live in a fixed
+ * 512 KiB array inside the library that every GPU using the library keeps
+ * until the process exits.  Limit: n <= 134,217,728 (32768 scan blocks of
+ * 4096 counts), else ENKFG_ECAPACITY.  The first call on a device looks up
+ * the array's device address (cudaGetSymbolAddress) with that device
+ * current, so make it before any stream capture.  All calls share the
+ * array: calls that overlap on the GPU race and must be serialised by the
+ * caller.  counts_dev may be NULL when n = 0.  Work is queued on `stream`
+ * (NULL: the legacy default stream). */
+ENKFG_API enkfg_status enkfg_local_offsets_noalloc(const int* counts_dev, long long n, long long* offsets_dev, void* stream);
+
 #ifdef __cplusplus
 }
 #endif
