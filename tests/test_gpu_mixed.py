@@ -1,0 +1,111 @@
+"""The mixed-precision path (S'S and S's as split-TF32 products on the tensor
+cores, FP64 solve) against the FP64 oracle.
+
+Contract: local-observation sets stay bit-exact; X5 (T), w, the analysis
+mean and the analysis spread are within 1e-5 relative of the FP64 oracle
+(max over points of max|a - b| / max|b|; mean and spread relative to the
+field's scale).  The measured errors are written to
+gpurun_out/mixed_errors.json when the directory exists.
+"""
+import json
+import os
+
+import numpy as np
+import pytest
+
+import oracle
+import synth
+from helpers import gpu_setup, obsset, prepare
+
+pytestmark = pytest.mark.gpu
+
+ERRS = {}
+
+
+def per_point(a, b):
+    a = a.reshape(a.shape[0] * a.shape[1], -1).astype(np.float64)
+    b = b.reshape(b.shape[0] * b.shape[1], -1).astype(np.float64)
+    den = np.maximum(np.abs(b).max(axis=1), 1e-300)
+    r = np.abs(a - b).max(axis=1) / den
+    return float(r.max()), float(np.sqrt(np.mean(r ** 2)))
+
+
+def analysis_stats(fields):
+    """ensemble mean and spread of [m][nj][ni]"""
+    f = fields.astype(np.float64)
+    return f.mean(axis=0), f.std(axis=0, ddof=1)
+
+
+def run_case(ctx, name, w, mode, scheme, S, s, tabs, path=1, update=True):
+    obs, _ = obsset(w)
+    ref = oracle.calctransforms(obs, mode=mode, scheme=scheme, nmem=w.nmem, nmem_dynamic=w.nmem_dynamic, alpha=1.0,
+                                stride=w.stride, x=w.x, y=w.y, S=S, s=s, want64=True, threads=8)
+    gpu_setup(ctx, w, S, s, tabs)
+    out = ctx.calctransforms(mode=mode, scheme=scheme, path=path, precision=1, want64=True)
+    assert np.array_equal(out["nlobs"], ref["nlobs"])
+    e = {}
+    if mode != 1:
+        e["X5_max"], e["X5_rms"] = per_point(out["T64"], ref["T64"])
+    e["w_max"], e["w_rms"] = per_point(out["w64"], ref["w64"])
+    if update and w.fields is not None and mode != 1:
+        fl = w.fields[0, 0]
+        got = ctx.updatefields(fl[None], w.numlevels, [0])[0]
+        exp = oracle.updatefields(fl, ref["T"], ref["w"], w.numlevels, mode=mode, nmem=w.nmem,
+                                  nmem_dynamic=w.nmem_dynamic, stride=w.stride)
+        gm, gs = analysis_stats(got)
+        rm, rs = analysis_stats(exp)
+        scale = np.abs(rm).max()
+        e["mean_max"] = float(np.abs(gm - rm).max() / scale)
+        e["mean_rms"] = float(np.sqrt(np.mean((gm - rm) ** 2)) / scale)
+        e["spread_max"] = float(np.abs(gs - rs).max() / max(np.abs(rs).max(), 1e-30))
+        e["spread_rms"] = float(np.sqrt(np.mean((gs - rs) ** 2)) / max(np.abs(rs).max(), 1e-30))
+    ERRS[name] = e
+    if os.path.isdir("gpurun_out"):
+        with open(os.path.join("gpurun_out", "mixed_errors.json"), "w") as f:
+            json.dump(ERRS, f, indent=1)
+    return e
+
+
+def test_mixed_etkf_workload1(ctx):
+    w = synth.make(1)
+    S, s = prepare(w)
+    _, tabs = obsset(w)
+    e = run_case(ctx, "workload1_etkf_m24", w, 0, 1, S, s, tabs)
+    assert e["X5_max"] < 1e-5 and e["w_max"] < 1e-5, e
+    assert e["mean_max"] < 1e-5 and e["spread_max"] < 1e-5, e
+
+
+def test_mixed_denkf_multitype(ctx):
+    w = synth.make(2, scale=0.1, nobs=6000, nmem=48)
+    w.locrad = 12.0
+    S, s = prepare(w)
+    _, tabs = obsset(w)
+    e = run_case(ctx, "workload2_denkf_m48_scaled", w, 0, 0, S, s, tabs)
+    assert e["X5_max"] < 1e-5 and e["w_max"] < 1e-5, e
+
+
+def test_mixed_enoi(ctx):
+    w = synth.make(1, scale=0.5, with_fields=False)
+    S, s = prepare(w)
+    _, tabs = obsset(w)
+    e = run_case(ctx, "workload1_enoi", w, 1, 0, S, s, tabs, update=False)
+    assert e["w_max"] < 1e-5, e
+
+
+def test_mixed_etkf_m96_dense(ctx):
+    """Workload-3 shape (m = 96, dense uniform obs, ETKF, stride 2) at reduced size."""
+    w = synth.make(3, scale=0.12, nobs=30000, nmem=96)
+    S, s = prepare(w)
+    _, tabs = obsset(w)
+    e = run_case(ctx, "workload3_etkf_m96_scaled", w, 0, 1, S, s, tabs)
+    assert e["X5_max"] < 1e-5 and e["w_max"] < 1e-5, e
+    assert e["mean_max"] < 1e-5 and e["spread_max"] < 1e-5, e
+
+
+def test_mixed_plain_grid_path(ctx):
+    """One CTA per point (non-persistent) launch of the mixed kernel."""
+    w = synth.make(1, scale=0.5, with_fields=False)
+    S, s = prepare(w)
+    _, tabs = obsset(w)
+    e = run_case(ctx, "workload1_etkf_plain_launch", w, 0, 1, S, s, tabs, path=0, update=False)
+    assert e["X5_max"] < 1e-5, e
