@@ -2,23 +2,26 @@
 // the 5th-generation tensor cores (tcgen05, TF32 inputs, FP32 accumulation in
 // tensor memory), everything else in FP64 as in calc.cu.
 //
-// Per chunk of kc local observations (kc a multiple of 8):
-//   * the tapered rows of [S | s] (m members plus the innovation as row m,
-//     rows m+1..127 zero) are written to shared memory as a K-major operand
-//     tile (rows = members, K = observations), split into a TF32 "hi" part
-//     (round-to-nearest) and the FP32 remainder "lo" = v - hi;
-//   * one thread issues, per K-step of 8 observations, three MMAs
-//     D = hi*hi' + hi*lo' + lo*hi' of shape M=128 x N x 8 into a TMEM
-//     accumulator (N = m+1 rounded up to 16).  A and B are the same tile,
-//     so D = [S|s]'[S|s] carries S'S, S's and s's in one product;
+// Per round of kc = 8*NA local observations:
+//   * the tapered rows of S (m members, rows m..127 zero) are written to
+//     shared memory as a K-major operand tile (rows = members, K =
+//     observations), split into TF32 hi = rn(v) and lo = rn(v - hi);
+//   * one thread issues, for each group q of 8 observations, three MMAs
+//     D_q = hi*hi' + hi*lo' + lo*hi' of shape M=128 x N x 8 into its own TMEM
+//     accumulator q (N = m rounded up to 16).  A and B are the same tile, so
+//     D_q is that group's contribution to S'S;
 //   * the MMAs' completion is signalled by tcgen05.commit on an mbarrier;
-//     the CTA then reads D out of TMEM (tcgen05.ld) and adds it to an FP64
-//     accumulator in shared memory.  Only kc observations are ever summed in
-//     FP32, so rounding stays at the level of the split (about 2^-21
-//     relative per product) instead of growing with the local obs count.
+//     the CTA then reads the NA accumulators out of TMEM (tcgen05.ld) and adds
+//     them, with error-free TwoSum steps, to a double-float (hi + lo FP32)
+//     accumulator in shared memory.  Only 8 observations are ever summed in
+//     FP32 inside the tensor core, so rounding stays near the split's own
+//     (about 2^-22 relative per product) whatever the local obs count;
+//   * S's is accumulated on the CUDA cores, one member per thread, with
+//     TwoProduct/TwoSum compensated FP32 (double-float) arithmetic.
 //
-// The FP64 accumulator then goes through the same FP64 solve as the plain
-// path (Householder + QL for ETKF, Cholesky for DEnKF/EnOI).
+// The accumulators are then converted to FP64 and go through the same FP64
+// solve as the plain path (Householder + QL for ETKF, Cholesky for
+// DEnKF/EnOI).
 //
 // Shared-memory operand layout (canonical K-major, no swizzle): core matrices
 // of 8 rows x 16 bytes (4 TF32) stored as 128 contiguous bytes; core matrix
@@ -145,15 +148,18 @@ __device__ __forceinline__ float to_tf32(float x)
 
 }  // namespace tc
 
+#define MX_NA 4            // TMEM accumulators (groups of 8 obs) per round
+
 struct MixedShared {
     float* tileH;      // [MX_ROWS x kc] core-matrix layout
     float* tileL;
-    double* Macc;      // [(m+1) x lda] FP64 accumulator of [S|s]'[S|s]
+    float2* Macc;      // [m x lda] double-float accumulator of S'S (later reused as FP64)
     int lda;
+    float* sl;         // [kc] tapered innovations of the round
     uint64_t* mbar;
     uint32_t taddr;
-    int N;             // MMA N
-    int kc;            // observations per chunk (multiple of 8)
+    int N;             // MMA N (m rounded up to 16)
+    int kc;            // observations per round (8 * MX_NA)
     int* err;          // shared error flag
 };
 
@@ -163,55 +169,75 @@ __device__ __forceinline__ int core_offset(int r, int k, int kc)
     return (((r >> 3) * (kc >> 2) + (k >> 2)) << 5) + ((r & 7) << 2) + (k & 3);
 }
 
+// error-free (TwoSum) accumulation of x into the double-float (a.x + a.y)
+__device__ __forceinline__ void df_add(float2& a, float x)
+{
+    float s = a.x + x;
+    float bp = s - a.x;
+    float e = (a.x - (s - bp)) + (x - bp);
+    a.x = s;
+    a.y += e;
+}
+
 struct GramProcTC {
     const CalcArgs& a;
     const PointScratch& s;
     MixedShared& ms;
     uint32_t& phase;
+    float bhi, blo;    // S's for member threadIdx.x (double-float)
     __device__ __forceinline__ GramProcTC(const CalcArgs& a_, const PointScratch& s_, MixedShared& ms_, uint32_t& ph)
-        : a(a_), s(s_), ms(ms_), phase(ph) {}
+        : a(a_), s(s_), ms(ms_), phase(ph), bhi(0.0f), blo(0.0f) {}
 
     __device__ void chunk(int nc, int t)
     {
         const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
-        const int m = a.m, mr = m + 1, kc = ms.kc;
+        const int m = a.m, kc = ms.kc;
         const bool tsum = a.want_diag && a.ntypes > 1;
         double ssq = 0.0;
         if (*ms.err) return;
-        // 1. tapered [S | s] rows of the chunk, split into TF32 hi + lo
-        for (int i = tid; i < kc * mr; i += CALC_NT) {
-            int k = i / mr, r = i - k * mr;
+        // 1. tapered S rows of the round, split into TF32 hi + lo; the
+        //    tapered innovations for S's
+        if (tid < kc) ms.sl[tid] = (tid < nc) ? (float)(a.ss[s.lid[tid]] * s.llc[tid]) : 0.0f;
+        for (int i = tid; i < kc * m; i += CALC_NT) {
+            int k = i / m, r = i - k * m;
             float v = 0.0f;
             if (k < nc) {
-                int pos = s.lid[k];
-                if (r < m) {
-                    v = __fmul_rn(a.St[(size_t)pos * a.mpad + r], (float)s.llc[k]);
-                    if (tsum) ssq += (double)v * (double)v;
-                } else {
-                    v = (float)(a.ss[pos] * s.llc[k]);
-                }
+                v = __fmul_rn(a.St[(size_t)s.lid[k] * a.mpad + r], (float)s.llc[k]);
+                if (tsum) ssq += (double)v * (double)v;
             }
             float hi = tc::to_tf32(v);
             int off = core_offset(r, k, kc);
             ms.tileH[off] = hi;
-            ms.tileL[off] = v - hi;
+            ms.tileL[off] = tc::to_tf32(v - hi);
         }
         tc::fence_async_smem();
         __syncthreads();
-        // 2. one thread issues the MMAs: D = H H' + H L' + L H'
+        // 2. one thread issues the MMAs: group q -> accumulator q
         if (tid == 0) {
             tc::fence_after();
             const uint32_t h0 = tc::smem_u32(ms.tileH), l0 = tc::smem_u32(ms.tileL);
             const uint32_t sbo = (uint32_t)kc * 32u, idesc = tc::idesc_tf32(MX_ROWS, ms.N);
-            for (int ks = 0; ks < kc / 8; ++ks) {
-                const uint32_t off = (uint32_t)ks * 256u;   // two 128-byte core matrices per K-step
+            for (int q = 0; q < kc / 8; ++q) {
+                const uint32_t off = (uint32_t)q * 256u;    // two 128-byte core matrices per group of 8
+                const uint32_t dq = ms.taddr + (uint32_t)(q * ms.N);
                 uint64_t dh = tc::desc_kmajor_noswizzle(h0 + off, 128u, sbo);
                 uint64_t dl = tc::desc_kmajor_noswizzle(l0 + off, 128u, sbo);
-                tc::mma_tf32(ms.taddr, dh, dh, idesc, ks > 0 ? 1u : 0u);
-                tc::mma_tf32(ms.taddr, dh, dl, idesc, 1u);
-                tc::mma_tf32(ms.taddr, dl, dh, idesc, 1u);
+                tc::mma_tf32(dq, dh, dh, idesc, 0u);
+                tc::mma_tf32(dq, dh, dl, idesc, 1u);
+                tc::mma_tf32(dq, dl, dh, idesc, 1u);
             }
             tc::commit(ms.mbar);
+        }
+        // S's on the CUDA cores while the tensor cores run (compensated FP32)
+        if (tid < m) {
+            for (int k = 0; k < nc; ++k) {
+                float v = __fmul_rn(a.St[(size_t)s.lid[k] * a.mpad + tid], (float)s.llc[k]);
+                float x = ms.sl[k];
+                float p = v * x, pe = fmaf(v, x, -p);
+                float sm = bhi + p, bp = sm - bhi;
+                blo += ((bhi - (sm - bp)) + (p - bp)) + pe;
+                bhi = sm;
+            }
         }
         // 3. bounded wait for the MMAs; on expiry record the error and wait
         // once more (bounded) so that nothing is in flight when TMEM is freed
@@ -224,22 +250,29 @@ struct GramProcTC {
         tc::fence_after();
         __syncthreads();
         if (*ms.err) return;
-        // 4. D (FP32, TMEM) -> FP64 accumulator.  Warps w and w+4 share the
-        // TMEM lanes 32*(w%4).., each reading half of the N columns.
+        // 4. accumulators (FP32, TMEM) -> double-float.  Warps w and w+4 share
+        // the TMEM lanes 32*(w%4).., each reading half of the N columns.
         {
             const int r = 32 * (wid & 3) + lane;
             const int half = ms.N >> 1;
             const int c0 = (wid >> 2) * half;
             const uint32_t lane_addr = ms.taddr + ((uint32_t)(32 * (wid & 3)) << 16);
+            const int ngroups = (nc + 7) / 8;
             for (int cg = c0; cg < c0 + half; cg += 8) {
-                float vv[8];
-                tc::tmem_ld8(lane_addr + (uint32_t)cg, vv);
-                if (r < mr) {
+                float2 acc[8];
 #pragma unroll
-                    for (int j = 0; j < 8; ++j) {
-                        int c = cg + j;
-                        if (c < mr) ms.Macc[r * ms.lda + c] += (double)vv[j];
-                    }
+                for (int j = 0; j < 8; ++j)
+                    acc[j] = (r < m && cg + j < m) ? ms.Macc[r * ms.lda + cg + j] : make_float2(0.f, 0.f);
+                for (int q = 0; q < ngroups; ++q) {
+                    float vv[8];
+                    tc::tmem_ld8(lane_addr + (uint32_t)(q * ms.N + cg), vv);
+#pragma unroll
+                    for (int j = 0; j < 8; ++j) df_add(acc[j], vv[j]);
+                }
+                if (r < m) {
+#pragma unroll
+                    for (int j = 0; j < 8; ++j)
+                        if (cg + j < m) ms.Macc[r * ms.lda + cg + j] = acc[j];
                 }
             }
         }
@@ -258,7 +291,8 @@ static size_t mixed_smem_bytes(int m, int kc, bool need_x)
     int lda = m + 2;
     size_t s = 0;
     s += 2 * (size_t)MX_ROWS * kc * 4;                     // tiles hi, lo
-    s += (size_t)(m + 1) * lda * 8;                        // Macc (also A)
+    s += (size_t)m * lda * 8;                              // Macc (also A)
+    s += (size_t)kc * 4;                                   // tapered innovations
     if (need_x) s += (size_t)m * lda * 8;                  // X
     s += (size_t)6 * (m + 1) * 8;                          // b d e cs sn v
     s += (size_t)ENKFG_MAXTYPES * 8 * 2;
@@ -280,7 +314,8 @@ __global__ void __launch_bounds__(CALC_NT) k_transforms_mixed(CalcArgs a, int kc
     unsigned char* sp = smem_raw;
     float* tileH = (float*)sp;        sp += (size_t)MX_ROWS * kcm * 4;
     float* tileL = (float*)sp;        sp += (size_t)MX_ROWS * kcm * 4;
-    double* Macc = (double*)sp;       sp += (size_t)(m + 1) * lda * 8;
+    double* Macc = (double*)sp;       sp += (size_t)m * lda * 8;
+    float* sl = (float*)sp;           sp += (size_t)((kcm + 3) & ~3) * 4;
     double* X = nullptr;
     if (need_x) { X = (double*)sp;    sp += (size_t)m * lda * 8; }
     double* b = (double*)sp;          sp += (m + 1) * 8;
@@ -311,7 +346,7 @@ __global__ void __launch_bounds__(CALC_NT) k_transforms_mixed(CalcArgs a, int kc
     tc::fence_before();
     __syncthreads();
     tc::fence_after();
-    MixedShared ms{ tileH, tileL, Macc, lda, mbar, *tslot, N, kcm, err };
+    MixedShared ms{ tileH, tileL, (float2*)Macc, lda, sl, mbar, *tslot, N, kcm, err };
     uint32_t phase = 0;
 
     for (int it = 0;; ++it) {
@@ -324,7 +359,7 @@ __global__ void __launch_bounds__(CALC_NT) k_transforms_mixed(CalcArgs a, int kc
             tpd[tid] = 0.0;
             tcount[tid] = 0;
         }
-        for (int i = tid; i < (m + 1) * lda; i += CALC_NT) Macc[i] = 0.0;
+        for (int i = tid; i < m * lda; i += CALC_NT) Macc[i] = 0.0;   // also zero as float2
         __syncthreads();
         GramProcTC proc(a, s, ms, phase);
         const int p = enumerate_obs(a, kcm, qx, qy, qz, s, proc, true);
@@ -337,8 +372,12 @@ __global__ void __launch_bounds__(CALC_NT) k_transforms_mixed(CalcArgs a, int kc
             __syncthreads();
             continue;
         }
-        // b = S's (column m), M = I + S'S in place
-        if (tid < m) b[tid] = Macc[tid * lda + m];
+        // double-float -> FP64 in place; b = S's from the member threads
+        for (int i = tid; i < m * lda; i += CALC_NT) {
+            float2 v2 = ((float2*)Macc)[i];
+            Macc[i] = (double)v2.x + (double)v2.y;
+        }
+        if (tid < m) b[tid] = (double)proc.bhi + (double)proc.blo;
         __syncthreads();
         const double trss = la::block_sum<CALC_NT>(tid < m ? Macc[tid * lda + tid] : 0.0, red);
         if (tid < m) Macc[tid * lda + tid] += 1.0;
@@ -358,21 +397,17 @@ enkfg_status launch_mixed(enkfg_ctx* ctx, CalcArgs& a, cudaStream_t st)
 {
     const int m = a.m;
     const bool need_x = (a.mode == ENKFG_MODE_ENOI || a.scheme == ENKFG_SCHEME_DENKF);
-    const int N = ((m + 1) + 15) / 16 * 16;
+    const int N = (m + 15) / 16 * 16;
     uint32_t tcols = 32;
-    while ((int)tcols < N) tcols <<= 1;
-    int kcm = 64;
+    while ((int)tcols < MX_NA * N) tcols <<= 1;
+    const int kcm = 8 * MX_NA;
     size_t smem = mixed_smem_bytes(m, kcm, need_x);
-    while (smem > 220 * 1024 && kcm > 16) {
-        kcm >>= 1;
-        smem = mixed_smem_bytes(m, kcm, need_x);
-    }
     if (smem > 227 * 1024) {
         set_err(ctx, "mixed path: nmem = %d needs %zu bytes of shared memory", m, smem);
         return ENKFG_EUNSUPPORTED;
     }
     // the per-type pass's FP64 chunk buffer (kcm x m doubles) lives in the tiles
-    if ((size_t)kcm * m * 8 > 2 * (size_t)MX_ROWS * kcm * 4) {
+    if (tcols > 512 || (size_t)kcm * m * 8 > 2 * (size_t)MX_ROWS * kcm * 4) {
         set_err(ctx, "mixed path: tile too small for the per-type pass");
         return ENKFG_EUNSUPPORTED;
     }
