@@ -323,9 +323,9 @@ enkfg_status run_update(enkfg_ctx* ctx, const enkfg_update_params* p, const int*
         set_err(ctx, "the resident transforms hold no T (EnOI)");
         return ENKFG_ESTATE;
     }
-    if (p->precision != ENKFG_PREC_FP64) {
-        set_err(ctx, "mixed-precision update is not available in this build");
-        return ENKFG_EUNSUPPORTED;
+    if (p->precision != ENKFG_PREC_FP64 && p->precision != ENKFG_PREC_MIXED) {
+        set_err(ctx, "bad precision %d", p->precision);
+        return ENKFG_EINVAL;
     }
     int j1 = p->j1, j2 = p->j2 < 0 ? ctx->mnj - 1 : p->j2;
     if (j1 < 0 || j2 >= ctx->mnj || j1 > j2 || j1 % ctx->stride != 0) {
