@@ -153,7 +153,7 @@ __global__ void __launch_bounds__(CALC_NT) k_transforms(CalcArgs a)
         }
         __syncthreads();
         GramProc64<R> proc(a, s, tile, sloc);
-        const int p = enumerate_obs(a, kc, qx, qy, qz, s, proc, true);
+        const int p = enumerate_obs<false>(a, kc, qx, qy, qz, s, proc, true);
         if (p == 0) {
             store_empty(a, pt);
             __syncthreads();
@@ -182,30 +182,74 @@ __global__ void __launch_bounds__(CALC_NT) k_transforms(CalcArgs a)
 }
 
 // ---------------------------------------------------------------------------
-// size-sorted work queue: counting sort of points by descending count bin
+// size-sorted work queue: a stable counting sort of the points by descending
+// local-obs count bin.  Within a bin the grid order is kept, so consecutive
+// queue items stay spatially close and share their observations in L2.
 // ---------------------------------------------------------------------------
-__global__ void k_bin_hist(int n, const int* __restrict__ counts, int* __restrict__ hist)
-{
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) atomicAdd(&hist[NBINS - 1 - count_bin(counts[i])], 1);
-}
+#define QS_T 1024
 
-__global__ void k_bin_scan(int* hist)
+__global__ void k_queue_rank(int n, const int* __restrict__ counts, int* __restrict__ rank,
+                             int* __restrict__ blkcnt)
 {
-    if (threadIdx.x == 0) {
-        int acc = 0;
-        for (int b = 0; b < NBINS; ++b) {
-            int v = hist[b];
-            hist[b] = acc;
-            acc += v;
-        }
+    __shared__ int wcnt[QS_T / 32][NBINS];
+    const int i = blockIdx.x * QS_T + threadIdx.x, lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const int b = (i < n) ? NBINS - 1 - count_bin(counts[i]) : NBINS;   // descending count
+    for (int k = threadIdx.x; k < (QS_T / 32) * NBINS; k += QS_T) (&wcnt[0][0])[k] = 0;
+    __syncthreads();
+    const unsigned same = __match_any_sync(0xffffffffu, b);
+    const int r_in_warp = __popc(same & ((1u << lane) - 1));
+    if (b < NBINS && r_in_warp == 0) wcnt[wid][b] = __popc(same);
+    __syncthreads();
+    if (b < NBINS) {
+        int before = 0;
+        for (int w = 0; w < wid; ++w) before += wcnt[w][b];
+        rank[i] = before + r_in_warp;
+    }
+    if (threadIdx.x < NBINS) {
+        int t = 0;
+        for (int w = 0; w < QS_T / 32; ++w) t += wcnt[w][threadIdx.x];
+        blkcnt[blockIdx.x * NBINS + threadIdx.x] = t;
     }
 }
 
-__global__ void k_bin_scatter(int n, const int* __restrict__ counts, int* __restrict__ hist, int* __restrict__ order)
+// blkcnt [nblk][NBINS] -> exclusive offsets of (block, bin) in bin-major order
+__global__ void k_queue_offsets(int nblk, int* blkcnt)
 {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) order[atomicAdd(&hist[NBINS - 1 - count_bin(counts[i])], 1)] = i;
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    int acc = 0;
+    for (int b = 0; b < NBINS; ++b)
+        for (int k = 0; k < nblk; ++k) {
+            int v = blkcnt[k * NBINS + b];
+            blkcnt[k * NBINS + b] = acc;
+            acc += v;
+        }
+}
+
+__global__ void k_queue_scatter(int n, const int* __restrict__ counts, const int* __restrict__ rank,
+                                const int* __restrict__ blkoff, int* __restrict__ order)
+{
+    const int i = blockIdx.x * QS_T + threadIdx.x;
+    if (i >= n) return;
+    const int b = NBINS - 1 - count_bin(counts[i]);
+    order[blkoff[blockIdx.x * NBINS + b] + rank[i]] = i;
+}
+
+enkfg_status build_queue(enkfg_ctx* ctx, int npts, cudaStream_t st)
+{
+    enkfg_status s;
+    const int nblk = div_up(npts, QS_T);
+    size_t need = (size_t)npts + (size_t)nblk * NBINS;
+    // the scratch capacity is kept in bytes (scan_counts shares the buffer)
+    if ((s = ensure(ctx, (char**)&ctx->d_scratch, &ctx->scratch_cap, need * sizeof(int)))) return s;
+    int* rank = (int*)ctx->d_scratch;
+    int* blk = rank + npts;
+    k_queue_rank<<<nblk, QS_T, 0, st>>>(npts, ctx->d_counts, rank, blk);
+    CKL();
+    k_queue_offsets<<<1, 32, 0, st>>>(nblk, blk);
+    CKL();
+    k_queue_scatter<<<nblk, QS_T, 0, st>>>(npts, ctx->d_counts, rank, blk, ctx->d_order);
+    CKL();
+    return ENKFG_OK;
 }
 
 template <int R>
@@ -218,14 +262,14 @@ static enkfg_status launch_R(enkfg_ctx* ctx, CalcArgs& a, cudaStream_t st)
         return ENKFG_EUNSUPPORTED;
     }
     CK(cudaFuncSetAttribute(k_transforms<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    int grid = a.npts;
+    int grid = a.nitems;
     if (a.persistent) {
         int per_sm = 0, nsm = 0;
         CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_transforms<R>, CALC_NT, smem));
         CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, ctx->device));
         if (per_sm < 1) per_sm = 1;
         grid = per_sm * nsm;
-        if (grid > a.npts) grid = a.npts;
+        if (grid > a.nitems) grid = a.nitems;
     }
     if (grid < 1) return ENKFG_OK;
     k_transforms<R><<<grid, CALC_NT, smem, st>>>(a);
@@ -234,6 +278,95 @@ static enkfg_status launch_R(enkfg_ctx* ctx, CalcArgs& a, cudaStream_t st)
 }
 
 enkfg_status launch_mixed(enkfg_ctx* ctx, CalcArgs& a, cudaStream_t st);
+
+static enkfg_status dispatch(enkfg_ctx* ctx, CalcArgs& a, int precision, cudaStream_t st)
+{
+    const int m = a.m;
+    if (precision == ENKFG_PREC_MIXED) return launch_mixed(ctx, a, st);
+    if (m <= 32) return launch_R<2>(ctx, a, st);
+    if (m <= 48) return launch_R<3>(ctx, a, st);
+    if (m <= 64) return launch_R<4>(ctx, a, st);
+    if (m <= 96) return launch_R<6>(ctx, a, st);
+    return launch_R<9>(ctx, a, st);
+}
+
+// Autotuner: for every local-obs count bin that holds points, time the
+// persistent kernel on (up to) TUNE_SAMPLE of that bin's points -- taken from
+// the middle of the bin's stretch of the queue, so spatially contiguous --
+// with each candidate chunk size, and keep the fastest.  The table lives in
+// the context and is reused by later batched calls (enkfg_autotune_reset
+// drops it).
+#define TUNE_SAMPLE 1536
+static enkfg_status autotune(enkfg_ctx* ctx, CalcArgs a, int precision, cudaStream_t st)
+{
+    const int npts = a.npts;
+    int* order = (int*)malloc((size_t)npts * sizeof(int));
+    int* counts = (int*)malloc((size_t)npts * sizeof(int));
+    if (!order || !counts) {
+        free(order);
+        free(counts);
+        return ENKFG_ENOMEM;
+    }
+    cudaMemcpyAsync(order, ctx->d_order, (size_t)npts * sizeof(int), cudaMemcpyDeviceToHost, st);
+    cudaMemcpyAsync(counts, ctx->d_counts, (size_t)npts * sizeof(int), cudaMemcpyDeviceToHost, st);
+    cudaError_t e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) {
+        free(order);
+        free(counts);
+        return cuda_fail(ctx, e, "autotune copy", __LINE__);
+    }
+    static const int cand64[4] = { 8, 16, 32, 64 };
+    static const int candmx[4] = { 8, 16, 24, 32 };
+    const int* cand = precision == ENKFG_PREC_MIXED ? candmx : cand64;
+    int table[NBINS];
+    for (int b = 0; b < NBINS; ++b) table[b] = precision == ENKFG_PREC_MIXED ? 32 : (b < 4 ? 8 : b < 6 ? 16 : b < 9 ? 32 : 64);
+    int* kct = ctx->d_qhead + 2 + NBINS;
+    enkfg_status s = ENKFG_OK;
+    int pos = 0;
+    while (pos < npts && s == ENKFG_OK) {
+        const int bin = count_bin(counts[order[pos]]);
+        int end = pos;
+        while (end < npts && count_bin(counts[order[end]]) == bin) ++end;
+        const int len = end - pos;
+        const int take = len < TUNE_SAMPLE ? len : TUNE_SAMPLE;
+        const int first = pos + (len - take) / 2;
+        if (take >= 64 && bin >= 2) {
+            float best = 1e30f;
+            for (int k = 0; k < 4; ++k) {
+                int tab[NBINS];
+                for (int q = 0; q < NBINS; ++q) tab[q] = cand[k];
+                cudaMemcpyAsync(kct, tab, sizeof(tab), cudaMemcpyHostToDevice, st);
+                CalcArgs t = a;
+                t.order = ctx->d_order + first;
+                t.nitems = take;
+                float ms = 0.0f;
+                for (int rep = 0; rep < 2; ++rep) {       // first repetition warms the caches
+                    cudaMemsetAsync(ctx->d_qhead, 0, sizeof(int), st);
+                    cudaEventRecord(ctx->ev[6], st);
+                    if ((s = dispatch(ctx, t, precision, st))) break;
+                    cudaEventRecord(ctx->ev[7], st);
+                    cudaEventSynchronize(ctx->ev[7]);
+                    cudaEventElapsedTime(&ms, ctx->ev[6], ctx->ev[7]);
+                }
+                if (s) break;
+                if (ms < best) {
+                    best = ms;
+                    table[bin] = cand[k];
+                }
+            }
+        }
+        pos = end;
+    }
+    free(order);
+    free(counts);
+    if (s) return s;
+    CK(cudaMemcpyAsync(kct, table, sizeof(table), cudaMemcpyHostToDevice, st));
+    CK(cudaStreamSynchronize(st));
+    memcpy(ctx->kc_table, table, sizeof(table));
+    ctx->kc_tuned = true;
+    ctx->kc_tuned_prec = precision;
+    return ENKFG_OK;
+}
 
 enkfg_status run_transforms(enkfg_ctx* ctx, const enkfg_calc_params* p, cudaStream_t st)
 {
@@ -275,6 +408,7 @@ enkfg_status run_transforms(enkfg_ctx* ctx, const enkfg_calc_params* p, cudaStre
     CalcArgs a;
     memset(&a, 0, sizeof(a));
     a.npts = npts;
+    a.nitems = npts;
     a.ntypes = ctx->ntypes;
     a.ndim = ctx->geographic ? 3 : 2;
     a.m = m;
@@ -310,31 +444,31 @@ enkfg_status run_transforms(enkfg_ctx* ctx, const enkfg_calc_params* p, cudaStre
     if (p->path == ENKFG_PATH_BATCHED) {
         // size-sorted queue
         if ((s = count_local(ctx, ctx->d_counts, nullptr, st))) return s;
-        int* hist = ctx->d_qhead + 2;
-        CK(cudaMemsetAsync(ctx->d_qhead, 0, (2 + NBINS) * sizeof(int), st));
-        k_bin_hist<<<div_up(npts, 256), 256, 0, st>>>(npts, ctx->d_counts, hist);
-        CKL();
-        k_bin_scan<<<1, 32, 0, st>>>(hist);
-        CKL();
-        k_bin_scatter<<<div_up(npts, 256), 256, 0, st>>>(npts, ctx->d_counts, hist, ctx->d_order);
-        CKL();
+        if ((s = build_queue(ctx, npts, st))) return s;
         a.persistent = 1;
         a.order = ctx->d_order;
         a.qhead = ctx->d_qhead;
         a.counts = ctx->d_counts;
-        a.kc_table = ctx->d_qhead + 2 + NBINS;   // filled by the tuner (defaults below)
-        static const int kc_default[NBINS] = { 8, 8, 8, 8, 16, 16, 32, 32, 32, 64, 64, 64, 64, 64, 64, 64 };
-        CK(cudaMemcpyAsync(ctx->d_qhead + 2 + NBINS, kc_default, sizeof(kc_default), cudaMemcpyHostToDevice, st));
+        a.kc_table = ctx->d_qhead + 2 + NBINS;   // chunk size per count bin (autotuned)
+        if (ctx->kc_tuned && ctx->kc_tuned_prec == p->precision) {
+            CK(cudaMemcpyAsync(ctx->d_qhead + 2 + NBINS, ctx->kc_table, sizeof(ctx->kc_table), cudaMemcpyHostToDevice,
+                               st));
+        } else {
+            static const int kc_default[NBINS] = { 8, 8, 8, 8, 16, 16, 32, 32, 32, 64, 64, 64, 64, 64, 64, 64 };
+            static const int kc_mixed[NBINS] = { 8, 8, 8, 8, 16, 16, 24, 32, 32, 32, 32, 32, 32, 32, 32, 32 };
+            CK(cudaMemcpyAsync(ctx->d_qhead + 2 + NBINS, p->precision == ENKFG_PREC_MIXED ? kc_mixed : kc_default,
+                               sizeof(kc_default), cudaMemcpyHostToDevice, st));
+        }
         CK(cudaMemsetAsync(ctx->d_qhead, 0, sizeof(int), st));
     }
     cudaEventRecord(ctx->ev[2], st);
-    if (p->precision == ENKFG_PREC_MIXED) s = launch_mixed(ctx, a, st);
-    else if (m <= 32) s = launch_R<2>(ctx, a, st);
-    else if (m <= 48) s = launch_R<3>(ctx, a, st);
-    else if (m <= 64) s = launch_R<4>(ctx, a, st);
-    else if (m <= 96) s = launch_R<6>(ctx, a, st);
-    else s = launch_R<9>(ctx, a, st);
-    if (s) return s;
+    if (p->path == ENKFG_PATH_BATCHED && p->tune && !(ctx->kc_tuned && ctx->kc_tuned_prec == p->precision)) {
+        if ((s = autotune(ctx, a, p->precision, st))) return s;
+        CK(cudaMemsetAsync(ctx->d_status_pt, 0, (size_t)npts * sizeof(int), st));
+        CK(cudaMemsetAsync(ctx->d_qhead, 0, sizeof(int), st));
+        cudaEventRecord(ctx->ev[2], st);
+    }
+    if ((s = dispatch(ctx, a, p->precision, st))) return s;
     cudaEventRecord(ctx->ev[3], st);
     ctx->t_mode = p->mode;
     ctx->t_nmem = m;

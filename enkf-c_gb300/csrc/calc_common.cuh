@@ -15,6 +15,7 @@
 
 struct CalcArgs {
     int npts, ntypes, ndim, m, md, mode, scheme, want_diag, persistent, kc;
+    int nitems;        // queue length (npts, or a sample while autotuning)
     double alpha;
     const TypeIndex* types;
     const long long* bstart;
@@ -112,10 +113,13 @@ struct PointScratch {
 // order and hand them to proc.chunk(nc, t) in chunks of kc entries
 // (lid/llc[0..nc)); chunks never straddle a type.  Returns the count of
 // local observations; per-type counts go to s.tcount if count_types.
-template <class Proc>
+// FAST: taper coefficients in FP32, stored as floats in s.llc (mixed path);
+// otherwise exact FP64 coefficients (bit-identical to the reference's).
+template <bool FAST, class Proc>
 __device__ int enumerate_obs(const CalcArgs& a, int kc, double qx, double qy, double qz, const PointScratch& s,
                              Proc& proc, bool count_types)
 {
+    float* llcf = reinterpret_cast<float*>(s.llc);
     const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
     int* wsum = s.ictl + 8;
     int total = 0;
@@ -152,7 +156,10 @@ __device__ int enumerate_obs(const CalcArgs& a, int kc, double qx, double qy, do
                     if (in) {
                         int pos = n0 + before + __popc(bal & ((1u << lane) - 1));
                         s.lid[pos] = (int)p;
-                        s.llc[pos] = exact::calclcoeff(ti.nlocrad, ti.locrad, ti.locweight, __dsqrt_rn(d2));
+                        if (FAST)
+                            llcf[pos] = exact::calclcoeff_f(ti.nlocrad, ti.locrad, ti.locweight, sqrtf((float)d2));
+                        else
+                            s.llc[pos] = exact::calclcoeff(ti.nlocrad, ti.locrad, ti.locweight, __dsqrt_rn(d2));
                     }
                     __syncthreads();
                     int n = n0 + tot;
@@ -162,14 +169,17 @@ __device__ int enumerate_obs(const CalcArgs& a, int kc, double qx, double qy, do
                         int rest = n - kc;
                         int id = 0;
                         double lc = 0.0;
+                        float lcf = 0.0f;
                         if (tid < rest) {
                             id = s.lid[kc + tid];
-                            lc = s.llc[kc + tid];
+                            if (FAST) lcf = llcf[kc + tid];
+                            else lc = s.llc[kc + tid];
                         }
                         __syncthreads();
                         if (tid < rest) {
                             s.lid[tid] = id;
-                            s.llc[tid] = lc;
+                            if (FAST) llcf[tid] = lcf;
+                            else s.llc[tid] = lc;
                         }
                         __syncthreads();
                         n = rest;
@@ -346,7 +356,7 @@ __device__ inline void solve_point(const CalcArgs& a, int pt, int p, int kc, dou
         } else {
             __syncthreads();
             QuadProc qp(a, s, tile, tld, Q, gq, lda);
-            enumerate_obs(a, kc, qx, qy, qz, s, qp, false);
+            enumerate_obs<false>(a, kc, qx, qy, qz, s, qp, false);
             if (tid < a.ntypes) {
                 int t = tid;
                 size_t k = (size_t)t * a.npts + pt;
@@ -375,7 +385,7 @@ __device__ __forceinline__ int next_item(const CalcArgs& a, int it, int* ictl)
         idx = ictl[6];
         __syncthreads();
     } else {
-        idx = (it == 0) ? (int)blockIdx.x : a.npts;
+        idx = (it == 0) ? (int)blockIdx.x : a.nitems;
     }
-    return idx < a.npts ? idx : -1;
+    return idx < a.nitems ? idx : -1;
 }

@@ -197,12 +197,13 @@ struct GramProcTC {
         if (*ms.err) return;
         // 1. tapered S rows of the round, split into TF32 hi + lo; the
         //    tapered innovations for S's
-        if (tid < kc) ms.sl[tid] = (tid < nc) ? (float)(a.ss[s.lid[tid]] * s.llc[tid]) : 0.0f;
+        const float* lcf = reinterpret_cast<const float*>(s.llc);   // FP32 taper (enumerate_obs<true>)
+        if (tid < kc) ms.sl[tid] = (tid < nc) ? (float)a.ss[s.lid[tid]] * lcf[tid] : 0.0f;
         for (int i = tid; i < kc * m; i += CALC_NT) {
             int k = i / m, r = i - k * m;
             float v = 0.0f;
             if (k < nc) {
-                v = __fmul_rn(a.St[(size_t)s.lid[k] * a.mpad + r], (float)s.llc[k]);
+                v = __fmul_rn(a.St[(size_t)s.lid[k] * a.mpad + r], lcf[k]);
                 if (tsum) ssq += (double)v * (double)v;
             }
             float hi = tc::to_tf32(v);
@@ -231,7 +232,7 @@ struct GramProcTC {
         // S's on the CUDA cores while the tensor cores run (compensated FP32)
         if (tid < m) {
             for (int k = 0; k < nc; ++k) {
-                float v = __fmul_rn(a.St[(size_t)s.lid[k] * a.mpad + tid], (float)s.llc[k]);
+                float v = __fmul_rn(a.St[(size_t)s.lid[k] * a.mpad + tid], lcf[k]);
                 float x = ms.sl[k];
                 float p = v * x, pe = fmaf(v, x, -p);
                 float sm = bhi + p, bp = sm - bhi;
@@ -288,7 +289,7 @@ struct GramProcTC {
 
 static size_t mixed_smem_bytes(int m, int kc, bool need_x)
 {
-    int lda = m + 2;
+    int lda = (m % 2 == 0) ? m + 1 : m + 2;
     size_t s = 0;
     s += 2 * (size_t)MX_ROWS * kc * 4;                     // tiles hi, lo
     s += (size_t)m * lda * 8;                              // Macc (also A)
@@ -309,7 +310,7 @@ __global__ void __launch_bounds__(CALC_NT) k_transforms_mixed(CalcArgs a, int kc
 {
     extern __shared__ __align__(128) unsigned char smem_raw[];
     const int tid = threadIdx.x, wid = tid >> 5;
-    const int m = a.m, lda = m + 2;
+    const int m = a.m, lda = (m % 2 == 0) ? m + 1 : m + 2;   // odd stride: fewer bank conflicts
     const bool need_x = (a.mode == ENKFG_MODE_ENOI || a.scheme == ENKFG_SCHEME_DENKF);
     unsigned char* sp = smem_raw;
     float* tileH = (float*)sp;        sp += (size_t)MX_ROWS * kcm * 4;
@@ -354,6 +355,12 @@ __global__ void __launch_bounds__(CALC_NT) k_transforms_mixed(CalcArgs a, int kc
         if (idx < 0 || *err) break;
         const int pt = a.order ? a.order[idx] : idx;
         const double qx = a.qx[pt], qy = a.qy[pt], qz = a.ndim == 3 ? a.qz[pt] : 0.0;
+        // observations per round: 8 x (accumulators used), per count bin when tuned
+        ms.kc = kcm;
+        if (a.kc_table != nullptr && a.counts != nullptr) {
+            int k = a.kc_table[count_bin(a.counts[pt])];
+            ms.kc = (k >= 8 && k <= kcm) ? (k & ~7) : kcm;
+        }
         if (tid < ENKFG_MAXTYPES) {
             tss[tid] = 0.0;
             tpd[tid] = 0.0;
@@ -362,7 +369,7 @@ __global__ void __launch_bounds__(CALC_NT) k_transforms_mixed(CalcArgs a, int kc
         for (int i = tid; i < m * lda; i += CALC_NT) Macc[i] = 0.0;   // also zero as float2
         __syncthreads();
         GramProcTC proc(a, s, ms, phase);
-        const int p = enumerate_obs(a, kcm, qx, qy, qz, s, proc, true);
+        const int p = enumerate_obs<true>(a, ms.kc, qx, qy, qz, s, proc, true);
         if (*err) {
             if (tid == 0) a.status[pt] = MX_TIMEOUT_CODE;
             break;
@@ -383,7 +390,7 @@ __global__ void __launch_bounds__(CALC_NT) k_transforms_mixed(CalcArgs a, int kc
         if (tid < m) Macc[tid * lda + tid] += 1.0;
         __syncthreads();
         // the per-type pass reuses the operand tiles as its FP64 chunk buffer
-        solve_point(a, pt, p, kcm, qx, qy, qz, Macc, X, lda, b, trss, d, e, cs, sn, v, s, (double*)tileH, m);
+        solve_point(a, pt, p, ms.kc, qx, qy, qz, Macc, X, lda, b, trss, d, e, cs, sn, v, s, (double*)tileH, m);
         if (a.want_diag && a.ntypes > 1) {
             for (int i = tid; i < 2 * MX_ROWS * kcm; i += CALC_NT) tileH[i] = 0.0f;
             __syncthreads();
@@ -421,8 +428,9 @@ enkfg_status launch_mixed(enkfg_ctx* ctx, CalcArgs& a, cudaStream_t st)
         // TMEM: at most 512 columns per SM across resident CTAs
         while (per_sm > 1 && (uint32_t)per_sm * tcols > 512) --per_sm;
         grid = per_sm * nsm;
-        if (grid > a.npts) grid = a.npts;
+        if (grid > a.nitems) grid = a.nitems;
     } else {
+        grid = a.nitems;
         // one CTA per point: limit residency so TMEM allocations never wait
         // on each other beyond 512 columns (the smem footprint already keeps
         // residency low; the allocation itself blocks, it does not fail)

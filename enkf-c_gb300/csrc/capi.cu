@@ -131,6 +131,21 @@ ENKFG_API enkfg_status enkfg_rebuild_index(enkfg_ctx* ctx)
     return ENKFG_OK;
 }
 
+ENKFG_API enkfg_status enkfg_autotune_table(const enkfg_ctx* ctx, int* table)
+{
+    if (!ctx || !table) return ENKFG_EINVAL;
+    if (!ctx->kc_tuned) return ENKFG_ESTATE;
+    memcpy(table, ctx->kc_table, sizeof(ctx->kc_table));
+    return ENKFG_OK;
+}
+
+ENKFG_API enkfg_status enkfg_autotune_reset(enkfg_ctx* ctx)
+{
+    if (!ctx) return ENKFG_EINVAL;
+    ctx->kc_tuned = false;
+    return ENKFG_OK;
+}
+
 ENKFG_API long long enkfg_kernel_launches(const enkfg_ctx* ctx)
 {
     return ctx ? ctx->launches : 0;

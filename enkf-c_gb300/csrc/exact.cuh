@@ -28,13 +28,15 @@ __device__ __forceinline__ double taper_gc(double x)
     double x2 = __dmul_rn(x, x);
     double x3 = __dmul_rn(x2, x);
     double f;
+    // x/4 and x/2 are exact scalings: multiplying by 0.25 and 0.5 gives the
+    // same double as the division, without the division's instruction sequence
     if (x < 1.0) {
-        double a = __dadd_rn(__ddiv_rn(-x3, 4.0), __ddiv_rn(x2, 2.0));
+        double a = __dadd_rn(__dmul_rn(-x3, 0.25), __dmul_rn(x2, 0.5));
         f = __dadd_rn(1.0, __dmul_rn(x2, a));
         f = __dadd_rn(f, __dmul_rn(x3, 5.0 / 8.0));
         f = __dsub_rn(f, __dmul_rn(x2, 5.0 / 3.0));
     } else {
-        double a = __dsub_rn(__ddiv_rn(x3, 12.0), __ddiv_rn(x2, 2.0));
+        double a = __dsub_rn(__ddiv_rn(x3, 12.0), __dmul_rn(x2, 0.5));
         f = __dmul_rn(x2, a);
         f = __dadd_rn(f, __dmul_rn(x3, 5.0 / 8.0));
         f = __dadd_rn(f, __dmul_rn(x2, 5.0 / 3.0));
@@ -51,6 +53,31 @@ __device__ __forceinline__ double calclcoeff(int nlocrad, const double* locrad, 
     double sum = 0.0;
     for (int i = 0; i < nlocrad; ++i)
         if (dist <= locrad[i]) sum = __dadd_rn(sum, __dmul_rn(locweight[i], taper_gc(__ddiv_rn(dist, locrad[i]))));
+    return sum;
+}
+
+// FP32 taper for the mixed-precision path: same pieces, float arithmetic
+// (about 1e-7 relative); the membership test stays exact in FP64.
+__device__ __forceinline__ float taper_gc_f(float x)
+{
+    if (x >= 1.0f) return 0.0f;
+    x *= 2.0f;
+    float x2 = x * x, x3 = x2 * x, f;
+    if (x < 1.0f)
+        f = 1.0f + x2 * (-x3 * 0.25f + x2 * 0.5f) + x3 * 0.625f - x2 * (5.0f / 3.0f);
+    else
+        f = x2 * (x3 * (1.0f / 12.0f) - x2 * 0.5f) + x3 * 0.625f + x2 * (5.0f / 3.0f) - x * 5.0f + 4.0f -
+            (2.0f / 3.0f) / x;
+    return f >= 0.0f ? f : 0.0f;
+}
+
+__device__ __forceinline__ float calclcoeff_f(int nlocrad, const double* locrad, const double* locweight, float dist)
+{
+    float sum = 0.0f;
+    for (int i = 0; i < nlocrad; ++i) {
+        float r = (float)locrad[i];
+        if (dist <= r) sum += (float)locweight[i] * taper_gc_f(dist / r);
+    }
     return sum;
 }
 

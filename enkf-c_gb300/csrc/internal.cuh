@@ -117,6 +117,9 @@ struct enkfg_ctx {
     int* d_order;               // [npoints]
     int* d_qhead;               // queue head + error flag
     int* d_status_pt;           // [npoints] per-point status
+    bool kc_tuned;              // d_qhead[2+16 ..] holds an autotuned chunk-size table
+    int kc_tuned_prec;          // precision the table was tuned for
+    int kc_table[16];           // host copy of the tuned table
     void* d_scratch;
     size_t scratch_cap;
     size_t counts_cap, order_cap, status_cap;

@@ -38,7 +38,8 @@ struct UpdArgs {
     float* fields;
     float* infl;
     size_t plane;               // jsize * mni
-    int nk;                     // cells per CTA
+    int nk;                     // cells per CTA (tile cell stride)
+    int G;                      // strided columns per CTA (version 2 kernel)
 };
 
 // One element of the interpolated X5 for model cell (jt, i) of the tile
@@ -82,158 +83,297 @@ __device__ __forceinline__ double warp_sum_d(double v)
 }
 
 #define MAXE_PER_LANE 5   // members per lane (nmem <= 160)
+#define UPD_FC 8          // field-layers per register block
 
-__global__ void __launch_bounds__(UPD_NT) k_update_fields(UpdArgs a)
+// double or double-float (FP32 pair) accumulation of the per-row sums the
+// reference keeps in double (update.c:381-383, 405-410, 437-441)
+template <bool F64>
+struct Acc;
+template <>
+struct Acc<true> {
+    double v;
+    __device__ __forceinline__ Acc() : v(0.0) {}
+    __device__ __forceinline__ void add(float x) { v += (double)x; }
+    __device__ __forceinline__ void add_prod(float a, float b) { v += (double)__fmul_rn(a, b); }
+    __device__ __forceinline__ void reduce()
+    {
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    }
+    __device__ __forceinline__ double value() const { return v; }
+};
+template <>
+struct Acc<false> {
+    float hi, lo;
+    __device__ __forceinline__ Acc() : hi(0.0f), lo(0.0f) {}
+    __device__ __forceinline__ void add(float x)
+    {
+        float s = hi + x, bp = s - hi;
+        lo += (hi - (s - bp)) + (x - bp);
+        hi = s;
+    }
+    __device__ __forceinline__ void add_prod(float a, float b) { add(__fmul_rn(a, b)); }
+    __device__ __forceinline__ void reduce()
+    {
+        for (int o = 16; o > 0; o >>= 1) {
+            float oh = __shfl_xor_sync(0xffffffffu, hi, o), ol = __shfl_xor_sync(0xffffffffu, lo, o);
+            add(oh);
+            lo += ol;
+        }
+    }
+    __device__ __forceinline__ double value() const { return (double)hi + (double)lo; }
+};
+
+// (float)(x - mean) with mean held in double (F64) or as a double-float
+__device__ __forceinline__ float sub_mean(float x, double mean) { return (float)((double)x - mean); }
+
+// das_updatefields, version 2.  A CTA owns one model row j and G strided
+// columns (cells i in [ii0*stride, (ii0+G)*stride)).  It builds, once, the
+// j-interpolated transforms Tjj/wjj of the G strided columns plus the i-
+// neighbour of the last one (the reference's Tjj, update.c:224-241), stages
+// the [nfield][nmem][cells] field block, and then every warp takes one cell:
+// lanes own output members, the i-interpolated X5 element (update.c:255-265,
+// same float operations) is formed in registers and applied to UPD_FC
+// field-layers at a time, and the per-row statistics use warp shuffles.
+template <bool F64>
+__global__ void __launch_bounds__(UPD_NT) k_update_v2(UpdArgs a)
 {
     extern __shared__ __align__(16) float usm[];
-    const int m = a.m, md = a.md, nk = a.nk, nf = a.nfield;
-    const int TLD = m + 1;
-    float* Tc = usm;                                   // [md][m+1]
-    float* wc = Tc + (size_t)md * TLD;                 // [m]
-    float* tile = wc + ((m + 3) & ~3);                 // [nf][m][nk]
-    float* Asm = tile + (size_t)nf * m * nk;           // [UPD_NT/32][m]
+    const int m = a.m, md = a.md, G = a.G, st = a.stride, nf = a.nfield;
+    const int TLD = m + 1, M4 = (m + 3) & ~3;
     const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
-    const int jt = blockIdx.y;
-    const int i0 = blockIdx.x * nk;
-    const int ncell = min(nk, a.mni - i0);
-    const int jj = a.j1 / a.stride + jt / a.stride, stepj = jt % a.stride;
-    const int jg = a.j1 + jt;
+    const int jt = blockIdx.y, jg = a.j1 + jt;
+    const int jj = a.j1 / st + jt / st, stepj = jt % st;
+    const int jj2 = (jj < a.nj - 1) ? jj + 1 : jj;
+    const int ii0 = blockIdx.x * G;
+    const int gv = min(G, a.ni - ii0);                       // strided columns of this CTA
+    const int i0 = ii0 * st;
+    const int ncell = min(gv * st, a.mni - i0);
+    const int CP = a.nk;                                     // cell stride of the tile
+    // carve (every region starts on a 16-byte boundary: Abuf is read as float4)
+    float* Tjj = usm;                                                    // [(G+1)][md][TLD]
+    float* Wjj = Tjj + (((size_t)(G + 1) * md * TLD + 3) & ~(size_t)3); // [(G+1)][M4]
+    float* tile = Wjj + (size_t)(G + 1) * M4;                            // [nf][m][CP]
+    float* Abuf = tile + (((size_t)nf * m * CP + 3) & ~(size_t)3);       // [8 warps][UPD_FC][M4]
 
-    // stage the field block
-    for (int idx = tid; idx < nf * m * nk; idx += UPD_NT) {
-        int c = idx % nk, fe = idx / nk;
+    // 1. Tjj / wjj for slots 0..gv (slot gv = i-neighbour of the last column)
+    {
+        const int last = ii0 + gv - 1;
+        const int nb = (last < a.ni - 1) ? last + 1 : (a.periodic_i ? (last + 1) % a.ni : last);
+        const float w2 = __fdiv_rn((float)stepj, (float)st), w1 = __fsub_rn(1.0f, w2);
+        const bool jint = (st > 1 && stepj > 0);
+        const int ntot = (gv + 1) * md * m;
+        for (int idx = tid; idx < ntot; idx += UPD_NT) {
+            int k = idx / (md * m), e = idx - k * (md * m);
+            int col = (k < gv) ? ii0 + k : nb;
+            float v = __ldg(&a.T[((size_t)jj * a.ni + col) * md * m + e]);
+            if (jint) {
+                float b = __ldg(&a.T[((size_t)jj2 * a.ni + col) * md * m + e]);
+                v = __fadd_rn(__fmul_rn(v, w1), __fmul_rn(b, w2));
+            }
+            int e1 = e / m, e2 = e - e1 * m;
+            Tjj[((size_t)k * md + e1) * TLD + e2] = v;
+        }
+        for (int idx = tid; idx < (gv + 1) * m; idx += UPD_NT) {
+            int k = idx / m, e = idx - k * m;
+            int col = (k < gv) ? ii0 + k : nb;
+            float v = __ldg(&a.w[((size_t)jj * a.ni + col) * m + e]);
+            if (jint) {
+                float b = __ldg(&a.w[((size_t)jj2 * a.ni + col) * m + e]);
+                v = __fadd_rn(__fmul_rn(v, w1), __fmul_rn(b, w2));
+            }
+            Wjj[k * M4 + e] = v;
+        }
+    }
+    // 2. stage the field block (NK consecutive floats per member row)
+    for (int idx = tid; idx < nf * m * CP; idx += UPD_NT) {
+        int c = idx % CP, fe = idx / CP;
         if (c < ncell) {
             int f = fe / m, e = fe - f * m;
             tile[idx] = a.fields[((size_t)f * m + e) * a.plane + (size_t)jt * a.mni + i0 + c];
         }
     }
-    float* Aw = Asm + wid * m;
+    __syncthreads();
 
-    for (int c = 0; c < ncell; ++c) {
+    float* Aw = Abuf + (size_t)wid * UPD_FC * M4;
+    const int EPL = (md + 31) >> 5;                          // output members per lane
+    for (int c = wid; c < ncell; c += UPD_NT / 32) {
         const int i = i0 + c;
-        const int ii = i / a.stride, stepi = i % a.stride;
-        __syncthreads();
-        for (int idx = tid; idx < md * m; idx += UPD_NT) {
-            int e1 = idx / m, e2 = idx - e1 * m;
-            Tc[e1 * TLD + e2] = interp_x5(a.T, md * m, idx, jj, stepj, ii, stepi, a);
-        }
-        for (int idx = tid; idx < m; idx += UPD_NT) wc[idx] = interp_x5(a.w, m, idx, jj, stepj, ii, stepi, a);
-        __syncthreads();
+        const int slot = i / st - ii0, stepi = i % st;
+        const bool iint = (st > 1 && stepi > 0);
+        const float u2 = __fdiv_rn((float)stepi, (float)st), u1 = __fsub_rn(1.0f, u2);
+        const float* Ta = Tjj + (size_t)slot * md * TLD;
+        const float* Tb = Tjj + (size_t)(slot + 1) * md * TLD;
         const int nl = a.numlevels[(size_t)jg * a.mni + i];
-        for (int f = wid; f < nf; f += UPD_NT / 32) {
-            float* v = tile + (size_t)f * m * nk;      // v[e * nk + c]
-            const int level = a.levels[f];
-            float inflation = a.inflation0;
-            bool masked = (a.surfk == 0) ? (nl <= level) : (nl <= (a.issurfacevar ? 0 : a.surfk - level));
-            if (masked) {
-                for (int e = lane; e < m; e += 32) v[e * nk + c] = 0.0f;
-                if (a.infl && lane == 0) a.infl[(size_t)f * a.plane + (size_t)jt * a.mni + i] = 0.0f;
-                continue;
-            }
-            // first member with a missing value (update.c:337-350)
-            int first = m;
-            for (int e0 = 0; e0 < m && first == m; e0 += 32) {
-                int e = e0 + lane;
-                bool bad = false;
-                if (e < m) {
-                    float x = v[e * nk + c];
-                    bad = !isfinite(x) || fabsf(x) > MAXOBSVAL_F;
+        const size_t ioff = (size_t)jt * a.mni + i;
+        for (int f0 = 0; f0 < nf; f0 += UPD_FC) {
+            const int fc = min(UPD_FC, nf - f0);
+            unsigned active = 0;                              // rows to update
+            double mean[UPD_FC];
+            // per row: mask, missing values, mean, anomalies (update.c:296-392)
+            for (int q = 0; q < fc; ++q) {
+                const int f = f0 + q;
+                float* v = tile + (size_t)f * m * CP;
+                const int level = a.levels[f];
+                mean[q] = 0.0;
+                bool masked = (a.surfk == 0) ? (nl <= level) : (nl <= (a.issurfacevar ? 0 : a.surfk - level));
+                if (masked) {
+                    for (int e = lane; e < m; e += 32) v[e * CP + c] = 0.0f;
+                    if (a.infl && lane == 0) a.infl[(size_t)f * a.plane + ioff] = 0.0f;
+                    continue;
                 }
-                unsigned bal = __ballot_sync(0xffffffffu, bad);
-                if (bal) first = e0 + __ffs(bal) - 1;
+                int first = m;
+                for (int e0 = 0; e0 < m && first == m; e0 += 32) {
+                    int e = e0 + lane;
+                    bool bad = false;
+                    if (e < m) {
+                        float x = v[e * CP + c];
+                        bad = !isfinite(x) || fabsf(x) > MAXOBSVAL_F;
+                    }
+                    unsigned bal = __ballot_sync(0xffffffffu, bad);
+                    if (bal) first = e0 + __ffs(bal) - 1;
+                }
+                if (a.infl && lane == 0) a.infl[(size_t)f * a.plane + ioff] = 0.0f;
+                if (first < md) {
+                    for (int e = lane; e < m; e += 32) v[e * CP + c] = 0.0f;
+                    continue;
+                } else if (first < m) {
+                    for (int e = md + lane; e < m; e += 32) v[e * CP + c] = 0.0f;
+                    if (md == 0) continue;
+                }
+                Acc<F64> sm;
+                for (int e = lane; e < md; e += 32) sm.add(v[e * CP + c]);
+                sm.reduce();
+                mean[q] = sm.value() / (double)md;
+                for (int e = lane; e < M4; e += 32) Aw[q * M4 + e] = (e < m) ? sub_mean(v[e * CP + c], mean[q]) : 0.0f;
+                active |= 1u << q;
             }
-            if (first < md) {
-                for (int e = lane; e < m; e += 32) v[e * nk + c] = 0.0f;
-                if (a.infl && lane == 0) a.infl[(size_t)f * a.plane + (size_t)jt * a.mni + i] = 0.0f;
-                continue;
-            } else if (first < m) {
-                for (int e = md + lane; e < m; e += 32) v[e * nk + c] = 0.0f;
-                if (md == 0) continue;
-            }
-            // ensemble mean of the dynamic members (FP64)
-            double s = 0.0;
-            for (int e = lane; e < md; e += 32) s += (double)v[e * nk + c];
-            const double v1_f = warp_sum_d(s) / (double)md;
-            // anomalies of all members
-            for (int e = lane; e < m; e += 32) Aw[e] = (float)((double)v[e * nk + c] - v1_f);
             __syncwarp();
-            // A^a = A^f T  (T[e1] is column e1 of the reference's m x m_dyn
-            // matrix, update.c:399)
-            float aa[MAXE_PER_LANE];
+            if (active == 0) continue;
+            // A^a = A^f T on the active rows: acc[q][k] for member lane+32k
+            float acc[UPD_FC][MAXE_PER_LANE];
 #pragma unroll
-            for (int k = 0; k < MAXE_PER_LANE; ++k) {
-                int e1 = lane + 32 * k;
-                float acc = 0.0f;
-                if (e1 < md) {
-                    const float* Tr = Tc + e1 * TLD;
-                    for (int e2 = 0; e2 < m; ++e2) acc = fmaf(Tr[e2], Aw[e2], acc);
-                }
-                aa[k] = acc;
-            }
-            // mean increment: sum of float products in FP64 (update.c:405-410)
-            s = 0.0;
-            for (int e = lane; e < m; e += 32) s += (double)__fmul_rn(Aw[e], wc[e]);
-            const double v1_a = warp_sum_d(s) + v1_f;
-            float af[MAXE_PER_LANE];
+            for (int q = 0; q < UPD_FC; ++q)
 #pragma unroll
-            for (int k = 0; k < MAXE_PER_LANE; ++k) {
-                int e1 = lane + 32 * k;
-                af[k] = (e1 < m) ? Aw[e1] : 0.0f;
-            }
-            if (a.mode == ENKFG_MODE_HYBRID) {
-                double k_d = (md > 1) ? sqrt((double)(m - 1) / (double)(md - 1)) : 1.0;
+                for (int k = 0; k < MAXE_PER_LANE; ++k) acc[q][k] = 0.0f;
+            for (int e2 = 0; e2 < m; e2 += 4) {
+                float4 av[UPD_FC];
 #pragma unroll
-                for (int k = 0; k < MAXE_PER_LANE; ++k)
-                    if (lane + 32 * k < md) {
-                        aa[k] = (float)((double)aa[k] / k_d);
-                        af[k] = (float)((double)af[k] / k_d);
+                for (int q = 0; q < UPD_FC; ++q)
+                    av[q] = (q < fc) ? *reinterpret_cast<const float4*>(&Aw[q * M4 + e2]) : make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+                for (int k = 0; k < MAXE_PER_LANE; ++k) {
+                    if (k >= EPL) break;
+                    const int e1 = lane + 32 * k;
+                    if (e1 < md) {
+                        float t4[4];
+#pragma unroll
+                        for (int u = 0; u < 4; ++u) {
+                            const int e = e2 + u;
+                            float t = 0.0f;
+                            if (e < m) {
+                                t = Ta[e1 * TLD + e];
+                                if (iint) t = __fadd_rn(__fmul_rn(t, u1), __fmul_rn(Tb[e1 * TLD + e], u2));
+                            }
+                            t4[u] = t;
+                        }
+#pragma unroll
+                        for (int q = 0; q < UPD_FC; ++q) {
+                            acc[q][k] = fmaf(t4[0], av[q].x, acc[q][k]);
+                            acc[q][k] = fmaf(t4[1], av[q].y, acc[q][k]);
+                            acc[q][k] = fmaf(t4[2], av[q].z, acc[q][k]);
+                            acc[q][k] = fmaf(t4[3], av[q].w, acc[q][k]);
+                        }
                     }
-            }
-            if (!isnan(a.inf_ratio)) {
-                double s2f = 0.0, s2a = 0.0;
-#pragma unroll
-                for (int k = 0; k < MAXE_PER_LANE; ++k)
-                    if (lane + 32 * k < md) {
-                        s2f += (double)__fmul_rn(af[k], af[k]);
-                        s2a += (double)__fmul_rn(aa[k], aa[k]);
-                    }
-                double v2_f = warp_sum_d(s2f), v2_a = warp_sum_d(s2a);
-                if (v2_a > 0.0) {
-                    inflation = (float)(sqrt(v2_f / v2_a) * a.inf_ratio + 1.0 - a.inf_ratio);
-                    if (inflation >= a.inflation0) inflation = a.inflation0;
                 }
             }
-            const bool inflate = __fsub_rn(inflation, 1.0f) > 1.0e-6f;
-            if (!inflate) inflation = 1.0f;
+            // interpolated w for the mean increment
+            float wl[MAXE_PER_LANE];
 #pragma unroll
             for (int k = 0; k < MAXE_PER_LANE; ++k) {
-                int e1 = lane + 32 * k;
-                if (e1 < md) {
-                    float va = inflate ? __fmul_rn(aa[k], inflation) : aa[k];
-                    va = (float)((double)va + v1_a);
-                    float vf = (float)((double)af[k] + v1_f);
-                    float out;
-                    if (!a.output_increment) out = va;
-                    else if (!a.applylog) out = __fsub_rn(va, vf);
-                    else {
-                        // --output-increment of a log10 variable: difference
-                        // in physical space, 0 where the forecast is not a
-                        // normal number (update.c:484-497)
-                        float avf = fabsf(vf);
-                        bool normal = (avf >= 1.17549435e-38f) && (avf <= 3.40282347e+38f);
-                        double ea = pow(10.0, (double)va), ef = pow(10.0, (double)vf);
-                        out = normal ? (float)(ea - ef) : 0.0f;
-                    }
-                    v[e1 * nk + c] = out;
+                const int e = lane + 32 * k;
+                float t = 0.0f;
+                if (e < m) {
+                    t = Wjj[slot * M4 + e];
+                    if (iint) t = __fadd_rn(__fmul_rn(t, u1), __fmul_rn(Wjj[(slot + 1) * M4 + e], u2));
                 }
+                wl[k] = t;
             }
-            if (a.infl && lane == 0) a.infl[(size_t)f * a.plane + (size_t)jt * a.mni + i] = inflation;
+            // per row: mean update, hybrid rescaling, inflation, output
+#pragma unroll
+            for (int q = 0; q < UPD_FC; ++q) {
+                if (!((active >> q) & 1u)) continue;
+                const int f = f0 + q;
+                float* v = tile + (size_t)f * m * CP;
+                float inflation = a.inflation0;
+                Acc<F64> sa;
+#pragma unroll
+                for (int k = 0; k < MAXE_PER_LANE; ++k) {
+                    const int e = lane + 32 * k;
+                    if (e < m) sa.add_prod(Aw[q * M4 + e], wl[k]);
+                }
+                sa.reduce();
+                const double v1_a = sa.value() + mean[q];
+                float af[MAXE_PER_LANE], aa[MAXE_PER_LANE];
+#pragma unroll
+                for (int k = 0; k < MAXE_PER_LANE; ++k) {
+                    const int e = lane + 32 * k;
+                    af[k] = (e < m) ? Aw[q * M4 + e] : 0.0f;
+                    aa[k] = acc[q][k];
+                }
+                if (a.mode == ENKFG_MODE_HYBRID) {
+                    const double k_d = (md > 1) ? sqrt((double)(m - 1) / (double)(md - 1)) : 1.0;
+#pragma unroll
+                    for (int k = 0; k < MAXE_PER_LANE; ++k)
+                        if (lane + 32 * k < md) {
+                            aa[k] = (float)((double)aa[k] / k_d);
+                            af[k] = (float)((double)af[k] / k_d);
+                        }
+                }
+                if (!isnan(a.inf_ratio)) {
+                    Acc<F64> s2f, s2a;
+#pragma unroll
+                    for (int k = 0; k < MAXE_PER_LANE; ++k)
+                        if (lane + 32 * k < md) {
+                            s2f.add_prod(af[k], af[k]);
+                            s2a.add_prod(aa[k], aa[k]);
+                        }
+                    s2f.reduce();
+                    s2a.reduce();
+                    const double v2_f = s2f.value(), v2_a = s2a.value();
+                    if (v2_a > 0.0) {
+                        inflation = (float)(sqrt(v2_f / v2_a) * a.inf_ratio + 1.0 - a.inf_ratio);
+                        if (inflation >= a.inflation0) inflation = a.inflation0;
+                    }
+                }
+                const bool inflate = __fsub_rn(inflation, 1.0f) > 1.0e-6f;
+                if (!inflate) inflation = 1.0f;
+#pragma unroll
+                for (int k = 0; k < MAXE_PER_LANE; ++k) {
+                    const int e1 = lane + 32 * k;
+                    if (e1 < md) {
+                        float va = inflate ? __fmul_rn(aa[k], inflation) : aa[k];
+                        va = (float)((double)va + v1_a);
+                        float vf = (float)((double)af[k] + mean[q]);
+                        float out;
+                        if (!a.output_increment) out = va;
+                        else if (!a.applylog) out = __fsub_rn(va, vf);
+                        else {
+                            float avf = fabsf(vf);
+                            bool normal = (avf >= 1.17549435e-38f) && (avf <= 3.40282347e+38f);
+                            double ea = pow(10.0, (double)va), ef = pow(10.0, (double)vf);
+                            out = normal ? (float)(ea - ef) : 0.0f;
+                        }
+                        v[e1 * CP + c] = out;
+                    }
+                }
+                if (a.infl && lane == 0) a.infl[(size_t)f * a.plane + ioff] = inflation;
+            }
             __syncwarp();
         }
     }
     __syncthreads();
-    for (int idx = tid; idx < nf * m * nk; idx += UPD_NT) {
-        int c = idx % nk, fe = idx / nk;
+    for (int idx = tid; idx < nf * m * CP; idx += UPD_NT) {
+        int c = idx % CP, fe = idx / CP;
         if (c < ncell) {
             int f = fe / m, e = fe - f * m;
             a.fields[((size_t)f * m + e) * a.plane + (size_t)jt * a.mni + i0 + c] = tile[idx];
@@ -371,25 +511,33 @@ enkfg_status run_update(enkfg_ctx* ctx, const enkfg_update_params* p, const int*
         cudaEventRecord(ctx->ev[5], st);
         return ENKFG_OK;
     }
-    if (a.m > 32 * MAXE_PER_LANE) {
+    if (a.m > 32 * MAXE_PER_LANE || a.md > 32 * MAXE_PER_LANE) {
         set_err(ctx, "nmem = %d too large for the update kernel", a.m);
         return ENKFG_EUNSUPPORTED;
     }
-    // choose cells per CTA and field-layers per launch to fit shared memory
+    // strided columns per CTA and field-layers per launch to fit shared memory
     const size_t smem_cap = 200 * 1024;
-    size_t fixed = ((size_t)a.md * (a.m + 1) + ((a.m + 3) & ~3) + (UPD_NT / 32) * a.m) * sizeof(float);
-    int nk = 32;
+    const int M4 = (a.m + 3) & ~3, TLD = a.m + 1;
+    auto need = [&](int G, int nf) {
+        size_t cp = (size_t)G * a.stride;
+        return ((((size_t)(G + 1) * a.md * TLD + 3) & ~(size_t)3) + (size_t)(G + 1) * M4 +
+                (((size_t)nf * a.m * cp + 3) & ~(size_t)3) + (size_t)(UPD_NT / 32) * UPD_FC * M4) * sizeof(float);
+    };
+    int G = a.stride >= 32 ? 1 : (32 + a.stride - 1) / a.stride;
     int fg = nfield;
-    while (nk > 4 && fixed + (size_t)fg * a.m * nk * 4 > smem_cap) nk >>= 1;
-    while (fg > 1 && fixed + (size_t)fg * a.m * nk * 4 > smem_cap) fg = (fg + 1) / 2;
+    while (G > 1 && need(G, fg) > smem_cap) --G;
+    while (fg > 1 && need(G, fg) > smem_cap) fg = (fg + 1) / 2;
     if (fg > 448) fg = 448;
-    size_t smem = fixed + (size_t)fg * a.m * nk * 4;
+    size_t smem = need(G, fg);
     if (smem > 227 * 1024) {
         set_err(ctx, "update tile does not fit in shared memory (nmem %d)", a.m);
         return ENKFG_EUNSUPPORTED;
     }
-    CK(cudaFuncSetAttribute(k_update_fields, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    a.nk = nk;
+    const bool f64 = (p->precision == ENKFG_PREC_FP64);
+    if (f64) CK(cudaFuncSetAttribute(k_update_v2<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    else CK(cudaFuncSetAttribute(k_update_v2<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    a.G = G;
+    a.nk = G * a.stride;
     for (int f0 = 0; f0 < nfield; f0 += fg) {
         int nf = nfield - f0 < fg ? nfield - f0 : fg;
         CK(cudaMemcpyAsync(d_levels, levels + f0, nf * sizeof(int), cudaMemcpyHostToDevice, st));
@@ -397,8 +545,9 @@ enkfg_status run_update(enkfg_ctx* ctx, const enkfg_update_params* p, const int*
         a.nfield = nf;
         a.fields = d_fields + (size_t)f0 * a.m * a.plane;
         a.infl = d_infl ? d_infl + (size_t)f0 * a.plane : nullptr;
-        dim3 g(div_up(a.mni, nk), a.jsize);
-        k_update_fields<<<g, UPD_NT, smem, st>>>(a);
+        dim3 g(div_up(a.ni, G), a.jsize);
+        if (f64) k_update_v2<true><<<g, UPD_NT, smem, st>>>(a);
+        else k_update_v2<false><<<g, UPD_NT, smem, st>>>(a);
         CKL();
         if (f0 + fg < nfield) CK(cudaStreamSynchronize(st));
     }

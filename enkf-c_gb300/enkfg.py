@@ -44,7 +44,8 @@ EXPORTS = ["enkfg_create", "enkfg_destroy", "enkfg_last_error", "enkfg_status_st
            "enkfg_calc_transforms", "enkfg_calc_transforms_dev", "enkfg_transforms_dev_ptr",
            "enkfg_set_transforms", "enkfg_update_fields", "enkfg_update_fields_dev", "enkfg_set_hybrid_ensemble",
            "enkfg_set_hybrid_ensemble_dev", "enkfg_kernel_launches", "enkfg_stage_times", "enkfg_set_stream",
-           "enkfg_set_HE_dev", "enkfg_rebuild_index", "enkfg_local_offsets_noalloc"]
+           "enkfg_set_HE_dev", "enkfg_rebuild_index", "enkfg_local_offsets_noalloc", "enkfg_autotune_table",
+           "enkfg_autotune_reset"]
 
 
 class EnkfgError(RuntimeError):
@@ -61,7 +62,7 @@ class Grid(C.Structure):
 
 class CalcParams(C.Structure):
     _fields_ = [("mode", C.c_int), ("scheme", C.c_int), ("alpha", C.c_double), ("path", C.c_int),
-                ("precision", C.c_int), ("want_diag", C.c_int)]
+                ("precision", C.c_int), ("want_diag", C.c_int), ("tune", C.c_int)]
 
 
 class Diag(C.Structure):
@@ -249,8 +250,16 @@ class Enkfg:
                                         _p(coeffs, C.c_double), C.c_longlong(total)))
         return counts.reshape(self.nj, self.ni), offsets, ids[:total], coeffs[:total]
 
+    def autotune_table(self):
+        t = (C.c_int * 16)()
+        st = self.L.enkfg_autotune_table(self.h, t)
+        return None if st != 0 else list(t)
+
+    def autotune_reset(self):
+        self._ck(self.L.enkfg_autotune_reset(self.h))
+
     def calctransforms(self, mode=MODE_ENKF, scheme=SCHEME_ETKF, alpha=1.0, path=PATH_PLAIN, precision=PREC_FP64,
-                       want64=False, want_diag=True):
+                       want64=False, want_diag=True, tune=False):
         npts = self.nj * self.ni
         m, md = self.nmem, self.nmem_dynamic
         enkf = mode != MODE_ENOI
@@ -269,15 +278,15 @@ class Enkfg:
                        psrf=np.zeros((nt, self.nj, self.ni), np.float32))
             dg = Diag(_p(out["nlobs"], C.c_int), _p(out["dfs"], C.c_float), _p(out["srf"], C.c_float),
                       _p(out["pnlobs"], C.c_int), _p(out["pdfs"], C.c_float), _p(out["psrf"], C.c_float))
-        prm = CalcParams(mode, scheme, float(alpha), path, precision, int(want_diag))
+        prm = CalcParams(mode, scheme, float(alpha), path, precision, int(want_diag), int(tune))
         self._ck(self.L.enkfg_calc_transforms(self.h, C.byref(prm), _p(T, C.c_float), _p(w, C.c_float),
                                               _p(T64, C.c_double), _p(w64, C.c_double),
                                               C.byref(dg) if dg is not None else None))
         return out
 
     def calctransforms_dev(self, mode=MODE_ENKF, scheme=SCHEME_ETKF, alpha=1.0, path=PATH_PLAIN,
-                           precision=PREC_FP64, want_diag=False, stream=None):
-        prm = CalcParams(mode, scheme, float(alpha), path, precision, int(want_diag))
+                           precision=PREC_FP64, want_diag=False, stream=None, tune=False):
+        prm = CalcParams(mode, scheme, float(alpha), path, precision, int(want_diag), int(tune))
         self._ck(self.L.enkfg_calc_transforms_dev(self.h, C.byref(prm), C.c_void_p(stream)))
 
     def set_transforms(self, T, w, mode=MODE_ENKF, nmem=None, nmem_dynamic=None):

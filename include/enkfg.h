@@ -127,6 +127,7 @@ typedef struct {
     int path;                   /* ENKFG_PATH_PLAIN or ENKFG_PATH_BATCHED */
     int precision;              /* ENKFG_PREC_FP64 or ENKFG_PREC_MIXED */
     int want_diag;              /* fill the enkf_diag.nc outputs */
+    int tune;                   /* batched path: autotune the chunk size per local-obs count bin on first use */
 } enkfg_calc_params;
 
 typedef struct {
@@ -196,6 +197,13 @@ ENKFG_API enkfg_status enkfg_set_HE_dev(enkfg_ctx* ctx, int nmem, int nmem_dynam
 /* Drop the spatial index so that the next transforms call rebuilds it
  * (obs_createkdtrees is part of every enkf_calc run, observations.c:1616). */
 ENKFG_API enkfg_status enkfg_rebuild_index(enkfg_ctx* ctx);
+
+/* The chunk sizes (observations per contraction step) the autotuner chose
+ * per local-obs count bin (bin b holds counts in [2^b - 1, 2^(b+1) - 1));
+ * table[16].  Returns ENKFG_ESTATE before the first tuned batched call. */
+ENKFG_API enkfg_status enkfg_autotune_table(const enkfg_ctx* ctx, int* table);
+/* Forget the tuned table (the next tuned batched call tunes again). */
+ENKFG_API enkfg_status enkfg_autotune_reset(enkfg_ctx* ctx);
 
 /* Number of kernels this context has launched (for launch accounting). */
 ENKFG_API long long enkfg_kernel_launches(const enkfg_ctx* ctx);

@@ -57,7 +57,8 @@ def test_update_stride1_inflation(ctx):
     assert not np.array_equal(got, fields)
 
 
-def test_update_stride3_mask_layers(ctx):
+@pytest.mark.parametrize("precision", [0, 1])
+def test_update_stride3_mask_layers(ctx, precision):
     w = synth.make(2, scale=0.1, nobs=5000, nmem=24)
     w.locrad = 10.0
     out = transforms(ctx, w, mode=0, scheme=0)
@@ -66,7 +67,7 @@ def test_update_stride3_mask_layers(ctx):
     nl = w.numlevels.copy()
     nl[nl > 0] = np.random.default_rng(0).integers(1, w.nlayers + 1, (nl > 0).sum())
     w.numlevels = nl
-    got, ref = run_both(ctx, w, out, fl, levels, inflation=1.1, inf_ratio=0.5)
+    got, ref = run_both(ctx, w, out, fl, levels, inflation=1.1, inf_ratio=0.5, precision=precision)
     assert close(got, ref) < 2e-5
     masked = nl[None, :, :] <= levels[:, None, None]
     assert np.all(got.transpose(1, 0, 2, 3)[:, masked] == 0.0)
@@ -111,7 +112,8 @@ def test_update_periodic_and_tile(ctx):
     assert close(got[0], ref) < 2e-5
 
 
-def test_update_hybrid(ctx):
+@pytest.mark.parametrize("precision", [0, 1])
+def test_update_hybrid(ctx, precision):
     w = synth.make(1, scale=0.5, nmem=24)
     w.nmem_dynamic = 16
     out = transforms(ctx, w, mode=2)
@@ -121,8 +123,20 @@ def test_update_hybrid(ctx):
     assert np.array_equal(hv, rv)
     fields = hv.reshape(1, w.nmem, w.nj, w.ni)
     got, ref = run_both(ctx, w, out, fields, np.array([0]), mode=2, nmem=24, nmem_dynamic=16, inflation=1.02,
-                        inf_ratio=0.3)
+                        inf_ratio=0.3, precision=precision)
     assert close(got, ref) < 2e-5
+
+
+def test_update_large_ensemble_many_layers(ctx):
+    """m = 96 (three members per lane) and more field-layers than one register block."""
+    w = synth.make(3, scale=0.06, nobs=3000, nmem=96)
+    w.nlayers = 10
+    out = transforms(ctx, w)
+    fl = w.fields.reshape(-1, *w.fields.shape[2:])
+    levels = np.tile(np.arange(w.fields.shape[1]), w.fields.shape[0])
+    for precision in (0, 1):
+        got, ref = run_both(ctx, w, out, fl, levels, inflation=1.03, precision=precision)
+        assert close(got, ref) < 2e-5
 
 
 def test_update_enoi_bg_bitexact(ctx):
