@@ -40,6 +40,7 @@ struct UpdArgs {
     size_t plane;               // jsize * mni
     int nk;                     // cells per CTA (tile cell stride)
     int G;                      // strided columns per CTA (version 2 kernel)
+    int fc;                     // field-layers per warp task (version 2 kernel)
 };
 
 // One element of the interpolated X5 for model cell (jt, i) of the tile
@@ -153,7 +154,8 @@ __global__ void __launch_bounds__(UPD_NT) k_update_v2(UpdArgs a)
     float* Tjj = usm;                                                    // [(G+1)][md][TLD]
     float* Wjj = Tjj + (((size_t)(G + 1) * md * TLD + 3) & ~(size_t)3); // [(G+1)][M4]
     float* tile = Wjj + (size_t)(G + 1) * M4;                            // [nf][m][CP]
-    float* Abuf = tile + (((size_t)nf * m * CP + 3) & ~(size_t)3);       // [8 warps][UPD_FC][M4]
+    float* Abuf = tile + (((size_t)nf * m * CP + 3) & ~(size_t)3);       // [8 warps][fcap][M4]
+    const int fcap = a.fc;                                               // rows per task (<= UPD_FC)
 
     // 1. Tjj / wjj for slots 0..gv (slot gv = i-neighbour of the last column)
     {
@@ -194,9 +196,13 @@ __global__ void __launch_bounds__(UPD_NT) k_update_v2(UpdArgs a)
     }
     __syncthreads();
 
-    float* Aw = Abuf + (size_t)wid * UPD_FC * M4;
+    float* Aw = Abuf + (size_t)wid * fcap * M4;
     const int EPL = (md + 31) >> 5;                          // output members per lane
-    for (int c = wid; c < ncell; c += UPD_NT / 32) {
+    // tasks = (cell, block of fcap field-layers), spread over the warps
+    const int nchunk = (nf + fcap - 1) / fcap;
+    for (int task = wid; task < ncell * nchunk; task += UPD_NT / 32) {
+        const int c = task % ncell;
+        const int f0 = (task / ncell) * fcap;
         const int i = i0 + c;
         const int slot = i / st - ii0, stepi = i % st;
         const bool iint = (st > 1 && stepi > 0);
@@ -205,8 +211,8 @@ __global__ void __launch_bounds__(UPD_NT) k_update_v2(UpdArgs a)
         const float* Tb = Tjj + (size_t)(slot + 1) * md * TLD;
         const int nl = a.numlevels[(size_t)jg * a.mni + i];
         const size_t ioff = (size_t)jt * a.mni + i;
-        for (int f0 = 0; f0 < nf; f0 += UPD_FC) {
-            const int fc = min(UPD_FC, nf - f0);
+        {
+            const int fc = min(fcap, nf - f0);
             unsigned active = 0;                              // rows to update
             double mean[UPD_FC];
             // per row: mask, missing values, mean, anomalies (update.c:296-392)
@@ -248,7 +254,10 @@ __global__ void __launch_bounds__(UPD_NT) k_update_v2(UpdArgs a)
                 active |= 1u << q;
             }
             __syncwarp();
-            if (active == 0) continue;
+            if (active == 0) {
+                __syncwarp();
+                continue;
+            }
             // A^a = A^f T on the active rows: acc[q][k] for member lane+32k
             float acc[UPD_FC][MAXE_PER_LANE];
 #pragma unroll
@@ -515,24 +524,30 @@ enkfg_status run_update(enkfg_ctx* ctx, const enkfg_update_params* p, const int*
         set_err(ctx, "nmem = %d too large for the update kernel", a.m);
         return ENKFG_EUNSUPPORTED;
     }
-    // strided columns per CTA and field-layers per launch to fit shared memory
-    const size_t smem_cap = 200 * 1024;
+    // strided columns per CTA, field-layers per warp task and per launch: keep
+    // two CTAs per SM (<= ~100 KB of shared memory each) when possible
+    const size_t smem_cap = 100 * 1024;
     const int M4 = (a.m + 3) & ~3, TLD = a.m + 1;
-    auto need = [&](int G, int nf) {
+    auto need = [&](int G, int nf, int fc) {
         size_t cp = (size_t)G * a.stride;
         return ((((size_t)(G + 1) * a.md * TLD + 3) & ~(size_t)3) + (size_t)(G + 1) * M4 +
-                (((size_t)nf * a.m * cp + 3) & ~(size_t)3) + (size_t)(UPD_NT / 32) * UPD_FC * M4) * sizeof(float);
+                (((size_t)nf * a.m * cp + 3) & ~(size_t)3) + (size_t)(UPD_NT / 32) * fc * M4) * sizeof(float);
     };
-    int G = a.stride >= 32 ? 1 : (32 + a.stride - 1) / a.stride;
+    int G = a.stride >= 16 ? 1 : (16 + a.stride - 1) / a.stride;
     int fg = nfield;
-    while (G > 1 && need(G, fg) > smem_cap) --G;
-    while (fg > 1 && need(G, fg) > smem_cap) fg = (fg + 1) / 2;
+    int fc = UPD_FC;
+    while (G > 1 && need(G, fg, fc) > smem_cap) --G;
+    if (need(G, fg, fc) > smem_cap) fc = 4;
+    while (fg > 1 && need(G, fg, fc) > smem_cap) fg = (fg + 1) / 2;
     if (fg > 448) fg = 448;
-    size_t smem = need(G, fg);
+    // enough warp tasks for the 8 warps of a CTA
+    if ((G * a.stride) * ((fg + fc - 1) / fc) < 16) fc = 4;
+    size_t smem = need(G, fg, fc);
     if (smem > 227 * 1024) {
         set_err(ctx, "update tile does not fit in shared memory (nmem %d)", a.m);
         return ENKFG_EUNSUPPORTED;
     }
+    a.fc = fc;
     const bool f64 = (p->precision == ENKFG_PREC_FP64);
     if (f64) CK(cudaFuncSetAttribute(k_update_v2<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     else CK(cudaFuncSetAttribute(k_update_v2<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));

@@ -3,8 +3,11 @@ cores, FP64 solve) against the FP64 oracle.
 
 Contract: local-observation sets stay bit-exact; X5 (T), w, the analysis
 mean and the analysis spread are within 1e-5 relative of the FP64 oracle
-(max over points of max|a - b| / max|b|; mean and spread relative to the
-field's scale).  The measured errors are written to
+(max over points of max|a - b| / max(max|b|, 1e-4 * max over all points |b|);
+mean and spread relative to the field's scale).  The floor matters only at
+points whose every local observation sits at the edge of the radius: there
+the taper, and with it w, is ~1e-20 in FP64, while the FP32 taper of the
+mixed path rounds it to 0.  The measured errors are written to
 gpurun_out/mixed_errors.json when the directory exists.
 """
 import json
@@ -25,7 +28,7 @@ ERRS = {}
 def per_point(a, b):
     a = a.reshape(a.shape[0] * a.shape[1], -1).astype(np.float64)
     b = b.reshape(b.shape[0] * b.shape[1], -1).astype(np.float64)
-    den = np.maximum(np.abs(b).max(axis=1), 1e-300)
+    den = np.maximum(np.abs(b).max(axis=1), max(1e-4 * np.abs(b).max(), 1e-300))
     r = np.abs(a - b).max(axis=1) / den
     return float(r.max()), float(np.sqrt(np.mean(r ** 2)))
 
