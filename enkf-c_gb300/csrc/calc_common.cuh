@@ -157,7 +157,7 @@ __device__ int enumerate_obs(const CalcArgs& a, int kc, double qx, double qy, do
                         int pos = n0 + before + __popc(bal & ((1u << lane) - 1));
                         s.lid[pos] = (int)p;
                         if (FAST)
-                            llcf[pos] = exact::calclcoeff_f(ti.nlocrad, ti.locrad, ti.locweight, sqrtf((float)d2));
+                            llcf[pos] = exact::calclcoeff_f(ti.nlocrad, ti.locrad, ti.locweight, d2);
                         else
                             s.llc[pos] = exact::calclcoeff(ti.nlocrad, ti.locrad, ti.locweight, __dsqrt_rn(d2));
                     }

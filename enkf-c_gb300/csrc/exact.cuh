@@ -56,27 +56,41 @@ __device__ __forceinline__ double calclcoeff(int nlocrad, const double* locrad, 
     return sum;
 }
 
-// FP32 taper for the mixed-precision path: same pieces, float arithmetic
-// (about 1e-7 relative); the membership test stays exact in FP64.
-__device__ __forceinline__ float taper_gc_f(float x)
+// FP32 taper for the mixed-precision path (about 1e-7 relative everywhere);
+// the membership test stays exact in FP64.  With z = 2 d / r, the outer piece
+// of the Gaspari-Cohn function, multiplied by 12 z, is the polynomial
+// z^6 - 6 z^5 + 7.5 z^4 + 20 z^3 - 60 z^2 + 48 z - 8 = (z - 2)^4 (z^2 + 2 z - 0.5),
+// so for 1 <= z < 2
+//     f = (2 - z)^4 (z^2 + 2 z - 0.5) / (12 z) = (4/3) u^4 (z^2 + 2 z - 0.5) / z,
+// u = 1 - d / r.  Taking u = (r^2 - d^2) / (r (r + d)) with r^2 - d^2 formed in
+// FP64 avoids the cancellation the expanded form suffers in FP32 near the
+// edge of the support.
+__device__ __forceinline__ float taper_gc_f(float u, float z)
 {
-    if (x >= 1.0f) return 0.0f;
-    x *= 2.0f;
-    float x2 = x * x, x3 = x2 * x, f;
-    if (x < 1.0f)
-        f = 1.0f + x2 * (-x3 * 0.25f + x2 * 0.5f) + x3 * 0.625f - x2 * (5.0f / 3.0f);
-    else
-        f = x2 * (x3 * (1.0f / 12.0f) - x2 * 0.5f) + x3 * 0.625f + x2 * (5.0f / 3.0f) - x * 5.0f + 4.0f -
-            (2.0f / 3.0f) / x;
+    if (u <= 0.0f) return 0.0f;
+    float f;
+    if (z < 1.0f) {
+        float z2 = z * z, z3 = z2 * z;
+        f = 1.0f + z2 * (-z3 * 0.25f + z2 * 0.5f) + z3 * 0.625f - z2 * (5.0f / 3.0f);
+    } else {
+        float u2 = u * u;
+        f = (4.0f / 3.0f) * (u2 * u2) * (z * z + 2.0f * z - 0.5f) / z;
+    }
     return f >= 0.0f ? f : 0.0f;
 }
 
-__device__ __forceinline__ float calclcoeff_f(int nlocrad, const double* locrad, const double* locweight, float dist)
+__device__ __forceinline__ float calclcoeff_f(int nlocrad, const double* locrad, const double* locweight, double d2)
 {
+    const float dist = sqrtf((float)d2);
     float sum = 0.0f;
     for (int i = 0; i < nlocrad; ++i) {
-        float r = (float)locrad[i];
-        if (dist <= r) sum += (float)locweight[i] * taper_gc_f(dist / r);
+        const double r = locrad[i];
+        const double e = r * r - d2;
+        if (e < 0.0) continue;
+        const float rf = (float)r;
+        const float u = (float)e / (rf * (rf + dist));
+        const float z = 2.0f * (1.0f - u);
+        sum += (float)locweight[i] * taper_gc_f(u, z);
     }
     return sum;
 }
