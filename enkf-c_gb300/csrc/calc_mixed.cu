@@ -139,6 +139,15 @@ __device__ __forceinline__ void tmem_ld8(uint32_t taddr, float (&v)[8])
     for (int k = 0; k < 8; ++k) v[k] = __uint_as_float(r[k]);
 }
 
+__device__ __forceinline__ void tmem_ld8_nowait(uint32_t taddr, uint32_t (&r)[8])
+{
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
+                 : "r"(taddr));
+}
+
+__device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
+
 __device__ __forceinline__ float to_tf32(float x)
 {
     uint32_t r;
@@ -179,14 +188,40 @@ __device__ __forceinline__ void df_add(float2& a, float x)
     a.y += e;
 }
 
+// HB: 8-column blocks of S'S each thread accumulates (half of the N columns
+// of its TMEM lane), held as double-floats in registers for the whole point.
+template <int HB>
 struct GramProcTC {
     const CalcArgs& a;
     const PointScratch& s;
     MixedShared& ms;
     uint32_t& phase;
     float bhi, blo;    // S's for member threadIdx.x (double-float)
+    float2 acc[HB][8]; // S'S row 32*(warp%4)+lane, columns (warp/4)*half + [0, 8*HB)
     __device__ __forceinline__ GramProcTC(const CalcArgs& a_, const PointScratch& s_, MixedShared& ms_, uint32_t& ph)
-        : a(a_), s(s_), ms(ms_), phase(ph), bhi(0.0f), blo(0.0f) {}
+        : a(a_), s(s_), ms(ms_), phase(ph), bhi(0.0f), blo(0.0f)
+    {
+#pragma unroll
+        for (int b = 0; b < HB; ++b)
+#pragma unroll
+            for (int j = 0; j < 8; ++j) acc[b][j] = make_float2(0.0f, 0.0f);
+    }
+
+    // write the accumulated S'S into the shared double-float matrix
+    __device__ __forceinline__ void store()
+    {
+        const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, m = a.m;
+        const int r = 32 * (wid & 3) + lane;
+        const int half = ms.N >> 1, c0 = (wid >> 2) * half;
+        if (r >= m) return;
+#pragma unroll
+        for (int b = 0; b < HB; ++b)
+#pragma unroll
+            for (int j = 0; j < 8; ++j) {
+                const int c = c0 + 8 * b + j;
+                if (8 * b < half && c < m) ms.Macc[r * ms.lda + c] = acc[b][j];
+            }
+    }
 
     __device__ void chunk(int nc, int t)
     {
@@ -251,29 +286,28 @@ struct GramProcTC {
         tc::fence_after();
         __syncthreads();
         if (*ms.err) return;
-        // 4. accumulators (FP32, TMEM) -> double-float.  Warps w and w+4 share
-        // the TMEM lanes 32*(w%4).., each reading half of the N columns.
+        // 4. accumulators (FP32, TMEM) -> double-float registers.  Warps w and
+        // w+4 share the TMEM lanes 32*(w%4).., each reading half of the N
+        // columns; the loads of all groups are issued before one wait.
         {
-            const int r = 32 * (wid & 3) + lane;
             const int half = ms.N >> 1;
             const int c0 = (wid >> 2) * half;
             const uint32_t lane_addr = ms.taddr + ((uint32_t)(32 * (wid & 3)) << 16);
             const int ngroups = (nc + 7) / 8;
-            for (int cg = c0; cg < c0 + half; cg += 8) {
-                float2 acc[8];
 #pragma unroll
-                for (int j = 0; j < 8; ++j)
-                    acc[j] = (r < m && cg + j < m) ? ms.Macc[r * ms.lda + cg + j] : make_float2(0.f, 0.f);
-                for (int q = 0; q < ngroups; ++q) {
-                    float vv[8];
-                    tc::tmem_ld8(lane_addr + (uint32_t)(q * ms.N + cg), vv);
+            for (int b = 0; b < HB; ++b) {
+                if (8 * b < half) {
+                    uint32_t v[MX_NA][8];
 #pragma unroll
-                    for (int j = 0; j < 8; ++j) df_add(acc[j], vv[j]);
-                }
-                if (r < m) {
+                    for (int q = 0; q < MX_NA; ++q)
+                        tc::tmem_ld8_nowait(lane_addr + (uint32_t)(q * ms.N + c0 + 8 * b), v[q]);
+                    tc::tmem_wait_ld();
 #pragma unroll
-                    for (int j = 0; j < 8; ++j)
-                        if (cg + j < m) ms.Macc[r * ms.lda + cg + j] = acc[j];
+                    for (int q = 0; q < MX_NA; ++q)
+                        if (q < ngroups) {
+#pragma unroll
+                            for (int j = 0; j < 8; ++j) df_add(acc[b][j], __uint_as_float(v[q][j]));
+                        }
                 }
             }
         }
@@ -306,6 +340,7 @@ static size_t mixed_smem_bytes(int m, int kc, bool need_x)
     return s;
 }
 
+template <int HB>
 __global__ void __launch_bounds__(CALC_NT) k_transforms_mixed(CalcArgs a, int kcm, int N, uint32_t tcols)
 {
     extern __shared__ __align__(128) unsigned char smem_raw[];
@@ -368,8 +403,10 @@ __global__ void __launch_bounds__(CALC_NT) k_transforms_mixed(CalcArgs a, int kc
         }
         for (int i = tid; i < m * lda; i += CALC_NT) Macc[i] = 0.0;   // also zero as float2
         __syncthreads();
-        GramProcTC proc(a, s, ms, phase);
+        GramProcTC<HB> proc(a, s, ms, phase);
         const int p = enumerate_obs<true>(a, ms.kc, qx, qy, qz, s, proc, true);
+        proc.store();
+        __syncthreads();
         if (*err) {
             if (tid == 0) a.status[pt] = MX_TIMEOUT_CODE;
             break;
@@ -400,6 +437,28 @@ __global__ void __launch_bounds__(CALC_NT) k_transforms_mixed(CalcArgs a, int kc
     if (wid == 0) tc::tmem_dealloc(*tslot, tcols);
 }
 
+template <int HB>
+static enkfg_status launch_mixed_hb(enkfg_ctx* ctx, CalcArgs& a, int kcm, int N, uint32_t tcols, size_t smem,
+                                    cudaStream_t st)
+{
+    CK(cudaFuncSetAttribute(k_transforms_mixed<HB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    int grid = a.nitems;
+    if (a.persistent) {
+        int per_sm = 0, nsm = 0;
+        CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_transforms_mixed<HB>, CALC_NT, smem));
+        CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, ctx->device));
+        if (per_sm < 1) per_sm = 1;
+        // TMEM: at most 512 columns per SM across resident CTAs
+        while (per_sm > 1 && (uint32_t)per_sm * tcols > 512) --per_sm;
+        grid = per_sm * nsm;
+        if (grid > a.nitems) grid = a.nitems;
+    }
+    if (grid < 1) return ENKFG_OK;
+    k_transforms_mixed<HB><<<grid, CALC_NT, smem, st>>>(a, kcm, N, tcols);
+    CKL();
+    return ENKFG_OK;
+}
+
 enkfg_status launch_mixed(enkfg_ctx* ctx, CalcArgs& a, cudaStream_t st)
 {
     const int m = a.m;
@@ -418,25 +477,10 @@ enkfg_status launch_mixed(enkfg_ctx* ctx, CalcArgs& a, cudaStream_t st)
         set_err(ctx, "mixed path: tile too small for the per-type pass");
         return ENKFG_EUNSUPPORTED;
     }
-    CK(cudaFuncSetAttribute(k_transforms_mixed, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    int grid = a.npts;
-    if (a.persistent) {
-        int per_sm = 0, nsm = 0;
-        CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_transforms_mixed, CALC_NT, smem));
-        CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, ctx->device));
-        if (per_sm < 1) per_sm = 1;
-        // TMEM: at most 512 columns per SM across resident CTAs
-        while (per_sm > 1 && (uint32_t)per_sm * tcols > 512) --per_sm;
-        grid = per_sm * nsm;
-        if (grid > a.nitems) grid = a.nitems;
-    } else {
-        grid = a.nitems;
-        // one CTA per point: limit residency so TMEM allocations never wait
-        // on each other beyond 512 columns (the smem footprint already keeps
-        // residency low; the allocation itself blocks, it does not fail)
-    }
-    if (grid < 1) return ENKFG_OK;
-    k_transforms_mixed<<<grid, CALC_NT, smem, st>>>(a, kcm, N, tcols);
-    CKL();
-    return ENKFG_OK;
+    const int hb = ((N >> 1) + 7) / 8;
+    if (hb <= 2) return launch_mixed_hb<2>(ctx, a, kcm, N, tcols, smem, st);
+    if (hb <= 3) return launch_mixed_hb<3>(ctx, a, kcm, N, tcols, smem, st);
+    if (hb <= 4) return launch_mixed_hb<4>(ctx, a, kcm, N, tcols, smem, st);
+    if (hb <= 6) return launch_mixed_hb<6>(ctx, a, kcm, N, tcols, smem, st);
+    return launch_mixed_hb<8>(ctx, a, kcm, N, tcols, smem, st);
 }
