@@ -96,6 +96,21 @@ class ClockSampler:
                 "reasons": reasons, "samples": len(self.samples)}
 
 
+def aggregate(local_ms: float, local_units: int, world: int, device=None):
+    """Replica aggregation across ranks: the job time is the slowest rank's
+    time (all-reduce MAX), the work is the sum of every rank's units (all-
+    reduce SUM).  Returns (max_ms, total_units).  Single process: identity."""
+    if world <= 1:
+        return local_ms, local_units
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([local_ms], dtype=torch.float64, device=device)
+    u = torch.tensor([float(local_units)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    dist.all_reduce(u, op=dist.ReduceOp.SUM)
+    return float(t.item()), int(round(u.item()))
+
+
 def workload(cfg: int, scale: float):
     import synth
     return synth.make(cfg, scale=scale)
@@ -193,14 +208,11 @@ def run_gpu(args, rank, world, local_rank):
         ev[1].record(stream)
         torch.cuda.synchronize()
     launches = ctx.launches - l0
-    total_ms = ev[0].elapsed_time(ev[1])
+    total_ms, units = aggregate(ev[0].elapsed_time(ev[1]), w.nanalyses * args.steps, world, dev)
     if world > 1:
-        t = torch.tensor([total_ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_ms = float(t.item())
         dist.barrier()
     ms_per_step = total_ms / args.steps
-    value = world * w.nanalyses * args.steps / (total_ms / 1e3)
+    value = units / (total_ms / 1e3)
 
     # dominant-kernel roofline: the transform kernel's FP64 contraction or
     # the update kernel's HBM traffic, whichever takes longer

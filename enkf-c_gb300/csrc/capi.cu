@@ -5,6 +5,10 @@
 #include <math.h>
 
 enkfg_status upload_obs_coords(enkfg_ctx* ctx, const float* lon, const float* lat, cudaStream_t st);
+enkfg_status run_adjoint(enkfg_ctx* ctx, const enkfg_calc_params* p, const double* d_wbar, const double* d_Tbar,
+                         double* d_dinn, double* d_dvar, double* d_drho, cudaStream_t st);
+enkfg_status run_adj_mean(enkfg_ctx* ctx, int m, int md, const float* d_field, const double* d_g, double* d_wbar,
+                          cudaStream_t st);
 enkfg_status upload_query_coords(enkfg_ctx* ctx, const enkfg_grid* g, cudaStream_t st);
 
 void set_err(enkfg_ctx* c, const char* fmt, ...)
@@ -32,6 +36,10 @@ enkfg_status cuda_fail(enkfg_ctx* c, cudaError_t e, const char* what, int line)
     } while (0)
 
 #define SETDEV() CK(cudaSetDevice(ctx->device))
+
+extern "C" {
+static enkfg_status check_calc(enkfg_ctx* ctx, const enkfg_calc_params* p);
+}
 
 static cudaStream_t pick(enkfg_ctx* ctx, void* stream)
 {
@@ -128,6 +136,100 @@ ENKFG_API enkfg_status enkfg_rebuild_index(enkfg_ctx* ctx)
     if (!ctx) return ENKFG_EINVAL;
     ctx->index_valid = false;
     ctx->gather_valid = false;
+    return ENKFG_OK;
+}
+
+ENKFG_API enkfg_status enkfg_adjoint_transforms(enkfg_ctx* ctx, const enkfg_calc_params* p, const double* wbar,
+                                                const double* Tbar, double* dinn, double* dvar, double* drad)
+{
+    if (!ctx) return ENKFG_EINVAL;
+    enkfg_status s = check_calc(ctx, p);
+    if (s) return s;
+    NEED(wbar && dinn && dvar && drad, ENKFG_EINVAL, "wbar and the three outputs are required");
+    SETDEV();
+    cudaStream_t st = ctx->stream;
+    const size_t npts = (size_t)ctx->nj * ctx->ni, m = ctx->nmem, md = ctx->nmem_dyn, n = ctx->nobs > 0 ? ctx->nobs : 1;
+    double *d_wbar = nullptr, *d_Tbar = nullptr, *d_out = nullptr;
+    cudaError_t e = cudaMalloc(&d_wbar, npts * m * sizeof(double));
+    if (e == cudaSuccess && Tbar) e = cudaMalloc(&d_Tbar, npts * md * m * sizeof(double));
+    if (e == cudaSuccess) e = cudaMalloc(&d_out, (2 * n + 1) * sizeof(double));
+    if (e == cudaSuccess) e = cudaMemcpyAsync(d_wbar, wbar, npts * m * sizeof(double), cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess && Tbar)
+        e = cudaMemcpyAsync(d_Tbar, Tbar, npts * md * m * sizeof(double), cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(d_out, 0, (2 * n + 1) * sizeof(double), st);
+    if (e == cudaSuccess) {
+        s = run_adjoint(ctx, p, d_wbar, d_Tbar, d_out, d_out + n, d_out + 2 * n, st);
+        if (!s && ctx->nobs > 0) {
+            cudaMemcpyAsync(dinn, d_out, ctx->nobs * sizeof(double), cudaMemcpyDeviceToHost, st);
+            cudaMemcpyAsync(dvar, d_out + n, ctx->nobs * sizeof(double), cudaMemcpyDeviceToHost, st);
+        }
+        if (!s) cudaMemcpyAsync(drad, d_out + 2 * n, sizeof(double), cudaMemcpyDeviceToHost, st);
+        e = cudaStreamSynchronize(st);
+    } else {
+        cudaGetLastError();
+        s = ENKFG_ENOMEM;
+        set_err(ctx, "adjoint: device allocation failed");
+    }
+    cudaFree(d_wbar);
+    cudaFree(d_Tbar);
+    cudaFree(d_out);
+    if (s) return s;
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "adjoint copy", __LINE__);
+    // dJ/dR -> dJ/d(estd^2): R = estd^2 rfactor
+    if (ctx->nobs > 0) {
+        short* ty = (short*)malloc(ctx->nobs * sizeof(short));
+        if (!ty) return ENKFG_ENOMEM;
+        CK(cudaMemcpy(ty, ctx->d_type, ctx->nobs * sizeof(short), cudaMemcpyDeviceToHost));
+        for (int o = 0; o < ctx->nobs; ++o) dvar[o] *= ctx->rfactor[ty[o]];
+        free(ty);
+    }
+    // per-point failures
+    int* h = (int*)malloc(npts * sizeof(int));
+    if (!h) return ENKFG_ENOMEM;
+    CK(cudaMemcpy(h, ctx->d_status_pt, npts * sizeof(int), cudaMemcpyDeviceToHost));
+    for (size_t k = 0; k < npts; ++k)
+        if (h[k]) {
+            set_err(ctx, "adjoint: eigendecomposition failed at point %zu", k);
+            free(h);
+            return ENKFG_ENUMERIC;
+        }
+    free(h);
+    return ENKFG_OK;
+}
+
+ENKFG_API enkfg_status enkfg_adjoint_mean(enkfg_ctx* ctx, int nmem, int nmem_dynamic, const float* field,
+                                          const double* dJ_dmean, double* wbar)
+{
+    if (!ctx) return ENKFG_EINVAL;
+    NEED(ctx->grid_set, ENKFG_ESTATE, "the grid must be set");
+    NEED(field && dJ_dmean && wbar && nmem >= 2 && nmem_dynamic >= 1 && nmem_dynamic <= nmem, ENKFG_EINVAL,
+         "bad arguments");
+    SETDEV();
+    cudaStream_t st = ctx->stream;
+    const size_t cells = (size_t)ctx->mni * ctx->mnj, npts = (size_t)ctx->nj * ctx->ni;
+    float* d_f = nullptr;
+    double *d_g = nullptr, *d_w = nullptr;
+    cudaError_t e = cudaMalloc(&d_f, (size_t)nmem * cells * sizeof(float));
+    if (e == cudaSuccess) e = cudaMalloc(&d_g, cells * sizeof(double));
+    if (e == cudaSuccess) e = cudaMalloc(&d_w, npts * nmem * sizeof(double));
+    enkfg_status s = ENKFG_OK;
+    if (e == cudaSuccess) {
+        cudaMemcpyAsync(d_f, field, (size_t)nmem * cells * sizeof(float), cudaMemcpyHostToDevice, st);
+        cudaMemcpyAsync(d_g, dJ_dmean, cells * sizeof(double), cudaMemcpyHostToDevice, st);
+        cudaMemsetAsync(d_w, 0, npts * nmem * sizeof(double), st);
+        s = run_adj_mean(ctx, nmem, nmem_dynamic, d_f, d_g, d_w, st);
+        if (!s) cudaMemcpyAsync(wbar, d_w, npts * nmem * sizeof(double), cudaMemcpyDeviceToHost, st);
+        e = cudaStreamSynchronize(st);
+    } else {
+        cudaGetLastError();
+        s = ENKFG_ENOMEM;
+        set_err(ctx, "adjoint_mean: device allocation failed");
+    }
+    cudaFree(d_f);
+    cudaFree(d_g);
+    cudaFree(d_w);
+    if (s) return s;
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "adjoint_mean", __LINE__);
     return ENKFG_OK;
 }
 

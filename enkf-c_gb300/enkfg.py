@@ -45,7 +45,7 @@ EXPORTS = ["enkfg_create", "enkfg_destroy", "enkfg_last_error", "enkfg_status_st
            "enkfg_set_transforms", "enkfg_update_fields", "enkfg_update_fields_dev", "enkfg_set_hybrid_ensemble",
            "enkfg_set_hybrid_ensemble_dev", "enkfg_kernel_launches", "enkfg_stage_times", "enkfg_set_stream",
            "enkfg_set_HE_dev", "enkfg_rebuild_index", "enkfg_local_offsets_noalloc", "enkfg_autotune_table",
-           "enkfg_autotune_reset"]
+           "enkfg_autotune_reset", "enkfg_adjoint_transforms", "enkfg_adjoint_mean"]
 
 
 class EnkfgError(RuntimeError):
@@ -296,6 +296,30 @@ class Enkfg:
         T = None if T is None else np.ascontiguousarray(T, np.float32)
         self._ck(self.L.enkfg_set_transforms(self.h, C.c_int(mode), C.c_int(m), C.c_int(md), _p(T, C.c_float),
                                              _p(w, C.c_float)))
+
+    # ---- adjoint (observation impact) -----------------------------------
+    def adjoint_transforms(self, wbar, Tbar=None, mode=MODE_ENKF, scheme=SCHEME_ETKF, alpha=1.0):
+        """dJ/d(innovation) [nobs], dJ/d(estd^2) [nobs], dJ/d(radius scale)."""
+        wbar = np.ascontiguousarray(wbar, np.float64)
+        Tbar = None if Tbar is None else np.ascontiguousarray(Tbar, np.float64)
+        dinn = np.zeros(self.nobs)
+        dvar = np.zeros(self.nobs)
+        drad = np.zeros(1)
+        prm = CalcParams(mode, scheme, float(alpha), PATH_PLAIN, PREC_FP64, 0, 0)
+        self._ck(self.L.enkfg_adjoint_transforms(self.h, C.byref(prm), _p(wbar, C.c_double), _p(Tbar, C.c_double),
+                                                 _p(dinn, C.c_double), _p(dvar, C.c_double), _p(drad, C.c_double)))
+        return dinn, dvar, float(drad[0])
+
+    def adjoint_mean(self, field, dJ_dmean, nmem=None, nmem_dynamic=None):
+        """wbar [nj][ni][m] from the forecast field [m][mnj][mni] and dJ/dmean [mnj][mni]."""
+        field = np.ascontiguousarray(field, np.float32)
+        g = np.ascontiguousarray(dJ_dmean, np.float64)
+        m = field.shape[0] if nmem is None else nmem
+        md = m if nmem_dynamic is None else nmem_dynamic
+        wbar = np.zeros((self.nj, self.ni, m))
+        self._ck(self.L.enkfg_adjoint_mean(self.h, C.c_int(m), C.c_int(md), _p(field, C.c_float), _p(g, C.c_double),
+                                           _p(wbar, C.c_double)))
+        return wbar
 
     # ---- update ----------------------------------------------------------
     def updatefields(self, fields, numlevels, levels, *, mode=MODE_ENKF, nmem=None, nmem_dynamic=None, surfk=0,

@@ -198,6 +198,26 @@ ENKFG_API enkfg_status enkfg_set_HE_dev(enkfg_ctx* ctx, int nmem, int nmem_dynam
  * (obs_createkdtrees is part of every enkf_calc run, observations.c:1616). */
 ENKFG_API enkfg_status enkfg_rebuild_index(enkfg_ctx* ctx);
 
+/* Observation impact: adjoint of the local analysis (no counterpart in the
+ * reference; it differentiates das_calctransforms, transforms.c:1150-1360).
+ * Given wbar = dJ/dw [nj][ni][m] (and optionally Tbar = dJ/dT
+ * [nj][ni][m_dyn][m], NULL if J does not depend on T) for the transforms of
+ * the current inputs, computes, in FP64,
+ *   dJ_dinnovation [nobs]  dJ/d(y - Hx) per observation,
+ *   dJ_dvariance   [nobs]  dJ/d(estd^2) per observation,
+ *   dJ_dradius     [1]     dJ/d(rho), rho a common scale of all LOCRAD
+ *                          values (dJ/dr = dJ/drho / r for one radius).
+ * Each point's eigendecomposition is recomputed; the T term uses the
+ * Daleckii-Krein form.  nmem <= 96. */
+ENKFG_API enkfg_status enkfg_adjoint_transforms(enkfg_ctx* ctx, const enkfg_calc_params* p, const double* wbar, const double* Tbar, double* dJ_dinnovation, double* dJ_dvariance, double* dJ_dradius);
+
+/* Adjoint of the analysis-mean update of one field-layer (update.c:380-410)
+ * and of the stride interpolation of w (update.c:195-272): field [nmem]
+ * [mnj][mni] is the forecast ensemble, dJ_dmean [mnj][mni] the gradient with
+ * respect to the analysis mean (0 on masked cells); wbar [nj][ni][m]
+ * receives dJ/dw at the strided points. */
+ENKFG_API enkfg_status enkfg_adjoint_mean(enkfg_ctx* ctx, int nmem, int nmem_dynamic, const float* field, const double* dJ_dmean, double* wbar);
+
 /* The chunk sizes (observations per contraction step) the autotuner chose
  * per local-obs count bin (bin b holds counts in [2^b - 1, 2^(b+1) - 1));
  * table[16].  Returns ENKFG_ESTATE before the first tuned batched call. */
