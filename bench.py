@@ -195,7 +195,7 @@ def run_gpu(args, rank, world, local_rank):
         import torch.distributed as dist
         dist.barrier()
     torch.cuda.synchronize()
-    calc_ms, upd_ms = [], []
+    calc_ms, upd_ms, kern_ms, ukern_ms = [], [], [], []
     l0 = ctx.launches
     with ClockSampler(local_rank) as clk:
         ev[0].record(stream)
@@ -205,33 +205,97 @@ def run_gpu(args, rank, world, local_rank):
             stream.synchronize()
             calc_ms.append(parts[0].elapsed_time(parts[1]))
             upd_ms.append(parts[1].elapsed_time(parts[2]))
+            # the library's CUDA events on the launching stream: [2] the
+            # transform kernel alone, [3] the update kernel(s)
+            st_ms = ctx.stage_times()
+            kern_ms.append(st_ms[2])
+            ukern_ms.append(st_ms[3])
         ev[1].record(stream)
         torch.cuda.synchronize()
     launches = ctx.launches - l0
     total_ms, units = aggregate(ev[0].elapsed_time(ev[1]), w.nanalyses * args.steps, world, dev)
+
+    # the same cycle replayed from a CUDA graph: everything after the index
+    # build (HE copy, innovations, standardisation, gather, transforms,
+    # update) captured once on the context's stream; the index build (host
+    # round trips for the bucket grid) stays eager before each replay
+    graph = None
+    if args.graph:
+        def cycle():
+            ctx.set_HE_dev(HE_d.data_ptr(), m, w.nmem_dynamic)
+            ctx.calcinnandspread(want=False)
+            ctx.standardise()
+            ctx.calctransforms_dev(mode=w.mode, scheme=w.scheme, alpha=w.alpha, path=path, precision=prec)
+            ctx.updatefields_dev(fields_d.data_ptr(), numlev_d.data_ptr(), nfl, levels, mode=w.mode, nmem=m,
+                                 nmem_dynamic=w.nmem_dynamic, inflation=w.inflation, inf_ratio=w.inf_ratio,
+                                 precision=prec)
+        try:
+            g = torch.cuda.CUDAGraph()
+            with torch.cuda.stream(stream):
+                ctx.rebuild_index()
+            stream.synchronize()
+            with torch.cuda.graph(g, stream=stream):
+                cycle()
+            gl0 = ctx.launches
+            for _ in range(args.warmup):
+                with torch.cuda.stream(stream):
+                    flush.zero_()
+                    ctx.rebuild_index()
+                    g.replay()
+            torch.cuda.synchronize()
+            ge = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+            ge[0].record(stream)
+            for _ in range(args.steps):
+                with torch.cuda.stream(stream):
+                    flush.zero_()
+                    ctx.rebuild_index()
+                    g.replay()
+            ge[1].record(stream)
+            torch.cuda.synchronize()
+            gms, gunits = aggregate(ge[0].elapsed_time(ge[1]), w.nanalyses * args.steps, world, dev)
+            graph = {"value": gunits / (gms / 1e3), "ms_per_step": gms / args.steps,
+                     "captured": "HE copy, innovations, standardisation, gather, transforms, update",
+                     "eager": "index build"}
+            del g
+        except Exception as exc:   # report, do not hide: the eager numbers stand
+            graph = {"error": str(exc)[:300]}
     if world > 1:
         dist.barrier()
     ms_per_step = total_ms / args.steps
     value = units / (total_ms / 1e3)
 
-    # dominant-kernel roofline: the transform kernel's FP64 contraction or
-    # the update kernel's HBM traffic, whichever takes longer
+    # rooflines.  Transform kernel (the dominant one): algorithmic FLOPs =
+    # sum over points of 2 m^2 p + 2 m p (S'S as a full m x m product and
+    # S's), over the kernel's own CUDA-event time.  FP64 path: against the
+    # nominal FP64 rate (FP64 is not among the measured peaks).  Mixed path:
+    # S'S runs as three TF32 products on the tensor cores, so the peak is the
+    # measured bf16 rate / 2 (TF32) / 3 (split products).  Update kernel:
+    # fields read + written and X5 read once, over its CUDA-event time,
+    # against the measured HBM copy bandwidth.
     peaks, peak_src = load_peaks()
     calc_t = statistics.median(calc_ms) / 1e3
     upd_t = statistics.median(upd_ms) / 1e3
+    kern_t = statistics.median(kern_ms) / 1e3
+    ukern_t = statistics.median(ukern_ms) / 1e3
     ub, _, _ = update_bytes(w, nfl)
     counts = ctx.findlocal(lists=False).astype(np.float64)
     flops = float((2.0 * m * m * counts + 2.0 * m * counts).sum())
-    if upd_t >= calc_t:
-        roof = {"kernel": "k_update_fields", "bound": "hbm", "achieved": ub / upd_t / 1e9,
-                "peak": peaks["hbm_gbs"], "unit": "GB/s", "peak_source": peak_src}
+    kname = "k_transforms_mixed" if prec == enkfg.PREC_MIXED else "k_transforms"
+    if prec == enkfg.PREC_MIXED:
+        roof = {"kernel": kname, "bound": "tensor", "achieved": flops / kern_t / 1e12,
+                "peak": peaks["bf16_tflops"] / 2.0 / 3.0, "unit": "TFLOP/s",
+                "peak_source": f"{peak_src} bf16 {peaks['bf16_tflops']} / 2 (TF32) / 3 (split products)"}
     else:
-        fp64_peak = 1250.0
-        roof = {"kernel": "k_transforms (calc stage)", "bound": "fp64", "achieved": flops / calc_t / 1e9,
-                "peak": fp64_peak, "unit": "GFLOP/s",
-                "peak_source": "GB300 nominal FP64 (not in MEASURED_PEAKS.json)"}
+        roof = {"kernel": kname, "bound": "fp64", "achieved": flops / kern_t / 1e12, "peak": 1.25,
+                "unit": "TFLOP/s", "peak_source": "GB300 nominal FP64 (FP64 is not among the measured peaks)"}
     roof["frac"] = roof["achieved"] / roof["peak"]
     roof["traffic"] = None
+    roof["kernel_ms"] = kern_t * 1e3
+    roof["flops_per_launch"] = flops
+    uroof = {"kernel": "k_update_cells" if m <= 64 else "k_update_v2", "bound": "hbm",
+             "achieved": ub / ukern_t / 1e9, "peak": peaks["hbm_gbs"], "unit": "GB/s",
+             "frac": ub / ukern_t / 1e9 / peaks["hbm_gbs"], "bytes_per_launch": ub, "kernel_ms": ukern_t * 1e3,
+             "peak_source": peak_src}
 
     # end to end through the host-buffer C ABI (pinned host memory)
     e2e = None
@@ -286,7 +350,8 @@ def run_gpu(args, rank, world, local_rank):
             "stages_ms": {"calc": statistics.median(calc_ms), "update": statistics.median(upd_ms)},
             "update_gbs": ub / upd_t / 1e9,
             "calc_gflops_fp64": flops / calc_t / 1e9,
-            "roofline": roof, "e2e": e2e, "cpu_baseline": cpu, "gpu_launches": int(launches),
+            "roofline": roof, "roofline_update": uroof, "graph": graph, "e2e": e2e, "cpu_baseline": cpu,
+            "gpu_launches": int(launches),
             "clocks": clk.summary(),
         }
         print(json.dumps(line))
@@ -395,6 +460,7 @@ def main():
     ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
     ap.add_argument("--cpu-rows", type=int, default=24)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--graph", type=int, default=1, help="also time the cycle replayed from a CUDA graph")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))

@@ -218,7 +218,7 @@ __global__ void __launch_bounds__(CALC_NT) k_adjoint(AdjArgs A)
     }
     // 1. forward recomputation: M, b, eigendecomposition, w
     GramProcAdj<R> gp(a, s, tile, sloc);
-    const int p = enumerate_obs<false>(a, a.kc, qx, qy, qz, s, gp, true);
+    const int p = enumerate_obs<0>(a, a.kc, qx, qy, qz, s, gp, true);
     if (p == 0) return;
     if (tx >= ty)
 #pragma unroll
@@ -353,7 +353,7 @@ __global__ void __launch_bounds__(CALC_NT) k_adjoint(AdjArgs A)
     // 3. per-observation sensitivities (second pass over the local obs; the
     //    chunks are staged in the tile region, P stays in W)
     AdjProc ap(A, s, tile, lam, w, Pp, LDA, MP, qx, qy, qz);
-    enumerate_obs<false>(a, a.kc, qx, qy, qz, s, ap, false);
+    enumerate_obs<0>(a, a.kc, qx, qy, qz, s, ap, false);
     double rs = la::block_sum<CALC_NT>(ap.rho_acc, red);
     if (tid == 0 && rs != 0.0) atomicAdd(A.drho, rs);
 }
@@ -450,12 +450,9 @@ enkfg_status run_adjoint(enkfg_ctx* ctx, const enkfg_calc_params* p, const doubl
     double *sig, *R;
     CK(cudaMalloc(&sig, (size_t)(ctx->nsorted > 0 ? ctx->nsorted : 1) * sizeof(double)));
     CK(cudaMalloc(&R, (size_t)(ctx->nsorted > 0 ? ctx->nsorted : 1) * sizeof(double)));
-    double sr[ENKFG_MAXTYPES];
-    for (int t = 0; t < ctx->ntypes; ++t) sr[t] = sqrt(ctx->rfactor[t]);
-    CK(cudaMemcpyAsync(ctx->d_rfac, sr, ctx->ntypes * sizeof(double), cudaMemcpyHostToDevice, st));
     if (ctx->nsorted > 0) {
         k_adj_sorted<<<div_up(ctx->nsorted, 256), 256, 0, st>>>(ctx->nsorted, ctx->d_sid, ctx->d_estd, ctx->d_type,
-                                                               ctx->d_rfac, sqrt((double)m - 1), sig, R);
+                                                               ctx->d_rfac_sqrt, sqrt((double)m - 1), sig, R);
         CKL();
     }
     AdjArgs A;

@@ -34,14 +34,13 @@ struct CalcSmem {
     static constexpr int MP = 16 * R;       // padded member count
     static constexpr int TLD = MP;          // tile row stride (doubles)
     static constexpr int LDA = MP + 1;      // matrix row stride (doubles)
-    static size_t bytes(int need_x)
+    static size_t bytes()
     {
         size_t s = 0;
         s += (size_t)KC_MAX * TLD * 8;                 // tile
         s += (size_t)LIST_EXTRA * 8;                   // list taper
         s += (size_t)KC_MAX * 8;                       // sloc
         s += (size_t)MP * LDA * 8;                     // A
-        if (need_x) s += (size_t)MP * LDA * 8;         // X (Cholesky inverse)
         s += (size_t)6 * MP * 8;                       // b d e cs sn v
         s += (size_t)ENKFG_MAXTYPES * 8 * 2;           // per-type ss, pdfs
         s += (size_t)(CALC_NT / 32) * 8;               // red
@@ -116,14 +115,11 @@ __global__ void __launch_bounds__(CALC_NT) k_transforms(CalcArgs a)
     constexpr int MP = 16 * R, TLD = MP, LDA = MP + 1;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
-    const bool need_x = (a.mode == ENKFG_MODE_ENOI || a.scheme == ENKFG_SCHEME_DENKF);
     unsigned char* sp = smem_raw;
     double* tile = (double*)sp;       sp += (size_t)KC_MAX * TLD * 8;
     double* llc = (double*)sp;        sp += (size_t)LIST_EXTRA * 8;
     double* sloc = (double*)sp;       sp += (size_t)KC_MAX * 8;
     double* A = (double*)sp;          sp += (size_t)MP * LDA * 8;
-    double* X = nullptr;
-    if (need_x) { X = (double*)sp;    sp += (size_t)MP * LDA * 8; }
     double* b = (double*)sp;          sp += MP * 8;
     double* d = (double*)sp;          sp += MP * 8;
     double* e = (double*)sp;          sp += MP * 8;
@@ -153,7 +149,7 @@ __global__ void __launch_bounds__(CALC_NT) k_transforms(CalcArgs a)
         }
         __syncthreads();
         GramProc64<R> proc(a, s, tile, sloc);
-        const int p = enumerate_obs<false>(a, kc, qx, qy, qz, s, proc, true);
+        const int p = enumerate_obs<0>(a, kc, qx, qy, qz, s, proc, true);
         if (p == 0) {
             store_empty(a, pt);
             __syncthreads();
@@ -177,7 +173,7 @@ __global__ void __launch_bounds__(CALC_NT) k_transforms(CalcArgs a)
         const double trss = la::block_sum<CALC_NT>(tid < m ? A[tid * LDA + tid] : 0.0, red);
         if (tid < m) A[tid * LDA + tid] += 1.0;
         __syncthreads();
-        solve_point(a, pt, p, kc, qx, qy, qz, A, X, LDA, b, trss, d, e, cs, sn, v, s, tile, TLD);
+        solve_point(a, pt, p, kc, qx, qy, qz, A, LDA, b, trss, d, e, cs, sn, v, s, tile, TLD);
     }
 }
 
@@ -255,8 +251,7 @@ enkfg_status build_queue(enkfg_ctx* ctx, int npts, cudaStream_t st)
 template <int R>
 static enkfg_status launch_R(enkfg_ctx* ctx, CalcArgs& a, cudaStream_t st)
 {
-    bool need_x = (a.mode == ENKFG_MODE_ENOI || a.scheme == ENKFG_SCHEME_DENKF);
-    size_t smem = CalcSmem<R>::bytes(need_x);
+    size_t smem = CalcSmem<R>::bytes();
     if (smem > 227 * 1024) {
         set_err(ctx, "nmem = %d needs %zu bytes of shared memory for this scheme", a.m, smem);
         return ENKFG_EUNSUPPORTED;
@@ -364,6 +359,7 @@ static enkfg_status autotune(enkfg_ctx* ctx, CalcArgs a, int precision, cudaStre
     CK(cudaStreamSynchronize(st));
     memcpy(ctx->kc_table, table, sizeof(table));
     ctx->kc_tuned = true;
+    ctx->kc_loaded = 3;
     ctx->kc_tuned_prec = precision;
     return ENKFG_OK;
 }
@@ -391,8 +387,9 @@ enkfg_status run_transforms(enkfg_ctx* ctx, const enkfg_calc_params* p, cudaStre
     size_t nT = enkf ? (size_t)npts * md * m : 1;
     if ((s = ensure(ctx, &ctx->d_T, &ctx->T_cap, nT))) return s;
     if ((s = ensure(ctx, &ctx->d_w, &ctx->w_cap, (size_t)npts * m))) return s;
-    if ((s = ensure(ctx, &ctx->d_T64, &ctx->T64_cap, nT))) return s;
-    if ((s = ensure(ctx, &ctx->d_w64, &ctx->w64_cap, (size_t)npts * m))) return s;
+    const bool w64 = ctx->want64;
+    if (w64 && (s = ensure(ctx, &ctx->d_T64, &ctx->T64_cap, nT))) return s;
+    if (w64 && (s = ensure(ctx, &ctx->d_w64, &ctx->w64_cap, (size_t)npts * m))) return s;
     if ((s = ensure(ctx, &ctx->d_nlobs, &ctx->nlobs_cap, (size_t)npts))) return s;
     if ((s = ensure(ctx, &ctx->d_dfs, &ctx->dfs_cap, (size_t)npts))) return s;
     if ((s = ensure(ctx, &ctx->d_srf, &ctx->srf_cap, (size_t)npts))) return s;
@@ -421,9 +418,12 @@ enkfg_status run_transforms(enkfg_ctx* ctx, const enkfg_calc_params* p, cudaStre
     a.types = ctx->d_types;
     a.bstart = ctx->d_bstart;
     a.sx = ctx->d_sx;
+    a.sxf = ctx->d_sxf;
+    a.syf = ctx->d_syf;
     a.sy = ctx->d_sy;
     a.sz = ctx->d_sz;
     a.St = ctx->d_St;
+    a.qscale = ctx->d_qscale;
     a.mpad = ctx->mpad;
     a.ss = ctx->d_ss;
     a.qx = ctx->d_qx;
@@ -431,8 +431,8 @@ enkfg_status run_transforms(enkfg_ctx* ctx, const enkfg_calc_params* p, cudaStre
     a.qz = ctx->d_qz;
     a.T = enkf ? ctx->d_T : nullptr;
     a.w = ctx->d_w;
-    a.T64 = enkf ? ctx->d_T64 : nullptr;
-    a.w64 = ctx->d_w64;
+    a.T64 = (enkf && w64) ? ctx->d_T64 : nullptr;
+    a.w64 = w64 ? ctx->d_w64 : nullptr;
     a.nlobs = ctx->d_nlobs;
     a.dfs = ctx->d_dfs;
     a.srf = ctx->d_srf;
@@ -450,14 +450,16 @@ enkfg_status run_transforms(enkfg_ctx* ctx, const enkfg_calc_params* p, cudaStre
         a.qhead = ctx->d_qhead;
         a.counts = ctx->d_counts;
         a.kc_table = ctx->d_qhead + 2 + NBINS;   // chunk size per count bin (autotuned)
-        if (ctx->kc_tuned && ctx->kc_tuned_prec == p->precision) {
-            CK(cudaMemcpyAsync(ctx->d_qhead + 2 + NBINS, ctx->kc_table, sizeof(ctx->kc_table), cudaMemcpyHostToDevice,
-                               st));
-        } else {
+        // the chunk-size table goes to the device only when it changes (no
+        // host-to-device copy in a steady cycle, which CUDA graphs capture)
+        const int want = (ctx->kc_tuned && ctx->kc_tuned_prec == p->precision) ? 3
+                         : (p->precision == ENKFG_PREC_MIXED ? 2 : 1);
+        if (ctx->kc_loaded != want) {
             static const int kc_default[NBINS] = { 8, 8, 8, 8, 16, 16, 32, 32, 32, 64, 64, 64, 64, 64, 64, 64 };
             static const int kc_mixed[NBINS] = { 8, 8, 8, 8, 16, 16, 24, 32, 32, 32, 32, 32, 32, 32, 32, 32 };
-            CK(cudaMemcpyAsync(ctx->d_qhead + 2 + NBINS, p->precision == ENKFG_PREC_MIXED ? kc_mixed : kc_default,
-                               sizeof(kc_default), cudaMemcpyHostToDevice, st));
+            const int* tab = want == 3 ? ctx->kc_table : (want == 2 ? kc_mixed : kc_default);
+            CK(cudaMemcpy(ctx->d_qhead + 2 + NBINS, tab, sizeof(kc_default), cudaMemcpyHostToDevice));
+            ctx->kc_loaded = want;
         }
         CK(cudaMemsetAsync(ctx->d_qhead, 0, sizeof(int), st));
     }

@@ -22,7 +22,10 @@ struct CalcArgs {
     const double* sx;
     const double* sy;
     const double* sz;
+    const float* sxf;  // FP32 coordinate copies (2-D; null: FP64 search only)
+    const float* syf;
     const float* St;
+    const float* qscale;   // [2][ENKFG_MAXMEM] mixed path: per-member quantum q and 1/q
     int mpad;
     const double* ss;
     const double* qx;
@@ -115,10 +118,23 @@ struct PointScratch {
 // local observations; per-type counts go to s.tcount if count_types.
 // FAST: taper coefficients in FP32, stored as floats in s.llc (mixed path);
 // otherwise exact FP64 coefficients (bit-identical to the reference's).
-template <bool FAST, class Proc>
+// The exact FP64 membership test for the few candidates whose FP32 squared
+// distance falls inside the undecided band.  Not inlined, so that its FP64
+// instructions stay off the common path (an if-converted FP64 block issues
+// on the 1/64-rate FP64 pipe even for predicated-off lanes).
+static __device__ __noinline__ bool exact_in2(double ox, double oy, double qx, double qy, double r2)
+{
+    return exact::dist2(ox, oy, qx, qy) <= r2;
+}
+
+// SEARCH: 0 exact FP64 distance and FP64 taper (bit-exact coefficients);
+// 1 FP64 distance, FP32 taper; 2 FP32 distance with the exact FP64 test only
+// inside the undecided band, FP32 taper from the double-float distance (2-D).
+template <int SEARCH, class Proc>
 __device__ int enumerate_obs(const CalcArgs& a, int kc, double qx, double qy, double qz, const PointScratch& s,
                              Proc& proc, bool count_types)
 {
+    constexpr bool FAST = SEARCH > 0;
     float* llcf = reinterpret_cast<float*>(s.llc);
     const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
     int* wsum = s.ictl + 8;
@@ -129,6 +145,11 @@ __device__ int enumerate_obs(const CalcArgs& a, int kc, double qx, double qy, do
         if (ti.pos_end > ti.pos_begin) {
             long long bk[27];
             int nb = calc_neighbours(ti, a.ndim, qx, qy, qz, bk);
+            // FP32 pre-test (SEARCH 2): the query split into hi + lo floats;
+            // candidates inside the band [rmax2_lo, rmax2_hi] take the exact
+            // FP64 test, which keeps the neighbour sets bit-exact
+            const float qxh = (float)qx, qyh = (float)qy;
+            const float qxl = (float)(qx - (double)qxh), qyl = (float)(qy - (double)qyh);
             if (tid == 0) s.ictl[0] = 0;
             __syncthreads();
             for (int k = 0; k < nb; ++k) {
@@ -137,10 +158,22 @@ __device__ int enumerate_obs(const CalcArgs& a, int kc, double qx, double qy, do
                     long long p = base + tid;
                     bool in = false;
                     double d2 = 0.0;
-                    if (p < b1) {
-                        d2 = a.ndim == 2 ? exact::dist2(a.sx[p], a.sy[p], qx, qy)
-                                         : exact::dist3(a.sx[p], a.sy[p], a.sz[p], qx, qy, qz);
-                        in = d2 <= ti.rmax2;
+                    float d2f = 0.0f, d2l = 0.0f;
+                    if constexpr (SEARCH == 2) {
+                        bool band = false;
+                        if (p < b1) {
+                            exact::dist2_df(a.sxf[p], a.syf[p], qxh, qxl, qyh, qyl, d2f, d2l);
+                            in = d2f <= ti.rmax2_lo;
+                            band = !in && d2f <= ti.rmax2_hi;
+                        }
+                        if (__any_sync(0xffffffffu, band))
+                            if (band) in = exact_in2(a.sx[p], a.sy[p], qx, qy, ti.rmax2);
+                    } else {
+                        if (p < b1) {
+                            d2 = a.ndim == 2 ? exact::dist2(a.sx[p], a.sy[p], qx, qy)
+                                             : exact::dist3(a.sx[p], a.sy[p], a.sz[p], qx, qy, qz);
+                            in = d2 <= ti.rmax2;
+                        }
                     }
                     unsigned bal = __ballot_sync(0xffffffffu, in);
                     if (lane == 0) wsum[wid] = __popc(bal);
@@ -156,7 +189,9 @@ __device__ int enumerate_obs(const CalcArgs& a, int kc, double qx, double qy, do
                     if (in) {
                         int pos = n0 + before + __popc(bal & ((1u << lane) - 1));
                         s.lid[pos] = (int)p;
-                        if (FAST)
+                        if constexpr (SEARCH == 2)
+                            llcf[pos] = exact::calclcoeff_df(ti, d2f, d2l);
+                        else if constexpr (SEARCH == 1)
                             llcf[pos] = exact::calclcoeff_f(ti.nlocrad, ti.locrad, ti.locweight, d2);
                         else
                             s.llc[pos] = exact::calclcoeff(ti.nlocrad, ti.locrad, ti.locweight, __dsqrt_rn(d2));
@@ -172,13 +207,13 @@ __device__ int enumerate_obs(const CalcArgs& a, int kc, double qx, double qy, do
                         float lcf = 0.0f;
                         if (tid < rest) {
                             id = s.lid[kc + tid];
-                            if (FAST) lcf = llcf[kc + tid];
+                            if constexpr (FAST) lcf = llcf[kc + tid];
                             else lc = s.llc[kc + tid];
                         }
                         __syncthreads();
                         if (tid < rest) {
                             s.lid[tid] = id;
-                            if (FAST) llcf[tid] = lcf;
+                            if constexpr (FAST) llcf[tid] = lcf;
                             else s.llc[tid] = lc;
                         }
                         __syncthreads();
@@ -268,20 +303,21 @@ __device__ inline void store_empty(const CalcArgs& a, int pt)
 }
 
 // FP64 solve of one point from M = I + S'S in A (n = m, stride lda) and b =
-// S's, then relaxation, float cast and diagnostics.  X: second m x lda
-// buffer (Cholesky path); tile/tld: FP64 chunk buffer for the per-type pass.
+// S's, then relaxation, float cast and diagnostics.  A is overwritten (by the
+// eigenvectors, or by M^-1); tile/tld: FP64 chunk buffer for the per-type
+// pass.
 __device__ inline void solve_point(const CalcArgs& a, int pt, int p, int kc, double qx, double qy, double qz,
-                                   double* A, double* X, int lda, double* b, double trss, double* d, double* e,
+                                   double* A, int lda, double* b, double trss, double* d, double* e,
                                    double* cs, double* sn, double* v, const PointScratch& s, double* tile, int tld)
 {
     const int tid = threadIdx.x, m = a.m, md = a.md;
-    const bool need_x = (a.mode == ENKFG_MODE_ENOI || a.scheme == ENKFG_SCHEME_DENKF);
+    const bool need_inv = (a.mode == ENKFG_MODE_ENOI || a.scheme == ENKFG_SCHEME_DENKF);
     const size_t tbase = (size_t)pt * md * m;
     int rc = 0;
     double dfs = 0.0;
     const double* Q;
     const double* gq;
-    if (!need_x) {
+    if (!need_inv) {
         // ETKF (calcs.c:300-412): T = M^-1/2, w = M^-1 S's
         rc = la::eig_sym<CALC_NT>(A, m, lda, d, e, cs, sn, s.ictl + 16, s.red);
         if (tid < m) {
@@ -316,19 +352,19 @@ __device__ inline void solve_point(const CalcArgs& a, int pt, int p, int kc, dou
         Q = A;
         gq = sn;
     } else {
-        // DEnKF (calcs.c:279-284) / EnOI: M^-1 by Cholesky
-        rc = la::chol_inverse<CALC_NT>(A, X, m, lda, s.ictl + 16);
+        // DEnKF (calcs.c:279-284) / EnOI: M^-1 in place (symmetric sweep)
+        rc = la::spd_inverse<CALC_NT>(A, m, lda, cs, sn, d, s.ictl + 16);
         if (tid < m) {
             double wv = 0.0;
-            for (int k = 0; k < m; ++k) wv = fma(X[tid * lda + k], b[k], wv);
+            for (int k = 0; k < m; ++k) wv = fma(A[tid * lda + k], b[k], wv);
             a.w[(size_t)pt * m + tid] = (float)wv;
             if (a.w64) a.w64[(size_t)pt * m + tid] = wv;
         }
-        dfs = la::block_sum<CALC_NT>(tid < m ? 1.0 - X[tid * lda + tid] : 0.0, s.red);
+        dfs = la::block_sum<CALC_NT>(tid < m ? 1.0 - A[tid * lda + tid] : 0.0, s.red);
         if (a.mode != ENKFG_MODE_ENOI && a.T != nullptr) {
             for (int i = tid; i < md * m; i += CALC_NT) {
                 int e1 = i / m, e2 = i - e1 * m;
-                double t = 0.5 * X[e1 * lda + e2];
+                double t = 0.5 * A[e1 * lda + e2];
                 if (e1 == e2) t += 0.5;
                 if (e1 == e2) t = (t - 1.0) * a.alpha + 1.0;
                 else t = t * a.alpha;
@@ -336,7 +372,7 @@ __device__ inline void solve_point(const CalcArgs& a, int pt, int p, int kc, dou
                 if (a.T64) a.T64[tbase + i] = t;
             }
         }
-        Q = X;
+        Q = A;
         gq = nullptr;
     }
     if (rc != 0 && tid == 0) a.status[pt] = rc;
@@ -356,7 +392,7 @@ __device__ inline void solve_point(const CalcArgs& a, int pt, int p, int kc, dou
         } else {
             __syncthreads();
             QuadProc qp(a, s, tile, tld, Q, gq, lda);
-            enumerate_obs<false>(a, kc, qx, qy, qz, s, qp, false);
+            enumerate_obs<0>(a, kc, qx, qy, qz, s, qp, false);
             if (tid < a.ntypes) {
                 int t = tid;
                 size_t k = (size_t)t * a.npts + pt;

@@ -2,26 +2,30 @@
 // the 5th-generation tensor cores (tcgen05, TF32 inputs, FP32 accumulation in
 // tensor memory), everything else in FP64 as in calc.cu.
 //
-// Per round of kc = 8*NA local observations:
-//   * the tapered rows of S (m members, rows m..127 zero) are written to
-//     shared memory as a K-major operand tile (rows = members, K =
-//     observations), split into TF32 hi = rn(v) and lo = rn(v - hi);
-//   * one thread issues, for each group q of 8 observations, three MMAs
-//     D_q = hi*hi' + hi*lo' + lo*hi' of shape M=128 x N x 8 into its own TMEM
-//     accumulator q (N = m rounded up to 16).  A and B are the same tile, so
-//     D_q is that group's contribution to S'S;
-//   * the MMAs' completion is signalled by tcgen05.commit on an mbarrier;
-//     the CTA then reads the NA accumulators out of TMEM (tcgen05.ld) and adds
-//     them, with error-free TwoSum steps, to a double-float (hi + lo FP32)
-//     accumulator in shared memory.  Only 8 observations are ever summed in
-//     FP32 inside the tensor core, so rounding stays near the split's own
-//     (about 2^-22 relative per product) whatever the local obs count;
-//   * S's is accumulated on the CUDA cores, one member per thread, with
-//     TwoProduct/TwoSum compensated FP32 (double-float) arithmetic.
+// Per round (chunk) of kc = 32 local observations:
+//   * the tapered rows of S (m members) are written to shared memory as a
+//     K-major operand tile (rows = members, K = observations), split into
+//     TF32 hi = rn(v) and lo = rn(v - hi), and kept as FP32 for S's;
+//   * one thread issues, for each group of 8 observations, three MMAs of
+//     shape M=128 x N x 8 (N = m rounded up to 16): hi*hi' into the group's
+//     TMEM accumulator, hi*lo' + lo*hi' into the round's cross-term one.  A
+//     and B are the same tile, so together they are the round's S'S;
+//   * the MMAs' completion is signalled by tcgen05.commit on the round's
+//     mbarrier.  Operand tiles are double buffered: while the tensor cores
+//     work on round c the CTA stages round c+1, then reads round c's
+//     accumulators out of TMEM (tcgen05.ld) and adds them, with error-free
+//     TwoSum steps, to double-float (hi + lo FP32) register accumulators.
+//     Each group of 8 observations has its own hi*hi' accumulator (nhh = 4
+//     per round, 2 when N > 96), so hi*hi' products are not summed inside
+//     the tensor core, whose FP32 accumulation truncates; the error stays at
+//     the level of the split itself (about 2^-22 relative per product);
+//   * S's is accumulated on the CUDA cores from the staged FP32 values, one
+//     member per thread, with TwoProduct/TwoSum compensated FP32
+//     (double-float) arithmetic.
 //
 // The accumulators are then converted to FP64 and go through the same FP64
-// solve as the plain path (Householder + QL for ETKF, Cholesky for
-// DEnKF/EnOI).
+// solve as the plain path (Householder + QL for ETKF, the symmetric sweep
+// inverse for DEnKF/EnOI).
 //
 // Shared-memory operand layout (canonical K-major, no swizzle): core matrices
 // of 8 rows x 16 bytes (4 TF32) stored as 128 contiguous bytes; core matrix
@@ -157,26 +161,28 @@ __device__ __forceinline__ float to_tf32(float x)
 
 }  // namespace tc
 
-#define MX_NA 4            // TMEM accumulators (groups of 8 obs) per round
+#define MX_KC 32            // observations per round
+#define MX_WIN 256          // observations per exact hi*hi' window (|k| <= 256: sums < 2^24 quanta)
+
+// Operand pieces per round: tapered value v = hi + mid + lo with hi = k q_r
+// (k integer, |k| <= 256, q_r the member's power-of-two quantum), mid =
+// tf32(v - hi), lo = tf32(v - hi - mid).
+#define MX_PIECES 3
 
 struct MixedShared {
-    float* tileH;      // [MX_ROWS x kc] core-matrix layout
-    float* tileL;
-    float2* Macc;      // [m x lda] double-float accumulator of S'S (later reused as FP64)
+    float* tile[2][MX_PIECES]; // [buffer][piece]: N rows x kc, core-matrix layout
+    float* tileV;          // [kc][ldv] tapered S of the round being staged (FP32)
+    int ldv;               // row stride of tileV: >= m, = 8 mod 32 (conflict-free staging)
+    const float* qs;       // [2][m]: quantum q_r and 1/q_r
+    float2* Macc;          // [m x lda] double-float S'S (later reused as FP64)
     int lda;
-    float* sl;         // [kc] tapered innovations of the round
-    uint64_t* mbar;
+    float* sl;             // [kc] tapered innovations of the round
+    uint64_t* mbar;        // [2] one per operand buffer
     uint32_t taddr;
-    int N;             // MMA N (m rounded up to 16)
-    int kc;            // observations per round (8 * MX_NA)
-    int* err;          // shared error flag
+    int N;                 // MMA N (m rounded up to 16)
+    int kc;                // observations per round
+    int* err;              // shared error flag
 };
-
-__device__ __forceinline__ int core_offset(int r, int k, int kc)
-{
-    // float index of element (row r, K index k) in the K-major no-swizzle tile
-    return (((r >> 3) * (kc >> 2) + (k >> 2)) << 5) + ((r & 7) << 2) + (k & 3);
-}
 
 // error-free (TwoSum) accumulation of x into the double-float (a.x + a.y)
 __device__ __forceinline__ void df_add(float2& a, float x)
@@ -188,18 +194,40 @@ __device__ __forceinline__ void df_add(float2& a, float x)
     a.y += e;
 }
 
+// mbarrier bookkeeping of the two operand buffers, kept across points:
+// parity of the next completion to wait for, and whether a commit is
+// outstanding
+struct MixedSync {
+    uint32_t phase[2];
+    bool outstanding[2];
+};
+
 // HB: 8-column blocks of S'S each thread accumulates (half of the N columns
 // of its TMEM lane), held as double-floats in registers for the whole point.
+//
+// TMEM: two accumulator sets (windows alternate), each [hi*hi' | rest] of N
+// columns: set s at columns 2 s N (hi*hi') and (2 s + 1) N (the other five
+// products).  A window collects up to MX_WIN observations; its hi*hi' sum is
+// exact in FP32 (every product is a multiple of q_r q_s below 2^16 of them),
+// the rest is 2^-8 of it or less.  A closed window is drained (tcgen05.ld,
+// TwoSum into the registers) one round later, while the next window runs.
 template <int HB>
 struct GramProcTC {
     const CalcArgs& a;
     const PointScratch& s;
     MixedShared& ms;
-    uint32_t& phase;
+    MixedSync& sy;
+    uint32_t& rnd;     // rounds issued by this CTA (all points): operand buffer = rnd & 1
+    int win;           // current window's accumulator set
+    int win_obs;       // observations in the current window
+    int drain_set;     // closed window awaiting its drain (-1: none)
+    int drain_buf;     // operand buffer whose commit closes it
     float bhi, blo;    // S's for member threadIdx.x (double-float)
     float2 acc[HB][8]; // S'S row 32*(warp%4)+lane, columns (warp/4)*half + [0, 8*HB)
-    __device__ __forceinline__ GramProcTC(const CalcArgs& a_, const PointScratch& s_, MixedShared& ms_, uint32_t& ph)
-        : a(a_), s(s_), ms(ms_), phase(ph), bhi(0.0f), blo(0.0f)
+    __device__ __forceinline__ GramProcTC(const CalcArgs& a_, const PointScratch& s_, MixedShared& ms_, MixedSync& sy_,
+                                          uint32_t& rnd_)
+        : a(a_), s(s_), ms(ms_), sy(sy_), rnd(rnd_), win(0), win_obs(0), drain_set(-1), drain_buf(0), bhi(0.0f),
+          blo(0.0f)
     {
 #pragma unroll
         for (int b = 0; b < HB; ++b)
@@ -223,51 +251,158 @@ struct GramProcTC {
             }
     }
 
+    // bounded wait for the outstanding commit of operand buffer `buf`; on
+    // expiry record the error and wait once more (bounded), so that nothing
+    // is in flight when TMEM is released.  Ends with a barrier, so every
+    // thread sees the same error flag.
+    __device__ __forceinline__ void wait_buf(int buf)
+    {
+        if (sy.outstanding[buf]) {
+            bool done = tc::mbar_wait_bounded(ms.mbar + buf, sy.phase[buf]);
+            if (!done) {
+                atomicExch(ms.err, 1);
+                tc::mbar_wait_bounded(ms.mbar + buf, sy.phase[buf]);
+            }
+            sy.phase[buf] ^= 1u;
+            sy.outstanding[buf] = false;
+        }
+        tc::fence_after();
+        __syncthreads();
+    }
+
+    // add accumulator set `set` to the registers (its MMAs have completed)
+    __device__ __forceinline__ void read_set(int set)
+    {
+        const int wid = threadIdx.x >> 5;
+        if (*ms.err) return;
+        if (32 * (wid & 3) < a.m) {
+            const int half = ms.N >> 1;
+            const int c0 = (wid >> 2) * half;
+            const uint32_t base = ms.taddr + ((uint32_t)(32 * (wid & 3)) << 16) + (uint32_t)(2 * set * ms.N + c0);
+            // one 8-column block per TMEM round trip (register budget)
+#pragma unroll
+            for (int b = 0; b < HB; ++b)
+                if (8 * b < half) {
+                    uint32_t vh[8], vr[8];
+                    tc::tmem_ld8_nowait(base + (uint32_t)(8 * b), vh);
+                    tc::tmem_ld8_nowait(base + (uint32_t)(ms.N + 8 * b), vr);
+                    tc::tmem_wait_ld();
+#pragma unroll
+                    for (int j = 0; j < 8; ++j) {
+                        df_add(acc[b][j], __uint_as_float(vh[j]));
+                        acc[b][j].y += __uint_as_float(vr[j]);   // <= 2^-8 of hi*hi'
+                    }
+                }
+        }
+        tc::fence_before();
+    }
+
     __device__ void chunk(int nc, int t)
     {
-        const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+        const int tid = threadIdx.x;
         const int m = a.m, kc = ms.kc;
         const bool tsum = a.want_diag && a.ntypes > 1;
         double ssq = 0.0;
         if (*ms.err) return;
-        // 1. tapered S rows of the round, split into TF32 hi + lo; the
-        //    tapered innovations for S's
-        const float* lcf = reinterpret_cast<const float*>(s.llc);   // FP32 taper (enumerate_obs<true>)
+        const int buf = (int)(rnd & 1u);
+        // 0. this operand buffer's previous MMAs were waited for at the end of
+        //    the last round (this only acts on the first round after an error)
+        if (sy.outstanding[buf]) {
+            wait_buf(buf);
+            if (*ms.err) return;
+        }
+        float* tH = ms.tile[buf][0];
+        float* tM = ms.tile[buf][1];
+        float* tL = ms.tile[buf][2];
+        // 1. tapered S rows of the round: hi / mid / lo pieces into this
+        //    round's operand tiles, FP32 copy for S's; tapered innovations
+        const float* lcf = reinterpret_cast<const float*>(s.llc);   // FP32 taper (enumerate_obs<1 or 2>)
+        const float* q = ms.qs;
+        const float* iq = ms.qs + m;
         if (tid < kc) ms.sl[tid] = (tid < nc) ? (float)a.ss[s.lid[tid]] * lcf[tid] : 0.0f;
-        for (int i = tid; i < kc * m; i += CALC_NT) {
-            int k = i / m, r = i - k * m;
-            float v = 0.0f;
-            if (k < nc) {
-                v = __fmul_rn(a.St[(size_t)s.lid[k] * a.mpad + r], lcf[k]);
-                if (tsum) ssq += (double)v * (double)v;
+        // one warp per core matrix (8 rows x 4 observations = 128 bytes):
+        // lane -> row r&7 = lane>>2, observation k&3 = lane&3, so the three
+        // piece stores are conflict-free; rows >= m stay zero.  (Two copies of
+        // the loop: an FP64 sum under a runtime flag inside the common loop
+        // would issue on the FP64 pipe even when off.)
+        {
+            const int lane = tid & 31, wid = tid >> 5;
+            const int nrg = (m + 7) >> 3, nkg = kc >> 2, ncm = nrg * nkg;
+            const int ldv = ms.ldv;
+            if (tsum) {
+                for (int c = wid; c < ncm; c += CALC_NT / 32) {
+                    const int rg = c / nkg, kg = c - rg * nkg;
+                    const int r = (rg << 3) + (lane >> 2), k = (kg << 2) + (lane & 3);
+                    if (r < m) {
+                        float v = 0.0f;
+                        if (k < nc) {
+                            v = __fmul_rn(__ldg(a.St + (size_t)s.lid[k] * a.mpad + r), lcf[k]);
+                            ssq += (double)v * (double)v;
+                        }
+                        const float hi = __fmul_rn(rintf(__fmul_rn(v, iq[r])), q[r]);
+                        const float r1 = __fsub_rn(v, hi);
+                        const float md = tc::to_tf32(r1);
+                        const int off = (c << 5) + lane;
+                        tH[off] = hi;
+                        tM[off] = md;
+                        tL[off] = tc::to_tf32(__fsub_rn(r1, md));
+                        ms.tileV[k * ldv + r] = v;
+                    }
+                }
+            } else {
+                for (int c = wid; c < ncm; c += CALC_NT / 32) {
+                    const int rg = c / nkg, kg = c - rg * nkg;
+                    const int r = (rg << 3) + (lane >> 2), k = (kg << 2) + (lane & 3);
+                    if (r < m) {
+                        float v = 0.0f;
+                        if (k < nc) v = __fmul_rn(__ldg(a.St + (size_t)s.lid[k] * a.mpad + r), lcf[k]);
+                        const float hi = __fmul_rn(rintf(__fmul_rn(v, iq[r])), q[r]);
+                        const float r1 = __fsub_rn(v, hi);
+                        const float md = tc::to_tf32(r1);
+                        const int off = (c << 5) + lane;
+                        tH[off] = hi;
+                        tM[off] = md;
+                        tL[off] = tc::to_tf32(__fsub_rn(r1, md));
+                        ms.tileV[k * ldv + r] = v;
+                    }
+                }
             }
-            float hi = tc::to_tf32(v);
-            int off = core_offset(r, k, kc);
-            ms.tileH[off] = hi;
-            ms.tileL[off] = tc::to_tf32(v - hi);
         }
         tc::fence_async_smem();
         __syncthreads();
-        // 2. one thread issues the MMAs: group q -> accumulator q
+        // 2. one thread issues the round's MMAs into the current window's
+        //    set: hi*hi' into the exact accumulator, the five other products
+        //    (hi*mid', mid*hi', hi*lo', lo*hi', mid*mid') into the rest.  A
+        //    and B are the same tiles; A has 128 rows, of which rows >= N
+        //    read the padding behind the tiles and land in accumulator rows
+        //    that are never read.
+        const int ngroups = (nc + 7) / 8;
         if (tid == 0) {
             tc::fence_after();
-            const uint32_t h0 = tc::smem_u32(ms.tileH), l0 = tc::smem_u32(ms.tileL);
             const uint32_t sbo = (uint32_t)kc * 32u, idesc = tc::idesc_tf32(MX_ROWS, ms.N);
-            for (int q = 0; q < kc / 8; ++q) {
-                const uint32_t off = (uint32_t)q * 256u;    // two 128-byte core matrices per group of 8
-                const uint32_t dq = ms.taddr + (uint32_t)(q * ms.N);
-                uint64_t dh = tc::desc_kmajor_noswizzle(h0 + off, 128u, sbo);
-                uint64_t dl = tc::desc_kmajor_noswizzle(l0 + off, 128u, sbo);
-                tc::mma_tf32(dq, dh, dh, idesc, 0u);
-                tc::mma_tf32(dq, dh, dl, idesc, 1u);
-                tc::mma_tf32(dq, dl, dh, idesc, 1u);
+            const uint32_t dhh = ms.taddr + (uint32_t)(2 * win * ms.N), dr = dhh + (uint32_t)ms.N;
+            const uint32_t h0 = tc::smem_u32(tH), m0 = tc::smem_u32(tM), l0 = tc::smem_u32(tL);
+            for (int g = 0; g < ngroups; ++g) {
+                const uint32_t off = (uint32_t)g * 256u;    // two 128-byte core matrices per group of 8
+                const uint64_t dh = tc::desc_kmajor_noswizzle(h0 + off, 128u, sbo);
+                const uint64_t dm = tc::desc_kmajor_noswizzle(m0 + off, 128u, sbo);
+                const uint64_t dl = tc::desc_kmajor_noswizzle(l0 + off, 128u, sbo);
+                const uint32_t fresh = (win_obs == 0 && g == 0) ? 0u : 1u;
+                tc::mma_tf32(dhh, dh, dh, idesc, fresh);
+                tc::mma_tf32(dr, dh, dm, idesc, fresh);
+                tc::mma_tf32(dr, dm, dh, idesc, 1u);
+                tc::mma_tf32(dr, dh, dl, idesc, 1u);
+                tc::mma_tf32(dr, dl, dh, idesc, 1u);
+                tc::mma_tf32(dr, dm, dm, idesc, 1u);
             }
-            tc::commit(ms.mbar);
+            tc::commit(ms.mbar + buf);
         }
-        // S's on the CUDA cores while the tensor cores run (compensated FP32)
+        sy.outstanding[buf] = true;
+        ++rnd;
+        // 3. S's from the staged FP32 values (compensated FP32)
         if (tid < m) {
             for (int k = 0; k < nc; ++k) {
-                float v = __fmul_rn(a.St[(size_t)s.lid[k] * a.mpad + tid], lcf[k]);
+                float v = ms.tileV[k * ms.ldv + tid];
                 float x = ms.sl[k];
                 float p = v * x, pe = fmaf(v, x, -p);
                 float sm = bhi + p, bp = sm - bhi;
@@ -275,60 +410,72 @@ struct GramProcTC {
                 bhi = sm;
             }
         }
-        // 3. bounded wait for the MMAs; on expiry record the error and wait
-        // once more (bounded) so that nothing is in flight when TMEM is freed
-        bool done = tc::mbar_wait_bounded(ms.mbar, phase);
-        if (!done) {
-            atomicExch(ms.err, 1);
-            tc::mbar_wait_bounded(ms.mbar, phase);
+        // 4. the window closed one round ago: its last commit is on the other
+        //    buffer; drain it while this round's MMAs run
+        if (drain_set >= 0) {
+            wait_buf(drain_buf);
+            read_set(drain_set);
+            drain_set = -1;
         }
-        phase ^= 1u;
-        tc::fence_after();
-        __syncthreads();
-        if (*ms.err) return;
-        // 4. accumulators (FP32, TMEM) -> double-float registers.  Warps w and
-        // w+4 share the TMEM lanes 32*(w%4).., each reading half of the N
-        // columns; the loads of all groups are issued before one wait.
-        {
-            const int half = ms.N >> 1;
-            const int c0 = (wid >> 2) * half;
-            const uint32_t lane_addr = ms.taddr + ((uint32_t)(32 * (wid & 3)) << 16);
-            const int ngroups = (nc + 7) / 8;
-#pragma unroll
-            for (int b = 0; b < HB; ++b) {
-                if (8 * b < half) {
-                    uint32_t v[MX_NA][8];
-#pragma unroll
-                    for (int q = 0; q < MX_NA; ++q)
-                        tc::tmem_ld8_nowait(lane_addr + (uint32_t)(q * ms.N + c0 + 8 * b), v[q]);
-                    tc::tmem_wait_ld();
-#pragma unroll
-                    for (int q = 0; q < MX_NA; ++q)
-                        if (q < ngroups) {
-#pragma unroll
-                            for (int j = 0; j < 8; ++j) df_add(acc[b][j], __uint_as_float(v[q][j]));
-                        }
-                }
-            }
+        // 5. close the current window when the next round might overflow it
+        win_obs += nc;
+        if (win_obs + kc > MX_WIN) {
+            drain_set = win;
+            drain_buf = buf;
+            win ^= 1;
+            win_obs = 0;
         }
-        tc::fence_before();
         if (tsum) {
             double v = la::block_sum<CALC_NT>(ssq, s.red);
             if (tid == 0) s.tss[t] += v;
         }
+        // 6. the previous round's MMAs (the other operand buffer, which the
+        //    next round stages into) ran during this round: wait for them
+        //    here, under the round's closing barrier
+        if (sy.outstanding[buf ^ 1]) {
+            bool done = tc::mbar_wait_bounded(ms.mbar + (buf ^ 1), sy.phase[buf ^ 1]);
+            if (!done) {
+                atomicExch(ms.err, 1);
+                tc::mbar_wait_bounded(ms.mbar + (buf ^ 1), sy.phase[buf ^ 1]);
+            }
+            sy.phase[buf ^ 1] ^= 1u;
+            sy.outstanding[buf ^ 1] = false;
+            tc::fence_after();
+        }
+        __syncthreads();
+    }
+    // drain what is left (after the enumeration; also after an error, so that
+    // no MMA is in flight when TMEM is released)
+    __device__ __forceinline__ void finish()
+    {
+        wait_buf(0);
+        wait_buf(1);
+        if (drain_set >= 0) read_set(drain_set);
+        if (win_obs > 0) read_set(win);
+        drain_set = -1;
+        win_obs = 0;
         __syncthreads();
     }
     __device__ __forceinline__ void type_end(int) {}
 };
 
-static size_t mixed_smem_bytes(int m, int kc, bool need_x)
+// operand tiles: 2 buffers x 3 pieces x N rows x kc, then the padding that
+// the 128-row A operand reads past the last tile (rows >= N, never used)
+static __host__ __device__ size_t mixed_tile_floats(int m, int kc)
+{
+    const int N = (m + 15) / 16 * 16;
+    return (size_t)2 * MX_PIECES * N * kc + (size_t)(MX_ROWS - N) * kc;
+}
+
+static size_t mixed_smem_bytes(int m, int kc)
 {
     int lda = (m % 2 == 0) ? m + 1 : m + 2;
     size_t s = 0;
-    s += 2 * (size_t)MX_ROWS * kc * 4;                     // tiles hi, lo
+    s += mixed_tile_floats(m, kc) * 4;                     // operand tiles + padding
+    s += (size_t)kc * (m + ((8 - m % 32) % 32 + 32) % 32) * 4;   // FP32 staged values (row stride = 8 mod 32)
+    s += (size_t)2 * m * 4;                                // quantum q, 1/q
     s += (size_t)m * lda * 8;                              // Macc (also A)
     s += (size_t)kc * 4;                                   // tapered innovations
-    if (need_x) s += (size_t)m * lda * 8;                  // X
     s += (size_t)6 * (m + 1) * 8;                          // b d e cs sn v
     s += (size_t)ENKFG_MAXTYPES * 8 * 2;
     s += (size_t)(CALC_NT / 32) * 8;
@@ -336,7 +483,7 @@ static size_t mixed_smem_bytes(int m, int kc, bool need_x)
     s += (size_t)LIST_EXTRA * 4;                           // lid
     s += (size_t)ENKFG_MAXTYPES * 4;
     s += 256;                                              // control ints
-    s += 64;                                               // mbarrier, tmem slot, flags
+    s += 64;                                               // mbarriers, tmem slot, flags
     return s;
 }
 
@@ -346,14 +493,15 @@ __global__ void __launch_bounds__(CALC_NT) k_transforms_mixed(CalcArgs a, int kc
     extern __shared__ __align__(128) unsigned char smem_raw[];
     const int tid = threadIdx.x, wid = tid >> 5;
     const int m = a.m, lda = (m % 2 == 0) ? m + 1 : m + 2;   // odd stride: fewer bank conflicts
-    const bool need_x = (a.mode == ENKFG_MODE_ENOI || a.scheme == ENKFG_SCHEME_DENKF);
+    const size_t ntile = mixed_tile_floats(m, kcm);         // [2][3][N x kc] + padding for A's rows >= N
     unsigned char* sp = smem_raw;
-    float* tileH = (float*)sp;        sp += (size_t)MX_ROWS * kcm * 4;
-    float* tileL = (float*)sp;        sp += (size_t)MX_ROWS * kcm * 4;
+    float* tiles = (float*)sp;        sp += ntile * 4;
+    const int ldv = m + ((8 - m % 32) % 32 + 32) % 32;        // >= m, = 8 mod 32
+    float* tileV = (float*)sp;        sp += (size_t)kcm * ldv * 4;
+    float* qs = (float*)sp;           sp += (size_t)2 * m * 4;
+    sp = (unsigned char*)(((uintptr_t)sp + 15) & ~(uintptr_t)15);
     double* Macc = (double*)sp;       sp += (size_t)m * lda * 8;
     float* sl = (float*)sp;           sp += (size_t)((kcm + 3) & ~3) * 4;
-    double* X = nullptr;
-    if (need_x) { X = (double*)sp;    sp += (size_t)m * lda * 8; }
     double* b = (double*)sp;          sp += (m + 1) * 8;
     double* d = (double*)sp;          sp += (m + 1) * 8;
     double* e = (double*)sp;          sp += (m + 1) * 8;
@@ -367,23 +515,30 @@ __global__ void __launch_bounds__(CALC_NT) k_transforms_mixed(CalcArgs a, int kc
     int* lid = (int*)sp;              sp += LIST_EXTRA * 4;
     int* tcount = (int*)sp;           sp += ENKFG_MAXTYPES * 4;
     int* ictl = (int*)sp;             sp += 256;
-    uint64_t* mbar = (uint64_t*)sp;   sp += 8;
+    uint64_t* mbar = (uint64_t*)sp;   sp += 8 * 2;
     uint32_t* tslot = (uint32_t*)sp;  sp += 8;
     int* err = (int*)sp;
     const PointScratch s{ lid, llc, ictl, tcount, tss, tpd, red };
+    const size_t piece = (size_t)N * kcm;
 
-    // set-up: TMEM columns, mbarrier, zeroed operand tiles
+    // set-up: TMEM columns, mbarriers, zeroed operand tiles, the quantum
     if (wid == 0) tc::tmem_alloc(tslot, tcols);
     if (tid == 0) {
-        tc::mbar_init(mbar, 1);
+        for (int i = 0; i < 2; ++i) tc::mbar_init(mbar + i, 1);
         *err = 0;
     }
-    for (int i = tid; i < 2 * MX_ROWS * kcm; i += CALC_NT) tileH[i] = 0.0f;   // tileL follows tileH
+    for (size_t i = tid; i < ntile; i += CALC_NT) tiles[i] = 0.0f;
+    for (int r = tid; r < m; r += CALC_NT) {
+        qs[r] = a.qscale[r];
+        qs[m + r] = a.qscale[ENKFG_MAXMEM + r];
+    }
     tc::fence_before();
     __syncthreads();
     tc::fence_after();
-    MixedShared ms{ tileH, tileL, (float2*)Macc, lda, sl, mbar, *tslot, N, kcm, err };
-    uint32_t phase = 0;
+    MixedShared ms{ { { tiles, tiles + piece, tiles + 2 * piece }, { tiles + 3 * piece, tiles + 4 * piece, tiles + 5 * piece } },
+                    tileV, ldv, qs, (float2*)Macc, lda, sl, mbar, *tslot, N, kcm, err };
+    MixedSync sy{ { 0u, 0u }, { false, false } };
+    uint32_t rnd = 0;
 
     for (int it = 0;; ++it) {
         const int idx = next_item(a, it, ictl);
@@ -403,8 +558,10 @@ __global__ void __launch_bounds__(CALC_NT) k_transforms_mixed(CalcArgs a, int kc
         }
         for (int i = tid; i < m * lda; i += CALC_NT) Macc[i] = 0.0;   // also zero as float2
         __syncthreads();
-        GramProcTC<HB> proc(a, s, ms, phase);
-        const int p = enumerate_obs<true>(a, ms.kc, qx, qy, qz, s, proc, true);
+        GramProcTC<HB> proc(a, s, ms, sy, rnd);
+        const int p = (a.sxf != nullptr && a.ndim == 2) ? enumerate_obs<2>(a, ms.kc, qx, qy, qz, s, proc, true)
+                                                        : enumerate_obs<1>(a, ms.kc, qx, qy, qz, s, proc, true);
+        proc.finish();
         proc.store();
         __syncthreads();
         if (*err) {
@@ -427,9 +584,9 @@ __global__ void __launch_bounds__(CALC_NT) k_transforms_mixed(CalcArgs a, int kc
         if (tid < m) Macc[tid * lda + tid] += 1.0;
         __syncthreads();
         // the per-type pass reuses the operand tiles as its FP64 chunk buffer
-        solve_point(a, pt, p, ms.kc, qx, qy, qz, Macc, X, lda, b, trss, d, e, cs, sn, v, s, (double*)tileH, m);
+        solve_point(a, pt, p, ms.kc, qx, qy, qz, Macc, lda, b, trss, d, e, cs, sn, v, s, (double*)tiles, m);
         if (a.want_diag && a.ntypes > 1) {
-            for (int i = tid; i < 2 * MX_ROWS * kcm; i += CALC_NT) tileH[i] = 0.0f;
+            for (size_t i = tid; i < ntile; i += CALC_NT) tiles[i] = 0.0f;
             __syncthreads();
         }
     }
@@ -462,18 +619,17 @@ static enkfg_status launch_mixed_hb(enkfg_ctx* ctx, CalcArgs& a, int kcm, int N,
 enkfg_status launch_mixed(enkfg_ctx* ctx, CalcArgs& a, cudaStream_t st)
 {
     const int m = a.m;
-    const bool need_x = (a.mode == ENKFG_MODE_ENOI || a.scheme == ENKFG_SCHEME_DENKF);
     const int N = (m + 15) / 16 * 16;
     uint32_t tcols = 32;
-    while ((int)tcols < MX_NA * N) tcols <<= 1;
-    const int kcm = 8 * MX_NA;
-    size_t smem = mixed_smem_bytes(m, kcm, need_x);
+    while ((int)tcols < 4 * N) tcols <<= 1;              // two windows x (hi*hi' | rest)
+    const int kcm = MX_KC;
+    size_t smem = mixed_smem_bytes(m, kcm);
     if (smem > 227 * 1024) {
         set_err(ctx, "mixed path: nmem = %d needs %zu bytes of shared memory", m, smem);
         return ENKFG_EUNSUPPORTED;
     }
     // the per-type pass's FP64 chunk buffer (kcm x m doubles) lives in the tiles
-    if (tcols > 512 || (size_t)kcm * m * 8 > 2 * (size_t)MX_ROWS * kcm * 4) {
+    if (tcols > 512 || (size_t)kcm * m * 8 > mixed_tile_floats(m, kcm) * 4) {
         set_err(ctx, "mixed path: tile too small for the per-type pass");
         return ENKFG_EUNSUPPORTED;
     }

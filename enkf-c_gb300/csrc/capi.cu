@@ -94,7 +94,10 @@ ENKFG_API enkfg_status enkfg_create(int device, enkfg_ctx** out)
     }
     for (int k = 0; k < 8; ++k) cudaEventCreate(&ctx->ev[k]);
     if (cudaMalloc(&ctx->d_qhead, 1024 * sizeof(int)) != cudaSuccess ||
-        cudaMalloc(&ctx->d_rfac, ENKFG_MAXTYPES * sizeof(double)) != cudaSuccess) {
+        cudaMalloc(&ctx->d_rfac, ENKFG_MAXTYPES * sizeof(double)) != cudaSuccess ||
+        cudaMalloc(&ctx->d_rfac_sqrt, ENKFG_MAXTYPES * sizeof(double)) != cudaSuccess ||
+        cudaMalloc(&ctx->d_smax, ENKFG_MAXMEM * sizeof(unsigned int)) != cudaSuccess ||
+        cudaMalloc(&ctx->d_qscale, 2 * ENKFG_MAXMEM * sizeof(float)) != cudaSuccess) {
         enkfg_destroy(ctx);
         return ENKFG_ENOMEM;
     }
@@ -107,9 +110,9 @@ ENKFG_API void enkfg_destroy(enkfg_ctx* ctx)
     if (!ctx) return;
     cudaSetDevice(ctx->device);
     cudaStreamSynchronize(ctx->stream);
-    void* ptrs[] = { ctx->d_lon, ctx->d_lat, ctx->d_type, ctx->d_status, ctx->d_estd, ctx->d_value, ctx->d_rfac,
+    void* ptrs[] = { ctx->d_lon, ctx->d_lat, ctx->d_type, ctx->d_status, ctx->d_estd, ctx->d_value, ctx->d_rfac, ctx->d_rfac_sqrt, ctx->d_gtmp, ctx->d_smax, ctx->d_qscale,
                      ctx->d_S, ctx->d_s, ctx->d_std, ctx->d_types, ctx->d_bstart, ctx->d_bfill, ctx->d_key,
-                     ctx->d_sid, ctx->d_sx, ctx->d_sy, ctx->d_sz, ctx->d_stype, ctx->d_St, ctx->d_ss, ctx->d_ox,
+                     ctx->d_sid, ctx->d_sx, ctx->d_sy, ctx->d_sz, ctx->d_sxf, ctx->d_syf, ctx->d_stype, ctx->d_St, ctx->d_ss, ctx->d_ox,
                      ctx->d_oy, ctx->d_oz, ctx->d_qx, ctx->d_qy, ctx->d_qz, ctx->d_T, ctx->d_w, ctx->d_T64,
                      ctx->d_w64, ctx->d_nlobs, ctx->d_dfs, ctx->d_srf, ctx->d_pnlobs, ctx->d_pdfs, ctx->d_psrf,
                      ctx->d_counts, ctx->d_order, ctx->d_qhead, ctx->d_status_pt, ctx->d_scratch,
@@ -136,7 +139,11 @@ ENKFG_API enkfg_status enkfg_rebuild_index(enkfg_ctx* ctx)
     if (!ctx) return ENKFG_EINVAL;
     ctx->index_valid = false;
     ctx->gather_valid = false;
-    return ENKFG_OK;
+    // build now, on the context's stream: the build reads sizes back to the
+    // host, so it must not be left to a later call that a CUDA graph captures
+    if (!ctx->obs_set || !ctx->types_set) return ENKFG_OK;
+    SETDEV();
+    return build_index(ctx, ctx->stream);
 }
 
 ENKFG_API enkfg_status enkfg_adjoint_transforms(enkfg_ctx* ctx, const enkfg_calc_params* p, const double* wbar,
@@ -245,6 +252,7 @@ ENKFG_API enkfg_status enkfg_autotune_reset(enkfg_ctx* ctx)
 {
     if (!ctx) return ENKFG_EINVAL;
     ctx->kc_tuned = false;
+    ctx->kc_loaded = 0;
     return ENKFG_OK;
 }
 
@@ -256,7 +264,18 @@ ENKFG_API long long enkfg_kernel_launches(const enkfg_ctx* ctx)
 ENKFG_API enkfg_status enkfg_stage_times(const enkfg_ctx* ctx, float* ms4)
 {
     if (!ctx || !ms4) return ENKFG_EINVAL;
-    for (int k = 0; k < 4; ++k) ms4[k] = ctx->stage_ms[k];
+    // from the stage events themselves when they have completed (the _dev
+    // entry points return before the work ends), else the last stored values
+    static const int pair[4][2] = { { 0, 1 }, { 1, 2 }, { 2, 3 }, { 4, 5 } };
+    for (int k = 0; k < 4; ++k) {
+        float v = 0.0f;
+        if (ctx->ev[pair[k][0]] && ctx->ev[pair[k][1]] &&
+            cudaEventElapsedTime(&v, ctx->ev[pair[k][0]], ctx->ev[pair[k][1]]) == cudaSuccess)
+            ms4[k] = v;
+        else
+            ms4[k] = ctx->stage_ms[k];
+    }
+    cudaGetLastError();
     return ENKFG_OK;
 }
 
@@ -285,6 +304,14 @@ ENKFG_API enkfg_status enkfg_set_obstypes(enkfg_ctx* ctx, int ntypes, const int*
     ctx->types_set = true;
     ctx->index_valid = false;
     ctx->gather_valid = false;
+    // sqrt(rfactor) per type for the standardisation, uploaded once here so
+    // that the per-cycle work has no host-to-device copy
+    {
+        double sr[ENKFG_MAXTYPES];
+        for (int t = 0; t < ntypes; ++t) sr[t] = sqrt(ctx->rfactor[t]);
+        SETDEV();
+        CK(cudaMemcpy(ctx->d_rfac_sqrt, sr, ntypes * sizeof(double), cudaMemcpyHostToDevice));
+    }
     return ENKFG_OK;
 }
 
@@ -401,7 +428,9 @@ ENKFG_API enkfg_status enkfg_calc_innovations(enkfg_ctx* ctx, double* s_f, doubl
         CK(cudaMemcpyAsync(s_f, ctx->d_s, ctx->nobs * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
     if (std_f && ctx->nobs > 0)
         CK(cudaMemcpyAsync(std_f, ctx->d_std, ctx->nobs * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
-    CK(cudaStreamSynchronize(ctx->stream));
+    // wait only when host outputs were asked for (the device-only call stays
+    // asynchronous, and can be captured into a CUDA graph)
+    if (s_f || std_f) CK(cudaStreamSynchronize(ctx->stream));
     ctx->s_mode = 2;
     ctx->gather_valid = false;
     return ENKFG_OK;
@@ -590,6 +619,7 @@ ENKFG_API enkfg_status enkfg_calc_transforms_dev(enkfg_ctx* ctx, const enkfg_cal
     enkfg_status s = check_calc(ctx, p);
     if (s) return s;
     SETDEV();
+    ctx->want64 = false;
     return run_transforms(ctx, p, pick(ctx, stream));
 }
 
@@ -606,6 +636,7 @@ ENKFG_API enkfg_status enkfg_calc_transforms(enkfg_ctx* ctx, const enkfg_calc_pa
     cudaStream_t st = ctx->stream;
     enkfg_calc_params q = *p;
     if (diag && diag->nlobs) q.want_diag = 1;
+    ctx->want64 = (T64 != nullptr || w64 != nullptr);
     if ((s = run_transforms(ctx, &q, st))) return s;
     if ((s = finish_calc(ctx, st))) return s;
     size_t npts = (size_t)ctx->nj * ctx->ni, m = ctx->nmem, md = ctx->nmem_dyn;

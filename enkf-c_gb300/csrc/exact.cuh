@@ -95,4 +95,56 @@ __device__ __forceinline__ float calclcoeff_f(int nlocrad, const double* locrad,
     return sum;
 }
 
+// Squared distance as a double-float (FP32 instructions only) for the mixed
+// path.  ox, oy: observation coordinates (floats, exact); the query is split
+// into hi + lo floats.  dx = (ox - qh) - ql is kept as the pair (xh, xl) with
+// the exact error of the first difference (TwoSum); the squares use the exact
+// FMA residual.  Returns the high part (d2h, also the FP32 squared distance)
+// and the low part d2l; together they carry about 2^-44 relative accuracy.
+__device__ __forceinline__ void dist2_df(float ox, float oy, float qxh, float qxl, float qyh, float qyl, float& d2h,
+                                         float& d2l)
+{
+    float xh = __fsub_rn(ox, qxh);
+    float xe;
+    {
+        // TwoSum error of xh = ox + (-qxh)
+        const float bp = __fsub_rn(xh, ox);
+        xe = __fadd_rn(__fsub_rn(ox, __fsub_rn(xh, bp)), __fsub_rn(-qxh, bp));
+    }
+    const float xl = __fsub_rn(xe, qxl);
+    float yh = __fsub_rn(oy, qyh);
+    float ye;
+    {
+        const float bp = __fsub_rn(yh, oy);
+        ye = __fadd_rn(__fsub_rn(oy, __fsub_rn(yh, bp)), __fsub_rn(-qyh, bp));
+    }
+    const float yl = __fsub_rn(ye, qyl);
+    const float px = __fmul_rn(xh, xh), pxe = fmaf(xh, xh, -px);
+    const float py = __fmul_rn(yh, yh), pye = fmaf(yh, yh, -py);
+    const float sh = __fadd_rn(px, py);
+    const float bp = __fsub_rn(sh, px);
+    const float se = __fadd_rn(__fsub_rn(px, __fsub_rn(sh, bp)), __fsub_rn(py, bp));
+    const float low = se + pxe + pye + 2.0f * (xh * xl + yh * yl) + (xl * xl + yl * yl);
+    d2h = __fadd_rn(sh, low);
+    d2l = __fsub_rn(low, __fsub_rn(d2h, sh));
+}
+
+// Taper coefficient from the double-float squared distance (mixed path):
+// e = r^2 - d^2 formed from double-float parts (no cancellation near the
+// edge), then the factorised outer piece as in calclcoeff_f.
+__device__ __forceinline__ float calclcoeff_df(const TypeIndex& t, float d2h, float d2l)
+{
+    const float dist = sqrtf(d2h);
+    float sum = 0.0f;
+    for (int i = 0; i < t.nlocrad; ++i) {
+        const float e = __fsub_rn(t.r2_f[i], d2h) + __fsub_rn(t.r2_fl[i], d2l);
+        if (e < 0.0f) continue;
+        const float rf = t.locrad_f[i];
+        const float u = e / (rf * (rf + dist));
+        const float z = 2.0f * (1.0f - u);
+        sum += t.locweight_f[i] * taper_gc_f(u, z);
+    }
+    return sum;
+}
+
 }  // namespace exact

@@ -163,7 +163,8 @@ __global__ void k_bucket_sort(long long nbuckets, const long long* __restrict__ 
 __global__ void k_sorted_coords(int nsorted, const int* __restrict__ sid, const double* __restrict__ ox,
                                 const double* __restrict__ oy, const double* __restrict__ oz,
                                 const short* __restrict__ type, double* __restrict__ sx, double* __restrict__ sy,
-                                double* __restrict__ sz, short* __restrict__ stype)
+                                double* __restrict__ sz, float* __restrict__ sxf, float* __restrict__ syf,
+                                short* __restrict__ stype)
 {
     int p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= nsorted) return;
@@ -171,6 +172,10 @@ __global__ void k_sorted_coords(int nsorted, const int* __restrict__ sid, const 
     sx[p] = ox[o];
     sy[p] = oy[o];
     if (sz) sz[p] = oz[o];
+    if (sxf) {
+        sxf[p] = (float)ox[o];
+        syf[p] = (float)oy[o];
+    }
     stype[p] = type[o];
 }
 
@@ -203,6 +208,46 @@ __global__ void k_gather_rows(int nsorted, int mpad, const int* __restrict__ sid
     float4* b = (float4*)(St + (size_t)p * mpad);
     for (int k = lane; k < mpad / 4; k += 32) b[k] = a[k];
     if (lane == 0) ss[p] = s[o];
+}
+
+// Largest |St| per member over all sorted rows (float bits: non-negative
+// floats order like their bit patterns), for the mixed path's quantum.
+__global__ void k_member_max(long long n4, int mpad, const float4* __restrict__ St, unsigned int* __restrict__ smax)
+{
+    __shared__ unsigned int sm[ENKFG_MAXMEM];
+    for (int r = threadIdx.x; r < mpad; r += blockDim.x) sm[r] = 0u;
+    __syncthreads();
+    const int q4 = mpad / 4;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n4; i += (long long)gridDim.x * blockDim.x) {
+        const float4 v = St[i];
+        const int r = 4 * (int)(i % q4);
+        atomicMax(&sm[r], __float_as_uint(fabsf(v.x)));
+        atomicMax(&sm[r + 1], __float_as_uint(fabsf(v.y)));
+        atomicMax(&sm[r + 2], __float_as_uint(fabsf(v.z)));
+        atomicMax(&sm[r + 3], __float_as_uint(fabsf(v.w)));
+    }
+    __syncthreads();
+    for (int r = threadIdx.x; r < mpad; r += blockDim.x)
+        if (sm[r]) atomicMax(&smax[r], sm[r]);
+}
+
+// Per-member quantum of the mixed path's split: the power of two q with
+// bound <= 256 q, bound = max |St| x (largest sum of taper weights) x
+// (1 + 2^-20) (the FP32 product S * taper may round up).  Then every tapered
+// value v of the member satisfies |rint(v / q)| <= 256.
+__global__ void k_quantum(int m, float lcmax, const unsigned int* __restrict__ smax, float* __restrict__ qscale)
+{
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= m) return;
+    const float bound = __uint_as_float(smax[r]) * lcmax * (1.0f + 9.5367431640625e-7f);
+    float q = 1.0f;
+    if (bound > 0.0f && isfinite(bound)) {
+        int e;
+        frexpf(bound, &e);               // bound = f 2^e, f in [0.5, 1)
+        q = ldexpf(1.0f, e - 8);
+    }
+    qscale[r] = q;
+    qscale[ENKFG_MAXMEM + r] = 1.0f / q;
 }
 
 // ---------------------------------------------------------------------------
@@ -334,6 +379,17 @@ enkfg_status build_index(enkfg_ctx* ctx, cudaStream_t st)
             }
             ti.rmax = rmax;
             ti.rmax2 = rmax * rmax;
+            for (int k = 0; k < ti.nlocrad; ++k) {
+                ti.locrad_f[k] = (float)ti.locrad[k];
+                ti.r2_f[k] = (float)(ti.locrad[k] * ti.locrad[k]);
+                ti.r2_fl[k] = (float)(ti.locrad[k] * ti.locrad[k] - (double)ti.r2_f[k]);
+                ti.locweight_f[k] = (float)ti.locweight[k];
+            }
+            // the FP32 squared distance (the high part of the double-float
+            // one) is within a few units of 2^-24 of the exact one; 2e-6
+            // relative leaves a margin of about 8x
+            ti.rmax2_lo = (float)(ti.rmax2 * (1.0 - 2e-6));
+            ti.rmax2_hi = (float)(ti.rmax2 * (1.0 + 2e-6));
             bool empty = (h[t * 6] == ~0ull);
             double lo[3] = { 0, 0, 0 }, hi[3] = { 0, 0, 0 };
             if (!empty)
@@ -376,15 +432,9 @@ enkfg_status build_index(enkfg_ctx* ctx, cudaStream_t st)
     CK(cudaMemcpyAsync(ctx->d_types, ctx->h_types, sizeof(TypeIndex) * ntypes, cudaMemcpyHostToDevice, st));
 
     // bucket counts, scan, scatter, sort
-    cudaFree(ctx->d_bstart);
-    cudaFree(ctx->d_bfill);
-    cudaFree(ctx->d_key);
-    ctx->d_bstart = nullptr;
-    ctx->d_bfill = nullptr;
-    ctx->d_key = nullptr;
-    CK(cudaMalloc(&ctx->d_bstart, (ctx->nbuckets + 1) * sizeof(long long)));
-    CK(cudaMalloc(&ctx->d_bfill, ctx->nbuckets * sizeof(int)));
-    CK(cudaMalloc(&ctx->d_key, (size_t)(nobs > 0 ? nobs : 1) * sizeof(int)));
+    if ((s = ensure(ctx, &ctx->d_bstart, &ctx->bstart_cap, (size_t)ctx->nbuckets + 1))) return s;
+    if ((s = ensure(ctx, &ctx->d_bfill, &ctx->bfill_cap, (size_t)ctx->nbuckets))) return s;
+    if ((s = ensure(ctx, &ctx->d_key, &ctx->key_cap, (size_t)(nobs > 0 ? nobs : 1)))) return s;
     CK(cudaMemsetAsync(ctx->d_bfill, 0, ctx->nbuckets * sizeof(int), st));
     if (nobs > 0) {
         k_keys<<<div_up(nobs, 256), 256, 0, st>>>(nobs, ndim, ctx->d_ox, ctx->d_oy, ctx->d_oz, ctx->d_type,
@@ -396,20 +446,25 @@ enkfg_status build_index(enkfg_ctx* ctx, cudaStream_t st)
     CK(cudaMemcpyAsync(&total, ctx->d_bstart + ctx->nbuckets, sizeof(long long), cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));
     ctx->nsorted = (int)total;
-    int ns = ctx->nsorted > 0 ? ctx->nsorted : 1;
-    cudaFree(ctx->d_sid);
-    cudaFree(ctx->d_sx);
-    cudaFree(ctx->d_sy);
-    cudaFree(ctx->d_sz);
-    cudaFree(ctx->d_stype);
-    ctx->d_sid = nullptr;
-    ctx->d_sx = ctx->d_sy = ctx->d_sz = nullptr;
-    ctx->d_stype = nullptr;
-    CK(cudaMalloc(&ctx->d_sid, ns * sizeof(int)));
-    CK(cudaMalloc(&ctx->d_sx, ns * sizeof(double)));
-    CK(cudaMalloc(&ctx->d_sy, ns * sizeof(double)));
-    if (ndim == 3) CK(cudaMalloc(&ctx->d_sz, ns * sizeof(double)));
-    CK(cudaMalloc(&ctx->d_stype, ns * sizeof(short)));
+    size_t ns = ctx->nsorted > 0 ? (size_t)ctx->nsorted : 1;
+    if ((s = ensure(ctx, &ctx->d_sid, &ctx->sid_cap, ns))) return s;
+    if ((s = ensure(ctx, &ctx->d_sx, &ctx->sx_cap, ns))) return s;
+    if ((s = ensure(ctx, &ctx->d_sy, &ctx->sy_cap, ns))) return s;
+    if ((s = ensure(ctx, &ctx->d_stype, &ctx->stype_cap, ns))) return s;
+    if (ndim == 3) {
+        if ((s = ensure(ctx, &ctx->d_sz, &ctx->sz_cap, ns))) return s;
+        // the FP32 search copies exist for 2-D only
+        cudaFree(ctx->d_sxf);
+        cudaFree(ctx->d_syf);
+        ctx->d_sxf = ctx->d_syf = nullptr;
+        ctx->sxf_cap = ctx->syf_cap = 0;
+    } else {
+        cudaFree(ctx->d_sz);
+        ctx->d_sz = nullptr;
+        ctx->sz_cap = 0;
+        if ((s = ensure(ctx, &ctx->d_sxf, &ctx->sxf_cap, ns))) return s;
+        if ((s = ensure(ctx, &ctx->d_syf, &ctx->syf_cap, ns))) return s;
+    }
     CK(cudaMemsetAsync(ctx->d_bfill, 0, ctx->nbuckets * sizeof(int), st));
     if (nobs > 0) {
         k_scatter<<<div_up(nobs, 256), 256, 0, st>>>(nobs, ctx->d_key, ctx->d_bstart, ctx->d_bfill, ctx->d_sid);
@@ -421,7 +476,7 @@ enkfg_status build_index(enkfg_ctx* ctx, cudaStream_t st)
     if (ctx->nsorted > 0) {
         k_sorted_coords<<<div_up(ctx->nsorted, 256), 256, 0, st>>>(ctx->nsorted, ctx->d_sid, ctx->d_ox, ctx->d_oy,
                                                                   ctx->d_oz, ctx->d_type, ctx->d_sx, ctx->d_sy,
-                                                                  ctx->d_sz, ctx->d_stype);
+                                                                  ctx->d_sz, ctx->d_sxf, ctx->d_syf, ctx->d_stype);
         CKL();
     }
     // per-type sorted ranges (bucket_base ranges are contiguous by type)
@@ -446,26 +501,36 @@ enkfg_status build_gather(enkfg_ctx* ctx, cudaStream_t st)
     int m = ctx->nmem, nobs = ctx->nobs;
     int mpad = (m + 3) & ~3;
     ctx->mpad = mpad;
-    int ns = ctx->nsorted > 0 ? ctx->nsorted : 1;
-    cudaFree(ctx->d_St);
-    cudaFree(ctx->d_ss);
-    ctx->d_St = nullptr;
-    ctx->d_ss = nullptr;
-    CK(cudaMalloc(&ctx->d_St, (size_t)ns * mpad * sizeof(float)));
-    CK(cudaMalloc(&ctx->d_ss, (size_t)ns * sizeof(double)));
+    size_t ns = ctx->nsorted > 0 ? (size_t)ctx->nsorted : 1;
+    enkfg_status s;
+    if ((s = ensure(ctx, &ctx->d_St, &ctx->St_cap, ns * mpad))) return s;
+    if ((s = ensure(ctx, &ctx->d_ss, &ctx->ss_cap, ns))) return s;
     if (nobs > 0 && ctx->nsorted > 0) {
-        float* tmp;
-        CK(cudaMalloc(&tmp, (size_t)nobs * mpad * sizeof(float)));
+        if ((s = ensure(ctx, &ctx->d_gtmp, &ctx->gtmp_cap, (size_t)nobs * mpad))) return s;
         dim3 g(div_up(nobs, 32), div_up(mpad, 32));
-        k_transpose_S<<<g, dim3(32, 8), 0, st>>>(m, nobs, mpad, ctx->d_S, tmp);
-        ctx->launches++;
-        k_gather_rows<<<div_up((long long)ctx->nsorted * 32, 256), 256, 0, st>>>(ctx->nsorted, mpad, ctx->d_sid, tmp,
-                                                                               ctx->d_s, ctx->d_St, ctx->d_ss);
-        ctx->launches++;
-        cudaError_t e = cudaGetLastError();
-        cudaStreamSynchronize(st);
-        cudaFree(tmp);
-        if (e != cudaSuccess) return cuda_fail(ctx, e, "gather", __LINE__);
+        k_transpose_S<<<g, dim3(32, 8), 0, st>>>(m, nobs, mpad, ctx->d_S, ctx->d_gtmp);
+        CKL();
+        k_gather_rows<<<div_up((long long)ctx->nsorted * 32, 256), 256, 0, st>>>(ctx->nsorted, mpad, ctx->d_sid,
+                                                                               ctx->d_gtmp, ctx->d_s, ctx->d_St,
+                                                                               ctx->d_ss);
+        CKL();
+    }
+    // the mixed path's per-member quantum
+    {
+        double lcmax = 0.0;
+        for (int t = 0; t < ctx->ntypes; ++t) {
+            double sw = 0.0;
+            for (int k = 0; k < ctx->nlocrad[t]; ++k) sw += fabs(ctx->locweight[t][k]);
+            if (sw > lcmax) lcmax = sw;
+        }
+        CK(cudaMemsetAsync(ctx->d_smax, 0, ENKFG_MAXMEM * sizeof(unsigned int), st));
+        const long long n4 = (long long)ctx->nsorted * (mpad / 4);
+        if (n4 > 0) {
+            k_member_max<<<304, 256, 0, st>>>(n4, mpad, (const float4*)ctx->d_St, ctx->d_smax);
+            CKL();
+        }
+        k_quantum<<<1, ENKFG_MAXMEM, 0, st>>>(m, (float)lcmax, ctx->d_smax, ctx->d_qscale);
+        CKL();
     }
     ctx->gather_valid = true;
     return ENKFG_OK;

@@ -29,6 +29,14 @@ struct TypeIndex {
     double locweight[ENKFG_MAXLOCRAD];
     double rmax;                // max(locrad)
     double rmax2;               // rmax * rmax (rounded as the reference rounds range*range)
+    // FP32 copies for the mixed path's search and taper: radii, squared
+    // radii, weights, and the band [rmax2_lo, rmax2_hi] around rmax2 inside
+    // which the FP32 distance cannot decide membership (exact FP64 test)
+    float locrad_f[ENKFG_MAXLOCRAD];
+    float r2_f[ENKFG_MAXLOCRAD];      // r^2 as a double-float r2_f + r2_fl
+    float r2_fl[ENKFG_MAXLOCRAD];
+    float locweight_f[ENKFG_MAXLOCRAD];
+    float rmax2_lo, rmax2_hi;
 };
 
 struct enkfg_ctx {
@@ -57,7 +65,8 @@ struct enkfg_ctx {
     short* d_status;
     float* d_estd;
     float* d_value;
-    double* d_rfac;             // [ntypes]
+    double* d_rfac;             // [ntypes] scratch
+    double* d_rfac_sqrt;        // [ntypes] sqrt(rfactor), uploaded with the obs types
     bool obs_set;
 
     // ensemble observations
@@ -78,6 +87,8 @@ struct enkfg_ctx {
     int* d_bfill;               // [nbuckets] scratch
     int* d_key;                 // [nobs] scratch
     int* d_sid;                 // [nsorted] obs id at sorted position
+    float* d_sxf;               // [nsorted] FP32 copies of d_sx, d_sy (2-D only; exact for float inputs)
+    float* d_syf;
     double* d_sx;               // [nsorted] kd coordinates in sorted order
     double* d_sy;
     double* d_sz;
@@ -85,6 +96,14 @@ struct enkfg_ctx {
     int mpad;                   // member stride of d_St (multiple of 4)
     float* d_St;                // [nsorted][mpad] standardised S, sorted, member-contiguous
     double* d_ss;               // [nsorted] standardised innovation, sorted
+    float* d_gtmp;              // [nobs][mpad] transpose scratch of the gather
+    unsigned int* d_smax;       // [ENKFG_MAXMEM] max |St| per member (float bits), mixed-path quantum
+    float* d_qscale;            // [2][ENKFG_MAXMEM] per-member quantum q and 1/q (powers of two)
+    // grow-only capacities: rebuilding the index or the gather keeps the
+    // device addresses when the sizes do not grow (CUDA graphs captured on
+    // the cycle keep pointing at valid buffers)
+    size_t bstart_cap, bfill_cap, key_cap, sid_cap, sx_cap, sy_cap, sz_cap, sxf_cap, syf_cap, stype_cap;
+    size_t St_cap, ss_cap, gtmp_cap;
     double* d_ox;               // [nobs] kd coordinates (original order)
     double* d_oy;
     double* d_oz;
@@ -98,6 +117,7 @@ struct enkfg_ctx {
 
     // transforms (resident)
     int t_mode, t_nmem, t_ndyn;
+    bool want64;                // the next calc also writes the FP64 T and w
     bool t_valid;
     float* d_T;                 // [nj*ni][ndyn][nmem]
     float* d_w;                 // [nj*ni][nmem]
@@ -120,11 +140,14 @@ struct enkfg_ctx {
     bool kc_tuned;              // d_qhead[2+16 ..] holds an autotuned chunk-size table
     int kc_tuned_prec;          // precision the table was tuned for
     int kc_table[16];           // host copy of the tuned table
+    int kc_loaded;              // table now on the device: 0 none, 1 FP64 default, 2 mixed default, 3 tuned
     void* d_scratch;
     size_t scratch_cap;
     size_t counts_cap, order_cap, status_cap;
 
     // update scratch
+    int h_levels[448];          // levels last uploaded for the update (d_qhead + 64)
+    int n_levels;               // their count (0: none)
     int* d_numlevels;
     size_t numlevels_cap;
     float* d_fields;

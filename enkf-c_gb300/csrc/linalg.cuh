@@ -10,12 +10,14 @@
 //                 applied to the eigenvector matrix are spread over the CTA;
 //                 the QL rotation chain itself is sequential and runs on one
 //                 thread while the others wait.
-//   chol_inverse  M^-1 of an SPD matrix by Cholesky factorisation and two
-//                 triangular solves against the identity.
+//   spd_inverse   M^-1 of an SPD matrix in place by the symmetric sweep
+//                 operator (Gauss-Jordan elimination without pivoting, kept
+//                 symmetric, on the upper triangle only).
 //
 // These replace LAPACK dgesvd (reference calc/calcs.c:338) and dpotrf/dpotri
-// (calcs.c:103-132).  Both are backward stable, so the results agree with
-// LAPACK's to a few units of rounding times the condition of M = I + S'S.
+// (calcs.c:103-132).  For M = I + S'S (eigenvalues >= 1) both are stable, so
+// the results agree with LAPACK's to a few units of rounding times the
+// condition of M.
 #pragma once
 
 namespace la {
@@ -154,23 +156,31 @@ __device__ int eig_sym(double* A, int n, int lda, double* d, double* e, double* 
                         ctl[3] = 1;
                     } else {
                         double g = (d[l + 1] - d[l]) / (2.0 * e[l]);
-                        double r = hypot(g, 1.0);
+                        double r = sqrt(fma(g, g, 1.0));
                         g = d[m] - d[l] + e[l] / (g + copysign(r, g));
                         double s = 1.0, c = 1.0, p = 0.0;
                         int i;
                         bool underflow = false;
+                        // This loop is one thread's chain of dependent FP64
+                        // operations, and GB300 issues FP64 at 1/64 of the
+                        // FP32 rate, so each rotation uses one reciprocal
+                        // square root and multiplies (no hypot, no divides).
+                        // f and g stay far from overflow for M = I + S'S.
                         for (i = m - 1; i >= l; --i) {
                             double f = s * e[i], b = c * e[i];
-                            r = hypot(f, g);
-                            e[i + 1] = r;
-                            if (r == 0.0) {
+                            const double t = fma(f, f, g * g);
+                            if (t == 0.0) {
+                                e[i + 1] = 0.0;
                                 d[i + 1] -= p;
                                 e[m] = 0.0;
                                 underflow = true;
                                 break;
                             }
-                            s = f / r;
-                            c = g / r;
+                            const double ri = rsqrt(t);
+                            r = t * ri;
+                            e[i + 1] = r;
+                            s = f * ri;
+                            c = g * ri;
                             g = d[i + 1] - p;
                             r = (d[i] - g) * s + 2.0 * c * b;
                             p = s * r;
@@ -213,60 +223,82 @@ __device__ int eig_sym(double* A, int n, int lda, double* d, double* e, double* 
     return ctl[3];
 }
 
-// M^-1 of the SPD matrix A (n x n, stride lda) into X (same shape); A is
-// overwritten by its Cholesky factor.  Returns 0, or 1 if a pivot is not
-// positive.
+// In-place inverse of the SPD matrix A (n x n, row stride lda; the upper
+// triangle is read) by the symmetric sweep operator.  Sweeping pivot k with
+// D = a_kk and u = column k of the current (symmetric) matrix:
+//     a_ij <- a_ij - u_i u_j / D   (i, j != k),
+//     a_ik <- u_i / D              (i != k),
+//     a_kk <- -1 / D,
+// and after all n pivots the matrix holds -A^-1.  Every step updates the
+// whole upper triangle in parallel (one FMA per element): warps take pairs
+// of rows (i, n-1-i), whose lengths add up to n+1, and lanes the columns, so
+// all threads stay busy instead of the serial chains of triangular solves.
+// Without pivoting this is stable for M = I + S'S (pivots >= 1).  On return A
+// holds the full symmetric A^-1.  U, V: n doubles each; piv: 2 doubles.
+// Returns 0, or 1 if a pivot was not positive.
 template <int NT>
-__device__ int chol_inverse(double* A, double* X, int n, int lda, int* ctl)
+__device__ int spd_inverse(double* A, int n, int lda, double* U, double* V, double* piv, int* ctl)
 {
-    const int tid = threadIdx.x;
-    if (tid == 0) ctl[3] = 0;
+    constexpr int NW = NT / 32;
+    const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+    const int npair = (n + 1) >> 1;
+    if (tid == 0) {
+        ctl[3] = 0;
+        double p0 = A[0];
+        if (!(p0 > 0.0)) {
+            ctl[3] = 1;
+            p0 = 1.0;
+        }
+        piv[0] = 1.0 / p0;
+    }
+    __syncthreads();
     for (int k = 0; k < n; ++k) {
-        if (tid == 0) {
-            double a = A[(size_t)k * lda + k];
-            if (!(a > 0.0)) {
-                ctl[3] = 1;
-                a = 1.0;
+        const double inv = piv[k & 1];
+        for (int i = tid; i < n; i += NT) {
+            const double u = (i <= k) ? A[(size_t)i * lda + k] : A[(size_t)k * lda + i];
+            U[i] = u;
+            V[i] = u * inv;
+        }
+        __syncthreads();
+        for (int pr = wid; pr < npair; pr += NW) {
+            const int i0 = pr, i1 = n - 1 - pr;
+            const int len0 = n - i0;
+            const int total = (i0 == i1) ? len0 : n + 1;
+            for (int c = lane; c < total; c += 32) {
+                int i, j;
+                if (c < len0) {
+                    i = i0;
+                    j = i0 + c;
+                } else {
+                    i = i1;
+                    j = i1 + (c - len0);
+                }
+                double* aij = A + (size_t)i * lda + j;
+                double v;
+                if (i == k) v = (j == k) ? -inv : V[j];
+                else if (j == k) v = V[i];
+                else v = fma(-U[i], V[j], *aij);
+                *aij = v;
+                if (i == k + 1 && j == k + 1) {
+                    if (!(v > 0.0)) {
+                        ctl[3] = 1;
+                        v = 1.0;
+                    }
+                    piv[(k + 1) & 1] = 1.0 / v;
+                }
             }
-            A[(size_t)k * lda + k] = sqrt(a);
-        }
-        __syncthreads();
-        double dk = A[(size_t)k * lda + k];
-        for (int i = k + 1 + tid; i < n; i += NT) A[(size_t)i * lda + k] /= dk;
-        __syncthreads();
-        int w = n - k - 1;
-        int tri = w * (w + 1) / 2;
-        for (int idx = tid; idx < tri; idx += NT) {
-            int a = (int)((sqrtf(8.0f * (float)idx + 1.0f) - 1.0f) * 0.5f);
-            while ((a + 1) * (a + 2) / 2 <= idx) ++a;
-            while (a * (a + 1) / 2 > idx) --a;
-            int b = idx - a * (a + 1) / 2;
-            int i = k + 1 + a, j = k + 1 + b;
-            A[(size_t)i * lda + j] -= A[(size_t)i * lda + k] * A[(size_t)j * lda + k];
         }
         __syncthreads();
     }
-    // forward: L Y = I (column-parallel), Y in X
-    for (int i = 0; i < n; ++i) {
-        const double* Li = A + (size_t)i * lda;
-        double inv = 1.0 / Li[i];
-        for (int j = tid; j < n; j += NT) {
-            double s = (i == j) ? 1.0 : 0.0;
-            for (int k = j; k < i; ++k) s -= Li[k] * X[(size_t)k * lda + j];
-            X[(size_t)i * lda + j] = (j <= i) ? s * inv : 0.0;
-        }
-        __syncthreads();
+    // -A^-1 (upper) -> A^-1 (both triangles)
+    for (int idx = tid; idx < n * n; idx += NT) {
+        const int i = idx / n, j = idx - i * n;
+        if (j < i) continue;
+        const double v = -A[(size_t)i * lda + j];
+        A[(size_t)i * lda + j] = v;
+        if (j != i) A[(size_t)j * lda + i] = v;
     }
-    // backward: L^T X = Y
-    for (int i = n - 1; i >= 0; --i) {
-        double inv = 1.0 / A[(size_t)i * lda + i];
-        for (int j = tid; j < n; j += NT) {
-            double s = X[(size_t)i * lda + j];
-            for (int k = i + 1; k < n; ++k) s -= A[(size_t)k * lda + i] * X[(size_t)k * lda + j];
-            X[(size_t)i * lda + j] = s * inv;
-        }
-        __syncthreads();
-    }
+    __syncthreads();
     return ctl[3];
 }
 

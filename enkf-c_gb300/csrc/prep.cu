@@ -82,14 +82,10 @@ enkfg_status run_innovations(enkfg_ctx* ctx, cudaStream_t st)
 
 enkfg_status run_standardise(enkfg_ctx* ctx, cudaStream_t st)
 {
-    double sr[ENKFG_MAXTYPES];
-    for (int t = 0; t < ctx->ntypes; ++t) sr[t] = sqrt(ctx->rfactor[t]);
-    CK(cudaMemcpyAsync(ctx->d_rfac, sr, ctx->ntypes * sizeof(double), cudaMemcpyHostToDevice, st));
     double mult = sqrt((double)ctx->nmem - 1);
     k_standardise<<<div_up(ctx->nobs, 256), 256, 0, st>>>(ctx->nmem, ctx->nobs, mult, ctx->d_S, ctx->d_s,
-                                                         ctx->d_estd, ctx->d_type, ctx->d_rfac);
+                                                         ctx->d_estd, ctx->d_type, ctx->d_rfac_sqrt);
     CKL();
-    CK(cudaStreamSynchronize(st));
     return ENKFG_OK;
 }
 

@@ -41,6 +41,7 @@ struct UpdArgs {
     int nk;                     // cells per CTA (tile cell stride)
     int G;                      // strided columns per CTA (version 2 kernel)
     int fc;                     // field-layers per warp task (version 2 kernel)
+    float inv_kd;               // 1 / k_d (hybrid rescaling, FP32 variant)
 };
 
 // One element of the interpolated X5 for model cell (jt, i) of the tile
@@ -124,8 +125,45 @@ struct Acc<false> {
     __device__ __forceinline__ double value() const { return (double)hi + (double)lo; }
 };
 
-// (float)(x - mean) with mean held in double (F64) or as a double-float
-__device__ __forceinline__ float sub_mean(float x, double mean) { return (float)((double)x - mean); }
+// The ensemble mean and the updated mean: double (F64, the reference's
+// arithmetic) or a double-float hi + lo (FP32 pipe only; GB300 issues FP64 at
+// 1/64 of the FP32 rate, and the conversions float <-> double run on the
+// FP64 pipe as well).
+template <bool F64>
+struct Mean;
+template <>
+struct Mean<true> {
+    double v;
+    __device__ __forceinline__ void set(const Acc<true>& s, int n) { v = s.value() / (double)n; }
+    __device__ __forceinline__ void zero() { v = 0.0; }
+    // (float)(x - mean)
+    __device__ __forceinline__ float sub(float x) const { return (float)((double)x - v); }
+    // (float)(x + mean)
+    __device__ __forceinline__ float add(float x) const { return (float)((double)x + v); }
+    // mean + s (the updated mean, update.c:405-410)
+    __device__ __forceinline__ Mean plus(const Acc<true>& s) const { Mean r; r.v = s.value() + v; return r; }
+};
+template <>
+struct Mean<false> {
+    float h, l;
+    __device__ __forceinline__ void set(const Acc<false>& s, int n)
+    {
+        const float fn = (float)n;
+        h = __fdiv_rn(s.hi, fn);
+        l = __fdiv_rn(fmaf(-h, fn, s.hi) + s.lo, fn);
+    }
+    __device__ __forceinline__ void zero() { h = l = 0.0f; }
+    __device__ __forceinline__ float sub(float x) const { return __fsub_rn(__fsub_rn(x, h), l); }
+    __device__ __forceinline__ float add(float x) const { return __fadd_rn(__fadd_rn(x, h), l); }
+    __device__ __forceinline__ Mean plus(const Acc<false>& s) const
+    {
+        Mean r;
+        const float sm = s.hi + h, bp = sm - s.hi;
+        r.l = ((s.hi - (sm - bp)) + (h - bp)) + (s.lo + l);
+        r.h = sm;
+        return r;
+    }
+};
 
 // das_updatefields, version 2.  A CTA owns one model row j and G strided
 // columns (cells i in [ii0*stride, (ii0+G)*stride)).  It builds, once, the
@@ -214,13 +252,13 @@ __global__ void __launch_bounds__(UPD_NT) k_update_v2(UpdArgs a)
         {
             const int fc = min(fcap, nf - f0);
             unsigned active = 0;                              // rows to update
-            double mean[UPD_FC];
+            Mean<F64> mean[UPD_FC];
             // per row: mask, missing values, mean, anomalies (update.c:296-392)
             for (int q = 0; q < fc; ++q) {
                 const int f = f0 + q;
                 float* v = tile + (size_t)f * m * CP;
                 const int level = a.levels[f];
-                mean[q] = 0.0;
+                mean[q].zero();
                 bool masked = (a.surfk == 0) ? (nl <= level) : (nl <= (a.issurfacevar ? 0 : a.surfk - level));
                 if (masked) {
                     for (int e = lane; e < m; e += 32) v[e * CP + c] = 0.0f;
@@ -249,8 +287,8 @@ __global__ void __launch_bounds__(UPD_NT) k_update_v2(UpdArgs a)
                 Acc<F64> sm;
                 for (int e = lane; e < md; e += 32) sm.add(v[e * CP + c]);
                 sm.reduce();
-                mean[q] = sm.value() / (double)md;
-                for (int e = lane; e < M4; e += 32) Aw[q * M4 + e] = (e < m) ? sub_mean(v[e * CP + c], mean[q]) : 0.0f;
+                mean[q].set(sm, md);
+                for (int e = lane; e < M4; e += 32) Aw[q * M4 + e] = (e < m) ? mean[q].sub(v[e * CP + c]) : 0.0f;
                 active |= 1u << q;
             }
             __syncwarp();
@@ -321,7 +359,7 @@ __global__ void __launch_bounds__(UPD_NT) k_update_v2(UpdArgs a)
                     if (e < m) sa.add_prod(Aw[q * M4 + e], wl[k]);
                 }
                 sa.reduce();
-                const double v1_a = sa.value() + mean[q];
+                const Mean<F64> v1_a = mean[q].plus(sa);
                 float af[MAXE_PER_LANE], aa[MAXE_PER_LANE];
 #pragma unroll
                 for (int k = 0; k < MAXE_PER_LANE; ++k) {
@@ -330,13 +368,23 @@ __global__ void __launch_bounds__(UPD_NT) k_update_v2(UpdArgs a)
                     aa[k] = acc[q][k];
                 }
                 if (a.mode == ENKFG_MODE_HYBRID) {
-                    const double k_d = (md > 1) ? sqrt((double)(m - 1) / (double)(md - 1)) : 1.0;
+                    if constexpr (F64) {
+                        const double k_d = (md > 1) ? sqrt((double)(m - 1) / (double)(md - 1)) : 1.0;
 #pragma unroll
-                    for (int k = 0; k < MAXE_PER_LANE; ++k)
-                        if (lane + 32 * k < md) {
-                            aa[k] = (float)((double)aa[k] / k_d);
-                            af[k] = (float)((double)af[k] / k_d);
-                        }
+                        for (int k = 0; k < MAXE_PER_LANE; ++k)
+                            if (lane + 32 * k < md) {
+                                aa[k] = (float)((double)aa[k] / k_d);
+                                af[k] = (float)((double)af[k] / k_d);
+                            }
+                    } else {
+                        const float rk = a.inv_kd;
+#pragma unroll
+                        for (int k = 0; k < MAXE_PER_LANE; ++k)
+                            if (lane + 32 * k < md) {
+                                aa[k] = __fmul_rn(aa[k], rk);
+                                af[k] = __fmul_rn(af[k], rk);
+                            }
+                    }
                 }
                 if (!isnan(a.inf_ratio)) {
                     Acc<F64> s2f, s2a;
@@ -348,10 +396,19 @@ __global__ void __launch_bounds__(UPD_NT) k_update_v2(UpdArgs a)
                         }
                     s2f.reduce();
                     s2a.reduce();
-                    const double v2_f = s2f.value(), v2_a = s2a.value();
-                    if (v2_a > 0.0) {
-                        inflation = (float)(sqrt(v2_f / v2_a) * a.inf_ratio + 1.0 - a.inf_ratio);
-                        if (inflation >= a.inflation0) inflation = a.inflation0;
+                    if constexpr (F64) {
+                        const double v2_f = s2f.value(), v2_a = s2a.value();
+                        if (v2_a > 0.0) {
+                            inflation = (float)(sqrt(v2_f / v2_a) * a.inf_ratio + 1.0 - a.inf_ratio);
+                            if (inflation >= a.inflation0) inflation = a.inflation0;
+                        }
+                    } else {
+                        const float v2_f = s2f.hi + s2f.lo, v2_a = s2a.hi + s2a.lo;
+                        if (v2_a > 0.0f) {
+                            const float r = (float)a.inf_ratio;
+                            inflation = fmaf(sqrtf(__fdiv_rn(v2_f, v2_a)), r, 1.0f - r);
+                            if (inflation >= a.inflation0) inflation = a.inflation0;
+                        }
                     }
                 }
                 const bool inflate = __fsub_rn(inflation, 1.0f) > 1.0e-6f;
@@ -361,8 +418,8 @@ __global__ void __launch_bounds__(UPD_NT) k_update_v2(UpdArgs a)
                     const int e1 = lane + 32 * k;
                     if (e1 < md) {
                         float va = inflate ? __fmul_rn(aa[k], inflation) : aa[k];
-                        va = (float)((double)va + v1_a);
-                        float vf = (float)((double)af[k] + mean[q]);
+                        va = v1_a.add(va);
+                        float vf = mean[q].add(af[k]);
                         float out;
                         if (!a.output_increment) out = va;
                         else if (!a.applylog) out = __fsub_rn(va, vf);
@@ -387,6 +444,236 @@ __global__ void __launch_bounds__(UPD_NT) k_update_v2(UpdArgs a)
             int f = fe / m, e = fe - f * m;
             a.fields[((size_t)f * m + e) * a.plane + (size_t)jt * a.mni + i0 + c] = tile[idx];
         }
+    }
+}
+
+// das_updatefields, thread-per-cell form for nmem <= 64 (MT = nmem rounded
+// up to a multiple of 8).  A CTA of 4 warps owns UPC_NC = 16 consecutive
+// cells of one model row: lane l of warp w takes cell i0 + (l & 15) and
+// field-layer 2 w + (l >> 4) (then + 8, ...).  The j-interpolated transforms
+// of the strided columns those cells touch (Tjj, update.c:224-241) are
+// staged once in shared memory, rows padded to a multiple of 4 floats and
+// slots spaced 4 words mod 32 apart, so that lanes on different slots read
+// different banks with 16-byte loads and lanes on the same slot share a
+// broadcast; about 74 KB at nmem 48 and stride 3, three CTAs per SM.  Per
+// cell and layer the thread keeps the member values in registers: member
+// planes load and store coalesced over the 16 consecutive cells, and the
+// mean, the mean increment and the spread sums are sequential sums over
+// members in the reference's order -- no cross-lane reductions.  Each row of
+// A^a = X5 A is formed and written at once; with spread-capped inflation
+// (inf_ratio set) the rows are formed twice, first for the spread.  The FP64
+// variant forms the i-interpolated X5 element with the reference's float
+// operations (update.c:255-265); the FP32 variant contracts it into an FMA.
+#define UPC_NC 16
+#define UPC_NT 128
+template <bool F64, int MT>
+__device__ __forceinline__ float x5_row(const float* __restrict__ Ta, const float* __restrict__ Tb, int e1, int m4, int m,
+                                        float u1, float u2, const float (&x)[MT])
+{
+    const float4* ta = reinterpret_cast<const float4*>(Ta + e1 * m4);
+    const float4* tb = reinterpret_cast<const float4*>(Tb + e1 * m4);
+    float s = 0.0f;
+#pragma unroll
+    for (int q = 0; q < MT / 4; ++q) {
+        if (4 * q < m) {
+            const float4 p = ta[q], r = tb[q];
+            float t0, t1, t2, t3;
+            if constexpr (F64) {
+                t0 = __fadd_rn(__fmul_rn(p.x, u1), __fmul_rn(r.x, u2));
+                t1 = __fadd_rn(__fmul_rn(p.y, u1), __fmul_rn(r.y, u2));
+                t2 = __fadd_rn(__fmul_rn(p.z, u1), __fmul_rn(r.z, u2));
+                t3 = __fadd_rn(__fmul_rn(p.w, u1), __fmul_rn(r.w, u2));
+            } else {
+                t0 = fmaf(p.x, u1, r.x * u2);
+                t1 = fmaf(p.y, u1, r.y * u2);
+                t2 = fmaf(p.z, u1, r.z * u2);
+                t3 = fmaf(p.w, u1, r.w * u2);
+            }
+            s = fmaf(t0, x[4 * q], s);
+            s = fmaf(t1, x[4 * q + 1], s);
+            s = fmaf(t2, x[4 * q + 2], s);
+            s = fmaf(t3, x[4 * q + 3], s);
+        }
+    }
+    return s;
+}
+
+template <bool F64, int MT>
+__global__ void __launch_bounds__(UPC_NT) k_update_cells(UpdArgs a, int sstride)
+{
+    extern __shared__ __align__(16) float usm[];
+    const int m = a.m, md = a.md, st = a.stride, nf = a.nfield;
+    const int m4 = (m + 3) & ~3;
+    const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+    const int jt = blockIdx.y, jg = a.j1 + jt;
+    const int jj = a.j1 / st + jt / st, stepj = jt % st;
+    const int jj2 = (jj < a.nj - 1) ? jj + 1 : jj;
+    const int i0 = blockIdx.x * UPC_NC;
+    const int ilast = min(i0 + UPC_NC, a.mni) - 1;
+    const int s0 = i0 / st;
+    const int ns = ilast / st - s0 + 2;                      // staged slots (the last one: i-neighbour)
+    const int nsmax = (UPC_NC - 1) / st + 3;
+    float* Tjj = usm;                                        // [nsmax][sstride]: [md][m4] per slot
+    float* Wjj = usm + (size_t)nsmax * sstride;              // [nsmax][m4]
+
+    // 1. stage: staged slot k holds strided column g(k) = s0 + k, wrapped
+    //    (periodic) or clamped past the last column, j-interpolated; pads 0
+    {
+        const float w2 = __fdiv_rn((float)stepj, (float)st), w1 = __fsub_rn(1.0f, w2);
+        const bool jint = (st > 1 && stepj > 0);
+        const int per = md * m4;
+        for (int idx = tid; idx < ns * per; idx += UPC_NT) {
+            const int k = idx / per, r = idx - k * per;
+            const int e1 = r / m4, e = r - e1 * m4;
+            int g = s0 + k;
+            if (g >= a.ni) g = a.periodic_i ? g - a.ni : a.ni - 1;
+            float v = 0.0f;
+            if (e < m) {
+                v = __ldg(a.T + (((size_t)jj * a.ni + g) * md + e1) * m + e);
+                if (jint)
+                    v = __fadd_rn(__fmul_rn(v, w1), __fmul_rn(__ldg(a.T + (((size_t)jj2 * a.ni + g) * md + e1) * m + e), w2));
+            }
+            Tjj[(size_t)k * sstride + r] = v;
+        }
+        for (int idx = tid; idx < ns * m4; idx += UPC_NT) {
+            const int k = idx / m4, e = idx - k * m4;
+            int g = s0 + k;
+            if (g >= a.ni) g = a.periodic_i ? g - a.ni : a.ni - 1;
+            float v = 0.0f;
+            if (e < m) {
+                v = __ldg(a.w + ((size_t)jj * a.ni + g) * m + e);
+                if (jint) v = __fadd_rn(__fmul_rn(v, w1), __fmul_rn(__ldg(a.w + ((size_t)jj2 * a.ni + g) * m + e), w2));
+            }
+            Wjj[k * m4 + e] = v;
+        }
+    }
+    __syncthreads();
+
+    const int i = i0 + (lane & 15);
+    if (i > ilast) return;                                   // no barrier below
+    const int ii = i / st, stepi = i % st;
+    const bool iint = (st > 1 && stepi > 0);
+    const float u2 = iint ? __fdiv_rn((float)stepi, (float)st) : 0.0f;
+    const float u1 = iint ? __fsub_rn(1.0f, u2) : 1.0f;
+    const float* Ta = Tjj + (size_t)(ii - s0) * sstride;
+    const float* Tb = Ta + sstride;
+    const float* Wa = Wjj + (ii - s0) * m4;
+    const float* Wb = Wa + m4;
+    const int nl = a.numlevels[(size_t)jg * a.mni + i];
+    const size_t ioff = (size_t)jt * a.mni + i;
+    const bool capped = !isnan(a.inf_ratio);
+
+    for (int f = 2 * wid + (lane >> 4); f < nf; f += 2 * (UPC_NT / 32)) {
+        float* v = a.fields + (size_t)f * m * a.plane + ioff;   // member e at v[e * plane]
+        const int level = a.levels[f];
+        const bool masked = (a.surfk == 0) ? (nl <= level) : (nl <= (a.issurfacevar ? 0 : a.surfk - level));
+        if (masked) {
+            for (int e = 0; e < m; ++e) v[(size_t)e * a.plane] = 0.0f;
+            if (a.infl) a.infl[(size_t)f * a.plane + ioff] = 0.0f;
+            continue;
+        }
+        float x[MT];
+        int first = m;
+#pragma unroll
+        for (int e = 0; e < MT; ++e) {
+            x[e] = 0.0f;
+            if (e < m) x[e] = v[(size_t)e * a.plane];
+        }
+#pragma unroll
+        for (int e = 0; e < MT; ++e)
+            if (e < m && first == m && (!isfinite(x[e]) || fabsf(x[e]) > MAXOBSVAL_F)) first = e;
+        if (a.infl) a.infl[(size_t)f * a.plane + ioff] = 0.0f;
+        if (first < md) {
+            for (int e = 0; e < m; ++e) v[(size_t)e * a.plane] = 0.0f;
+            continue;
+        }
+        if (first < m) {
+            for (int e = md; e < m; ++e) v[(size_t)e * a.plane] = 0.0f;
+#pragma unroll
+            for (int e = 0; e < MT; ++e)
+                if (e >= md) x[e] = 0.0f;
+        }
+        // mean over the dynamic members (update.c:381-383)
+        Acc<F64> sm;
+#pragma unroll
+        for (int e = 0; e < MT; ++e)
+            if (e < md) sm.add(x[e]);
+        Mean<F64> mean;
+        mean.set(sm, md);
+        // anomalies (float) and the mean increment (update.c:381-410)
+        Acc<F64> sa;
+#pragma unroll
+        for (int e = 0; e < MT; ++e)
+            if (e < m) {
+                x[e] = mean.sub(x[e]);
+                const float wc = __fadd_rn(__fmul_rn(Wa[e], u1), __fmul_rn(Wb[e], u2));
+                sa.add_prod(x[e], wc);
+            }
+        const Mean<F64> v1_a = mean.plus(sa);
+        // hybrid rescaling factor (update.c:420-427)
+        const bool hyb = (a.mode == ENKFG_MODE_HYBRID);
+        const double k_d = (F64 && hyb && md > 1) ? sqrt((double)(m - 1) / (double)(md - 1)) : 1.0;
+        auto rescale = [&](float y) -> float {
+            if (!hyb) return y;
+            if constexpr (F64) return (float)((double)y / k_d);
+            else return __fmul_rn(y, a.inv_kd);
+        };
+        // spread-capped inflation (update.c:432-458): needs every row first
+        float inflation = a.inflation0;
+        if (capped) {
+            Acc<F64> s2f, s2a;
+#pragma unroll
+            for (int e = 0; e < MT; ++e)
+                if (e < md) {
+                    const float y = rescale(x[e]);
+                    s2f.add_prod(y, y);
+                }
+            for (int e1 = 0; e1 < md; ++e1) {
+                const float y = rescale(x5_row<F64, MT>(Ta, Tb, e1, m4, m, u1, u2, x));
+                s2a.add_prod(y, y);
+            }
+            if constexpr (F64) {
+                const double v2_f = s2f.value(), v2_a = s2a.value();
+                if (v2_a > 0.0) {
+                    inflation = (float)(sqrt(v2_f / v2_a) * a.inf_ratio + 1.0 - a.inf_ratio);
+                    if (inflation >= a.inflation0) inflation = a.inflation0;
+                }
+            } else {
+                const float v2_f = s2f.hi + s2f.lo, v2_a = s2a.hi + s2a.lo;
+                if (v2_a > 0.0f) {
+                    const float r = (float)a.inf_ratio;
+                    inflation = fmaf(sqrtf(__fdiv_rn(v2_f, v2_a)), r, 1.0f - r);
+                    if (inflation >= a.inflation0) inflation = a.inflation0;
+                }
+            }
+        }
+        const bool inflate = __fsub_rn(inflation, 1.0f) > 1.0e-6f;
+        if (!inflate) inflation = 1.0f;
+        // A^a = X5 A row by row (update.c:399) and the output (update.c:460-516)
+        for (int e1 = 0; e1 < md; ++e1) {
+            const float y = rescale(x5_row<F64, MT>(Ta, Tb, e1, m4, m, u1, u2, x));
+            float va = inflate ? __fmul_rn(y, inflation) : y;
+            va = v1_a.add(va);
+            float out;
+            if (!a.output_increment) out = va;
+            else {
+                // forecast member value (its anomaly, hybrid-rescaled, plus the mean)
+                float xf = 0.0f;
+#pragma unroll
+                for (int e = 0; e < MT; ++e)
+                    if (e == e1) xf = x[e];
+                const float vf = mean.add(rescale(xf));
+                if (!a.applylog) out = __fsub_rn(va, vf);
+                else {
+                    const float avf = fabsf(vf);
+                    const bool normal = (avf >= 1.17549435e-38f) && (avf <= 3.40282347e+38f);
+                    const double ea = pow(10.0, (double)va), ef = pow(10.0, (double)vf);
+                    out = normal ? (float)(ea - ef) : 0.0f;
+                }
+            }
+            v[(size_t)e1 * a.plane] = out;
+        }
+        if (a.infl) a.infl[(size_t)f * a.plane + ioff] = inflation;
     }
 }
 
@@ -456,9 +743,22 @@ enkfg_status run_hybrid(enkfg_ctx* ctx, int nmem, int nmem_d, double gamma, int 
     return ENKFG_OK;
 }
 
+// The field-layer levels of one launch group go to the device only when they
+// differ from the group last uploaded (no host-to-device copy in a steady
+// cycle, which CUDA graphs capture).  Synchronous copy: it is rare.
+static enkfg_status upload_levels(enkfg_ctx* ctx, const int* levels, int nf, int* d_levels)
+{
+    if (ctx->n_levels == nf && memcmp(ctx->h_levels, levels, nf * sizeof(int)) == 0) return ENKFG_OK;
+    CK(cudaMemcpy(d_levels, levels, nf * sizeof(int), cudaMemcpyHostToDevice));
+    memcpy(ctx->h_levels, levels, nf * sizeof(int));
+    ctx->n_levels = nf;
+    return ENKFG_OK;
+}
+
 enkfg_status run_update(enkfg_ctx* ctx, const enkfg_update_params* p, const int* d_numlevels, int nfield,
                         const int* levels, float* d_fields, float* d_infl, cudaStream_t st)
 {
+    enkfg_status s;
     if (!ctx->t_valid) {
         set_err(ctx, "no transforms in the context");
         return ENKFG_ESTATE;
@@ -503,12 +803,13 @@ enkfg_status run_update(enkfg_ctx* ctx, const enkfg_update_params* p, const int*
     a.T = ctx->d_T;
     a.w = ctx->d_w;
     a.plane = (size_t)a.jsize * a.mni;
+    a.inv_kd = (float)(1.0 / ((a.md > 1) ? sqrt((double)(a.m - 1) / (double)(a.md - 1)) : 1.0));
     int* d_levels = ctx->d_qhead + 64;       // up to 448 levels per launch group
     cudaEventRecord(ctx->ev[4], st);
     if (p->mode == ENKFG_MODE_ENOI) {
         for (int f0 = 0; f0 < nfield; f0 += 448) {
             int nf = nfield - f0 < 448 ? nfield - f0 : 448;
-            CK(cudaMemcpyAsync(d_levels, levels + f0, nf * sizeof(int), cudaMemcpyHostToDevice, st));
+            if ((s = upload_levels(ctx, levels + f0, nf, d_levels))) return s;
             a.levels = d_levels;
             a.nfield = nf;
             a.fields = d_fields + (size_t)f0 * (a.m + 1) * a.plane;
@@ -519,6 +820,45 @@ enkfg_status run_update(enkfg_ctx* ctx, const enkfg_update_params* p, const int*
         }
         cudaEventRecord(ctx->ev[5], st);
         return ENKFG_OK;
+    }
+    // thread-per-cell kernel (nmem <= 64) when its staged slots fit
+    if (a.m <= 64) {
+        const int MT = a.m <= 24 ? 24 : a.m <= 32 ? 32 : a.m <= 48 ? 48 : 64;
+        const int m4 = (a.m + 3) & ~3;
+        int sstride = a.md * m4;
+        sstride += (4 - sstride % 32 + 32) % 32;             // slot stride = 4 mod 32 words
+        const size_t nsmax = (size_t)(UPC_NC - 1) / a.stride + 3;
+        const size_t smem = (nsmax * sstride + nsmax * m4) * sizeof(float);
+        if (smem <= 200 * 1024) {
+            const bool f64 = (p->precision == ENKFG_PREC_FP64);
+            auto launch = [&](auto kern) -> enkfg_status {
+                CK(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+                for (int f0 = 0; f0 < nfield; f0 += 448) {
+                    int nf = nfield - f0 < 448 ? nfield - f0 : 448;
+                    if ((s = upload_levels(ctx, levels + f0, nf, d_levels))) return s;
+                    a.levels = d_levels;
+                    a.nfield = nf;
+                    a.fields = d_fields + (size_t)f0 * a.m * a.plane;
+                    a.infl = d_infl ? d_infl + (size_t)f0 * a.plane : nullptr;
+                    dim3 g(div_up(a.mni, UPC_NC), a.jsize);
+                    kern<<<g, UPC_NT, smem, st>>>(a, sstride);
+                    CKL();
+                    if (f0 + 448 < nfield) CK(cudaStreamSynchronize(st));
+                }
+                cudaEventRecord(ctx->ev[5], st);
+                return ENKFG_OK;
+            };
+            if (f64) {
+                if (MT == 24) return launch(k_update_cells<true, 24>);
+                if (MT == 32) return launch(k_update_cells<true, 32>);
+                if (MT == 48) return launch(k_update_cells<true, 48>);
+                return launch(k_update_cells<true, 64>);
+            }
+            if (MT == 24) return launch(k_update_cells<false, 24>);
+            if (MT == 32) return launch(k_update_cells<false, 32>);
+            if (MT == 48) return launch(k_update_cells<false, 48>);
+            return launch(k_update_cells<false, 64>);
+        }
     }
     if (a.m > 32 * MAXE_PER_LANE || a.md > 32 * MAXE_PER_LANE) {
         set_err(ctx, "nmem = %d too large for the update kernel", a.m);
@@ -555,7 +895,7 @@ enkfg_status run_update(enkfg_ctx* ctx, const enkfg_update_params* p, const int*
     a.nk = G * a.stride;
     for (int f0 = 0; f0 < nfield; f0 += fg) {
         int nf = nfield - f0 < fg ? nfield - f0 : fg;
-        CK(cudaMemcpyAsync(d_levels, levels + f0, nf * sizeof(int), cudaMemcpyHostToDevice, st));
+        if ((s = upload_levels(ctx, levels + f0, nf, d_levels))) return s;
         a.levels = d_levels;
         a.nfield = nf;
         a.fields = d_fields + (size_t)f0 * a.m * a.plane;

@@ -194,8 +194,12 @@ ENKFG_API enkfg_status enkfg_set_stream(enkfg_ctx* ctx, void* stream);
  * into the context, as enkfg_set_HE does from the host. */
 ENKFG_API enkfg_status enkfg_set_HE_dev(enkfg_ctx* ctx, int nmem, int nmem_dynamic, const float* HE_dev);
 
-/* Drop the spatial index so that the next transforms call rebuilds it
- * (obs_createkdtrees is part of every enkf_calc run, observations.c:1616). */
+/* Rebuild the spatial index now, on the context's stream (obs_createkdtrees
+ * is part of every enkf_calc run, observations.c:1616).  The build reads
+ * bucket counts back to the host, so it stays outside CUDA-graph capture; the
+ * calls after it (innovations, standardisation, transforms, update) can be
+ * captured, and the index's device buffers keep their addresses while the
+ * observation count does not grow. */
 ENKFG_API enkfg_status enkfg_rebuild_index(enkfg_ctx* ctx);
 
 /* Observation impact: adjoint of the local analysis (no counterpart in the
@@ -229,7 +233,9 @@ ENKFG_API enkfg_status enkfg_autotune_reset(enkfg_ctx* ctx);
 ENKFG_API long long enkfg_kernel_launches(const enkfg_ctx* ctx);
 /* Last stage timings in milliseconds, measured with CUDA events on the
  * launching stream: [0] index build, [1] count/queue, [2] transforms,
- * [3] update. */
+ * [3] update.  Read after the stream has finished the work (the _dev entry
+ * points return before it ends); stages run inside a CUDA graph keep the
+ * values of their last eager run. */
 ENKFG_API enkfg_status enkfg_stage_times(const enkfg_ctx* ctx, float* ms4);
 
 /* No counterpart in the reference.  CSR offsets of local-observation
