@@ -202,15 +202,17 @@ struct MixedSync {
     bool outstanding[2];
 };
 
-// HB: 8-column blocks of S'S each thread accumulates (half of the N columns
-// of its TMEM lane), held as double-floats in registers for the whole point.
+// HB: 8-column blocks of S'S each thread drains (half of the N columns of its
+// TMEM lane).  The double-float S'S lives in shared memory (Macc, m x lda
+// float2): a thread adds its own (row, column) entries at each drain, so no
+// registers are held across the point.
 //
 // TMEM: two accumulator sets (windows alternate), each [hi*hi' | rest] of N
 // columns: set s at columns 2 s N (hi*hi') and (2 s + 1) N (the other five
 // products).  A window collects up to MX_WIN observations; its hi*hi' sum is
 // exact in FP32 (every product is a multiple of q_r q_s below 2^16 of them),
 // the rest is 2^-8 of it or less.  A closed window is drained (tcgen05.ld,
-// TwoSum into the registers) one round later, while the next window runs.
+// TwoSum into Macc) one round later, while the next window runs.
 template <int HB>
 struct GramProcTC {
     const CalcArgs& a;
@@ -222,33 +224,12 @@ struct GramProcTC {
     int win_obs;       // observations in the current window
     int drain_set;     // closed window awaiting its drain (-1: none)
     int drain_buf;     // operand buffer whose commit closes it
-    float bhi, blo;    // S's for member threadIdx.x (double-float)
-    float2 acc[HB][8]; // S'S row 32*(warp%4)+lane, columns (warp/4)*half + [0, 8*HB)
+    float bh[4], bl[4]; // S's for member threadIdx.x: four double-float partial sums
     __device__ __forceinline__ GramProcTC(const CalcArgs& a_, const PointScratch& s_, MixedShared& ms_, MixedSync& sy_,
                                           uint32_t& rnd_)
-        : a(a_), s(s_), ms(ms_), sy(sy_), rnd(rnd_), win(0), win_obs(0), drain_set(-1), drain_buf(0), bhi(0.0f),
-          blo(0.0f)
+        : a(a_), s(s_), ms(ms_), sy(sy_), rnd(rnd_), win(0), win_obs(0), drain_set(-1), drain_buf(0)
     {
-#pragma unroll
-        for (int b = 0; b < HB; ++b)
-#pragma unroll
-            for (int j = 0; j < 8; ++j) acc[b][j] = make_float2(0.0f, 0.0f);
-    }
-
-    // write the accumulated S'S into the shared double-float matrix
-    __device__ __forceinline__ void store()
-    {
-        const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, m = a.m;
-        const int r = 32 * (wid & 3) + lane;
-        const int half = ms.N >> 1, c0 = (wid >> 2) * half;
-        if (r >= m) return;
-#pragma unroll
-        for (int b = 0; b < HB; ++b)
-#pragma unroll
-            for (int j = 0; j < 8; ++j) {
-                const int c = c0 + 8 * b + j;
-                if (8 * b < half && c < m) ms.Macc[r * ms.lda + c] = acc[b][j];
-            }
+        for (int j = 0; j < 4; ++j) bh[j] = bl[j] = 0.0f;
     }
 
     // bounded wait for the outstanding commit of operand buffer `buf`; on
@@ -270,16 +251,19 @@ struct GramProcTC {
         __syncthreads();
     }
 
-    // add accumulator set `set` to the registers (its MMAs have completed)
+    // add accumulator set `set` to the shared double-float S'S (its MMAs
+    // have completed); thread (warp w, lane l) owns row 32 (w % 4) + l and
+    // columns (w / 4) N/2 + [0, N/2)
     __device__ __forceinline__ void read_set(int set)
     {
-        const int wid = threadIdx.x >> 5;
+        const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
         if (*ms.err) return;
+        const int r = 32 * (wid & 3) + lane;
         if (32 * (wid & 3) < a.m) {
             const int half = ms.N >> 1;
             const int c0 = (wid >> 2) * half;
             const uint32_t base = ms.taddr + ((uint32_t)(32 * (wid & 3)) << 16) + (uint32_t)(2 * set * ms.N + c0);
-            // one 8-column block per TMEM round trip (register budget)
+            float2* row = ms.Macc + (size_t)(r < a.m ? r : 0) * ms.lda;
 #pragma unroll
             for (int b = 0; b < HB; ++b)
                 if (8 * b < half) {
@@ -287,10 +271,17 @@ struct GramProcTC {
                     tc::tmem_ld8_nowait(base + (uint32_t)(8 * b), vh);
                     tc::tmem_ld8_nowait(base + (uint32_t)(ms.N + 8 * b), vr);
                     tc::tmem_wait_ld();
+                    if (r < a.m) {
 #pragma unroll
-                    for (int j = 0; j < 8; ++j) {
-                        df_add(acc[b][j], __uint_as_float(vh[j]));
-                        acc[b][j].y += __uint_as_float(vr[j]);   // <= 2^-8 of hi*hi'
+                        for (int j = 0; j < 8; ++j) {
+                            const int c = c0 + 8 * b + j;
+                            if (c < a.m) {
+                                float2 acc = row[c];
+                                df_add(acc, __uint_as_float(vh[j]));
+                                acc.y += __uint_as_float(vr[j]);   // <= 2^-8 of hi*hi'
+                                row[c] = acc;
+                            }
+                        }
                     }
                 }
         }
@@ -377,7 +368,9 @@ struct GramProcTC {
         //    read the padding behind the tiles and land in accumulator rows
         //    that are never read.
         const int ngroups = (nc + 7) / 8;
-        if (tid == 0) {
+        // the issuing thread is in the last warp, so that S's (threads < m)
+        // runs at the same time
+        if (tid == CALC_NT - 32) {
             tc::fence_after();
             const uint32_t sbo = (uint32_t)kc * 32u, idesc = tc::idesc_tf32(MX_ROWS, ms.N);
             const uint32_t dhh = ms.taddr + (uint32_t)(2 * win * ms.N), dr = dhh + (uint32_t)ms.N;
@@ -399,15 +392,23 @@ struct GramProcTC {
         }
         sy.outstanding[buf] = true;
         ++rnd;
-        // 3. S's from the staged FP32 values (compensated FP32)
+        // 3. S's from the staged FP32 values (compensated FP32, four
+        //    independent double-float partial sums for ILP)
         if (tid < m) {
-            for (int k = 0; k < nc; ++k) {
-                float v = ms.tileV[k * ms.ldv + tid];
-                float x = ms.sl[k];
-                float p = v * x, pe = fmaf(v, x, -p);
-                float sm = bhi + p, bp = sm - bhi;
-                blo += ((bhi - (sm - bp)) + (p - bp)) + pe;
-                bhi = sm;
+            // unrolled by 4 (static partial-sum index; tileV and sl are zero
+            // past nc, so the padded tail adds nothing)
+            const int nc4 = (nc + 3) & ~3;
+            for (int k0 = 0; k0 < nc4; k0 += 4) {
+#pragma unroll
+                for (int j = 0; j < 4; ++j) {
+                    const int k = k0 + j;
+                    const float v = ms.tileV[k * ms.ldv + tid];
+                    const float x = ms.sl[k];
+                    const float p = v * x, pe = fmaf(v, x, -p);
+                    const float sm = bh[j] + p, bp = sm - bh[j];
+                    bl[j] += ((bh[j] - (sm - bp)) + (p - bp)) + pe;
+                    bh[j] = sm;
+                }
             }
         }
         // 4. the window closed one round ago: its last commit is on the other
@@ -562,7 +563,6 @@ __global__ void __launch_bounds__(CALC_NT) k_transforms_mixed(CalcArgs a, int kc
         const int p = (a.sxf != nullptr && a.ndim == 2) ? enumerate_obs<2>(a, ms.kc, qx, qy, qz, s, proc, true)
                                                         : enumerate_obs<1>(a, ms.kc, qx, qy, qz, s, proc, true);
         proc.finish();
-        proc.store();
         __syncthreads();
         if (*err) {
             if (tid == 0) a.status[pt] = MX_TIMEOUT_CODE;
@@ -578,7 +578,9 @@ __global__ void __launch_bounds__(CALC_NT) k_transforms_mixed(CalcArgs a, int kc
             float2 v2 = ((float2*)Macc)[i];
             Macc[i] = (double)v2.x + (double)v2.y;
         }
-        if (tid < m) b[tid] = (double)proc.bhi + (double)proc.blo;
+        if (tid < m)
+            b[tid] = (((double)proc.bh[0] + (double)proc.bh[1]) + ((double)proc.bh[2] + (double)proc.bh[3])) +
+                     (((double)proc.bl[0] + (double)proc.bl[1]) + ((double)proc.bl[2] + (double)proc.bl[3]));
         __syncthreads();
         const double trss = la::block_sum<CALC_NT>(tid < m ? Macc[tid * lda + tid] : 0.0, red);
         if (tid < m) Macc[tid * lda + tid] += 1.0;
