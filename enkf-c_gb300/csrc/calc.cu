@@ -138,7 +138,7 @@ __global__ void __launch_bounds__(CALC_NT) k_transforms(CalcArgs a)
     for (int it = 0;; ++it) {
         const int idx = next_item(a, it, ictl);
         if (idx < 0) break;
-        const int pt = a.order ? a.order[idx] : idx;
+        const int pt = a.order ? a.order[idx] : a.item0 + idx;
         int kc = a.kc;
         if (a.kc_table != nullptr && a.counts != nullptr) kc = a.kc_table[count_bin(a.counts[pt])];
         const double qx = a.qx[pt], qy = a.qy[pt], qz = a.ndim == 3 ? a.qz[pt] : 0.0;
@@ -152,6 +152,7 @@ __global__ void __launch_bounds__(CALC_NT) k_transforms(CalcArgs a)
         const int p = enumerate_obs<0>(a, kc, qx, qy, qz, s, proc, true);
         if (p == 0) {
             store_empty(a, pt);
+            if (a.defer && tid == 0) a.eaux[2 * (size_t)idx] = 0.0;
             __syncthreads();
             continue;
         }
@@ -173,7 +174,7 @@ __global__ void __launch_bounds__(CALC_NT) k_transforms(CalcArgs a)
         const double trss = la::block_sum<CALC_NT>(tid < m ? A[tid * LDA + tid] : 0.0, red);
         if (tid < m) A[tid * LDA + tid] += 1.0;
         __syncthreads();
-        solve_point(a, pt, p, kc, qx, qy, qz, A, LDA, b, trss, d, e, cs, sn, v, s, tile, TLD);
+        solve_point(a, pt, idx, p, kc, qx, qy, qz, A, LDA, b, trss, d, e, cs, sn, v, s, tile, TLD);
     }
 }
 
@@ -248,6 +249,27 @@ enkfg_status build_queue(enkfg_ctx* ctx, int npts, cudaStream_t st)
     return ENKFG_OK;
 }
 
+enkfg_status resident_ctas(enkfg_ctx* ctx, const void* fn, int nt, size_t dsmem, int* per_sm)
+{
+    cudaFuncAttributes fa;
+    int smem_sm = 0, reserved = 0, regs_sm = 0, thr_sm = 0, blk_sm = 0;
+    CK(cudaFuncGetAttributes(&fa, fn));
+    CK(cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, ctx->device));
+    CK(cudaDeviceGetAttribute(&reserved, cudaDevAttrReservedSharedMemoryPerBlock, ctx->device));
+    CK(cudaDeviceGetAttribute(&regs_sm, cudaDevAttrMaxRegistersPerMultiprocessor, ctx->device));
+    CK(cudaDeviceGetAttribute(&thr_sm, cudaDevAttrMaxThreadsPerMultiProcessor, ctx->device));
+    CK(cudaDeviceGetAttribute(&blk_sm, cudaDevAttrMaxBlocksPerMultiprocessor, ctx->device));
+    const size_t per_blk = dsmem + fa.sharedSizeBytes + (size_t)reserved;
+    int n = per_blk > 0 ? (int)((size_t)smem_sm / per_blk) : blk_sm;
+    const int warps = (nt + 31) / 32;
+    const int warp_regs = ((fa.numRegs * 32 + 255) / 256) * 256;   // allocation unit: 256 registers a warp
+    if (warp_regs > 0 && regs_sm / (warp_regs * warps) < n) n = regs_sm / (warp_regs * warps);
+    if (thr_sm / (warps * 32) < n) n = thr_sm / (warps * 32);
+    if (blk_sm < n) n = blk_sm;
+    *per_sm = n < 1 ? 1 : n;
+    return ENKFG_OK;
+}
+
 template <int R>
 static enkfg_status launch_R(enkfg_ctx* ctx, CalcArgs& a, cudaStream_t st)
 {
@@ -257,12 +279,15 @@ static enkfg_status launch_R(enkfg_ctx* ctx, CalcArgs& a, cudaStream_t st)
         return ENKFG_EUNSUPPORTED;
     }
     CK(cudaFuncSetAttribute(k_transforms<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    CK(cudaFuncSetAttribute(k_transforms<R>, cudaFuncAttributePreferredSharedMemoryCarveout, cudaSharedmemCarveoutMaxShared));
     int grid = a.nitems;
     if (a.persistent) {
+        // the residency count is computed rather than taken from the occupancy
+        // query, which reports one CTA per SM for these kernels where two run
         int per_sm = 0, nsm = 0;
-        CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_transforms<R>, CALC_NT, smem));
+        enkfg_status s = resident_ctas(ctx, (const void*)k_transforms<R>, CALC_NT, smem, &per_sm);
+        if (s) return s;
         CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, ctx->device));
-        if (per_sm < 1) per_sm = 1;
         grid = per_sm * nsm;
         if (grid > a.nitems) grid = a.nitems;
     }
@@ -361,6 +386,132 @@ static enkfg_status autotune(enkfg_ctx* ctx, CalcArgs a, int precision, cudaStre
     ctx->kc_tuned = true;
     ctx->kc_loaded = 3;
     ctx->kc_tuned_prec = precision;
+    return ENKFG_OK;
+}
+
+// ---------------------------------------------------------------------------
+// batched ETKF eigensolver.  The QL iteration of tql2 is a chain of dependent
+// FP64 operations on the tridiagonal alone; run inside the point's CTA it
+// leaves the SM idle (GB300 issues FP64 at 1/64 of the FP32 rate, so every
+// link costs tens of cycles).  Here the transform kernels stop an ETKF point
+// after tred2 (saving Q, the tridiagonal and S's), k_ql_batch runs the QL
+// chains with one thread per point, logging the rotations, and k_eig_finish
+// replays the rotations onto Q (rows in parallel) and forms T, w and the
+// diagnostics.  A point whose log would overflow, or whose QL does not
+// converge in the chain, takes tql2 in k_eig_finish instead.
+// ---------------------------------------------------------------------------
+#define QLB_T 32
+
+__global__ void __launch_bounds__(QLB_T) k_ql_batch(int nslots, int m, const double* __restrict__ eaux,
+                                                    const double* __restrict__ ed, const double* __restrict__ ee,
+                                                    double* __restrict__ eval, double2* __restrict__ rot, int rcap,
+                                                    int2* __restrict__ hdr, int hcap, int* __restrict__ nh)
+{
+    extern __shared__ double qsm[];   // [2][m][QLB_T]: one column of d and of e per thread
+    const int lane = threadIdx.x;
+    const int slot = blockIdx.x * QLB_T + lane;
+    if (slot >= nslots || !(eaux[2 * (size_t)slot] > 0.0)) return;   // no barrier below
+    double* dcol = qsm + lane;
+    double* ecol = qsm + (size_t)m * QLB_T + lane;
+    for (int i = 0; i < m; ++i) {
+        dcol[i * QLB_T] = ed[(size_t)slot * m + i];
+        ecol[i * QLB_T] = ee[(size_t)slot * m + i];
+    }
+    int n = 0;
+    const int stt = la::ql_chain(dcol, ecol, m, QLB_T, rot + (size_t)slot * rcap, rcap, hdr + (size_t)slot * hcap,
+                                 hcap, &n);
+    nh[slot] = stt == 0 ? n : -stt;
+    for (int i = 0; i < m; ++i) eval[(size_t)slot * m + i] = dcol[i * QLB_T];
+}
+
+__global__ void __launch_bounds__(CALC_NT) k_eig_finish(CalcArgs a, const double* __restrict__ eval,
+                                                        const double2* __restrict__ rot, int rcap,
+                                                        const int2* __restrict__ hdr, int hcap,
+                                                        const int* __restrict__ nh)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int m = a.m, lda = (m % 2 == 0) ? m + 1 : m + 2;
+    const int tid = threadIdx.x, slot = blockIdx.x;
+    double* A = (double*)smem_raw;
+    double* d = A + (size_t)m * lda;
+    double* e = d + m;
+    double* b = e + m;
+    double* cs = b + m;
+    double* sn = cs + m;
+    double* v = sn + m;
+    double* red = v + m;
+    int* ctl = (int*)(red + CALC_NT / 32);
+    const double pd = a.eaux[2 * (size_t)slot];
+    if (!(pd > 0.0)) return;   // empty point: written by the transform kernel
+    const int pt = a.order ? a.order[slot] : a.item0 + slot;
+    const double trss = a.eaux[2 * (size_t)slot + 1];
+    const int stt = nh[slot];
+    for (int i = tid; i < m * m; i += CALC_NT) {
+        const int r = i / m, c = i - r * m;
+        A[r * lda + c] = a.eq[(size_t)slot * m * m + i];
+    }
+    for (int i = tid; i < m; i += CALC_NT) {
+        b[i] = a.eb[(size_t)slot * m + i];
+        d[i] = stt >= 0 ? eval[(size_t)slot * m + i] : a.ed[(size_t)slot * m + i];
+        e[i] = a.ee[(size_t)slot * m + i];
+    }
+    __syncthreads();
+    int rc = 0;
+    if (stt >= 0) la::ql_replay<CALC_NT>(A, m, lda, rot + (size_t)slot * rcap, hdr + (size_t)slot * hcap, stt);
+    else rc = la::tql2<CALC_NT>(A, m, lda, d, e, cs, sn, ctl);
+    const double dfs = etkf_outputs(a, pt, A, lda, d, b, cs, sn, v, red);
+    if (rc != 0 && tid == 0) a.status[pt] = rc;
+    if (a.want_diag) diag_single(a, pt, (int)pd, dfs, trss);
+}
+
+static enkfg_status run_etkf_batched(enkfg_ctx* ctx, const CalcArgs& a0, int precision, cudaStream_t st)
+{
+    enkfg_status s;
+    const int m = a0.m, nitems = a0.nitems;
+    const int rcap = m * m + 64 * m;         // QL typically needs about 0.75 m^2 rotations
+    const int hcap = 8 * m;
+    const size_t per = (size_t)m * m * 8 + (size_t)5 * m * 8 + 16 + (size_t)rcap * 16 + (size_t)hcap * 8 + 4;
+    size_t B = ((size_t)2 << 30) / per;      // about 2 GB of scratch per batch
+    if (B < 256) B = 256;
+    if (B > (size_t)nitems) B = (size_t)nitems;
+    if ((s = ensure(ctx, &ctx->d_eq, &ctx->eq_cap, B * m * m))) return s;
+    if ((s = ensure(ctx, &ctx->d_ed, &ctx->ed_cap, B * m))) return s;
+    if ((s = ensure(ctx, &ctx->d_ee, &ctx->ee_cap, B * m))) return s;
+    if ((s = ensure(ctx, &ctx->d_eb, &ctx->eb_cap, B * m))) return s;
+    if ((s = ensure(ctx, &ctx->d_eaux, &ctx->eaux_cap, B * 2))) return s;
+    if ((s = ensure(ctx, &ctx->d_eval, &ctx->eval_cap, B * m))) return s;
+    if ((s = ensure(ctx, &ctx->d_erot, &ctx->erot_cap, B * rcap))) return s;
+    if ((s = ensure(ctx, &ctx->d_ehdr, &ctx->ehdr_cap, B * hcap))) return s;
+    if ((s = ensure(ctx, &ctx->d_enh, &ctx->enh_cap, B))) return s;
+    const size_t qsmem = (size_t)2 * m * QLB_T * 8;
+    const int lda = (m % 2 == 0) ? m + 1 : m + 2;
+    const size_t fsmem = ((size_t)m * lda + 6 * (size_t)m + CALC_NT / 32) * 8 + 16;
+    CK(cudaFuncSetAttribute(k_ql_batch, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)qsmem));
+    CK(cudaFuncSetAttribute(k_eig_finish, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fsmem));
+    for (int i0 = 0; i0 < nitems; i0 += (int)B) {
+        const int nb = (nitems - i0 < (int)B) ? nitems - i0 : (int)B;
+        CalcArgs b = a0;
+        b.defer = 1;
+        b.nitems = nb;
+        if (a0.order) {
+            b.order = a0.order + i0;
+            b.item0 = 0;
+        } else {
+            b.item0 = a0.item0 + i0;
+        }
+        b.eq = ctx->d_eq;
+        b.ed = ctx->d_ed;
+        b.ee = ctx->d_ee;
+        b.eb = ctx->d_eb;
+        b.eaux = ctx->d_eaux;
+        if (b.persistent) CK(cudaMemsetAsync(ctx->d_qhead, 0, sizeof(int), st));
+        if ((s = dispatch(ctx, b, precision, st))) return s;
+        k_ql_batch<<<div_up(nb, QLB_T), QLB_T, qsmem, st>>>(nb, m, ctx->d_eaux, ctx->d_ed, ctx->d_ee, ctx->d_eval,
+                                                           ctx->d_erot, rcap, ctx->d_ehdr, hcap, ctx->d_enh);
+        CKL();
+        k_eig_finish<<<nb, CALC_NT, fsmem, st>>>(b, ctx->d_eval, ctx->d_erot, rcap, ctx->d_ehdr, hcap, ctx->d_enh);
+        CKL();
+    }
     return ENKFG_OK;
 }
 
@@ -470,7 +621,14 @@ enkfg_status run_transforms(enkfg_ctx* ctx, const enkfg_calc_params* p, cudaStre
         CK(cudaMemsetAsync(ctx->d_qhead, 0, sizeof(int), st));
         cudaEventRecord(ctx->ev[2], st);
     }
-    if ((s = dispatch(ctx, a, p->precision, st))) return s;
+    // ETKF: the batched eigensolver (the per-type diagnostics need the
+    // point's own QL pass, so they keep the in-kernel one)
+    const bool defer = (p->mode != ENKFG_MODE_ENOI && p->scheme == ENKFG_SCHEME_ETKF && !(a.want_diag && a.ntypes > 1));
+    if (defer) {
+        if ((s = run_etkf_batched(ctx, a, p->precision, st))) return s;
+    } else {
+        if ((s = dispatch(ctx, a, p->precision, st))) return s;
+    }
     cudaEventRecord(ctx->ev[3], st);
     ctx->t_mode = p->mode;
     ctx->t_nmem = m;

@@ -46,6 +46,15 @@ struct CalcArgs {
     float* pdfs;
     float* psrf;
     int* status;
+    // batched ETKF eigensolver: with defer set, the transform kernels stop an
+    // ETKF point after the tridiagonalisation and save it in slot idx (the
+    // point's position in this launch); item0: first point when order is null
+    int defer, item0;
+    double* eq;        // [slots][m][m] Q of tred2
+    double* ed;        // [slots][m] tridiagonal: diagonal
+    double* ee;        // [slots][m] and off-diagonal (QL form)
+    double* eb;        // [slots][m] S's
+    double* eaux;      // [slots][2] local obs count p, tr(S'S)
 };
 
 __host__ __device__ static inline int count_bin(int p)
@@ -302,12 +311,68 @@ __device__ inline void store_empty(const CalcArgs& a, int pt)
     }
 }
 
+// ETKF outputs from the eigendecomposition M = Z diag(d) Z' (Z in the columns
+// of A): w = Z diag(1/d) Z' b, T = Z diag(d^-1/2) Z' relaxed by alpha and
+// cast (calcs.c:300-412, transforms.c:1270-1296).  cs, sn, v: scratch of m
+// doubles (cs = d^-1/2 and sn = 1/d on return).  Returns dfs = m - tr(M^-1).
+__device__ inline double etkf_outputs(const CalcArgs& a, int pt, const double* A, int lda, const double* d,
+                                      const double* b, double* cs, double* sn, double* v, double* red)
+{
+    const int tid = threadIdx.x, m = a.m, md = a.md;
+    const size_t tbase = (size_t)pt * md * m;
+    if (tid < m) {
+        double lam = d[tid];
+        cs[tid] = 1.0 / sqrt(lam);
+        sn[tid] = 1.0 / lam;
+        double c = 0.0;
+        for (int q = 0; q < m; ++q) c = fma(A[q * lda + tid], b[q], c);
+        v[tid] = c * sn[tid];
+    }
+    __syncthreads();
+    if (tid < m) {
+        double wv = 0.0;
+        for (int k = 0; k < m; ++k) wv = fma(A[tid * lda + k], v[k], wv);
+        a.w[(size_t)pt * m + tid] = (float)wv;
+        if (a.w64) a.w64[(size_t)pt * m + tid] = wv;
+    }
+    const double dfs = la::block_sum<CALC_NT>(tid < m ? 1.0 - sn[tid] : 0.0, red);
+    if (a.mode != ENKFG_MODE_ENOI && a.T != nullptr) {
+        for (int i = tid; i < md * m; i += CALC_NT) {
+            int e1 = i / m, e2 = i - e1 * m;
+            double t = 0.0;
+            const double* z1 = A + e1 * lda;
+            const double* z2 = A + e2 * lda;
+            for (int k = 0; k < m; ++k) t = fma(z1[k] * cs[k], z2[k], t);
+            if (e1 == e2) t = (t - 1.0) * a.alpha + 1.0;   // transforms.c:1276-1286
+            else t = t * a.alpha;
+            a.T[tbase + i] = (float)t;
+            if (a.T64) a.T64[tbase + i] = t;
+        }
+    }
+    return dfs;
+}
+
+// Diagnostics of a point when there is one observation type
+// (transforms.c:1298-1345): nlobs, dfs, srf and their per-type copies.
+__device__ inline void diag_single(const CalcArgs& a, int pt, int p, double dfs, double trss)
+{
+    float dfs_f = (float)dfs;
+    if (threadIdx.x == 0) {
+        a.nlobs[pt] = p;
+        a.dfs[pt] = dfs_f;
+        a.srf[pt] = (float)(sqrt(trss / (double)dfs_f) - 1.0);
+        a.pnlobs[pt] = p;
+        a.pdfs[pt] = dfs_f;
+        a.psrf[pt] = (dfs_f > 1.0e-6f) ? (float)(sqrt(trss / (double)dfs_f) - 1.0) : 0.0f;
+    }
+}
+
 // FP64 solve of one point from M = I + S'S in A (n = m, stride lda) and b =
 // S's, then relaxation, float cast and diagnostics.  A is overwritten (by the
 // eigenvectors, or by M^-1); tile/tld: FP64 chunk buffer for the per-type
 // pass.
-__device__ inline void solve_point(const CalcArgs& a, int pt, int p, int kc, double qx, double qy, double qz,
-                                   double* A, int lda, double* b, double trss, double* d, double* e,
+__device__ inline void solve_point(const CalcArgs& a, int pt, int slot, int p, int kc, double qx, double qy,
+                                   double qz, double* A, int lda, double* b, double trss, double* d, double* e,
                                    double* cs, double* sn, double* v, const PointScratch& s, double* tile, int tld)
 {
     const int tid = threadIdx.x, m = a.m, md = a.md;
@@ -317,38 +382,31 @@ __device__ inline void solve_point(const CalcArgs& a, int pt, int p, int kc, dou
     double dfs = 0.0;
     const double* Q;
     const double* gq;
+    if (!need_inv && a.defer) {
+        // batched eigensolver: tridiagonalise here, save the slot; the QL
+        // chains run one thread per point and the rest in k_eig_finish
+        la::tred2<CALC_NT>(A, m, lda, d, e, s.red);
+        const size_t q0 = (size_t)slot * m * m;
+        for (int i = tid; i < m * m; i += CALC_NT) {
+            const int r = i / m, c = i - r * m;
+            a.eq[q0 + i] = A[r * lda + c];
+        }
+        if (tid < m) {
+            a.ed[(size_t)slot * m + tid] = d[tid];
+            a.ee[(size_t)slot * m + tid] = e[tid];
+            a.eb[(size_t)slot * m + tid] = b[tid];
+        }
+        if (tid == 0) {
+            a.eaux[2 * (size_t)slot] = (double)p;
+            a.eaux[2 * (size_t)slot + 1] = trss;
+        }
+        __syncthreads();
+        return;
+    }
     if (!need_inv) {
         // ETKF (calcs.c:300-412): T = M^-1/2, w = M^-1 S's
         rc = la::eig_sym<CALC_NT>(A, m, lda, d, e, cs, sn, s.ictl + 16, s.red);
-        if (tid < m) {
-            double lam = d[tid];
-            cs[tid] = 1.0 / sqrt(lam);
-            sn[tid] = 1.0 / lam;
-            double c = 0.0;
-            for (int q = 0; q < m; ++q) c = fma(A[q * lda + tid], b[q], c);
-            v[tid] = c * sn[tid];
-        }
-        __syncthreads();
-        if (tid < m) {
-            double wv = 0.0;
-            for (int k = 0; k < m; ++k) wv = fma(A[tid * lda + k], v[k], wv);
-            a.w[(size_t)pt * m + tid] = (float)wv;
-            if (a.w64) a.w64[(size_t)pt * m + tid] = wv;
-        }
-        dfs = la::block_sum<CALC_NT>(tid < m ? 1.0 - sn[tid] : 0.0, s.red);
-        if (a.mode != ENKFG_MODE_ENOI && a.T != nullptr) {
-            for (int i = tid; i < md * m; i += CALC_NT) {
-                int e1 = i / m, e2 = i - e1 * m;
-                double t = 0.0;
-                const double* z1 = A + e1 * lda;
-                const double* z2 = A + e2 * lda;
-                for (int k = 0; k < m; ++k) t = fma(z1[k] * cs[k], z2[k], t);
-                if (e1 == e2) t = (t - 1.0) * a.alpha + 1.0;   // transforms.c:1276-1286
-                else t = t * a.alpha;
-                a.T[tbase + i] = (float)t;
-                if (a.T64) a.T64[tbase + i] = t;
-            }
-        }
+        dfs = etkf_outputs(a, pt, A, lda, d, b, cs, sn, v, s.red);
         Q = A;
         gq = sn;
     } else {
@@ -384,11 +442,7 @@ __device__ inline void solve_point(const CalcArgs& a, int pt, int p, int kc, dou
             a.srf[pt] = (float)(sqrt(trss / (double)dfs_f) - 1.0);
         }
         if (a.ntypes == 1) {
-            if (tid == 0) {
-                a.pnlobs[pt] = p;
-                a.pdfs[pt] = dfs_f;
-                a.psrf[pt] = (dfs_f > 1.0e-6f) ? (float)(sqrt(trss / (double)dfs_f) - 1.0) : 0.0f;
-            }
+            diag_single(a, pt, p, dfs, trss);
         } else {
             __syncthreads();
             QuadProc qp(a, s, tile, tld, Q, gq, lda);

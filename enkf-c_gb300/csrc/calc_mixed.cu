@@ -544,7 +544,7 @@ __global__ void __launch_bounds__(CALC_NT) k_transforms_mixed(CalcArgs a, int kc
     for (int it = 0;; ++it) {
         const int idx = next_item(a, it, ictl);
         if (idx < 0 || *err) break;
-        const int pt = a.order ? a.order[idx] : idx;
+        const int pt = a.order ? a.order[idx] : a.item0 + idx;
         const double qx = a.qx[pt], qy = a.qy[pt], qz = a.ndim == 3 ? a.qz[pt] : 0.0;
         // observations per round: 8 x (accumulators used), per count bin when tuned
         ms.kc = kcm;
@@ -570,6 +570,7 @@ __global__ void __launch_bounds__(CALC_NT) k_transforms_mixed(CalcArgs a, int kc
         }
         if (p == 0) {
             store_empty(a, pt);
+            if (a.defer && tid == 0) a.eaux[2 * (size_t)idx] = 0.0;
             __syncthreads();
             continue;
         }
@@ -586,7 +587,7 @@ __global__ void __launch_bounds__(CALC_NT) k_transforms_mixed(CalcArgs a, int kc
         if (tid < m) Macc[tid * lda + tid] += 1.0;
         __syncthreads();
         // the per-type pass reuses the operand tiles as its FP64 chunk buffer
-        solve_point(a, pt, p, ms.kc, qx, qy, qz, Macc, lda, b, trss, d, e, cs, sn, v, s, (double*)tiles, m);
+        solve_point(a, pt, idx, p, ms.kc, qx, qy, qz, Macc, lda, b, trss, d, e, cs, sn, v, s, (double*)tiles, m);
         if (a.want_diag && a.ntypes > 1) {
             for (size_t i = tid; i < ntile; i += CALC_NT) tiles[i] = 0.0f;
             __syncthreads();
@@ -601,12 +602,14 @@ static enkfg_status launch_mixed_hb(enkfg_ctx* ctx, CalcArgs& a, int kcm, int N,
                                     cudaStream_t st)
 {
     CK(cudaFuncSetAttribute(k_transforms_mixed<HB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    CK(cudaFuncSetAttribute(k_transforms_mixed<HB>, cudaFuncAttributePreferredSharedMemoryCarveout, cudaSharedmemCarveoutMaxShared));
     int grid = a.nitems;
     if (a.persistent) {
+        // computed residency (the occupancy query reports one CTA per SM here)
         int per_sm = 0, nsm = 0;
-        CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_transforms_mixed<HB>, CALC_NT, smem));
+        enkfg_status s = resident_ctas(ctx, (const void*)k_transforms_mixed<HB>, CALC_NT, smem, &per_sm);
+        if (s) return s;
         CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, ctx->device));
-        if (per_sm < 1) per_sm = 1;
         // TMEM: at most 512 columns per SM across resident CTAs
         while (per_sm > 1 && (uint32_t)per_sm * tcols > 512) --per_sm;
         grid = per_sm * nsm;

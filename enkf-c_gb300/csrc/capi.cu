@@ -110,7 +110,7 @@ ENKFG_API void enkfg_destroy(enkfg_ctx* ctx)
     if (!ctx) return;
     cudaSetDevice(ctx->device);
     cudaStreamSynchronize(ctx->stream);
-    void* ptrs[] = { ctx->d_lon, ctx->d_lat, ctx->d_type, ctx->d_status, ctx->d_estd, ctx->d_value, ctx->d_rfac, ctx->d_rfac_sqrt, ctx->d_gtmp, ctx->d_smax, ctx->d_qscale,
+    void* ptrs[] = { ctx->d_lon, ctx->d_lat, ctx->d_type, ctx->d_status, ctx->d_estd, ctx->d_value, ctx->d_rfac, ctx->d_rfac_sqrt, ctx->d_gtmp, ctx->d_smax, ctx->d_qscale, ctx->d_eq, ctx->d_ed, ctx->d_ee, ctx->d_eb, ctx->d_eaux, ctx->d_eval, ctx->d_erot, ctx->d_ehdr, ctx->d_enh,
                      ctx->d_S, ctx->d_s, ctx->d_std, ctx->d_types, ctx->d_bstart, ctx->d_bfill, ctx->d_key,
                      ctx->d_sid, ctx->d_sx, ctx->d_sy, ctx->d_sz, ctx->d_sxf, ctx->d_syf, ctx->d_stype, ctx->d_St, ctx->d_ss, ctx->d_ox,
                      ctx->d_oy, ctx->d_oz, ctx->d_qx, ctx->d_qy, ctx->d_qz, ctx->d_T, ctx->d_w, ctx->d_T64,

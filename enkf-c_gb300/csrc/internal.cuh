@@ -132,6 +132,18 @@ struct enkfg_ctx {
     float* d_psrf;
     size_t nlobs_cap, dfs_cap, srf_cap, pnlobs_cap, pdfs_cap, psrf_cap;
 
+    // batched ETKF eigensolver scratch (per slot of a batch of points)
+    double* d_eq;               // [slots][m][m]
+    double* d_ed;               // [slots][m]
+    double* d_ee;               // [slots][m]
+    double* d_eb;               // [slots][m]
+    double* d_eaux;             // [slots][2]
+    double* d_eval;             // [slots][m]
+    double2* d_erot;            // [slots][rcap]
+    int2* d_ehdr;               // [slots][hcap]
+    int* d_enh;                 // [slots]
+    size_t eq_cap, ed_cap, ee_cap, eb_cap, eaux_cap, eval_cap, erot_cap, ehdr_cap, enh_cap;
+
     // work queue / scratch
     int* d_counts;              // [npoints]
     int* d_order;               // [npoints]
@@ -205,6 +217,10 @@ enkfg_status build_gather(enkfg_ctx* ctx, cudaStream_t st);
 enkfg_status count_local(enkfg_ctx* ctx, int* d_counts, int* d_pcounts, cudaStream_t st);
 enkfg_status list_local(enkfg_ctx* ctx, const long long* d_offsets, int* d_ids, double* d_coeffs, cudaStream_t st);
 enkfg_status run_transforms(enkfg_ctx* ctx, const enkfg_calc_params* p, cudaStream_t st);
+// CTAs of `fn` (nt threads, dsmem bytes of dynamic shared memory) that fit on
+// one SM at once, from the shared memory (with the per-block reserve),
+// register and thread limits of the device.
+enkfg_status resident_ctas(enkfg_ctx* ctx, const void* fn, int nt, size_t dsmem, int* per_sm);
 enkfg_status run_update(enkfg_ctx* ctx, const enkfg_update_params* p, const int* d_numlevels, int nfield,
                         const int* levels, float* d_fields, float* d_infl, cudaStream_t st);
 enkfg_status run_innovations(enkfg_ctx* ctx, cudaStream_t st);

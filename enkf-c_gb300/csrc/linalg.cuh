@@ -36,13 +36,13 @@ __device__ __forceinline__ double block_sum(double v, double* red)
     return s;
 }
 
-// A: n x n, row stride lda, symmetric (both triangles valid on entry).
-// On return: column k of A is the eigenvector of eigenvalue d[k].
-// e, cs, sn: scratch of n doubles each; ctl: 4 ints; red: NT/32 doubles.
-// Returns 0 or 1 (QL did not converge).
+// Householder tridiagonalisation of the symmetric A (n x n, row stride lda,
+// both triangles valid on entry) with the transformations accumulated: on
+// return A holds the orthogonal Q, d the diagonal and e the off-diagonal of
+// the tridiagonal matrix in QL form (e[i] couples i and i+1, e[n-1] = 0).
+// red: NT/32 doubles.
 template <int NT>
-__device__ int eig_sym(double* A, int n, int lda, double* d, double* e, double* cs, double* sn, int* ctl,
-                       double* red)
+__device__ void tred2(double* A, int n, int lda, double* d, double* e, double* red)
 {
     const int tid = threadIdx.x;
     // ---- Householder reduction (rows n-1 .. 1) ----
@@ -133,12 +133,22 @@ __device__ int eig_sym(double* A, int n, int lda, double* d, double* e, double* 
         if (tid == 0) Ai[i] = 1.0;
         __syncthreads();
     }
-    // ---- implicit QL on (d, e) with rotations applied to the rows of A ----
     if (tid == 0) {
         for (int i = 1; i < n; ++i) e[i - 1] = e[i];
         e[n - 1] = 0.0;
-        ctl[3] = 0;
     }
+    __syncthreads();
+}
+
+// Implicit QL on the tridiagonal (d, e) of tred2 with the rotations applied to
+// the rows of A: on return column k of A is the eigenvector of eigenvalue
+// d[k].  cs, sn: scratch of n doubles each; ctl: 4 ints.  Returns 0 or 1 (QL
+// did not converge).
+template <int NT>
+__device__ int tql2(double* A, int n, int lda, double* d, double* e, double* cs, double* sn, int* ctl)
+{
+    const int tid = threadIdx.x;
+    if (tid == 0) ctl[3] = 0;
     __syncthreads();
     for (int l = 0; l < n; ++l) {
         int iter = 0;
@@ -221,6 +231,110 @@ __device__ int eig_sym(double* A, int n, int lda, double* d, double* e, double* 
         }
     }
     return ctl[3];
+}
+
+// A: n x n, row stride lda, symmetric (both triangles valid on entry).
+// On return: column k of A is the eigenvector of eigenvalue d[k].
+// e, cs, sn: scratch of n doubles each; ctl: 4 ints; red: NT/32 doubles.
+// Returns 0 or 1 (QL did not converge).
+template <int NT>
+__device__ int eig_sym(double* A, int n, int lda, double* d, double* e, double* cs, double* sn, int* ctl,
+                       double* red)
+{
+    tred2<NT>(A, n, lda, d, e, red);
+    return tql2<NT>(A, n, lda, d, e, cs, sn, ctl);
+}
+
+// The scalar part of tql2 for one point, run by one thread (batched over
+// points, one thread each): implicit QL on (d, e) (element i at d[i * ds],
+// e[i * ds]) with the same operations as tql2, leaving the eigenvalues in d.
+// The rotations are not applied; they are logged for ql_replay: rot[] gets
+// (c, s) of every rotation in order, hdr[] one (first, last) index pair per QL
+// sweep (rotations i = first down to last; first < last: none).  Returns 0,
+// 1 (no convergence) or 2 (the log capacity rcap / hcap was exceeded).
+__device__ inline int ql_chain(double* d, double* e, int n, int ds, double2* rot, int rcap, int2* hdr, int hcap,
+                               int* nh_out)
+{
+    int nr = 0, nh = 0;
+    for (int l = 0; l < n; ++l) {
+        int iter = 0;
+        for (;;) {
+            int mm;
+            for (mm = l; mm < n - 1; ++mm) {
+                const double dd = fabs(d[mm * ds]) + fabs(d[(mm + 1) * ds]);
+                if (fabs(e[mm * ds]) <= 2.220446049250313e-16 * dd) break;
+            }
+            if (mm == l) break;
+            if (iter >= 60) return 1;
+            ++iter;
+            if (nh >= hcap || nr + (mm - l) > rcap) return 2;
+            double g = (d[(l + 1) * ds] - d[l * ds]) / (2.0 * e[l * ds]);
+            double r = sqrt(fma(g, g, 1.0));
+            g = d[mm * ds] - d[l * ds] + e[l * ds] / (g + copysign(r, g));
+            double sv = 1.0, c = 1.0, p = 0.0;
+            int i;
+            bool underflow = false;
+            for (i = mm - 1; i >= l; --i) {
+                const double f = sv * e[i * ds], b = c * e[i * ds];
+                const double t = fma(f, f, g * g);
+                if (t == 0.0) {
+                    e[(i + 1) * ds] = 0.0;
+                    d[(i + 1) * ds] -= p;
+                    e[mm * ds] = 0.0;
+                    underflow = true;
+                    break;
+                }
+                const double ri = rsqrt(t);
+                r = t * ri;
+                e[(i + 1) * ds] = r;
+                sv = f * ri;
+                c = g * ri;
+                g = d[(i + 1) * ds] - p;
+                r = (d[i * ds] - g) * sv + 2.0 * c * b;
+                p = sv * r;
+                d[(i + 1) * ds] = g + p;
+                g = c * r - b;
+                rot[nr++] = make_double2(c, sv);
+            }
+            hdr[nh++] = make_int2(mm - 1, underflow ? i + 1 : l);
+            if (!underflow) {
+                d[l * ds] -= p;
+                e[l * ds] = g;
+                e[mm * ds] = 0.0;
+            }
+        }
+    }
+    *nh_out = nh;
+    return 0;
+}
+
+// Apply a ql_chain log to the rows of A (n x n, row stride lda; Q of tred2),
+// giving the eigenvectors in the columns as tql2 does.  Rows are
+// independent, one thread each; the log is read through the read-only cache
+// (every thread reads the same rotation: a broadcast).
+template <int NT>
+__device__ void ql_replay(double* A, int n, int lda, const double2* __restrict__ rot, const int2* __restrict__ hdr,
+                          int nh)
+{
+    for (int k = threadIdx.x; k < n; k += NT) {
+        double* Ak = A + (size_t)k * lda;
+        int r = 0;
+        for (int h = 0; h < nh; ++h) {
+            const int2 hl = __ldg(hdr + h);
+            if (hl.x >= hl.y) {
+                double carry = Ak[hl.x + 1];
+                for (int i = hl.x; i >= hl.y; --i) {
+                    const double2 q = __ldg(rot + r);
+                    ++r;
+                    const double zi = Ak[i];
+                    Ak[i + 1] = q.y * zi + q.x * carry;
+                    carry = q.x * zi - q.y * carry;
+                }
+                Ak[hl.y] = carry;
+            }
+        }
+    }
+    __syncthreads();
 }
 
 // In-place inverse of the SPD matrix A (n x n, row stride lda; the upper
