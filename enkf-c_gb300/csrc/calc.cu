@@ -249,7 +249,7 @@ enkfg_status build_queue(enkfg_ctx* ctx, int npts, cudaStream_t st)
     return ENKFG_OK;
 }
 
-enkfg_status resident_ctas(enkfg_ctx* ctx, const void* fn, int nt, size_t dsmem, int* per_sm)
+enkfg_status resident_ctas(enkfg_ctx* ctx, const void* fn, int nt, size_t dsmem, int* per_sm, int* carveout)
 {
     cudaFuncAttributes fa;
     int smem_sm = 0, reserved = 0, regs_sm = 0, thr_sm = 0, blk_sm = 0;
@@ -267,6 +267,9 @@ enkfg_status resident_ctas(enkfg_ctx* ctx, const void* fn, int nt, size_t dsmem,
     if (thr_sm / (warps * 32) < n) n = thr_sm / (warps * 32);
     if (blk_sm < n) n = blk_sm;
     *per_sm = n < 1 ? 1 : n;
+    const size_t need = (size_t)*per_sm * per_blk;
+    int pct = smem_sm > 0 ? (int)((need * 100 + (size_t)smem_sm - 1) / (size_t)smem_sm) : 100;
+    *carveout = pct > 100 ? 100 : pct;
     return ENKFG_OK;
 }
 
@@ -279,14 +282,16 @@ static enkfg_status launch_R(enkfg_ctx* ctx, CalcArgs& a, cudaStream_t st)
         return ENKFG_EUNSUPPORTED;
     }
     CK(cudaFuncSetAttribute(k_transforms<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    CK(cudaFuncSetAttribute(k_transforms<R>, cudaFuncAttributePreferredSharedMemoryCarveout, cudaSharedmemCarveoutMaxShared));
+    // the residency count is computed rather than taken from the occupancy
+    // query, which reports one CTA per SM for these kernels where two run;
+    // the carveout asks for just the shared memory those CTAs need
+    int per_sm = 0, carve = 100;
+    enkfg_status s = resident_ctas(ctx, (const void*)k_transforms<R>, CALC_NT, smem, &per_sm, &carve);
+    if (s) return s;
+    CK(cudaFuncSetAttribute(k_transforms<R>, cudaFuncAttributePreferredSharedMemoryCarveout, carve));
     int grid = a.nitems;
     if (a.persistent) {
-        // the residency count is computed rather than taken from the occupancy
-        // query, which reports one CTA per SM for these kernels where two run
-        int per_sm = 0, nsm = 0;
-        enkfg_status s = resident_ctas(ctx, (const void*)k_transforms<R>, CALC_NT, smem, &per_sm);
-        if (s) return s;
+        int nsm = 0;
         CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, ctx->device));
         grid = per_sm * nsm;
         if (grid > a.nitems) grid = a.nitems;
@@ -335,9 +340,11 @@ static enkfg_status autotune(enkfg_ctx* ctx, CalcArgs a, int precision, cudaStre
         free(counts);
         return cuda_fail(ctx, e, "autotune copy", __LINE__);
     }
+    // the mixed kernel's rounds are powers of two (8, 16 or 32 observations)
     static const int cand64[4] = { 8, 16, 32, 64 };
-    static const int candmx[4] = { 8, 16, 24, 32 };
+    static const int candmx[3] = { 8, 16, 32 };
     const int* cand = precision == ENKFG_PREC_MIXED ? candmx : cand64;
+    const int ncand = precision == ENKFG_PREC_MIXED ? 3 : 4;
     int table[NBINS];
     for (int b = 0; b < NBINS; ++b) table[b] = precision == ENKFG_PREC_MIXED ? 32 : (b < 4 ? 8 : b < 6 ? 16 : b < 9 ? 32 : 64);
     int* kct = ctx->d_qhead + 2 + NBINS;
@@ -352,7 +359,7 @@ static enkfg_status autotune(enkfg_ctx* ctx, CalcArgs a, int precision, cudaStre
         const int first = pos + (len - take) / 2;
         if (take >= 64 && bin >= 2) {
             float best = 1e30f;
-            for (int k = 0; k < 4; ++k) {
+            for (int k = 0; k < ncand; ++k) {
                 int tab[NBINS];
                 for (int q = 0; q < NBINS; ++q) tab[q] = cand[k];
                 cudaMemcpyAsync(kct, tab, sizeof(tab), cudaMemcpyHostToDevice, st);

@@ -1,38 +1,42 @@
-// calc_mixed.cu -- mixed-precision local-analysis transforms: S'S and S's on
-// the 5th-generation tensor cores (tcgen05, TF32 inputs, FP32 accumulation in
-// tensor memory), everything else in FP64 as in calc.cu.
+// calc_mixed.cu -- mixed-precision local-analysis transforms: S'S on the
+// 5th-generation tensor cores (tcgen05, TF32 inputs, FP32 accumulation in
+// tensor memory), S's in compensated FP32 on the CUDA cores, everything else
+// in FP64 as in calc.cu.
 //
-// Per round (chunk) of kc = 32 local observations:
-//   * the tapered rows of S (m members) are written to shared memory as a
-//     K-major operand tile (rows = members, K = observations), split into
-//     TF32 hi = rn(v) and lo = rn(v - hi), and kept as FP32 for S's;
-//   * one thread issues, for each group of 8 observations, three MMAs of
-//     shape M=128 x N x 8 (N = m rounded up to 16): hi*hi' into the group's
-//     TMEM accumulator, hi*lo' + lo*hi' into the round's cross-term one.  A
-//     and B are the same tile, so together they are the round's S'S;
-//   * the MMAs' completion is signalled by tcgen05.commit on the round's
-//     mbarrier.  Operand tiles are double buffered: while the tensor cores
-//     work on round c the CTA stages round c+1, then reads round c's
-//     accumulators out of TMEM (tcgen05.ld) and adds them, with error-free
-//     TwoSum steps, to double-float (hi + lo FP32) register accumulators.
-//     Each group of 8 observations has its own hi*hi' accumulator (nhh = 4
-//     per round, 2 when N > 96), so hi*hi' products are not summed inside
-//     the tensor core, whose FP32 accumulation truncates; the error stays at
-//     the level of the split itself (about 2^-22 relative per product);
-//   * S's is accumulated on the CUDA cores from the staged FP32 values, one
-//     member per thread, with TwoProduct/TwoSum compensated FP32
-//     (double-float) arithmetic.
+// Per local analysis (one CTA, persistent over a work queue):
+//   * the search appends accepted observations (position, FP32 taper) to a
+//     list segment of up to ~1000 entries; each full segment is consumed in
+//     rounds of kc = 32 observations before the search goes on;
+//   * the S rows of round j + 1 (mpad floats per observation) and their
+//     innovations are copied into shared memory with cp.async while round j
+//     is split and multiplied, so no round waits for its L2 gathers;
+//   * a round's tapered values v are split into hi = rint(v / q_r) q_r (q_r
+//     a power-of-two quantum per member, |hi / q_r| <= 256), mid = tf32(v -
+//     hi) and lo = tf32(v - hi - mid), written as K-major operand tiles;
+//   * one thread issues, per group of 8 observations, six MMAs of shape
+//     M=128 x N x 8 (N = m rounded up to 16): hi*hi' into an exact
+//     accumulator and hi*mid' + mid*hi' + hi*lo' + lo*hi' + mid*mid' into a
+//     second one.  Windows of up to 256 observations keep the hi*hi' sum
+//     exact in FP32 (every term is a multiple of q_r q_s, below 2^24 of
+//     them in total);
+//   * two TMEM accumulator sets alternate between windows; a closed window
+//     is read out (tcgen05.ld) one round later, while the next window's
+//     MMAs run, and added with TwoSum steps to a double-float (hi + lo FP32)
+//     S'S in shared memory;
+//   * operand tiles are double buffered: the MMAs of round j run while round
+//     j + 1 is staged; completion is signalled by tcgen05.commit on the
+//     buffer's mbarrier.
 //
-// The accumulators are then converted to FP64 and go through the same FP64
-// solve as the plain path (Householder + QL for ETKF, the symmetric sweep
-// inverse for DEnKF/EnOI).
+// The double-float S'S is then converted to FP64 and goes through the same
+// FP64 solve as the plain path (Householder + QL for ETKF, the symmetric
+// sweep inverse for DEnKF/EnOI).
 //
 // Shared-memory operand layout (canonical K-major, no swizzle): core matrices
 // of 8 rows x 16 bytes (4 TF32) stored as 128 contiguous bytes; core matrix
 // (row group g, K group q) at (g * kc/4 + q) * 128 bytes.  Descriptor:
 // leading (K) byte offset 128, stride (row-group) byte offset kc*32.
 //
-// Every wait on the MMA mbarrier is bounded; on expiry the CTA records an
+// Every wait on an MMA mbarrier is bounded; on expiry the CTA records an
 // error status for the point, stops, releases its TMEM and returns.
 #include "calc_common.cuh"
 
@@ -77,6 +81,30 @@ __device__ __forceinline__ void commit(uint64_t* mbar)
 {
     asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(mbar))
                  : "memory");
+}
+
+// Warp-collective forms: every lane of a converged warp passes the same
+// (warp-uniform) operands and elect.sync picks the one lane that issues --
+// always the same lane while the whole warp is active, so the commit tracks
+// that lane's MMAs.
+__device__ __forceinline__ void mma_tf32_warp(uint32_t dtmem, uint64_t da, uint64_t db, uint32_t idesc, uint32_t acc)
+{
+    asm volatile(
+        "{\n\t.reg .pred p, e;\n\t.reg .b32 r;\n\t"
+        "elect.sync r|e, 0xffffffff;\n\t"
+        "setp.ne.b32 p, %4, 0;\n\t"
+        "@e tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(dtmem),
+        "l"(da), "l"(db), "r"(idesc), "r"(acc));
+}
+
+__device__ __forceinline__ void commit_warp(uint64_t* mbar)
+{
+    asm volatile(
+        "{\n\t.reg .pred e;\n\t.reg .b32 r;\n\t"
+        "elect.sync r|e, 0xffffffff;\n\t"
+        "@e tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n\t}\n" ::"r"(
+            smem_u32(mbar))
+        : "memory");
 }
 
 __device__ __forceinline__ void fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
@@ -159,6 +187,24 @@ __device__ __forceinline__ float to_tf32(float x)
     return __uint_as_float(r);
 }
 
+// asynchronous global -> shared copies (16 bytes through L2 only, 8 bytes)
+__device__ __forceinline__ void cp_async16(void* dst, const void* src)
+{
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_u32(dst)),
+                 "l"((unsigned long long)__cvta_generic_to_global(src))
+                 : "memory");
+}
+
+__device__ __forceinline__ void cp_async8(void* dst, const void* src)
+{
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(smem_u32(dst)),
+                 "l"((unsigned long long)__cvta_generic_to_global(src))
+                 : "memory");
+}
+
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
+
 }  // namespace tc
 
 #define MX_KC 32            // observations per round
@@ -169,19 +215,29 @@ __device__ __forceinline__ float to_tf32(float x)
 // tf32(v - hi), lo = tf32(v - hi - mid).
 #define MX_PIECES 3
 
+// (Base pointers and strides rather than arrays of pointers: an array indexed
+// by the buffer number would live in local memory.)
 struct MixedShared {
-    float* tile[2][MX_PIECES]; // [buffer][piece]: N rows x kc, core-matrix layout
-    float* tileV;          // [kc][ldv] tapered S of the round being staged (FP32)
-    int ldv;               // row stride of tileV: >= m, = 8 mod 32 (conflict-free staging)
+    float* tiles;          // [buffer][piece][N x kc], core-matrix layout
+    int piece;             // floats per piece tile
+    float* raw;            // [buffer][kcm][ldv] untapered S rows of a round (cp.async)
+    int rawsz;             // floats per raw buffer
+    double* sraw;          // [buffer][kcm] innovations of those observations (cp.async)
+    int kcm;
+    int ldv;               // row stride of raw: >= mpad, = 8 mod 32 (conflict-free reads)
     const float* qs;       // [2][m]: quantum q_r and 1/q_r
     float2* Macc;          // [m x lda] double-float S'S (later reused as FP64)
     int lda;
     float* sl;             // [kc] tapered innovations of the round
+    float* lr;             // [kc] taper coefficients of the round (0 past its end)
     uint64_t* mbar;        // [2] one per operand buffer
     uint32_t taddr;
     int N;                 // MMA N (m rounded up to 16)
     int kc;                // observations per round
     int* err;              // shared error flag
+    __device__ __forceinline__ float* tile(int buf, int pc) const { return tiles + (buf * MX_PIECES + pc) * piece; }
+    __device__ __forceinline__ float* rawb(int rb) const { return raw + rb * rawsz; }
+    __device__ __forceinline__ double* srawb(int rb) const { return sraw + rb * kcm; }
 };
 
 // error-free (TwoSum) accumulation of x into the double-float (a.x + a.y)
@@ -194,12 +250,19 @@ __device__ __forceinline__ void df_add(float2& a, float x)
     a.y += e;
 }
 
-// mbarrier bookkeeping of the two operand buffers, kept across points:
-// parity of the next completion to wait for, and whether a commit is
-// outstanding
+// mbarrier bookkeeping of the two operand buffers, kept across points: bit
+// b of `phase` is the parity of buffer b's next completion, bit b of `out`
+// says whether a commit on it is outstanding
 struct MixedSync {
-    uint32_t phase[2];
-    bool outstanding[2];
+    uint32_t phase;
+    uint32_t out;
+    __device__ __forceinline__ bool outstanding(int b) const { return (out >> b) & 1u; }
+    __device__ __forceinline__ uint32_t parity(int b) const { return (phase >> b) & 1u; }
+    __device__ __forceinline__ void completed(int b)
+    {
+        phase ^= 1u << b;
+        out &= ~(1u << b);
+    }
 };
 
 // HB: 8-column blocks of S'S each thread drains (half of the N columns of its
@@ -224,11 +287,17 @@ struct GramProcTC {
     int win_obs;       // observations in the current window
     int drain_set;     // closed window awaiting its drain (-1: none)
     int drain_buf;     // operand buffer whose commit closes it
-    float bh[4], bl[4]; // S's for member threadIdx.x: four double-float partial sums
+    int sgroups;       // S's thread groups: CALC_NT / (m rounded up to 32)
+    int s_g, s_r;      // this thread's group and member
+    float bh[4], bl[4]; // S's for member s_r, group s_g: four double-float partial sums
     __device__ __forceinline__ GramProcTC(const CalcArgs& a_, const PointScratch& s_, MixedShared& ms_, MixedSync& sy_,
                                           uint32_t& rnd_)
         : a(a_), s(s_), ms(ms_), sy(sy_), rnd(rnd_), win(0), win_obs(0), drain_set(-1), drain_buf(0)
     {
+        const int mr = (a.m + 31) & ~31;
+        sgroups = CALC_NT / mr;
+        s_g = (int)threadIdx.x / mr;
+        s_r = (int)threadIdx.x - s_g * mr;
         for (int j = 0; j < 4; ++j) bh[j] = bl[j] = 0.0f;
     }
 
@@ -238,14 +307,13 @@ struct GramProcTC {
     // thread sees the same error flag.
     __device__ __forceinline__ void wait_buf(int buf)
     {
-        if (sy.outstanding[buf]) {
-            bool done = tc::mbar_wait_bounded(ms.mbar + buf, sy.phase[buf]);
+        if (sy.outstanding(buf)) {
+            bool done = tc::mbar_wait_bounded(ms.mbar + buf, sy.parity(buf));
             if (!done) {
                 atomicExch(ms.err, 1);
-                tc::mbar_wait_bounded(ms.mbar + buf, sy.phase[buf]);
+                tc::mbar_wait_bounded(ms.mbar + buf, sy.parity(buf));
             }
-            sy.phase[buf] ^= 1u;
-            sy.outstanding[buf] = false;
+            sy.completed(buf);
         }
         tc::fence_after();
         __syncthreads();
@@ -288,73 +356,97 @@ struct GramProcTC {
         tc::fence_before();
     }
 
-    __device__ void chunk(int nc, int t)
+    // issue the asynchronous copies of a round's S rows (mpad floats each,
+    // 16-byte pieces) and innovations into raw buffer rb; rows past nc are
+    // zeroed with plain stores
+    __device__ __forceinline__ void stage_rows(const int* lid, int base, int nc, int rb)
+    {
+        const int tid = threadIdx.x, kc = ms.kc, m4 = a.mpad >> 2;
+        float* dst = ms.rawb(rb);
+        for (int i = tid; i < kc * m4; i += CALC_NT) {
+            const int k = i / m4, c = i - k * m4;
+            float* d = dst + k * ms.ldv + 4 * c;
+            if (k < nc) tc::cp_async16(d, a.St + (size_t)lid[base + k] * a.mpad + 4 * c);
+            else *reinterpret_cast<float4*>(d) = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        }
+        if (tid < kc) {
+            double* d = ms.srawb(rb) + tid;
+            if (tid < nc) tc::cp_async8(d, a.ss + lid[base + tid]);
+            else *d = 0.0;
+        }
+        tc::cp_async_commit();
+    }
+
+    // one round: nc (<= kc) observations at list positions [base, base + nc)
+    // whose rows are in raw buffer rb
+    __device__ void round(const float* lcf, int base, int nc, int t, int rb)
     {
         const int tid = threadIdx.x;
         const int m = a.m, kc = ms.kc;
         const bool tsum = a.want_diag && a.ntypes > 1;
         double ssq = 0.0;
-        if (*ms.err) return;
         const int buf = (int)(rnd & 1u);
         // 0. this operand buffer's previous MMAs were waited for at the end of
         //    the last round (this only acts on the first round after an error)
-        if (sy.outstanding[buf]) {
+        if (sy.outstanding(buf)) {
             wait_buf(buf);
             if (*ms.err) return;
         }
-        float* tH = ms.tile[buf][0];
-        float* tM = ms.tile[buf][1];
-        float* tL = ms.tile[buf][2];
-        // 1. tapered S rows of the round: hi / mid / lo pieces into this
-        //    round's operand tiles, FP32 copy for S's; tapered innovations
-        const float* lcf = reinterpret_cast<const float*>(s.llc);   // FP32 taper (enumerate_obs<1 or 2>)
+        float* tH = ms.tile(buf, 0);
+        float* tM = ms.tile(buf, 1);
+        float* tL = ms.tile(buf, 2);
+        const float* raw = ms.rawb(rb);
         const float* q = ms.qs;
         const float* iq = ms.qs + m;
-        if (tid < kc) ms.sl[tid] = (tid < nc) ? (float)a.ss[s.lid[tid]] * lcf[tid] : 0.0f;
-        // one warp per core matrix (8 rows x 4 observations = 128 bytes):
-        // lane -> row r&7 = lane>>2, observation k&3 = lane&3, so the three
-        // piece stores are conflict-free; rows >= m stay zero.  (Two copies of
-        // the loop: an FP64 sum under a runtime flag inside the common loop
-        // would issue on the FP64 pipe even when off.)
+        // 1. taper and tapered innovations of the round (zero past nc)
+        if (tid < kc) {
+            const float c = tid < nc ? lcf[base + tid] : 0.0f;
+            ms.lr[tid] = c;
+            ms.sl[tid] = tid < nc ? (float)ms.srawb(rb)[tid] * c : 0.0f;
+        }
+        // tapered S: hi / mid / lo pieces into this round's operand tiles.
+        // One warp per core matrix (8 rows x 4 observations = 128 bytes):
+        // lane -> row r&7 = lane>>2, observation k&3 = lane&3, so the piece
+        // stores and the raw reads (row stride = 8 mod 32) are conflict-free;
+        // rows >= m stay zero.  kc is a power of two, so warp w keeps one
+        // K group (observations 4 kg .. 4 kg + 3, one taper per thread) and
+        // walks the row groups.  Rows of raw past nc are zero.  (Two copies
+        // of the loop: an FP64 sum under a runtime flag inside the common
+        // loop would issue on the FP64 pipe even when off.)
         {
             const int lane = tid & 31, wid = tid >> 5;
-            const int nrg = (m + 7) >> 3, nkg = kc >> 2, ncm = nrg * nkg;
-            const int ldv = ms.ldv;
+            const int nrg = (m + 7) >> 3, nkg = kc >> 2;
+            const int kg = wid & (nkg - 1), rg0 = wid / nkg, rstep = (CALC_NT / 32) / nkg;
+            const int k = (kg << 2) + (lane & 3);
+            const float ck = k < nc ? lcf[base + k] : 0.0f;
+            const float* rp = raw + k * ms.ldv + (lane >> 2);
             if (tsum) {
-                for (int c = wid; c < ncm; c += CALC_NT / 32) {
-                    const int rg = c / nkg, kg = c - rg * nkg;
-                    const int r = (rg << 3) + (lane >> 2), k = (kg << 2) + (lane & 3);
+                for (int rg = rg0; rg < nrg; rg += rstep) {
+                    const int r = (rg << 3) + (lane >> 2);
                     if (r < m) {
-                        float v = 0.0f;
-                        if (k < nc) {
-                            v = __fmul_rn(__ldg(a.St + (size_t)s.lid[k] * a.mpad + r), lcf[k]);
-                            ssq += (double)v * (double)v;
-                        }
+                        const float v = __fmul_rn(rp[rg << 3], ck);
+                        ssq += (double)v * (double)v;
                         const float hi = __fmul_rn(rintf(__fmul_rn(v, iq[r])), q[r]);
                         const float r1 = __fsub_rn(v, hi);
                         const float md = tc::to_tf32(r1);
-                        const int off = (c << 5) + lane;
+                        const int off = ((rg * nkg + kg) << 5) + lane;
                         tH[off] = hi;
                         tM[off] = md;
                         tL[off] = tc::to_tf32(__fsub_rn(r1, md));
-                        ms.tileV[k * ldv + r] = v;
                     }
                 }
             } else {
-                for (int c = wid; c < ncm; c += CALC_NT / 32) {
-                    const int rg = c / nkg, kg = c - rg * nkg;
-                    const int r = (rg << 3) + (lane >> 2), k = (kg << 2) + (lane & 3);
+                for (int rg = rg0; rg < nrg; rg += rstep) {
+                    const int r = (rg << 3) + (lane >> 2);
                     if (r < m) {
-                        float v = 0.0f;
-                        if (k < nc) v = __fmul_rn(__ldg(a.St + (size_t)s.lid[k] * a.mpad + r), lcf[k]);
+                        const float v = __fmul_rn(rp[rg << 3], ck);
                         const float hi = __fmul_rn(rintf(__fmul_rn(v, iq[r])), q[r]);
                         const float r1 = __fsub_rn(v, hi);
                         const float md = tc::to_tf32(r1);
-                        const int off = (c << 5) + lane;
+                        const int off = ((rg * nkg + kg) << 5) + lane;
                         tH[off] = hi;
                         tM[off] = md;
                         tL[off] = tc::to_tf32(__fsub_rn(r1, md));
-                        ms.tileV[k * ldv + r] = v;
                     }
                 }
             }
@@ -368,41 +460,43 @@ struct GramProcTC {
         //    read the padding behind the tiles and land in accumulator rows
         //    that are never read.
         const int ngroups = (nc + 7) / 8;
-        // the issuing thread is in the last warp, so that S's (threads < m)
-        // runs at the same time
-        if (tid == CALC_NT - 32) {
+        // the last warp issues (one elected lane), so that the S's of the
+        // first warps runs at the same time
+        if ((tid >> 5) == CALC_NT / 32 - 1) {
             tc::fence_after();
             const uint32_t sbo = (uint32_t)kc * 32u, idesc = tc::idesc_tf32(MX_ROWS, ms.N);
             const uint32_t dhh = ms.taddr + (uint32_t)(2 * win * ms.N), dr = dhh + (uint32_t)ms.N;
-            const uint32_t h0 = tc::smem_u32(tH), m0 = tc::smem_u32(tM), l0 = tc::smem_u32(tL);
-            for (int g = 0; g < ngroups; ++g) {
-                const uint32_t off = (uint32_t)g * 256u;    // two 128-byte core matrices per group of 8
-                const uint64_t dh = tc::desc_kmajor_noswizzle(h0 + off, 128u, sbo);
-                const uint64_t dm = tc::desc_kmajor_noswizzle(m0 + off, 128u, sbo);
-                const uint64_t dl = tc::desc_kmajor_noswizzle(l0 + off, 128u, sbo);
+            // a group of 8 observations is two 128-byte core matrices further
+            // on: 256 bytes, 16 in the descriptor's address field (addresses
+            // below 256 KB do not carry out of the field)
+            uint64_t dh = tc::desc_kmajor_noswizzle(tc::smem_u32(tH), 128u, sbo);
+            uint64_t dm = tc::desc_kmajor_noswizzle(tc::smem_u32(tM), 128u, sbo);
+            uint64_t dl = tc::desc_kmajor_noswizzle(tc::smem_u32(tL), 128u, sbo);
+            for (int g = 0; g < ngroups; ++g, dh += 16u, dm += 16u, dl += 16u) {
                 const uint32_t fresh = (win_obs == 0 && g == 0) ? 0u : 1u;
-                tc::mma_tf32(dhh, dh, dh, idesc, fresh);
-                tc::mma_tf32(dr, dh, dm, idesc, fresh);
-                tc::mma_tf32(dr, dm, dh, idesc, 1u);
-                tc::mma_tf32(dr, dh, dl, idesc, 1u);
-                tc::mma_tf32(dr, dl, dh, idesc, 1u);
-                tc::mma_tf32(dr, dm, dm, idesc, 1u);
+                tc::mma_tf32_warp(dhh, dh, dh, idesc, fresh);
+                tc::mma_tf32_warp(dr, dh, dm, idesc, fresh);
+                tc::mma_tf32_warp(dr, dm, dh, idesc, 1u);
+                tc::mma_tf32_warp(dr, dh, dl, idesc, 1u);
+                tc::mma_tf32_warp(dr, dl, dh, idesc, 1u);
+                tc::mma_tf32_warp(dr, dm, dm, idesc, 1u);
             }
-            tc::commit(ms.mbar + buf);
+            tc::commit_warp(ms.mbar + buf);
         }
-        sy.outstanding[buf] = true;
+        sy.out |= 1u << buf;
         ++rnd;
-        // 3. S's from the staged FP32 values (compensated FP32, four
-        //    independent double-float partial sums for ILP)
-        if (tid < m) {
-            // unrolled by 4 (static partial-sum index; tileV and sl are zero
-            // past nc, so the padded tail adds nothing)
-            const int nc4 = (nc + 3) & ~3;
-            for (int k0 = 0; k0 < nc4; k0 += 4) {
+        // 3. S's from the staged rows (compensated FP32): thread group g of
+        //    sgroups takes member r = tid - g mr and observations g, g + G,
+        //    ...; four independent double-float partial sums for ILP.  Raw
+        //    rows, lr and sl are zero past nc, so the tail adds nothing.
+        if (s_r < m && s_g < sgroups) {
+            const int G = sgroups;
+            for (int k0 = s_g; k0 < kc; k0 += 4 * G) {
 #pragma unroll
                 for (int j = 0; j < 4; ++j) {
-                    const int k = k0 + j;
-                    const float v = ms.tileV[k * ms.ldv + tid];
+                    const int k = k0 + j * G;
+                    if (k >= kc) break;
+                    const float v = __fmul_rn(raw[k * ms.ldv + s_r], ms.lr[k]);
                     const float x = ms.sl[k];
                     const float p = v * x, pe = fmaf(v, x, -p);
                     const float sm = bh[j] + p, bp = sm - bh[j];
@@ -432,19 +526,49 @@ struct GramProcTC {
         }
         // 6. the previous round's MMAs (the other operand buffer, which the
         //    next round stages into) ran during this round: wait for them
-        //    here, under the round's closing barrier
-        if (sy.outstanding[buf ^ 1]) {
-            bool done = tc::mbar_wait_bounded(ms.mbar + (buf ^ 1), sy.phase[buf ^ 1]);
+        //    here, and for this thread's copies of the next round's rows,
+        //    under the round's closing barrier
+        if (sy.outstanding(buf ^ 1)) {
+            bool done = tc::mbar_wait_bounded(ms.mbar + (buf ^ 1), sy.parity(buf ^ 1));
             if (!done) {
                 atomicExch(ms.err, 1);
-                tc::mbar_wait_bounded(ms.mbar + (buf ^ 1), sy.phase[buf ^ 1]);
+                tc::mbar_wait_bounded(ms.mbar + (buf ^ 1), sy.parity(buf ^ 1));
             }
-            sy.phase[buf ^ 1] ^= 1u;
-            sy.outstanding[buf ^ 1] = false;
+            sy.completed(buf ^ 1);
             tc::fence_after();
         }
+        tc::cp_async_wait_all();
         __syncthreads();
     }
+
+    // the rounds of a list segment of n entries of type t: all of them when
+    // `final`, else the whole rounds (the rest stays for the next segment).
+    // The rows of round j + 1 are copied in while round j is split and
+    // multiplied.  Returns the entries consumed.
+    __device__ int segment(const int* lid, const float* lcf, int n, int t, bool final)
+    {
+        const int kc = ms.kc;
+        const int nr = final ? (n + kc - 1) / kc : n / kc;
+        const int used = final ? n : nr * kc;
+        if (nr == 0 || *ms.err) return used;
+        stage_rows(lid, 0, n < kc ? n : kc, 0);
+        tc::cp_async_wait_all();
+        __syncthreads();
+        for (int j = 0; j < nr; ++j) {
+            const int base = j * kc, rb = j & 1;
+            const int nc = (n - base < kc) ? n - base : kc;
+            if (j + 1 < nr) {
+                const int nn = n - base - kc;
+                stage_rows(lid, base + kc, nn < kc ? nn : kc, rb ^ 1);
+            }
+            round(lcf, base, nc, t, rb);
+            if (*ms.err) break;
+        }
+        tc::cp_async_wait_all();   // nothing in flight after an early exit
+        __syncthreads();
+        return used;
+    }
+
     // drain what is left (after the enumeration; also after an error, so that
     // no MMA is in flight when TMEM is released)
     __device__ __forceinline__ void finish()
@@ -460,6 +584,184 @@ struct GramProcTC {
     __device__ __forceinline__ void type_end(int) {}
 };
 
+// Warp 0: the neighbour cells of the query (up to 9 in 2-D, 27 in 3-D), in
+// the order calc_neighbours visits them (z, then y, then x ascending), one
+// lane each: sb0[j] = first sorted position of the j-th existing cell's
+// bucket, scum[j] = sizes of the buckets before it, scum[nb] = their total,
+// scum[28] = nb.
+__device__ __forceinline__ void neighbour_ranges(const CalcArgs& a, const TypeIndex& t, double qx, double qy,
+                                                 double qz, long long* sb0, int* scum)
+{
+    const int lane = threadIdx.x & 31, ndim = a.ndim;
+    const double fx = floor((qx - t.x0) * t.inv_cell), fy = floor((qy - t.y0) * t.inv_cell);
+    const double fz = ndim == 3 ? floor((qz - t.z0) * t.inv_cell) : 0.0;
+    bool inside = fx >= -1.0 && fx <= (double)t.ncx && fy >= -1.0 && fy <= (double)t.ncy;
+    if (ndim == 3) inside = inside && fz >= -1.0 && fz <= (double)t.ncz;
+    bool valid = false;
+    long long b0 = 0;
+    int sz = 0;
+    if (inside && lane < (ndim == 3 ? 27 : 9)) {
+        const int cx = (int)fx, cy = (int)fy, cz = (int)fz;
+        const int r9 = ndim == 3 ? lane % 9 : lane;
+        const int z = ndim == 3 ? cz + lane / 9 - 1 : 0, y = cy + r9 / 3 - 1, x = cx + r9 % 3 - 1;
+        valid = z >= 0 && z < t.ncz && y >= 0 && y < t.ncy && x >= 0 && x < t.ncx;
+        if (valid) {
+            const unsigned int code = (ndim == 2) ? (cc_spread2(x) | (cc_spread2(y) << 1))
+                                                  : (cc_spread3(x) | (cc_spread3(y) << 1) | (cc_spread3(z) << 2));
+            const long long bk = t.bucket_base + (long long)code;
+            b0 = a.bstart[bk];
+            sz = (int)(a.bstart[bk + 1] - b0);
+        }
+    }
+    const unsigned bal = __ballot_sync(0xffffffffu, valid);
+    int incl = sz;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int v = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += v;
+    }
+    if (valid) {
+        const int pos = __popc(bal & ((1u << lane) - 1));
+        sb0[pos] = b0;
+        scum[pos] = incl - sz;
+    }
+    if (lane == 31) {
+        const int nb = __popc(bal);
+        scum[nb] = incl;
+        scum[28] = nb;
+    }
+}
+
+// Local-observation enumeration for the mixed path (the search of
+// obs_findlocal in common/observations.c, with the acceptance tests of
+// enumerate_obs): the candidates are the concatenated position ranges of the
+// neighbour buckets, taken 256 at a time across bucket boundaries (the order
+// is still bucket, then position), with each thread's coordinates for the
+// next block loaded while the current block is tested.  Accepted
+// observations are appended to a list of lseg + CALC_NT entries (position,
+// FP32 taper); whenever it holds lseg or more, the processor consumes its
+// whole rounds (proc.segment) and the rest moves to the front.  A type's
+// tail is consumed before the next type starts.  SEARCH 2: FP32 pre-test
+// with an exact FP64 test in the band (2-D); SEARCH 1: exact FP64 distances.
+// Returns the number of local observations.
+template <int SEARCH, class Proc>
+__device__ int enumerate_obs_seg(const CalcArgs& a, int lseg, double qx, double qy, double qz, int* lid, float* lcf,
+                                 int* wsum, long long* sb0, int* scum, int* tcount, Proc& proc)
+{
+    const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+    int total = 0;
+    for (int t = 0; t < a.ntypes; ++t) {
+        const TypeIndex& ti = a.types[t];
+        int n = 0;   // list entries (the same in every thread)
+        int tcnt = 0;
+        if (ti.pos_end > ti.pos_begin) {
+            if (wid == 0) neighbour_ranges(a, ti, qx, qy, qz, sb0, scum);
+            __syncthreads();
+            const int nb = scum[28], ncand = scum[nb];
+            const float qxh = (float)qx, qyh = (float)qy;
+            const float qxl = (float)(qx - (double)qxh), qyl = (float)(qy - (double)qyh);
+            // candidate c -> sorted position; j only moves forward
+            int j = 0;
+            auto position = [&](int c) -> long long {
+                while (j + 1 < nb && scum[j + 1] <= c) ++j;
+                return sb0[j] + (long long)(c - scum[j]);
+            };
+            long long pn = -1;
+            float nxf = 0.0f, nyf = 0.0f;
+            double nx = 0.0, ny = 0.0, nz = 0.0;
+            if (tid < ncand) {
+                pn = position(tid);
+                if constexpr (SEARCH == 2) {
+                    nxf = a.sxf[pn];
+                    nyf = a.syf[pn];
+                } else {
+                    nx = a.sx[pn];
+                    ny = a.sy[pn];
+                    if (a.ndim == 3) nz = a.sz[pn];
+                }
+            }
+            for (int base = 0; base < ncand; base += CALC_NT) {
+                const long long p = pn;
+                const float xf = nxf, yf = nyf;
+                const double x = nx, y = ny, z = nz;
+                pn = -1;
+                if (base + CALC_NT + tid < ncand) {
+                    pn = position(base + CALC_NT + tid);
+                    if constexpr (SEARCH == 2) {
+                        nxf = a.sxf[pn];
+                        nyf = a.syf[pn];
+                    } else {
+                        nx = a.sx[pn];
+                        ny = a.sy[pn];
+                        if (a.ndim == 3) nz = a.sz[pn];
+                    }
+                }
+                bool in = false;
+                float d2f = 0.0f, d2l = 0.0f;
+                double d2 = 0.0;
+                if constexpr (SEARCH == 2) {
+                    bool band = false;
+                    if (p >= 0) {
+                        exact::dist2_df(xf, yf, qxh, qxl, qyh, qyl, d2f, d2l);
+                        in = d2f <= ti.rmax2_lo;
+                        band = !in && d2f <= ti.rmax2_hi;
+                    }
+                    if (__any_sync(0xffffffffu, band))
+                        if (band) in = exact_in2(a.sx[p], a.sy[p], qx, qy, ti.rmax2);
+                } else {
+                    if (p >= 0) {
+                        d2 = a.ndim == 2 ? exact::dist2(x, y, qx, qy) : exact::dist3(x, y, z, qx, qy, qz);
+                        in = d2 <= ti.rmax2;
+                    }
+                }
+                const unsigned bal = __ballot_sync(0xffffffffu, in);
+                if (lane == 0) wsum[wid] = __popc(bal);
+                __syncthreads();
+                int before = 0, tot = 0;
+#pragma unroll
+                for (int w = 0; w < CALC_NT / 32; ++w) {
+                    const int c = wsum[w];
+                    before += (w < wid) ? c : 0;
+                    tot += c;
+                }
+                if (in) {
+                    const int pos = n + before + __popc(bal & ((1u << lane) - 1));
+                    lid[pos] = (int)p;
+                    if constexpr (SEARCH == 2)
+                        lcf[pos] = exact::calclcoeff_df(ti, d2f, d2l);
+                    else
+                        lcf[pos] = exact::calclcoeff_f(ti.nlocrad, ti.locrad, ti.locweight, d2);
+                }
+                n += tot;
+                tcnt += tot;
+                __syncthreads();   // list entries visible; wsum free
+                if (n >= lseg) {
+                    const int used = proc.segment(lid, lcf, n, t, false);
+                    const int rest = n - used;   // < kc <= CALC_NT
+                    int id = 0;
+                    float c = 0.0f;
+                    if (tid < rest) {
+                        id = lid[used + tid];
+                        c = lcf[used + tid];
+                    }
+                    __syncthreads();
+                    if (tid < rest) {
+                        lid[tid] = id;
+                        lcf[tid] = c;
+                    }
+                    __syncthreads();
+                    n = rest;
+                }
+            }
+            if (n > 0) proc.segment(lid, lcf, n, t, true);
+        }
+        if (tid == 0) tcount[t] = tcnt;
+        total += tcnt;
+        __syncthreads();
+    }
+    return total;
+}
+
 // operand tiles: 2 buffers x 3 pieces x N rows x kc, then the padding that
 // the 128-row A operand reads past the last tile (rows >= N, never used)
 static __host__ __device__ size_t mixed_tile_floats(int m, int kc)
@@ -468,28 +770,46 @@ static __host__ __device__ size_t mixed_tile_floats(int m, int kc)
     return (size_t)2 * MX_PIECES * N * kc + (size_t)(MX_ROWS - N) * kc;
 }
 
-static size_t mixed_smem_bytes(int m, int kc)
+// row stride of the raw S rows: >= mpad (a multiple of 4: 16-byte copies)
+// and = 8 mod 32, so that the 8 rows x 4 observations a warp reads per core
+// matrix fall in distinct banks
+static __host__ __device__ int mixed_ldv(int m)
+{
+    return m + ((8 - m % 32) % 32 + 32) % 32;
+}
+
+// local-observation list: lseg + CALC_NT entries of (position, FP32 taper);
+// the FP64 per-type pass reuses it as LIST_EXTRA (position, FP64 taper)
+static __host__ __device__ size_t mixed_list_bytes(int lseg)
+{
+    const size_t a = (size_t)(lseg + CALC_NT) * 8, b = (size_t)LIST_EXTRA * 12 + 8;
+    return a > b ? a : b;
+}
+
+static size_t mixed_smem_bytes(int m, int kc, int lseg)
 {
     int lda = (m % 2 == 0) ? m + 1 : m + 2;
     size_t s = 0;
     s += mixed_tile_floats(m, kc) * 4;                     // operand tiles + padding
-    s += (size_t)kc * (m + ((8 - m % 32) % 32 + 32) % 32) * 4;   // FP32 staged values (row stride = 8 mod 32)
+    s += (size_t)2 * kc * mixed_ldv(m) * 4;                // raw S rows, two buffers
+    s += (size_t)2 * kc * 8;                               // raw innovations, two buffers
     s += (size_t)2 * m * 4;                                // quantum q, 1/q
+    s += 16;                                               // alignment
     s += (size_t)m * lda * 8;                              // Macc (also A)
-    s += (size_t)kc * 4;                                   // tapered innovations
+    s += (size_t)2 * ((kc + 3) & ~3) * 4;                  // tapered innovations, taper of the round
     s += (size_t)6 * (m + 1) * 8;                          // b d e cs sn v
     s += (size_t)ENKFG_MAXTYPES * 8 * 2;
     s += (size_t)(CALC_NT / 32) * 8;
-    s += (size_t)LIST_EXTRA * 8;                           // llc
-    s += (size_t)LIST_EXTRA * 4;                           // lid
+    s += mixed_list_bytes(lseg);
     s += (size_t)ENKFG_MAXTYPES * 4;
     s += 256;                                              // control ints
+    s += 28 * 8 + 29 * 4 + 8;                              // neighbour bucket ranges
     s += 64;                                               // mbarriers, tmem slot, flags
     return s;
 }
 
 template <int HB>
-__global__ void __launch_bounds__(CALC_NT) k_transforms_mixed(CalcArgs a, int kcm, int N, uint32_t tcols)
+__global__ void __launch_bounds__(CALC_NT, 2) k_transforms_mixed(CalcArgs a, int kcm, int N, uint32_t tcols, int lseg)
 {
     extern __shared__ __align__(128) unsigned char smem_raw[];
     const int tid = threadIdx.x, wid = tid >> 5;
@@ -497,12 +817,14 @@ __global__ void __launch_bounds__(CALC_NT) k_transforms_mixed(CalcArgs a, int kc
     const size_t ntile = mixed_tile_floats(m, kcm);         // [2][3][N x kc] + padding for A's rows >= N
     unsigned char* sp = smem_raw;
     float* tiles = (float*)sp;        sp += ntile * 4;
-    const int ldv = m + ((8 - m % 32) % 32 + 32) % 32;        // >= m, = 8 mod 32
-    float* tileV = (float*)sp;        sp += (size_t)kcm * ldv * 4;
+    const int ldv = mixed_ldv(m);
+    float* raw0 = (float*)sp;         sp += (size_t)2 * kcm * ldv * 4;   // two buffers
+    double* sraw0 = (double*)sp;      sp += (size_t)2 * kcm * 8;
     float* qs = (float*)sp;           sp += (size_t)2 * m * 4;
     sp = (unsigned char*)(((uintptr_t)sp + 15) & ~(uintptr_t)15);
     double* Macc = (double*)sp;       sp += (size_t)m * lda * 8;
     float* sl = (float*)sp;           sp += (size_t)((kcm + 3) & ~3) * 4;
+    float* lr = (float*)sp;           sp += (size_t)((kcm + 3) & ~3) * 4;
     double* b = (double*)sp;          sp += (m + 1) * 8;
     double* d = (double*)sp;          sp += (m + 1) * 8;
     double* e = (double*)sp;          sp += (m + 1) * 8;
@@ -512,14 +834,21 @@ __global__ void __launch_bounds__(CALC_NT) k_transforms_mixed(CalcArgs a, int kc
     double* tss = (double*)sp;        sp += ENKFG_MAXTYPES * 8;
     double* tpd = (double*)sp;        sp += ENKFG_MAXTYPES * 8;
     double* red = (double*)sp;        sp += (CALC_NT / 32) * 8;
-    double* llc = (double*)sp;        sp += (size_t)LIST_EXTRA * 8;
-    int* lid = (int*)sp;              sp += LIST_EXTRA * 4;
+    unsigned char* list = sp;         sp += mixed_list_bytes(lseg);
     int* tcount = (int*)sp;           sp += ENKFG_MAXTYPES * 4;
     int* ictl = (int*)sp;             sp += 256;
+    long long* nb0 = (long long*)sp;  sp += 28 * 8;
+    int* ncum = (int*)sp;             sp += 29 * 4 + 4;
     uint64_t* mbar = (uint64_t*)sp;   sp += 8 * 2;
     uint32_t* tslot = (uint32_t*)sp;  sp += 8;
     int* err = (int*)sp;
-    const PointScratch s{ lid, llc, ictl, tcount, tss, tpd, red };
+    // the search list (lseg + CALC_NT positions, then their FP32 tapers);
+    // the FP64 per-type pass views the same bytes as LIST_EXTRA positions
+    // and FP64 tapers
+    int* slid = (int*)list;
+    float* slcf = (float*)(list + (size_t)(lseg + CALC_NT) * 4);
+    double* llc = (double*)(list + (size_t)LIST_EXTRA * 4 + 8 - ((size_t)LIST_EXTRA * 4) % 8);
+    const PointScratch s{ slid, llc, ictl, tcount, tss, tpd, red };
     const size_t piece = (size_t)N * kcm;
 
     // set-up: TMEM columns, mbarriers, zeroed operand tiles, the quantum
@@ -536,9 +865,9 @@ __global__ void __launch_bounds__(CALC_NT) k_transforms_mixed(CalcArgs a, int kc
     tc::fence_before();
     __syncthreads();
     tc::fence_after();
-    MixedShared ms{ { { tiles, tiles + piece, tiles + 2 * piece }, { tiles + 3 * piece, tiles + 4 * piece, tiles + 5 * piece } },
-                    tileV, ldv, qs, (float2*)Macc, lda, sl, mbar, *tslot, N, kcm, err };
-    MixedSync sy{ { 0u, 0u }, { false, false } };
+    MixedShared ms{ tiles, (int)piece, raw0, kcm * ldv, sraw0, kcm, ldv, qs, (float2*)Macc, lda, sl, lr, mbar, *tslot,
+                    N, kcm, err };
+    MixedSync sy{ 0u, 0u };
     uint32_t rnd = 0;
 
     for (int it = 0;; ++it) {
@@ -546,11 +875,12 @@ __global__ void __launch_bounds__(CALC_NT) k_transforms_mixed(CalcArgs a, int kc
         if (idx < 0 || *err) break;
         const int pt = a.order ? a.order[idx] : a.item0 + idx;
         const double qx = a.qx[pt], qy = a.qy[pt], qz = a.ndim == 3 ? a.qz[pt] : 0.0;
-        // observations per round: 8 x (accumulators used), per count bin when tuned
+        // observations per round: 8, 16 or 32 (a power of two), per count
+        // bin when tuned
         ms.kc = kcm;
         if (a.kc_table != nullptr && a.counts != nullptr) {
-            int k = a.kc_table[count_bin(a.counts[pt])];
-            ms.kc = (k >= 8 && k <= kcm) ? (k & ~7) : kcm;
+            const int k = a.kc_table[count_bin(a.counts[pt])];
+            ms.kc = k >= kcm ? kcm : k >= 16 ? 16 : 8;
         }
         if (tid < ENKFG_MAXTYPES) {
             tss[tid] = 0.0;
@@ -560,8 +890,9 @@ __global__ void __launch_bounds__(CALC_NT) k_transforms_mixed(CalcArgs a, int kc
         for (int i = tid; i < m * lda; i += CALC_NT) Macc[i] = 0.0;   // also zero as float2
         __syncthreads();
         GramProcTC<HB> proc(a, s, ms, sy, rnd);
-        const int p = (a.sxf != nullptr && a.ndim == 2) ? enumerate_obs<2>(a, ms.kc, qx, qy, qz, s, proc, true)
-                                                        : enumerate_obs<1>(a, ms.kc, qx, qy, qz, s, proc, true);
+        const int p = (a.sxf != nullptr && a.ndim == 2)
+                          ? enumerate_obs_seg<2>(a, lseg, qx, qy, qz, slid, slcf, ictl + 8, nb0, ncum, tcount, proc)
+                          : enumerate_obs_seg<1>(a, lseg, qx, qy, qz, slid, slcf, ictl + 8, nb0, ncum, tcount, proc);
         proc.finish();
         __syncthreads();
         if (*err) {
@@ -574,14 +905,24 @@ __global__ void __launch_bounds__(CALC_NT) k_transforms_mixed(CalcArgs a, int kc
             __syncthreads();
             continue;
         }
-        // double-float -> FP64 in place; b = S's from the member threads
+        // S's: each thread group's partial sums in FP64, into the raw row
+        // buffers (idle between points), summed over the groups below
+        double* bpart = (double*)raw0;
+        if (proc.s_r < m && proc.s_g < proc.sgroups)
+            bpart[proc.s_g * m + proc.s_r] =
+                (((double)proc.bh[0] + (double)proc.bh[1]) + ((double)proc.bh[2] + (double)proc.bh[3])) +
+                (((double)proc.bl[0] + (double)proc.bl[1]) + ((double)proc.bl[2] + (double)proc.bl[3]));
+        // double-float -> FP64 in place
         for (int i = tid; i < m * lda; i += CALC_NT) {
             float2 v2 = ((float2*)Macc)[i];
             Macc[i] = (double)v2.x + (double)v2.y;
         }
-        if (tid < m)
-            b[tid] = (((double)proc.bh[0] + (double)proc.bh[1]) + ((double)proc.bh[2] + (double)proc.bh[3])) +
-                     (((double)proc.bl[0] + (double)proc.bl[1]) + ((double)proc.bl[2] + (double)proc.bl[3]));
+        __syncthreads();
+        if (tid < m) {
+            double acc = 0.0;
+            for (int g = 0; g < proc.sgroups; ++g) acc += bpart[g * m + tid];
+            b[tid] = acc;
+        }
         __syncthreads();
         const double trss = la::block_sum<CALC_NT>(tid < m ? Macc[tid * lda + tid] : 0.0, red);
         if (tid < m) Macc[tid * lda + tid] += 1.0;
@@ -599,16 +940,18 @@ __global__ void __launch_bounds__(CALC_NT) k_transforms_mixed(CalcArgs a, int kc
 
 template <int HB>
 static enkfg_status launch_mixed_hb(enkfg_ctx* ctx, CalcArgs& a, int kcm, int N, uint32_t tcols, size_t smem,
-                                    cudaStream_t st)
+                                    int lseg, cudaStream_t st)
 {
     CK(cudaFuncSetAttribute(k_transforms_mixed<HB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    CK(cudaFuncSetAttribute(k_transforms_mixed<HB>, cudaFuncAttributePreferredSharedMemoryCarveout, cudaSharedmemCarveoutMaxShared));
+    // computed residency (the occupancy query reports one CTA per SM here)
+    // and the carveout that holds it, the rest staying L1
+    int per_sm = 0, carve = 100;
+    enkfg_status s = resident_ctas(ctx, (const void*)k_transforms_mixed<HB>, CALC_NT, smem, &per_sm, &carve);
+    if (s) return s;
+    CK(cudaFuncSetAttribute(k_transforms_mixed<HB>, cudaFuncAttributePreferredSharedMemoryCarveout, carve));
     int grid = a.nitems;
     if (a.persistent) {
-        // computed residency (the occupancy query reports one CTA per SM here)
-        int per_sm = 0, nsm = 0;
-        enkfg_status s = resident_ctas(ctx, (const void*)k_transforms_mixed<HB>, CALC_NT, smem, &per_sm);
-        if (s) return s;
+        int nsm = 0;
         CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, ctx->device));
         // TMEM: at most 512 columns per SM across resident CTAs
         while (per_sm > 1 && (uint32_t)per_sm * tcols > 512) --per_sm;
@@ -616,7 +959,7 @@ static enkfg_status launch_mixed_hb(enkfg_ctx* ctx, CalcArgs& a, int kcm, int N,
         if (grid > a.nitems) grid = a.nitems;
     }
     if (grid < 1) return ENKFG_OK;
-    k_transforms_mixed<HB><<<grid, CALC_NT, smem, st>>>(a, kcm, N, tcols);
+    k_transforms_mixed<HB><<<grid, CALC_NT, smem, st>>>(a, kcm, N, tcols, lseg);
     CKL();
     return ENKFG_OK;
 }
@@ -628,7 +971,13 @@ enkfg_status launch_mixed(enkfg_ctx* ctx, CalcArgs& a, cudaStream_t st)
     uint32_t tcols = 32;
     while ((int)tcols < 4 * N) tcols <<= 1;              // two windows x (hi*hi' | rest)
     const int kcm = MX_KC;
-    size_t smem = mixed_smem_bytes(m, kcm);
+    // list segment: 1024 entries, fewer where that keeps two CTAs per SM
+    // (113 KB each) or the CTA within 227 KB; at least 256
+    int lseg = 1024;
+    const size_t two = 113 * 1024, one = 227 * 1024;
+    const size_t lim = mixed_smem_bytes(m, kcm, 256) <= two ? two : one;
+    while (lseg > 256 && mixed_smem_bytes(m, kcm, lseg) > lim) lseg >>= 1;
+    size_t smem = mixed_smem_bytes(m, kcm, lseg);
     if (smem > 227 * 1024) {
         set_err(ctx, "mixed path: nmem = %d needs %zu bytes of shared memory", m, smem);
         return ENKFG_EUNSUPPORTED;
@@ -639,9 +988,9 @@ enkfg_status launch_mixed(enkfg_ctx* ctx, CalcArgs& a, cudaStream_t st)
         return ENKFG_EUNSUPPORTED;
     }
     const int hb = ((N >> 1) + 7) / 8;
-    if (hb <= 2) return launch_mixed_hb<2>(ctx, a, kcm, N, tcols, smem, st);
-    if (hb <= 3) return launch_mixed_hb<3>(ctx, a, kcm, N, tcols, smem, st);
-    if (hb <= 4) return launch_mixed_hb<4>(ctx, a, kcm, N, tcols, smem, st);
-    if (hb <= 6) return launch_mixed_hb<6>(ctx, a, kcm, N, tcols, smem, st);
-    return launch_mixed_hb<8>(ctx, a, kcm, N, tcols, smem, st);
+    if (hb <= 2) return launch_mixed_hb<2>(ctx, a, kcm, N, tcols, smem, lseg, st);
+    if (hb <= 3) return launch_mixed_hb<3>(ctx, a, kcm, N, tcols, smem, lseg, st);
+    if (hb <= 4) return launch_mixed_hb<4>(ctx, a, kcm, N, tcols, smem, lseg, st);
+    if (hb <= 6) return launch_mixed_hb<6>(ctx, a, kcm, N, tcols, smem, lseg, st);
+    return launch_mixed_hb<8>(ctx, a, kcm, N, tcols, smem, lseg, st);
 }

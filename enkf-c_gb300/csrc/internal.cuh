@@ -219,8 +219,10 @@ enkfg_status list_local(enkfg_ctx* ctx, const long long* d_offsets, int* d_ids, 
 enkfg_status run_transforms(enkfg_ctx* ctx, const enkfg_calc_params* p, cudaStream_t st);
 // CTAs of `fn` (nt threads, dsmem bytes of dynamic shared memory) that fit on
 // one SM at once, from the shared memory (with the per-block reserve),
-// register and thread limits of the device.
-enkfg_status resident_ctas(enkfg_ctx* ctx, const void* fn, int nt, size_t dsmem, int* per_sm);
+// register and thread limits of the device; and the shared-memory carveout
+// (percent of the maximum) that holds that many, so that the rest of the
+// unified L1 / shared array stays L1.
+enkfg_status resident_ctas(enkfg_ctx* ctx, const void* fn, int nt, size_t dsmem, int* per_sm, int* carveout);
 enkfg_status run_update(enkfg_ctx* ctx, const enkfg_update_params* p, const int* d_numlevels, int nfield,
                         const int* levels, float* d_fields, float* d_infl, cudaStream_t st);
 enkfg_status run_innovations(enkfg_ctx* ctx, cudaStream_t st);
