@@ -276,7 +276,11 @@ struct MixedSync {
 // exact in FP32 (every product is a multiple of q_r q_s below 2^16 of them),
 // the rest is 2^-8 of it or less.  A closed window is drained (tcgen05.ld,
 // TwoSum into Macc) one round later, while the next window runs.
-template <int HB>
+// FS: S's fused into the split -- each thread multiplies its observation's
+// tapered innovation into every row it splits and keeps a double-float sum
+// per row (2 HB rows at most) in registers for the whole point; otherwise
+// S's is a separate pass over the staged rows by thread groups.
+template <int HB, bool FS>
 struct GramProcTC {
     const CalcArgs& a;
     const PointScratch& s;
@@ -290,6 +294,7 @@ struct GramProcTC {
     int sgroups;       // S's thread groups: CALC_NT / (m rounded up to 32)
     int s_g, s_r;      // this thread's group and member
     float bh[4], bl[4]; // S's for member s_r, group s_g: four double-float partial sums
+    float fh[FS ? 2 * HB : 1], fl[FS ? 2 * HB : 1];   // fused S's: per row slot
     __device__ __forceinline__ GramProcTC(const CalcArgs& a_, const PointScratch& s_, MixedShared& ms_, MixedSync& sy_,
                                           uint32_t& rnd_)
         : a(a_), s(s_), ms(ms_), sy(sy_), rnd(rnd_), win(0), win_obs(0), drain_set(-1), drain_buf(0)
@@ -298,6 +303,8 @@ struct GramProcTC {
         sgroups = CALC_NT / mr;
         s_g = (int)threadIdx.x / mr;
         s_r = (int)threadIdx.x - s_g * mr;
+#pragma unroll
+        for (int i = 0; i < (FS ? 2 * HB : 1); ++i) fh[i] = fl[i] = 0.0f;
         for (int j = 0; j < 4; ++j) bh[j] = bl[j] = 0.0f;
     }
 
@@ -377,6 +384,51 @@ struct GramProcTC {
         tc::cp_async_commit();
     }
 
+    // the hi / mid / lo pieces of this thread's values in one round (and,
+    // with FS, their products with the observation's tapered innovation xk
+    // into the row sums); returns the sum of squares when TS
+    template <bool TS>
+    __device__ __forceinline__ double split_rows(float* tH, float* tM, float* tL, const float* rp, float ck, float xk,
+                                                 int nrg, int nkg, int kg, int rg0, int rstep, int lane)
+    {
+        const int m = a.m;
+        const float* q = ms.qs;
+        const float* iq = ms.qs + m;
+        double ssq = 0.0;
+        auto one = [&](int rg, int r) -> float {
+            const float v = __fmul_rn(rp[rg << 3], ck);
+            if (TS) ssq += (double)v * (double)v;
+            const float hi = __fmul_rn(rintf(__fmul_rn(v, iq[r])), q[r]);
+            const float r1 = __fsub_rn(v, hi);
+            const float md = tc::to_tf32(r1);
+            const int off = ((rg * nkg + kg) << 5) + lane;
+            tH[off] = hi;
+            tM[off] = md;
+            tL[off] = tc::to_tf32(__fsub_rn(r1, md));
+            return v;
+        };
+        if constexpr (FS) {
+#pragma unroll
+            for (int i = 0; i < 2 * HB; ++i) {
+                const int rg = rg0 + i * rstep;
+                const int r = (rg << 3) + (lane >> 2);
+                if (rg < nrg && r < m) {
+                    const float v = one(rg, r);
+                    const float p = v * xk, pe = fmaf(v, xk, -p);
+                    const float sm = fh[i] + p, bp = sm - fh[i];
+                    fl[i] += ((fh[i] - (sm - bp)) + (p - bp)) + pe;
+                    fh[i] = sm;
+                }
+            }
+        } else {
+            for (int rg = rg0; rg < nrg; rg += rstep) {
+                const int r = (rg << 3) + (lane >> 2);
+                if (r < m) one(rg, r);
+            }
+        }
+        return ssq;
+    }
+
     // one round: nc (<= kc) observations at list positions [base, base + nc)
     // whose rows are in raw buffer rb
     __device__ void round(const float* lcf, int base, int nc, int t, int rb)
@@ -396,10 +448,9 @@ struct GramProcTC {
         float* tM = ms.tile(buf, 1);
         float* tL = ms.tile(buf, 2);
         const float* raw = ms.rawb(rb);
-        const float* q = ms.qs;
-        const float* iq = ms.qs + m;
-        // 1. taper and tapered innovations of the round (zero past nc)
-        if (tid < kc) {
+        // 1. taper and tapered innovations of the round (zero past nc), for
+        //    the separate S's pass
+        if (!FS && tid < kc) {
             const float c = tid < nc ? lcf[base + tid] : 0.0f;
             ms.lr[tid] = c;
             ms.sl[tid] = tid < nc ? (float)ms.srawb(rb)[tid] * c : 0.0f;
@@ -419,37 +470,10 @@ struct GramProcTC {
             const int kg = wid & (nkg - 1), rg0 = wid / nkg, rstep = (CALC_NT / 32) / nkg;
             const int k = (kg << 2) + (lane & 3);
             const float ck = k < nc ? lcf[base + k] : 0.0f;
+            const float xk = (FS && k < nc) ? __fmul_rn((float)ms.srawb(rb)[k], ck) : 0.0f;
             const float* rp = raw + k * ms.ldv + (lane >> 2);
-            if (tsum) {
-                for (int rg = rg0; rg < nrg; rg += rstep) {
-                    const int r = (rg << 3) + (lane >> 2);
-                    if (r < m) {
-                        const float v = __fmul_rn(rp[rg << 3], ck);
-                        ssq += (double)v * (double)v;
-                        const float hi = __fmul_rn(rintf(__fmul_rn(v, iq[r])), q[r]);
-                        const float r1 = __fsub_rn(v, hi);
-                        const float md = tc::to_tf32(r1);
-                        const int off = ((rg * nkg + kg) << 5) + lane;
-                        tH[off] = hi;
-                        tM[off] = md;
-                        tL[off] = tc::to_tf32(__fsub_rn(r1, md));
-                    }
-                }
-            } else {
-                for (int rg = rg0; rg < nrg; rg += rstep) {
-                    const int r = (rg << 3) + (lane >> 2);
-                    if (r < m) {
-                        const float v = __fmul_rn(rp[rg << 3], ck);
-                        const float hi = __fmul_rn(rintf(__fmul_rn(v, iq[r])), q[r]);
-                        const float r1 = __fsub_rn(v, hi);
-                        const float md = tc::to_tf32(r1);
-                        const int off = ((rg * nkg + kg) << 5) + lane;
-                        tH[off] = hi;
-                        tM[off] = md;
-                        tL[off] = tc::to_tf32(__fsub_rn(r1, md));
-                    }
-                }
-            }
+            if (tsum) ssq = split_rows<true>(tH, tM, tL, rp, ck, xk, nrg, nkg, kg, rg0, rstep, lane);
+            else split_rows<false>(tH, tM, tL, rp, ck, xk, nrg, nkg, kg, rg0, rstep, lane);
         }
         tc::fence_async_smem();
         __syncthreads();
@@ -489,7 +513,7 @@ struct GramProcTC {
         //    sgroups takes member r = tid - g mr and observations g, g + G,
         //    ...; four independent double-float partial sums for ILP.  Raw
         //    rows, lr and sl are zero past nc, so the tail adds nothing.
-        if (s_r < m && s_g < sgroups) {
+        if (!FS && s_r < m && s_g < sgroups) {
             const int G = sgroups;
             for (int k0 = s_g; k0 < kc; k0 += 4 * G) {
 #pragma unroll
@@ -808,7 +832,7 @@ static size_t mixed_smem_bytes(int m, int kc, int lseg)
     return s;
 }
 
-template <int HB>
+template <int HB, bool FS>
 __global__ void __launch_bounds__(CALC_NT, 2) k_transforms_mixed(CalcArgs a, int kcm, int N, uint32_t tcols, int lseg)
 {
     extern __shared__ __align__(128) unsigned char smem_raw[];
@@ -889,7 +913,7 @@ __global__ void __launch_bounds__(CALC_NT, 2) k_transforms_mixed(CalcArgs a, int
         }
         for (int i = tid; i < m * lda; i += CALC_NT) Macc[i] = 0.0;   // also zero as float2
         __syncthreads();
-        GramProcTC<HB> proc(a, s, ms, sy, rnd);
+        GramProcTC<HB, FS> proc(a, s, ms, sy, rnd);
         const int p = (a.sxf != nullptr && a.ndim == 2)
                           ? enumerate_obs_seg<2>(a, lseg, qx, qy, qz, slid, slcf, ictl + 8, nb0, ncum, tcount, proc)
                           : enumerate_obs_seg<1>(a, lseg, qx, qy, qz, slid, slcf, ictl + 8, nb0, ncum, tcount, proc);
@@ -905,13 +929,33 @@ __global__ void __launch_bounds__(CALC_NT, 2) k_transforms_mixed(CalcArgs a, int
             __syncthreads();
             continue;
         }
-        // S's: each thread group's partial sums in FP64, into the raw row
-        // buffers (idle between points), summed over the groups below
+        // S's: partial sums in FP64 into the raw row buffers (idle between
+        // points), summed below -- fused: the four lanes of a row group (four
+        // observations) combined by shuffles, then one partial per K group
+        // (each (K group, row) is written by exactly one warp); separate
+        // pass: one partial per thread group
         double* bpart = (double*)raw0;
-        if (proc.s_r < m && proc.s_g < proc.sgroups)
-            bpart[proc.s_g * m + proc.s_r] =
-                (((double)proc.bh[0] + (double)proc.bh[1]) + ((double)proc.bh[2] + (double)proc.bh[3])) +
-                (((double)proc.bl[0] + (double)proc.bl[1]) + ((double)proc.bl[2] + (double)proc.bl[3]));
+        int nparts;
+        if constexpr (FS) {
+            const int lane = tid & 31;
+            const int nkg = ms.kc >> 2, nrg = (m + 7) >> 3;
+            const int kg = wid & (nkg - 1), rg0 = wid / nkg, rstep = (CALC_NT / 32) / nkg;
+#pragma unroll
+            for (int i = 0; i < 2 * HB; ++i) {
+                double d = (double)proc.fh[i] + (double)proc.fl[i];
+                d += __shfl_xor_sync(0xffffffffu, d, 1);
+                d += __shfl_xor_sync(0xffffffffu, d, 2);
+                const int rg = rg0 + i * rstep, r = (rg << 3) + (lane >> 2);
+                if ((lane & 3) == 0 && rg < nrg && r < m) bpart[kg * m + r] = d;
+            }
+            nparts = nkg;
+        } else {
+            if (proc.s_r < m && proc.s_g < proc.sgroups)
+                bpart[proc.s_g * m + proc.s_r] =
+                    (((double)proc.bh[0] + (double)proc.bh[1]) + ((double)proc.bh[2] + (double)proc.bh[3])) +
+                    (((double)proc.bl[0] + (double)proc.bl[1]) + ((double)proc.bl[2] + (double)proc.bl[3]));
+            nparts = proc.sgroups;
+        }
         // double-float -> FP64 in place
         for (int i = tid; i < m * lda; i += CALC_NT) {
             float2 v2 = ((float2*)Macc)[i];
@@ -920,7 +964,7 @@ __global__ void __launch_bounds__(CALC_NT, 2) k_transforms_mixed(CalcArgs a, int
         __syncthreads();
         if (tid < m) {
             double acc = 0.0;
-            for (int g = 0; g < proc.sgroups; ++g) acc += bpart[g * m + tid];
+            for (int g = 0; g < nparts; ++g) acc += bpart[g * m + tid];
             b[tid] = acc;
         }
         __syncthreads();
@@ -938,17 +982,17 @@ __global__ void __launch_bounds__(CALC_NT, 2) k_transforms_mixed(CalcArgs a, int
     if (wid == 0) tc::tmem_dealloc(*tslot, tcols);
 }
 
-template <int HB>
+template <int HB, bool FS>
 static enkfg_status launch_mixed_hb(enkfg_ctx* ctx, CalcArgs& a, int kcm, int N, uint32_t tcols, size_t smem,
                                     int lseg, cudaStream_t st)
 {
-    CK(cudaFuncSetAttribute(k_transforms_mixed<HB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    CK(cudaFuncSetAttribute(k_transforms_mixed<HB, FS>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     // computed residency (the occupancy query reports one CTA per SM here)
     // and the carveout that holds it, the rest staying L1
     int per_sm = 0, carve = 100;
-    enkfg_status s = resident_ctas(ctx, (const void*)k_transforms_mixed<HB>, CALC_NT, smem, &per_sm, &carve);
+    enkfg_status s = resident_ctas(ctx, (const void*)k_transforms_mixed<HB, FS>, CALC_NT, smem, &per_sm, &carve);
     if (s) return s;
-    CK(cudaFuncSetAttribute(k_transforms_mixed<HB>, cudaFuncAttributePreferredSharedMemoryCarveout, carve));
+    CK(cudaFuncSetAttribute(k_transforms_mixed<HB, FS>, cudaFuncAttributePreferredSharedMemoryCarveout, carve));
     int grid = a.nitems;
     if (a.persistent) {
         int nsm = 0;
@@ -959,7 +1003,7 @@ static enkfg_status launch_mixed_hb(enkfg_ctx* ctx, CalcArgs& a, int kcm, int N,
         if (grid > a.nitems) grid = a.nitems;
     }
     if (grid < 1) return ENKFG_OK;
-    k_transforms_mixed<HB><<<grid, CALC_NT, smem, st>>>(a, kcm, N, tcols, lseg);
+    k_transforms_mixed<HB, FS><<<grid, CALC_NT, smem, st>>>(a, kcm, N, tcols, lseg);
     CKL();
     return ENKFG_OK;
 }
@@ -988,9 +1032,10 @@ enkfg_status launch_mixed(enkfg_ctx* ctx, CalcArgs& a, cudaStream_t st)
         return ENKFG_EUNSUPPORTED;
     }
     const int hb = ((N >> 1) + 7) / 8;
-    if (hb <= 2) return launch_mixed_hb<2>(ctx, a, kcm, N, tcols, smem, lseg, st);
-    if (hb <= 3) return launch_mixed_hb<3>(ctx, a, kcm, N, tcols, smem, lseg, st);
-    if (hb <= 4) return launch_mixed_hb<4>(ctx, a, kcm, N, tcols, smem, lseg, st);
-    if (hb <= 6) return launch_mixed_hb<6>(ctx, a, kcm, N, tcols, smem, lseg, st);
-    return launch_mixed_hb<8>(ctx, a, kcm, N, tcols, smem, lseg, st);
+    // S's fused into the split up to 8 rows per thread (registers)
+    if (hb <= 2) return launch_mixed_hb<2, true>(ctx, a, kcm, N, tcols, smem, lseg, st);
+    if (hb <= 3) return launch_mixed_hb<3, true>(ctx, a, kcm, N, tcols, smem, lseg, st);
+    if (hb <= 4) return launch_mixed_hb<4, true>(ctx, a, kcm, N, tcols, smem, lseg, st);
+    if (hb <= 6) return launch_mixed_hb<6, false>(ctx, a, kcm, N, tcols, smem, lseg, st);
+    return launch_mixed_hb<8, false>(ctx, a, kcm, N, tcols, smem, lseg, st);
 }
