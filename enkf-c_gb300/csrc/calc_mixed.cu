@@ -137,9 +137,11 @@ __device__ __forceinline__ uint64_t now_ns()
     return t;
 }
 
-// wait for phase `parity` of the mbarrier, at most MX_WAIT_NS; true if it completed
+// wait for phase `parity` of the mbarrier, at most MX_WAIT_NS; true if it
+// completed (the clock is read only when the first try fails)
 __device__ __forceinline__ bool mbar_wait_bounded(uint64_t* mbar, uint32_t parity)
 {
+    if (mbar_try_wait(mbar, parity)) return true;
     const uint64_t t0 = now_ns();
     for (;;) {
         if (mbar_try_wait(mbar, parity)) return true;
@@ -227,7 +229,9 @@ struct MixedShared {
     int ldv;               // row stride of raw: >= mpad, = 8 mod 32 (conflict-free reads)
     const float* qs;       // [2][m]: quantum q_r and 1/q_r
     float2* Macc;          // [m x lda] double-float S'S (later reused as FP64)
+    float* Mrest;          // [m x lda] stacked form: the remainder products from the offset lanes
     int lda;
+    int stacked;           // tile order [hi mid lo Z] [lo hi mid] (else [hi mid lo] x 2)
     float* sl;             // [kc] tapered innovations of the round
     float* lr;             // [kc] taper coefficients of the round (0 past its end)
     uint64_t* mbar;        // [2] one per operand buffer
@@ -235,7 +239,12 @@ struct MixedShared {
     int N;                 // MMA N (m rounded up to 16)
     int kc;                // observations per round
     int* err;              // shared error flag
-    __device__ __forceinline__ float* tile(int buf, int pc) const { return tiles + (buf * MX_PIECES + pc) * piece; }
+    __device__ __forceinline__ float* tile(int buf, int pc) const
+    {
+        const int idx = stacked ? (buf == 0 ? pc : (pc == 2 ? 4 : 5 + pc)) : buf * MX_PIECES + pc;
+        return tiles + idx * piece;
+    }
+    __device__ __forceinline__ float* zblock() const { return tiles + 3 * piece; }   // stacked: N zero rows
     __device__ __forceinline__ float* rawb(int rb) const { return raw + rb * rawsz; }
     __device__ __forceinline__ double* srawb(int rb) const { return sraw + rb * kcm; }
 };
@@ -276,11 +285,17 @@ struct MixedSync {
 // exact in FP32 (every product is a multiple of q_r q_s below 2^16 of them),
 // the rest is 2^-8 of it or less.  A closed window is drained (tcgen05.ld,
 // TwoSum into Macc) one round later, while the next window runs.
+// ST: stacked products (N <= 64) -- A = [hi; mid] takes two pieces in one
+// MMA: per group of 8 observations hi*[hi; mid]' into the first accumulator
+// (rows < N: hi*hi', exact; rows N..2N-1: mid*hi'), mid and lo times [hi;
+// mid]' and lo*hi' (A = [lo; Z] or [Z; lo]) into the second: four MMAs
+// instead of six, and row r's remainder is acc1[N+r] + acc2[r] + acc2[N+r]
+// (mid*lo' included).
 // FS: S's fused into the split -- each thread multiplies its observation's
 // tapered innovation into every row it splits and keeps a double-float sum
 // per row (2 HB rows at most) in registers for the whole point; otherwise
 // S's is a separate pass over the staged rows by thread groups.
-template <int HB, bool FS>
+template <int HB, bool FS, bool ST>
 struct GramProcTC {
     const CalcArgs& a;
     const PointScratch& s;
@@ -310,9 +325,10 @@ struct GramProcTC {
 
     // bounded wait for the outstanding commit of operand buffer `buf`; on
     // expiry record the error and wait once more (bounded), so that nothing
-    // is in flight when TMEM is released.  Ends with a barrier, so every
-    // thread sees the same error flag.
-    __device__ __forceinline__ void wait_buf(int buf)
+    // is in flight when TMEM is released.  With `sync` it ends with a
+    // barrier, so every thread sees the same error flag (without, the
+    // caller's next barrier does that).
+    __device__ __forceinline__ void wait_buf(int buf, bool sync = true)
     {
         if (sy.outstanding(buf)) {
             bool done = tc::mbar_wait_bounded(ms.mbar + buf, sy.parity(buf));
@@ -323,7 +339,7 @@ struct GramProcTC {
             sy.completed(buf);
         }
         tc::fence_after();
-        __syncthreads();
+        if (sync) __syncthreads();
     }
 
     // add accumulator set `set` to the shared double-float S'S (its MMAs
@@ -334,11 +350,16 @@ struct GramProcTC {
         const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
         if (*ms.err) return;
         const int r = 32 * (wid & 3) + lane;
-        if (32 * (wid & 3) < a.m) {
+        // stacked: lanes N..N+m-1 hold remainder products of row r - N
+        const int lanes = ST ? ms.N + a.m : a.m;
+        if (32 * (wid & 3) < lanes) {
             const int half = ms.N >> 1;
             const int c0 = (wid >> 2) * half;
             const uint32_t base = ms.taddr + ((uint32_t)(32 * (wid & 3)) << 16) + (uint32_t)(2 * set * ms.N + c0);
-            float2* row = ms.Macc + (size_t)(r < a.m ? r : 0) * ms.lda;
+            const bool direct = r < a.m;
+            const bool offset = ST && r >= ms.N && r < ms.N + a.m;
+            float2* row = ms.Macc + (size_t)(direct ? r : 0) * ms.lda;
+            float* rrow = ST ? ms.Mrest + (size_t)(offset ? r - ms.N : 0) * ms.lda : nullptr;
 #pragma unroll
             for (int b = 0; b < HB; ++b)
                 if (8 * b < half) {
@@ -346,7 +367,7 @@ struct GramProcTC {
                     tc::tmem_ld8_nowait(base + (uint32_t)(8 * b), vh);
                     tc::tmem_ld8_nowait(base + (uint32_t)(ms.N + 8 * b), vr);
                     tc::tmem_wait_ld();
-                    if (r < a.m) {
+                    if (direct) {
 #pragma unroll
                         for (int j = 0; j < 8; ++j) {
                             const int c = c0 + 8 * b + j;
@@ -356,6 +377,12 @@ struct GramProcTC {
                                 acc.y += __uint_as_float(vr[j]);   // <= 2^-8 of hi*hi'
                                 row[c] = acc;
                             }
+                        }
+                    } else if (offset) {
+#pragma unroll
+                        for (int j = 0; j < 8; ++j) {
+                            const int c = c0 + 8 * b + j;
+                            if (c < a.m) rrow[c] += __uint_as_float(vh[j]) + __uint_as_float(vr[j]);
                         }
                     }
                 }
@@ -496,14 +523,26 @@ struct GramProcTC {
             uint64_t dh = tc::desc_kmajor_noswizzle(tc::smem_u32(tH), 128u, sbo);
             uint64_t dm = tc::desc_kmajor_noswizzle(tc::smem_u32(tM), 128u, sbo);
             uint64_t dl = tc::desc_kmajor_noswizzle(tc::smem_u32(tL), 128u, sbo);
-            for (int g = 0; g < ngroups; ++g, dh += 16u, dm += 16u, dl += 16u) {
-                const uint32_t fresh = (win_obs == 0 && g == 0) ? 0u : 1u;
-                tc::mma_tf32_warp(dhh, dh, dh, idesc, fresh);
-                tc::mma_tf32_warp(dr, dh, dm, idesc, fresh);
-                tc::mma_tf32_warp(dr, dm, dh, idesc, 1u);
-                tc::mma_tf32_warp(dr, dh, dl, idesc, 1u);
-                tc::mma_tf32_warp(dr, dl, dh, idesc, 1u);
-                tc::mma_tf32_warp(dr, dm, dm, idesc, 1u);
+            if constexpr (ST) {
+                // A = [lo; Z] (buffer 0) or [Z; lo] (buffer 1) for lo*hi'
+                uint64_t dz = tc::desc_kmajor_noswizzle(tc::smem_u32(buf == 0 ? tL : ms.zblock()), 128u, sbo);
+                for (int g = 0; g < ngroups; ++g, dh += 16u, dm += 16u, dl += 16u, dz += 16u) {
+                    const uint32_t fresh = (win_obs == 0 && g == 0) ? 0u : 1u;
+                    tc::mma_tf32_warp(dhh, dh, dh, idesc, fresh);   // [hi; mid] hi'
+                    tc::mma_tf32_warp(dr, dh, dm, idesc, fresh);    // [hi; mid] mid'
+                    tc::mma_tf32_warp(dr, dh, dl, idesc, 1u);       // [hi; mid] lo'
+                    tc::mma_tf32_warp(dr, dz, dh, idesc, 1u);       // lo hi'
+                }
+            } else {
+                for (int g = 0; g < ngroups; ++g, dh += 16u, dm += 16u, dl += 16u) {
+                    const uint32_t fresh = (win_obs == 0 && g == 0) ? 0u : 1u;
+                    tc::mma_tf32_warp(dhh, dh, dh, idesc, fresh);
+                    tc::mma_tf32_warp(dr, dh, dm, idesc, fresh);
+                    tc::mma_tf32_warp(dr, dm, dh, idesc, 1u);
+                    tc::mma_tf32_warp(dr, dh, dl, idesc, 1u);
+                    tc::mma_tf32_warp(dr, dl, dh, idesc, 1u);
+                    tc::mma_tf32_warp(dr, dm, dm, idesc, 1u);
+                }
             }
             tc::commit_warp(ms.mbar + buf);
         }
@@ -532,7 +571,7 @@ struct GramProcTC {
         // 4. the window closed one round ago: its last commit is on the other
         //    buffer; drain it while this round's MMAs run
         if (drain_set >= 0) {
-            wait_buf(drain_buf);
+            wait_buf(drain_buf, false);
             read_set(drain_set);
             drain_set = -1;
         }
@@ -787,10 +826,13 @@ __device__ int enumerate_obs_seg(const CalcArgs& a, int lseg, double qx, double 
 }
 
 // operand tiles: 2 buffers x 3 pieces x N rows x kc, then the padding that
-// the 128-row A operand reads past the last tile (rows >= N, never used)
-static __host__ __device__ size_t mixed_tile_floats(int m, int kc)
+// the 128-row A operand reads past the last tile (rows >= N, never used);
+// stacked (N <= 64): [hi mid lo] [Z] [lo hi mid] and the 128 - 2N rows that
+// A = [hi; mid; ...] of buffer 1 reads past its mid piece
+static __host__ __device__ size_t mixed_tile_floats(int m, int kc, int st)
 {
     const int N = (m + 15) / 16 * 16;
+    if (st) return (size_t)7 * N * kc + (size_t)(MX_ROWS - 2 * N) * kc;   // 6 pieces + Z + A's reach past b1.mid
     return (size_t)2 * MX_PIECES * N * kc + (size_t)(MX_ROWS - N) * kc;
 }
 
@@ -810,11 +852,12 @@ static __host__ __device__ size_t mixed_list_bytes(int lseg)
     return a > b ? a : b;
 }
 
-static size_t mixed_smem_bytes(int m, int kc, int lseg)
+static size_t mixed_smem_bytes(int m, int kc, int lseg, int st)
 {
     int lda = (m % 2 == 0) ? m + 1 : m + 2;
     size_t s = 0;
-    s += mixed_tile_floats(m, kc) * 4;                     // operand tiles + padding
+    s += mixed_tile_floats(m, kc, st) * 4;                 // operand tiles + padding
+    if (st) s += (size_t)m * lda * 4;                      // Mrest
     s += (size_t)2 * kc * mixed_ldv(m) * 4;                // raw S rows, two buffers
     s += (size_t)2 * kc * 8;                               // raw innovations, two buffers
     s += (size_t)2 * m * 4;                                // quantum q, 1/q
@@ -832,13 +875,13 @@ static size_t mixed_smem_bytes(int m, int kc, int lseg)
     return s;
 }
 
-template <int HB, bool FS>
+template <int HB, bool FS, bool ST>
 __global__ void __launch_bounds__(CALC_NT, 2) k_transforms_mixed(CalcArgs a, int kcm, int N, uint32_t tcols, int lseg)
 {
     extern __shared__ __align__(128) unsigned char smem_raw[];
     const int tid = threadIdx.x, wid = tid >> 5;
     const int m = a.m, lda = (m % 2 == 0) ? m + 1 : m + 2;   // odd stride: fewer bank conflicts
-    const size_t ntile = mixed_tile_floats(m, kcm);         // [2][3][N x kc] + padding for A's rows >= N
+    const size_t ntile = mixed_tile_floats(m, kcm, ST);     // operand pieces + padding for A's rows
     unsigned char* sp = smem_raw;
     float* tiles = (float*)sp;        sp += ntile * 4;
     const int ldv = mixed_ldv(m);
@@ -847,6 +890,7 @@ __global__ void __launch_bounds__(CALC_NT, 2) k_transforms_mixed(CalcArgs a, int
     float* qs = (float*)sp;           sp += (size_t)2 * m * 4;
     sp = (unsigned char*)(((uintptr_t)sp + 15) & ~(uintptr_t)15);
     double* Macc = (double*)sp;       sp += (size_t)m * lda * 8;
+    float* Mrest = (float*)sp;        sp += ST ? (size_t)m * lda * 4 : 0;
     float* sl = (float*)sp;           sp += (size_t)((kcm + 3) & ~3) * 4;
     float* lr = (float*)sp;           sp += (size_t)((kcm + 3) & ~3) * 4;
     double* b = (double*)sp;          sp += (m + 1) * 8;
@@ -889,8 +933,8 @@ __global__ void __launch_bounds__(CALC_NT, 2) k_transforms_mixed(CalcArgs a, int
     tc::fence_before();
     __syncthreads();
     tc::fence_after();
-    MixedShared ms{ tiles, (int)piece, raw0, kcm * ldv, sraw0, kcm, ldv, qs, (float2*)Macc, lda, sl, lr, mbar, *tslot,
-                    N, kcm, err };
+    MixedShared ms{ tiles, (int)piece, raw0, kcm * ldv, sraw0, kcm, ldv, qs, (float2*)Macc, Mrest, lda, ST ? 1 : 0,
+                    sl, lr, mbar, *tslot, N, kcm, err };
     MixedSync sy{ 0u, 0u };
     uint32_t rnd = 0;
 
@@ -911,9 +955,20 @@ __global__ void __launch_bounds__(CALC_NT, 2) k_transforms_mixed(CalcArgs a, int
             tpd[tid] = 0.0;
             tcount[tid] = 0;
         }
-        for (int i = tid; i < m * lda; i += CALC_NT) Macc[i] = 0.0;   // also zero as float2
+        for (int i = tid; i < m * lda; i += CALC_NT) {
+            Macc[i] = 0.0;   // also zero as float2
+            if (ST) Mrest[i] = 0.0f;
+        }
+        // pieces N x kc apart (contiguous, as the stacked A = [hi; mid]
+        // needs); the Z block at this spacing is cleared (the previous
+        // point's MMAs have completed).  Rows >= m of the other pieces may
+        // hold stale values: they only reach accumulator rows and columns
+        // that are never read.
+        ms.piece = N * ms.kc;
+        if (ST)
+            for (int i = tid; i < ms.piece; i += CALC_NT) ms.zblock()[i] = 0.0f;
         __syncthreads();
-        GramProcTC<HB, FS> proc(a, s, ms, sy, rnd);
+        GramProcTC<HB, FS, ST> proc(a, s, ms, sy, rnd);
         const int p = (a.sxf != nullptr && a.ndim == 2)
                           ? enumerate_obs_seg<2>(a, lseg, qx, qy, qz, slid, slcf, ictl + 8, nb0, ncum, tcount, proc)
                           : enumerate_obs_seg<1>(a, lseg, qx, qy, qz, slid, slcf, ictl + 8, nb0, ncum, tcount, proc);
@@ -959,7 +1014,7 @@ __global__ void __launch_bounds__(CALC_NT, 2) k_transforms_mixed(CalcArgs a, int
         // double-float -> FP64 in place
         for (int i = tid; i < m * lda; i += CALC_NT) {
             float2 v2 = ((float2*)Macc)[i];
-            Macc[i] = (double)v2.x + (double)v2.y;
+            Macc[i] = ST ? ((double)v2.x + (double)v2.y) + (double)Mrest[i] : (double)v2.x + (double)v2.y;
         }
         __syncthreads();
         if (tid < m) {
@@ -982,17 +1037,17 @@ __global__ void __launch_bounds__(CALC_NT, 2) k_transforms_mixed(CalcArgs a, int
     if (wid == 0) tc::tmem_dealloc(*tslot, tcols);
 }
 
-template <int HB, bool FS>
+template <int HB, bool FS, bool ST>
 static enkfg_status launch_mixed_hb(enkfg_ctx* ctx, CalcArgs& a, int kcm, int N, uint32_t tcols, size_t smem,
                                     int lseg, cudaStream_t st)
 {
-    CK(cudaFuncSetAttribute(k_transforms_mixed<HB, FS>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    CK(cudaFuncSetAttribute(k_transforms_mixed<HB, FS, ST>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     // computed residency (the occupancy query reports one CTA per SM here)
     // and the carveout that holds it, the rest staying L1
     int per_sm = 0, carve = 100;
-    enkfg_status s = resident_ctas(ctx, (const void*)k_transforms_mixed<HB, FS>, CALC_NT, smem, &per_sm, &carve);
+    enkfg_status s = resident_ctas(ctx, (const void*)k_transforms_mixed<HB, FS, ST>, CALC_NT, smem, &per_sm, &carve);
     if (s) return s;
-    CK(cudaFuncSetAttribute(k_transforms_mixed<HB, FS>, cudaFuncAttributePreferredSharedMemoryCarveout, carve));
+    CK(cudaFuncSetAttribute(k_transforms_mixed<HB, FS, ST>, cudaFuncAttributePreferredSharedMemoryCarveout, carve));
     int grid = a.nitems;
     if (a.persistent) {
         int nsm = 0;
@@ -1003,7 +1058,7 @@ static enkfg_status launch_mixed_hb(enkfg_ctx* ctx, CalcArgs& a, int kcm, int N,
         if (grid > a.nitems) grid = a.nitems;
     }
     if (grid < 1) return ENKFG_OK;
-    k_transforms_mixed<HB, FS><<<grid, CALC_NT, smem, st>>>(a, kcm, N, tcols, lseg);
+    k_transforms_mixed<HB, FS, ST><<<grid, CALC_NT, smem, st>>>(a, kcm, N, tcols, lseg);
     CKL();
     return ENKFG_OK;
 }
@@ -1019,23 +1074,25 @@ enkfg_status launch_mixed(enkfg_ctx* ctx, CalcArgs& a, cudaStream_t st)
     // (113 KB each) or the CTA within 227 KB; at least 256
     int lseg = 1024;
     const size_t two = 113 * 1024, one = 227 * 1024;
-    const size_t lim = mixed_smem_bytes(m, kcm, 256) <= two ? two : one;
-    while (lseg > 256 && mixed_smem_bytes(m, kcm, lseg) > lim) lseg >>= 1;
-    size_t smem = mixed_smem_bytes(m, kcm, lseg);
+    const int stk = N <= 64 ? 1 : 0;                     // stacked products
+    const size_t lim = mixed_smem_bytes(m, kcm, 256, stk) <= two ? two : one;
+    while (lseg > 256 && mixed_smem_bytes(m, kcm, lseg, stk) > lim) lseg >>= 1;
+    size_t smem = mixed_smem_bytes(m, kcm, lseg, stk);
     if (smem > 227 * 1024) {
         set_err(ctx, "mixed path: nmem = %d needs %zu bytes of shared memory", m, smem);
         return ENKFG_EUNSUPPORTED;
     }
     // the per-type pass's FP64 chunk buffer (kcm x m doubles) lives in the tiles
-    if (tcols > 512 || (size_t)kcm * m * 8 > mixed_tile_floats(m, kcm) * 4) {
+    if (tcols > 512 || (size_t)kcm * m * 8 > mixed_tile_floats(m, kcm, stk) * 4) {
         set_err(ctx, "mixed path: tile too small for the per-type pass");
         return ENKFG_EUNSUPPORTED;
     }
     const int hb = ((N >> 1) + 7) / 8;
     // S's fused into the split up to 8 rows per thread (registers)
-    if (hb <= 2) return launch_mixed_hb<2, true>(ctx, a, kcm, N, tcols, smem, lseg, st);
-    if (hb <= 3) return launch_mixed_hb<3, true>(ctx, a, kcm, N, tcols, smem, lseg, st);
-    if (hb <= 4) return launch_mixed_hb<4, true>(ctx, a, kcm, N, tcols, smem, lseg, st);
-    if (hb <= 6) return launch_mixed_hb<6, false>(ctx, a, kcm, N, tcols, smem, lseg, st);
-    return launch_mixed_hb<8, false>(ctx, a, kcm, N, tcols, smem, lseg, st);
+    // (N <= 64 is hb <= 4: fused S's and stacked products together)
+    if (hb <= 2) return launch_mixed_hb<2, true, true>(ctx, a, kcm, N, tcols, smem, lseg, st);
+    if (hb <= 3) return launch_mixed_hb<3, true, true>(ctx, a, kcm, N, tcols, smem, lseg, st);
+    if (hb <= 4) return launch_mixed_hb<4, true, true>(ctx, a, kcm, N, tcols, smem, lseg, st);
+    if (hb <= 6) return launch_mixed_hb<6, false, false>(ctx, a, kcm, N, tcols, smem, lseg, st);
+    return launch_mixed_hb<8, false, false>(ctx, a, kcm, N, tcols, smem, lseg, st);
 }
