@@ -39,6 +39,16 @@ for _p in (ROOT, PKG):
 import numpy as np  # noqa: E402
 
 METRIC = "local analyses/s (calc + update cycle)"
+
+# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per local
+# analysis of one ncu capture of each kernel on workload 2 at half edge
+# length (15,000 analyses): k_transforms_mixed 25.8 + 83.5 MB, k_update_cells
+# 305.0 + 162.0 MB.  Traffic grows with the analyses (and, for the update,
+# with the cells they cover), so a full launch scales by the analyses.
+TRAFFIC_PER_ANALYSIS = {
+    (2, "k_transforms_mixed"): (25.85e6 + 83.54e6) / 15000,
+    (2, "k_update_cells"): (304.96e6 + 162.01e6) / 15000,
+}
 UNIT = "analyses/s"
 
 
@@ -286,11 +296,13 @@ def run_gpu(args, rank, world, local_rank):
     # sum over points of 2 m^2 p + 2 m p (S'S as a full m x m product and
     # S's), over the kernel's own CUDA-event time.  FP64 path: against the
     # nominal FP64 rate (FP64 is not among the measured peaks).  Mixed path:
-    # S'S runs as six TF32 products on the tensor cores (hi*hi', hi*mid',
-    # mid*hi', hi*lo', lo*hi', mid*mid'), so the peak is the measured bf16
-    # rate / 2 (TF32) / 6 (split products).  Update kernel:
-    # fields read + written and X5 read once, over its CUDA-event time,
-    # against the measured HBM copy bandwidth.
+    # against the measured bf16 rate / 2 (dense TF32); the tensor work it
+    # issues per algorithmic flop is reported beside it (per group of 8
+    # observations: 4 MMAs of 128 x N x 8 in the stacked form, N <= 64,
+    # else 6).  Update kernel: fields read + written and X5 read once, over
+    # its CUDA-event time, against the measured HBM copy bandwidth.
+    # traffic: DRAM bytes (read + write) per analysis from one ncu capture of
+    # each kernel on workload 2 at half edge length, scaled to the launch.
     peaks, peak_src = load_peaks()
     calc_t = statistics.median(calc_ms) / 1e3
     upd_t = statistics.median(upd_ms) / 1e3
@@ -301,17 +313,25 @@ def run_gpu(args, rank, world, local_rank):
     flops = float((2.0 * m * m * counts + 2.0 * m * counts).sum())
     kname = "k_transforms_mixed" if prec == enkfg.PREC_MIXED else "k_transforms"
     if prec == enkfg.PREC_MIXED:
+        N = (m + 15) // 16 * 16
+        nmma = 4 if N <= 64 else 6
+        issued = float((nmma * 2.0 * 128 * N * 8 * np.ceil(counts / 8.0)).sum())
         roof = {"kernel": kname, "bound": "tensor", "achieved": flops / kern_t / 1e12,
-                "peak": peaks["bf16_tflops"] / 2.0 / 6.0, "unit": "TFLOP/s",
-                "peak_source": f"{peak_src} bf16 {peaks['bf16_tflops']} / 2 (TF32) / 6 (split products)"}
+                "peak": peaks["bf16_tflops"] / 2.0, "unit": "TFLOP/s",
+                "peak_source": f"{peak_src} bf16 {peaks['bf16_tflops']} / 2 (dense TF32)",
+                "mma_per_8_obs": nmma, "issued_per_algorithmic_flop": issued / flops,
+                "issued_tflops": issued / kern_t / 1e12}
     else:
         roof = {"kernel": kname, "bound": "fp64", "achieved": flops / kern_t / 1e12, "peak": 1.25,
                 "unit": "TFLOP/s", "peak_source": "GB300 nominal FP64 (FP64 is not among the measured peaks)"}
     roof["frac"] = roof["achieved"] / roof["peak"]
-    roof["traffic"] = None
+    tpa = TRAFFIC_PER_ANALYSIS.get((w.cfg, kname))
+    roof["traffic"] = tpa * w.nanalyses if tpa else None
     roof["kernel_ms"] = kern_t * 1e3
     roof["flops_per_launch"] = flops
+    upa = TRAFFIC_PER_ANALYSIS.get((w.cfg, "k_update_cells")) if m <= 64 else None
     uroof = {"kernel": "k_update_cells" if m <= 64 else "k_update_v2", "bound": "hbm",
+             "traffic": upa * w.nanalyses if upa else None,
              "achieved": ub / ukern_t / 1e9, "peak": peaks["hbm_gbs"], "unit": "GB/s",
              "frac": ub / ukern_t / 1e9 / peaks["hbm_gbs"], "bytes_per_launch": ub, "kernel_ms": ukern_t * 1e3,
              "peak_source": peak_src}
