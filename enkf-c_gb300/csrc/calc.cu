@@ -600,8 +600,8 @@ enkfg_status run_transforms(enkfg_ctx* ctx, const enkfg_calc_params* p, cudaStre
     a.status = ctx->d_status_pt;
 
     if (p->path == ENKFG_PATH_BATCHED) {
-        // size-sorted queue
-        if ((s = count_local(ctx, ctx->d_counts, nullptr, st))) return s;
+        // size-sorted queue (by candidate count)
+        if ((s = count_candidates(ctx, ctx->d_counts, st))) return s;
         if ((s = build_queue(ctx, npts, st))) return s;
         a.persistent = 1;
         a.order = ctx->d_order;

@@ -65,19 +65,52 @@ static double dkey_inv(unsigned long long k)
     return d;
 }
 
-__global__ void k_bbox(int nobs, int ndim, const double* __restrict__ ox, const double* __restrict__ oy,
-                       const double* __restrict__ oz, const short* __restrict__ type,
-                       const short* __restrict__ status, unsigned long long* __restrict__ box)
+// box[t*6 + 2*axis + 0] = min key, + 1 = max key (as max of keys).  A thread
+// keeps the running bounds of a run of observations of one type (a grid-
+// stride sweep) and flushes them to the block's shared copy when the type
+// changes; each block then merges into the global box once per entry.
+#define BBOX_T 256
+__global__ void __launch_bounds__(BBOX_T) k_bbox(int nobs, int ndim, int ntypes, const double* __restrict__ ox,
+                                                 const double* __restrict__ oy, const double* __restrict__ oz,
+                                                 const short* __restrict__ type, const short* __restrict__ status,
+                                                 unsigned long long* __restrict__ box)
 {
-    // box[t*6 + 2*axis + 0] = min key, + 1 = max key (as max of keys)
-    int o = blockIdx.x * blockDim.x + threadIdx.x;
-    if (o >= nobs || status[o] != 0) return;
-    int t = type[o];
-    double v[3] = { ox[o], oy[o], ndim == 3 ? oz[o] : 0.0 };
-    for (int a = 0; a < ndim; ++a) {
-        unsigned long long k = dkey(v[a]);
-        atomicMin(&box[t * 6 + 2 * a], k);
-        atomicMax(&box[t * 6 + 2 * a + 1], k);
+    __shared__ unsigned long long sb[ENKFG_MAXTYPES * 6];
+    for (int i = threadIdx.x; i < ntypes * 6; i += BBOX_T) sb[i] = (i & 1) ? 0ull : ~0ull;
+    __syncthreads();
+    int cur = -1;
+    unsigned long long lo[3] = { ~0ull, ~0ull, ~0ull }, hi[3] = { 0ull, 0ull, 0ull };
+    auto flush = [&]() {
+        if (cur < 0) return;
+        for (int a = 0; a < ndim; ++a) {
+            atomicMin(&sb[cur * 6 + 2 * a], lo[a]);
+            atomicMax(&sb[cur * 6 + 2 * a + 1], hi[a]);
+            lo[a] = ~0ull;
+            hi[a] = 0ull;
+        }
+    };
+    for (int o = blockIdx.x * BBOX_T + threadIdx.x; o < nobs; o += gridDim.x * BBOX_T) {
+        if (status[o] != 0) continue;
+        const int t = type[o];
+        if (t != cur) {
+            flush();
+            cur = t;
+        }
+        const double v[3] = { ox[o], oy[o], ndim == 3 ? oz[o] : 0.0 };
+        for (int a = 0; a < ndim; ++a) {
+            const unsigned long long k = dkey(v[a]);
+            lo[a] = k < lo[a] ? k : lo[a];
+            hi[a] = k > hi[a] ? k : hi[a];
+        }
+    }
+    flush();
+    __syncthreads();
+    for (int i = threadIdx.x; i < ntypes * 6; i += BBOX_T) {
+        if (i & 1) {
+            if (sb[i] != 0ull) atomicMax(&box[i], sb[i]);
+        } else if (sb[i] != ~0ull) {
+            atomicMin(&box[i], sb[i]);
+        }
     }
 }
 
@@ -355,8 +388,9 @@ enkfg_status build_index(enkfg_ctx* ctx, cudaStream_t st)
             }
         cudaMemcpyAsync(d_box, h, ntypes * 6 * sizeof(unsigned long long), cudaMemcpyHostToDevice, st);
         if (nobs > 0) {
-            k_bbox<<<div_up(nobs, 256), 256, 0, st>>>(nobs, ndim, ctx->d_ox, ctx->d_oy, ctx->d_oz, ctx->d_type,
-                                                     ctx->d_status, d_box);
+            const int nb = div_up(nobs, BBOX_T * 8) < 2 * 152 ? div_up(nobs, BBOX_T * 8) : 2 * 152;
+            k_bbox<<<nb, BBOX_T, 0, st>>>(nobs, ndim, ntypes, ctx->d_ox, ctx->d_oy, ctx->d_oz, ctx->d_type,
+                                          ctx->d_status, d_box);
             ctx->launches++;
         }
         cudaMemcpyAsync(h, d_box, ntypes * 6 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, st);
@@ -602,6 +636,40 @@ __global__ void k_count_local(int npts, int ntypes, int ndim, const TypeIndex* _
         total += nt;
     }
     if (lane == 0) counts[pt] = total;
+}
+
+// Candidate count of every strided point: the observations in its
+// neighbour buckets (the search's candidates, no distance tests).  The
+// batched path orders its work queue and picks the round size by this
+// count, which is proportional to the local count at a fraction of the
+// cost; one thread per point.
+__global__ void k_count_candidates(int npts, int ntypes, int ndim, const TypeIndex* __restrict__ types,
+                                   const long long* __restrict__ bstart, const double* __restrict__ qx,
+                                   const double* __restrict__ qy, const double* __restrict__ qz,
+                                   int* __restrict__ counts)
+{
+    const int pt = blockIdx.x * blockDim.x + threadIdx.x;
+    if (pt >= npts) return;
+    const double x = qx[pt], y = qy[pt], z = ndim == 3 ? qz[pt] : 0.0;
+    long long total = 0;
+    for (int t = 0; t < ntypes; ++t) {
+        const TypeIndex& ti = types[t];
+        if (ti.pos_end <= ti.pos_begin) continue;
+        long long bk[27];
+        const int nb = neighbour_buckets(ti, ndim, x, y, z, bk);
+        for (int k = 0; k < nb; ++k) total += bstart[bk[k] + 1] - bstart[bk[k]];
+    }
+    counts[pt] = total < 0x7fffffffll ? (int)total : 0x7fffffff;
+}
+
+enkfg_status count_candidates(enkfg_ctx* ctx, int* d_counts, cudaStream_t st)
+{
+    int npts = ctx->nj * ctx->ni;
+    int ndim = ctx->geographic ? 3 : 2;
+    k_count_candidates<<<div_up(npts, 256), 256, 0, st>>>(npts, ctx->ntypes, ndim, ctx->d_types, ctx->d_bstart,
+                                                          ctx->d_qx, ctx->d_qy, ctx->d_qz, d_counts);
+    CKL();
+    return ENKFG_OK;
 }
 
 enkfg_status count_local(enkfg_ctx* ctx, int* d_counts, int* d_pcounts, cudaStream_t st)

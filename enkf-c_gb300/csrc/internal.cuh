@@ -215,6 +215,7 @@ enkfg_status scan_counts(enkfg_ctx* ctx, const int* d_in, long long* d_out, long
 enkfg_status build_index(enkfg_ctx* ctx, cudaStream_t st);
 enkfg_status build_gather(enkfg_ctx* ctx, cudaStream_t st);
 enkfg_status count_local(enkfg_ctx* ctx, int* d_counts, int* d_pcounts, cudaStream_t st);
+enkfg_status count_candidates(enkfg_ctx* ctx, int* d_counts, cudaStream_t st);
 enkfg_status list_local(enkfg_ctx* ctx, const long long* d_offsets, int* d_ids, double* d_coeffs, cudaStream_t st);
 enkfg_status run_transforms(enkfg_ctx* ctx, const enkfg_calc_params* p, cudaStream_t st);
 // CTAs of `fn` (nt threads, dsmem bytes of dynamic shared memory) that fit on

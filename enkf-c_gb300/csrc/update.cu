@@ -460,42 +460,65 @@ __global__ void __launch_bounds__(UPD_NT) k_update_v2(UpdArgs a)
 // planes load and store coalesced over the 16 consecutive cells, and the
 // mean, the mean increment and the spread sums are sequential sums over
 // members in the reference's order -- no cross-lane reductions.  Each row of
-// A^a = X5 A is formed and written at once; with spread-capped inflation
-// (inf_ratio set) the rows are formed twice, first for the spread.  The FP64
-// variant forms the i-interpolated X5 element with the reference's float
-// operations (update.c:255-265); the FP32 variant contracts it into an FMA.
+// A^a = X5 A is formed and written at once, several rows at a time
+// (independent sums, so that the FMA chains overlap); with spread-capped
+// inflation (inf_ratio set) the rows are formed twice, first for the spread.
+// The FP64 variant forms the i-interpolated X5 element with the reference's
+// float operations (update.c:255-265) and sums each row in the reference's
+// order; the FP32 variant applies the two strided columns' rows to the
+// member values separately and interpolates the two sums (u1 Ta x + u2 Tb x).
 #define UPC_NC 16
 #define UPC_NT 128
+// rows e1b .. e1b+R-1 (those below md) of A^a = X5 A for one cell and layer
+// (R = 4 rows at a time in the FP32 variant, 2 in the FP64 one, whose
+// per-element interpolation needs more registers)
+template <bool F64>
+struct X5Rows {
+    static constexpr int R = F64 ? 2 : 4;
+};
+
 template <bool F64, int MT>
-__device__ __forceinline__ float x5_row(const float* __restrict__ Ta, const float* __restrict__ Tb, int e1, int m4, int m,
-                                        float u1, float u2, const float (&x)[MT])
+__device__ __forceinline__ void x5_rows(const float* __restrict__ Ta, const float* __restrict__ Tb, int e1b, int m4,
+                                        int m, int md, float u1, float u2, const float (&x)[MT],
+                                        float (&y)[X5Rows<F64>::R])
 {
-    const float4* ta = reinterpret_cast<const float4*>(Ta + e1 * m4);
-    const float4* tb = reinterpret_cast<const float4*>(Tb + e1 * m4);
-    float s = 0.0f;
+    constexpr int R = X5Rows<F64>::R;
+    float sa[R], sb[R];
+#pragma unroll
+    for (int r = 0; r < R; ++r) sa[r] = sb[r] = 0.0f;
 #pragma unroll
     for (int q = 0; q < MT / 4; ++q) {
         if (4 * q < m) {
-            const float4 p = ta[q], r = tb[q];
-            float t0, t1, t2, t3;
-            if constexpr (F64) {
-                t0 = __fadd_rn(__fmul_rn(p.x, u1), __fmul_rn(r.x, u2));
-                t1 = __fadd_rn(__fmul_rn(p.y, u1), __fmul_rn(r.y, u2));
-                t2 = __fadd_rn(__fmul_rn(p.z, u1), __fmul_rn(r.z, u2));
-                t3 = __fadd_rn(__fmul_rn(p.w, u1), __fmul_rn(r.w, u2));
-            } else {
-                t0 = fmaf(p.x, u1, r.x * u2);
-                t1 = fmaf(p.y, u1, r.y * u2);
-                t2 = fmaf(p.z, u1, r.z * u2);
-                t3 = fmaf(p.w, u1, r.w * u2);
+#pragma unroll
+            for (int r = 0; r < R; ++r) {
+                if (e1b + r < md) {
+                    const float4 p = reinterpret_cast<const float4*>(Ta + (e1b + r) * m4)[q];
+                    const float4 t = reinterpret_cast<const float4*>(Tb + (e1b + r) * m4)[q];
+                    if constexpr (F64) {
+                        const float t0 = __fadd_rn(__fmul_rn(p.x, u1), __fmul_rn(t.x, u2));
+                        const float t1 = __fadd_rn(__fmul_rn(p.y, u1), __fmul_rn(t.y, u2));
+                        const float t2 = __fadd_rn(__fmul_rn(p.z, u1), __fmul_rn(t.z, u2));
+                        const float t3 = __fadd_rn(__fmul_rn(p.w, u1), __fmul_rn(t.w, u2));
+                        sa[r] = fmaf(t0, x[4 * q], sa[r]);
+                        sa[r] = fmaf(t1, x[4 * q + 1], sa[r]);
+                        sa[r] = fmaf(t2, x[4 * q + 2], sa[r]);
+                        sa[r] = fmaf(t3, x[4 * q + 3], sa[r]);
+                    } else {
+                        sa[r] = fmaf(p.x, x[4 * q], sa[r]);
+                        sb[r] = fmaf(t.x, x[4 * q], sb[r]);
+                        sa[r] = fmaf(p.y, x[4 * q + 1], sa[r]);
+                        sb[r] = fmaf(t.y, x[4 * q + 1], sb[r]);
+                        sa[r] = fmaf(p.z, x[4 * q + 2], sa[r]);
+                        sb[r] = fmaf(t.z, x[4 * q + 2], sb[r]);
+                        sa[r] = fmaf(p.w, x[4 * q + 3], sa[r]);
+                        sb[r] = fmaf(t.w, x[4 * q + 3], sb[r]);
+                    }
+                }
             }
-            s = fmaf(t0, x[4 * q], s);
-            s = fmaf(t1, x[4 * q + 1], s);
-            s = fmaf(t2, x[4 * q + 2], s);
-            s = fmaf(t3, x[4 * q + 3], s);
         }
     }
-    return s;
+#pragma unroll
+    for (int r = 0; r < R; ++r) y[r] = F64 ? sa[r] : fmaf(sa[r], u1, sb[r] * u2);
 }
 
 template <bool F64, int MT>
@@ -522,18 +545,42 @@ __global__ void __launch_bounds__(UPC_NT) k_update_cells(UpdArgs a, int sstride)
         const float w2 = __fdiv_rn((float)stepj, (float)st), w1 = __fsub_rn(1.0f, w2);
         const bool jint = (st > 1 && stepj > 0);
         const int per = md * m4;
-        for (int idx = tid; idx < ns * per; idx += UPC_NT) {
-            const int k = idx / per, r = idx - k * per;
-            const int e1 = r / m4, e = r - e1 * m4;
-            int g = s0 + k;
-            if (g >= a.ni) g = a.periodic_i ? g - a.ni : a.ni - 1;
-            float v = 0.0f;
-            if (e < m) {
-                v = __ldg(a.T + (((size_t)jj * a.ni + g) * md + e1) * m + e);
-                if (jint)
-                    v = __fadd_rn(__fmul_rn(v, w1), __fmul_rn(__ldg(a.T + (((size_t)jj2 * a.ni + g) * md + e1) * m + e), w2));
+        if ((m & 3) == 0 && ((uintptr_t)a.T & 15) == 0) {
+            // rows of m = m4 floats, 16-byte aligned: four elements a load
+            const int q4 = m4 >> 2, per4 = md * q4;
+            for (int k = 0; k < ns; ++k) {
+                int g = s0 + k;
+                if (g >= a.ni) g = a.periodic_i ? g - a.ni : a.ni - 1;
+                const float4* ta = reinterpret_cast<const float4*>(a.T + ((size_t)jj * a.ni + g) * md * m);
+                const float4* tb = reinterpret_cast<const float4*>(a.T + ((size_t)jj2 * a.ni + g) * md * m);
+                float4* dst = reinterpret_cast<float4*>(Tjj + (size_t)k * sstride);
+                for (int i = tid; i < per4; i += UPC_NT) {
+                    float4 v = __ldg(ta + i);
+                    if (jint) {
+                        const float4 u = __ldg(tb + i);
+                        v.x = __fadd_rn(__fmul_rn(v.x, w1), __fmul_rn(u.x, w2));
+                        v.y = __fadd_rn(__fmul_rn(v.y, w1), __fmul_rn(u.y, w2));
+                        v.z = __fadd_rn(__fmul_rn(v.z, w1), __fmul_rn(u.z, w2));
+                        v.w = __fadd_rn(__fmul_rn(v.w, w1), __fmul_rn(u.w, w2));
+                    }
+                    dst[i] = v;   // row e1 = i / q4 at e1 * m4: the same offset, m4 = m
+                }
             }
-            Tjj[(size_t)k * sstride + r] = v;
+        } else {
+            for (int idx = tid; idx < ns * per; idx += UPC_NT) {
+                const int k = idx / per, r = idx - k * per;
+                const int e1 = r / m4, e = r - e1 * m4;
+                int g = s0 + k;
+                if (g >= a.ni) g = a.periodic_i ? g - a.ni : a.ni - 1;
+                float v = 0.0f;
+                if (e < m) {
+                    v = __ldg(a.T + (((size_t)jj * a.ni + g) * md + e1) * m + e);
+                    if (jint)
+                        v = __fadd_rn(__fmul_rn(v, w1),
+                                      __fmul_rn(__ldg(a.T + (((size_t)jj2 * a.ni + g) * md + e1) * m + e), w2));
+                }
+                Tjj[(size_t)k * sstride + r] = v;
+            }
         }
         for (int idx = tid; idx < ns * m4; idx += UPC_NT) {
             const int k = idx / m4, e = idx - k * m4;
@@ -628,9 +675,15 @@ __global__ void __launch_bounds__(UPC_NT) k_update_cells(UpdArgs a, int sstride)
                     const float y = rescale(x[e]);
                     s2f.add_prod(y, y);
                 }
-            for (int e1 = 0; e1 < md; ++e1) {
-                const float y = rescale(x5_row<F64, MT>(Ta, Tb, e1, m4, m, u1, u2, x));
-                s2a.add_prod(y, y);
+            for (int e1b = 0; e1b < md; e1b += X5Rows<F64>::R) {
+                float y4[X5Rows<F64>::R];
+                x5_rows<F64, MT>(Ta, Tb, e1b, m4, m, md, u1, u2, x, y4);
+#pragma unroll
+                for (int r = 0; r < X5Rows<F64>::R; ++r)
+                    if (e1b + r < md) {
+                        const float y = rescale(y4[r]);
+                        s2a.add_prod(y, y);
+                    }
             }
             if constexpr (F64) {
                 const double v2_f = s2f.value(), v2_a = s2a.value();
@@ -649,9 +702,15 @@ __global__ void __launch_bounds__(UPC_NT) k_update_cells(UpdArgs a, int sstride)
         }
         const bool inflate = __fsub_rn(inflation, 1.0f) > 1.0e-6f;
         if (!inflate) inflation = 1.0f;
-        // A^a = X5 A row by row (update.c:399) and the output (update.c:460-516)
-        for (int e1 = 0; e1 < md; ++e1) {
-            const float y = rescale(x5_row<F64, MT>(Ta, Tb, e1, m4, m, u1, u2, x));
+        // A^a = X5 A (update.c:399) and the output (update.c:460-516)
+        for (int e1b = 0; e1b < md; e1b += X5Rows<F64>::R) {
+          float y4[X5Rows<F64>::R];
+          x5_rows<F64, MT>(Ta, Tb, e1b, m4, m, md, u1, u2, x, y4);
+#pragma unroll
+          for (int r = 0; r < X5Rows<F64>::R; ++r) {
+            const int e1 = e1b + r;
+            if (e1 >= md) break;
+            const float y = rescale(y4[r]);
             float va = inflate ? __fmul_rn(y, inflation) : y;
             va = v1_a.add(va);
             float out;
@@ -672,6 +731,7 @@ __global__ void __launch_bounds__(UPC_NT) k_update_cells(UpdArgs a, int sstride)
                 }
             }
             v[(size_t)e1 * a.plane] = out;
+          }
         }
         if (a.infl) a.infl[(size_t)f * a.plane + ioff] = inflation;
     }
