@@ -471,6 +471,82 @@ __global__ void __launch_bounds__(CALC_NT) k_eig_finish(CalcArgs a, const double
     if (a.want_diag) diag_single(a, pt, (int)pd, dfs, trss);
 }
 
+// Batched DEnKF / EnOI solve: the transform kernels save M (upper triangle)
+// and S's per slot; one CTA of INV_NT threads per point inverts M with the
+// symmetric sweep and forms w, dfs and T.  Inside the transform kernel the
+// sweep leaves the FP64 units idle between pivots (barriers, the pivot's
+// reciprocal); here a dozen points per SM keep them busy.
+#define INV_NT 64
+
+__global__ void __launch_bounds__(INV_NT) k_inv_finish(CalcArgs a)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int m = a.m, lda = (m % 2 == 0) ? m + 1 : m + 2;
+    const int tid = threadIdx.x, slot = blockIdx.x;
+    double* A = (double*)smem_raw;
+    double* b = A + (size_t)m * lda;
+    double* U = b + m;
+    double* V = U + m;
+    double* piv = V + m;
+    double* red = piv + 2;
+    int* ctl = (int*)(red + INV_NT / 32);
+    const double pd = a.eaux[2 * (size_t)slot];
+    if (!(pd > 0.0)) return;   // empty point: written by the transform kernel
+    const int pt = a.order ? a.order[slot] : a.item0 + slot;
+    const double trss = a.eaux[2 * (size_t)slot + 1];
+    const size_t q0 = (size_t)slot * m * m;
+    for (int i = tid; i < m * m; i += INV_NT) {
+        const int r = i / m, c = i - r * m;
+        if (c >= r) A[r * lda + c] = a.eq[q0 + i];
+    }
+    for (int i = tid; i < m; i += INV_NT) b[i] = a.eb[(size_t)slot * m + i];
+    __syncthreads();
+    const int rc = la::spd_inverse<INV_NT>(A, m, lda, U, V, piv, ctl);
+    const double dfs = denkf_outputs<INV_NT>(a, pt, A, lda, b, red);
+    if (rc != 0 && tid == 0) a.status[pt] = rc;
+    if (a.want_diag) diag_single(a, pt, (int)pd, dfs, trss);
+}
+
+static enkfg_status run_inv_batched(enkfg_ctx* ctx, const CalcArgs& a0, int precision, cudaStream_t st)
+{
+    enkfg_status s;
+    const int m = a0.m, nitems = a0.nitems;
+    const size_t per = (size_t)m * m * 8 + (size_t)m * 8 + 16;
+    size_t B = ((size_t)2 << 30) / per;      // about 2 GB of scratch per batch
+    if (B < 256) B = 256;
+    if (B > (size_t)nitems) B = (size_t)nitems;
+    if ((s = ensure(ctx, &ctx->d_eq, &ctx->eq_cap, B * m * m))) return s;
+    if ((s = ensure(ctx, &ctx->d_eb, &ctx->eb_cap, B * m))) return s;
+    if ((s = ensure(ctx, &ctx->d_eaux, &ctx->eaux_cap, B * 2))) return s;
+    const int lda = (m % 2 == 0) ? m + 1 : m + 2;
+    const size_t ismem = ((size_t)m * lda + 3 * (size_t)m + 2 + INV_NT / 32) * 8 + 16;
+    if (ismem > 227 * 1024) {
+        set_err(ctx, "batched inverse: nmem = %d needs %zu bytes of shared memory", m, ismem);
+        return ENKFG_EUNSUPPORTED;
+    }
+    CK(cudaFuncSetAttribute(k_inv_finish, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ismem));
+    for (int i0 = 0; i0 < nitems; i0 += (int)B) {
+        const int nb = (nitems - i0 < (int)B) ? nitems - i0 : (int)B;
+        CalcArgs b = a0;
+        b.defer = 1;
+        b.nitems = nb;
+        if (a0.order) {
+            b.order = a0.order + i0;
+            b.item0 = 0;
+        } else {
+            b.item0 = a0.item0 + i0;
+        }
+        b.eq = ctx->d_eq;
+        b.eb = ctx->d_eb;
+        b.eaux = ctx->d_eaux;
+        if (b.persistent) CK(cudaMemsetAsync(ctx->d_qhead, 0, sizeof(int), st));
+        if ((s = dispatch(ctx, b, precision, st))) return s;
+        k_inv_finish<<<nb, INV_NT, ismem, st>>>(b);
+        CKL();
+    }
+    return ENKFG_OK;
+}
+
 static enkfg_status run_etkf_batched(enkfg_ctx* ctx, const CalcArgs& a0, int precision, cudaStream_t st)
 {
     enkfg_status s;
@@ -628,11 +704,15 @@ enkfg_status run_transforms(enkfg_ctx* ctx, const enkfg_calc_params* p, cudaStre
         CK(cudaMemsetAsync(ctx->d_qhead, 0, sizeof(int), st));
         cudaEventRecord(ctx->ev[2], st);
     }
-    // ETKF: the batched eigensolver (the per-type diagnostics need the
-    // point's own QL pass, so they keep the in-kernel one)
-    const bool defer = (p->mode != ENKFG_MODE_ENOI && p->scheme == ENKFG_SCHEME_ETKF && !(a.want_diag && a.ntypes > 1));
-    if (defer) {
+    // ETKF: the batched eigensolver; DEnKF / EnOI: the batched inverse (the
+    // per-type diagnostics need the point's own solve for their second
+    // pass, so they keep the in-kernel one)
+    const bool etkf = (p->mode != ENKFG_MODE_ENOI && p->scheme == ENKFG_SCHEME_ETKF);
+    const bool defer = !(a.want_diag && a.ntypes > 1);
+    if (defer && etkf) {
         if ((s = run_etkf_batched(ctx, a, p->precision, st))) return s;
+    } else if (defer) {
+        if ((s = run_inv_batched(ctx, a, p->precision, st))) return s;
     } else {
         if ((s = dispatch(ctx, a, p->precision, st))) return s;
     }

@@ -367,6 +367,38 @@ __device__ inline void diag_single(const CalcArgs& a, int pt, int p, double dfs,
     }
 }
 
+// DEnKF / EnOI outputs from M^-1 in A (calcs.c:279-284): w = M^-1 S's, the
+// degrees of freedom m - tr(M^-1), and (DEnKF) T = (I + M^-1) / 2 with the
+// relaxation; returns dfs.  Threads of a block of NT.
+template <int NT>
+__device__ inline double denkf_outputs(const CalcArgs& a, int pt, const double* A, int lda, const double* b,
+                                       double* red)
+{
+    const int tid = threadIdx.x, m = a.m, md = a.md;
+    const size_t tbase = (size_t)pt * md * m;
+    double dpart = 0.0;
+    for (int r = tid; r < m; r += NT) {
+        double wv = 0.0;
+        for (int k = 0; k < m; ++k) wv = fma(A[r * lda + k], b[k], wv);
+        a.w[(size_t)pt * m + r] = (float)wv;
+        if (a.w64) a.w64[(size_t)pt * m + r] = wv;
+        dpart += 1.0 - A[r * lda + r];
+    }
+    const double dfs = la::block_sum<NT>(dpart, red);
+    if (a.mode != ENKFG_MODE_ENOI && a.T != nullptr) {
+        for (int i = tid; i < md * m; i += NT) {
+            int e1 = i / m, e2 = i - e1 * m;
+            double t = 0.5 * A[e1 * lda + e2];
+            if (e1 == e2) t += 0.5;
+            if (e1 == e2) t = (t - 1.0) * a.alpha + 1.0;
+            else t = t * a.alpha;
+            a.T[tbase + i] = (float)t;
+            if (a.T64) a.T64[tbase + i] = t;
+        }
+    }
+    return dfs;
+}
+
 // FP64 solve of one point from M = I + S'S in A (n = m, stride lda) and b =
 // S's, then relaxation, float cast and diagnostics.  A is overwritten (by the
 // eigenvectors, or by M^-1); tile/tld: FP64 chunk buffer for the per-type
@@ -375,13 +407,28 @@ __device__ inline void solve_point(const CalcArgs& a, int pt, int slot, int p, i
                                    double qz, double* A, int lda, double* b, double trss, double* d, double* e,
                                    double* cs, double* sn, double* v, const PointScratch& s, double* tile, int tld)
 {
-    const int tid = threadIdx.x, m = a.m, md = a.md;
+    const int tid = threadIdx.x, m = a.m;
     const bool need_inv = (a.mode == ENKFG_MODE_ENOI || a.scheme == ENKFG_SCHEME_DENKF);
-    const size_t tbase = (size_t)pt * md * m;
     int rc = 0;
     double dfs = 0.0;
     const double* Q;
     const double* gq;
+    if (need_inv && a.defer) {
+        // batched inverse: save the upper triangle of M, S's and the point's
+        // count and tr(S'S); k_inv_finish does the rest
+        const size_t q0 = (size_t)slot * m * m;
+        for (int i = tid; i < m * m; i += CALC_NT) {
+            const int r = i / m, c = i - r * m;
+            if (c >= r) a.eq[q0 + i] = A[r * lda + c];
+        }
+        if (tid < m) a.eb[(size_t)slot * m + tid] = b[tid];
+        if (tid == 0) {
+            a.eaux[2 * (size_t)slot] = (double)p;
+            a.eaux[2 * (size_t)slot + 1] = trss;
+        }
+        __syncthreads();
+        return;
+    }
     if (!need_inv && a.defer) {
         // batched eigensolver: tridiagonalise here, save the slot; the QL
         // chains run one thread per point and the rest in k_eig_finish
@@ -412,24 +459,7 @@ __device__ inline void solve_point(const CalcArgs& a, int pt, int slot, int p, i
     } else {
         // DEnKF (calcs.c:279-284) / EnOI: M^-1 in place (symmetric sweep)
         rc = la::spd_inverse<CALC_NT>(A, m, lda, cs, sn, d, s.ictl + 16);
-        if (tid < m) {
-            double wv = 0.0;
-            for (int k = 0; k < m; ++k) wv = fma(A[tid * lda + k], b[k], wv);
-            a.w[(size_t)pt * m + tid] = (float)wv;
-            if (a.w64) a.w64[(size_t)pt * m + tid] = wv;
-        }
-        dfs = la::block_sum<CALC_NT>(tid < m ? 1.0 - A[tid * lda + tid] : 0.0, s.red);
-        if (a.mode != ENKFG_MODE_ENOI && a.T != nullptr) {
-            for (int i = tid; i < md * m; i += CALC_NT) {
-                int e1 = i / m, e2 = i - e1 * m;
-                double t = 0.5 * A[e1 * lda + e2];
-                if (e1 == e2) t += 0.5;
-                if (e1 == e2) t = (t - 1.0) * a.alpha + 1.0;
-                else t = t * a.alpha;
-                a.T[tbase + i] = (float)t;
-                if (a.T64) a.T64[tbase + i] = t;
-            }
-        }
+        dfs = denkf_outputs<CALC_NT>(a, pt, A, lda, b, s.red);
         Q = A;
         gq = nullptr;
     }
