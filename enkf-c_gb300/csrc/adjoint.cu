@@ -194,7 +194,7 @@ __global__ void __launch_bounds__(CALC_NT) k_adjoint(AdjArgs A)
     double* sn = (double*)sp;     sp += MP * 8;
     double* w = (double*)sp;      sp += MP * 8;
     double* lam = (double*)sp;    sp += MP * 8;
-    double* tmp = (double*)sp;    sp += MP * 8;
+    sp += MP * 8;                 // (spare row: keeps the layout of the shared-memory size formula)
     double* tss = (double*)sp;    sp += ENKFG_MAXTYPES * 8;
     double* tpd = (double*)sp;    sp += ENKFG_MAXTYPES * 8;
     double* red = (double*)sp;    sp += (CALC_NT / 32) * 8;

@@ -385,7 +385,16 @@ __device__ inline double denkf_outputs(const CalcArgs& a, int pt, const double* 
         dpart += 1.0 - A[r * lda + r];
     }
     const double dfs = la::block_sum<NT>(dpart, red);
-    if (a.mode != ENKFG_MODE_ENOI && a.T != nullptr) {
+    if (a.mode != ENKFG_MODE_ENOI && a.T != nullptr && a.T64 == nullptr && a.alpha == 1.0) {
+        // no relaxation, float output only: off the diagonal (float)(a / 2)
+        // is (float)a / 2 (halving commutes with rounding), so only the
+        // diagonal needs FP64 arithmetic
+        for (int i = tid; i < md * m; i += NT) {
+            int e1 = i / m, e2 = i - e1 * m;
+            a.T[tbase + i] = (e1 == e2) ? (float)(0.5 * A[e1 * lda + e2] + 0.5)
+                                        : 0.5f * (float)A[e1 * lda + e2];
+        }
+    } else if (a.mode != ENKFG_MODE_ENOI && a.T != nullptr) {
         for (int i = tid; i < md * m; i += NT) {
             int e1 = i / m, e2 = i - e1 * m;
             double t = 0.5 * A[e1 * lda + e2];

@@ -344,18 +344,18 @@ __device__ void ql_replay(double* A, int n, int lda, const double2* __restrict__
 //     a_ik <- u_i / D              (i != k),
 //     a_kk <- -1 / D,
 // and after all n pivots the matrix holds -A^-1.  Every step updates the
-// whole upper triangle in parallel (one FMA per element): warps take pairs
-// of rows (i, n-1-i), whose lengths add up to n+1, and lanes the columns, so
-// all threads stay busy instead of the serial chains of triangular solves.
+// whole upper triangle in parallel (one FMA per element): the rows, paired
+// as (i, n-1-i) so that each pair holds n+1 elements, are laid end to end
+// and dealt to the threads one element each, so all threads stay busy
+// instead of the serial chains of triangular solves (and every warp
+// instruction of the FP64 update but the last is full).
 // Without pivoting this is stable for M = I + S'S (pivots >= 1).  On return A
 // holds the full symmetric A^-1.  U, V: n doubles each; piv: 2 doubles.
 // Returns 0, or 1 if a pivot was not positive.
 template <int NT>
 __device__ int spd_inverse(double* A, int n, int lda, double* U, double* V, double* piv, int* ctl)
 {
-    constexpr int NW = NT / 32;
-    const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
-    const int npair = (n + 1) >> 1;
+    const int tid = threadIdx.x;
     if (tid == 0) {
         ctl[3] = 0;
         double p0 = A[0];
@@ -374,11 +374,15 @@ __device__ int spd_inverse(double* A, int n, int lda, double* U, double* V, doub
             V[i] = u * inv;
         }
         __syncthreads();
-        for (int pr = wid; pr < npair; pr += NW) {
-            const int i0 = pr, i1 = n - 1 - pr;
-            const int len0 = n - i0;
-            const int total = (i0 == i1) ? len0 : n + 1;
-            for (int c = lane; c < total; c += 32) {
+        // the upper triangle as row pairs (i, n-1-i) of n+1 elements, laid
+        // end to end and dealt to the threads one element each: every warp
+        // instruction but the last updates 32 elements
+        const int ntri = n * (n + 1) / 2, np1 = n + 1;
+        for (int el = tid; el < ntri; el += NT) {
+            {
+                const int pr = el / np1, c = el - pr * np1;
+                const int i0 = pr, i1 = n - 1 - pr;
+                const int len0 = n - i0;
                 int i, j;
                 if (c < len0) {
                     i = i0;
@@ -404,11 +408,12 @@ __device__ int spd_inverse(double* A, int n, int lda, double* U, double* V, doub
         }
         __syncthreads();
     }
-    // -A^-1 (upper) -> A^-1 (both triangles)
+    // -A^-1 (upper) -> A^-1 (both triangles); the negation is a sign flip
     for (int idx = tid; idx < n * n; idx += NT) {
         const int i = idx / n, j = idx - i * n;
         if (j < i) continue;
-        const double v = -A[(size_t)i * lda + j];
+        const double v =
+            __longlong_as_double(__double_as_longlong(A[(size_t)i * lda + j]) ^ (long long)0x8000000000000000ull);
         A[(size_t)i * lda + j] = v;
         if (j != i) A[(size_t)j * lda + i] = v;
     }
