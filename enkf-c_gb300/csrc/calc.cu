@@ -476,7 +476,7 @@ __global__ void __launch_bounds__(CALC_NT) k_eig_finish(CalcArgs a, const double
 // symmetric sweep and forms w, dfs and T.  Inside the transform kernel the
 // sweep leaves the FP64 units idle between pivots (barriers, the pivot's
 // reciprocal); here a dozen points per SM keep them busy.
-#define INV_NT 64
+#define INV_NT 128
 
 __global__ void __launch_bounds__(INV_NT) k_inv_finish(CalcArgs a)
 {
