@@ -68,44 +68,44 @@ __host__ __device__ __forceinline__ uint32_t idesc_tf32(int M, int N)
     return (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
 }
 
-__device__ __forceinline__ void mma_tf32(uint32_t dtmem, uint64_t da, uint64_t db, uint32_t idesc, uint32_t acc)
+// Warp-collective issue: every lane of a converged warp passes the same
+// (warp-uniform) operands and one lane, picked once by elect.sync, issues --
+// the same lane for the MMAs and their commit, so the commit tracks them.
+// the elected lane of a converged warp (1 there, 0 elsewhere); the forms
+// below take it, so that one election serves all of a round's MMAs
+__device__ __forceinline__ uint32_t elect_lane()
 {
+    uint32_t r;
     asm volatile(
-        "{\n\t.reg .pred p;\n\t"
-        "setp.ne.b32 p, %4, 0;\n\t"
-        "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(dtmem),
-        "l"(da), "l"(db), "r"(idesc), "r"(acc));
+        "{\n\t.reg .pred e;\n\t.reg .b32 x;\n\t"
+        "elect.sync x|e, 0xffffffff;\n\t"
+        "selp.u32 %0, 1, 0, e;\n\t}\n"
+        : "=r"(r));
+    return r;
 }
 
-__device__ __forceinline__ void commit(uint64_t* mbar)
-{
-    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(mbar))
-                 : "memory");
-}
-
-// Warp-collective forms: every lane of a converged warp passes the same
-// (warp-uniform) operands and elect.sync picks the one lane that issues --
-// always the same lane while the whole warp is active, so the commit tracks
-// that lane's MMAs.
-__device__ __forceinline__ void mma_tf32_warp(uint32_t dtmem, uint64_t da, uint64_t db, uint32_t idesc, uint32_t acc)
+__device__ __forceinline__ void mma_tf32_lead(uint32_t dtmem, uint64_t da, uint64_t db, uint32_t idesc, uint32_t acc,
+                                              uint32_t lead)
 {
     asm volatile(
-        "{\n\t.reg .pred p, e;\n\t.reg .b32 r;\n\t"
-        "elect.sync r|e, 0xffffffff;\n\t"
+        "{\n\t.reg .pred p, e;\n\t"
+        "setp.ne.b32 e, %5, 0;\n\t"
         "setp.ne.b32 p, %4, 0;\n\t"
         "@e tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(dtmem),
-        "l"(da), "l"(db), "r"(idesc), "r"(acc));
+        "l"(da), "l"(db), "r"(idesc), "r"(acc), "r"(lead));
 }
 
-__device__ __forceinline__ void commit_warp(uint64_t* mbar)
+__device__ __forceinline__ void commit_lead(uint64_t* mbar, uint32_t lead)
 {
     asm volatile(
-        "{\n\t.reg .pred e;\n\t.reg .b32 r;\n\t"
-        "elect.sync r|e, 0xffffffff;\n\t"
+        "{\n\t.reg .pred e;\n\t"
+        "setp.ne.b32 e, %1, 0;\n\t"
         "@e tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n\t}\n" ::"r"(
-            smem_u32(mbar))
+            smem_u32(mbar)),
+        "r"(lead)
         : "memory");
 }
+
 
 __device__ __forceinline__ void fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
 __device__ __forceinline__ void fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
@@ -526,25 +526,28 @@ struct GramProcTC {
             if constexpr (ST) {
                 // A = [lo; Z] (buffer 0) or [Z; lo] (buffer 1) for lo*hi'
                 uint64_t dz = tc::desc_kmajor_noswizzle(tc::smem_u32(buf == 0 ? tL : ms.zblock()), 128u, sbo);
+                const uint32_t lead = tc::elect_lane();
                 for (int g = 0; g < ngroups; ++g, dh += 16u, dm += 16u, dl += 16u, dz += 16u) {
                     const uint32_t fresh = (win_obs == 0 && g == 0) ? 0u : 1u;
-                    tc::mma_tf32_warp(dhh, dh, dh, idesc, fresh);   // [hi; mid] hi'
-                    tc::mma_tf32_warp(dr, dh, dm, idesc, fresh);    // [hi; mid] mid'
-                    tc::mma_tf32_warp(dr, dh, dl, idesc, 1u);       // [hi; mid] lo'
-                    tc::mma_tf32_warp(dr, dz, dh, idesc, 1u);       // lo hi'
+                    tc::mma_tf32_lead(dhh, dh, dh, idesc, fresh, lead);   // [hi; mid] hi'
+                    tc::mma_tf32_lead(dr, dh, dm, idesc, fresh, lead);    // [hi; mid] mid'
+                    tc::mma_tf32_lead(dr, dh, dl, idesc, 1u, lead);       // [hi; mid] lo'
+                    tc::mma_tf32_lead(dr, dz, dh, idesc, 1u, lead);       // lo hi'
                 }
+                tc::commit_lead(ms.mbar + buf, lead);
             } else {
+                const uint32_t lead = tc::elect_lane();
                 for (int g = 0; g < ngroups; ++g, dh += 16u, dm += 16u, dl += 16u) {
                     const uint32_t fresh = (win_obs == 0 && g == 0) ? 0u : 1u;
-                    tc::mma_tf32_warp(dhh, dh, dh, idesc, fresh);
-                    tc::mma_tf32_warp(dr, dh, dm, idesc, fresh);
-                    tc::mma_tf32_warp(dr, dm, dh, idesc, 1u);
-                    tc::mma_tf32_warp(dr, dh, dl, idesc, 1u);
-                    tc::mma_tf32_warp(dr, dl, dh, idesc, 1u);
-                    tc::mma_tf32_warp(dr, dm, dm, idesc, 1u);
+                    tc::mma_tf32_lead(dhh, dh, dh, idesc, fresh, lead);
+                    tc::mma_tf32_lead(dr, dh, dm, idesc, fresh, lead);
+                    tc::mma_tf32_lead(dr, dm, dh, idesc, 1u, lead);
+                    tc::mma_tf32_lead(dr, dh, dl, idesc, 1u, lead);
+                    tc::mma_tf32_lead(dr, dl, dh, idesc, 1u, lead);
+                    tc::mma_tf32_lead(dr, dm, dm, idesc, 1u, lead);
                 }
+                tc::commit_lead(ms.mbar + buf, lead);
             }
-            tc::commit_warp(ms.mbar + buf);
         }
         sy.out |= 1u << buf;
         ++rnd;
