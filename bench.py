@@ -342,7 +342,10 @@ def run_gpu(args, rank, world, local_rank):
         HE_pin = torch.from_numpy(w.HE).pin_memory().numpy()
         f_pin = torch.from_numpy(fields_h).pin_memory().numpy()
         ctx.set_stream(None)
+        # caller-owned pinned outputs (as a host application would keep its
+        # transform and field buffers); the fields are updated in place
         T_h = torch.empty((w.nj_s, w.ni_s, w.nmem_dynamic, m), dtype=torch.float32).pin_memory().numpy()
+        W_h = torch.empty((w.nj_s, w.ni_s, m), dtype=torch.float32).pin_memory().numpy()
 
         def e2e_step():
             ctx.rebuild_index()
@@ -350,9 +353,9 @@ def run_gpu(args, rank, world, local_rank):
             ctx.calcinnandspread(want=False)
             ctx.standardise()
             out = ctx.calctransforms(mode=w.mode, scheme=w.scheme, alpha=w.alpha, path=path, precision=prec,
-                                     want_diag=False)
+                                     want_diag=False, T_out=T_h if w.mode != enkfg.MODE_ENOI else None, w_out=W_h)
             res = ctx.updatefields(f_pin, w.numlevels, levels, mode=w.mode, nmem=m, nmem_dynamic=w.nmem_dynamic,
-                                   inflation=w.inflation, inf_ratio=w.inf_ratio, precision=prec)
+                                   inflation=w.inflation, inf_ratio=w.inf_ratio, precision=prec, inplace=True)
             return out, res
 
         for _ in range(max(1, min(args.warmup, 2))):
@@ -368,7 +371,7 @@ def run_gpu(args, rank, world, local_rank):
         d2h = out["w"].nbytes + (out["T"].nbytes if out["T"] is not None else 0) + res.nbytes
         e2e = {"value": w.nanalyses / te, "unit": UNIT, "ms_per_step": te * 1e3, "h2d_bytes_per_step": int(h2d),
                "d2h_bytes_per_step": int(d2h)}
-        del T_h
+        del T_h, W_h
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:

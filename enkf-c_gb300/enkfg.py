@@ -259,12 +259,21 @@ class Enkfg:
         self._ck(self.L.enkfg_autotune_reset(self.h))
 
     def calctransforms(self, mode=MODE_ENKF, scheme=SCHEME_ETKF, alpha=1.0, path=PATH_PLAIN, precision=PREC_FP64,
-                       want64=False, want_diag=True, tune=False):
+                       want64=False, want_diag=True, tune=False, T_out=None, w_out=None):
+        """T_out / w_out: caller-owned float32 arrays of the output shapes
+        (e.g. in pinned memory) to write T and w into; allocated if None."""
         npts = self.nj * self.ni
         m, md = self.nmem, self.nmem_dynamic
         enkf = mode != MODE_ENOI
-        T = np.zeros((self.nj, self.ni, md, m), np.float32) if enkf else None
-        w = np.zeros((self.nj, self.ni, m), np.float32)
+
+        def out_array(a, shape):
+            if a is None:
+                return np.zeros(shape, np.float32)
+            if a.dtype != np.float32 or a.shape != shape or not a.flags.c_contiguous:
+                raise ValueError(f"output array must be C-contiguous float32 {shape}")
+            return a
+        T = out_array(T_out, (self.nj, self.ni, md, m)) if enkf else None
+        w = out_array(w_out, (self.nj, self.ni, m))
         T64 = np.zeros((self.nj, self.ni, md, m)) if (want64 and enkf) else None
         w64 = np.zeros((self.nj, self.ni, m)) if want64 else None
         out = dict(T=T, w=w, T64=T64, w64=w64)
@@ -324,10 +333,16 @@ class Enkfg:
     # ---- update ----------------------------------------------------------
     def updatefields(self, fields, numlevels, levels, *, mode=MODE_ENKF, nmem=None, nmem_dynamic=None, surfk=0,
                      issurfacevar=0, inflation=1.0, inf_ratio=float("nan"), output_increment=0, applylog=0, j1=0,
-                     j2=-1, precision=PREC_FP64, want_infl=False):
+                     j2=-1, precision=PREC_FP64, want_infl=False, inplace=False):
         """fields [nfield][nmem(+1 for EnOI)][jsize][mni] float32, updated
-        and returned (a copy); levels [nfield]."""
-        f = np.ascontiguousarray(fields, np.float32).copy()
+        and returned (a copy, or `fields` itself when inplace -- which then
+        must be C-contiguous float32); levels [nfield]."""
+        if inplace:
+            if fields.dtype != np.float32 or not fields.flags.c_contiguous:
+                raise ValueError("inplace update needs a C-contiguous float32 array")
+            f = fields
+        else:
+            f = np.ascontiguousarray(fields, np.float32).copy()
         nl = np.ascontiguousarray(numlevels, np.int32)
         lv = np.ascontiguousarray(levels, np.int32)
         nfield = f.shape[0]
