@@ -205,7 +205,7 @@ def run_gpu(args, rank, world, local_rank):
         import torch.distributed as dist
         dist.barrier()
     torch.cuda.synchronize()
-    calc_ms, upd_ms, kern_ms, ukern_ms = [], [], [], []
+    calc_ms, upd_ms, kern_ms, ukern_ms, fin_ms = [], [], [], [], []
     l0 = ctx.launches
     with ClockSampler(local_rank) as clk:
         ev[0].record(stream)
@@ -215,10 +215,14 @@ def run_gpu(args, rank, world, local_rank):
             stream.synchronize()
             calc_ms.append(parts[0].elapsed_time(parts[1]))
             upd_ms.append(parts[1].elapsed_time(parts[2]))
-            # the library's CUDA events on the launching stream: [2] the
-            # transform kernel alone, [3] the update kernel(s)
+            # the library's CUDA events on the launching stream: the
+            # transform kernel alone (kernel_times [0]), the batched
+            # eigensolver / inverse after it ([1]), the update kernel(s)
+            # (stage_times [3])
             st_ms = ctx.stage_times()
-            kern_ms.append(st_ms[2])
+            kt = ctx.kernel_times()
+            kern_ms.append(kt[0])
+            fin_ms.append(kt[1])
             ukern_ms.append(st_ms[3])
         ev[1].record(stream)
         torch.cuda.synchronize()
@@ -328,6 +332,7 @@ def run_gpu(args, rank, world, local_rank):
     tpa = TRAFFIC_PER_ANALYSIS.get((w.cfg, kname))
     roof["traffic"] = tpa * w.nanalyses if tpa else None
     roof["kernel_ms"] = kern_t * 1e3
+    roof["finishing_kernels_ms"] = statistics.median(fin_ms)
     roof["flops_per_launch"] = flops
     upa = TRAFFIC_PER_ANALYSIS.get((w.cfg, "k_update_cells")) if m <= 64 else None
     uroof = {"kernel": "k_update_cells" if m <= 64 else "k_update_v2", "bound": "hbm",

@@ -540,7 +540,9 @@ static enkfg_status run_inv_batched(enkfg_ctx* ctx, const CalcArgs& a0, int prec
         b.eb = ctx->d_eb;
         b.eaux = ctx->d_eaux;
         if (b.persistent) CK(cudaMemsetAsync(ctx->d_qhead, 0, sizeof(int), st));
+        if (i0 == 0) cudaEventRecord(ctx->ev[8], st);
         if ((s = dispatch(ctx, b, precision, st))) return s;
+        if (i0 == 0) cudaEventRecord(ctx->ev[9], st);
         k_inv_finish<<<nb, INV_NT, ismem, st>>>(b);
         CKL();
     }
@@ -588,7 +590,9 @@ static enkfg_status run_etkf_batched(enkfg_ctx* ctx, const CalcArgs& a0, int pre
         b.eb = ctx->d_eb;
         b.eaux = ctx->d_eaux;
         if (b.persistent) CK(cudaMemsetAsync(ctx->d_qhead, 0, sizeof(int), st));
+        if (i0 == 0) cudaEventRecord(ctx->ev[8], st);
         if ((s = dispatch(ctx, b, precision, st))) return s;
+        if (i0 == 0) cudaEventRecord(ctx->ev[9], st);
         k_ql_batch<<<div_up(nb, QLB_T), QLB_T, qsmem, st>>>(nb, m, ctx->d_eaux, ctx->d_ed, ctx->d_ee, ctx->d_eval,
                                                            ctx->d_erot, rcap, ctx->d_ehdr, hcap, ctx->d_enh);
         CKL();
@@ -714,7 +718,9 @@ enkfg_status run_transforms(enkfg_ctx* ctx, const enkfg_calc_params* p, cudaStre
     } else if (defer) {
         if ((s = run_inv_batched(ctx, a, p->precision, st))) return s;
     } else {
+        cudaEventRecord(ctx->ev[8], st);
         if ((s = dispatch(ctx, a, p->precision, st))) return s;
+        cudaEventRecord(ctx->ev[9], st);
     }
     cudaEventRecord(ctx->ev[3], st);
     ctx->t_mode = p->mode;

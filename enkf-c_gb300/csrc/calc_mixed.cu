@@ -182,11 +182,11 @@ __device__ __forceinline__ void tmem_ld8_nowait(uint32_t taddr, uint32_t (&r)[8]
 
 __device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
 
-__device__ __forceinline__ float to_tf32(float x)
+// FP32 -> TF32, round to nearest, ties away from zero, on the bits: finite
+// inputs (a carry into the exponent gives the next binade, as it should)
+__device__ __forceinline__ float tf32_rna(float x)
 {
-    uint32_t r;
-    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
-    return __uint_as_float(r);
+    return __uint_as_float((__float_as_uint(x) + 0x1000u) & 0xFFFFE000u);
 }
 
 // asynchronous global -> shared copies (16 bytes through L2 only, 8 bytes)
@@ -227,7 +227,7 @@ struct MixedShared {
     double* sraw;          // [buffer][kcm] innovations of those observations (cp.async)
     int kcm;
     int ldv;               // row stride of raw: >= mpad, = 8 mod 32 (conflict-free reads)
-    const float* qs;       // [2][m]: quantum q_r and 1/q_r
+    const float* qs;       // [2][m]: quantum q_r and the rounding constant 1.5 2^23 q_r
     float2* Macc;          // [m x lda] double-float S'S (later reused as FP64)
     float* Mrest;          // [m x lda] stacked form: the remainder products from the offset lanes
     int lda;
@@ -419,19 +419,24 @@ struct GramProcTC {
                                                  int nrg, int nkg, int kg, int rg0, int rstep, int lane)
     {
         const int m = a.m;
-        const float* q = ms.qs;
-        const float* iq = ms.qs + m;
+        const float* cq = ms.qs + m;   // 1.5 2^23 q_r: (v + c) - c rounds v to a multiple of q_r
         double ssq = 0.0;
         auto one = [&](int rg, int r) -> float {
             const float v = __fmul_rn(rp[rg << 3], ck);
             if (TS) ssq += (double)v * (double)v;
-            const float hi = __fmul_rn(rintf(__fmul_rn(v, iq[r])), q[r]);
+            // hi = q rint(v / q): |v| <= 256 q < 2^22 q keeps v + c in the
+            // binade of c, whose spacing is q (ties to even, as rint)
+            const float hi = __fsub_rn(__fadd_rn(v, cq[r]), cq[r]);
             const float r1 = __fsub_rn(v, hi);
-            const float md = tc::to_tf32(r1);
+            // mid = r1 and lo = r1 - mid rounded to TF32, to nearest with
+            // ties away from zero (half a TF32 unit added to the magnitude
+            // bits, then the 13 low bits cleared); cut toward zero instead,
+            // both would lean the same way and their error would add up
+            const float md = tc::tf32_rna(r1);
             const int off = ((rg * nkg + kg) << 5) + lane;
             tH[off] = hi;
             tM[off] = md;
-            tL[off] = tc::to_tf32(__fsub_rn(r1, md));
+            tL[off] = tc::tf32_rna(__fsub_rn(r1, md));
             return v;
         };
         if constexpr (FS) {
@@ -863,7 +868,7 @@ static size_t mixed_smem_bytes(int m, int kc, int lseg, int st)
     if (st) s += (size_t)m * lda * 4;                      // Mrest
     s += (size_t)2 * kc * mixed_ldv(m) * 4;                // raw S rows, two buffers
     s += (size_t)2 * kc * 8;                               // raw innovations, two buffers
-    s += (size_t)2 * m * 4;                                // quantum q, 1/q
+    s += (size_t)2 * m * 4;                                // quantum q, rounding constant
     s += 16;                                               // alignment
     s += (size_t)m * lda * 8;                              // Macc (also A)
     s += (size_t)2 * ((kc + 3) & ~3) * 4;                  // tapered innovations, taper of the round
@@ -931,7 +936,7 @@ __global__ void __launch_bounds__(CALC_NT, 2) k_transforms_mixed(CalcArgs a, int
     for (size_t i = tid; i < ntile; i += CALC_NT) tiles[i] = 0.0f;
     for (int r = tid; r < m; r += CALC_NT) {
         qs[r] = a.qscale[r];
-        qs[m + r] = a.qscale[ENKFG_MAXMEM + r];
+        qs[m + r] = 12582912.0f * a.qscale[r];   // 1.5 2^23 q_r
     }
     tc::fence_before();
     __syncthreads();

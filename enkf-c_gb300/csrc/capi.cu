@@ -92,7 +92,7 @@ ENKFG_API enkfg_status enkfg_create(int device, enkfg_ctx** out)
         free(ctx);
         return ENKFG_ECUDA;
     }
-    for (int k = 0; k < 8; ++k) cudaEventCreate(&ctx->ev[k]);
+    for (int k = 0; k < 10; ++k) cudaEventCreate(&ctx->ev[k]);
     if (cudaMalloc(&ctx->d_qhead, 1024 * sizeof(int)) != cudaSuccess ||
         cudaMalloc(&ctx->d_rfac, ENKFG_MAXTYPES * sizeof(double)) != cudaSuccess ||
         cudaMalloc(&ctx->d_rfac_sqrt, ENKFG_MAXTYPES * sizeof(double)) != cudaSuccess ||
@@ -119,7 +119,7 @@ ENKFG_API void enkfg_destroy(enkfg_ctx* ctx)
                      ctx->d_numlevels, ctx->d_fields, ctx->d_infl };
     for (size_t k = 0; k < sizeof(ptrs) / sizeof(ptrs[0]); ++k)
         if (ptrs[k]) cudaFree(ptrs[k]);
-    for (int k = 0; k < 8; ++k)
+    for (int k = 0; k < 10; ++k)
         if (ctx->ev[k]) cudaEventDestroy(ctx->ev[k]);
     if (ctx->own_stream) ctx->stream = ctx->own_stream;
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
@@ -275,6 +275,16 @@ ENKFG_API enkfg_status enkfg_stage_times(const enkfg_ctx* ctx, float* ms4)
         else
             ms4[k] = ctx->stage_ms[k];
     }
+    cudaGetLastError();
+    return ENKFG_OK;
+}
+
+ENKFG_API enkfg_status enkfg_kernel_times(const enkfg_ctx* ctx, float* ms2)
+{
+    if (!ctx || !ms2) return ENKFG_EINVAL;
+    ms2[0] = ms2[1] = 0.0f;
+    if (cudaEventElapsedTime(&ms2[0], ctx->ev[8], ctx->ev[9]) != cudaSuccess) ms2[0] = 0.0f;
+    if (cudaEventElapsedTime(&ms2[1], ctx->ev[9], ctx->ev[3]) != cudaSuccess) ms2[1] = 0.0f;
     cudaGetLastError();
     return ENKFG_OK;
 }

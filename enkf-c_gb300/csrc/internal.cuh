@@ -46,7 +46,7 @@ struct enkfg_ctx {
     char err[1024];
     long long launches;
     float stage_ms[4];
-    cudaEvent_t ev[8];
+    cudaEvent_t ev[10];         // [8, 9]: the transform kernel alone (first batch)
 
     // observation types
     int ntypes;

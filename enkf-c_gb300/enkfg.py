@@ -43,7 +43,7 @@ EXPORTS = ["enkfg_create", "enkfg_destroy", "enkfg_last_error", "enkfg_status_st
            "enkfg_set_S", "enkfg_get_S", "enkfg_set_grid", "enkfg_transform_dims", "enkfg_local_obs",
            "enkfg_calc_transforms", "enkfg_calc_transforms_dev", "enkfg_transforms_dev_ptr",
            "enkfg_set_transforms", "enkfg_update_fields", "enkfg_update_fields_dev", "enkfg_set_hybrid_ensemble",
-           "enkfg_set_hybrid_ensemble_dev", "enkfg_kernel_launches", "enkfg_stage_times", "enkfg_set_stream",
+           "enkfg_set_hybrid_ensemble_dev", "enkfg_kernel_launches", "enkfg_stage_times", "enkfg_kernel_times", "enkfg_set_stream",
            "enkfg_set_HE_dev", "enkfg_rebuild_index", "enkfg_local_offsets_noalloc", "enkfg_autotune_table",
            "enkfg_autotune_reset", "enkfg_adjoint_transforms", "enkfg_adjoint_mean"]
 
@@ -141,6 +141,12 @@ class Enkfg:
     def stage_times(self):
         ms = (C.c_float * 4)()
         self._ck(self.L.enkfg_stage_times(self.h, ms))
+        return list(ms)
+
+    def kernel_times(self):
+        """[transform kernel ms, rest of the transform stage ms]"""
+        ms = (C.c_float * 2)()
+        self._ck(self.L.enkfg_kernel_times(self.h, ms))
         return list(ms)
 
     # ---- inputs ----------------------------------------------------------

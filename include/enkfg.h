@@ -237,6 +237,12 @@ ENKFG_API long long enkfg_kernel_launches(const enkfg_ctx* ctx);
  * points return before it ends); stages run inside a CUDA graph keep the
  * values of their last eager run. */
 ENKFG_API enkfg_status enkfg_stage_times(const enkfg_ctx* ctx, float* ms4);
+/* The last transform stage split in milliseconds (CUDA events on the
+ * launching stream): [0] the transform kernel (the first batch's, when the
+ * stage runs in batches), [1] from its end to the end of the stage (the
+ * batched eigensolver or inverse, later batches).  No reference
+ * counterpart: it refines stage [2] of enkfg_stage_times. */
+ENKFG_API enkfg_status enkfg_kernel_times(const enkfg_ctx* ctx, float* ms2);
 
 /* No counterpart in the reference.  CSR offsets of local-observation
  * counts (offsets[k] = counts[0] + ... + counts[k-1], offsets[n] = total; the
