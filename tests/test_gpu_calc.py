@@ -141,6 +141,25 @@ def test_transforms_multitype_stride(ctx, mode, scheme):
         assert rel(out["psrf"], ref["psrf"]) < 1e-4
 
 
+@pytest.mark.parametrize("mode,scheme", [(0, 0), (1, 0), (0, 1)])
+def test_transforms_batched_solvers(ctx, mode, scheme):
+    """Without per-type diagnostics the solve leaves the transform kernel: the
+    batched DEnKF/EnOI inverse and the batched ETKF eigensolver, plain and
+    batched paths, against the FP64 oracle."""
+    w = synth.make(2, scale=0.1, nobs=6000, with_fields=False, nmem=20)
+    w.locrad = 12.0
+    S, s = prepare(w)
+    obs, tabs = obsset(w)
+    ref = oracle.calctransforms(obs, mode=mode, scheme=scheme, nmem=w.nmem, nmem_dynamic=w.nmem, alpha=0.7,
+                                stride=w.stride, x=w.x, y=w.y, S=S, s=s, want64=True, threads=4)
+    gpu_setup(ctx, w, S, s, tabs)
+    for path in (0, 1):
+        out = ctx.calctransforms(mode=mode, scheme=scheme, alpha=0.7, path=path, want64=True, want_diag=False)
+        if mode != 1:
+            assert per_point_rel(out["T64"], ref["T64"]) < 1e-10
+        assert per_point_rel(out["w64"], ref["w64"]) < 1e-10
+
+
 def test_transforms_hybrid_dynamic_subset(ctx):
     """m_dyn < m (hybrid): T is the leading m_dyn columns."""
     w = synth.make(1, scale=0.5, with_fields=False)
