@@ -549,6 +549,43 @@ static enkfg_status run_inv_batched(enkfg_ctx* ctx, const CalcArgs& a0, int prec
     return ENKFG_OK;
 }
 
+// Batched Householder tridiagonalisation for the ETKF eigensolver: one small
+// CTA per point (dozens per SM at small nmem), from the upper triangle of M
+// the transform kernel saved; Q, the diagonal and the off-diagonal go back
+// to the slot for k_ql_batch and k_eig_finish.  In the transform kernel the
+// reduction's FP64 divisions and dependent FMA chains left the SM idle.
+template <int NT>
+__global__ void __launch_bounds__(NT) k_tred_batch(CalcArgs a)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int m = a.m, lda = (m % 2 == 0) ? m + 1 : m + 2;
+    const int tid = threadIdx.x, slot = blockIdx.x;
+    double* A = (double*)smem_raw;
+    double* d = A + (size_t)m * lda;
+    double* e = d + m;
+    double* red = e + m;
+    if (!(a.eaux[2 * (size_t)slot] > 0.0)) return;   // empty point
+    const size_t q0 = (size_t)slot * m * m;
+    for (int i = tid; i < m * m; i += NT) {
+        const int r = i / m, c = i - r * m;
+        if (c >= r) {
+            const double v = a.eq[q0 + i];
+            A[r * lda + c] = v;
+            A[c * lda + r] = v;
+        }
+    }
+    __syncthreads();
+    la::tred2<NT>(A, m, lda, d, e, red);
+    for (int i = tid; i < m * m; i += NT) {
+        const int r = i / m, c = i - r * m;
+        a.eq[q0 + i] = A[r * lda + c];
+    }
+    for (int i = tid; i < m; i += NT) {
+        a.ed[(size_t)slot * m + i] = d[i];
+        a.ee[(size_t)slot * m + i] = e[i];
+    }
+}
+
 static enkfg_status run_etkf_batched(enkfg_ctx* ctx, const CalcArgs& a0, int precision, cudaStream_t st)
 {
     enkfg_status s;
@@ -571,6 +608,10 @@ static enkfg_status run_etkf_batched(enkfg_ctx* ctx, const CalcArgs& a0, int pre
     const size_t qsmem = (size_t)2 * m * QLB_T * 8;
     const int lda = (m % 2 == 0) ? m + 1 : m + 2;
     const size_t fsmem = ((size_t)m * lda + 6 * (size_t)m + CALC_NT / 32) * 8 + 16;
+    const size_t tsmem = ((size_t)m * lda + 2 * (size_t)m + 4) * 8 + 16;
+    const bool tr64 = m <= 64;   // 64 threads up to nmem 64, else 128
+    if (tr64) CK(cudaFuncSetAttribute(k_tred_batch<64>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tsmem));
+    else CK(cudaFuncSetAttribute(k_tred_batch<128>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tsmem));
     CK(cudaFuncSetAttribute(k_ql_batch, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)qsmem));
     CK(cudaFuncSetAttribute(k_eig_finish, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fsmem));
     for (int i0 = 0; i0 < nitems; i0 += (int)B) {
@@ -593,6 +634,9 @@ static enkfg_status run_etkf_batched(enkfg_ctx* ctx, const CalcArgs& a0, int pre
         if (i0 == 0) cudaEventRecord(ctx->ev[8], st);
         if ((s = dispatch(ctx, b, precision, st))) return s;
         if (i0 == 0) cudaEventRecord(ctx->ev[9], st);
+        if (tr64) k_tred_batch<64><<<nb, 64, tsmem, st>>>(b);
+        else k_tred_batch<128><<<nb, 128, tsmem, st>>>(b);
+        CKL();
         k_ql_batch<<<div_up(nb, QLB_T), QLB_T, qsmem, st>>>(nb, m, ctx->d_eaux, ctx->d_ed, ctx->d_ee, ctx->d_eval,
                                                            ctx->d_erot, rcap, ctx->d_ehdr, hcap, ctx->d_enh);
         CKL();

@@ -422,36 +422,17 @@ __device__ inline void solve_point(const CalcArgs& a, int pt, int slot, int p, i
     double dfs = 0.0;
     const double* Q;
     const double* gq;
-    if (need_inv && a.defer) {
-        // batched inverse: save the upper triangle of M, S's and the point's
-        // count and tr(S'S); k_inv_finish does the rest
+    if (a.defer) {
+        // batched solve: save the upper triangle of M, S's and the point's
+        // count and tr(S'S); the batched inverse (k_inv_finish) or the
+        // batched eigensolver (k_tred_batch, k_ql_batch, k_eig_finish) does
+        // the rest
         const size_t q0 = (size_t)slot * m * m;
         for (int i = tid; i < m * m; i += CALC_NT) {
             const int r = i / m, c = i - r * m;
             if (c >= r) a.eq[q0 + i] = A[r * lda + c];
         }
         if (tid < m) a.eb[(size_t)slot * m + tid] = b[tid];
-        if (tid == 0) {
-            a.eaux[2 * (size_t)slot] = (double)p;
-            a.eaux[2 * (size_t)slot + 1] = trss;
-        }
-        __syncthreads();
-        return;
-    }
-    if (!need_inv && a.defer) {
-        // batched eigensolver: tridiagonalise here, save the slot; the QL
-        // chains run one thread per point and the rest in k_eig_finish
-        la::tred2<CALC_NT>(A, m, lda, d, e, s.red);
-        const size_t q0 = (size_t)slot * m * m;
-        for (int i = tid; i < m * m; i += CALC_NT) {
-            const int r = i / m, c = i - r * m;
-            a.eq[q0 + i] = A[r * lda + c];
-        }
-        if (tid < m) {
-            a.ed[(size_t)slot * m + tid] = d[tid];
-            a.ee[(size_t)slot * m + tid] = e[tid];
-            a.eb[(size_t)slot * m + tid] = b[tid];
-        }
         if (tid == 0) {
             a.eaux[2 * (size_t)slot] = (double)p;
             a.eaux[2 * (size_t)slot + 1] = trss;
