@@ -58,9 +58,12 @@ __device__ void tred2(double* A, int n, int lda, double* d, double* e, double* r
                 if (tid == 0) e[i] = Ai[l];
                 __syncthreads();
             } else {
+                // one division a step, multiplications per element (FP64
+                // division is a long instruction sequence on GB300)
+                const double iscale = 1.0 / scale;
                 part = 0.0;
                 for (int k = tid; k <= l; k += NT) {
-                    double v = Ai[k] / scale;
+                    double v = Ai[k] * iscale;
                     Ai[k] = v;
                     part += v * v;
                 }
@@ -75,15 +78,16 @@ __device__ void tred2(double* A, int n, int lda, double* d, double* e, double* r
                 }
                 __syncthreads();
                 // p = A u / h (into e[0..l]); column i keeps u / h
+                const double ih = 1.0 / h;
                 for (int j = tid; j <= l; j += NT) {
                     double g2 = 0.0;
                     const double* Aj = A + (size_t)j * lda;
                     for (int k = 0; k <= j; ++k) g2 += Aj[k] * Ai[k];
                     for (int k = j + 1; k <= l; ++k) g2 += A[(size_t)k * lda + j] * Ai[k];
-                    e[j] = g2 / h;
+                    e[j] = g2 * ih;
                 }
                 __syncthreads();
-                for (int j = tid; j <= l; j += NT) A[(size_t)j * lda + i] = Ai[j] / h;
+                for (int j = tid; j <= l; j += NT) A[(size_t)j * lda + i] = Ai[j] * ih;
                 part = 0.0;
                 for (int j = tid; j <= l; j += NT) part += e[j] * Ai[j];
                 double ff = block_sum<NT>(part, red);
