@@ -341,6 +341,47 @@ def run_gpu(args, rank, world, local_rank):
              "frac": ub / ukern_t / 1e9 / peaks["hbm_gbs"], "bytes_per_launch": ub, "kernel_ms": ukern_t * 1e3,
              "peak_source": peak_src}
 
+    # the forward operator on the device (das_getHE; H_surf_standard with
+    # bilinear interpolation): HE [m][nobs] of the observed layer (field 0,
+    # layer 0) from the resident ensemble, one launch per observation type.
+    # Algorithmic bytes: the observed layer read once and HE written once.
+    def measure_he():
+        ctx.set_obs_positions(w.lon.astype(np.float64), w.lat.astype(np.float64))
+        layer = fields_d[0]                                  # [m][nj][ni]
+        hb = layer.numel() * 4 + m * w.nobs * 4
+
+        def he_pass(evs=None):
+            ctx.begin_HE(m, w.nmem_dynamic)
+            with torch.cuda.stream(stream):
+                flush.zero_()
+            if evs:
+                evs[0].record(stream)
+            for t in range(w.ntypes):
+                ctx.map_obs_dev(t, layer.data_ptr(), m, w.ni, w.nj, numlev_d.data_ptr(), stream=stream.cuda_stream)
+            if evs:
+                evs[1].record(stream)
+            ctx.finish_HE()
+
+        for _ in range(3):
+            he_pass()
+        he_ms = []
+        for _ in range(5):
+            evs = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+            he_pass(evs)
+            torch.cuda.synchronize()
+            he_ms.append(evs[0].elapsed_time(evs[1]))
+        ht = statistics.median(he_ms) / 1e3
+        return {"kernel": "k_map_obs", "ms": ht * 1e3, "launches_per_pass": w.ntypes,
+                "obs_member_values_per_s": w.nobs * m / ht, "bytes_per_pass": hb, "achieved_gbs": hb / ht / 1e9,
+                "peak_gbs": peaks["hbm_gbs"], "frac": hb / ht / 1e9 / peaks["hbm_gbs"]}
+
+    he_stage = None
+    if args.he:
+        try:
+            he_stage = measure_he()
+        except Exception as exc:   # report, do not hide: the cycle's numbers stand
+            he_stage = {"error": str(exc)[:300]}
+
     # end to end through the host-buffer C ABI (pinned host memory)
     e2e = None
     if rank == 0 or world > 1:
@@ -400,6 +441,7 @@ def run_gpu(args, rank, world, local_rank):
             "roofline": roof, "roofline_update": uroof, "graph": graph, "e2e": e2e, "cpu_baseline": cpu,
             "gpu_launches": int(launches),
             "plain_gpu_fp64": plain64,
+            "he_stage": he_stage,
             "speedup_vs_plain_gpu_fp64": (value / plain64["value"]) if plain64 else None,
             "clocks": clk.summary(),
         }
@@ -511,6 +553,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--graph", type=int, default=1, help="also time the cycle replayed from a CUDA graph")
     ap.add_argument("--compare-fp64", type=int, default=1, help="also time the plain GPU FP64 path")
+    ap.add_argument("--he", type=int, default=1, help="also time the device forward operator (HE stage)")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))

@@ -27,15 +27,6 @@ enkfg_status cuda_fail(enkfg_ctx* c, cudaError_t e, const char* what, int line)
     return ENKFG_ECUDA;
 }
 
-#define NEED(cond, code, ...)                \
-    do {                                     \
-        if (!(cond)) {                       \
-            set_err(ctx, __VA_ARGS__);       \
-            return code;                     \
-        }                                    \
-    } while (0)
-
-#define SETDEV() CK(cudaSetDevice(ctx->device))
 
 extern "C" {
 static enkfg_status check_calc(enkfg_ctx* ctx, const enkfg_calc_params* p);
@@ -116,7 +107,8 @@ ENKFG_API void enkfg_destroy(enkfg_ctx* ctx)
                      ctx->d_oy, ctx->d_oz, ctx->d_qx, ctx->d_qy, ctx->d_qz, ctx->d_T, ctx->d_w, ctx->d_T64,
                      ctx->d_w64, ctx->d_nlobs, ctx->d_dfs, ctx->d_srf, ctx->d_pnlobs, ctx->d_pdfs, ctx->d_psrf,
                      ctx->d_counts, ctx->d_order, ctx->d_qhead, ctx->d_status_pt, ctx->d_scratch,
-                     ctx->d_numlevels, ctx->d_fields, ctx->d_infl };
+                     ctx->d_numlevels, ctx->d_fields, ctx->d_infl, ctx->d_fi, ctx->d_fj, ctx->d_fk, ctx->d_Hx,
+                     ctx->d_hflag, ctx->d_hids, ctx->d_hsrc, ctx->d_hlev, ctx->d_hoff };
     for (size_t k = 0; k < sizeof(ptrs) / sizeof(ptrs[0]); ++k)
         if (ptrs[k]) cudaFree(ptrs[k]);
     for (int k = 0; k < 10; ++k)
@@ -338,7 +330,8 @@ ENKFG_API enkfg_status enkfg_set_obs(enkfg_ctx* ctx, int nobs, const float* lon,
     size_t n = nobs > 0 ? nobs : 1, cap;
     void** bufs[] = { (void**)&ctx->d_lon, (void**)&ctx->d_lat, (void**)&ctx->d_type, (void**)&ctx->d_status,
                       (void**)&ctx->d_estd, (void**)&ctx->d_value, (void**)&ctx->d_ox, (void**)&ctx->d_oy,
-                      (void**)&ctx->d_oz };
+                      (void**)&ctx->d_oz, (void**)&ctx->d_fi, (void**)&ctx->d_fj, (void**)&ctx->d_fk,
+                      (void**)&ctx->d_Hx };
     for (size_t k = 0; k < sizeof(bufs) / sizeof(bufs[0]); ++k) {
         if (*bufs[k]) cudaFree(*bufs[k]);
         *bufs[k] = nullptr;
@@ -355,6 +348,8 @@ ENKFG_API enkfg_status enkfg_set_obs(enkfg_ctx* ctx, int nobs, const float* lon,
     CK(cudaMalloc(&ctx->d_oy, n * sizeof(double)));
     if (ctx->geographic) CK(cudaMalloc(&ctx->d_oz, n * sizeof(double)));
     ctx->nobs = nobs;
+    ctx->pos_set = ctx->pos_3d = false;
+    ctx->he_nmem = 0;
     if (nobs > 0) {
         CK(cudaMemcpyAsync(ctx->d_lon, lon, nobs * sizeof(float), cudaMemcpyHostToDevice, ctx->stream));
         CK(cudaMemcpyAsync(ctx->d_lat, lat, nobs * sizeof(float), cudaMemcpyHostToDevice, ctx->stream));
@@ -372,7 +367,7 @@ ENKFG_API enkfg_status enkfg_set_obs(enkfg_ctx* ctx, int nobs, const float* lon,
     return ENKFG_OK;
 }
 
-static enkfg_status alloc_S(enkfg_ctx* ctx, int nmem, int nmem_dynamic)
+enkfg_status alloc_S(enkfg_ctx* ctx, int nmem, int nmem_dynamic)
 {
     if (ctx->d_S) cudaFree(ctx->d_S);
     if (ctx->d_s) cudaFree(ctx->d_s);

@@ -166,6 +166,25 @@ struct enkfg_ctx {
     size_t fields_cap;
     float* d_infl;
     size_t infl_cap;
+
+    // forward-operator (HE) stage
+    double* d_fi;               // [nobs] observation.fij[0]
+    double* d_fj;               // [nobs] observation.fij[1]
+    float* d_fk;                // [nobs] observation.fk (NULL until given)
+    float* d_Hx;                // [nobs] EnOI background row
+    unsigned long long* d_hflag;// [4] first bad forecast (obs << 32 | value bits), first position off the grid, BADFC count
+    int* d_hids;
+    size_t hids_cap;
+    float* d_hsrc;              // host fields staged on the device
+    size_t hsrc_cap;
+    int* d_hlev;
+    size_t hlev_cap;
+    float* d_hoff;
+    size_t hoff_cap;
+    int he_nmem, he_nmem_dyn;   // ensemble of the open HE stage (0: none open)
+    bool he_bg;                 // the open stage has a background row
+    bool pos_set;               // observation positions uploaded
+    bool pos_3d;                // with fk
 };
 
 // ---------------------------------------------------------------------------
@@ -186,6 +205,16 @@ enkfg_status cuda_fail(enkfg_ctx* c, cudaError_t e, const char* what, int line);
         cudaError_t e_ = cudaGetLastError();                            \
         if (e_ != cudaSuccess) return cuda_fail(ctx, e_, "kernel launch", __LINE__); \
     } while (0)
+
+#define NEED(cond, code, ...)                \
+    do {                                     \
+        if (!(cond)) {                       \
+            set_err(ctx, __VA_ARGS__);       \
+            return code;                     \
+        }                                    \
+    } while (0)
+
+#define SETDEV() CK(cudaSetDevice(ctx->device))
 
 template <typename T>
 static inline enkfg_status ensure(enkfg_ctx* ctx, T** p, size_t* cap, size_t n)
@@ -227,5 +256,7 @@ enkfg_status resident_ctas(enkfg_ctx* ctx, const void* fn, int nt, size_t dsmem,
 enkfg_status run_update(enkfg_ctx* ctx, const enkfg_update_params* p, const int* d_numlevels, int nfield,
                         const int* levels, float* d_fields, float* d_infl, cudaStream_t st);
 enkfg_status run_innovations(enkfg_ctx* ctx, cudaStream_t st);
+// (re)allocate S, s and std_f for nmem members of the current observations
+extern "C" enkfg_status alloc_S(enkfg_ctx* ctx, int nmem, int nmem_dynamic);
 enkfg_status run_standardise(enkfg_ctx* ctx, cudaStream_t st);
 enkfg_status run_hybrid(enkfg_ctx* ctx, int nmem, int nmem_d, double gamma, int nij, float* d_v, cudaStream_t st);

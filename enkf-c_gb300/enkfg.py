@@ -45,13 +45,21 @@ EXPORTS = ["enkfg_create", "enkfg_destroy", "enkfg_last_error", "enkfg_status_st
            "enkfg_set_transforms", "enkfg_update_fields", "enkfg_update_fields_dev", "enkfg_set_hybrid_ensemble",
            "enkfg_set_hybrid_ensemble_dev", "enkfg_kernel_launches", "enkfg_stage_times", "enkfg_kernel_times", "enkfg_set_stream",
            "enkfg_set_HE_dev", "enkfg_rebuild_index", "enkfg_local_offsets_noalloc", "enkfg_autotune_table",
-           "enkfg_autotune_reset", "enkfg_adjoint_transforms", "enkfg_adjoint_mean"]
+           "enkfg_autotune_reset", "enkfg_adjoint_transforms", "enkfg_adjoint_mean", "enkfg_set_obs_positions",
+           "enkfg_begin_HE", "enkfg_map_obs", "enkfg_map_obs_dev", "enkfg_finish_HE"]
 
 
 class EnkfgError(RuntimeError):
     def __init__(self, status: int, msg: str):
         super().__init__(f"{STATUS.get(status, status)}: {msg}")
         self.status = status
+
+
+class HopParams(C.Structure):
+    """enkfg_hop_params: one forward-operator call (H_surf_standard /
+    H_subsurf_standard, model2obs.c:127-348)."""
+    _fields_ = [("ni", C.c_int), ("nj", C.c_int), ("nk", C.c_int), ("three_d", C.c_int), ("ksurf", C.c_int),
+                ("periodic_i", C.c_int), ("offset_kind", C.c_int), ("skip_bad", C.c_int)]
 
 
 class Grid(C.Structure):
@@ -178,6 +186,59 @@ class Enkfg:
         md = m if nmem_dynamic is None else int(nmem_dynamic)
         self.nmem, self.nmem_dynamic = m, md
         self._ck(self.L.enkfg_set_HE(self.h, C.c_int(m), C.c_int(md), _p(HE, C.c_float)))
+
+    # ---- forward operator on the device (das_getHE, ensobs.c:46-490) -----
+    def set_obs_positions(self, fi, fj, fk=None):
+        """observation.fij[0..1] (double) and observation.fk (float, or None)."""
+        fi = np.ascontiguousarray(fi, np.float64)
+        fj = np.ascontiguousarray(fj, np.float64)
+        fk = None if fk is None else np.ascontiguousarray(fk, np.float32)
+        self._ck(self.L.enkfg_set_obs_positions(self.h, _p(fi, C.c_double), _p(fj, C.c_double), _p(fk, C.c_float)))
+
+    def begin_HE(self, nmem, nmem_dynamic=None, with_background=False):
+        md = nmem if nmem_dynamic is None else int(nmem_dynamic)
+        self.nmem, self.nmem_dynamic = int(nmem), md
+        self._ck(self.L.enkfg_begin_HE(self.h, C.c_int(int(nmem)), C.c_int(md), C.c_int(int(with_background))))
+
+    def map_obs(self, obstype, fields, numlevels, *, mem0=0, ids=None, three_d=False, ksurf=0, periodic_i=False,
+                offset=None, offset_kind=0, skip_bad=False):
+        """H for one observation type over members mem0.. (mem0 = -1: the EnOI
+        background).  fields [nfield][nk][nj][ni] (three_d) or [nfield][nj][ni]."""
+        fields = np.ascontiguousarray(fields, np.float32)
+        if three_d:
+            nfield, nk, nj, ni = fields.shape
+        else:
+            (nfield, nj, ni), nk = fields.shape, 1
+        prm = HopParams(ni, nj, nk, int(three_d), int(ksurf), int(bool(periodic_i)),
+                        int(offset_kind) if offset is not None else 0, int(bool(skip_bad)))
+        nl = np.ascontiguousarray(numlevels, np.int32)
+        off = None if offset is None else np.ascontiguousarray(offset, np.float32)
+        idv = None if ids is None else np.ascontiguousarray(ids, np.int32)
+        nids = self.nobs if idv is None else idv.size
+        self._ck(self.L.enkfg_map_obs(self.h, C.byref(prm), C.c_int(int(obstype)), C.c_int(nids), _p(idv, C.c_int),
+                                      C.c_int(int(mem0)), C.c_int(nfield), _p(fields, C.c_float), _p(nl, C.c_int),
+                                      _p(off, C.c_float)))
+
+    def map_obs_dev(self, obstype, fields_ptr, nfield, ni, nj, numlevels_ptr, *, nk=1, mem0=0, ids_ptr=None,
+                    nids=None, three_d=False, ksurf=0, periodic_i=False, offset_ptr=None, offset_kind=0,
+                    skip_bad=False, stream=None):
+        """Device-pointer form of map_obs (int addresses, e.g. tensor.data_ptr())."""
+        prm = HopParams(int(ni), int(nj), int(nk), int(three_d), int(ksurf), int(bool(periodic_i)),
+                        int(offset_kind) if offset_ptr else 0, int(bool(skip_bad)))
+        n = self.nobs if nids is None else int(nids)
+        self._ck(self.L.enkfg_map_obs_dev(self.h, C.byref(prm), C.c_int(int(obstype)), C.c_int(n),
+                                          C.c_void_p(ids_ptr) if ids_ptr else None, C.c_int(int(mem0)),
+                                          C.c_int(int(nfield)), C.c_void_p(fields_ptr), C.c_void_p(numlevels_ptr),
+                                          C.c_void_p(offset_ptr) if offset_ptr else None,
+                                          C.c_void_p(stream) if stream else None))
+
+    def finish_HE(self, mode=0, gamma=0.0, skip_bad=False):
+        """Returns (number of bad-forecast observations, statuses [nobs])."""
+        nbad = C.c_int(0)
+        status = np.zeros(self.nobs, np.int16)
+        self._ck(self.L.enkfg_finish_HE(self.h, C.c_int(int(mode)), C.c_double(gamma), C.c_int(int(skip_bad)),
+                                        C.byref(nbad), _p(status, C.c_short)))
+        return nbad.value, status
 
     def set_stream(self, stream):
         """Bind a cudaStream_t (int address, e.g. torch.cuda.Stream().cuda_stream)."""

@@ -80,6 +80,57 @@ ENKFG_API enkfg_status enkfg_set_obs(enkfg_ctx* ctx, int nobs, const float* lon,
  * dasystem.h:95).  nmem_dynamic < nmem for hybrid ensembles. */
 ENKFG_API enkfg_status enkfg_set_HE(enkfg_ctx* ctx, int nmem, int nmem_dynamic, const float* HE);
 
+/* ---- forward operator on the device (das_getHE, calc/ensobs.c:46-490) ----
+ * Instead of enkfg_set_HE, HE can be built on the device from the ensemble
+ * fields: enkfg_set_obs_positions once, enkfg_begin_HE, one enkfg_map_obs per
+ * observation type and member block (the reference calls H per type and
+ * member, ensobs.c:181-300), then enkfg_finish_HE. */
+
+/* Fractional grid positions of the observations (observation.fij[0..1],
+ * double, and observation.fk, float; observations.h:47-100).  fk may be NULL
+ * when no observation type is 3-D. */
+ENKFG_API enkfg_status enkfg_set_obs_positions(enkfg_ctx* ctx, const double* fi, const double* fj, const float* fk);
+
+/* das_getHE set-up (ensobs.c:72-83): HE [nmem][nobs] in the context filled
+ * with NaN, plus, when with_background (EnOI), the background row Hx. */
+ENKFG_API enkfg_status enkfg_begin_HE(enkfg_ctx* ctx, int nmem, int nmem_dynamic, int with_background);
+
+typedef struct {
+    int ni, nj, nk;             /* the variable's grid; nk = 1 for a 2-D field */
+    int three_d;                /* 0: H_surf_standard (2-D interpolation of one layer), 1: H_subsurf_standard */
+    int ksurf;                  /* grid_getsurflayerid: 0 or nk - 1 (3-D) */
+    int periodic_i;
+    int offset_kind;            /* "<type>:OFFSET" data: 0 none, 1 [nk], 2 [nj][ni], 3 [nk][nj][ni] */
+    int skip_bad;               /* --skip-bad-forecast-obs */
+} enkfg_hop_params;
+
+/* H_surf_standard / H_subsurf_standard (model2obs.c:127-181, 256-348) with
+ * evaluate_2d_obs / interpolate_3d_obs (model2obs.c:37-124), footprint 0, on a
+ * structured grid (interpolate2d_structured / interpolate3d_structured,
+ * utils.c:1140-1366), for members mem0 .. mem0 + nfield - 1 at once
+ * (mem0 = -1 with nfield = 1: the EnOI background row).  fields is
+ * [nfield][nk][nj][ni] (3-D) or [nfield][nj][ni] (2-D: the layer the
+ * reference reads), numlevels [nj][ni], offset laid out per offset_kind (or
+ * NULL).  The observations are ids[nids] (all of type obstype), or, when ids
+ * is NULL, every observation of type obstype with status 0 (obs_find_bytype,
+ * observations.c:1543).  A forecast that is not finite or exceeds 999999 in
+ * magnitude is ENKFG_ENUMERIC unless skip_bad (then NaN); a position off the
+ * grid is ENKFG_EINVAL. */
+ENKFG_API enkfg_status enkfg_map_obs(enkfg_ctx* ctx, const enkfg_hop_params* p, int obstype, int nids, const int* ids, int mem0, int nfield, const float* fields, const int* numlevels, const float* offset);
+/* Device-resident form: ids/fields/numlevels/offset are device addresses;
+ * nothing is synchronised, and errors surface in enkfg_finish_HE. */
+ENKFG_API enkfg_status enkfg_map_obs_dev(enkfg_ctx* ctx, const enkfg_hop_params* p, int obstype, int nids, const int* ids_dev, int mem0, int nfield, const float* fields_dev, const int* numlevels_dev, const float* offset_dev, void* stream);
+
+/* End of das_getHE (ensobs.c:372-490): with skip_bad, observations with a NaN
+ * forecast in any member (or in Hx) get status 10 (STATUS_BADFC); then for
+ * ENKFG_MODE_ENOI every member is recentred on the background (S_e += Hx -
+ * mean, float) and for ENKFG_MODE_HYBRID the dynamic and static anomalies are
+ * scaled by k_d = sqrt((m-1)/(m_d-1)) and k_s = sqrt(gamma (m-1)/(m_s-1)) about
+ * the dynamic mean.  nbad (or NULL) receives the number of observations with
+ * status 10 and status (or NULL) the statuses [nobs].  HE is then ready for
+ * enkfg_calc_innovations. */
+ENKFG_API enkfg_status enkfg_finish_HE(enkfg_ctx* ctx, int mode, double gamma, int skip_bad, int* nbad, short* status);
+
 /* das_calcinnandspread (ensobs.c:541-690): HE -> HA in place on the device,
  * innovations s_f = y - Hx and spread std_f; either output may be NULL. */
 ENKFG_API enkfg_status enkfg_calc_innovations(enkfg_ctx* ctx, double* s_f, double* std_f);

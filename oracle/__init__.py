@@ -374,3 +374,133 @@ def sethybridensemble(v, nmem_d, gamma):
     lib().or_sethybridensemble(C.c_int(m), C.c_int(nmem_d), C.c_int(m - nmem_d), C.c_double(gamma),
                                C.c_int(nij), _p(v, C.c_float), _p(vmean, C.c_double))
     return v, vmean
+
+
+# ---------------------------------------------------------------------------
+# forward operator (calc/model2obs.c) and the end of das_getHE (calc/ensobs.c)
+# ---------------------------------------------------------------------------
+
+REFLIB_UTILS = os.path.join(HERE, "_ref", "libenkf_ref_utils.so")
+_refu = None
+
+
+def reflib_utils():
+    """The reference's own common/utils.c (interpolation, taper), or None."""
+    global _refu
+    with _lock:
+        if _refu is None and os.path.exists(REFLIB_UTILS):
+            L = C.CDLL(REFLIB_UTILS)
+            L.interpolate2d_structured.restype = C.c_float
+            L.interpolate2d_structured.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_int]
+            L.interpolate3d_structured.restype = C.c_float
+            L.interpolate3d_structured.argtypes = [C.c_void_p, C.c_double, C.c_int, C.c_int, C.c_int, C.c_int,
+                                                   C.c_void_p, C.c_void_p, C.c_int]
+            L.taper_gc.restype = C.c_double
+            L.taper_gc.argtypes = [C.c_double]
+            L.ll2xyz.argtypes = [C.c_void_p, C.c_void_p]
+            _refu = L
+    return _refu
+
+
+def _rows(a: np.ndarray, t):
+    """Row-pointer array (the reference's alloc2d/alloc3d view) over a
+    contiguous array's leading dimensions."""
+    lead = int(np.prod(a.shape[:-1]))
+    flat = a.reshape(lead, a.shape[-1])
+    base = flat.ctypes.data
+    rows = (C.c_void_p * lead)(*[base + r * flat.strides[0] for r in range(lead)])
+    return rows
+
+
+def ref_interp2d(fi, fj, v, mask, periodic_i=0):
+    """interpolate2d_structured from the reference build, one position."""
+    L = reflib_utils()
+    v = np.ascontiguousarray(v, np.float32)
+    mask = np.ascontiguousarray(mask, np.int32)
+    nj, ni = v.shape
+    vr, mr = _rows(v, C.c_float), _rows(mask, C.c_int)
+    fij = (C.c_double * 3)(float(fi), float(fj), float("nan"))
+    return np.float32(L.interpolate2d_structured(fij, ni, nj, vr, mr, int(periodic_i)))
+
+
+def ref_interp3d(fi, fj, fk, v, nlevels, ktop, periodic_i=0):
+    """interpolate3d_structured from the reference build, one position;
+    v is [nk][nj][ni]."""
+    L = reflib_utils()
+    v = np.ascontiguousarray(v, np.float32)
+    nl = np.ascontiguousarray(nlevels, np.int32)
+    nk, nj, ni = v.shape
+    # alloc3d view: k -> row-pointer block, row -> data
+    rows = _rows(v, C.c_float)
+    planes = (C.c_void_p * nk)(*[C.addressof(rows) + k * nj * C.sizeof(C.c_void_p) for k in range(nk)])
+    fij = (C.c_double * 3)(float(fi), float(fj), float("nan"))
+    # the reference passes observation.fk (a float) as a double
+    fk = float(np.float32(fk))
+    return np.float32(L.interpolate3d_structured(fij, fk, ni, nj, nk, int(ktop), planes, _rows(nl, C.c_int),
+                                                 int(periodic_i)))
+
+
+def ref_taper_gc(x: float) -> float:
+    return reflib_utils().taper_gc(float(x))
+
+
+def interp2d(fi, fj, v, mask, periodic_i=0):
+    """or_interp2d, one position: (value, badpos)."""
+    v = np.ascontiguousarray(v, np.float32)
+    mask = np.ascontiguousarray(mask, np.int32)
+    nj, ni = v.shape
+    bad = C.c_int(0)
+    L = lib()
+    L.or_interp2d.restype = C.c_float
+    r = L.or_interp2d(C.c_double(fi), C.c_double(fj), C.c_int(ni), C.c_int(nj), _p(v, C.c_float),
+                      _p(mask, C.c_int), C.c_int(int(periodic_i)), C.byref(bad))
+    return np.float32(r), bool(bad.value)
+
+
+def interp3d(fi, fj, fk, v, nlevels, ktop, periodic_i=0):
+    """or_interp3d, one position (fk rounded to float as observation.fk)."""
+    v = np.ascontiguousarray(v, np.float32)
+    nl = np.ascontiguousarray(nlevels, np.int32)
+    nk, nj, ni = v.shape
+    bad = C.c_int(0)
+    L = lib()
+    L.or_interp3d.restype = C.c_float
+    r = L.or_interp3d(C.c_double(fi), C.c_double(fj), C.c_double(float(np.float32(fk))), C.c_int(ni), C.c_int(nj),
+                      C.c_int(nk), C.c_int(int(ktop)), _p(v, C.c_float), _p(nl, C.c_int),
+                      C.c_int(int(periodic_i)), C.byref(bad))
+    return np.float32(r), bool(bad.value)
+
+
+def map_obs(HE, row, field, numlevels, ids, fi, fj, fk=None, *, three_d=False, ktop=0, periodic_i=0,
+            offset=None, offset_kind=0, skip_bad=False):
+    """or_map_obs for one member: HE[row][ids] filled in place (HE float32
+    [rows][nobs]).  Returns the oracle's code (0, 1 + id of a bad forecast,
+    -(1 + id) of a position off the grid)."""
+    field = np.ascontiguousarray(field, np.float32)
+    if three_d:
+        nk, nj, ni = field.shape
+    else:
+        (nj, ni), nk = field.shape, 1
+    ids = np.ascontiguousarray(ids, np.int32)
+    fi = np.ascontiguousarray(fi, np.float64)
+    fj = np.ascontiguousarray(fj, np.float64)
+    fk = np.ascontiguousarray(fk if fk is not None else np.zeros(fi.size), np.float32)
+    off = np.ascontiguousarray(offset, np.float32) if offset is not None else None
+    dst = HE[row]
+    assert dst.flags.c_contiguous and dst.dtype == np.float32
+    return lib().or_map_obs(C.c_int(int(three_d)), C.c_int(ni), C.c_int(nj), C.c_int(nk), C.c_int(int(ktop)),
+                            C.c_int(int(periodic_i)), _p(np.ascontiguousarray(numlevels, np.int32), C.c_int),
+                            _p(off, C.c_float), C.c_int(int(offset_kind) if off is not None else 0),
+                            _p(field, C.c_float), C.c_int(ids.size), _p(ids, C.c_int), _p(fi, C.c_double),
+                            _p(fj, C.c_double), _p(fk, C.c_float), C.c_int(int(skip_bad)), _p(dst, C.c_float))
+
+
+def finish_HE(HE, status, *, mode, nmem_dynamic, gamma=0.0, Hx=None, skip_bad=False):
+    """or_finish_HE on copies: returns (HE, status, nbad)."""
+    S = np.ascontiguousarray(HE, np.float32).copy()
+    st = np.ascontiguousarray(status, np.int16).copy()
+    m, n = S.shape
+    hx = np.ascontiguousarray(Hx, np.float32) if Hx is not None else None
+    nbad = lib().or_finish_HE(C.c_int(mode), C.c_int(m), C.c_int(nmem_dynamic), C.c_double(gamma), C.c_int(n),
+                              _p(S, C.c_float), _p(hx, C.c_float), C.c_int(int(skip_bad)), _p(st, C.c_short))
+    return S, st, nbad

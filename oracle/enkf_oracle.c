@@ -710,6 +710,243 @@ void or_standardise(int nmem, int nobs, float* S, double* s_f, const float* estd
 }
 
 /* ---------------------------------------------------------------------------
+ * forward operator (calc/model2obs.c, common/utils.c) and the end of das_getHE
+ * (calc/ensobs.c)
+ * ------------------------------------------------------------------------- */
+
+#define OR_EPS_EDGE 1.0e-7                   /* common/utils.c:51 (EPS_FLOAT) */
+#define OR_STATUS_BADFC 10                   /* common/global.h:62 */
+
+/* Horizontal corner indices and weights of a fractional position: lower and
+ * upper index with weights (ceil - f) and (f - floor); a position on an integer
+ * takes its one index with weight 1; the edge rules wrap (periodic in i) or
+ * repeat the inner index (utils.c:1158-1184, 1270-1311).  Returns 0 where the
+ * reference's index assert would fail. */
+static int or_corners(double fi, double fj, int ni, int nj, int periodic_i, int i[2], int j[2], double wi[2], double wj[2])
+{
+    i[0] = (int) floor(fi);
+    wi[0] = ceil(fi) - fi;
+    i[1] = (int) ceil(fi);
+    wi[1] = fi - floor(fi);
+    j[0] = (int) floor(fj);
+    wj[0] = ceil(fj) - fj;
+    j[1] = (int) ceil(fj);
+    wj[1] = fj - floor(fj);
+    if (i[0] == i[1])
+        wi[0] = 1.0;
+    if (j[0] == j[1])
+        wj[0] = 1.0;
+    if (i[0] == -1)
+        i[0] = periodic_i ? ni - 1 : i[1];
+    if (i[1] == ni)
+        i[1] = periodic_i ? 0 : i[0];
+    if (j[0] == -1)
+        j[0] = j[1];
+    if (j[1] == nj)
+        j[1] = j[0];
+    return i[0] >= 0 && i[0] < ni && i[1] >= 0 && i[1] < ni && j[0] >= 0 && j[0] < nj && j[1] >= 0 && j[1] < nj;
+}
+
+/* interpolate2d_structured (common/utils.c:1140-1210): the four corners in
+ * the order (j1,i1) (j1,i2) (j2,i1) (j2,i2), each kept where mask != 0, the
+ * double sum renormalised by the kept weights and cast to float. */
+float or_interp2d(double fi, double fj, int ni, int nj, const float* v, const int* mask, int periodic_i, int* badpos)
+{
+    int i[2], j[2], a, b;
+    double wi[2], wj[2], sum = 0.0, w = 0.0;
+
+    /* positions at or below -1 fail the reference's assert (or read outside
+     * the row with weight 0); NaN fails here too */
+    if (!(fi > -1.0 && fj > -1.0)) {
+        *badpos = 1;
+        return NAN;
+    }
+    if (fi >= (double) ni)
+        fi = (double) ni - OR_EPS_EDGE;
+    if (fj >= (double) nj)
+        fj = (double) nj - OR_EPS_EDGE;
+    if (!or_corners(fi, fj, ni, nj, periodic_i, i, j, wi, wj)) {
+        *badpos = 1;
+        return NAN;
+    }
+    for (b = 0; b < 2; ++b)
+        for (a = 0; a < 2; ++a) {
+            size_t c = (size_t) j[b] * ni + i[a];
+
+            if (mask[c]) {
+                double ww = wj[b] * wi[a];
+
+                sum += v[c] * ww;
+                w += ww;
+            }
+        }
+    sum /= w;
+    return (float) sum;
+}
+
+/* interpolate3d_structured (common/utils.c:1252-1366): fk clamped to
+ * [0, nk-1]; layer k is wet at (j,i) when nlevels[j][i] > |ktop - k|; the
+ * eight corners in the order k1 then k2, each (j1,i1) (j1,i2) (j2,i1) (j2,i2),
+ * weight (wj wi) wk. */
+float or_interp3d(double fi, double fj, double fk, int ni, int nj, int nk, int ktop, const float* v, const int* nlevels, int periodic_i, int* badpos)
+{
+    int i[2], j[2], k[2], ktp[2], a, b, c;
+    double wi[2], wj[2], wk[2], sum = 0.0, w = 0.0;
+    size_t nij = (size_t) ni * nj;
+
+    if (!(fi > -1.0 && fj > -1.0) || isnan(fk)) {
+        *badpos = 1;
+        return NAN;
+    }
+    /* note the strict test on i (utils.c:1265) */
+    if (fi > (double) ni)
+        fi = (double) ni - OR_EPS_EDGE;
+    if (fj >= (double) nj)
+        fj = (double) nj - OR_EPS_EDGE;
+    if (fk < 0.0)
+        fk = 0.0;
+    if (fk > (double) (nk - 1))
+        fk = (double) (nk - 1);
+    k[0] = (int) floor(fk);
+    wk[0] = ceil(fk) - fk;
+    k[1] = (int) ceil(fk);
+    wk[1] = fk - floor(fk);
+    if (wk[0] == 0.0 && wk[1] == 0.0)
+        wk[0] = 1.0;
+    if (k[0] == k[1])
+        wk[0] = 1.0;
+    ktp[0] = abs(ktop - k[0]);
+    ktp[1] = abs(ktop - k[1]);
+    if (!or_corners(fi, fj, ni, nj, periodic_i, i, j, wi, wj)) {
+        *badpos = 1;
+        return NAN;
+    }
+    for (c = 0; c < 2; ++c)
+        for (b = 0; b < 2; ++b)
+            for (a = 0; a < 2; ++a) {
+                size_t q = (size_t) j[b] * ni + i[a];
+
+                if (nlevels[q] > ktp[c]) {
+                    double ww = wj[b] * wi[a] * wk[c];
+
+                    sum += v[(size_t) k[c] * nij + q] * ww;
+                    w += ww;
+                }
+            }
+    sum = sum / w;
+    return (float) sum;
+}
+
+/* H_surf_standard / H_subsurf_standard (calc/model2obs.c:127-181, 256-348):
+ * the field minus its OFFSET data, then evaluate_2d_obs / interpolate_3d_obs
+ * (calc/model2obs.c:37-124) with footprint 0, including the bad-forecast rule
+ * (!finite or |v| > MAXOBSVAL: NaN with --skip-bad-forecast-obs, else quit). */
+int or_map_obs(int three_d, int ni, int nj, int nk, int ktop, int periodic_i, const int* numlevels, const float* offset, int offset_kind, const float* field, int nids, const int* ids, const double* fi, const double* fj, const float* fk, int skip_bad, float* dst)
+{
+    size_t nij = (size_t) ni * nj, nv = three_d ? nij * (size_t) nk : nij, q;
+    const float* src = field;
+    float* tmp = NULL;
+    int n, rc = 0;
+
+    if (offset != NULL && offset_kind > 0) {
+        tmp = malloc(nv * sizeof(float));
+        for (q = 0; q < nv; ++q) {
+            float off = offset_kind == 1 ? offset[q / nij] : offset_kind == 2 ? offset[q % nij] : offset[q];
+
+            tmp[q] = field[q] - off;
+        }
+        src = tmp;
+    }
+    for (n = 0; n < nids; ++n) {
+        int id = ids[n], bad = 0;
+        float v = three_d ? or_interp3d(fi[id], fj[id], (double) fk[id], ni, nj, nk, ktop, src, numlevels, periodic_i, &bad)
+            : or_interp2d(fi[id], fj[id], ni, nj, src, numlevels, periodic_i, &bad);
+
+        if (bad) {
+            rc = -(1 + id);
+            break;
+        }
+        if (!isfinite(v) || fabs(v) > OR_MAXOBSVAL) {
+            if (!skip_bad) {
+                rc = 1 + id;
+                break;
+            }
+            v = NAN;
+        }
+        dst[id] = v;
+    }
+    free(tmp);
+    return rc;
+}
+
+/* das_getHE after the forward operators (calc/ensobs.c:372-490): the
+ * bad-forecast status, then the EnOI recentring on the background (float
+ * mean) or the hybrid rescaling (double means, k_d and k_s). */
+int or_finish_HE(int mode, int nmem, int nmem_d, double gamma, int nobs, float* S, const float* Hx, int skip_bad, short* status)
+{
+    int e, i, nbad = 0;
+
+    if (skip_bad) {
+        for (e = 0; e < nmem; ++e)
+            for (i = 0; i < nobs; ++i)
+                if (isnan(S[(size_t) e * nobs + i]))
+                    status[i] = OR_STATUS_BADFC;
+        if (mode == OR_MODE_ENOI)
+            for (i = 0; i < nobs; ++i)
+                if (isnan(Hx[i]))
+                    status[i] = OR_STATUS_BADFC;
+    }
+    for (i = 0; i < nobs; ++i)
+        nbad += status[i] == OR_STATUS_BADFC;
+
+    if (mode == OR_MODE_ENOI) {
+        float* mean = calloc(nobs > 0 ? nobs : 1, sizeof(float));
+
+        for (e = 0; e < nmem; ++e)
+            for (i = 0; i < nobs; ++i)
+                mean[i] += S[(size_t) e * nobs + i];
+        for (i = 0; i < nobs; ++i)
+            mean[i] /= (float) nmem;
+        for (e = 0; e < nmem; ++e)
+            for (i = 0; i < nobs; ++i)
+                S[(size_t) e * nobs + i] += Hx[i] - mean[i];
+        free(mean);
+    } else if (mode == OR_MODE_HYBRID) {
+        int nmem_s = nmem - nmem_d;
+        double k_d = (nmem_d > 1) ? sqrt((double) (nmem - 1) / (double) (nmem_d - 1)) : 0.0;
+        double k_s = sqrt(gamma * (double) (nmem - 1) / (double) (nmem_s - 1));
+        double* md = calloc(nobs > 0 ? nobs : 1, sizeof(double));
+        double* ms = calloc(nobs > 0 ? nobs : 1, sizeof(double));
+
+        for (e = 0; e < nmem_d; ++e)
+            for (i = 0; i < nobs; ++i)
+                md[i] += S[(size_t) e * nobs + i];
+        for (i = 0; i < nobs; ++i)
+            md[i] /= (double) nmem_d;
+        for (e = 0; e < nmem_d; ++e)
+            for (i = 0; i < nobs; ++i) {
+                float* p = &S[(size_t) e * nobs + i];
+
+                *p = (*p - md[i]) * k_d + md[i];
+            }
+        for (e = nmem_d; e < nmem; ++e)
+            for (i = 0; i < nobs; ++i)
+                ms[i] += S[(size_t) e * nobs + i];
+        for (i = 0; i < nobs; ++i)
+            ms[i] /= (double) nmem_s;
+        for (e = nmem_d; e < nmem; ++e)
+            for (i = 0; i < nobs; ++i) {
+                float* p = &S[(size_t) e * nobs + i];
+
+                *p = (*p - ms[i]) * k_s + md[i];
+            }
+        free(md);
+        free(ms);
+    }
+    return nbad;
+}
+
+/* ---------------------------------------------------------------------------
  * update (update/update.c, common/dasystem.c)
  * ------------------------------------------------------------------------- */
 

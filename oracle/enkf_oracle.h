@@ -82,6 +82,34 @@ void or_calcinnandspread(int nmem, int nobs, float* S, const float* value, const
 /* das_standardise (ensobs.c:849-898). rfactor is per type. */
 void or_standardise(int nmem, int nobs, float* S, double* s_f, const float* estd, const short* type, const double* rfactor);
 
+/* Forward operator on a structured grid, footprint 0.
+ * or_interp2d: interpolate2d_structured (utils.c:1140-1210); v [nj][ni],
+ * mask [nj][ni] (numlevels, nonzero = wet).
+ * or_interp3d: interpolate3d_structured (utils.c:1252-1366); v [nk][nj][ni],
+ * nlevels [nj][ni], ktop the surface layer (0 or nk - 1).
+ * Both return NaN and set *badpos where the reference's index assert would
+ * fail (the position is off the grid). */
+float or_interp2d(double fi, double fj, int ni, int nj, const float* v, const int* mask, int periodic_i, int* badpos);
+float or_interp3d(double fi, double fj, double fk, int ni, int nj, int nk, int ktop, const float* v, const int* nlevels, int periodic_i, int* badpos);
+
+/* H_surf_standard / H_subsurf_standard (model2obs.c:127-181, 256-348) with
+ * evaluate_2d_obs / interpolate_3d_obs (model2obs.c:37-124) for one member:
+ * the observations ids[nids] (all of one type) are interpolated from field
+ * (2-D: [nj][ni], the surface layer; 3-D: [nk][nj][ni]) minus the OFFSET data
+ * (offset_kind 0 none, 1 [nk], 2 [nj][ni], 3 [nk][nj][ni]) into dst[id].
+ * A value that is not finite or exceeds 999999 in magnitude becomes NaN when
+ * skip_bad, else the call stops and returns 1 + the observation id (the
+ * reference quits there).  Returns -(1 + id) for a position off the grid. */
+int or_map_obs(int three_d, int ni, int nj, int nk, int ktop, int periodic_i, const int* numlevels, const float* offset, int offset_kind, const float* field, int nids, const int* ids, const double* fi, const double* fj, const float* fk, int skip_bad, float* dst);
+
+/* End of das_getHE (ensobs.c:372-490) on HE [nmem][nobs] (and the EnOI
+ * background row Hx [nobs]): with skip_bad, observations with a NaN forecast
+ * get status 10 (STATUS_BADFC); then EnOI: S_e += Hx - mean (float); hybrid:
+ * dynamic anomalies scaled by k_d and static ones by k_s about their own
+ * means, both recentred on the dynamic mean.  Returns the number of
+ * observations with status 10. */
+int or_finish_HE(int mode, int nmem, int nmem_d, double gamma, int nobs, float* S, const float* Hx, int skip_bad, short* status);
+
 typedef struct {
     int mode;                   /* OR_MODE_ENKF / OR_MODE_HYBRID (fields), OR_MODE_ENOI (bg) */
     int nmem, nmem_dynamic;

@@ -16,8 +16,14 @@ GPU library without needing the reference at test time:
                   transforms.c:1250-1258 (restated here), numerics from the
                   reference's calcs.c: double T and w before the float cast.
                   The inputs (obs, S, s) are stored alongside.
+  model2obs.npz   interpolate2d_structured / interpolate3d_structured
+                  (common/utils.c, from oracle/_ref/libenkf_ref_utils.so) on
+                  seeded fields, wet-level counts, OFFSET data and positions
+                  (integer positions, all edges, periodic and not, both
+                  surface-layer conventions): the HE that H_surf_standard /
+                  H_subsurf_standard (calc/model2obs.c) give with footprint 0.
 
-Usage:  python tests/golden/make_golden.py
+Usage:  python tests/golden/make_golden.py [fixture ...]   (default: all)
 """
 from __future__ import annotations
 
@@ -113,10 +119,48 @@ def transforms():
     print("transforms:", pts.size, "points, mean p", nl.mean())
 
 
+def model2obs():
+    rng = np.random.default_rng(20250)
+    ni, nj, nk, m, n = 23, 17, 5, 3, 600
+    nl = rng.integers(0, nk + 1, (nj, ni)).astype(np.int32)
+    f2 = rng.normal(10.0, 2.0, (m, nj, ni)).astype(np.float32)
+    f3 = rng.normal(10.0, 2.0, (m, nk, nj, ni)).astype(np.float32)
+    off2 = rng.normal(0.0, 0.5, (nj, ni)).astype(np.float32)
+    off1 = rng.normal(0.0, 0.5, nk).astype(np.float32)
+    fi = rng.uniform(-0.99, ni + 0.5, n)
+    fj = rng.uniform(-0.99, nj + 0.5, n)
+    fi[:80] = np.maximum(np.floor(fi[:80]), 0.0)   # on grid lines (-1 fails the reference's assert)
+    fj[40:120] = np.maximum(np.floor(fj[40:120]), 0.0)
+    fi[120:140] = rng.uniform(-0.99, 0.0, 20)      # below the first column
+    fi[140:160] = rng.uniform(ni - 1.0, ni, 20)    # past the last column
+    fj[160:180] = rng.uniform(nj - 1.0, nj + 0.5, 20)
+    fi[fi == ni] = ni - 0.25                       # the 3-D rule asserts on fi == ni (utils.c:1265)
+    fk = rng.uniform(-0.6, nk - 0.4, n).astype(np.float32)
+    fk[::7] = np.round(fk[::7])
+    out = dict(ni=np.array(ni), nj=np.array(nj), nk=np.array(nk), numlevels=nl, f2=f2, f3=f3, off2=off2, off1=off1,
+               fi=fi, fj=fj, fk=fk)
+    for per in (0, 1):
+        he2 = np.empty((m, n), np.float32)
+        for e in range(m):
+            v = f2[e] - off2
+            for o in range(n):
+                he2[e, o] = oracle.ref_interp2d(fi[o], fj[o], v, nl, per)
+        out[f"he2_p{per}"] = he2
+        for ktop in (0, nk - 1):
+            he3 = np.empty((m, n), np.float32)
+            for e in range(m):
+                v = f3[e] - off1[:, None, None]
+                for o in range(n):
+                    he3[e, o] = oracle.ref_interp3d(fi[o], fj[o], fk[o], v, nl, ktop, per)
+            out[f"he3_p{per}_k{ktop}"] = he3
+    np.savez_compressed(os.path.join(HERE, "model2obs.npz"), **out)
+    print("model2obs:", n, "positions,", int(np.isnan(out["he2_p0"]).sum()), "all-dry 2-D cases")
+
+
 if __name__ == "__main__":
     oracle.build()
-    if oracle.reflib() is None:
-        sys.exit("the reference library oracle/_ref/libenkf_ref.so could not be built")
-    numerics()
-    kdtree()
-    transforms()
+    if oracle.reflib() is None or oracle.reflib_utils() is None:
+        sys.exit("the reference libraries under oracle/_ref could not be built")
+    which = sys.argv[1:] or ["numerics", "kdtree", "transforms", "model2obs"]
+    for name in which:
+        {"numerics": numerics, "kdtree": kdtree, "transforms": transforms, "model2obs": model2obs}[name]()

@@ -146,3 +146,119 @@ def test_hybrid_semantics():
     assert np.allclose(mean, v[:6].astype(np.float64).mean(0))
     k_d = np.sqrt(9.0 / 5.0)
     assert np.allclose(out[:6], (v[:6] - mean) * k_d + mean, atol=1e-5)
+
+
+# ---------------------------------------------------------------------------
+# forward operator (calc/model2obs.c; common/utils.c interpolation)
+# ---------------------------------------------------------------------------
+
+def same_bits(a, b):
+    """float32 arrays equal bit for bit, any NaN matching any NaN."""
+    a = np.asarray(a, np.float32)
+    b = np.asarray(b, np.float32)
+    na, nb = np.isnan(a), np.isnan(b)
+    return bool(np.array_equal(na, nb) and np.array_equal(a[~na].view(np.uint32), b[~nb].view(np.uint32)))
+
+
+def test_model2obs_against_reference_golden():
+    g = np.load(os.path.join(GOLD, "model2obs.npz"))
+    nk = int(g["nk"])
+    m, n = g["he2_p0"].shape
+    ids = np.arange(n, dtype=np.int32)
+    for per in (0, 1):
+        HE = np.full((m, n), np.nan, np.float32)
+        for e in range(m):
+            assert oracle.map_obs(HE, e, g["f2"][e], g["numlevels"], ids, g["fi"], g["fj"], periodic_i=per,
+                                  offset=g["off2"], offset_kind=2, skip_bad=True) == 0
+        assert same_bits(HE, g[f"he2_p{per}"]), f"2-D periodic={per}"
+        for ktop in (0, nk - 1):
+            HE = np.full((m, n), np.nan, np.float32)
+            for e in range(m):
+                assert oracle.map_obs(HE, e, g["f3"][e], g["numlevels"], ids, g["fi"], g["fj"], g["fk"],
+                                      three_d=True, ktop=ktop, periodic_i=per, offset=g["off1"], offset_kind=1,
+                                      skip_bad=True) == 0
+            assert same_bits(HE, g[f"he3_p{per}_k{ktop}"]), f"3-D periodic={per} ktop={ktop}"
+
+
+@pytest.mark.skipif(oracle.reflib_utils() is None, reason="reference library not built here")
+def test_interpolation_equals_reference_build_random():
+    rng = np.random.default_rng(7)
+    nj, ni, nk = 9, 11, 5
+    v = rng.standard_normal((nk, nj, ni)).astype(np.float32)
+    nl = rng.integers(0, nk + 1, (nj, ni)).astype(np.int32)
+    for t in range(1500):
+        fi = rng.uniform(-0.999, ni + 0.5)
+        fj = rng.uniform(-0.999, nj + 0.5)
+        if t % 7 == 0:
+            fi = float(rng.integers(0, ni))
+        if t % 11 == 0:
+            fj = float(rng.integers(0, nj))
+        fk = rng.uniform(-0.5, nk - 0.5) if t % 5 else float(rng.integers(0, nk))
+        for per in (0, 1):
+            a = oracle.ref_interp2d(fi, fj, v[0], nl, per)
+            b, bad = oracle.interp2d(fi, fj, v[0], nl, per)
+            assert not bad and same_bits(a, b), (fi, fj, per)
+            if fi == ni:
+                continue
+            for ktop in (0, nk - 1):
+                a = oracle.ref_interp3d(fi, fj, fk, v, nl, ktop, per)
+                b, bad = oracle.interp3d(fi, fj, fk, v, nl, ktop, per)
+                assert not bad and same_bits(a, b), (fi, fj, fk, ktop, per)
+
+
+@pytest.mark.skipif(oracle.reflib_utils() is None, reason="reference library not built here")
+def test_taper_equals_reference_build():
+    # the reference asserts 0 <= x <= 1 + 1e-8 (utils.c:1428)
+    for x in np.concatenate([np.linspace(0.0, 1.0, 2001), np.random.default_rng(3).uniform(0, 1, 500)]):
+        assert oracle.taper_gc(x) == oracle.ref_taper_gc(x)
+
+
+def test_map_obs_positions_off_grid_and_bad_forecasts():
+    nj, ni = 6, 7
+    f = np.full((nj, ni), 5.0, np.float32)
+    nl = np.ones((nj, ni), np.int32)
+    fi = np.array([1.5, -1.0, 2.0, np.nan])
+    fj = np.array([1.5, 2.0, -1.5, 1.0])
+    HE = np.full((1, 4), np.nan, np.float32)
+    # positions at or below -1 and NaN are off the grid: -(1 + id) of the first
+    assert oracle.map_obs(HE, 0, f, nl, np.array([0, 1]), fi, fj) == -2
+    assert oracle.map_obs(HE, 0, f, nl, np.array([2]), fi, fj) == -3
+    assert oracle.map_obs(HE, 0, f, nl, np.array([3]), fi, fj) == -4
+    # a huge value: 1 + id, or NaN with skip_bad
+    f[1, 1] = 5e6
+    HE[:] = np.nan
+    assert oracle.map_obs(HE, 0, f, nl, np.array([0]), fi, fj) == 1
+    assert oracle.map_obs(HE, 0, f, nl, np.array([0]), fi, fj, skip_bad=True) == 0 and np.isnan(HE[0, 0])
+    # all corners dry: 0/0 is not finite, a bad forecast
+    f[1, 1] = 5.0
+    nl[1:3, 1:3] = 0
+    assert oracle.map_obs(HE, 0, f, nl, np.array([0]), fi, fj) == 1
+
+
+def test_finish_HE_semantics():
+    rng = np.random.default_rng(11)
+    m, md, n = 10, 6, 200
+    HE = rng.normal(3.0, 1.0, (m, n)).astype(np.float32)
+    Hx = rng.normal(3.0, 1.0, n).astype(np.float32)
+    st = np.zeros(n, np.int16)
+    # EnOI: members recentred on the background, anomalies kept
+    S, st2, nbad = oracle.finish_HE(HE, st, mode=1, nmem_dynamic=m, Hx=Hx)
+    assert nbad == 0
+    assert np.allclose(S.mean(0), Hx, atol=1e-5)
+    assert np.allclose(S - S.mean(0), HE - HE.mean(0), atol=1e-5)
+    # hybrid: dynamic anomalies x k_d, static anomalies x k_s, all about the dynamic mean
+    g = 0.5
+    S, _, _ = oracle.finish_HE(HE, st, mode=2, nmem_dynamic=md, gamma=g)
+    md_mean = HE[:md].astype(np.float64).mean(0)
+    kd = np.sqrt((m - 1) / (md - 1))
+    ks = np.sqrt(g * (m - 1) / (m - md - 1))
+    assert np.allclose(S[:md], (HE[:md] - md_mean) * kd + md_mean, atol=1e-5)
+    assert np.allclose(S[md:], (HE[md:] - HE[md:].astype(np.float64).mean(0)) * ks + md_mean, atol=1e-5)
+    # bad forecasts: a NaN in any member (or in Hx for EnOI) marks STATUS_BADFC (10)
+    HE[3, 5] = np.nan
+    Hx[7] = np.nan
+    st[9] = 2
+    S, st2, nbad = oracle.finish_HE(HE, st, mode=1, nmem_dynamic=m, Hx=Hx, skip_bad=True)
+    assert nbad == 2 and st2[5] == 10 and st2[7] == 10 and st2[9] == 2
+    S, st2, nbad = oracle.finish_HE(HE, st, mode=0, nmem_dynamic=m, skip_bad=False)
+    assert nbad == 0 and st2[5] == 0
