@@ -44,13 +44,16 @@ def test_he_against_reference_golden(ctx):
     g = np.load(os.path.join(GOLD, "model2obs.npz"))
     nk = int(g["nk"])
     m, n = g["he2_p0"].shape
-    setup_obs(ctx, g["fi"], g["fj"], g["fk"])
+    # each case starts from fresh statuses: finish_HE(skip_bad) marks the
+    # all-dry observations STATUS_BADFC, and later calls select status 0 only
     for per in (0, 1):
+        setup_obs(ctx, g["fi"], g["fj"], g["fk"])
         ctx.begin_HE(m)
         ctx.map_obs(0, g["f2"], g["numlevels"], periodic_i=per, offset=g["off2"], offset_kind=2, skip_bad=True)
         ctx.finish_HE(skip_bad=True)
         assert same_bits(ctx.get_S()[0], g[f"he2_p{per}"]), f"2-D periodic={per}"
         for ktop in (0, nk - 1):
+            setup_obs(ctx, g["fi"], g["fj"], g["fk"])
             ctx.begin_HE(m)
             ctx.map_obs(0, g["f3"], g["numlevels"], three_d=True, ksurf=ktop, periodic_i=per, offset=g["off1"],
                         offset_kind=1, skip_bad=True)
