@@ -219,14 +219,17 @@ def test_he_device_pointer_form(ctx):
     fj = rng.uniform(0.0, nj - 1.0, n)
     fk = rng.uniform(0.0, nk - 1.0, n).astype(np.float32)
     setup_obs(ctx, fi, fj, fk)
+    # wet-level counts leave some positions with every corner dry: those
+    # forecasts are NaN (skip_bad), in both forms alike
     ctx.begin_HE(m)
-    ctx.map_obs(0, fields, nl, three_d=True, ksurf=0)
+    ctx.map_obs(0, fields, nl, three_d=True, ksurf=0, skip_bad=True)
+    ctx.finish_HE()
     host = ctx.get_S()[0]
     f_d = torch.from_numpy(fields).cuda()
     nl_d = torch.from_numpy(nl).cuda()
     ids_d = torch.arange(n, dtype=torch.int32, device="cuda")
     ctx.begin_HE(m)
     ctx.map_obs_dev(0, f_d.data_ptr(), m, ni, nj, nl_d.data_ptr(), nk=nk, ids_ptr=ids_d.data_ptr(), nids=n,
-                    three_d=True, ksurf=0)
+                    three_d=True, ksurf=0, skip_bad=True)
     ctx.finish_HE()
     assert same_bits(ctx.get_S()[0], host)
