@@ -7,17 +7,19 @@
 // weights of the observation are formed once and applied to each member's
 // field.  The arithmetic is the reference's, operation by operation in
 // double with round-to-nearest intrinsics (no contraction), so HE is
-// bit-identical to the reference's on the same positions and fields.
+// bit-identical to the reference's on the same positions and fields.  FP64
+// bounds the kernel on this part: conversions run on the integer pipe, and
+// the division by the kept weights' sum becomes a product by its reciprocal
+// wherever the float rounding of the quotient is decided with a margin.
 #include "internal.cuh"
 #include <math.h>
 
 namespace {
 
 constexpr int MAP_NT = 256;
-constexpr int MAP_MG = 4;                  // members per thread
+constexpr int MAP_MG = 16;                 // members per thread
 constexpr short STATUS_BADFC = 10;         // common/global.h:62
 constexpr double EPS_EDGE = 1.0e-7;        // common/utils.c:51
-constexpr double MAXOBSVAL = 999999.0;     // common/global.h:119
 
 struct MapArgs {
     const double* fi;
@@ -61,6 +63,37 @@ __device__ __forceinline__ bool corners(double fi, double fj, int ni, int nj, in
     if (j[0] == -1) j[0] = j[1];
     if (j[1] == nj) j[1] = j[0];
     return i[0] >= 0 && i[0] < ni && i[1] >= 0 && i[1] < ni && j[0] >= 0 && j[0] < nj && j[1] >= 0 && j[1] < nj;
+}
+
+// float -> double (exact) on the integer pipe for normal floats; FP64 is the
+// scarce unit on this part, and the conversion instruction runs on it
+__device__ __forceinline__ double widen(float v)
+{
+    const unsigned u = __float_as_uint(v);
+    const unsigned ex = (u >> 23) & 0xffu;
+    if (ex == 0u || ex == 0xffu) return (double)v;
+    return __longlong_as_double((long long)(((unsigned long long)(u & 0x80000000u) << 32) |
+                                            ((unsigned long long)(ex + 896u) << 52) |
+                                            ((unsigned long long)(u & 0x7fffffu) << 29)));
+}
+
+// Round-to-nearest float of a double q on the integer pipe, when that
+// rounding is decided with a margin: q a normal double of moderate exponent
+// whose low 29 mantissa bits are more than 8 double ulps away from the float
+// tie point.  Then any double within 2.5 ulps of q (in particular the
+// correctly rounded quotient the reference forms, when q approximates it to
+// within 2 ulps) has the same float rounding.  Returns false otherwise.
+__device__ __forceinline__ bool narrow_decided(double q, float& r)
+{
+    const unsigned long long b = (unsigned long long)__double_as_longlong(q);
+    const int ex = (int)((b >> 52) & 0x7ffu);
+    if (ex < 1023 - 100 || ex > 1023 + 100) return false;          // also NaN / inf / 0
+    const long long dt = (long long)(b & ((1ull << 29) - 1)) - (1ll << 28);
+    if (dt >= -8 && dt <= 8) return false;
+    unsigned f = ((unsigned)(b >> 63) << 31) | ((unsigned)(ex - 896) << 23) | (unsigned)((b >> 29) & 0x7fffffu);
+    f += dt > 0 ? 1u : 0u;                                         // a carry moves into the exponent
+    r = __uint_as_float(f);
+    return true;
 }
 
 __device__ __forceinline__ float offset_at(const MapArgs& a, long long q, long long nij)
@@ -145,19 +178,29 @@ __global__ void __launch_bounds__(MAP_NT) k_map_obs(MapArgs a)
             cell[c] = q;
         }
     }
+    // the kept weights' sum is the same for every member; its reciprocal
+    // turns the per-member division into a product, checked for a decided
+    // float rounding (the exact division where it is not)
+    double w = 0.0;
+#pragma unroll
+    for (int c = 0; c < NC; ++c)
+        if (wet[c]) w = __dadd_rn(w, ww[c]);
+    const bool wpos = w > 0.0;
+    const double rw = wpos ? __drcp_rn(w) : 0.0;
+#pragma unroll 2
     for (int e = e0; e < e1; ++e) {
         const float* f = a.fields + e * a.fstride;
-        double sum = 0.0, w = 0.0;
+        double sum = 0.0;
 #pragma unroll
         for (int c = 0; c < NC; ++c) {
             if (!wet[c]) continue;
             float v = __ldg(f + cell[c]);
             if (a.offset_kind) v = __fsub_rn(v, offset_at(a, cell[c], nij));
-            sum = __dadd_rn(sum, __dmul_rn((double)v, ww[c]));
-            w = __dadd_rn(w, ww[c]);
+            sum = __dadd_rn(sum, __dmul_rn(widen(v), ww[c]));
         }
-        float r = __double2float_rn(__ddiv_rn(sum, w));
-        if (!isfinite(r) || fabs((double)r) > MAXOBSVAL) {
+        float r;
+        if (!(wpos && narrow_decided(__dmul_rn(sum, rw), r))) r = __double2float_rn(__ddiv_rn(sum, w));
+        if (!(fabsf(r) <= 999999.0f)) {                           // not finite, or |r| > MAXOBSVAL
             if (!a.skip_bad)
                 atomicMin(&a.flag[0], ((unsigned long long)o << 32) | __float_as_uint(r));
             r = __int_as_float(0x7fc00000);
