@@ -17,7 +17,7 @@ CSRC = os.path.join(PKG, "csrc")
 OUTDIR = os.path.join(PKG, "_lib")
 LIB = os.path.join(OUTDIR, "libenkfg.so")
 SOURCES = ["capi.cu", "prep.cu", "index.cu", "calc.cu", "calc_mixed.cu", "update.cu", "adjoint.cu", "noalloc.cu",
-           "model2obs.cu"]
+           "model2obs.cu", "ncio.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-fvisibility=hidden",
          "--expt-relaxed-constexpr", "-I" + os.path.join(ROOT, "include")]
@@ -44,7 +44,7 @@ def build(force: bool = False, verbose: bool = False, extra=None) -> str:
     objs, jobs = [], []
     for src in SOURCES:
         s = os.path.join(CSRC, src)
-        o = os.path.join(OUTDIR, src.replace(".cu", ".o"))
+        o = os.path.join(OUTDIR, os.path.splitext(src)[0] + ".o")
         objs.append(o)
         if force or _stale(o, [s] + headers):
             cmd = [nvcc()] + ARCH + FLAGS + (extra or []) + ["-c", s, "-o", o]

@@ -46,7 +46,9 @@ EXPORTS = ["enkfg_create", "enkfg_destroy", "enkfg_last_error", "enkfg_status_st
            "enkfg_set_hybrid_ensemble_dev", "enkfg_kernel_launches", "enkfg_stage_times", "enkfg_kernel_times", "enkfg_set_stream",
            "enkfg_set_HE_dev", "enkfg_rebuild_index", "enkfg_local_offsets_noalloc", "enkfg_autotune_table",
            "enkfg_autotune_reset", "enkfg_adjoint_transforms", "enkfg_adjoint_mean", "enkfg_set_obs_positions",
-           "enkfg_begin_HE", "enkfg_map_obs", "enkfg_map_obs_dev", "enkfg_finish_HE"]
+           "enkfg_begin_HE", "enkfg_map_obs", "enkfg_map_obs_dev", "enkfg_finish_HE", "enkfg_nc_last_error",
+           "enkfg_nc_write_transforms", "enkfg_nc_write_diag", "enkfg_nc_inq_var", "enkfg_nc_get_vara_float",
+           "enkfg_nc_read_layer", "enkfg_nc_write_layer"]
 
 
 class EnkfgError(RuntimeError):
@@ -445,3 +447,80 @@ class Enkfg:
         self._ck(self.L.enkfg_set_hybrid_ensemble(self.h, C.c_int(m), C.c_int(nmem_dynamic), C.c_double(gamma),
                                                   C.c_int(nij), _p(v, C.c_float)))
         return v
+
+
+# ---------------------------------------------------------------------------
+# NetCDF classic files (host only; no context, no GPU)
+# ---------------------------------------------------------------------------
+
+NC_MAXDIMS = 8
+
+
+def _nc_ck(st):
+    if st != 0:
+        L = load()
+        L.enkfg_nc_last_error.restype = C.c_char_p
+        raise EnkfgError(st, L.enkfg_nc_last_error().decode())
+
+
+def nc_write_transforms(path, T, w, stride=1, grid_name=""):
+    """transforms.nc (calc/transforms.c:54-131); T [nj][ni][m_dyn][m] or None
+    (EnOI), w [nj][ni][m]."""
+    w = np.ascontiguousarray(w, np.float32)
+    nj, ni, m = w.shape
+    Tc = None if T is None else np.ascontiguousarray(T, np.float32)
+    md = 0 if Tc is None else Tc.shape[2]
+    _nc_ck(load().enkfg_nc_write_transforms(os.fsencode(path), C.c_int(nj), C.c_int(ni), C.c_int(md), C.c_int(m),
+                                            _p(Tc, C.c_float), _p(w, C.c_float), C.c_int(int(stride)),
+                                            grid_name.encode()))
+
+
+def nc_write_diag(path, type_names, nlobs, dfs, srf, pnlobs, pdfs, psrf, stride=1):
+    """enkf_diag.nc (calc/transforms.c:380-470)."""
+    nlobs = np.ascontiguousarray(nlobs, np.int32)
+    nj, ni = nlobs.shape
+    nt = len(type_names)
+    names = (C.c_char_p * nt)(*[n.encode() for n in type_names])
+    arrs = [np.ascontiguousarray(a, t) for a, t in ((dfs, np.float32), (srf, np.float32), (pnlobs, np.int32),
+                                                    (pdfs, np.float32), (psrf, np.float32))]
+    _nc_ck(load().enkfg_nc_write_diag(os.fsencode(path), C.c_int(nj), C.c_int(ni), C.c_int(nt), names,
+                                      C.c_int(int(stride)), _p(nlobs, C.c_int), _p(arrs[0], C.c_float),
+                                      _p(arrs[1], C.c_float), _p(arrs[2], C.c_int), _p(arrs[3], C.c_float),
+                                      _p(arrs[4], C.c_float)))
+
+
+def nc_inq_var(path, var):
+    """(dims tuple, NetCDF type code, has record dimension)."""
+    nd = C.c_int(0)
+    dims = (C.c_longlong * NC_MAXDIMS)()
+    t = C.c_int(0)
+    rec = C.c_int(0)
+    _nc_ck(load().enkfg_nc_inq_var(os.fsencode(path), var.encode(), C.byref(nd), dims, C.byref(t), C.byref(rec)))
+    return tuple(dims[k] for k in range(nd.value)), t.value, bool(rec.value)
+
+
+def nc_get_vara_float(path, var, start=None, count=None):
+    dims, _, _ = nc_inq_var(path, var)
+    start = [0] * len(dims) if start is None else list(start)
+    count = [d - s for d, s in zip(dims, start)] if count is None else list(count)
+    out = np.empty([int(c) for c in count], np.float32)
+    st = (C.c_longlong * max(1, len(dims)))(*start)
+    ct = (C.c_longlong * max(1, len(dims)))(*count)
+    _nc_ck(load().enkfg_nc_get_vara_float(os.fsencode(path), var.encode(), st, ct, _p(out, C.c_float)))
+    return out
+
+
+def nc_read_layer(path, var, ni, nj, nk=1, k=0, r=-1):
+    """ncu_readfield (common/ncutils.c:102-530): layer k of record r."""
+    v = np.empty((nj, ni), np.float32)
+    _nc_ck(load().enkfg_nc_read_layer(os.fsencode(path), var.encode(), C.c_int(r), C.c_int(k), C.c_int(ni),
+                                      C.c_int(nj), C.c_int(nk), _p(v, C.c_float)))
+    return v
+
+
+def nc_write_layer(path, var, v, nk=1, k=0):
+    """ncu_writefield (common/ncutils.c:537-700), into an existing file."""
+    v = np.ascontiguousarray(v, np.float32)
+    nj, ni = v.shape
+    _nc_ck(load().enkfg_nc_write_layer(os.fsencode(path), var.encode(), C.c_int(int(k)), C.c_int(ni), C.c_int(nj),
+                                       C.c_int(int(nk)), _p(v, C.c_float)))

@@ -313,6 +313,53 @@ ENKFG_API enkfg_status enkfg_kernel_times(const enkfg_ctx* ctx, float* ms2);
  * (NULL: the legacy default stream). */
 ENKFG_API enkfg_status enkfg_local_offsets_noalloc(const int* counts_dev, long long n, long long* offsets_dev, void* stream);
 
+/* ---- NetCDF classic files around the path (the reference reads and writes
+ * them through NetCDF-C: common/ncw.c, common/ncutils.c) ----
+ * Host only: these calls need no context and no GPU.  Formats: CDF-1,
+ * CDF-2 (64-bit offset) and CDF-5 (64-bit data) are read; files are written
+ * as CDF-2, or CDF-5 when a variable exceeds 4 GiB.  NetCDF-4 (HDF5) files
+ * are not handled.  Errors: enkfg_nc_last_error() (per thread). */
+#define ENKFG_NC_MAXDIMS 8
+ENKFG_API const char* enkfg_nc_last_error(void);
+
+/* transforms.nc as nc_createtransforms / nc_writetransforms write it
+ * (calc/transforms.c:54-131): dimensions j, i, m_dyn, m; float T
+ * [j][i][m_dyn][m] and w [j][i][m]; global attributes stride (int) and
+ * grid_name (text).  T NULL (EnOI): no m_dyn and no T. */
+ENKFG_API enkfg_status enkfg_nc_write_transforms(const char* path, int nj, int ni, int nmem_dynamic, int nmem, const float* T, const float* w, int stride, const char* grid_name);
+
+/* enkf_diag.nc (calc/transforms.c:380-470): dimensions nobstypes, j, i; int
+ * nlobs [j][i], float dfs and srf [j][i], int pnlobs and float pdfs, psrf
+ * [nobstypes][j][i] with the reference's long_name / comment attributes;
+ * global attributes stride and, per observation type, <name> = its index. */
+ENKFG_API enkfg_status enkfg_nc_write_diag(const char* path, int nj, int ni, int ntypes, const char* const* type_names, int stride, const int* nlobs, const float* dfs, const float* srf, const int* pnlobs, const float* pdfs, const float* psrf);
+
+/* Shape of a variable: ndims, dims [ENKFG_NC_MAXDIMS] (the record dimension
+ * at its current length), its NetCDF type code, and whether the first
+ * dimension is the record dimension.  Any output may be NULL. */
+ENKFG_API enkfg_status enkfg_nc_inq_var(const char* path, const char* var, int* ndims, long long* dims, int* type, int* has_record);
+
+/* A hyperslab [start, start + count) of a numeric variable as float (the
+ * native type converted as nc_get_vara_float does; doubles beyond the float
+ * range read as NaN, ncw_get_vara_float_fixerange, common/ncw.c:1078), no
+ * attributes applied. */
+ENKFG_API enkfg_status enkfg_nc_get_vara_float(const char* path, const char* var, const long long* start, const long long* count, float* out);
+
+/* ncu_readfield (common/ncutils.c:102-530) on a structured grid: layer k of
+ * record r (r < 0: the only record) of `var` laid out [r][k][j][i],
+ * [k][j][i], [r][j][i] or [j][i], into v [nj][ni]; fill values (_FillValue
+ * or the type's default), missing_value and values outside valid_min /
+ * valid_max / valid_range become NaN, then scale_factor and add_offset are
+ * applied in float. */
+ENKFG_API enkfg_status enkfg_nc_read_layer(const char* path, const char* var, int r, int k, int ni, int nj, int nk, float* v);
+
+/* ncu_writefield (common/ncutils.c:537-700) on a structured grid, into an
+ * existing file: layer k (or the last record) of a float or double
+ * variable; add_offset and scale_factor undone, values clamped to the valid
+ * range, NaN written as the fill value (or missing_value).  Packed integer
+ * variables are ENKFG_EUNSUPPORTED. */
+ENKFG_API enkfg_status enkfg_nc_write_layer(const char* path, const char* var, int k, int ni, int nj, int nk, const float* v);
+
 #ifdef __cplusplus
 }
 #endif

@@ -1,0 +1,218 @@
+"""NetCDF classic I/O of libenkfg (host only, no GPU), checked against scipy's
+independent reader and writer of the classic format (versions 1 and 2).
+
+Files: transforms.nc (calc/transforms.c:54-131), enkf_diag.nc
+(calc/transforms.c:380-470), member fields read as ncu_readfield does
+(common/ncutils.c:102-530) and analysis layers written as ncu_writefield does
+(common/ncutils.c:537-700).  The expected values of the attribute rules
+(fill, missing, valid range, scale and offset) are restated here in numpy.
+"""
+import numpy as np
+import pytest
+
+scipy_io = pytest.importorskip("scipy.io")
+netcdf_file = scipy_io.netcdf_file
+
+FILL_F = np.float32(9.9692099683868690e+36)
+
+
+@pytest.fixture(scope="module")
+def nc():
+    import build
+    build.build()
+    import enkfg
+    return enkfg
+
+
+def read_rules(raw, fill=None, missing=None, vmin=None, vmax=None, vrange=None, sf=None, ao=None,
+               default_fill=None):
+    """ncu_readfield's value rules on native values `raw`."""
+    raw = np.asarray(raw)
+    if raw.dtype == np.float64:
+        with np.errstate(over="ignore"):
+            v = raw.astype(np.float32)
+        bad = ~np.isfinite(raw) | (np.abs(raw) > np.finfo(np.float32).max)
+        v[bad] = np.nan
+    else:
+        v = raw.astype(np.float32)
+    f = fill if fill is not None else default_fill
+    mask = np.zeros(raw.shape, bool)
+    if f is not None:
+        mask |= raw == np.asarray(f, raw.dtype)
+    if missing is not None:
+        mask |= raw == np.asarray(missing, raw.dtype)
+    if vmin is not None:
+        mask |= raw < vmin
+    if vmax is not None:
+        mask |= raw > vmax
+    if vrange is not None:
+        mask |= (raw < vrange[0]) | (raw > vrange[1])
+    v[mask] = np.nan
+    if sf is not None:
+        v = (v * np.float32(sf)).astype(np.float32)
+    if ao is not None:
+        v = (v + np.float32(ao)).astype(np.float32)
+    return v
+
+
+def same(a, b):
+    a = np.asarray(a, np.float32)
+    b = np.asarray(b, np.float32)
+    return np.array_equal(np.isnan(a), np.isnan(b)) and np.array_equal(a[~np.isnan(a)], b[~np.isnan(b)])
+
+
+def test_transforms_file_read_by_scipy(nc, tmp_path):
+    rng = np.random.default_rng(1)
+    nj, ni, md, m = 7, 9, 5, 6
+    T = rng.standard_normal((nj, ni, md, m)).astype(np.float32)
+    w = rng.standard_normal((nj, ni, m)).astype(np.float32)
+    p = tmp_path / "transforms.nc"
+    nc.nc_write_transforms(p, T, w, stride=3, grid_name="t-grid")
+    with netcdf_file(p, "r", mmap=False) as f:
+        assert f.version_byte == 2
+        assert f.dimensions == {"j": nj, "i": ni, "m_dyn": md, "m": m}
+        assert f.variables["T"].dimensions == ("j", "i", "m_dyn", "m")
+        assert f.variables["w"].dimensions == ("j", "i", "m")
+        assert np.array_equal(f.variables["T"][:], T) and np.array_equal(f.variables["w"][:], w)
+        assert int(f.stride) == 3 and f.grid_name == b"t-grid"
+    # and through this library's own reader
+    assert np.array_equal(nc.nc_get_vara_float(p, "T"), T)
+    assert np.array_equal(nc.nc_get_vara_float(p, "w", [2, 3, 0], [4, 5, m]), w[2:6, 3:8])
+    assert nc.nc_inq_var(p, "T") == ((nj, ni, md, m), 5, False)
+    # EnOI: no T, no m_dyn
+    p2 = tmp_path / "transforms-enoi.nc"
+    nc.nc_write_transforms(p2, None, w, stride=1, grid_name="g")
+    with netcdf_file(p2, "r", mmap=False) as f:
+        assert f.dimensions == {"j": nj, "i": ni, "m": m} and "T" not in f.variables
+        assert np.array_equal(f.variables["w"][:], w)
+
+
+def test_diag_file_read_by_scipy(nc, tmp_path):
+    rng = np.random.default_rng(2)
+    nj, ni, nt = 5, 4, 3
+    nlobs = rng.integers(0, 100, (nj, ni)).astype(np.int32)
+    dfs = rng.random((nj, ni)).astype(np.float32)
+    srf = rng.random((nj, ni)).astype(np.float32)
+    pn = rng.integers(0, 50, (nt, nj, ni)).astype(np.int32)
+    pd = rng.random((nt, nj, ni)).astype(np.float32)
+    ps = rng.random((nt, nj, ni)).astype(np.float32)
+    p = tmp_path / "enkf_diag.nc"
+    nc.nc_write_diag(p, ["SST", "SLA", "TEM"], nlobs, dfs, srf, pn, pd, ps, stride=2)
+    with netcdf_file(p, "r", mmap=False) as f:
+        assert f.dimensions == {"nobstypes": nt, "j": nj, "i": ni}
+        for name, a in (("nlobs", nlobs), ("dfs", dfs), ("srf", srf), ("pnlobs", pn), ("pdfs", pd), ("psrf", ps)):
+            assert np.array_equal(f.variables[name][:], a), name
+        assert f.variables["dfs"].long_name == b"local DFS (Degrees of Freedom for Signal)"
+        assert int(f.stride) == 2 and int(f.SST) == 0 and int(f.SLA) == 1 and int(f.TEM) == 2
+
+
+@pytest.mark.parametrize("version", [1, 2])
+def test_read_layer_rules(nc, tmp_path, version):
+    rng = np.random.default_rng(10 + version)
+    nk, nj, ni = 4, 6, 8
+    p = tmp_path / f"member_v{version}.nc"
+    f3 = rng.normal(15, 2, (nk, nj, ni)).astype(np.float32)
+    f3[0, 1, 2] = -999.0                                   # its _FillValue
+    f3[1, 2, 3] = FILL_F                                   # the default fill: not the fill here
+    d2 = rng.normal(0, 1, (nj, ni)).astype(np.float32)
+    d2[3, 3] = FILL_F                                      # the default fill (no attribute)
+    packed = rng.integers(-3000, 3000, (nk, nj, ni)).astype(np.int16)
+    packed[2, 0, 0] = -32767                               # default short fill
+    packed[2, 0, 1] = 7777                                 # missing_value
+    packed[2, 0, 2] = 2999                                 # outside valid_range
+    dbl = rng.normal(0, 1, (nj, ni))
+    dbl[1, 1] = 1e300                                      # beyond the float range
+    rec = rng.normal(0, 1, (2, nk, nj, ni)).astype(np.float32)
+    with netcdf_file(p, "w", version=version) as f:
+        f.createDimension("time", None)
+        f.createDimension("k", nk)
+        f.createDimension("j", nj)
+        f.createDimension("i", ni)
+        v = f.createVariable("temp", "f4", ("k", "j", "i"))
+        v[:] = f3
+        v._FillValue = np.float32(-999.0)
+        v = f.createVariable("eta", "f4", ("j", "i"))
+        v[:] = d2
+        v = f.createVariable("salt", "i2", ("k", "j", "i"))
+        v[:] = packed
+        v.scale_factor = np.float32(0.01)
+        v.add_offset = np.float32(35.0)
+        v.missing_value = np.int16(7777)
+        v.valid_range = np.array([-2999, 2998], np.int16)
+        v = f.createVariable("dbl", "f8", ("j", "i"))
+        v[:] = dbl
+        v = f.createVariable("u", "f4", ("time", "k", "j", "i"))
+        v[:] = rec
+    for k in range(nk):
+        got = nc.nc_read_layer(p, "temp", ni, nj, nk, k=k)
+        assert same(got, read_rules(f3[k], fill=np.float32(-999.0))), k
+        got = nc.nc_read_layer(p, "salt", ni, nj, nk, k=k)
+        exp = read_rules(packed[k], missing=7777, vrange=(-2999, 2998), sf=0.01, ao=35.0, default_fill=-32767)
+        assert same(got, exp), k
+    assert same(nc.nc_read_layer(p, "eta", ni, nj, nk), read_rules(d2, default_fill=FILL_F))
+    assert np.isnan(nc.nc_read_layer(p, "eta", ni, nj, nk)[3, 3])
+    got = nc.nc_read_layer(p, "dbl", ni, nj, nk)
+    assert np.isnan(got[1, 1]) and same(got, read_rules(dbl, default_fill=9.9692099683868690e+36))
+    assert same(nc.nc_read_layer(p, "u", ni, nj, nk, k=2, r=1), rec[1, 2])
+    with pytest.raises(Exception):                         # two records and no record given
+        nc.nc_read_layer(p, "u", ni, nj, nk, k=0, r=-1)
+    with pytest.raises(Exception):                         # grid mismatch
+        nc.nc_read_layer(p, "temp", ni + 1, nj, nk)
+    # hyperslabs of a record variable against numpy slicing
+    for _ in range(20):
+        st = [int(rng.integers(0, d)) for d in rec.shape]
+        ct = [int(rng.integers(1, d - s + 1)) for d, s in zip(rec.shape, st)]
+        sl = tuple(slice(s, s + c) for s, c in zip(st, ct))
+        assert np.array_equal(nc.nc_get_vara_float(p, "u", st, ct), rec[sl])
+
+
+def test_write_layer_rules(nc, tmp_path):
+    rng = np.random.default_rng(3)
+    nk, nj, ni = 3, 5, 7
+    p = tmp_path / "analysis.nc"
+    with netcdf_file(p, "w", version=2) as f:
+        f.createDimension("time", None)
+        f.createDimension("k", nk)
+        f.createDimension("j", nj)
+        f.createDimension("i", ni)
+        v = f.createVariable("temp", "f4", ("k", "j", "i"))
+        v[:] = np.zeros((nk, nj, ni), np.float32)
+        v._FillValue = np.float32(-1.0e10)
+        v.add_offset = np.float32(10.0)
+        v.scale_factor = np.float32(0.5)
+        v.valid_max = np.float32(30.0)
+        v = f.createVariable("ssh", "f8", ("time", "j", "i"))
+        v[:] = np.zeros((2, nj, ni))
+    a = rng.normal(12, 5, (nj, ni)).astype(np.float32)
+    a[0, 0] = np.nan
+    nc.nc_write_layer(p, "temp", a, nk=nk, k=1)
+    b = rng.normal(0, 1, (nj, ni)).astype(np.float32)
+    nc.nc_write_layer(p, "ssh", b, nk=nk, k=0)
+    exp = ((a - np.float32(10.0)) / np.float32(0.5)).astype(np.float32)
+    exp = np.where(exp > np.float32(30.0), np.float32(30.0), exp)
+    exp[0, 0] = np.float32(-1.0e10)
+    with netcdf_file(p, "r", mmap=False) as f:
+        got = f.variables["temp"][:].copy()
+        assert np.array_equal(got[1], exp)
+        assert np.array_equal(got[0], np.zeros((nj, ni), np.float32))
+        ssh = f.variables["ssh"][:].copy()
+        assert np.array_equal(ssh[1], b.astype(np.float64)) and np.array_equal(ssh[0], np.zeros((nj, ni)))
+
+
+def test_errors(nc, tmp_path):
+    p = tmp_path / "not.nc"
+    p.write_bytes(b"HDF\x89 not classic")
+    with pytest.raises(Exception) as ei:
+        nc.nc_inq_var(p, "x")
+    assert "not a NetCDF classic file" in str(ei.value)
+    with pytest.raises(Exception):
+        nc.nc_inq_var(tmp_path / "missing.nc", "x")
+    q = tmp_path / "packed.nc"
+    with netcdf_file(q, "w", version=1) as f:
+        f.createDimension("j", 2)
+        f.createDimension("i", 3)
+        v = f.createVariable("s", "i2", ("j", "i"))
+        v[:] = np.zeros((2, 3), np.int16)
+    with pytest.raises(Exception) as ei:
+        nc.nc_write_layer(q, "s", np.zeros((2, 3), np.float32))
+    assert getattr(ei.value, "status", None) == 8
