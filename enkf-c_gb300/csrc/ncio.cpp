@@ -16,6 +16,8 @@
 #include <stdlib.h>
 #include <string.h>
 
+#include <new>
+#include <stdexcept>
 #include <string>
 #include <vector>
 
@@ -639,6 +641,19 @@ Var fixed_var(const char* nm, int type, std::initializer_list<int> dimids)
     return v;
 }
 
+// the entry points: no C++ exception crosses the C ABI
+template <typename F>
+enkfg_status guarded(F f)
+{
+    try {
+        return f();
+    } catch (const std::bad_alloc&) {
+        return fail(ENKFG_ENOMEM, "out of host memory");
+    } catch (const std::exception& e) {
+        return fail(ENKFG_EINVAL, "%s", e.what());
+    }
+}
+
 }  // namespace
 
 extern "C" {
@@ -648,7 +663,7 @@ ENKFG_API const char* enkfg_nc_last_error(void)
     return g_err;
 }
 
-ENKFG_API enkfg_status enkfg_nc_write_transforms(const char* path, int nj, int ni, int nmem_dynamic, int nmem,
+static enkfg_status impl_write_transforms(const char* path, int nj, int ni, int nmem_dynamic, int nmem,
                                                  const float* T, const float* w, int stride, const char* grid_name)
 {
     if (nj < 1 || ni < 1 || nmem < 1 || !w || (T && (nmem_dynamic < 1 || nmem_dynamic > nmem)))
@@ -673,7 +688,7 @@ ENKFG_API enkfg_status enkfg_nc_write_transforms(const char* path, int nj, int n
     return write_fixed(path, nc, data);
 }
 
-ENKFG_API enkfg_status enkfg_nc_write_diag(const char* path, int nj, int ni, int ntypes, const char* const* type_names,
+static enkfg_status impl_write_diag(const char* path, int nj, int ni, int ntypes, const char* const* type_names,
                                            int stride, const int* nlobs, const float* dfs, const float* srf,
                                            const int* pnlobs, const float* pdfs, const float* psrf)
 {
@@ -712,7 +727,7 @@ ENKFG_API enkfg_status enkfg_nc_write_diag(const char* path, int nj, int ni, int
     return write_fixed(path, nc, { { nlobs }, { dfs }, { srf }, { pnlobs }, { pdfs }, { psrf } });
 }
 
-ENKFG_API enkfg_status enkfg_nc_inq_var(const char* path, const char* var, int* ndims, long long* dims, int* type,
+static enkfg_status impl_inq_var(const char* path, const char* var, int* ndims, long long* dims, int* type,
                                         int* has_record)
 {
     File F;
@@ -731,7 +746,7 @@ ENKFG_API enkfg_status enkfg_nc_inq_var(const char* path, const char* var, int* 
     return ENKFG_OK;
 }
 
-ENKFG_API enkfg_status enkfg_nc_get_vara_float(const char* path, const char* var, const long long* start,
+static enkfg_status impl_get_vara_float(const char* path, const char* var, const long long* start,
                                                const long long* count, float* out)
 {
     File F;
@@ -750,7 +765,7 @@ ENKFG_API enkfg_status enkfg_nc_get_vara_float(const char* path, const char* var
     return ENKFG_OK;
 }
 
-ENKFG_API enkfg_status enkfg_nc_read_layer(const char* path, const char* var, int r, int k, int ni, int nj, int nk,
+static enkfg_status impl_read_layer(const char* path, const char* var, int r, int k, int ni, int nj, int nk,
                                            float* v)
 {
     if (ni < 1 || nj < 1 || nk < 1 || !v) return fail(ENKFG_EINVAL, "bad layer arguments");
@@ -810,7 +825,7 @@ ENKFG_API enkfg_status enkfg_nc_read_layer(const char* path, const char* var, in
     return ENKFG_OK;
 }
 
-ENKFG_API enkfg_status enkfg_nc_write_layer(const char* path, const char* var, int k, int ni, int nj, int nk,
+static enkfg_status impl_write_layer(const char* path, const char* var, int k, int ni, int nj, int nk,
                                             const float* v)
 {
     if (ni < 1 || nj < 1 || nk < 1 || !v) return fail(ENKFG_EINVAL, "bad layer arguments");
@@ -915,4 +930,35 @@ ENKFG_API enkfg_status enkfg_nc_write_layer(const char* path, const char* var, i
     });
 }
 
+
+
+ENKFG_API enkfg_status enkfg_nc_write_transforms(const char* path, int nj, int ni, int nmem_dynamic, int nmem, const float* T, const float* w, int stride, const char* grid_name)
+{
+    return guarded([&] { return impl_write_transforms(path, nj, ni, nmem_dynamic, nmem, T, w, stride, grid_name); });
+}
+
+ENKFG_API enkfg_status enkfg_nc_write_diag(const char* path, int nj, int ni, int ntypes, const char* const* type_names, int stride, const int* nlobs, const float* dfs, const float* srf, const int* pnlobs, const float* pdfs, const float* psrf)
+{
+    return guarded([&] { return impl_write_diag(path, nj, ni, ntypes, type_names, stride, nlobs, dfs, srf, pnlobs, pdfs, psrf); });
+}
+
+ENKFG_API enkfg_status enkfg_nc_inq_var(const char* path, const char* var, int* ndims, long long* dims, int* type, int* has_record)
+{
+    return guarded([&] { return impl_inq_var(path, var, ndims, dims, type, has_record); });
+}
+
+ENKFG_API enkfg_status enkfg_nc_get_vara_float(const char* path, const char* var, const long long* start, const long long* count, float* out)
+{
+    return guarded([&] { return impl_get_vara_float(path, var, start, count, out); });
+}
+
+ENKFG_API enkfg_status enkfg_nc_read_layer(const char* path, const char* var, int r, int k, int ni, int nj, int nk, float* v)
+{
+    return guarded([&] { return impl_read_layer(path, var, r, k, ni, nj, nk, v); });
+}
+
+ENKFG_API enkfg_status enkfg_nc_write_layer(const char* path, const char* var, int k, int ni, int nj, int nk, const float* v)
+{
+    return guarded([&] { return impl_write_layer(path, var, k, ni, nj, nk, v); });
+}
 }  // extern "C"
