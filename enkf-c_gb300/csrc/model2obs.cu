@@ -29,6 +29,7 @@ struct MapArgs {
     const short* status;
     const int* ids;             // nullptr: every obs of type otype with status 0
     int nids;
+    int nobs;
     int otype;
     int ni, nj, nk, ktop, periodic_i;
     const int* numlevels;       // [nj][ni]
@@ -40,7 +41,7 @@ struct MapArgs {
     float* dst;                 // row of the first member; rows nobs apart
     long long dstride;
     int skip_bad;
-    unsigned long long* flag;   // [0] bad forecast key, [1] position off the grid
+    unsigned long long* flag;   // [0] bad forecast key, [1] position off the grid, [3] id out of range
 };
 
 // corner indices and weights, the reference's edge rules (utils.c:1158-1184)
@@ -114,6 +115,10 @@ __global__ void __launch_bounds__(MAP_NT) k_map_obs(MapArgs a)
     int o = k;
     if (a.ids) {
         o = a.ids[k];
+        if ((unsigned)o >= (unsigned)a.nobs) {        // a caller's device list is checked here
+            atomicMin(&a.flag[3], (unsigned long long)k);
+            return;
+        }
     } else if (a.type[o] != a.otype || a.status[o] != 0) {
         return;
     }
@@ -294,6 +299,7 @@ static enkfg_status launch_map(enkfg_ctx* ctx, const enkfg_hop_params* p, int ob
     a.status = ctx->d_status;
     a.ids = d_ids;
     a.nids = d_ids ? nids : ctx->nobs;
+    a.nobs = ctx->nobs;
     a.otype = obstype;
     a.ni = p->ni;
     a.nj = p->nj;
@@ -323,9 +329,10 @@ static enkfg_status launch_map(enkfg_ctx* ctx, const enkfg_hop_params* p, int ob
 // reads the error flags (synchronises `st`)
 static enkfg_status check_flags(enkfg_ctx* ctx, cudaStream_t st, int skip_bad)
 {
-    unsigned long long f[2];
+    unsigned long long f[4];
     CK(cudaMemcpyAsync(f, ctx->d_hflag, sizeof(f), cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));
+    NEED(f[3] == ~0ull, ENKFG_EINVAL, "ids[%llu]: observation id out of range", f[3]);
     NEED(f[1] == ~0ull, ENKFG_EINVAL, "obs # %llu: position off the model grid", f[1]);
     if (!skip_bad && f[0] != ~0ull) {
         const unsigned bits = (unsigned)(f[0] & 0xffffffffu);
@@ -385,8 +392,8 @@ ENKFG_API enkfg_status enkfg_begin_HE(enkfg_ctx* ctx, int nmem, int nmem_dynamic
     if (!ctx->d_hflag) CK(cudaMalloc(&ctx->d_hflag, 4 * sizeof(unsigned long long)));
     // NaN everywhere (all bits set is a NaN), as the reference's set-up
     CK(cudaMemsetAsync(ctx->d_S, 0xff, (size_t)nmem * n * sizeof(float), ctx->stream));
-    CK(cudaMemsetAsync(ctx->d_hflag, 0xff, 2 * sizeof(unsigned long long), ctx->stream));
-    CK(cudaMemsetAsync(ctx->d_hflag + 2, 0, 2 * sizeof(unsigned long long), ctx->stream));
+    CK(cudaMemsetAsync(ctx->d_hflag, 0xff, 4 * sizeof(unsigned long long), ctx->stream));
+    CK(cudaMemsetAsync(ctx->d_hflag + 2, 0, sizeof(unsigned long long), ctx->stream));
     ctx->he_nmem = nmem;
     ctx->he_nmem_dyn = nmem_dynamic;
     ctx->he_bg = with_background != 0;

@@ -118,7 +118,8 @@ typedef struct {
  * grid is ENKFG_EINVAL. */
 ENKFG_API enkfg_status enkfg_map_obs(enkfg_ctx* ctx, const enkfg_hop_params* p, int obstype, int nids, const int* ids, int mem0, int nfield, const float* fields, const int* numlevels, const float* offset);
 /* Device-resident form: ids/fields/numlevels/offset are device addresses;
- * nothing is synchronised, and errors surface in enkfg_finish_HE. */
+ * nothing is synchronised, and errors (an id outside 0..nobs-1 included)
+ * surface in enkfg_finish_HE. */
 ENKFG_API enkfg_status enkfg_map_obs_dev(enkfg_ctx* ctx, const enkfg_hop_params* p, int obstype, int nids, const int* ids_dev, int mem0, int nfield, const float* fields_dev, const int* numlevels_dev, const float* offset_dev, void* stream);
 
 /* End of das_getHE (ensobs.c:372-490): with skip_bad, observations with a NaN
