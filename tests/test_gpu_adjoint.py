@@ -57,13 +57,14 @@ CHECKS = {}
 
 
 def record(name, summary):
-    """Keep the measured errors (gpurun_out/adjoint_checks.json when the
-    directory exists)."""
+    """Keep the measured errors (adjoint_checks.json in the directory named
+    by ENKFG_RESULTS_DIR, when that is set)."""
     import json
     import os
     CHECKS[name] = summary
-    if os.path.isdir("gpurun_out"):
-        with open(os.path.join("gpurun_out", "adjoint_checks.json"), "w") as f:
+    out = os.environ.get("ENKFG_RESULTS_DIR")
+    if out and os.path.isdir(out):
+        with open(os.path.join(out, "adjoint_checks.json"), "w") as f:
             json.dump(CHECKS, f, indent=1)
 
 

@@ -8,7 +8,8 @@ mean and spread relative to the field's scale).  The floor matters only at
 points whose every local observation sits at the edge of the radius: there
 the taper, and with it w, is ~1e-20 in FP64, while the FP32 taper of the
 mixed path rounds it to 0.  The measured errors are written to
-gpurun_out/mixed_errors.json when the directory exists.
+mixed_errors.json in the directory named by ENKFG_RESULTS_DIR, when that is
+set.
 """
 import json
 import os
@@ -63,8 +64,9 @@ def run_case(ctx, name, w, mode, scheme, S, s, tabs, path=1, update=True):
         e["spread_max"] = float(np.abs(gs - rs).max() / max(np.abs(rs).max(), 1e-30))
         e["spread_rms"] = float(np.sqrt(np.mean((gs - rs) ** 2)) / max(np.abs(rs).max(), 1e-30))
     ERRS[name] = e
-    if os.path.isdir("gpurun_out"):
-        with open(os.path.join("gpurun_out", "mixed_errors.json"), "w") as f:
+    out = os.environ.get("ENKFG_RESULTS_DIR")
+    if out and os.path.isdir(out):
+        with open(os.path.join(out, "mixed_errors.json"), "w") as f:
             json.dump(ERRS, f, indent=1)
     return e
 
