@@ -216,3 +216,100 @@ def test_errors(nc, tmp_path):
     with pytest.raises(Exception) as ei:
         nc.nc_write_layer(q, "s", np.zeros((2, 3), np.float32))
     assert getattr(ei.value, "status", None) == 8
+
+
+def _cdf5(path, dims, variables, numrecs=0):
+    """A CDF-5 (64-bit data) file written here from the published format
+    description, independently of the library: dims [(name, len)] (len 0:
+    the record dimension), variables [(name, dimids, nc_type, data,
+    atts)]; data big-endian, fixed variables first, then records."""
+    import struct
+
+    def name(s):
+        b = s.encode()
+        return struct.pack(">Q", len(b)) + b + b"\0" * (-len(b) % 4)
+
+    def att_list(atts):
+        if not atts:
+            return b"\0" * 12
+        out = struct.pack(">IQ", 0x0C, len(atts))
+        for an, at, av in atts:
+            raw = np.asarray(av).astype(at).tobytes()
+            out += name(an) + struct.pack(">IQ", {">f4": 5, ">i2": 3, ">i4": 4}[at], np.asarray(av).size)
+            out += raw + b"\0" * (-len(raw) % 4)
+        return out
+
+    def rec(v):
+        return dims[v[1][0]][1] == 0 if v[1] else False
+
+    codes = {">i1": 1, ">i2": 3, ">i4": 4, ">f4": 5, ">f8": 6, ">u1": 7, ">u2": 8, ">u4": 9, ">i8": 10, ">u8": 11}
+
+    def vbytes(v):
+        n = np.dtype(v[2]).itemsize
+        for d in v[1][1:] if rec(v) else v[1]:
+            n *= dims[d][1]
+        return n
+
+    def header(begins):
+        h = b"CDF\x05" + struct.pack(">Q", numrecs)
+        h += struct.pack(">IQ", 0x0A, len(dims)) + b"".join(name(n) + struct.pack(">Q", ln) for n, ln in dims)
+        h += b"\0" * 12
+        h += struct.pack(">IQ", 0x0B, len(variables))
+        for v, b in zip(variables, begins):
+            h += name(v[0]) + struct.pack(">Q", len(v[1])) + b"".join(struct.pack(">Q", d) for d in v[1])
+            h += att_list(v[4]) + struct.pack(">I", codes[v[2]]) + struct.pack(">Q", vbytes(v) + (-vbytes(v) % 4))
+            h += struct.pack(">Q", b)
+        return h
+
+    fixed = [v for v in variables if not rec(v)]
+    recs = [v for v in variables if rec(v)]
+    hlen = len(header([0] * len(variables)))
+    begins, off = {}, hlen
+    for v in fixed:
+        begins[v[0]] = off
+        off += vbytes(v) + (-vbytes(v) % 4)
+    rsize = sum(vbytes(v) + (-vbytes(v) % 4) for v in recs) if len(recs) != 1 else (vbytes(recs[0]) if recs else 0)
+    for v in recs:
+        begins[v[0]] = off
+        off += vbytes(v) + (-vbytes(v) % 4) if len(recs) != 1 else vbytes(v)
+    body = bytearray()
+    for v in fixed:
+        raw = np.ascontiguousarray(v[3]).astype(v[2]).tobytes()
+        body += raw + b"\0" * (-len(raw) % 4)
+    for r in range(numrecs):
+        for v in recs:
+            raw = np.ascontiguousarray(v[3][r]).astype(v[2]).tobytes()
+            body += raw + (b"\0" * (-len(raw) % 4) if len(recs) != 1 else b"")
+    assert rsize >= 0
+    with open(path, "wb") as f:
+        f.write(header([begins[v[0]] for v in variables]) + bytes(body))
+
+
+def test_read_cdf5(nc, tmp_path):
+    rng = np.random.default_rng(4)
+    nk, nj, ni = 3, 4, 5
+    i8 = rng.integers(-2**40, 2**40, (nj, ni)).astype(np.int64)
+    u2 = rng.integers(0, 60000, (nk, nj, ni)).astype(np.uint16)
+    u2[1, 2, 3] = 65535                                     # the default ushort fill
+    f3 = rng.normal(0, 1, (nk, nj, ni)).astype(np.float32)
+    b1 = rng.integers(-100, 100, (nj, ni)).astype(np.int8)  # odd sizes: padding
+    recs = rng.normal(0, 1, (3, nj, ni)).astype(np.float32)
+    dims = [("time", 0), ("k", nk), ("j", nj), ("i", ni)]
+    p = tmp_path / "cdf5.nc"
+    _cdf5(p, dims, [("big", [2, 3], ">i8", i8, []),
+                    ("u", [1, 2, 3], ">u2", u2, [("scale_factor", ">f4", np.float32(0.5))]),
+                    ("temp", [1, 2, 3], ">f4", f3, []),
+                    ("b", [2, 3], ">i1", b1, []),
+                    ("eta", [0, 2, 3], ">f4", recs, []),
+                    ("sal", [0, 2, 3], ">f4", recs + 1, [])], numrecs=3)
+    assert nc.nc_inq_var(p, "eta") == ((3, nj, ni), 5, True)
+    assert nc.nc_inq_var(p, "big") == ((nj, ni), 10, False)
+    assert np.array_equal(nc.nc_get_vara_float(p, "big"), i8.astype(np.float32))
+    assert np.array_equal(nc.nc_get_vara_float(p, "b"), b1.astype(np.float32))
+    assert np.array_equal(nc.nc_get_vara_float(p, "temp"), f3)
+    got = nc.nc_read_layer(p, "u", ni, nj, nk, k=1)
+    assert same(got, read_rules(u2[1], sf=0.5, default_fill=65535))
+    assert np.isnan(got[2, 3])
+    for r in range(3):
+        assert np.array_equal(nc.nc_read_layer(p, "eta", ni, nj, nk, r=r), recs[r])
+        assert np.array_equal(nc.nc_read_layer(p, "sal", ni, nj, nk, r=r), recs[r] + 1)
