@@ -313,3 +313,33 @@ def test_read_cdf5(nc, tmp_path):
     for r in range(3):
         assert np.array_equal(nc.nc_read_layer(p, "eta", ni, nj, nk, r=r), recs[r])
         assert np.array_equal(nc.nc_read_layer(p, "sal", ni, nj, nk, r=r), recs[r] + 1)
+
+
+def test_malformed_files_are_errors_not_crashes(nc, tmp_path):
+    """Truncated and corrupted headers end in an error status (the process
+    survives every case)."""
+    rng = np.random.default_rng(6)
+    good = tmp_path / "good.nc"
+    T = rng.standard_normal((3, 4, 2, 5)).astype(np.float32)
+    w = rng.standard_normal((3, 4, 5)).astype(np.float32)
+    nc.nc_write_transforms(good, T, w, stride=2, grid_name="g")
+    data = good.read_bytes()
+    hdr = data.find(b"grid_name") + 64                      # well inside the header
+    bad = tmp_path / "bad.nc"
+    outcomes = {"error": 0, "ok": 0}
+    for t in range(300):
+        b = bytearray(data)
+        if t % 3 == 0:
+            b = b[: int(rng.integers(0, len(b)))]
+        else:
+            for _ in range(int(rng.integers(1, 4))):
+                b[int(rng.integers(4, hdr))] = int(rng.integers(0, 256))
+        bad.write_bytes(bytes(b))
+        try:
+            nc.nc_inq_var(bad, "T")
+            nc.nc_get_vara_float(bad, "w", [0, 0, 0], [1, 1, 5])
+            nc.nc_read_layer(bad, "w", 5, 4, 1)
+            outcomes["ok"] += 1
+        except Exception:
+            outcomes["error"] += 1
+    assert outcomes["error"] > 0
