@@ -327,7 +327,7 @@ ENKFG_API enkfg_status enkfg_set_obs(enkfg_ctx* ctx, int nobs, const float* lon,
         NEED(type[o] >= 0 && type[o] < ctx->ntypes, ENKFG_EINVAL, "obs %d: type %d out of range", o, (int)type[o]);
     SETDEV();
     enkfg_status s;
-    size_t n = nobs > 0 ? nobs : 1, cap;
+    size_t n = nobs > 0 ? nobs : 1;
     void** bufs[] = { (void**)&ctx->d_lon, (void**)&ctx->d_lat, (void**)&ctx->d_type, (void**)&ctx->d_status,
                       (void**)&ctx->d_estd, (void**)&ctx->d_value, (void**)&ctx->d_ox, (void**)&ctx->d_oy,
                       (void**)&ctx->d_oz, (void**)&ctx->d_fi, (void**)&ctx->d_fj, (void**)&ctx->d_fk,
@@ -336,8 +336,6 @@ ENKFG_API enkfg_status enkfg_set_obs(enkfg_ctx* ctx, int nobs, const float* lon,
         if (*bufs[k]) cudaFree(*bufs[k]);
         *bufs[k] = nullptr;
     }
-    (void)cap;
-    (void)s;
     CK(cudaMalloc(&ctx->d_lon, n * sizeof(float)));
     CK(cudaMalloc(&ctx->d_lat, n * sizeof(float)));
     CK(cudaMalloc(&ctx->d_type, n * sizeof(short)));
