@@ -186,7 +186,7 @@ struct or_obsset {
 };
 
 /* ll2xyz (utils.c:1449-1458) */
-static void or_ll2xyz(const double in[2], double out[3])
+void or_ll2xyz(const double in[2], double out[3])
 {
     double lon = in[0] * OR_DEG2RAD;
     double lat = in[1] * OR_DEG2RAD;

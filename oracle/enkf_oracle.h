@@ -82,6 +82,10 @@ void or_calcinnandspread(int nmem, int nobs, float* S, const float* value, const
 /* das_standardise (ensobs.c:849-898). rfactor is per type. */
 void or_standardise(int nmem, int nobs, float* S, double* s_f, const float* estd, const short* type, const double* rfactor);
 
+/* ll2xyz (utils.c:1449-1458): lon/lat in degrees to xyz on the sphere of
+ * radius 6371 km. */
+void or_ll2xyz(const double in[2], double out[3]);
+
 /* Forward operator on a structured grid, footprint 0.
  * or_interp2d: interpolate2d_structured (utils.c:1140-1210); v [nj][ni],
  * mask [nj][ni] (numlevels, nonzero = wet).

@@ -262,3 +262,16 @@ def test_finish_HE_semantics():
     assert nbad == 2 and st2[5] == 10 and st2[7] == 10 and st2[9] == 2
     S, st2, nbad = oracle.finish_HE(HE, st, mode=0, nmem_dynamic=m, skip_bad=False)
     assert nbad == 0 and st2[5] == 0
+
+
+@pytest.mark.skipif(oracle.reflib_utils() is None, reason="reference library not built here")
+def test_ll2xyz_equals_reference_build():
+    import ctypes as C
+    rng = np.random.default_rng(8)
+    L, R = oracle.lib(), oracle.reflib_utils()
+    for _ in range(2000):
+        ll = (C.c_double * 2)(rng.uniform(-360, 360), rng.uniform(-90, 90))
+        a, b = (C.c_double * 3)(), (C.c_double * 3)()
+        L.or_ll2xyz(ll, a)
+        R.ll2xyz(ll, b)
+        assert list(a) == list(b)
