@@ -275,3 +275,62 @@ def test_ll2xyz_equals_reference_build():
         L.or_ll2xyz(ll, a)
         R.ll2xyz(ll, b)
         assert list(a) == list(b)
+
+
+# ---------------------------------------------------------------------------
+# known answers of the per-point numerics (calc/calcs.c), for the oracle and,
+# where it is built here, the reference itself
+# ---------------------------------------------------------------------------
+
+def _impls():
+    out = [("oracle", oracle.calc_wT)]
+    if oracle.reflib() is not None:
+        out.append(("reference", oracle.ref_calc_wT))
+    return out
+
+
+@pytest.mark.parametrize("name,calc", _impls())
+def test_single_observation_closed_form(name, calc):
+    rng = np.random.default_rng(31)
+    m = 9
+    S = rng.normal(0, 0.7, (m, 1))                   # one observation: S [m][p = 1]
+    d = np.array([0.8])
+    a = float((S[:, 0] ** 2).sum())
+    ss = np.outer(S[:, 0], S[:, 0])
+    w_exact = S[:, 0] * d[0] / (1.0 + a)
+    # ETKF: T = (I + s s')^(-1/2) = I + (1/sqrt(1 + a) - 1) s s' / a
+    w, T, _ = calc(0, 1, m, m, d, S)
+    assert np.abs(w - w_exact).max() < 1e-13, name
+    assert np.abs(T - (np.eye(m) + (1.0 / np.sqrt(1.0 + a) - 1.0) * ss / a)).max() < 1e-13, name
+    # DEnKF: T = (I + M^-1) / 2 = I - s s' / (2 (1 + a))
+    w, T, _ = calc(0, 0, m, m, d, S)
+    assert np.abs(w - w_exact).max() < 1e-13, name
+    assert np.abs(T - (np.eye(m) - ss / (2.0 * (1.0 + a)))).max() < 1e-13, name
+    # EnOI: w only
+    w, _, _ = calc(1, 0, m, m, d, S)
+    assert np.abs(w - w_exact).max() < 1e-13, name
+
+
+@pytest.mark.parametrize("name,calc", _impls())
+@pytest.mark.parametrize("p", [5, 40])              # p < m and p >= m: the two branches of calcs.c
+def test_transform_identities(name, calc, p):
+    rng = np.random.default_rng(32 + p)
+    m = 16
+    S = rng.normal(0, 0.5, (m, p))
+    S -= S.mean(axis=0)                              # member-mean-free anomalies, as after das_calcinnandspread
+    d = rng.normal(0, 1, p)
+    M = np.eye(m) + S @ S.T
+    lam, U = np.linalg.eigh(M)                       # an independent path: numpy's symmetric eigensolver
+    T_etkf = (U / np.sqrt(lam)) @ U.T
+    Minv = (U / lam) @ U.T
+    w_exact = Minv @ (S @ d)
+    w_e, T_e, _ = calc(0, 1, m, m, d, S)
+    w_d, T_d, _ = calc(0, 0, m, m, d, S)
+    assert np.abs(T_e - T_e.T).max() < 1e-12, name                     # ETKF transform is symmetric
+    assert np.abs(T_e - T_etkf).max() < 1e-11, name
+    assert np.abs(T_d - 0.5 * (np.eye(m) + Minv)).max() < 1e-11, name
+    assert np.abs(w_e - w_exact).max() < 1e-11 and np.abs(w_d - w_exact).max() < 1e-11, name
+    assert np.abs(w_e - w_d).max() < 1e-12, name                        # the schemes agree on w
+    ones = np.ones(m)
+    assert np.abs(T_e @ ones - ones).max() < 1e-12, name                # the mean is kept
+    assert np.abs(T_d @ ones - ones).max() < 1e-12, name
