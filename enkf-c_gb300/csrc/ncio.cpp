@@ -641,6 +641,53 @@ Var fixed_var(const char* nm, int type, std::initializer_list<int> dimids)
     return v;
 }
 
+// The value rules of ncu_readfield / ncu_read3dfield (common/ncutils.c:
+// 300-530, 1015-1245): values equal to the fill value (the attribute, else
+// the type's default) or to missing_value, and values outside valid_min /
+// valid_max / valid_range, become NaN, compared on the native values
+// (integers and bit patterns alike); then scale_factor and add_offset as
+// floats.  ncu_read3dfield masks only when one of those five attributes is
+// present (only_with_atts).
+void apply_read_rules(const Var& V, const std::vector<unsigned char>& raw, float* v, bool only_with_atts)
+{
+    const int t = V.type, ts = type_size(t);
+    const size_t n = raw.size() / ts;
+    auto same = [&](const unsigned char* p, const Att& a) {
+        if (a.n != 1) return false;
+        if (a.type == t) return memcmp(p, a.raw.data(), ts) == 0;
+        return decode(p, t) == a.num(0);
+    };
+    const Att* fillv = V.att("_FillValue");
+    unsigned char dfill[8];
+    default_fill_raw(t, dfill);
+    const Att* miss = V.att("missing_value");
+    const Att* vmin = V.att("valid_min");
+    const Att* vmax = V.att("valid_max");
+    const Att* vrng = V.att("valid_range");
+    const bool mask = !only_with_atts || fillv || miss || vmin || vmax || vrng;
+    if (vrng && vrng->n != 2) vrng = nullptr;
+    for (size_t q = 0; mask && q < n; ++q) {
+        const unsigned char* p = raw.data() + q * ts;
+        bool out = fillv ? same(p, *fillv) : memcmp(p, dfill, ts) == 0;
+        if (!out && miss) out = same(p, *miss);
+        if (!out && (vmin || vmax || vrng)) {
+            const double x = decode(p, t);
+            if (vmin && vmin->n == 1 && x < vmin->num(0)) out = true;
+            if (vmax && vmax->n == 1 && x > vmax->num(0)) out = true;
+            if (vrng && (x < vrng->num(0) || x > vrng->num(1))) out = true;
+        }
+        if (out) v[q] = NAN;
+    }
+    if (const Att* a = V.att("scale_factor")) {
+        const float sf = (float)a->num(0);
+        for (size_t q = 0; q < n; ++q) v[q] *= sf;
+    }
+    if (const Att* a = V.att("add_offset")) {
+        const float ao = (float)a->num(0);
+        for (size_t q = 0; q < n; ++q) v[q] += ao;
+    }
+}
+
 // the entry points: no C++ exception crosses the C ABI
 template <typename F>
 enkfg_status guarded(F f)
@@ -784,44 +831,64 @@ static enkfg_status impl_read_layer(const char* path, const char* var, int r, in
     const size_t n = raw.size() / ts;
     for (size_t q = 0; q < n; ++q) v[q] = to_float(raw.data() + q * ts, t);
 
-    // values equal to the fill value (the attribute, else the type's
-    // default) or to missing_value, and values outside valid_min / valid_max
-    // / valid_range, are NaN (common/ncutils.c:300-490); compared on the
-    // native values, integers and bit patterns alike
-    auto same = [&](const unsigned char* p, const Att& a) {
-        if (a.n != 1) return false;
-        if (a.type == t) return memcmp(p, a.raw.data(), ts) == 0;
-        return decode(p, t) == a.num(0);
-    };
-    const Att* fillv = V->att("_FillValue");
-    unsigned char dfill[8];
-    default_fill_raw(t, dfill);
-    const Att* miss = V->att("missing_value");
-    const Att* vmin = V->att("valid_min");
-    const Att* vmax = V->att("valid_max");
-    const Att* vrng = V->att("valid_range");
-    if (vrng && vrng->n != 2) vrng = nullptr;
-    for (size_t q = 0; q < n; ++q) {
-        const unsigned char* p = raw.data() + q * ts;
-        bool out = fillv ? same(p, *fillv) : memcmp(p, dfill, ts) == 0;
-        if (!out && miss) out = same(p, *miss);
-        if (!out && (vmin || vmax || vrng)) {
-            const double x = decode(p, t);
-            if (vmin && vmin->n == 1 && x < vmin->num(0)) out = true;
-            if (vmax && vmax->n == 1 && x > vmax->num(0)) out = true;
-            if (vrng && (x < vrng->num(0) || x > vrng->num(1))) out = true;
+    apply_read_rules(*V, raw, v, false);
+    return ENKFG_OK;
+}
+
+static enkfg_status impl_read_field3d(const char* path, const char* var, int r, int ni, int nj, int nk, float* v)
+{
+    if (ni < 1 || nj < 1 || nk < 1 || !v) return fail(ENKFG_EINVAL, "bad field arguments");
+    File F;
+    NcFile nc;
+    enkfg_status s = open_parse(path, "rb", F, nc);
+    if (s) return s;
+    const Var* V = var ? nc.var(var) : nullptr;
+    if (!V) return fail(ENKFG_EINVAL, "%s: no variable \"%s\"", path, var ? var : "(null)");
+    if (V->type == T_CHAR) return fail(ENKFG_EINVAL, "%s: %s is text", path, var);
+    // the ncu_read3dfield dimension rules on a structured grid
+    // (common/ncutils.c:923-990): [r][k][j][i] or [k][j][i]
+    const int nd = (int)V->dimids.size();
+    const bool rec = nc.is_rec(*V);
+    long long dl[4] = { 0, 0, 0, 0 };
+    for (int d = 0; d < nd && d < 4; ++d) dl[d] = nc.dimlen(*V, d);
+    if (rec && dl[0] == 0) return fail(ENKFG_EINVAL, "%s: %s: empty record dimension", path, var);
+    long long start[4] = { 0, 0, 0, 0 }, count[4] = { 0, 0, 0, 0 };
+    if (nd == 4) {
+        if (r < 0) {
+            if (dl[0] > 1) return fail(ENKFG_EINVAL, "%s: %s: not supposed to have multiple records", path, var);
+            r = 0;
         }
-        if (out) v[q] = NAN;
+        if (r >= dl[0]) return fail(ENKFG_EINVAL, "%s: %s: cannot read record %d (nr = %lld)", path, var, r, dl[0]);
+        if (dl[3] != ni || dl[2] != nj || dl[1] != nk)
+            return fail(ENKFG_EINVAL, "%s: %s: dimensions %lld x %lld x %lld do not match %d x %d x %d", path, var,
+                        dl[3], dl[2], dl[1], ni, nj, nk);
+        const long long s4[4] = { r, 0, 0, 0 }, c4[4] = { 1, nk, nj, ni };
+        memcpy(start, s4, sizeof(s4));
+        memcpy(count, c4, sizeof(c4));
+    } else if (nd == 3) {
+        if (rec) return fail(ENKFG_EINVAL, "%s: %s: a 2-D variable with records is not a 3-D field", path, var);
+        if (r > 0) return fail(ENKFG_EINVAL, "%s: %s: no record %d in a 3-dimensional variable", path, var, r);
+        if (dl[2] != ni || dl[1] != nj || dl[0] != nk)
+            return fail(ENKFG_EINVAL, "%s: %s: dimensions %lld x %lld x %lld do not match %d x %d x %d", path, var,
+                        dl[2], dl[1], dl[0], ni, nj, nk);
+        const long long s3[3] = { 0, 0, 0 }, c3[3] = { nk, nj, ni };
+        memcpy(start, s3, sizeof(s3));
+        memcpy(count, c3, sizeof(c3));
+    } else {
+        return fail(ENKFG_EINVAL, "%s: %s: cannot read a 3-D field from %d dimensions", path, var, nd);
     }
-    // then scale_factor and add_offset, as floats (ncutils.c:495-515)
-    if (const Att* a = V->att("scale_factor")) {
-        const float sf = (float)a->num(0);
-        for (size_t q = 0; q < n; ++q) v[q] *= sf;
+    std::vector<unsigned char> raw;
+    if ((s = read_raw(F.f, nc, *V, start, count, raw))) return s;
+    const int t = V->type, ts = type_size(t);
+    const size_t n = raw.size() / ts;
+    for (size_t q = 0; q < n; ++q) {
+        v[q] = to_float(raw.data() + q * ts, t);
+        // a double beyond the float range stops the reference's read
+        // (ncw_get_vara_float without the range fix)
+        if (t == T_DOUBLE && v[q] != v[q] && decode(raw.data() + q * ts, t) == decode(raw.data() + q * ts, t))
+            return fail(ENKFG_EINVAL, "%s: %s: value %zu outside the float range", path, var, q);
     }
-    if (const Att* a = V->att("add_offset")) {
-        const float ao = (float)a->num(0);
-        for (size_t q = 0; q < n; ++q) v[q] += ao;
-    }
+    apply_read_rules(*V, raw, v, true);
     return ENKFG_OK;
 }
 
@@ -955,6 +1022,11 @@ ENKFG_API enkfg_status enkfg_nc_get_vara_float(const char* path, const char* var
 ENKFG_API enkfg_status enkfg_nc_read_layer(const char* path, const char* var, int r, int k, int ni, int nj, int nk, float* v)
 {
     return guarded([&] { return impl_read_layer(path, var, r, k, ni, nj, nk, v); });
+}
+
+ENKFG_API enkfg_status enkfg_nc_read_field3d(const char* path, const char* var, int r, int ni, int nj, int nk, float* v)
+{
+    return guarded([&] { return impl_read_field3d(path, var, r, ni, nj, nk, v); });
 }
 
 ENKFG_API enkfg_status enkfg_nc_write_layer(const char* path, const char* var, int k, int ni, int nj, int nk, const float* v)

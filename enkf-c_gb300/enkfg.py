@@ -48,7 +48,7 @@ EXPORTS = ["enkfg_create", "enkfg_destroy", "enkfg_last_error", "enkfg_status_st
            "enkfg_autotune_reset", "enkfg_adjoint_transforms", "enkfg_adjoint_mean", "enkfg_set_obs_positions",
            "enkfg_begin_HE", "enkfg_map_obs", "enkfg_map_obs_dev", "enkfg_finish_HE", "enkfg_nc_last_error",
            "enkfg_nc_write_transforms", "enkfg_nc_write_diag", "enkfg_nc_inq_var", "enkfg_nc_get_vara_float",
-           "enkfg_nc_read_layer", "enkfg_nc_write_layer"]
+           "enkfg_nc_read_layer", "enkfg_nc_read_field3d", "enkfg_nc_write_layer"]
 
 
 class EnkfgError(RuntimeError):
@@ -515,6 +515,14 @@ def nc_read_layer(path, var, ni, nj, nk=1, k=0, r=-1):
     v = np.empty((nj, ni), np.float32)
     _nc_ck(load().enkfg_nc_read_layer(os.fsencode(path), var.encode(), C.c_int(r), C.c_int(k), C.c_int(ni),
                                       C.c_int(nj), C.c_int(nk), _p(v, C.c_float)))
+    return v
+
+
+def nc_read_field3d(path, var, ni, nj, nk, r=-1):
+    """ncu_read3dfield (common/ncutils.c:923-1245): the [nk][nj][ni] field."""
+    v = np.empty((nk, nj, ni), np.float32)
+    _nc_ck(load().enkfg_nc_read_field3d(os.fsencode(path), var.encode(), C.c_int(r), C.c_int(ni), C.c_int(nj),
+                                        C.c_int(nk), _p(v, C.c_float)))
     return v
 
 

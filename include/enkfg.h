@@ -354,6 +354,14 @@ ENKFG_API enkfg_status enkfg_nc_get_vara_float(const char* path, const char* var
  * applied in float. */
 ENKFG_API enkfg_status enkfg_nc_read_layer(const char* path, const char* var, int r, int k, int ni, int nj, int nk, float* v);
 
+/* ncu_read3dfield (common/ncutils.c:923-1245) on a structured grid: the
+ * whole field of record r (r < 0: the only record) of `var` laid out
+ * [r][k][j][i] or [k][j][i], into v [nk][nj][ni]; the value rules of
+ * enkfg_nc_read_layer, except that values are masked only when one of
+ * _FillValue, missing_value, valid_min, valid_max or valid_range is present,
+ * and a double beyond the float range is an error. */
+ENKFG_API enkfg_status enkfg_nc_read_field3d(const char* path, const char* var, int r, int ni, int nj, int nk, float* v);
+
 /* ncu_writefield (common/ncutils.c:537-700) on a structured grid, into an
  * existing file: layer k (or the last record) of a float or double
  * variable; add_offset and scale_factor undone, values clamped to the valid

@@ -343,3 +343,38 @@ def test_malformed_files_are_errors_not_crashes(nc, tmp_path):
         except Exception:
             outcomes["error"] += 1
     assert outcomes["error"] > 0
+
+
+def test_read_field3d_rules(nc, tmp_path):
+    rng = np.random.default_rng(7)
+    nk, nj, ni = 3, 4, 6
+    p = tmp_path / "member3d.nc"
+    a = rng.normal(10, 1, (nk, nj, ni)).astype(np.float32)
+    a[1, 1, 1] = FILL_F                     # default fill, but no masking attribute: kept
+    b = rng.integers(-500, 500, (2, nk, nj, ni)).astype(np.int16)
+    b[1, 2, 0, 0] = -32767                  # default short fill, masked because missing_value is present
+    b[1, 0, 1, 1] = 99
+    c = rng.normal(0, 1, (nk, nj, ni))
+    with netcdf_file(p, "w", version=2) as f:
+        f.createDimension("time", None)
+        f.createDimension("k", nk)
+        f.createDimension("j", nj)
+        f.createDimension("i", ni)
+        v = f.createVariable("a", "f4", ("k", "j", "i"))
+        v[:] = a
+        v = f.createVariable("b", "i2", ("time", "k", "j", "i"))
+        v[:] = b
+        v.missing_value = np.int16(99)
+        v.scale_factor = np.float32(0.1)
+        v = f.createVariable("c", "f8", ("k", "j", "i"))
+        v[:] = c
+    got = nc.nc_read_field3d(p, "a", ni, nj, nk)
+    assert np.array_equal(got, a)                                   # FILL_F kept (no attributes)
+    got = nc.nc_read_field3d(p, "b", ni, nj, nk, r=1)
+    assert same(got, read_rules(b[1], missing=99, sf=0.1, default_fill=-32767))
+    assert np.isnan(got[2, 0, 0]) and np.isnan(got[0, 1, 1])
+    assert same(nc.nc_read_field3d(p, "c", ni, nj, nk), c.astype(np.float32))
+    with pytest.raises(Exception):
+        nc.nc_read_field3d(p, "b", ni, nj, nk)                      # two records, none named
+    with pytest.raises(Exception):
+        nc.nc_read_field3d(p, "a", ni, nj, nk + 1)                  # layer count mismatch
