@@ -50,3 +50,23 @@ def test_status_strings_and_errors_without_device(lib):
     # calls on a NULL context fail cleanly
     assert lib.enkfg_standardise(None) == 1
     assert lib.enkfg_set_grid(None, None) == 1
+
+
+def test_plain_c_client(tmp_path):
+    """A C99 program that includes only enkfg.h and links libenkfg.so, as
+    EnKF-C's host code would (tests/c_client.c)."""
+    import shutil
+    import subprocess
+    import build
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    lib = build.build()
+    exe = tmp_path / "c_client"
+    src = os.path.join(ROOT, "tests", "c_client.c")
+    r = subprocess.run([cc, "-std=c99", "-Wall", "-Wextra", "-Werror", "-I", os.path.join(ROOT, "include"), src,
+                        "-o", str(exe), "-L", os.path.dirname(lib), "-lenkfg", "-Wl,-rpath," + os.path.dirname(lib),
+                        "-lm"], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    r = subprocess.run([str(exe), str(tmp_path / "t.nc")], capture_output=True, text=True, timeout=120)
+    assert r.returncode == 0 and r.stdout.strip() == "ok", r.stdout + r.stderr
