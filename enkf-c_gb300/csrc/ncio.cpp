@@ -617,6 +617,12 @@ enkfg_status write_fixed(const char* path, NcFile& nc, const std::vector<FixedVa
         const Var& v = nc.vars[k];
         const long long n = nc.data_bytes(v) / 4;    // int32 and float only here
         const uint32_t* src = (const uint32_t*)data[k].data;
+        if (!src) {
+            // no data yet: the variable's space is reserved (written row by
+            // row later); the file is extended to its full size at the end
+            if (fseeko(f, (off_t)v.vsize, SEEK_CUR) != 0) return fail(ENKFG_EINVAL, "%s: seek failed", path);
+            continue;
+        }
         const long long chunk = 1 << 20;
         for (long long a = 0; a < n; a += chunk) {
             const long long m = n - a < chunk ? n - a : chunk;
@@ -628,8 +634,31 @@ enkfg_status write_fixed(const char* path, NcFile& nc, const std::vector<FixedVa
         const unsigned char z[4] = { 0, 0, 0, 0 };
         if (padn > 0 && fwrite(z, 1, (size_t)padn, f) != (size_t)padn) return fail(ENKFG_EINVAL, "%s: write failed", path);
     }
+    const long long end = ftello(f);
+    if (end != off) {
+        const unsigned char z = 0;
+        if (fseeko(f, (off_t)(off - 1), SEEK_SET) != 0 || fwrite(&z, 1, 1, f) != 1)
+            return fail(ENKFG_EINVAL, "%s: write failed", path);
+    }
     if (fflush(f) != 0) return fail(ENKFG_EINVAL, "%s: write failed", path);
     return ENKFG_OK;
+}
+
+// big-endian images of host values written into a hyperslab of a float or
+// int variable of an open file
+enkfg_status write_slab(FILE* f, const NcFile& nc, const Var& v, const long long* start, const long long* count,
+                        const void* host)
+{
+    long long total = 1;
+    for (size_t d = 0; d < v.dimids.size(); ++d) total *= count[d];
+    std::vector<unsigned char> raw((size_t)total * 4);
+    const uint32_t* src = (const uint32_t*)host;
+    for (long long q = 0; q < total; ++q) put_be(raw.data() + q * 4, src[q], 4);
+    return for_runs(nc, v, start, count, [&](long long off, long long m, long long at) -> enkfg_status {
+        if (fseeko(f, (off_t)off, SEEK_SET) != 0 || fwrite(raw.data() + at * 4, 4, (size_t)m, f) != (size_t)m)
+            return fail(ENKFG_EINVAL, "%s: write failed at byte %lld", v.name.c_str(), off);
+        return ENKFG_OK;
+    });
 }
 
 Var fixed_var(const char* nm, int type, std::initializer_list<int> dimids)
@@ -710,29 +739,73 @@ ENKFG_API const char* enkfg_nc_last_error(void)
     return g_err;
 }
 
-static enkfg_status impl_write_transforms(const char* path, int nj, int ni, int nmem_dynamic, int nmem,
-                                                 const float* T, const float* w, int stride, const char* grid_name)
+// the transforms.nc layout of nc_createtransforms (calc/transforms.c:54-94)
+static NcFile transforms_file(int nj, int ni, int nmem_dynamic, int nmem, bool with_T, int stride,
+                              const char* grid_name)
 {
-    if (nj < 1 || ni < 1 || nmem < 1 || !w || (T && (nmem_dynamic < 1 || nmem_dynamic > nmem)))
-        return fail(ENKFG_EINVAL, "bad transforms dimensions %d x %d, m_dyn %d, m %d", nj, ni, nmem_dynamic, nmem);
     NcFile nc;
     nc.dims.push_back({ "j", nj });
     nc.dims.push_back({ "i", ni });
-    std::vector<FixedVar> data;
-    if (T) {
+    if (with_T) {
         nc.dims.push_back({ "m_dyn", nmem_dynamic });
         nc.dims.push_back({ "m", nmem });
         nc.vars.push_back(fixed_var("T", T_FLOAT, { 0, 1, 2, 3 }));
         nc.vars.push_back(fixed_var("w", T_FLOAT, { 0, 1, 3 }));
-        data = { { T }, { w } };
     } else {
         nc.dims.push_back({ "m", nmem });
         nc.vars.push_back(fixed_var("w", T_FLOAT, { 0, 1, 2 }));
-        data = { { w } };
     }
     nc.gatts.push_back(int_att("stride", stride));
     nc.gatts.push_back(text_att("grid_name", grid_name ? grid_name : ""));
+    return nc;
+}
+
+static enkfg_status impl_write_transforms(const char* path, int nj, int ni, int nmem_dynamic, int nmem,
+                                          const float* T, const float* w, int stride, const char* grid_name)
+{
+    if (nj < 1 || ni < 1 || nmem < 1 || !w || (T && (nmem_dynamic < 1 || nmem_dynamic > nmem)))
+        return fail(ENKFG_EINVAL, "bad transforms dimensions %d x %d, m_dyn %d, m %d", nj, ni, nmem_dynamic, nmem);
+    NcFile nc = transforms_file(nj, ni, nmem_dynamic, nmem, T != nullptr, stride, grid_name);
+    std::vector<FixedVar> data;
+    if (T)
+        data = { { T }, { w } };
+    else
+        data = { { w } };
     return write_fixed(path, nc, data);
+}
+
+static enkfg_status impl_create_transforms(const char* path, int nj, int ni, int nmem_dynamic, int nmem, int with_T,
+                                           int stride, const char* grid_name)
+{
+    if (nj < 1 || ni < 1 || nmem < 1 || (with_T && (nmem_dynamic < 1 || nmem_dynamic > nmem)))
+        return fail(ENKFG_EINVAL, "bad transforms dimensions %d x %d, m_dyn %d, m %d", nj, ni, nmem_dynamic, nmem);
+    NcFile nc = transforms_file(nj, ni, nmem_dynamic, nmem, with_T != 0, stride, grid_name);
+    std::vector<FixedVar> data(nc.vars.size(), FixedVar{ nullptr });
+    return write_fixed(path, nc, data);
+}
+
+static enkfg_status impl_write_transforms_row(const char* path, int j, const float* Tj, const float* wj)
+{
+    File F;
+    NcFile nc;
+    enkfg_status s = open_parse(path, "r+b", F, nc);
+    if (s) return s;
+    const Var* W = nc.var("w");
+    const Var* T = nc.var("T");
+    if (!W || W->type != T_FLOAT || W->dimids.size() != 3 || nc.is_rec(*W))
+        return fail(ENKFG_EINVAL, "%s: not a transforms file (no float w [j][i][m])", path);
+    const long long nj = nc.dimlen(*W, 0), ni = nc.dimlen(*W, 1), m = nc.dimlen(*W, 2);
+    if (j < 0 || j >= nj) return fail(ENKFG_EINVAL, "%s: row %d outside 0..%lld", path, j, nj - 1);
+    if (!wj || (T && !Tj)) return fail(ENKFG_EINVAL, "%s: row data missing", path);
+    if (T) {
+        if (T->type != T_FLOAT || T->dimids.size() != 4 || nc.dimlen(*T, 0) != nj || nc.dimlen(*T, 1) != ni ||
+            nc.dimlen(*T, 3) != m)
+            return fail(ENKFG_EINVAL, "%s: T does not match w", path);
+        const long long st4[4] = { j, 0, 0, 0 }, ct4[4] = { 1, ni, nc.dimlen(*T, 2), m };
+        if ((s = write_slab(F.f, nc, *T, st4, ct4, Tj))) return s;
+    }
+    const long long st3[3] = { j, 0, 0 }, ct3[3] = { 1, ni, m };
+    return write_slab(F.f, nc, *W, st3, ct3, wj);
 }
 
 static enkfg_status impl_write_diag(const char* path, int nj, int ni, int ntypes, const char* const* type_names,
@@ -1002,6 +1075,17 @@ static enkfg_status impl_write_layer(const char* path, const char* var, int k, i
 ENKFG_API enkfg_status enkfg_nc_write_transforms(const char* path, int nj, int ni, int nmem_dynamic, int nmem, const float* T, const float* w, int stride, const char* grid_name)
 {
     return guarded([&] { return impl_write_transforms(path, nj, ni, nmem_dynamic, nmem, T, w, stride, grid_name); });
+}
+
+ENKFG_API enkfg_status enkfg_nc_create_transforms(const char* path, int nj, int ni, int nmem_dynamic, int nmem,
+                                                  int with_T, int stride, const char* grid_name)
+{
+    return guarded([&] { return impl_create_transforms(path, nj, ni, nmem_dynamic, nmem, with_T, stride, grid_name); });
+}
+
+ENKFG_API enkfg_status enkfg_nc_write_transforms_row(const char* path, int j, const float* Tj, const float* wj)
+{
+    return guarded([&] { return impl_write_transforms_row(path, j, Tj, wj); });
 }
 
 ENKFG_API enkfg_status enkfg_nc_write_diag(const char* path, int nj, int ni, int ntypes, const char* const* type_names, int stride, const int* nlobs, const float* dfs, const float* srf, const int* pnlobs, const float* pdfs, const float* psrf)

@@ -47,7 +47,8 @@ EXPORTS = ["enkfg_create", "enkfg_destroy", "enkfg_last_error", "enkfg_status_st
            "enkfg_set_HE_dev", "enkfg_rebuild_index", "enkfg_local_offsets_noalloc", "enkfg_autotune_table",
            "enkfg_autotune_reset", "enkfg_adjoint_transforms", "enkfg_adjoint_mean", "enkfg_set_obs_positions",
            "enkfg_begin_HE", "enkfg_map_obs", "enkfg_map_obs_dev", "enkfg_finish_HE", "enkfg_nc_last_error",
-           "enkfg_nc_write_transforms", "enkfg_nc_write_diag", "enkfg_nc_inq_var", "enkfg_nc_get_vara_float",
+           "enkfg_nc_write_transforms", "enkfg_nc_create_transforms", "enkfg_nc_write_transforms_row",
+           "enkfg_nc_write_diag", "enkfg_nc_inq_var", "enkfg_nc_get_vara_float",
            "enkfg_nc_read_layer", "enkfg_nc_read_field3d", "enkfg_nc_write_layer"]
 
 
@@ -473,6 +474,21 @@ def nc_write_transforms(path, T, w, stride=1, grid_name=""):
     _nc_ck(load().enkfg_nc_write_transforms(os.fsencode(path), C.c_int(nj), C.c_int(ni), C.c_int(md), C.c_int(m),
                                             _p(Tc, C.c_float), _p(w, C.c_float), C.c_int(int(stride)),
                                             grid_name.encode()))
+
+
+def nc_create_transforms(path, nj, ni, nmem_dynamic, nmem, with_T=True, stride=1, grid_name=""):
+    """nc_createtransforms (calc/transforms.c:54-94): the file, rows to follow."""
+    _nc_ck(load().enkfg_nc_create_transforms(os.fsencode(path), C.c_int(nj), C.c_int(ni), C.c_int(nmem_dynamic),
+                                             C.c_int(nmem), C.c_int(int(with_T)), C.c_int(int(stride)),
+                                             grid_name.encode()))
+
+
+def nc_write_transforms_row(path, j, Tj, wj):
+    """nc_writetransforms (calc/transforms.c:98-131): strided row j."""
+    wj = np.ascontiguousarray(wj, np.float32)
+    Tj = None if Tj is None else np.ascontiguousarray(Tj, np.float32)
+    _nc_ck(load().enkfg_nc_write_transforms_row(os.fsencode(path), C.c_int(int(j)), _p(Tj, C.c_float),
+                                                _p(wj, C.c_float)))
 
 
 def nc_write_diag(path, type_names, nlobs, dfs, srf, pnlobs, pdfs, psrf, stride=1):

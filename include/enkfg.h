@@ -329,6 +329,13 @@ ENKFG_API const char* enkfg_nc_last_error(void);
  * grid_name (text).  T NULL (EnOI): no m_dyn and no T. */
 ENKFG_API enkfg_status enkfg_nc_write_transforms(const char* path, int nj, int ni, int nmem_dynamic, int nmem, const float* T, const float* w, int stride, const char* grid_name);
 
+/* The same file row by row, as the reference fills it: nc_createtransforms
+ * (calc/transforms.c:54-94) makes the file with its variables' space
+ * reserved; nc_writetransforms (calc/transforms.c:98-131) writes strided row
+ * j: Tj [ni][m_dyn][m] (NULL for a file without T) and wj [ni][m]. */
+ENKFG_API enkfg_status enkfg_nc_create_transforms(const char* path, int nj, int ni, int nmem_dynamic, int nmem, int with_T, int stride, const char* grid_name);
+ENKFG_API enkfg_status enkfg_nc_write_transforms_row(const char* path, int j, const float* Tj, const float* wj);
+
 /* enkf_diag.nc (calc/transforms.c:380-470): dimensions nobstypes, j, i; int
  * nlobs [j][i], float dfs and srf [j][i], int pnlobs and float pdfs, psrf
  * [nobstypes][j][i] with the reference's long_name / comment attributes;

@@ -378,3 +378,30 @@ def test_read_field3d_rules(nc, tmp_path):
         nc.nc_read_field3d(p, "b", ni, nj, nk)                      # two records, none named
     with pytest.raises(Exception):
         nc.nc_read_field3d(p, "a", ni, nj, nk + 1)                  # layer count mismatch
+
+
+def test_transforms_row_by_row(nc, tmp_path):
+    """nc_createtransforms then nc_writetransforms per strided row, in any
+    row order, give the file the whole-array writer gives."""
+    rng = np.random.default_rng(12)
+    nj, ni, md, m = 6, 5, 3, 4
+    T = rng.standard_normal((nj, ni, md, m)).astype(np.float32)
+    w = rng.standard_normal((nj, ni, m)).astype(np.float32)
+    p = tmp_path / "rows.nc"
+    nc.nc_create_transforms(p, nj, ni, md, m, with_T=True, stride=2, grid_name="g1")
+    for j in rng.permutation(nj):
+        nc.nc_write_transforms_row(p, int(j), T[j], w[j])
+    q = tmp_path / "whole.nc"
+    nc.nc_write_transforms(q, T, w, stride=2, grid_name="g1")
+    assert p.read_bytes() == q.read_bytes()
+    with netcdf_file(p, "r", mmap=False) as f:
+        assert np.array_equal(f.variables["T"][:], T) and np.array_equal(f.variables["w"][:], w)
+    # EnOI (no T) and a row out of range
+    e = tmp_path / "enoi.nc"
+    nc.nc_create_transforms(e, nj, ni, 0, m, with_T=False)
+    for j in range(nj):
+        nc.nc_write_transforms_row(e, j, None, w[j])
+    with netcdf_file(e, "r", mmap=False) as f:
+        assert np.array_equal(f.variables["w"][:], w) and "T" not in f.variables
+    with pytest.raises(Exception):
+        nc.nc_write_transforms_row(e, nj, None, w[0])
