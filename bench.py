@@ -40,14 +40,14 @@ import numpy as np  # noqa: E402
 
 METRIC = "local analyses/s (calc + update cycle)"
 
-# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per local
-# analysis of one ncu capture of each kernel on workload 2 at half edge
-# length (15,000 analyses): k_transforms_mixed 25.8 + 83.5 MB, k_update_cells
-# 305.0 + 162.0 MB.  Traffic grows with the analyses (and, for the update,
-# with the cells they cover), so a full launch scales by the analyses.
+# DRAM bytes per local analysis from one ncu capture of the current version
+# of a kernel on workload 2 at half edge length (15,000 analyses):
+# k_update_cells 462.6 MB (dram__bytes.sum.per_second x duration).  Traffic
+# grows with the analyses (and, for the update, with the cells they cover),
+# so a full launch scales by the analyses.  A kernel without a capture of
+# its current version reports no traffic.
 TRAFFIC_PER_ANALYSIS = {
-    (2, "k_transforms_mixed"): (25.85e6 + 83.54e6) / 15000,
-    (2, "k_update_cells"): (304.96e6 + 162.01e6) / 15000,
+    (2, "k_update_cells"): 462.6e6 / 15000,
 }
 UNIT = "analyses/s"
 
@@ -331,6 +331,8 @@ def run_gpu(args, rank, world, local_rank):
     roof["frac"] = roof["achieved"] / roof["peak"]
     tpa = TRAFFIC_PER_ANALYSIS.get((w.cfg, kname))
     roof["traffic"] = tpa * w.nanalyses if tpa else None
+    if tpa is None:
+        roof["traffic_note"] = "no ncu capture of this version of the kernel"
     roof["kernel_ms"] = kern_t * 1e3
     roof["finishing_kernels_ms"] = statistics.median(fin_ms)
     roof["flops_per_launch"] = flops
