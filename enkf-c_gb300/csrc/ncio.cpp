@@ -670,6 +670,50 @@ Var fixed_var(const char* nm, int type, std::initializer_list<int> dimids)
     return v;
 }
 
+// A float stored into an integer variable as NetCDF's put conversion does
+// it: a C conversion (truncation toward zero), with values outside the type's
+// range refused (NC_ERANGE, on which the reference's writer stops).
+bool pack_integer(float x, int t, uint64_t& out)
+{
+    if (x != x) return false;
+    switch (t) {
+    case T_BYTE:
+        if (x < -128.0f || x > 127.0f) return false;
+        out = (uint8_t)(int8_t)x;
+        return true;
+    case T_UBYTE:
+        if (x < 0.0f || x > 255.0f) return false;
+        out = (uint8_t)x;
+        return true;
+    case T_SHORT:
+        if (x < -32768.0f || x > 32767.0f) return false;
+        out = (uint16_t)(int16_t)x;
+        return true;
+    case T_USHORT:
+        if (x < 0.0f || x > 65535.0f) return false;
+        out = (uint16_t)x;
+        return true;
+    case T_INT:
+        if (x < -2147483648.0f || x >= 2147483648.0f) return false;
+        out = (uint32_t)(int32_t)x;
+        return true;
+    case T_UINT:
+        if (x < 0.0f || x >= 4294967296.0f) return false;
+        out = (uint32_t)x;
+        return true;
+    case T_INT64:
+        if (x < -9223372036854775808.0f || x >= 9223372036854775808.0f) return false;
+        out = (uint64_t)(int64_t)x;
+        return true;
+    case T_UINT64:
+        if (x < 0.0f || x >= 18446744073709551616.0f) return false;
+        out = (uint64_t)x;
+        return true;
+    default:
+        return false;
+    }
+}
+
 // The value rules of ncu_readfield / ncu_read3dfield (common/ncutils.c:
 // 300-530, 1015-1245): values equal to the fill value (the attribute, else
 // the type's default) or to missing_value, and values outside valid_min /
@@ -975,9 +1019,7 @@ static enkfg_status impl_write_layer(const char* path, const char* var, int k, i
     if (s) return s;
     const Var* V = var ? nc.var(var) : nullptr;
     if (!V) return fail(ENKFG_EINVAL, "%s: no variable \"%s\"", path, var ? var : "(null)");
-    if (V->type != T_FLOAT && V->type != T_DOUBLE)
-        return fail(ENKFG_EUNSUPPORTED, "%s: %s: only float and double variables are written (type %d)", path, var,
-                    V->type);
+    if (V->type == T_CHAR) return fail(ENKFG_EUNSUPPORTED, "%s: %s: a text variable", path, var);
     // the ncu_writefield dimension rules (common/ncutils.c:553-640): the last
     // record of a record variable, layer k otherwise
     const int nd = (int)V->dimids.size();
@@ -1056,11 +1098,17 @@ static enkfg_status impl_write_layer(const char* path, const char* var, int k, i
             uint32_t b;
             memcpy(&b, &x[q], 4);
             put_be(raw.data() + q * 4, b, 4);
-        } else {
+        } else if (V->type == T_DOUBLE) {
             const double d = (double)x[q];
             uint64_t b;
             memcpy(&b, &d, 8);
             put_be(raw.data() + q * 8, b, 8);
+        } else {
+            uint64_t b;
+            if (!pack_integer(x[q], V->type, b))
+                return fail(ENKFG_EINVAL, "%s: %s: value %g at %zu outside the range of the variable's type", path,
+                            var, (double)x[q], q);
+            put_be(raw.data() + q * ts, b, ts);
         }
     }
     return for_runs(nc, *V, start, count, [&](long long off, long long m, long long at) -> enkfg_status {

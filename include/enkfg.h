@@ -370,10 +370,11 @@ ENKFG_API enkfg_status enkfg_nc_read_layer(const char* path, const char* var, in
 ENKFG_API enkfg_status enkfg_nc_read_field3d(const char* path, const char* var, int r, int ni, int nj, int nk, float* v);
 
 /* ncu_writefield (common/ncutils.c:537-700) on a structured grid, into an
- * existing file: layer k (or the last record) of a float or double
- * variable; add_offset and scale_factor undone, values clamped to the valid
- * range, NaN written as the fill value (or missing_value).  Packed integer
- * variables are ENKFG_EUNSUPPORTED. */
+ * existing file: layer k (or the last record) of a numeric variable;
+ * add_offset and scale_factor undone, values clamped to the valid range, NaN
+ * written as the fill value (or missing_value), then stored in the
+ * variable's type (integers by truncation toward zero, as NetCDF's put
+ * conversion; a value outside the type's range is ENKFG_EINVAL). */
 ENKFG_API enkfg_status enkfg_nc_write_layer(const char* path, const char* var, int k, int ni, int nj, int nk, const float* v);
 
 #ifdef __cplusplus

@@ -207,15 +207,52 @@ def test_errors(nc, tmp_path):
     assert "not a NetCDF classic file" in str(ei.value)
     with pytest.raises(Exception):
         nc.nc_inq_var(tmp_path / "missing.nc", "x")
-    q = tmp_path / "packed.nc"
+    q = tmp_path / "text.nc"
     with netcdf_file(q, "w", version=1) as f:
         f.createDimension("j", 2)
         f.createDimension("i", 3)
-        v = f.createVariable("s", "i2", ("j", "i"))
-        v[:] = np.zeros((2, 3), np.int16)
+        v = f.createVariable("s", "c", ("j", "i"))
+        v[:] = np.full((2, 3), b"a")
     with pytest.raises(Exception) as ei:
         nc.nc_write_layer(q, "s", np.zeros((2, 3), np.float32))
     assert getattr(ei.value, "status", None) == 8
+
+
+def test_write_layer_packed(nc, tmp_path):
+    """Packed short and byte variables: offset and scale undone in float,
+    clamped, NaN to the fill value, then truncated toward zero."""
+    rng = np.random.default_rng(13)
+    nj, ni = 6, 7
+    p = tmp_path / "packed.nc"
+    with netcdf_file(p, "w", version=2) as f:
+        f.createDimension("j", nj)
+        f.createDimension("i", ni)
+        v = f.createVariable("salt", "i2", ("j", "i"))
+        v[:] = np.zeros((nj, ni), np.int16)
+        v.scale_factor = np.float32(0.001)
+        v.add_offset = np.float32(35.0)
+        v._FillValue = np.int16(-32767)
+        v.valid_range = np.array([-30000, 30000], np.int16)
+        v = f.createVariable("flag", "i1", ("j", "i"))
+        v[:] = np.zeros((nj, ni), np.int8)
+    a = rng.normal(35.0, 5.0, (nj, ni)).astype(np.float32)
+    a[0, 0] = np.nan
+    a[1, 1] = 80.0                                          # beyond valid_range: clamped
+    nc.nc_write_layer(p, "salt", a)
+    x = ((a - np.float32(35.0)) / np.float32(0.001)).astype(np.float32)
+    x = np.where(x < np.float32(-30000), np.float32(-30000), x)
+    x = np.where(x > np.float32(30000), np.float32(30000), x)
+    x[0, 0] = np.float32(-32767)
+    b = rng.uniform(-100.0, 100.0, (nj, ni)).astype(np.float32)
+    nc.nc_write_layer(p, "flag", b)
+    with netcdf_file(p, "r", mmap=False) as f:
+        assert np.array_equal(f.variables["salt"][:], np.trunc(x).astype(np.int16))
+        assert np.array_equal(f.variables["flag"][:], np.trunc(b).astype(np.int8))
+    # and back through the reader: the same values to the packing step
+    back = nc.nc_read_layer(p, "salt", ni, nj)
+    assert np.isnan(back[0, 0]) and np.abs(back[2:, :] - a[2:, :]).max() < 2e-3
+    with pytest.raises(Exception):
+        nc.nc_write_layer(p, "flag", np.full((nj, ni), 300.0, np.float32))
 
 
 def _cdf5(path, dims, variables, numrecs=0):
