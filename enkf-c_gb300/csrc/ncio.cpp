@@ -114,6 +114,25 @@ float to_float(const unsigned char* p, int t)
     }
 }
 
+// n values of native type t (big-endian) as floats; the float type, the
+// common case for model fields and transforms, is a byte swap
+void to_float_n(const unsigned char* raw, int t, size_t n, float* out)
+{
+#if defined(__BYTE_ORDER__) && __BYTE_ORDER__ == __ORDER_LITTLE_ENDIAN__
+    if (t == T_FLOAT) {
+        for (size_t q = 0; q < n; ++q) {
+            uint32_t b;
+            memcpy(&b, raw + q * 4, 4);
+            b = __builtin_bswap32(b);
+            memcpy(out + q, &b, 4);
+        }
+        return;
+    }
+#endif
+    const int ts = type_size(t);
+    for (size_t q = 0; q < n; ++q) out[q] = to_float(raw + q * ts, t);
+}
+
 struct Att {
     std::string name;
     int type = 0;
@@ -925,7 +944,7 @@ static enkfg_status impl_get_vara_float(const char* path, const char* var, const
     if ((s = read_raw(F.f, nc, *v, start, count, raw))) return s;
     const int ts = type_size(v->type);
     const size_t n = raw.size() / ts;
-    for (size_t q = 0; q < n; ++q) out[q] = to_float(raw.data() + q * ts, v->type);
+    to_float_n(raw.data(), v->type, n, out);
     return ENKFG_OK;
 }
 
@@ -946,7 +965,7 @@ static enkfg_status impl_read_layer(const char* path, const char* var, int r, in
     if ((s = read_raw(F.f, nc, *V, start, count, raw))) return s;
     const int t = V->type, ts = type_size(t);
     const size_t n = raw.size() / ts;
-    for (size_t q = 0; q < n; ++q) v[q] = to_float(raw.data() + q * ts, t);
+    to_float_n(raw.data(), t, n, v);
 
     apply_read_rules(*V, raw, v, false);
     return ENKFG_OK;
