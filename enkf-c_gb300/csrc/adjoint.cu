@@ -467,6 +467,7 @@ enkfg_status run_adjoint(enkfg_ctx* ctx, const enkfg_calc_params* p, const doubl
     a.mode = p->mode;
     a.scheme = p->scheme;
     a.alpha = p->alpha;
+    a.wait_ns = ctx->wait_ns;
     a.kc = 32;
     a.types = ctx->d_types;
     a.bstart = ctx->d_bstart;

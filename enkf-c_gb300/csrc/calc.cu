@@ -696,6 +696,7 @@ enkfg_status run_transforms(enkfg_ctx* ctx, const enkfg_calc_params* p, cudaStre
     a.scheme = p->scheme;
     a.want_diag = p->want_diag ? 1 : 0;
     a.alpha = p->alpha;
+    a.wait_ns = ctx->wait_ns;
     a.kc = 32;
     a.types = ctx->d_types;
     a.bstart = ctx->d_bstart;

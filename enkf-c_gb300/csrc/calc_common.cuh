@@ -17,6 +17,7 @@ struct CalcArgs {
     int npts, ntypes, ndim, m, md, mode, scheme, want_diag, persistent, kc;
     int nitems;        // queue length (npts, or a sample while autotuning)
     double alpha;
+    unsigned long long wait_ns;   // bound on a device wait (mixed path), ns
     const TypeIndex* types;
     const long long* bstart;
     const double* sx;

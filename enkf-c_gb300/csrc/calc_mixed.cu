@@ -41,8 +41,12 @@
 #include "calc_common.cuh"
 
 #define MX_ROWS 128
-#define MX_WAIT_NS 2000000000ull   // 2 s bound on any wait for the tensor cores
-#define MX_TIMEOUT_CODE 99
+// Bound on a wait for the tensor cores: the context's limit (a.wait_ns,
+// enkfg_set_wait_limit, 2 s by default) for the first wait; after it expires
+// the drain before TMEM is released waits at most MX_WAIT_NS, whatever the
+// limit, so that no MMA is in flight when its TMEM is freed.
+#define MX_WAIT_NS ENKFG_DEFAULT_WAIT_NS
+#define MX_TIMEOUT_CODE ENKFG_POINT_TIMEOUT
 
 namespace tc {
 
@@ -137,15 +141,15 @@ __device__ __forceinline__ uint64_t now_ns()
     return t;
 }
 
-// wait for phase `parity` of the mbarrier, at most MX_WAIT_NS; true if it
+// wait for phase `parity` of the mbarrier, at most limit_ns; true if it
 // completed (the clock is read only when the first try fails)
-__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* mbar, uint32_t parity)
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* mbar, uint32_t parity, uint64_t limit_ns)
 {
     if (mbar_try_wait(mbar, parity)) return true;
     const uint64_t t0 = now_ns();
     for (;;) {
         if (mbar_try_wait(mbar, parity)) return true;
-        if (now_ns() - t0 > MX_WAIT_NS) return false;
+        if (now_ns() - t0 > limit_ns) return false;
     }
 }
 
@@ -331,10 +335,10 @@ struct GramProcTC {
     __device__ __forceinline__ void wait_buf(int buf, bool sync = true)
     {
         if (sy.outstanding(buf)) {
-            bool done = tc::mbar_wait_bounded(ms.mbar + buf, sy.parity(buf));
+            bool done = tc::mbar_wait_bounded(ms.mbar + buf, sy.parity(buf), a.wait_ns);
             if (!done) {
                 atomicExch(ms.err, 1);
-                tc::mbar_wait_bounded(ms.mbar + buf, sy.parity(buf));
+                tc::mbar_wait_bounded(ms.mbar + buf, sy.parity(buf), MX_WAIT_NS);
             }
             sy.completed(buf);
         }
@@ -600,10 +604,10 @@ struct GramProcTC {
         //    here, and for this thread's copies of the next round's rows,
         //    under the round's closing barrier
         if (sy.outstanding(buf ^ 1)) {
-            bool done = tc::mbar_wait_bounded(ms.mbar + (buf ^ 1), sy.parity(buf ^ 1));
+            bool done = tc::mbar_wait_bounded(ms.mbar + (buf ^ 1), sy.parity(buf ^ 1), a.wait_ns);
             if (!done) {
                 atomicExch(ms.err, 1);
-                tc::mbar_wait_bounded(ms.mbar + (buf ^ 1), sy.parity(buf ^ 1));
+                tc::mbar_wait_bounded(ms.mbar + (buf ^ 1), sy.parity(buf ^ 1), MX_WAIT_NS);
             }
             sy.completed(buf ^ 1);
             tc::fence_after();

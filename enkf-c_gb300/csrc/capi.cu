@@ -65,6 +65,13 @@ ENKFG_API const char* enkfg_last_error(const enkfg_ctx* ctx)
     return ctx ? ctx->err : "no context";
 }
 
+ENKFG_API enkfg_status enkfg_set_wait_limit(enkfg_ctx* ctx, unsigned long long ns)
+{
+    if (!ctx) return ENKFG_EINVAL;
+    ctx->wait_ns = ns ? ns : ENKFG_DEFAULT_WAIT_NS;
+    return ENKFG_OK;
+}
+
 ENKFG_API enkfg_status enkfg_create(int device, enkfg_ctx** out)
 {
     if (!out) return ENKFG_EINVAL;
@@ -79,6 +86,7 @@ ENKFG_API enkfg_status enkfg_create(int device, enkfg_ctx** out)
     enkfg_ctx* ctx = (enkfg_ctx*)calloc(1, sizeof(enkfg_ctx));
     if (!ctx) return ENKFG_ENOMEM;
     ctx->device = device;
+    ctx->wait_ns = ENKFG_DEFAULT_WAIT_NS;
     if (cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess) {
         free(ctx);
         return ENKFG_ECUDA;
@@ -599,6 +607,13 @@ static enkfg_status finish_calc(enkfg_ctx* ctx, cudaStream_t st)
     int* h = (int*)malloc(npts * sizeof(int));
     if (!h) return ENKFG_ENOMEM;
     CK(cudaMemcpy(h, ctx->d_status_pt, npts * sizeof(int), cudaMemcpyDeviceToHost));
+    for (int k = 0; k < npts; ++k)
+        if (h[k] == ENKFG_POINT_TIMEOUT) {
+            set_err(ctx, "local analysis (j=%d, i=%d): a device wait exceeded its limit (%llu ns)", k / ctx->ni,
+                    k % ctx->ni, ctx->wait_ns);
+            free(h);
+            return ENKFG_ETIMEOUT;
+        }
     for (int k = 0; k < npts; ++k)
         if (h[k]) {
             set_err(ctx, "local analysis (j=%d, i=%d): factorisation failed (code %d)", k / ctx->ni, k % ctx->ni, h[k]);

@@ -65,10 +65,12 @@ static double dkey_inv(unsigned long long k)
     return d;
 }
 
-// box[t*6 + 2*axis + 0] = min key, + 1 = max key (as max of keys).  A thread
-// keeps the running bounds of a run of observations of one type (a grid-
-// stride sweep) and flushes them to the block's shared copy when the type
-// changes; each block then merges into the global box once per entry.
+// Per type: the bounding box of the valid observations as ordered keys
+// (box[t*6 + 2a] min, box[t*6 + 2a + 1] max of axis a) and their number
+// (box[ntypes*6 + t]).  A thread keeps the running bounds and count of a run
+// of observations of one type (a grid-stride sweep) and flushes them to the
+// block's shared copy when the type changes; each block then merges into the
+// global box once per entry.
 #define BBOX_T 256
 __global__ void __launch_bounds__(BBOX_T) k_bbox(int nobs, int ndim, int ntypes, const double* __restrict__ ox,
                                                  const double* __restrict__ oy, const double* __restrict__ oz,
@@ -76,9 +78,12 @@ __global__ void __launch_bounds__(BBOX_T) k_bbox(int nobs, int ndim, int ntypes,
                                                  unsigned long long* __restrict__ box)
 {
     __shared__ unsigned long long sb[ENKFG_MAXTYPES * 6];
+    __shared__ unsigned long long sn[ENKFG_MAXTYPES];
     for (int i = threadIdx.x; i < ntypes * 6; i += BBOX_T) sb[i] = (i & 1) ? 0ull : ~0ull;
+    for (int i = threadIdx.x; i < ntypes; i += BBOX_T) sn[i] = 0ull;
     __syncthreads();
     int cur = -1;
+    unsigned long long cnt = 0;
     unsigned long long lo[3] = { ~0ull, ~0ull, ~0ull }, hi[3] = { 0ull, 0ull, 0ull };
     auto flush = [&]() {
         if (cur < 0) return;
@@ -88,6 +93,8 @@ __global__ void __launch_bounds__(BBOX_T) k_bbox(int nobs, int ndim, int ntypes,
             lo[a] = ~0ull;
             hi[a] = 0ull;
         }
+        atomicAdd(&sn[cur], cnt);
+        cnt = 0;
     };
     for (int o = blockIdx.x * BBOX_T + threadIdx.x; o < nobs; o += gridDim.x * BBOX_T) {
         if (status[o] != 0) continue;
@@ -96,6 +103,7 @@ __global__ void __launch_bounds__(BBOX_T) k_bbox(int nobs, int ndim, int ntypes,
             flush();
             cur = t;
         }
+        ++cnt;
         const double v[3] = { ox[o], oy[o], ndim == 3 ? oz[o] : 0.0 };
         for (int a = 0; a < ndim; ++a) {
             const unsigned long long k = dkey(v[a]);
@@ -112,6 +120,8 @@ __global__ void __launch_bounds__(BBOX_T) k_bbox(int nobs, int ndim, int ntypes,
             atomicMin(&box[i], sb[i]);
         }
     }
+    for (int i = threadIdx.x; i < ntypes; i += BBOX_T)
+        if (sn[i] != 0ull) atomicAdd(&box[ntypes * 6 + i], sn[i]);
 }
 
 __global__ void k_keys(int nobs, int ndim, const double* __restrict__ ox, const double* __restrict__ oy,
@@ -373,27 +383,29 @@ enkfg_status scan_counts(enkfg_ctx* ctx, const int* d_in, long long* d_out, long
 enkfg_status build_index(enkfg_ctx* ctx, cudaStream_t st)
 {
     int nobs = ctx->nobs, ntypes = ctx->ntypes, ndim = ctx->geographic ? 3 : 2;
-    size_t cap;
     enkfg_status s;
 
     // bounding boxes
     unsigned long long* d_box;
-    CK(cudaMalloc(&d_box, (size_t)ntypes * 6 * sizeof(unsigned long long)));
+    const size_t box_bytes = (size_t)ntypes * 7 * sizeof(unsigned long long);
+    CK(cudaMalloc(&d_box, box_bytes));
     {
-        unsigned long long* h = (unsigned long long*)malloc(ntypes * 6 * sizeof(unsigned long long));
-        for (int t = 0; t < ntypes; ++t)
+        unsigned long long* h = (unsigned long long*)malloc(box_bytes);
+        for (int t = 0; t < ntypes; ++t) {
             for (int a = 0; a < 3; ++a) {
                 h[t * 6 + 2 * a] = ~0ull;
                 h[t * 6 + 2 * a + 1] = 0ull;
             }
-        cudaMemcpyAsync(d_box, h, ntypes * 6 * sizeof(unsigned long long), cudaMemcpyHostToDevice, st);
+            h[ntypes * 6 + t] = 0ull;
+        }
+        cudaMemcpyAsync(d_box, h, box_bytes, cudaMemcpyHostToDevice, st);
         if (nobs > 0) {
             const int nb = div_up(nobs, BBOX_T * 8) < 2 * 152 ? div_up(nobs, BBOX_T * 8) : 2 * 152;
             k_bbox<<<nb, BBOX_T, 0, st>>>(nobs, ndim, ntypes, ctx->d_ox, ctx->d_oy, ctx->d_oz, ctx->d_type,
                                           ctx->d_status, d_box);
             ctx->launches++;
         }
-        cudaMemcpyAsync(h, d_box, ntypes * 6 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, st);
+        cudaMemcpyAsync(h, d_box, box_bytes, cudaMemcpyDeviceToHost, st);
         cudaError_t e = cudaStreamSynchronize(st);
         cudaFree(d_box);
         if (e != cudaSuccess) {
@@ -433,10 +445,18 @@ enkfg_status build_index(enkfg_ctx* ctx, cudaStream_t st)
                 }
             // cell edge: at least the radius (slightly enlarged so that
             // rounding in the cell arithmetic cannot skip a neighbour cell),
-            // and at most 4096 cells per axis
+            // and no more cells per axis than 4000 (2-D) / 1000 (3-D) or
+            // than the type's observation count allows: about 4 cells per
+            // observation in 2-D and one per two in 3-D, so that the bucket
+            // table (a power of two per axis) stays within a small multiple
+            // of the observations however small the radius is against the
+            // extent (a sphere's bounding cube is mostly empty)
             double ext = 0.0;
             for (int a = 0; a < ndim; ++a) ext = fmax(ext, hi[a] - lo[a]);
-            double cell = fmax(rmax * (1.0 + 1e-9), ext / (ndim == 2 ? 4000.0 : 1000.0));
+            const double nt = (double)(h[ntypes * 6 + t] > 0 ? h[ntypes * 6 + t] : 1);
+            double axis = ndim == 2 ? fmin(4000.0, floor(sqrt(4.0 * nt))) : fmin(1000.0, floor(cbrt(0.5 * nt)));
+            if (axis < 1.0) axis = 1.0;
+            double cell = fmax(rmax * (1.0 + 1e-9), ext / axis);
             if (!(cell > 0.0)) cell = 1.0;
             ti.inv_cell = 1.0 / cell;
             ti.x0 = lo[0];
@@ -461,7 +481,6 @@ enkfg_status build_index(enkfg_ctx* ctx, cudaStream_t st)
         set_err(ctx, "spatial index too large (%lld buckets)", ctx->nbuckets);
         return ENKFG_ECAPACITY;
     }
-    cap = 0;
     if (ctx->d_types == nullptr) CK(cudaMalloc(&ctx->d_types, sizeof(TypeIndex) * ENKFG_MAXTYPES));
     CK(cudaMemcpyAsync(ctx->d_types, ctx->h_types, sizeof(TypeIndex) * ntypes, cudaMemcpyHostToDevice, st));
 

@@ -9,6 +9,11 @@
 
 #define ENKFG_VERSION 1
 
+// default bound on a device wait (mixed path: waits for the tensor cores)
+#define ENKFG_DEFAULT_WAIT_NS 2000000000ull
+// per-point status a transform kernel records when a bounded wait expired
+#define ENKFG_POINT_TIMEOUT 99
+
 // ---------------------------------------------------------------------------
 // Per-type spatial index description (device copy lives in ctx->d_types).
 // The observations of one type are bucketed on a uniform grid of cells of
@@ -45,6 +50,7 @@ struct enkfg_ctx {
     cudaStream_t own_stream;    // the context's own stream while a caller stream is bound
     char err[1024];
     long long launches;
+    unsigned long long wait_ns; // bound on a device wait (enkfg_set_wait_limit)
     float stage_ms[4];
     cudaEvent_t ev[10];         // [8, 9]: the transform kernel alone (first batch)
 

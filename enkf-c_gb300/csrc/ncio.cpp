@@ -175,11 +175,15 @@ struct NcFile {
         const Dim& D = dims[v.dimids[d]];
         return D.len == 0 ? numrecs : D.len;
     }
-    // bytes of one record (record variables) or of the whole variable, unpadded
+    // bytes of one record (record variables) or of the whole variable,
+    // unpadded; -1 if a length is negative or the product overflows
     long long data_bytes(const Var& v) const
     {
         long long n = type_size(v.type);
-        for (size_t d = is_rec(v) ? 1 : 0; d < v.dimids.size(); ++d) n *= dims[v.dimids[d]].len;
+        for (size_t d = is_rec(v) ? 1 : 0; d < v.dimids.size(); ++d) {
+            const long long len = dims[v.dimids[d]].len;
+            if (len < 0 || __builtin_mul_overflow(n, len, &n) || n > (1LL << 62)) return -1;
+        }
         return n;
     }
     const Var* var(const char* nm) const
@@ -188,19 +192,24 @@ struct NcFile {
             if (v.name == nm) return &v;
         return nullptr;
     }
-    void layout_records()
+    // the record size; false if a variable's size is negative or overflows
+    bool layout_records()
     {
         int nrec = 0;
         recsize = 0;
-        for (const Var& v : vars)
+        for (const Var& v : vars) {
+            const long long b = data_bytes(v);
+            if (b < 0) return false;
             if (is_rec(v)) {
                 ++nrec;
-                recsize += pad4(data_bytes(v));
+                if (__builtin_add_overflow(recsize, pad4(b), &recsize) || recsize > (1LL << 62)) return false;
             }
+        }
         // a single record variable is not padded (classic format rule)
         if (nrec == 1)
             for (const Var& v : vars)
                 if (is_rec(v)) recsize = data_bytes(v);
+        return true;
     }
 };
 
@@ -222,7 +231,7 @@ struct Cursor {
     }
     bool bytes(long long k, std::vector<unsigned char>& out)
     {
-        if (k < 0 || at + (size_t)pad4(k) > n) return ok = false;
+        if (k < 0 || k > (long long)(n - at) || at + (size_t)pad4(k) > n) return ok = false;
         out.assign(p + at, p + at + k);
         at += pad4(k);
         return true;
@@ -271,6 +280,9 @@ enkfg_status parse_header(FILE* f, const char* path, NcFile& nc)
                 a.type = (int)c.take(4);
                 a.n = (long long)c.take(nn);
                 if (!c.ok || type_size(a.type) == 0) return c.ok = false;
+                // the count is checked against the header bytes left before
+                // it is multiplied by the type size
+                if (a.n < 0 || a.n > (long long)(c.n - c.at) / type_size(a.type)) return c.ok = false;
                 if (!c.bytes(a.n * type_size(a.type), a.raw)) return false;
                 out.push_back(std::move(a));
             }
@@ -285,6 +297,7 @@ enkfg_status parse_header(FILE* f, const char* path, NcFile& nc)
                 Dim d;
                 if (!name(d.name)) break;
                 d.len = (long long)c.take(nn);
+                if (d.len < 0) c.ok = false;
                 nc.dims.push_back(d);
             }
         }
@@ -308,13 +321,19 @@ enkfg_status parse_header(FILE* f, const char* path, NcFile& nc)
                     v.type = (int)c.take(4);
                     v.vsize = (long long)c.take(nn);
                     v.begin = (long long)c.take(ob);
-                    if (type_size(v.type) == 0) c.ok = false;
+                    if (type_size(v.type) == 0 || v.vsize < 0 || v.begin < 0) c.ok = false;
                     nc.vars.push_back(std::move(v));
                 }
             }
         }
         if (c.ok) {
-            nc.layout_records();
+            if (!nc.layout_records())
+                return fail(ENKFG_EINVAL, "%s: a variable's size in the NetCDF header overflows", path);
+            for (const Var& v : nc.vars) {
+                long long end;
+                if (__builtin_add_overflow(v.begin, nc.data_bytes(v), &end))
+                    return fail(ENKFG_EINVAL, "%s: a variable's offset in the NetCDF header overflows", path);
+            }
             if (streaming) {
                 // numrecs not yet written: count the complete records on disk
                 long long first = -1;

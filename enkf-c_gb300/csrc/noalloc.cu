@@ -11,30 +11,96 @@
 // offsets with the block sums in the fixed array below instead.
 //
 // The array is a file-scope __device__ object: every GPU that loads this
-// library keeps it (512 KiB) until the process exits.  Host
-// code cannot use the array's name as a device address, so the address is
-// looked up once per device with cudaGetSymbolAddress, on the first call
-// made with that device current; that first call should therefore be made
-// before any stream capture.  All calls share the array: calls that overlap
-// on the GPU (different streams, or different host threads on the same
-// device) race on it and must be serialised by the caller.  The array keeps
-// the previous call's block sums; nothing in it needs to start at zero,
-// because each call writes every entry it reads (its nb block sums, then
-// their nb + 1 offsets) before reading it.
+// library keeps it (512 KiB) until the process exits.  Host code cannot use
+// the array's name as a device address; the address comes from
+// cudaGetSymbolAddress, called with the caller's device (context) current.
+// Outside stream capture every call looks the address up again (a symbol
+// lookup, no allocation), so a device reset, which reloads the module, or a
+// caller's own driver-API context on the same device, where the array has
+// another address, always gets the right one.  The address is also recorded
+// per CUDA context, and a call made while `stream` is being captured uses the
+// recorded one: the first call in a context must therefore come before any
+// capture in it (otherwise ENKFG_ESTATE), and after a device reset one
+// uncaptured call must come before the next capture.  All calls share the
+// array: calls that overlap on the GPU (different streams, or different host
+// threads on the same device) race on it and must be serialised by the
+// caller.  The array keeps the previous call's block sums; nothing in it
+// needs to start at zero, because each call writes every entry it reads (its
+// nb block sums, then their nb + 1 offsets) before reading it.
 #include "internal.cuh"
+#include <cuda.h>
 #include <mutex>
 
 #define NA_T 1024
 #define NA_IPT 4
 #define NA_PER (NA_T * NA_IPT)                   // counts per scan block
 #define NA_MAX_BLOCKS 32768                      // -> at most 134,217,728 counts
-#define NA_MAX_DEVICES 64
+#define NA_MAX_CONTEXTS 64
 
 // block sums [NA_MAX_BLOCKS] followed by their exclusive scan [NA_MAX_BLOCKS + 1]
 static __device__ __align__(256) long long g_noalloc_scratch[2 * NA_MAX_BLOCKS + 2];
 
 static std::mutex g_noalloc_mu;
-static long long* g_noalloc_ptr[NA_MAX_DEVICES];
+// the scratch array's address in each CUDA context seen so far
+struct NaContextAddr {
+    CUcontext cx;
+    long long* ptr;
+};
+static NaContextAddr g_noalloc_addr[NA_MAX_CONTEXTS];
+static int g_noalloc_naddr = 0;
+typedef CUresult (*NaCtxGetCurrent)(CUcontext*);
+static NaCtxGetCurrent g_ctx_get_current = nullptr;
+
+// The scratch array's address in the current context (see the file comment).
+static enkfg_status noalloc_scratch(cudaStream_t st, long long** out)
+{
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(st, &cs) != cudaSuccess) {
+        cudaGetLastError();
+        return ENKFG_ECUDA;
+    }
+    std::lock_guard<std::mutex> lock(g_noalloc_mu);
+    if (g_ctx_get_current == nullptr) {
+        if (cs != cudaStreamCaptureStatusNone) return ENKFG_ESTATE;
+        void* fn = nullptr;
+        cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &fn, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+            q != cudaDriverEntryPointSuccess || fn == nullptr) {
+            cudaGetLastError();
+            return ENKFG_ECUDA;
+        }
+        g_ctx_get_current = (NaCtxGetCurrent)fn;
+    }
+    void* p = nullptr;
+    if (cs == cudaStreamCaptureStatusNone) {
+        // this also makes the device's primary context current if the
+        // caller has not touched the device yet
+        if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || p == nullptr) {
+            cudaGetLastError();
+            return ENKFG_ECUDA;
+        }
+    }
+    CUcontext cx = nullptr;
+    if (g_ctx_get_current(&cx) != CUDA_SUCCESS || cx == nullptr) return ENKFG_ECUDA;
+    int k = 0;
+    while (k < g_noalloc_naddr && g_noalloc_addr[k].cx != cx) ++k;
+    if (cs != cudaStreamCaptureStatusNone) {
+        if (k == g_noalloc_naddr) return ENKFG_ESTATE;   // no uncaptured call in this context yet
+        *out = g_noalloc_addr[k].ptr;
+        return ENKFG_OK;
+    }
+    if (k == g_noalloc_naddr) {
+        if (g_noalloc_naddr < NA_MAX_CONTEXTS) {
+            ++g_noalloc_naddr;
+        } else {
+            k = NA_MAX_CONTEXTS - 1;   // table full: the newest entry is replaced
+        }
+        g_noalloc_addr[k].cx = cx;
+    }
+    g_noalloc_addr[k].ptr = (long long*)p;
+    *out = (long long*)p;
+    return ENKFG_OK;
+}
 
 __global__ void k_na_scan_block(const int* __restrict__ in, long long n, long long* __restrict__ out,
                                 long long* __restrict__ bsum)
@@ -122,26 +188,10 @@ extern "C" ENKFG_API enkfg_status enkfg_local_offsets_noalloc(const int* counts_
 {
     if ((counts_dev == nullptr && n > 0) || offsets_dev == nullptr || n < 0) return ENKFG_EINVAL;
     if (n > (long long)NA_MAX_BLOCKS * NA_PER) return ENKFG_ECAPACITY;
-    int dev = 0;
-    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= NA_MAX_DEVICES) {
-        cudaGetLastError();
-        return ENKFG_ECUDA;
-    }
-    long long* scratch;
-    {
-        // set-up, once per device: the device address of the scratch array
-        std::lock_guard<std::mutex> lock(g_noalloc_mu);
-        if (g_noalloc_ptr[dev] == nullptr) {
-            void* p = nullptr;
-            if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || p == nullptr) {
-                cudaGetLastError();
-                return ENKFG_ECUDA;
-            }
-            g_noalloc_ptr[dev] = (long long*)p;
-        }
-        scratch = g_noalloc_ptr[dev];
-    }
     cudaStream_t st = (cudaStream_t)stream;
+    long long* scratch = nullptr;
+    enkfg_status s0 = noalloc_scratch(st, &scratch);
+    if (s0 != ENKFG_OK) return s0;
     int nb = (int)((n + NA_PER - 1) / NA_PER);
     if (nb < 1) nb = 1;
     long long* bsum = scratch;                 // fully written by k_na_scan_block

@@ -36,21 +36,80 @@ def _rng(cfg: int, stream: int) -> np.random.Generator:
     return np.random.default_rng(cfg * 1000 + stream)
 
 
-def grf(rng: np.random.Generator, nj: int, ni: int, length: float, std: float = 1.0,
-        count: int = 1) -> np.ndarray:
-    """`count` independent Gaussian random fields [count][nj][ni] (float32)."""
+def _fft_workers() -> int:
+    import os
+    return max(1, os.cpu_count() or 1)
+
+
+def grf_filter(noise: np.ndarray, length: float, std: float = 1.0) -> np.ndarray:
+    """Gaussian random fields from white noise [count][nj][ni] (float32): the
+    noise filtered in Fourier space by a Gaussian kernel of the given length
+    scale, each field centred and scaled to `std`."""
+    import scipy.fft as sfft
+    count, nj, ni = noise.shape
     ky = np.fft.fftfreq(nj)[:, None]
     kx = np.fft.rfftfreq(ni)[None, :]
     # Gaussian covariance exp(-r^2 / (2 L^2)) <-> amplitude filter exp(-pi^2 k^2 L^2)
     filt = np.exp(-(np.pi ** 2) * (kx ** 2 + ky ** 2) * length ** 2).astype(np.float32)
+    wk = _fft_workers()
     out = np.empty((count, nj, ni), np.float32)
-    for c in range(count):
-        noise = rng.standard_normal((nj, ni), dtype=np.float32)
-        f = np.fft.irfft2(np.fft.rfft2(noise) * filt, s=(nj, ni)).astype(np.float32)
-        f -= f.mean()
-        f *= std / max(float(f.std()), 1e-30)
-        out[c] = f
+    step = 16
+    for c0 in range(0, count, step):
+        spec = sfft.rfft2(noise[c0:c0 + step], workers=wk)
+        spec *= filt
+        f = sfft.irfft2(spec, s=(nj, ni), workers=wk).astype(np.float32)
+        f -= f.mean(axis=(1, 2), keepdims=True)
+        sd = np.sqrt(np.einsum("kij,kij->k", f, f, dtype=np.float64) / (nj * ni))
+        f *= (std / np.maximum(sd, 1e-30)).astype(np.float32)[:, None, None]
+        out[c0:c0 + step] = f
     return out
+
+
+def grf(rng: np.random.Generator, nj: int, ni: int, length: float, std: float = 1.0,
+        count: int = 1) -> np.ndarray:
+    """`count` independent Gaussian random fields [count][nj][ni] (float32)."""
+    noise = rng.standard_normal((count, nj, ni), dtype=np.float32)
+    return grf_filter(noise, length, std)
+
+
+def _layer_noise(cfg: int, stream: int, f: int, k: int, count: int, nj: int, ni: int, ex=None) -> np.ndarray:
+    """White noise of layer k of field f: every member draws from its own
+    seeded generator (config * 1000 + stream, field, layer, member), so the
+    values do not depend on how the draws are spread over threads."""
+    out = np.empty((count, nj, ni), np.float32)
+
+    def draw(e):
+        np.random.default_rng([cfg * 1000 + stream, f, k, e]).standard_normal((nj, ni), dtype=np.float32,
+                                                                               out=out[e])
+    if ex is None:
+        for e in range(count):
+            draw(e)
+    else:
+        list(ex.map(draw, range(count)))
+    return out
+
+
+def ensemble_layers(cfg: int, nf: int, nl: int, m: int, md: int, nj: int, ni: int, length: float,
+                    bg: float = 15.0):
+    """Yield (f, k, layer [m][nj][ni]) of the ensemble in field, layer order.
+    Layer k of a field is 0.8 layer k-1 + 0.6 new (inter-layer correlation
+    0.8); static members (md..m-1, hybrid) are 0.7 x one field-level draw."""
+    import concurrent.futures as cf
+    with cf.ThreadPoolExecutor(max_workers=_fft_workers()) as ex:
+        for f in range(nf):
+            static = None
+            if md < m:
+                static = grf_filter(_layer_noise(cfg, 6, f, 0, m - md, nj, ni, ex), length) * np.float32(0.7)
+            prev = None
+            for k in range(nl):
+                new = grf_filter(_layer_noise(cfg, 0, f, k, m, nj, ni, ex), length)
+                lay = new if prev is None else (np.float32(0.8) * prev + np.float32(0.6) * new)
+                prev = lay
+                out = lay.copy()
+                if static is not None:
+                    out[md:] = static
+                out += np.float32(bg)
+                yield f, k, out
 
 
 def bilinear(field: np.ndarray, x: np.ndarray, y: np.ndarray) -> np.ndarray:
@@ -244,26 +303,15 @@ def make(cfg: int, *, scale: float = 1.0, nobs: Optional[int] = None, with_field
     status = np.zeros(lon.size, np.int16)
 
     # ensemble (observed field = field 0, layer 0) and truth
-    re = _rng(cfg, 0)
     bg = 15.0
     fields = None
     if with_fields:
         fields = np.empty((nf, nl, m, nj, ni), np.float32)
-        for f in range(nf):
-            prev = None
-            for k in range(nl):
-                new = grf(re, nj, ni, L, 1.0, count=m)
-                lay = new if prev is None else (0.8 * prev + 0.6 * new).astype(np.float32)
-                fields[f, k] = lay
-                prev = lay
-        if cfg == 5 and md < m:
-            rs = _rng(cfg, 6)
-            for f in range(nf):
-                fields[f, :, md:] = grf(rs, nj, ni, L, 1.0, count=m - md)[None] * 0.7
-        fields += bg
+        for f, k, lay in ensemble_layers(cfg, nf, nl, m, md, nj, ni, L, bg):
+            fields[f, k] = lay
         obs_member = fields[0, 0]
     else:
-        obs_member = grf(re, nj, ni, L, 1.0, count=m) + bg
+        obs_member = next(ensemble_layers(cfg, 1, 1, m, md, nj, ni, L, bg))[2]
     truth = grf(_rng(cfg, 1), nj, ni, L, 1.0)[0] + bg
     noise = _rng(cfg, 3).standard_normal(lon.size).astype(np.float32)
     value = (bilinear(truth, lon, lat) + estd * noise).astype(np.float32)

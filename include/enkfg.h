@@ -62,6 +62,15 @@ typedef struct enkfg_ctx enkfg_ctx;
  * in dasystem/observations (dasystem.h:60-128) for the hot path. */
 ENKFG_API enkfg_status enkfg_create(int device, enkfg_ctx** ctx);
 ENKFG_API void enkfg_destroy(enkfg_ctx* ctx);
+
+/* Bound on each device wait of this context, in nanoseconds (0: the default,
+ * 2 s).  No counterpart in the reference, which has no device waits: the
+ * mixed-precision transform kernel waits on mbarriers for its tensor-core
+ * MMAs; a wait that exceeds the bound makes the point's status a timeout,
+ * the kernel drains its MMAs (at most 2 s more) and releases its tensor
+ * memory, and enkfg_calc_transforms returns ENKFG_ETIMEOUT.  The context
+ * stays usable. */
+ENKFG_API enkfg_status enkfg_set_wait_limit(enkfg_ctx* ctx, unsigned long long ns);
 ENKFG_API const char* enkfg_last_error(const enkfg_ctx* ctx);
 ENKFG_API const char* enkfg_status_string(enkfg_status st);
 ENKFG_API int enkfg_version(void);
@@ -306,9 +315,12 @@ ENKFG_API enkfg_status enkfg_kernel_times(const enkfg_ctx* ctx, float* ms2);
  * the caller's device buffers, and the scan's block sums live in a fixed
  * 512 KiB array inside the library that every GPU using the library keeps
  * until the process exits.  Limit: n <= 134,217,728 (32768 scan blocks of
- * 4096 counts), else ENKFG_ECAPACITY.  The first call on a device looks up
- * the array's device address (cudaGetSymbolAddress) with that device
- * current, so make it before any stream capture.  All calls share the
+ * 4096 counts), else ENKFG_ECAPACITY.  Outside stream capture each call
+ * looks up the array's device address in the current CUDA context
+ * (cudaGetSymbolAddress; a lookup, no allocation) and records it for that
+ * context; a call made while `stream` is being captured uses the recorded
+ * address, so the first call in a context, and the first after a device
+ * reset, must come before any capture (else ENKFG_ESTATE).  All calls share the
  * array: calls that overlap on the GPU race and must be serialised by the
  * caller.  counts_dev may be NULL when n = 0.  Work is queued on `stream`
  * (NULL: the legacy default stream). */

@@ -9,6 +9,12 @@ leg of the benchmark import it; the product never does.
   _ref/libenkf_ref.so the reference's own calc/calcs.c + common/kdtree.c,
                      compiled unmodified by oracle/ref/Makefile where the
                      reference sources exist; used to pin the restatement.
+  _ref/libenkf_ref_update.so  the reference's update/update.c (field update,
+                     background update) and common/dasystem.c (hybrid
+                     ensemble), compiled unmodified the same way.
+
+The reference tree is ENKFG_REFERENCE_DIR when set, else the default of
+oracle/ref/Makefile.
 """
 from __future__ import annotations
 
@@ -24,7 +30,6 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB = os.path.join(HERE, "liboracle.so")
 REFLIB = os.path.join(HERE, "_ref", "libenkf_ref.so")
-REFDIR = "/root/reference/enkf"
 MAXLOCRAD = 8
 
 _lock = threading.Lock()
@@ -50,13 +55,25 @@ def blas_path() -> str:
     return os.path.realpath(cands[0])
 
 
+def refdir() -> str:
+    """The reference tree: ENKFG_REFERENCE_DIR, else the reference build
+    recipe's default (oracle/ref/Makefile)."""
+    d = os.environ.get("ENKFG_REFERENCE_DIR")
+    if d:
+        return d
+    r = subprocess.run(["make", "-s", "--no-print-directory", "print-refdir"], cwd=os.path.join(HERE, "ref"),
+                       capture_output=True, text=True)
+    return r.stdout.strip()
+
+
 def build(force: bool = False) -> str:
     """Compile liboracle.so in place (and _ref when the reference is present)."""
     if force or not os.path.exists(LIB) or os.path.getmtime(LIB) < max(
             os.path.getmtime(os.path.join(HERE, f)) for f in ("enkf_oracle.c", "or_blas.c", "enkf_oracle.h")):
         subprocess.run(["make", "-s", "-B" if force else "all"], cwd=HERE, check=True)
-    if os.path.isdir(REFDIR):
-        subprocess.run(["make", "-s", "REFDIR=" + REFDIR], cwd=os.path.join(HERE, "ref"), check=True)
+    rd = refdir()
+    if rd and os.path.isdir(rd):
+        subprocess.run(["make", "-s", "REFDIR=" + rd], cwd=os.path.join(HERE, "ref"), check=True)
     return LIB
 
 
@@ -504,3 +521,68 @@ def finish_HE(HE, status, *, mode, nmem_dynamic, gamma=0.0, Hx=None, skip_bad=Fa
     nbad = lib().or_finish_HE(C.c_int(mode), C.c_int(m), C.c_int(nmem_dynamic), C.c_double(gamma), C.c_int(n),
                               _p(S, C.c_float), _p(hx, C.c_float), C.c_int(int(skip_bad)), _p(st, C.c_short))
     return S, st, nbad
+
+
+# ---------------------------------------------------------------------------
+# the reference's own field update (update/update.c) and hybrid ensemble
+# (common/dasystem.c), compiled unmodified (oracle/ref/ref_update.c)
+# ---------------------------------------------------------------------------
+
+REFLIB_UPDATE = os.path.join(HERE, "_ref", "libenkf_ref_update.so")
+_refup = None
+
+
+def reflib_update():
+    """libenkf_ref_update.so, or None where it is not built."""
+    global _refup
+    with _lock:
+        if _refup is None and os.path.exists(REFLIB_UPDATE):
+            L = C.CDLL(REFLIB_UPDATE)
+            if L.or_blas_load(blas_path().encode()) != 0:
+                return None
+            L.ref_update_layer.argtypes = [C.c_int] * 12 + [C.c_float, C.c_double, C.c_int, C.c_int] + \
+                [C.c_void_p] * 4
+            L.ref_sethybridensemble.argtypes = [C.c_int, C.c_int, C.c_double, C.c_int, C.c_void_p]
+            _refup = L
+    return _refup
+
+
+def ref_update_layer(v, T, w, numlevels, *, mode, nmem, nmem_dynamic, stride, periodic_i=0, level=0, surfk=0,
+                     issurfacevar=0, inflation=1.0, inf_ratio=float("nan"), output_increment=0, applylog=0,
+                     j1=0, j2=None):
+    """das_updatefields (ENKF/HYBRID) or das_updatebg (ENOI) of the
+    reference itself on one field-layer, model rows j1..j2.  v is [nmem][jsize]
+    [mni] (ENOI: [nmem + 1][jsize][mni], the background last); returns the
+    updated copy."""
+    L = reflib_update()
+    if L is None:
+        raise RuntimeError("reference update library not built")
+    v = np.ascontiguousarray(v, np.float32).copy()
+    nl = np.ascontiguousarray(numlevels, np.int32).copy()
+    mnj, mni = nl.shape
+    if j2 is None:
+        j2 = mnj - 1
+    Tc = None if T is None else np.ascontiguousarray(T, np.float32)
+    wc = np.ascontiguousarray(w, np.float32)
+    # this library's mode codes (0 ENKF, 1 ENOI, 2 HYBRID) -> the
+    # reference's MODE_ENKF 1, MODE_ENOI 2, MODE_HYBRID 3 (common/global.h:64-67)
+    L.ref_update_layer(int(mode) + 1, int(nmem), int(nmem_dynamic), int(stride), int(periodic_i), int(mni), int(mnj),
+                       int(j1), int(j2), int(level), int(surfk), int(issurfacevar), float(inflation),
+                       float(inf_ratio), int(output_increment), int(applylog),
+                       None if Tc is None else Tc.ctypes.data, wc.ctypes.data, nl.ctypes.data, v.ctypes.data)
+    return v
+
+
+def ref_sethybridensemble(v, nmem_d, gamma):
+    """das_sethybridensemble of the reference itself; v is [nmem][nij]
+    (copied).  Returns (v, vmean)."""
+    L = reflib_update()
+    if L is None:
+        raise RuntimeError("reference update library not built")
+    v = np.ascontiguousarray(v, np.float32)
+    m, nij = v.shape
+    buf = np.zeros((m + 2, nij), np.float32)
+    buf[:m] = v
+    L.ref_sethybridensemble(int(m), int(nmem_d), float(gamma), int(nij), buf.ctypes.data)
+    vmean = buf[m:].reshape(-1).view(np.float64)[:nij].copy()
+    return buf[:m].copy(), vmean

@@ -22,6 +22,14 @@ GPU library without needing the reference at test time:
                   (integer positions, all edges, periodic and not, both
                   surface-layer conventions): the HE that H_surf_standard /
                   H_subsurf_standard (calc/model2obs.c) give with footprint 0.
+  update.npz      das_updatefields / das_updatebg (update/update.c) and
+                  das_sethybridensemble (common/dasystem.c), from
+                  oracle/_ref/libenkf_ref_update.so (both files compiled
+                  unmodified), on seeded transforms, fields and wet-level
+                  counts: strides 1, 2 and 3, periodic i, field tiles
+                  (j1..j2), land and level masks with surfk 0 and > 0,
+                  missing values in dynamic and static members, spread-capped
+                  inflation, increments, log10 fields, hybrid and EnOI.
 
 Usage:  python tests/golden/make_golden.py [fixture ...]   (default: all)
 """
@@ -157,10 +165,83 @@ def model2obs():
     print("model2obs:", n, "positions,", int(np.isnan(out["he2_p0"]).sum()), "all-dry 2-D cases")
 
 
+# the update cases: (name, mode (0 ENKF, 1 ENOI, 2 HYBRID), nj, ni, m, m_dyn,
+# stride, periodic_i, j1, j2 (-1: last row), level, surfk, issurfacevar,
+# inflation, inf_ratio, output_increment, applylog)
+UPDATE_CASES = [
+    ("enkf_s1_infl", 0, 24, 31, 12, 12, 1, 0, 0, -1, 0, 0, 0, 1.05, float("nan"), 0, 0),
+    ("enkf_s3_mask_ratio", 0, 37, 44, 16, 16, 3, 0, 0, -1, 1, 0, 0, 1.1, 0.5, 0, 0),
+    ("enkf_s2_periodic_tile", 0, 30, 25, 12, 12, 2, 1, 6, 19, 0, 0, 0, 1.0, float("nan"), 0, 0),
+    ("enkf_s3_surfk", 0, 28, 34, 12, 12, 3, 0, 3, 20, 2, 4, 0, 1.02, 0.3, 0, 0),
+    ("enkf_s3_surfk_surfacevar", 0, 28, 34, 12, 12, 3, 1, 0, -1, 0, 4, 1, 1.0, float("nan"), 0, 0),
+    ("enkf_s2_increment", 0, 26, 29, 12, 12, 2, 0, 0, -1, 0, 0, 0, 1.0, float("nan"), 1, 0),
+    ("enkf_s2_increment_log", 0, 26, 29, 12, 12, 2, 0, 0, -1, 0, 0, 0, 1.0, float("nan"), 1, 1),
+    ("hybrid_s3", 2, 31, 40, 18, 12, 3, 0, 0, -1, 0, 0, 0, 1.04, 0.4, 0, 0),
+    ("hybrid_s1_missing_static", 2, 20, 22, 16, 10, 1, 0, 0, -1, 0, 0, 0, 1.0, float("nan"), 0, 0),
+    ("enoi_s3", 1, 31, 40, 14, 14, 3, 0, 0, -1, 0, 0, 0, 1.0, float("nan"), 0, 0),
+    ("enoi_s2_tile_surfk", 1, 30, 27, 10, 10, 2, 1, 4, 21, 1, 3, 0, 1.0, float("nan"), 0, 0),
+]
+
+
+def update():
+    rng = np.random.default_rng(20260)
+    out = {"names": np.array([c[0] for c in UPDATE_CASES])}
+    for k, (name, mode, mnj, mni, m, md, stride, per, j1, j2, level, surfk, issv, infl, ratio, inc,
+            alog) in enumerate(UPDATE_CASES):
+        nj = (mnj - 1) // stride + 1
+        ni = (mni - 1) // stride + 1
+        j2 = mnj - 1 if j2 < 0 else j2
+        jsize = j2 - j1 + 1
+        # transforms near the identity (ETKF-like) and small mean weights
+        T = (np.eye(m, dtype=np.float64)[None, None, :md, :] +
+             0.15 * rng.standard_normal((nj, ni, md, m))).astype(np.float32)
+        w = (0.08 * rng.standard_normal((nj, ni, m))).astype(np.float32)
+        nk = 5
+        numlevels = rng.integers(0, nk + 1, (mnj, mni)).astype(np.int32)
+        numlevels[rng.random((mnj, mni)) < 0.55] = nk
+        base = 15.0 + 2.0 * np.sin(np.arange(mni)[None, :] / 5.0) * np.cos(np.arange(mnj)[:, None] / 7.0)
+        rows = m + 1 if mode == 1 else m
+        v = (base[None, j1:j2 + 1, :] + rng.standard_normal((rows, jsize, mni))).astype(np.float32)
+        if alog:
+            v = np.log10(np.abs(v) + 1.0).astype(np.float32)
+        if mode == 2:
+            # the hybrid ensemble as das_update builds it before the update
+            flat = v.reshape(m, -1)
+            hv, vmean = oracle.ref_sethybridensemble(flat, md, 0.5)
+            out[f"u{k}_hyb_in"] = flat.copy()
+            out[f"u{k}_hyb_out"] = hv.copy()
+            out[f"u{k}_hyb_mean"] = vmean
+            v = hv.reshape(m, jsize, mni).copy()
+        # missing values: a dynamic member's NaN, a value above MAXOBSVAL,
+        # a static member's missing value (hybrid), a missing background
+        cells = rng.integers(0, [jsize, mni], (4, 2))
+        v[0, cells[0, 0], cells[0, 1]] = np.nan
+        v[min(1, rows - 1), cells[1, 0], cells[1, 1]] = 2.0e6
+        if mode == 2:
+            v[m - 1, cells[2, 0], cells[2, 1]] = -3.0e6
+        if mode == 1:
+            v[m, cells[3, 0], cells[3, 1]] = 5.0e6
+        res = oracle.ref_update_layer(v, None if mode == 1 else T, w, numlevels, mode=mode, nmem=m, nmem_dynamic=md,
+                                      stride=stride, periodic_i=per, level=level, surfk=surfk, issurfacevar=issv,
+                                      inflation=infl, inf_ratio=ratio, output_increment=inc, applylog=alog, j1=j1,
+                                      j2=j2)
+        out[f"u{k}_prm"] = np.array([mode, mnj, mni, m, md, stride, per, j1, j2, level, surfk, issv, inc, alog],
+                                    np.int32)
+        out[f"u{k}_infl"] = np.array([infl, ratio])
+        out[f"u{k}_T"] = T
+        out[f"u{k}_w"] = w
+        out[f"u{k}_numlevels"] = numlevels
+        out[f"u{k}_v"] = v
+        out[f"u{k}_out"] = res
+    np.savez_compressed(os.path.join(HERE, "update.npz"), **out)
+    print("update:", len(UPDATE_CASES), "cases")
+
+
 if __name__ == "__main__":
     oracle.build()
-    if oracle.reflib() is None or oracle.reflib_utils() is None:
+    if oracle.reflib() is None or oracle.reflib_utils() is None or oracle.reflib_update() is None:
         sys.exit("the reference libraries under oracle/_ref could not be built")
-    which = sys.argv[1:] or ["numerics", "kdtree", "transforms", "model2obs"]
+    which = sys.argv[1:] or ["numerics", "kdtree", "transforms", "model2obs", "update"]
     for name in which:
-        {"numerics": numerics, "kdtree": kdtree, "transforms": transforms, "model2obs": model2obs}[name]()
+        {"numerics": numerics, "kdtree": kdtree, "transforms": transforms, "model2obs": model2obs,
+         "update": update}[name]()

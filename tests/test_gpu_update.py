@@ -151,3 +151,45 @@ def test_update_enoi_bg_bitexact(ctx):
     got = ctx.updatebg(fields, nl, [0], nmem=m, nmem_dynamic=m)
     ref = oracle.updatebg(fields[0], out["w"], nl, nmem=m, stride=2)
     assert np.array_equal(got[0], ref)
+
+
+def _golden_update():
+    import os
+    return np.load(os.path.join(os.path.dirname(__file__), "golden", "update.npz"))
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_update_against_reference_golden(ctx, precision):
+    """The device update against the reference's own update/update.c and
+    common/dasystem.c (compiled unmodified; tests/golden/update.npz): every
+    case of strides, periodic i, tiles, masks with surfk 0 and > 0, missing
+    values, spread-capped inflation, increments, log fields, hybrid (the
+    hybrid ensemble bit for bit) and EnOI (bit for bit, NaN payloads aside)."""
+    g = _golden_update()
+    nl1, lr1, lw1 = oracle.locrad_table(1, 5.0)
+    for k, name in enumerate(g["names"]):
+        mode, mnj, mni, m, md, stride, per, j1, j2, level, surfk, issv, inc, alog = [int(x) for x in g[f"u{k}_prm"]]
+        infl, ratio = [float(x) for x in g[f"u{k}_infl"]]
+        ctx.set_obstypes(nl1, lr1, lw1, np.ones(1))
+        ctx.set_obs(np.array([1.0], np.float32), np.array([1.0], np.float32), np.zeros(1, np.int16),
+                    np.zeros(1, np.int16), np.ones(1, np.float32), np.zeros(1, np.float32))
+        ctx.set_grid(np.arange(mni, dtype=np.float64), np.arange(mnj, dtype=np.float64), stride=stride,
+                     periodic_i=bool(per))
+        ctx.set_transforms(None if mode == 1 else g[f"u{k}_T"], g[f"u{k}_w"], mode=mode, nmem=m,
+                           nmem_dynamic=md if mode != 1 else m)
+        if f"u{k}_hyb_in" in g.files:
+            hv = ctx.sethybridensemble(g[f"u{k}_hyb_in"], md, 0.5)
+            assert np.array_equal(hv, g[f"u{k}_hyb_out"]), name
+        v = g[f"u{k}_v"][None]
+        exp = g[f"u{k}_out"]
+        got = ctx.updatefields(v, g[f"u{k}_numlevels"], [level], mode=mode, nmem=m,
+                               nmem_dynamic=md if mode != 1 else m, surfk=surfk, issurfacevar=issv, inflation=infl,
+                               inf_ratio=ratio, output_increment=inc, applylog=alog, j1=j1, j2=j2,
+                               precision=precision)[0]
+        if mode == 1:
+            assert np.array_equal(got, exp, equal_nan=True), name
+            continue
+        # masked and missing cells are exact zeros in both
+        assert np.array_equal(got == 0.0, exp == 0.0), name
+        tol = 1e-4 if alog else 2e-5
+        assert close(got, exp) < tol, (name, close(got, exp))

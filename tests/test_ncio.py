@@ -442,3 +442,38 @@ def test_transforms_row_by_row(nc, tmp_path):
         assert np.array_equal(f.variables["w"][:], w) and "T" not in f.variables
     with pytest.raises(Exception):
         nc.nc_write_transforms_row(e, nj, None, w[0])
+
+
+def test_overflowing_sizes_are_errors(nc, tmp_path):
+    """Sizes in a CDF-5 header that are negative as signed 64-bit numbers, or
+    whose products with the type size overflow, are refused before any
+    arithmetic on them (the reader returns an error status)."""
+    import struct
+    f3 = np.arange(20, dtype=np.float32).reshape(4, 5)
+    p = tmp_path / "ok5.nc"
+    _cdf5(p, [("j", 4), ("i", 5)], [("v", [0, 1], ">f4", f3, [("scale_factor", ">f4", np.float32(2.0))])])
+    data = p.read_bytes()
+    assert np.array_equal(nc.nc_get_vara_float(p, "v"), f3)
+    bad = tmp_path / "bad5.nc"
+
+    def refused(b):
+        bad.write_bytes(bytes(b))
+        with pytest.raises(Exception):
+            nc.nc_get_vara_float(bad, "v")
+
+    # the attribute's value count: 2^62 + 1 floats (x 4 bytes wraps to 4)
+    at = data.find(b"scale_factor") + 12 + 4
+    b = bytearray(data)
+    b[at:at + 8] = struct.pack(">Q", (1 << 62) + 1)
+    refused(b)
+    # a dimension length with the top bit set (negative as a signed number)
+    dj = data.find(b"j\0\0\0") + 4
+    b = bytearray(data)
+    b[dj:dj + 8] = struct.pack(">Q", 1 << 63)
+    refused(b)
+    # both lengths 2^32: 4 x 2^64 bytes overflows
+    di = data.find(b"i\0\0\0", dj) + 4
+    b = bytearray(data)
+    b[dj:dj + 8] = struct.pack(">Q", 1 << 32)
+    b[di:di + 8] = struct.pack(">Q", 1 << 32)
+    refused(b)
