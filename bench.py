@@ -1,14 +1,15 @@
 """Benchmark of the EnKF-C analysis cycle (calc + update) on GB300.
 
-Workload (default): the 600x900 batched DEnKF workload -- 30% land, 4 layers,
-2 fields, 48 members, 400k observations on swaths and over the ocean, radius
-30 cells, stride 3 (60,000 local analyses per cycle).  Synthetic, seeded
-inputs (enkf-c_gb300/synth.py).
+Workload (default): workload 3, the largest that fits one GPU -- a 1000x1000
+grid, 10 layers x 2 fields, 96 members, 2M uniform observations, ETKF,
+radius 25 cells, stride 2 (250,000 local analyses per cycle; about 30 GB
+resident).  --config 2 runs the 600x900 batched DEnKF workload (60,000
+analyses).  Synthetic, seeded inputs (enkf-c_gb300/synth.py).
 
 One step = one full cycle on the device with every input resident in HBM:
 spatial index build, innovations (das_calcinnandspread), standardisation,
-local-analysis transforms for all 60,000 points, and the X5 update of all
-8 field-layers.  `value` = local analyses per second of that cycle.
+local-analysis transforms for all points, and the X5 update of all
+field-layers.  `value` = local analyses per second of that cycle.
 
 `e2e` = the same cycle through the host-buffer C ABI (HE, fields in pinned
 host memory; T, w and the updated fields copied back), timed on the host.
@@ -17,7 +18,8 @@ Multi-GPU: the cycle does not exchange data between GPUs, so --gpus N runs N
 independent replicas (one process per GPU); value = all analyses / max time.
 
 --impl reference times the CPU restatement of the reference (oracle/) on the
-host cores over a bounded sample of the same workload.
+host cores over a bounded random sample of the same workload, the threads
+taking work units from a shared queue.
 """
 from __future__ import annotations
 
@@ -215,10 +217,10 @@ def run_gpu(args, rank, world, local_rank):
             stream.synchronize()
             calc_ms.append(parts[0].elapsed_time(parts[1]))
             upd_ms.append(parts[1].elapsed_time(parts[2]))
-            # the library's CUDA events on the launching stream: the
-            # transform kernel alone (kernel_times [0]), the batched
-            # eigensolver / inverse after it ([1]), the update kernel(s)
-            # (stage_times [3])
+            # the library's CUDA events on the launching stream, summed over
+            # the transform stage's batches: the transform kernels
+            # (kernel_times [0]), the solve kernels after them ([1]); the
+            # update kernel(s) (stage_times [3])
             st_ms = ctx.stage_times()
             kt = ctx.kernel_times()
             kern_ms.append(kt[0])
@@ -280,7 +282,7 @@ def run_gpu(args, rank, world, local_rank):
         step(path=enkfg.PATH_PLAIN, prec=enkfg.PREC_FP64)
         torch.cuda.synchronize()
         pe = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
-        npl = 2
+        npl = 1
         pe[0].record(stream)
         for _ in range(npl):
             step(path=enkfg.PATH_PLAIN, prec=enkfg.PREC_FP64)
@@ -334,7 +336,7 @@ def run_gpu(args, rank, world, local_rank):
     if tpa is None:
         roof["traffic_note"] = "no ncu capture of this version of the kernel"
     roof["kernel_ms"] = kern_t * 1e3
-    roof["finishing_kernels_ms"] = statistics.median(fin_ms)
+    roof["solve_kernels_ms"] = statistics.median(fin_ms)
     roof["flops_per_launch"] = flops
     upa = TRAFFIC_PER_ANALYSIS.get((w.cfg, "k_update_cells")) if m <= 64 else None
     uroof = {"kernel": "k_update_cells" if m <= 64 else "k_update_v2", "bound": "hbm",
@@ -423,7 +425,7 @@ def run_gpu(args, rank, world, local_rank):
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
-        cpu = cpu_baseline(w, args.cpu_rows)
+        cpu = cpu_baseline(w, args.cpu_units)
 
     if rank == 0:
         line = {
@@ -431,15 +433,13 @@ def run_gpu(args, rank, world, local_rank):
             "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64" if prec == enkfg.PREC_FP64 else "f32/tf32-split",
             "data": "synthetic (seeded, enkf-c_gb300/synth.py)",
-            "config": {"workload": f"workload {w.cfg}: {w.ni}x{w.nj} grid, {w.nlayers} layers x {w.nfields} fields, "
-                                   f"m={m}, {w.nobs} obs, {'DEnKF' if w.scheme == 0 else 'ETKF'}, radius "
-                                   f"{w.locrad:g}, stride {w.stride}",
+            "config": {"workload": workload_name(w),
                        "local_analyses": w.nanalyses, "path": args.path, "precision": args.precision,
-                       "parallelism": f"replicas x{world}", "l2": "256 MB flush before every step; "
-                                                             "fields (830 MB) exceed L2"},
+                       "parallelism": f"replicas x{world}",
+                       "l2": f"256 MB flush before every step; fields ({fields_h.nbytes / 1e9:.2f} GB) exceed L2"},
             "stages_ms": {"calc": statistics.median(calc_ms), "update": statistics.median(upd_ms)},
             "update_gbs": ub / upd_t / 1e9,
-            "calc_gflops_fp64": flops / calc_t / 1e9,
+            "calc_algorithmic_tflops": flops / calc_t / 1e12,
             "roofline": roof, "roofline_update": uroof, "graph": graph, "e2e": e2e, "cpu_baseline": cpu,
             "gpu_launches": int(launches),
             "plain_gpu_fp64": plain64,
@@ -454,12 +454,18 @@ def run_gpu(args, rank, world, local_rank):
 # ---------------------------------------------------------------------------
 # CPU (oracle) side
 # ---------------------------------------------------------------------------
-def cpu_sample(w, rows, threads):
-    """The calc + update cycle of the CPU restatement: per-cycle set-up (kd-trees,
-    innovations, standardisation) on the whole domain, the transforms of `rows`
-    strided rows spread over the domain, and the update of the model rows they
-    cover.  Returns (analyses in the sample, set-up s, calc s, update s,
-    sampled rows)."""
+UNIT_COLS = 50   # strided columns in one CPU work unit (one queue item)
+
+
+def cpu_sample(w, per_worker, threads, seed=0):
+    """The calc + update cycle of the CPU restatement on a bounded sample:
+    per-cycle set-up (kd-trees, innovations, standardisation) on the whole
+    domain; the transforms of `per_worker` x `threads` work units (pieces of
+    UNIT_COLS strided columns of one strided row, drawn at random over the
+    domain) taken from a shared queue by the threads as they come free (the
+    reference's dynamic mpiqueue schedule); and the update of the model rows
+    of the sampled strided rows, all field-layers.  Returns a dict with the
+    sample's analyses, model rows updated and the times (s)."""
     import concurrent.futures as cf
 
     import oracle
@@ -468,15 +474,20 @@ def cpu_sample(w, rows, threads):
     obs = oracle.ObsSet(w.lon, w.lat, w.otype, w.status, w.ntypes, nl, lr, lw)
     S, s = oracle.prepare(w.HE, w.value, w.status, w.estd, w.otype, np.ones(w.ntypes))
     t_setup = time.perf_counter() - t0
-    sel = [int(r) for r in np.unique(np.linspace(0, w.nj_s - 1, rows).astype(int))]
+    allu = [(jj, i0, min(i0 + UNIT_COLS, w.ni_s)) for jj in range(w.nj_s) for i0 in range(0, w.ni_s, UNIT_COLS)]
+    rng = np.random.default_rng(seed)
+    k = min(len(allu), max(1, per_worker * threads))
+    units = [allu[i] for i in sorted(rng.choice(len(allu), k, replace=False))]
+    n_an = sum(u[2] - u[1] for u in units)
     t0 = time.perf_counter()
     out = oracle.calctransforms(obs, mode=w.mode, scheme=w.scheme, nmem=w.nmem, nmem_dynamic=w.nmem_dynamic,
-                                alpha=w.alpha, stride=w.stride, x=w.x, y=w.y, S=S, s=s, rows=sel, threads=threads,
-                                want_diag=False)
+                                alpha=w.alpha, stride=w.stride, x=w.x, y=w.y, S=S, s=s, threads=threads,
+                                want_diag=False, units=units)
     t_calc = time.perf_counter() - t0
     nfl = w.nfields * w.nlayers
     fl = w.fields.reshape(nfl, w.nmem, w.nj, w.ni)
     T = out["T"] if out["T"] is not None else np.zeros((w.nj_s, w.ni_s, 1, w.nmem), np.float32)
+    rows = sorted({u[0] for u in units})
 
     def upd(args_):
         jj, f = args_
@@ -488,57 +499,71 @@ def cpu_sample(w, rows, threads):
 
     t0 = time.perf_counter()
     with cf.ThreadPoolExecutor(max_workers=threads) as ex:
-        list(ex.map(upd, [(jj, f) for jj in sel for f in range(nfl)]))
+        list(ex.map(upd, [(jj, f) for jj in rows for f in range(nfl)]))
     t_upd = time.perf_counter() - t0
-    return len(sel) * w.ni_s, t_setup, t_calc, t_upd, len(sel)
+    return dict(analyses=n_an, units=len(units), rows=len(rows), setup=t_setup, calc=t_calc, update=t_upd)
 
 
-def cpu_rate(w, n, ts, tc, tu, nrows):
-    """Analyses/s of a full cycle extrapolated from the row sample."""
-    full = ts + (tc + tu) * (w.nj_s / nrows)
+def cpu_rate(w, smp):
+    """Analyses/s of a full cycle from a sample: set-up once, the transforms
+    scaled by analyses, the update by strided rows."""
+    full = smp["setup"] + smp["calc"] * (w.nanalyses / smp["analyses"]) + smp["update"] * (w.nj_s / smp["rows"])
     return w.nanalyses / full, full
 
 
-def cpu_baseline(w, rows):
+def cpu_sample_text(w, smp, threads, full):
+    return (f"{smp['units']} work units of {UNIT_COLS} strided columns ({smp['analyses']} of {w.nanalyses} local "
+            f"analyses, {threads} threads pulling from a shared queue) and the model rows of {smp['rows']} strided "
+            f"rows x {w.nfields * w.nlayers} field-layers; set-up {smp['setup']:.2f} s, calc {smp['calc']:.2f} s, "
+            f"update {smp['update']:.2f} s; scaled to the full cycle ({full:.1f} s): calc by analyses, update by "
+            f"rows; C restatement of the reference (oracle/) + OpenBLAS, one thread per worker")
+
+
+def cpu_baseline(w, per_worker):
     threads = os.cpu_count() or 1
-    n, ts, tc, tu, nrows = cpu_sample(w, rows, threads)
-    v, full = cpu_rate(w, n, ts, tc, tu, nrows)
-    return {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
-            "sample": f"{nrows} of {w.nj_s} strided rows ({n} local analyses) and their model rows x "
-                      f"{w.nfields * w.nlayers} field-layers, extrapolated to the full cycle ({full:.1f} s): "
-                      f"set-up {ts:.2f} s, calc {tc:.2f} s, update {tu:.2f} s; C restatement of the reference "
-                      f"(oracle/) + OpenBLAS, {threads} threads"}
+    smp = cpu_sample(w, per_worker, threads)
+    v, full = cpu_rate(w, smp)
+    return {"value": v, "unit": UNIT, "cores": threads, "kind": "port", "sample": cpu_sample_text(w, smp, threads, full)}
 
 
 def run_reference(args, rank, world):
+    """The CPU restatement of the reference on the host cores.  Each step
+    runs the per-cycle set-up on the whole domain and a bounded random sample
+    of the transforms and the update (cpu_sample); value = the full cycle's
+    analyses / its time scaled from the samples, ms_per_step = the measured
+    wall time of a step (the sample)."""
     if rank != 0:
         return
     import oracle
     oracle.build()
     w = workload(args.config, args.scale)
     threads = os.cpu_count() or 1
-    kind = "port"
-    for _ in range(args.warmup):
-        cpu_sample(w, max(1, args.cpu_rows // 4), threads)
-    times = []
-    for _ in range(args.steps):
-        n, ts, tc, tu, nrows = cpu_sample(w, args.cpu_rows, threads)
-        times.append(cpu_rate(w, n, ts, tc, tu, nrows)[1])
-    value = w.nanalyses * len(times) / sum(times)
-    ts = sum(times)
+    for k in range(args.warmup):
+        cpu_sample(w, 1, threads, seed=1000 + k)
+    fulls, walls, smp = [], [], None
+    for k in range(args.steps):
+        t0 = time.perf_counter()
+        smp = cpu_sample(w, args.cpu_units, threads, seed=k)
+        walls.append(time.perf_counter() - t0)
+        fulls.append(cpu_rate(w, smp)[1])
+    value = w.nanalyses * len(fulls) / sum(fulls)
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": ts / args.steps * 1e3, "higher_is_better": True,
+            "warmup": args.warmup, "ms_per_step": statistics.mean(walls) * 1e3, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
             "impl": "reference",
-            "config": {"workload": f"workload {w.cfg}: {w.ni}x{w.nj}, m={w.nmem}, {w.nobs} obs", "path": "cpu",
-                       "parallelism": f"{threads} host threads"},
-            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": kind,
-                             "sample": f"{args.cpu_rows} strided rows per step of {w.nj_s}, extrapolated to the full "
-                                       f"cycle; CPU restatement of the "
-                                       f"reference (oracle/, C + OpenBLAS); the reference's own build needs MPI and "
-                                       f"NetCDF, absent here"},
+            "config": {"workload": workload_name(w), "path": "cpu", "parallelism": f"{threads} host threads"},
+            "full_cycle_s": statistics.mean(fulls),
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                             "sample": cpu_sample_text(w, smp, threads, statistics.mean(fulls)) +
+                             "; the reference's own build needs MPI and NetCDF, absent here"},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
+
+
+def workload_name(w):
+    return (f"workload {w.cfg}: {w.ni}x{w.nj} grid, {w.nlayers} layers x {w.nfields} fields, m={w.nmem}"
+            f"{f' ({w.nmem_dynamic} dynamic)' if w.nmem_dynamic < w.nmem else ''}, {w.nobs} obs, "
+            f"{'DEnKF' if w.scheme == 0 else 'ETKF'}, radius {w.locrad:g}, stride {w.stride}")
 
 
 def main():
@@ -547,11 +572,11 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--config", type=int, default=2)
+    ap.add_argument("--config", type=int, default=3)
     ap.add_argument("--scale", type=float, default=1.0)
     ap.add_argument("--path", default="batched", choices=["plain", "batched"])
     ap.add_argument("--precision", default="mixed", choices=["fp64", "mixed"])
-    ap.add_argument("--cpu-rows", type=int, default=24)
+    ap.add_argument("--cpu-units", type=int, default=8, help="CPU work units per host thread in a sample")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--graph", type=int, default=1, help="also time the cycle replayed from a CUDA graph")
     ap.add_argument("--compare-fp64", type=int, default=1, help="also time the plain GPU FP64 path")

@@ -16,8 +16,8 @@ ROOT = os.path.dirname(PKG)
 CSRC = os.path.join(PKG, "csrc")
 OUTDIR = os.path.join(PKG, "_lib")
 LIB = os.path.join(OUTDIR, "libenkfg.so")
-SOURCES = ["capi.cu", "prep.cu", "index.cu", "calc.cu", "calc_mixed.cu", "update.cu", "adjoint.cu", "noalloc.cu",
-           "model2obs.cu", "ncio.cpp"]
+SOURCES = ["capi.cu", "prep.cu", "index.cu", "calc.cu", "calc_mixed.cu", "etkf_mixed.cu", "update.cu", "adjoint.cu",
+           "noalloc.cu", "model2obs.cu", "ncio.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-fvisibility=hidden",
          "--expt-relaxed-constexpr", "-I" + os.path.join(ROOT, "include")]

@@ -34,12 +34,15 @@ struct CalcSmem {
     static constexpr int MP = 16 * R;       // padded member count
     static constexpr int TLD = MP;          // tile row stride (doubles)
     static constexpr int LDA = MP + 1;      // matrix row stride (doubles)
+    // observations per chunk at most: KC_MAX, but 32 for the largest
+    // ensembles, whose FP64 M (144 x 145 doubles) leaves no room for more
+    static constexpr int KC = (R >= 9) ? 32 : KC_MAX;
     static size_t bytes()
     {
         size_t s = 0;
-        s += (size_t)KC_MAX * TLD * 8;                 // tile
+        s += (size_t)KC * TLD * 8;                     // tile
         s += (size_t)LIST_EXTRA * 8;                   // list taper
-        s += (size_t)KC_MAX * 8;                       // sloc
+        s += (size_t)KC * 8;                           // sloc
         s += (size_t)MP * LDA * 8;                     // A
         s += (size_t)6 * MP * 8;                       // b d e cs sn v
         s += (size_t)ENKFG_MAXTYPES * 8 * 2;           // per-type ss, pdfs
@@ -112,13 +115,13 @@ struct GramProc64 {
 template <int R>
 __global__ void __launch_bounds__(CALC_NT) k_transforms(CalcArgs a)
 {
-    constexpr int MP = 16 * R, TLD = MP, LDA = MP + 1;
+    constexpr int MP = 16 * R, TLD = MP, LDA = MP + 1, KC = CalcSmem<R>::KC;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
     unsigned char* sp = smem_raw;
-    double* tile = (double*)sp;       sp += (size_t)KC_MAX * TLD * 8;
+    double* tile = (double*)sp;       sp += (size_t)KC * TLD * 8;
     double* llc = (double*)sp;        sp += (size_t)LIST_EXTRA * 8;
-    double* sloc = (double*)sp;       sp += (size_t)KC_MAX * 8;
+    double* sloc = (double*)sp;       sp += (size_t)KC * 8;
     double* A = (double*)sp;          sp += (size_t)MP * LDA * 8;
     double* b = (double*)sp;          sp += MP * 8;
     double* d = (double*)sp;          sp += MP * 8;
@@ -141,6 +144,7 @@ __global__ void __launch_bounds__(CALC_NT) k_transforms(CalcArgs a)
         const int pt = a.order ? a.order[idx] : a.item0 + idx;
         int kc = a.kc;
         if (a.kc_table != nullptr && a.counts != nullptr) kc = a.kc_table[count_bin(a.counts[pt])];
+        if (kc > KC) kc = KC;
         const double qx = a.qx[pt], qy = a.qy[pt], qz = a.ndim == 3 ? a.qz[pt] : 0.0;
         if (tid < ENKFG_MAXTYPES) {
             tss[tid] = 0.0;
@@ -301,8 +305,6 @@ static enkfg_status launch_R(enkfg_ctx* ctx, CalcArgs& a, cudaStream_t st)
     CKL();
     return ENKFG_OK;
 }
-
-enkfg_status launch_mixed(enkfg_ctx* ctx, CalcArgs& a, cudaStream_t st);
 
 static enkfg_status dispatch(enkfg_ctx* ctx, CalcArgs& a, int precision, cudaStream_t st)
 {
@@ -507,6 +509,29 @@ __global__ void __launch_bounds__(INV_NT) k_inv_finish(CalcArgs a)
     if (a.want_diag) diag_single(a, pt, (int)pd, dfs, trss);
 }
 
+// Per-batch timing: events before and after each batch's transform kernel
+// and after its solve kernels, summed by enkfg_kernel_times.  Events are
+// created on first use (outside stream capture); batches past
+// ENKFG_TIMED_BATCHES, or marked while no event could be created, are not
+// timed.
+void batch_mark(enkfg_ctx* ctx, int k, cudaStream_t st)
+{
+    if (k == 0) ++ctx->nbatch;
+    const int b = ctx->nbatch - 1;
+    if (b < 0 || b >= ENKFG_TIMED_BATCHES) return;
+    const int idx = 3 * b + k;
+    while (ctx->nbev <= idx) {
+        cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+        if (cudaStreamIsCapturing(st, &cs) != cudaSuccess || cs != cudaStreamCaptureStatusNone ||
+            cudaEventCreate(&ctx->bev[ctx->nbev]) != cudaSuccess) {
+            cudaGetLastError();
+            return;
+        }
+        ++ctx->nbev;
+    }
+    cudaEventRecord(ctx->bev[idx], st);
+}
+
 static enkfg_status run_inv_batched(enkfg_ctx* ctx, const CalcArgs& a0, int precision, cudaStream_t st)
 {
     enkfg_status s;
@@ -540,11 +565,12 @@ static enkfg_status run_inv_batched(enkfg_ctx* ctx, const CalcArgs& a0, int prec
         b.eb = ctx->d_eb;
         b.eaux = ctx->d_eaux;
         if (b.persistent) CK(cudaMemsetAsync(ctx->d_qhead, 0, sizeof(int), st));
-        if (i0 == 0) cudaEventRecord(ctx->ev[8], st);
+        batch_mark(ctx, 0, st);
         if ((s = dispatch(ctx, b, precision, st))) return s;
-        if (i0 == 0) cudaEventRecord(ctx->ev[9], st);
+        batch_mark(ctx, 1, st);
         k_inv_finish<<<nb, INV_NT, ismem, st>>>(b);
         CKL();
+        batch_mark(ctx, 2, st);
     }
     return ENKFG_OK;
 }
@@ -631,9 +657,9 @@ static enkfg_status run_etkf_batched(enkfg_ctx* ctx, const CalcArgs& a0, int pre
         b.eb = ctx->d_eb;
         b.eaux = ctx->d_eaux;
         if (b.persistent) CK(cudaMemsetAsync(ctx->d_qhead, 0, sizeof(int), st));
-        if (i0 == 0) cudaEventRecord(ctx->ev[8], st);
+        batch_mark(ctx, 0, st);
         if ((s = dispatch(ctx, b, precision, st))) return s;
-        if (i0 == 0) cudaEventRecord(ctx->ev[9], st);
+        batch_mark(ctx, 1, st);
         if (tr64) k_tred_batch<64><<<nb, 64, tsmem, st>>>(b);
         else k_tred_batch<128><<<nb, 128, tsmem, st>>>(b);
         CKL();
@@ -642,6 +668,7 @@ static enkfg_status run_etkf_batched(enkfg_ctx* ctx, const CalcArgs& a0, int pre
         CKL();
         k_eig_finish<<<nb, CALC_NT, fsmem, st>>>(b, ctx->d_eval, ctx->d_erot, rcap, ctx->d_ehdr, hcap, ctx->d_enh);
         CKL();
+        batch_mark(ctx, 2, st);
     }
     return ENKFG_OK;
 }
@@ -697,6 +724,7 @@ enkfg_status run_transforms(enkfg_ctx* ctx, const enkfg_calc_params* p, cudaStre
     a.want_diag = p->want_diag ? 1 : 0;
     a.alpha = p->alpha;
     a.wait_ns = ctx->wait_ns;
+    a.wait_drill = ctx->wait_drill;
     a.kc = 32;
     a.types = ctx->d_types;
     a.bstart = ctx->d_bstart;
@@ -758,14 +786,18 @@ enkfg_status run_transforms(enkfg_ctx* ctx, const enkfg_calc_params* p, cudaStre
     // pass, so they keep the in-kernel one)
     const bool etkf = (p->mode != ENKFG_MODE_ENOI && p->scheme == ENKFG_SCHEME_ETKF);
     const bool defer = !(a.want_diag && a.ntypes > 1);
-    if (defer && etkf) {
+    ctx->nbatch = 0;
+    if (defer && etkf && p->precision == ENKFG_PREC_MIXED && etkf_mixed_supported(m)) {
+        if ((s = run_etkf_mixed(ctx, a, st))) return s;
+    } else if (defer && etkf) {
         if ((s = run_etkf_batched(ctx, a, p->precision, st))) return s;
     } else if (defer) {
         if ((s = run_inv_batched(ctx, a, p->precision, st))) return s;
     } else {
-        cudaEventRecord(ctx->ev[8], st);
+        batch_mark(ctx, 0, st);
         if ((s = dispatch(ctx, a, p->precision, st))) return s;
-        cudaEventRecord(ctx->ev[9], st);
+        batch_mark(ctx, 1, st);
+        batch_mark(ctx, 2, st);
     }
     cudaEventRecord(ctx->ev[3], st);
     ctx->t_mode = p->mode;

@@ -18,6 +18,7 @@ struct CalcArgs {
     int nitems;        // queue length (npts, or a sample while autotuning)
     double alpha;
     unsigned long long wait_ns;   // bound on a device wait (mixed path), ns
+    int wait_drill;               // the mixed kernel's timeout drill (enkfg_set_wait_drill)
     const TypeIndex* types;
     const long long* bstart;
     const double* sx;

@@ -932,9 +932,12 @@ __global__ void __launch_bounds__(CALC_NT, 2) k_transforms_mixed(CalcArgs a, int
     const size_t piece = (size_t)N * kcm;
 
     // set-up: TMEM columns, mbarriers, zeroed operand tiles, the quantum
+    // drill_bar: an mbarrier nothing arrives at (the timeout drill's wait)
+    __shared__ uint64_t drill_bar;
     if (wid == 0) tc::tmem_alloc(tslot, tcols);
     if (tid == 0) {
         for (int i = 0; i < 2; ++i) tc::mbar_init(mbar + i, 1);
+        tc::mbar_init(&drill_bar, 1);
         *err = 0;
     }
     for (size_t i = tid; i < ntile; i += CALC_NT) tiles[i] = 0.0f;
@@ -954,6 +957,16 @@ __global__ void __launch_bounds__(CALC_NT, 2) k_transforms_mixed(CalcArgs a, int
         const int idx = next_item(a, it, ictl);
         if (idx < 0 || *err) break;
         const int pt = a.order ? a.order[idx] : a.item0 + idx;
+        if (a.wait_drill && it == 0) {
+            // the timeout drill: a bounded wait that nothing completes, so
+            // that it expires (enkfg_set_wait_drill)
+            if (tid == 0 && !tc::mbar_wait_bounded(&drill_bar, 0, a.wait_ns)) atomicExch(err, 1);
+            __syncthreads();
+            if (*err) {
+                if (tid == 0) a.status[pt] = MX_TIMEOUT_CODE;
+                break;
+            }
+        }
         const double qx = a.qx[pt], qy = a.qy[pt], qz = a.ndim == 3 ? a.qz[pt] : 0.0;
         // observations per round: 8, 16 or 32 (a power of two), per count
         // bin when tuned

@@ -72,6 +72,13 @@ ENKFG_API enkfg_status enkfg_set_wait_limit(enkfg_ctx* ctx, unsigned long long n
     return ENKFG_OK;
 }
 
+ENKFG_API enkfg_status enkfg_set_wait_drill(enkfg_ctx* ctx, int on)
+{
+    if (!ctx) return ENKFG_EINVAL;
+    ctx->wait_drill = on ? 1 : 0;
+    return ENKFG_OK;
+}
+
 ENKFG_API enkfg_status enkfg_create(int device, enkfg_ctx** out)
 {
     if (!out) return ENKFG_EINVAL;
@@ -110,6 +117,8 @@ ENKFG_API void enkfg_destroy(enkfg_ctx* ctx)
     cudaSetDevice(ctx->device);
     cudaStreamSynchronize(ctx->stream);
     void* ptrs[] = { ctx->d_lon, ctx->d_lat, ctx->d_type, ctx->d_status, ctx->d_estd, ctx->d_value, ctx->d_rfac, ctx->d_rfac_sqrt, ctx->d_gtmp, ctx->d_smax, ctx->d_qscale, ctx->d_eq, ctx->d_ed, ctx->d_ee, ctx->d_eb, ctx->d_eaux, ctx->d_eval, ctx->d_erot, ctx->d_ehdr, ctx->d_enh,
+                     ctx->d_emq, ctx->d_emmhl, ctx->d_emd, ctx->d_eme, ctx->d_emrot, ctx->d_emhdr, ctx->d_emnh,
+                     ctx->d_emz0, ctx->d_emp,
                      ctx->d_S, ctx->d_s, ctx->d_std, ctx->d_types, ctx->d_bstart, ctx->d_bfill, ctx->d_key,
                      ctx->d_sid, ctx->d_sx, ctx->d_sy, ctx->d_sz, ctx->d_sxf, ctx->d_syf, ctx->d_stype, ctx->d_St, ctx->d_ss, ctx->d_ox,
                      ctx->d_oy, ctx->d_oz, ctx->d_qx, ctx->d_qy, ctx->d_qz, ctx->d_T, ctx->d_w, ctx->d_T64,
@@ -121,6 +130,7 @@ ENKFG_API void enkfg_destroy(enkfg_ctx* ctx)
         if (ptrs[k]) cudaFree(ptrs[k]);
     for (int k = 0; k < 10; ++k)
         if (ctx->ev[k]) cudaEventDestroy(ctx->ev[k]);
+    for (int k = 0; k < ctx->nbev; ++k) cudaEventDestroy(ctx->bev[k]);
     if (ctx->own_stream) ctx->stream = ctx->own_stream;
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
     free(ctx);
@@ -283,8 +293,12 @@ ENKFG_API enkfg_status enkfg_kernel_times(const enkfg_ctx* ctx, float* ms2)
 {
     if (!ctx || !ms2) return ENKFG_EINVAL;
     ms2[0] = ms2[1] = 0.0f;
-    if (cudaEventElapsedTime(&ms2[0], ctx->ev[8], ctx->ev[9]) != cudaSuccess) ms2[0] = 0.0f;
-    if (cudaEventElapsedTime(&ms2[1], ctx->ev[9], ctx->ev[3]) != cudaSuccess) ms2[1] = 0.0f;
+    const int nb = ctx->nbatch < ENKFG_TIMED_BATCHES ? ctx->nbatch : ENKFG_TIMED_BATCHES;
+    for (int b = 0; b < nb && 3 * b + 2 < ctx->nbev; ++b) {
+        float t0 = 0.0f, t1 = 0.0f;
+        if (cudaEventElapsedTime(&t0, ctx->bev[3 * b], ctx->bev[3 * b + 1]) == cudaSuccess) ms2[0] += t0;
+        if (cudaEventElapsedTime(&t1, ctx->bev[3 * b + 1], ctx->bev[3 * b + 2]) == cudaSuccess) ms2[1] += t1;
+    }
     cudaGetLastError();
     return ENKFG_OK;
 }

@@ -1,0 +1,504 @@
+// etkf_mixed.cu -- the ETKF solve of the mixed-precision batched path.
+//
+// For every local analysis the transform kernel leaves M = I + S'S (FP64,
+// upper triangle), S's, p and tr(S'S) in a batch slot; the reference then
+// needs T = M^-1/2 and w = M^-1 S's (calc/calcs.c:300-412).  GB300 issues
+// FP64 at 1/64 of its FP32 rate, so an FP64 eigensolver at nmem = 96 costs
+// about 10 m^3 FP64 operations a point and dominates the cycle.  Here the
+// eigendecomposition only seeds a Newton correction:
+//
+//   1. M = Q diag(lambda) Q' in FP32 (Householder tridiagonalisation, then
+//      the implicit QL chains one thread per point with their rotations
+//      logged, then the log replayed onto Q) -- the FP64 pipeline of
+//      calc.cu with F = float;
+//   2. Z0 = Q diag(lambda^-1/2) Q' (FP32);
+//   3. the residual R = I - Z0 M Z0 in double-float arithmetic (every
+//      product of a float pair exact through an FMA, every sum a TwoSum), so
+//      that R, of order 1e-4, is known to about 1e-12 absolute;
+//   4. the correction D solving D (M Z0) + (Z0 M) D = R, in the eigenbasis
+//      of step 1: D~ = Q' R Q, D~_ij /= (lambda_i^1/2 + lambda_j^1/2),
+//      D = Q D~ Q' (FP32: D is of the size of R);
+//   5. T = Z0 + D (summed in FP64), relaxed and cast as the reference does;
+//   6. w by iterative refinement: w += Q diag(1/lambda) Q' r with the
+//      residual r = S's - M w in FP64, three times.
+//
+// The FP32 decomposition is backward stable with an error of order u32
+// lambda_max (about 1e-4 at lambda_max ~ 1e3), which is the error of Z0; one
+// Newton step squares it, and the errors of solving the correction in an
+// approximate eigenbasis are of the same order.  w converges by a factor of
+// about u32 lambda_max per step.  All matrices are zero-padded to MP = 16 R
+// rows and columns; the work per point is a handful of m^3 FP32 GEMM-like
+// loops on a 16 x 16 thread grid (R x R outputs per thread) and one
+// double-float product pair.
+#include "calc_common.cuh"
+
+#define EM_TRED_NT 128
+#define EM_QL_T 32
+#define EM_REPLAY_NT 128
+#define EM_NT 256
+#define EM_KCH 16      // rows of the global operand staged per step
+
+// ---------------------------------------------------------------------------
+// per-slot scratch of the refined solve (float unless noted)
+// ---------------------------------------------------------------------------
+struct EmSlots {
+    float* q;          // [slots][m][m]  Q of tred2, then the eigenvectors (columns)
+    float2* mhl;       // [slots][m][m]  M as a double-float pair (hi, lo), both triangles
+    float* d;          // [slots][m]     tridiagonal diagonal, then the eigenvalues
+    float* e;          // [slots][m]     tridiagonal off-diagonal
+    float2* rot;       // [slots][rcap]  QL rotation log
+    int2* hdr;         // [slots][hcap]
+    int* nh;           // [slots]        sweeps logged (< 0: the chain failed)
+    float* z0;         // [slots][MP][MP] Z0
+    float2* p;         // [slots][MP][MP] P = M Z0 (double-float)
+    int rcap, hcap, mp;
+};
+
+// ---------------------------------------------------------------------------
+// 1a. FP32 Householder tridiagonalisation, one CTA per slot.  Also splits M
+//     into its double-float pair for the residual.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(EM_TRED_NT) k_em_tred(CalcArgs a, EmSlots z)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int m = a.m, lda = m + 1;
+    const int tid = threadIdx.x, slot = blockIdx.x;
+    float* A = (float*)smem_raw;
+    float* d = A + (size_t)m * lda;
+    float* e = d + m;
+    float* red = e + m;
+    if (!(a.eaux[2 * (size_t)slot] > 0.0)) return;   // empty point
+    const size_t q0 = (size_t)slot * m * m;
+    for (int i = tid; i < m * m; i += EM_TRED_NT) {
+        const int r = i / m, c = i - r * m;
+        const double v = (c >= r) ? a.eq[q0 + i] : a.eq[q0 + (size_t)c * m + r];
+        const float hi = (float)v;
+        A[r * lda + c] = hi;
+        z.mhl[q0 + i] = make_float2(hi, (float)(v - (double)hi));
+    }
+    __syncthreads();
+    la::tred2<EM_TRED_NT>(A, m, lda, d, e, red);
+    for (int i = tid; i < m * m; i += EM_TRED_NT) {
+        const int r = i / m, c = i - r * m;
+        z.q[q0 + i] = A[r * lda + c];
+    }
+    for (int i = tid; i < m; i += EM_TRED_NT) {
+        z.d[(size_t)slot * m + i] = d[i];
+        z.e[(size_t)slot * m + i] = e[i];
+    }
+}
+
+// ---------------------------------------------------------------------------
+// 1b. FP32 QL chains, one thread per slot, rotations logged.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(EM_QL_T) k_em_ql(int nslots, int m, const double* __restrict__ eaux, EmSlots z)
+{
+    extern __shared__ float qsf[];   // [2][m][EM_QL_T]
+    const int lane = threadIdx.x;
+    const int slot = blockIdx.x * EM_QL_T + lane;
+    if (slot >= nslots || !(eaux[2 * (size_t)slot] > 0.0)) return;   // no barrier below
+    float* dcol = qsf + lane;
+    float* ecol = qsf + (size_t)m * EM_QL_T + lane;
+    for (int i = 0; i < m; ++i) {
+        dcol[i * EM_QL_T] = z.d[(size_t)slot * m + i];
+        ecol[i * EM_QL_T] = z.e[(size_t)slot * m + i];
+    }
+    int n = 0;
+    const int stt = la::ql_chain(dcol, ecol, m, EM_QL_T, z.rot + (size_t)slot * z.rcap, z.rcap,
+                                 z.hdr + (size_t)slot * z.hcap, z.hcap, &n);
+    z.nh[slot] = stt == 0 ? n : -stt;
+    if (stt == 0)
+        for (int i = 0; i < m; ++i) z.d[(size_t)slot * m + i] = dcol[i * EM_QL_T];
+}
+
+// ---------------------------------------------------------------------------
+// 1c. The log replayed onto Q (rows in parallel); a point whose chain failed
+//     (log full, or no convergence within the chain) runs tql2 in the CTA.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(EM_REPLAY_NT) k_em_replay(CalcArgs a, EmSlots z)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int m = a.m, lda = m + 1;
+    const int tid = threadIdx.x, slot = blockIdx.x;
+    float* A = (float*)smem_raw;
+    float* d = A + (size_t)m * lda;
+    float* e = d + m;
+    float* cs = e + m;
+    float* sn = cs + m;
+    int* ctl = (int*)(sn + m);
+    if (!(a.eaux[2 * (size_t)slot] > 0.0)) return;
+    const size_t q0 = (size_t)slot * m * m;
+    for (int i = tid; i < m * m; i += EM_REPLAY_NT) {
+        const int r = i / m, c = i - r * m;
+        A[r * lda + c] = z.q[q0 + i];
+    }
+    const int stt = z.nh[slot];
+    for (int i = tid; i < m; i += EM_REPLAY_NT) {
+        d[i] = z.d[(size_t)slot * m + i];
+        e[i] = z.e[(size_t)slot * m + i];
+    }
+    __syncthreads();
+    int rc = 0;
+    if (stt >= 0) la::ql_replay<EM_REPLAY_NT>(A, m, lda, z.rot + (size_t)slot * z.rcap, z.hdr + (size_t)slot * z.hcap,
+                                            stt);
+    else rc = la::tql2<EM_REPLAY_NT>(A, m, lda, d, e, cs, sn, ctl);
+    if (rc != 0 && tid == 0) {
+        const int pt = a.order ? a.order[slot] : a.item0 + slot;
+        a.status[pt] = rc;
+    }
+    for (int i = tid; i < m * m; i += EM_REPLAY_NT) {
+        const int r = i / m, c = i - r * m;
+        z.q[q0 + i] = A[r * lda + c];
+    }
+    if (stt < 0)
+        for (int i = tid; i < m; i += EM_REPLAY_NT) z.d[(size_t)slot * m + i] = d[i];
+}
+
+// ---------------------------------------------------------------------------
+// 2-6. the refinement, one CTA of 256 threads (a 16 x 16 grid) per slot
+// ---------------------------------------------------------------------------
+namespace em {
+
+// acc (hi, lo) += (ah + al) b: the product ah b exactly (FMA), summed into
+// hi by TwoSum; the errors, and al b, into lo
+__device__ __forceinline__ void df_fma(float& sh, float& sl, float ah, float al, float b)
+{
+    const float p = ah * b;
+    const float e = fmaf(ah, b, -p);
+    const float s = sh + p;
+    const float v = s - sh;
+    const float t = (sh - (s - v)) + (p - v);
+    sh = s;
+    sl += t + e;
+    sl = fmaf(al, b, sl);
+}
+
+// C = op(X) op(Y) for MP x MP float matrices in shared memory (row stride
+// lda): thread (ty, tx) of the 16 x 16 grid owns rows ty + 16 r and columns
+// tx + 16 c; k runs over the first n indices (the rest are zero padding).
+// C may alias X or Y.
+template <int R, bool TX, bool TY>
+__device__ __forceinline__ void mm(float* C, const float* X, const float* Y, int n, int lda)
+{
+    const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+    float acc[R][R];
+#pragma unroll
+    for (int r = 0; r < R; ++r)
+#pragma unroll
+        for (int c = 0; c < R; ++c) acc[r][c] = 0.0f;
+    for (int k = 0; k < n; ++k) {
+        float xv[R], yv[R];
+#pragma unroll
+        for (int r = 0; r < R; ++r) xv[r] = TX ? X[k * lda + ty + 16 * r] : X[(ty + 16 * r) * lda + k];
+#pragma unroll
+        for (int c = 0; c < R; ++c) yv[c] = TY ? Y[(tx + 16 * c) * lda + k] : Y[k * lda + tx + 16 * c];
+#pragma unroll
+        for (int r = 0; r < R; ++r)
+#pragma unroll
+            for (int c = 0; c < R; ++c) acc[r][c] = fmaf(xv[r], yv[c], acc[r][c]);
+    }
+    __syncthreads();
+#pragma unroll
+    for (int r = 0; r < R; ++r)
+#pragma unroll
+        for (int c = 0; c < R; ++c) C[(ty + 16 * r) * lda + tx + 16 * c] = acc[r][c];
+    __syncthreads();
+}
+
+}  // namespace em
+
+template <int R>
+__global__ void __launch_bounds__(EM_NT, 1) k_em_refine(CalcArgs a, EmSlots z)
+{
+    constexpr int MP = 16 * R, LDA = MP + 1;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int m = a.m, md = a.md;
+    const int tid = threadIdx.x, slot = blockIdx.x, tx = tid & 15, ty = tid >> 4;
+    float* Q = (float*)smem_raw;                     // [MP][LDA] eigenvectors (columns)
+    float* A = Q + MP * LDA;                         // [MP][LDA]
+    float* B = A + MP * LDA;                         // [MP][LDA]
+    float2* S = (float2*)(B + MP * LDA);             // [EM_KCH][MP] staged rows of P
+    float* lam = (float*)(S + EM_KCH * MP);          // [MP] eigenvalues
+    float* sig = lam + MP;                           // [MP] lambda^1/2
+    float* vf = sig + MP;                            // [MP] float vector
+    float* vt = vf + MP;                             // [MP] float vector
+    double* bv = (double*)(vt + MP);                 // [MP] S's
+    double* wv = bv + MP;                            // [MP] w
+    double* rv = wv + MP;                            // [MP] residual
+    double* red = rv + MP;                           // [EM_NT / 32]
+    const double pd = a.eaux[2 * (size_t)slot];
+    if (!(pd > 0.0)) return;   // empty point: written by the transform kernel
+    const int pt = a.order ? a.order[slot] : a.item0 + slot;
+    const double trss = a.eaux[2 * (size_t)slot + 1];
+    const size_t q0 = (size_t)slot * m * m, z0 = (size_t)slot * MP * MP;
+
+    // eigenvectors and eigenvalues (zero padding beyond m)
+    for (int i = tid; i < MP * MP; i += EM_NT) {
+        const int r = i / MP, c = i - r * MP;
+        Q[r * LDA + c] = (r < m && c < m) ? z.q[q0 + (size_t)r * m + c] : 0.0f;
+    }
+    for (int i = tid; i < MP; i += EM_NT) {
+        const float l = i < m ? z.d[(size_t)slot * m + i] : 0.0f;
+        lam[i] = l;
+        sig[i] = i < m ? sqrtf(l) : 0.0f;
+        bv[i] = i < m ? a.eb[(size_t)slot * m + i] : 0.0;
+    }
+    __syncthreads();
+
+    // 2. Z0 = Q diag(lambda^-1/2) Q'  (B = Q diag, A = B Q')
+    for (int i = tid; i < MP * MP; i += EM_NT) {
+        const int r = i / MP, c = i - r * MP;
+        B[r * LDA + c] = c < m ? Q[r * LDA + c] * rsqrtf(lam[c]) : 0.0f;
+    }
+    __syncthreads();
+    em::mm<R, false, true>(A, B, Q, m, LDA);
+    for (int i = tid; i < MP * MP; i += EM_NT) {
+        const int r = i / MP, c = i - r * MP;
+        z.z0[z0 + i] = A[r * LDA + c];
+    }
+
+    // 3a. P = M Z0 (double-float; M as its hi/lo pair, rows from global)
+    {
+        float ph[R][R], pl[R][R];
+#pragma unroll
+        for (int r = 0; r < R; ++r)
+#pragma unroll
+            for (int c = 0; c < R; ++c) ph[r][c] = pl[r][c] = 0.0f;
+        for (int k = 0; k < m; ++k) {
+            float2 mv[R];
+            float zv[R];
+#pragma unroll
+            for (int r = 0; r < R; ++r) {
+                const int i = ty + 16 * r;
+                mv[r] = i < m ? z.mhl[q0 + (size_t)i * m + k] : make_float2(0.0f, 0.0f);
+            }
+#pragma unroll
+            for (int c = 0; c < R; ++c) zv[c] = A[k * LDA + tx + 16 * c];
+#pragma unroll
+            for (int r = 0; r < R; ++r)
+#pragma unroll
+                for (int c = 0; c < R; ++c) em::df_fma(ph[r][c], pl[r][c], mv[r].x, mv[r].y, zv[c]);
+        }
+#pragma unroll
+        for (int r = 0; r < R; ++r)
+#pragma unroll
+            for (int c = 0; c < R; ++c)
+                z.p[z0 + (size_t)(ty + 16 * r) * MP + tx + 16 * c] = make_float2(ph[r][c], pl[r][c]);
+    }
+    __syncthreads();   // P complete in global memory for the whole CTA
+
+    // 3b. R = I - Z0 P (double-float), R_hi into B
+    {
+        float rh[R][R], rl[R][R];
+#pragma unroll
+        for (int r = 0; r < R; ++r)
+#pragma unroll
+            for (int c = 0; c < R; ++c) rh[r][c] = rl[r][c] = 0.0f;
+        for (int k0 = 0; k0 < m; k0 += EM_KCH) {
+            const int kn = (m - k0 < EM_KCH) ? m - k0 : EM_KCH;
+            for (int i = tid; i < kn * MP; i += EM_NT) {
+                const int kk = i / MP, c = i - kk * MP;
+                S[kk * MP + c] = z.p[z0 + (size_t)(k0 + kk) * MP + c];
+            }
+            __syncthreads();
+            for (int kk = 0; kk < kn; ++kk) {
+                float zv[R];
+                float2 pv[R];
+#pragma unroll
+                for (int r = 0; r < R; ++r) zv[r] = A[(ty + 16 * r) * LDA + k0 + kk];
+#pragma unroll
+                for (int c = 0; c < R; ++c) pv[c] = S[kk * MP + tx + 16 * c];
+#pragma unroll
+                for (int r = 0; r < R; ++r)
+#pragma unroll
+                    for (int c = 0; c < R; ++c) em::df_fma(rh[r][c], rl[r][c], pv[c].x, pv[c].y, zv[r]);
+            }
+            __syncthreads();
+        }
+#pragma unroll
+        for (int r = 0; r < R; ++r)
+#pragma unroll
+            for (int c = 0; c < R; ++c) {
+                const int i = ty + 16 * r, j = tx + 16 * c;
+                // (delta - hi) is exact near 1 (Sterbenz), then the low part
+                const float one = (i == j && i < m) ? 1.0f : 0.0f;
+                B[i * LDA + j] = (i < m && j < m) ? (one - rh[r][c]) - rl[r][c] : 0.0f;
+            }
+    }
+    __syncthreads();
+
+    // 4. D~ = Q' R Q, D~_ij /= (sigma_i + sigma_j), D = Q D~ Q'
+    em::mm<R, true, false>(A, Q, B, m, LDA);
+    em::mm<R, false, false>(B, A, Q, m, LDA);
+    for (int i = tid; i < MP * MP; i += EM_NT) {
+        const int r = i / MP, c = i - r * MP;
+        B[r * LDA + c] = (r < m && c < m) ? B[r * LDA + c] / (sig[r] + sig[c]) : 0.0f;
+    }
+    __syncthreads();
+    em::mm<R, false, false>(A, Q, B, m, LDA);
+    em::mm<R, false, true>(B, A, Q, m, LDA);
+
+    // 5. T = Z0 + D in FP64, relaxed and cast (transforms.c:1270-1296);
+    //    tr(M^-1) = |T|_F^2 for the degrees of freedom
+    const size_t tbase = (size_t)pt * md * m;
+    double tr = 0.0;
+    for (int i = tid; i < m * m; i += EM_NT) {
+        const int e1 = i / m, e2 = i - e1 * m;
+        const double t = (double)z.z0[z0 + (size_t)e1 * MP + e2] + (double)B[e1 * LDA + e2];
+        tr = fma(t, t, tr);
+        if (e1 < md && a.mode != ENKFG_MODE_ENOI && a.T != nullptr) {
+            const double tt = (e1 == e2) ? (t - 1.0) * a.alpha + 1.0 : t * a.alpha;
+            a.T[tbase + (size_t)e1 * m + e2] = (float)tt;
+            if (a.T64) a.T64[tbase + (size_t)e1 * m + e2] = tt;
+        }
+    }
+    const double trinv = la::block_sum<EM_NT>(tr, red);
+
+    // 6. w = M^-1 S's by iterative refinement: r = S's - M w in FP64 (M from
+    //    the slot's FP64 upper triangle), w += Q diag(1/lambda) Q' r in FP32
+    for (int i = tid; i < MP; i += EM_NT) {
+        wv[i] = 0.0;
+        rv[i] = bv[i];
+    }
+    __syncthreads();
+    for (int it = 0; it < 3; ++it) {
+        if (tid < m) {
+            float t = 0.0f;
+            for (int k = 0; k < m; ++k) t = fmaf(Q[k * LDA + tid], (float)rv[k], t);
+            vt[tid] = t / lam[tid];
+        }
+        __syncthreads();
+        if (tid < m) {
+            float y = 0.0f;
+            for (int k = 0; k < m; ++k) y = fmaf(Q[tid * LDA + k], vt[k], y);
+            wv[tid] += (double)y;
+        }
+        __syncthreads();
+        if (tid < m) {
+            double r = bv[tid];
+            for (int k = 0; k < m; ++k) {
+                const double mik = (k >= tid) ? a.eq[q0 + (size_t)tid * m + k] : a.eq[q0 + (size_t)k * m + tid];
+                r = fma(-mik, wv[k], r);
+            }
+            rv[tid] = r;
+        }
+        __syncthreads();
+    }
+    if (tid < m) {
+        a.w[(size_t)pt * m + tid] = (float)wv[tid];
+        if (a.w64) a.w64[(size_t)pt * m + tid] = wv[tid];
+    }
+    if (a.want_diag) diag_single(a, pt, (int)pd, (double)m - trinv, trss);
+}
+
+bool etkf_mixed_supported(int m) { return m >= 2 && m <= 96; }
+
+template <int R>
+static size_t em_refine_smem()
+{
+    constexpr int MP = 16 * R, LDA = MP + 1;
+    return (size_t)3 * MP * LDA * 4 + (size_t)EM_KCH * MP * 8 + (size_t)4 * MP * 4 + (size_t)3 * MP * 8 +
+           (EM_NT / 32) * 8;
+}
+
+template <int R>
+static enkfg_status em_launch_refine(enkfg_ctx* ctx, const CalcArgs& b, const EmSlots& z, int nb, cudaStream_t st)
+{
+    const size_t smem = em_refine_smem<R>();
+    CK(cudaFuncSetAttribute(k_em_refine<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    k_em_refine<R><<<nb, EM_NT, smem, st>>>(b, z);
+    CKL();
+    return ENKFG_OK;
+}
+
+// The mixed-precision ETKF transform stage in batches of points: the
+// transform kernel (S'S and S's on the tensor cores, M saved per slot), then
+// the FP32 eigendecomposition and the refined solve of every slot.
+enkfg_status run_etkf_mixed(enkfg_ctx* ctx, const CalcArgs& a0, cudaStream_t st)
+{
+    enkfg_status s;
+    const int m = a0.m, nitems = a0.nitems;
+    // the register tile of the refinement kernel: R = 2, 3, 4 or 6 (16 R >= m)
+    int R = (m + 15) / 16;
+    if (R < 2) R = 2;
+    if (R == 5) R = 6;
+    const int MP = 16 * R;
+    const int rcap = m * m + 64 * m;         // QL typically needs about 0.75 m^2 rotations
+    const int hcap = 8 * m;
+    const size_t per = (size_t)m * m * 8 + (size_t)3 * m * 8 + 16     // M, S's, aux (FP64 slots)
+                       + (size_t)m * m * 12 + (size_t)2 * m * 4           // Q, M hi/lo, d, e
+                       + (size_t)rcap * 8 + (size_t)hcap * 8 + 4          // rotation log
+                       + (size_t)MP * MP * 12;                            // Z0, P
+    size_t B = ((size_t)8 << 30) / per;      // about 8 GB of scratch per batch
+    if (B < 256) B = 256;
+    if (B > (size_t)nitems) B = (size_t)nitems;
+    if ((s = ensure(ctx, &ctx->d_eq, &ctx->eq_cap, B * m * m))) return s;
+    if ((s = ensure(ctx, &ctx->d_eb, &ctx->eb_cap, B * m))) return s;
+    if ((s = ensure(ctx, &ctx->d_eaux, &ctx->eaux_cap, B * 2))) return s;
+    if ((s = ensure(ctx, &ctx->d_emq, &ctx->emq_cap, B * m * m))) return s;
+    if ((s = ensure(ctx, &ctx->d_emmhl, &ctx->emmhl_cap, B * m * m))) return s;
+    if ((s = ensure(ctx, &ctx->d_emd, &ctx->emd_cap, B * m))) return s;
+    if ((s = ensure(ctx, &ctx->d_eme, &ctx->eme_cap, B * m))) return s;
+    if ((s = ensure(ctx, &ctx->d_emrot, &ctx->emrot_cap, B * rcap))) return s;
+    if ((s = ensure(ctx, &ctx->d_emhdr, &ctx->emhdr_cap, B * hcap))) return s;
+    if ((s = ensure(ctx, &ctx->d_emnh, &ctx->emnh_cap, B))) return s;
+    if ((s = ensure(ctx, &ctx->d_emz0, &ctx->emz0_cap, B * MP * MP))) return s;
+    if ((s = ensure(ctx, &ctx->d_emp, &ctx->emp_cap, B * MP * MP))) return s;
+    EmSlots z;
+    z.q = ctx->d_emq;
+    z.mhl = ctx->d_emmhl;
+    z.d = ctx->d_emd;
+    z.e = ctx->d_eme;
+    z.rot = ctx->d_emrot;
+    z.hdr = ctx->d_emhdr;
+    z.nh = ctx->d_emnh;
+    z.z0 = ctx->d_emz0;
+    z.p = ctx->d_emp;
+    z.rcap = rcap;
+    z.hcap = hcap;
+    z.mp = MP;
+    const int lda = m + 1;
+    const size_t tsmem = ((size_t)m * lda + 2 * (size_t)m + EM_TRED_NT / 32) * 4 + 16;
+    const size_t qsmem = (size_t)2 * m * EM_QL_T * 4;
+    const size_t rsmem = ((size_t)m * lda + 4 * (size_t)m) * 4 + 16;
+    CK(cudaFuncSetAttribute(k_em_tred, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tsmem));
+    CK(cudaFuncSetAttribute(k_em_ql, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)qsmem));
+    CK(cudaFuncSetAttribute(k_em_replay, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rsmem));
+    for (int i0 = 0; i0 < nitems; i0 += (int)B) {
+        const int nb = (nitems - i0 < (int)B) ? nitems - i0 : (int)B;
+        CalcArgs b = a0;
+        b.defer = 1;
+        b.nitems = nb;
+        if (a0.order) {
+            b.order = a0.order + i0;
+            b.item0 = 0;
+        } else {
+            b.item0 = a0.item0 + i0;
+        }
+        b.eq = ctx->d_eq;
+        b.eb = ctx->d_eb;
+        b.eaux = ctx->d_eaux;
+        if (b.persistent) CK(cudaMemsetAsync(ctx->d_qhead, 0, sizeof(int), st));
+        batch_mark(ctx, 0, st);
+        if ((s = launch_mixed(ctx, b, st))) return s;
+        batch_mark(ctx, 1, st);
+        k_em_tred<<<nb, EM_TRED_NT, tsmem, st>>>(b, z);
+        CKL();
+        k_em_ql<<<div_up(nb, EM_QL_T), EM_QL_T, qsmem, st>>>(nb, m, ctx->d_eaux, z);
+        CKL();
+        k_em_replay<<<nb, EM_REPLAY_NT, rsmem, st>>>(b, z);
+        CKL();
+        switch (R) {
+        case 2: s = em_launch_refine<2>(ctx, b, z, nb, st); break;
+        case 3: s = em_launch_refine<3>(ctx, b, z, nb, st); break;
+        case 4: s = em_launch_refine<4>(ctx, b, z, nb, st); break;
+        case 6: s = em_launch_refine<6>(ctx, b, z, nb, st); break;
+        default:
+            set_err(ctx, "the refined ETKF solve supports nmem <= 96 (got %d)", m);
+            return ENKFG_EUNSUPPORTED;
+        }
+        if (s) return s;
+        batch_mark(ctx, 2, st);
+    }
+    return ENKFG_OK;
+}

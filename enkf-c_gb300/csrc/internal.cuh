@@ -9,6 +9,8 @@
 
 #define ENKFG_VERSION 1
 
+struct CalcArgs;
+
 // default bound on a device wait (mixed path: waits for the tensor cores)
 #define ENKFG_DEFAULT_WAIT_NS 2000000000ull
 // per-point status a transform kernel records when a bounded wait expired
@@ -51,6 +53,7 @@ struct enkfg_ctx {
     char err[1024];
     long long launches;
     unsigned long long wait_ns; // bound on a device wait (enkfg_set_wait_limit)
+    int wait_drill;             // enkfg_set_wait_drill
     float stage_ms[4];
     cudaEvent_t ev[10];         // [8, 9]: the transform kernel alone (first batch)
 
@@ -149,6 +152,24 @@ struct enkfg_ctx {
     int2* d_ehdr;               // [slots][hcap]
     int* d_enh;                 // [slots]
     size_t eq_cap, ed_cap, ee_cap, eb_cap, eaux_cap, eval_cap, erot_cap, ehdr_cap, enh_cap;
+
+    // refined mixed-precision ETKF solve scratch (per slot; etkf_mixed.cu)
+    float* d_emq;               // [slots][m][m]
+    float2* d_emmhl;            // [slots][m][m]
+    float* d_emd;               // [slots][m]
+    float* d_eme;               // [slots][m]
+    float2* d_emrot;            // [slots][rcap]
+    int2* d_emhdr;              // [slots][hcap]
+    int* d_emnh;                // [slots]
+    float* d_emz0;              // [slots][MP][MP]
+    float2* d_emp;              // [slots][MP][MP]
+    size_t emq_cap, emmhl_cap, emd_cap, eme_cap, emrot_cap, emhdr_cap, emnh_cap, emz0_cap, emp_cap;
+    // per-batch timing of the last transform stage: events before the
+    // transform kernel, after it and after the batch's solve kernels
+#define ENKFG_TIMED_BATCHES 256
+    cudaEvent_t bev[3 * ENKFG_TIMED_BATCHES];
+    int nbev;                   // events created so far
+    int nbatch;                 // batches marked in the last transform stage
 
     // work queue / scratch
     int* d_counts;              // [npoints]
@@ -253,6 +274,14 @@ enkfg_status count_local(enkfg_ctx* ctx, int* d_counts, int* d_pcounts, cudaStre
 enkfg_status count_candidates(enkfg_ctx* ctx, int* d_counts, cudaStream_t st);
 enkfg_status list_local(enkfg_ctx* ctx, const long long* d_offsets, int* d_ids, double* d_coeffs, cudaStream_t st);
 enkfg_status run_transforms(enkfg_ctx* ctx, const enkfg_calc_params* p, cudaStream_t st);
+// per-batch timing (calc.cu): k = 0 before a batch's transform kernel, 1
+// after it, 2 after the batch's solve kernels
+void batch_mark(enkfg_ctx* ctx, int k, cudaStream_t st);
+// the transform stage's FP32 eigendecomposition + refined solve for ETKF on
+// the mixed path (etkf_mixed.cu); false if nmem is beyond its register tiles
+bool etkf_mixed_supported(int m);
+enkfg_status run_etkf_mixed(enkfg_ctx* ctx, const CalcArgs& a0, cudaStream_t st);
+enkfg_status launch_mixed(enkfg_ctx* ctx, CalcArgs& a, cudaStream_t st);
 // CTAs of `fn` (nt threads, dsmem bytes of dynamic shared memory) that fit on
 // one SM at once, from the shared memory (with the per-block reserve),
 // register and thread limits of the device; and the shared-memory carveout

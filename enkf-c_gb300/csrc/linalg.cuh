@@ -18,19 +18,36 @@
 // (calcs.c:103-132).  For M = I + S'S (eigenvalues >= 1) both are stable, so
 // the results agree with LAPACK's to a few units of rounding times the
 // condition of M.
+//
+// The eigensolver routines are templates on the scalar type F: double for
+// the FP64 solve, float for the FP32 decomposition that seeds the refined
+// inverse square root of the mixed-precision path.
 #pragma once
 
 namespace la {
 
-template <int NT>
-__device__ __forceinline__ double block_sum(double v, double* red)
+// unit roundoff used by the QL convergence test: 2^-52 (double), 2^-23 (float)
+template <typename F> struct Eps;
+template <> struct Eps<double> { static constexpr double value = 2.220446049250313e-16; };
+template <> struct Eps<float> { static constexpr float value = 1.1920929e-07f; };
+
+// (c, s) pair of a logged rotation
+template <typename F> struct Vec2;
+template <> struct Vec2<double> { typedef double2 type; };
+template <> struct Vec2<float> { typedef float2 type; };
+
+__device__ __forceinline__ double rsq(double x) { return rsqrt(x); }
+__device__ __forceinline__ float rsq(float x) { return rsqrtf(x); }
+
+template <int NT, typename F>
+__device__ __forceinline__ F block_sum(F v, F* red)
 {
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
     int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     __syncthreads();
     if (lane == 0) red[wid] = v;
     __syncthreads();
-    double s = 0.0;
+    F s = F(0);
 #pragma unroll
     for (int w = 0; w < NT / 32; ++w) s += red[w];
     return s;
@@ -41,35 +58,35 @@ __device__ __forceinline__ double block_sum(double v, double* red)
 // return A holds the orthogonal Q, d the diagonal and e the off-diagonal of
 // the tridiagonal matrix in QL form (e[i] couples i and i+1, e[n-1] = 0).
 // red: NT/32 doubles.
-template <int NT>
-__device__ void tred2(double* A, int n, int lda, double* d, double* e, double* red)
+template <int NT, typename F>
+__device__ void tred2(F* A, int n, int lda, F* d, F* e, F* red)
 {
     const int tid = threadIdx.x;
     // ---- Householder reduction (rows n-1 .. 1) ----
     for (int i = n - 1; i >= 1; --i) {
         int l = i - 1;
-        double* Ai = A + (size_t)i * lda;
-        double h = 0.0;
+        F* Ai = A + (size_t)i * lda;
+        F h = F(0);
         if (l > 0) {
-            double part = 0.0;
+            F part = F(0);
             for (int k = tid; k <= l; k += NT) part += fabs(Ai[k]);
-            double scale = block_sum<NT>(part, red);
-            if (scale == 0.0) {
+            F scale = block_sum<NT>(part, red);
+            if (scale == F(0)) {
                 if (tid == 0) e[i] = Ai[l];
                 __syncthreads();
             } else {
                 // one division a step, multiplications per element (FP64
                 // division is a long instruction sequence on GB300)
-                const double iscale = 1.0 / scale;
-                part = 0.0;
+                const F iscale = F(1) / scale;
+                part = F(0);
                 for (int k = tid; k <= l; k += NT) {
-                    double v = Ai[k] * iscale;
+                    F v = Ai[k] * iscale;
                     Ai[k] = v;
                     part += v * v;
                 }
                 h = block_sum<NT>(part, red);
-                double f = Ai[l];
-                double g = (f >= 0.0) ? -sqrt(h) : sqrt(h);
+                F f = Ai[l];
+                F g = (f >= F(0)) ? -sqrt(h) : sqrt(h);
                 h -= f * g;
                 __syncthreads();
                 if (tid == 0) {
@@ -78,20 +95,20 @@ __device__ void tred2(double* A, int n, int lda, double* d, double* e, double* r
                 }
                 __syncthreads();
                 // p = A u / h (into e[0..l]); column i keeps u / h
-                const double ih = 1.0 / h;
+                const F ih = F(1) / h;
                 for (int j = tid; j <= l; j += NT) {
-                    double g2 = 0.0;
-                    const double* Aj = A + (size_t)j * lda;
+                    F g2 = F(0);
+                    const F* Aj = A + (size_t)j * lda;
                     for (int k = 0; k <= j; ++k) g2 += Aj[k] * Ai[k];
                     for (int k = j + 1; k <= l; ++k) g2 += A[(size_t)k * lda + j] * Ai[k];
                     e[j] = g2 * ih;
                 }
                 __syncthreads();
                 for (int j = tid; j <= l; j += NT) A[(size_t)j * lda + i] = Ai[j] * ih;
-                part = 0.0;
+                part = F(0);
                 for (int j = tid; j <= l; j += NT) part += e[j] * Ai[j];
-                double ff = block_sum<NT>(part, red);
-                double hh = ff / (h + h);
+                F ff = block_sum<NT>(part, red);
+                F hh = ff / (h + h);
                 for (int j = tid; j <= l; j += NT) e[j] = e[j] - hh * Ai[j];
                 __syncthreads();
                 // rank-2 update of the lower triangle rows 0..l
@@ -113,17 +130,17 @@ __device__ void tred2(double* A, int n, int lda, double* d, double* e, double* r
         __syncthreads();
     }
     if (tid == 0) {
-        d[0] = 0.0;
-        e[0] = 0.0;
+        d[0] = F(0);
+        e[0] = F(0);
     }
     __syncthreads();
     // ---- accumulate the transformations ----
     for (int i = 0; i < n; ++i) {
         int l = i - 1;
-        double* Ai = A + (size_t)i * lda;
-        if (d[i] != 0.0) {
+        F* Ai = A + (size_t)i * lda;
+        if (d[i] != F(0)) {
             for (int j = tid; j <= l; j += NT) {
-                double g = 0.0;
+                F g = F(0);
                 for (int k = 0; k <= l; ++k) g += Ai[k] * A[(size_t)k * lda + j];
                 for (int k = 0; k <= l; ++k) A[(size_t)k * lda + j] -= g * A[(size_t)k * lda + i];
             }
@@ -131,15 +148,15 @@ __device__ void tred2(double* A, int n, int lda, double* d, double* e, double* r
         __syncthreads();
         if (tid == 0) d[i] = Ai[i];
         for (int j = tid; j <= l; j += NT) {
-            A[(size_t)j * lda + i] = 0.0;
-            Ai[j] = 0.0;
+            A[(size_t)j * lda + i] = F(0);
+            Ai[j] = F(0);
         }
-        if (tid == 0) Ai[i] = 1.0;
+        if (tid == 0) Ai[i] = F(1);
         __syncthreads();
     }
     if (tid == 0) {
         for (int i = 1; i < n; ++i) e[i - 1] = e[i];
-        e[n - 1] = 0.0;
+        e[n - 1] = F(0);
     }
     __syncthreads();
 }
@@ -148,8 +165,8 @@ __device__ void tred2(double* A, int n, int lda, double* d, double* e, double* r
 // the rows of A: on return column k of A is the eigenvector of eigenvalue
 // d[k].  cs, sn: scratch of n doubles each; ctl: 4 ints.  Returns 0 or 1 (QL
 // did not converge).
-template <int NT>
-__device__ int tql2(double* A, int n, int lda, double* d, double* e, double* cs, double* sn, int* ctl)
+template <int NT, typename F>
+__device__ int tql2(F* A, int n, int lda, F* d, F* e, F* cs, F* sn, int* ctl)
 {
     const int tid = threadIdx.x;
     if (tid == 0) ctl[3] = 0;
@@ -160,8 +177,8 @@ __device__ int tql2(double* A, int n, int lda, double* d, double* e, double* cs,
             if (tid == 0) {
                 int m;
                 for (m = l; m < n - 1; ++m) {
-                    double dd = fabs(d[m]) + fabs(d[m + 1]);
-                    if (fabs(e[m]) <= 2.220446049250313e-16 * dd) break;
+                    F dd = fabs(d[m]) + fabs(d[m + 1]);
+                    if (fabs(e[m]) <= Eps<F>::value * dd) break;
                 }
                 ctl[0] = m;
                 if (m != l) {
@@ -169,10 +186,10 @@ __device__ int tql2(double* A, int n, int lda, double* d, double* e, double* cs,
                         ctl[0] = l;
                         ctl[3] = 1;
                     } else {
-                        double g = (d[l + 1] - d[l]) / (2.0 * e[l]);
-                        double r = sqrt(fma(g, g, 1.0));
+                        F g = (d[l + 1] - d[l]) / (F(2) * e[l]);
+                        F r = sqrt(fma(g, g, F(1)));
                         g = d[m] - d[l] + e[l] / (g + copysign(r, g));
-                        double s = 1.0, c = 1.0, p = 0.0;
+                        F s = F(1), c = F(1), p = F(0);
                         int i;
                         bool underflow = false;
                         // This loop is one thread's chain of dependent FP64
@@ -181,22 +198,22 @@ __device__ int tql2(double* A, int n, int lda, double* d, double* e, double* cs,
                         // square root and multiplies (no hypot, no divides).
                         // f and g stay far from overflow for M = I + S'S.
                         for (i = m - 1; i >= l; --i) {
-                            double f = s * e[i], b = c * e[i];
-                            const double t = fma(f, f, g * g);
-                            if (t == 0.0) {
-                                e[i + 1] = 0.0;
+                            F f = s * e[i], b = c * e[i];
+                            const F t = fma(f, f, g * g);
+                            if (t == F(0)) {
+                                e[i + 1] = F(0);
                                 d[i + 1] -= p;
-                                e[m] = 0.0;
+                                e[m] = F(0);
                                 underflow = true;
                                 break;
                             }
-                            const double ri = rsqrt(t);
+                            const F ri = rsq(t);
                             r = t * ri;
                             e[i + 1] = r;
                             s = f * ri;
                             c = g * ri;
                             g = d[i + 1] - p;
-                            r = (d[i] - g) * s + 2.0 * c * b;
+                            r = (d[i] - g) * s + F(2) * c * b;
                             p = s * r;
                             d[i + 1] = g + p;
                             g = c * r - b;
@@ -208,7 +225,7 @@ __device__ int tql2(double* A, int n, int lda, double* d, double* e, double* cs,
                         if (!underflow) {
                             d[l] -= p;
                             e[l] = g;
-                            e[m] = 0.0;
+                            e[m] = F(0);
                         }
                     }
                 }
@@ -219,12 +236,12 @@ __device__ int tql2(double* A, int n, int lda, double* d, double* e, double* cs,
             ++iter;
             int i_hi = ctl[1], i_lo = ctl[2];
             for (int k = tid; k < n; k += NT) {
-                double* Ak = A + (size_t)k * lda;
+                F* Ak = A + (size_t)k * lda;
                 if (i_hi >= i_lo) {
-                    double carry = Ak[i_hi + 1];
+                    F carry = Ak[i_hi + 1];
                     for (int i = i_hi; i >= i_lo; --i) {
-                        double zi = Ak[i];
-                        double c = cs[i], s = sn[i];
+                        F zi = Ak[i];
+                        F c = cs[i], s = sn[i];
                         Ak[i + 1] = s * zi + c * carry;
                         carry = c * zi - s * carry;
                     }
@@ -241,9 +258,8 @@ __device__ int tql2(double* A, int n, int lda, double* d, double* e, double* cs,
 // On return: column k of A is the eigenvector of eigenvalue d[k].
 // e, cs, sn: scratch of n doubles each; ctl: 4 ints; red: NT/32 doubles.
 // Returns 0 or 1 (QL did not converge).
-template <int NT>
-__device__ int eig_sym(double* A, int n, int lda, double* d, double* e, double* cs, double* sn, int* ctl,
-                       double* red)
+template <int NT, typename F>
+__device__ int eig_sym(F* A, int n, int lda, F* d, F* e, F* cs, F* sn, int* ctl, F* red)
 {
     tred2<NT>(A, n, lda, d, e, red);
     return tql2<NT>(A, n, lda, d, e, cs, sn, ctl);
@@ -256,7 +272,8 @@ __device__ int eig_sym(double* A, int n, int lda, double* d, double* e, double* 
 // (c, s) of every rotation in order, hdr[] one (first, last) index pair per QL
 // sweep (rotations i = first down to last; first < last: none).  Returns 0,
 // 1 (no convergence) or 2 (the log capacity rcap / hcap was exceeded).
-__device__ inline int ql_chain(double* d, double* e, int n, int ds, double2* rot, int rcap, int2* hdr, int hcap,
+template <typename F>
+__device__ inline int ql_chain(F* d, F* e, int n, int ds, typename Vec2<F>::type* rot, int rcap, int2* hdr, int hcap,
                                int* nh_out)
 {
     int nr = 0, nh = 0;
@@ -265,46 +282,48 @@ __device__ inline int ql_chain(double* d, double* e, int n, int ds, double2* rot
         for (;;) {
             int mm;
             for (mm = l; mm < n - 1; ++mm) {
-                const double dd = fabs(d[mm * ds]) + fabs(d[(mm + 1) * ds]);
-                if (fabs(e[mm * ds]) <= 2.220446049250313e-16 * dd) break;
+                const F dd = fabs(d[mm * ds]) + fabs(d[(mm + 1) * ds]);
+                if (fabs(e[mm * ds]) <= Eps<F>::value * dd) break;
             }
             if (mm == l) break;
             if (iter >= 60) return 1;
             ++iter;
             if (nh >= hcap || nr + (mm - l) > rcap) return 2;
-            double g = (d[(l + 1) * ds] - d[l * ds]) / (2.0 * e[l * ds]);
-            double r = sqrt(fma(g, g, 1.0));
+            F g = (d[(l + 1) * ds] - d[l * ds]) / (F(2) * e[l * ds]);
+            F r = sqrt(fma(g, g, F(1)));
             g = d[mm * ds] - d[l * ds] + e[l * ds] / (g + copysign(r, g));
-            double sv = 1.0, c = 1.0, p = 0.0;
+            F sv = F(1), c = F(1), p = F(0);
             int i;
             bool underflow = false;
             for (i = mm - 1; i >= l; --i) {
-                const double f = sv * e[i * ds], b = c * e[i * ds];
-                const double t = fma(f, f, g * g);
-                if (t == 0.0) {
-                    e[(i + 1) * ds] = 0.0;
+                const F f = sv * e[i * ds], b = c * e[i * ds];
+                const F t = fma(f, f, g * g);
+                if (t == F(0)) {
+                    e[(i + 1) * ds] = F(0);
                     d[(i + 1) * ds] -= p;
-                    e[mm * ds] = 0.0;
+                    e[mm * ds] = F(0);
                     underflow = true;
                     break;
                 }
-                const double ri = rsqrt(t);
+                const F ri = rsq(t);
                 r = t * ri;
                 e[(i + 1) * ds] = r;
                 sv = f * ri;
                 c = g * ri;
                 g = d[(i + 1) * ds] - p;
-                r = (d[i * ds] - g) * sv + 2.0 * c * b;
+                r = (d[i * ds] - g) * sv + F(2) * c * b;
                 p = sv * r;
                 d[(i + 1) * ds] = g + p;
                 g = c * r - b;
-                rot[nr++] = make_double2(c, sv);
+                rot[nr].x = c;
+                rot[nr].y = sv;
+                ++nr;
             }
             hdr[nh++] = make_int2(mm - 1, underflow ? i + 1 : l);
             if (!underflow) {
                 d[l * ds] -= p;
                 e[l * ds] = g;
-                e[mm * ds] = 0.0;
+                e[mm * ds] = F(0);
             }
         }
     }
@@ -316,21 +335,21 @@ __device__ inline int ql_chain(double* d, double* e, int n, int ds, double2* rot
 // giving the eigenvectors in the columns as tql2 does.  Rows are
 // independent, one thread each; the log is read through the read-only cache
 // (every thread reads the same rotation: a broadcast).
-template <int NT>
-__device__ void ql_replay(double* A, int n, int lda, const double2* __restrict__ rot, const int2* __restrict__ hdr,
-                          int nh)
+template <int NT, typename F>
+__device__ void ql_replay(F* A, int n, int lda, const typename Vec2<F>::type* __restrict__ rot,
+                          const int2* __restrict__ hdr, int nh)
 {
     for (int k = threadIdx.x; k < n; k += NT) {
-        double* Ak = A + (size_t)k * lda;
+        F* Ak = A + (size_t)k * lda;
         int r = 0;
         for (int h = 0; h < nh; ++h) {
             const int2 hl = __ldg(hdr + h);
             if (hl.x >= hl.y) {
-                double carry = Ak[hl.x + 1];
+                F carry = Ak[hl.x + 1];
                 for (int i = hl.x; i >= hl.y; --i) {
-                    const double2 q = __ldg(rot + r);
+                    const typename Vec2<F>::type q = __ldg(rot + r);
                     ++r;
-                    const double zi = Ak[i];
+                    const F zi = Ak[i];
                     Ak[i + 1] = q.y * zi + q.x * carry;
                     carry = q.x * zi - q.y * carry;
                 }

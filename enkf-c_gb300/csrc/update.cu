@@ -806,12 +806,15 @@ enkfg_status run_hybrid(enkfg_ctx* ctx, int nmem, int nmem_d, double gamma, int 
 // The field-layer levels of one launch group go to the device only when they
 // differ from the group last uploaded (no host-to-device copy in a steady
 // cycle, which CUDA graphs capture).  Synchronous copy: it is rare.
-static enkfg_status upload_levels(enkfg_ctx* ctx, const int* levels, int nf, int* d_levels)
+// The field-layers' levels on the device, copied only when they change: in
+// stream order on `st` (after the kernels that read the previous ones), from
+// the context's host copy.
+static enkfg_status upload_levels(enkfg_ctx* ctx, const int* levels, int nf, int* d_levels, cudaStream_t st)
 {
     if (ctx->n_levels == nf && memcmp(ctx->h_levels, levels, nf * sizeof(int)) == 0) return ENKFG_OK;
-    CK(cudaMemcpy(d_levels, levels, nf * sizeof(int), cudaMemcpyHostToDevice));
     memcpy(ctx->h_levels, levels, nf * sizeof(int));
     ctx->n_levels = nf;
+    CK(cudaMemcpyAsync(d_levels, ctx->h_levels, nf * sizeof(int), cudaMemcpyHostToDevice, st));
     return ENKFG_OK;
 }
 
@@ -869,14 +872,13 @@ enkfg_status run_update(enkfg_ctx* ctx, const enkfg_update_params* p, const int*
     if (p->mode == ENKFG_MODE_ENOI) {
         for (int f0 = 0; f0 < nfield; f0 += 448) {
             int nf = nfield - f0 < 448 ? nfield - f0 : 448;
-            if ((s = upload_levels(ctx, levels + f0, nf, d_levels))) return s;
+            if ((s = upload_levels(ctx, levels + f0, nf, d_levels, st))) return s;
             a.levels = d_levels;
             a.nfield = nf;
             a.fields = d_fields + (size_t)f0 * (a.m + 1) * a.plane;
             dim3 g(div_up(a.mni, 128), a.jsize);
             k_update_bg<<<g, 128, 0, st>>>(a);
             CKL();
-            CK(cudaStreamSynchronize(st));
         }
         cudaEventRecord(ctx->ev[5], st);
         return ENKFG_OK;
@@ -895,7 +897,7 @@ enkfg_status run_update(enkfg_ctx* ctx, const enkfg_update_params* p, const int*
                 CK(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
                 for (int f0 = 0; f0 < nfield; f0 += 448) {
                     int nf = nfield - f0 < 448 ? nfield - f0 : 448;
-                    if ((s = upload_levels(ctx, levels + f0, nf, d_levels))) return s;
+                    if ((s = upload_levels(ctx, levels + f0, nf, d_levels, st))) return s;
                     a.levels = d_levels;
                     a.nfield = nf;
                     a.fields = d_fields + (size_t)f0 * a.m * a.plane;
@@ -903,7 +905,6 @@ enkfg_status run_update(enkfg_ctx* ctx, const enkfg_update_params* p, const int*
                     dim3 g(div_up(a.mni, UPC_NC), a.jsize);
                     kern<<<g, UPC_NT, smem, st>>>(a, sstride);
                     CKL();
-                    if (f0 + 448 < nfield) CK(cudaStreamSynchronize(st));
                 }
                 cudaEventRecord(ctx->ev[5], st);
                 return ENKFG_OK;
@@ -953,18 +954,23 @@ enkfg_status run_update(enkfg_ctx* ctx, const enkfg_update_params* p, const int*
     else CK(cudaFuncSetAttribute(k_update_v2<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     a.G = G;
     a.nk = G * a.stride;
-    for (int f0 = 0; f0 < nfield; f0 += fg) {
-        int nf = nfield - f0 < fg ? nfield - f0 : fg;
-        if ((s = upload_levels(ctx, levels + f0, nf, d_levels))) return s;
-        a.levels = d_levels;
-        a.nfield = nf;
-        a.fields = d_fields + (size_t)f0 * a.m * a.plane;
-        a.infl = d_infl ? d_infl + (size_t)f0 * a.plane : nullptr;
-        dim3 g(div_up(a.ni, G), a.jsize);
-        if (f64) k_update_v2<true><<<g, UPD_NT, smem, st>>>(a);
-        else k_update_v2<false><<<g, UPD_NT, smem, st>>>(a);
-        CKL();
-        if (f0 + fg < nfield) CK(cudaStreamSynchronize(st));
+    // the levels of up to 448 field-layers go to the device once; launch
+    // groups index into them, so nothing waits between groups (and the
+    // steady cycle, with unchanged levels, makes no host copy)
+    for (int g0 = 0; g0 < nfield; g0 += 448) {
+        const int ng = nfield - g0 < 448 ? nfield - g0 : 448;
+        if ((s = upload_levels(ctx, levels + g0, ng, d_levels, st))) return s;
+        for (int f0 = g0; f0 < g0 + ng; f0 += fg) {
+            const int nf = g0 + ng - f0 < fg ? g0 + ng - f0 : fg;
+            a.levels = d_levels + (f0 - g0);
+            a.nfield = nf;
+            a.fields = d_fields + (size_t)f0 * a.m * a.plane;
+            a.infl = d_infl ? d_infl + (size_t)f0 * a.plane : nullptr;
+            dim3 g(div_up(a.ni, G), a.jsize);
+            if (f64) k_update_v2<true><<<g, UPD_NT, smem, st>>>(a);
+            else k_update_v2<false><<<g, UPD_NT, smem, st>>>(a);
+            CKL();
+        }
     }
     cudaEventRecord(ctx->ev[5], st);
     return ENKFG_OK;

@@ -71,6 +71,12 @@ ENKFG_API void enkfg_destroy(enkfg_ctx* ctx);
  * memory, and enkfg_calc_transforms returns ENKFG_ETIMEOUT.  The context
  * stays usable. */
 ENKFG_API enkfg_status enkfg_set_wait_limit(enkfg_ctx* ctx, unsigned long long ns);
+/* A drill of that timeout path, off by default; no counterpart in the
+ * reference.  With `on`, every CTA of the mixed-precision transform kernel
+ * first waits (within the bound above) on an mbarrier that nothing arrives
+ * at, so the wait expires: the call returns ENKFG_ETIMEOUT without a fault
+ * or a hang, and the context stays usable once the drill is off. */
+ENKFG_API enkfg_status enkfg_set_wait_drill(enkfg_ctx* ctx, int on);
 ENKFG_API const char* enkfg_last_error(const enkfg_ctx* ctx);
 ENKFG_API const char* enkfg_status_string(enkfg_status st);
 ENKFG_API int enkfg_version(void);
@@ -299,9 +305,9 @@ ENKFG_API long long enkfg_kernel_launches(const enkfg_ctx* ctx);
  * values of their last eager run. */
 ENKFG_API enkfg_status enkfg_stage_times(const enkfg_ctx* ctx, float* ms4);
 /* The last transform stage split in milliseconds (CUDA events on the
- * launching stream): [0] the transform kernel (the first batch's, when the
- * stage runs in batches), [1] from its end to the end of the stage (the
- * batched eigensolver or inverse, later batches).  No reference
+ * launching stream, summed over the stage's batches): [0] the transform
+ * kernels (local observations, S'S and S's), [1] the solve kernels after
+ * them (the batched eigensolver, refined solve or inverse).  No reference
  * counterpart: it refines stage [2] of enkfg_stage_times. */
 ENKFG_API enkfg_status enkfg_kernel_times(const enkfg_ctx* ctx, float* ms2);
 

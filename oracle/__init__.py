@@ -120,7 +120,8 @@ class CalcParams(C.Structure):
     _fields_ = [("mode", C.c_int), ("scheme", C.c_int), ("nmem", C.c_int), ("nmem_dynamic", C.c_int),
                 ("alpha", C.c_double), ("stride", C.c_int), ("mni", C.c_int), ("mnj", C.c_int),
                 ("x", C.POINTER(C.c_double)), ("y", C.POINTER(C.c_double)),
-                ("x2d", C.POINTER(C.c_double)), ("y2d", C.POINTER(C.c_double))]
+                ("x2d", C.POINTER(C.c_double)), ("y2d", C.POINTER(C.c_double)), ("ii0", C.c_int),
+                ("ii1", C.c_int)]
 
 
 class UpdateParams(C.Structure):
@@ -269,11 +270,13 @@ def standardise(S, s_f, estd, otype, rfactor):
 
 
 def calctransforms(obs: ObsSet, *, mode, scheme, nmem, nmem_dynamic, alpha, stride, x, y, S, s,
-                   rows=None, threads: int = 1, want64=False, want_diag=True, x2d=None, y2d=None):
+                   rows=None, threads: int = 1, want64=False, want_diag=True, x2d=None, y2d=None, units=None):
     """das_calctransforms over strided rows `rows` (default all; a (first,
     last+1) tuple or a list of rows), run on `threads` host threads
-    (contiguous row blocks, as distribute_iterations assigns them).  Returns a
-    dict of full-size outputs (rows not computed stay zero)."""
+    (contiguous row blocks, as distribute_iterations assigns them); or, with
+    `units`, over a list of (row, first column, end column) pieces taken
+    from a shared queue by the threads as they come free.  Returns a dict of
+    full-size outputs (points not computed stay zero)."""
     x = np.ascontiguousarray(x, np.float64)
     y = np.ascontiguousarray(y, np.float64)
     mni = x.size if x2d is None else x2d.shape[1]
@@ -298,7 +301,42 @@ def calctransforms(obs: ObsSet, *, mode, scheme, nmem, nmem_dynamic, alpha, stri
     x2 = None if x2d is None else np.ascontiguousarray(x2d, np.float64)
     y2 = None if y2d is None else np.ascontiguousarray(y2d, np.float64)
     P = CalcParams(mode, scheme, m, md, float(alpha), stride, mni, mnj, _p(x, C.c_double), _p(y, C.c_double),
-                   _p(x2, C.c_double), _p(y2, C.c_double))
+                   _p(x2, C.c_double), _p(y2, C.c_double), 0, 0)
+    if units is not None:
+        # a work queue of (strided row, first column, end column) units taken
+        # by the threads as they come free (the dynamic schedule of the
+        # reference's mpiqueue, common/mpiqueue.c:124-248)
+        units = [tuple(int(v) for v in u) for u in units]
+        nxt = [0]
+        qlock = threading.Lock()
+        L = lib()
+        rcs = []
+
+        def worker():
+            while True:
+                with qlock:
+                    k = nxt[0]
+                    nxt[0] += 1
+                if k >= len(units):
+                    return
+                jj, i0, i1 = units[k]
+                Pk = CalcParams(mode, scheme, m, md, float(alpha), stride, mni, mnj, _p(x, C.c_double),
+                                _p(y, C.c_double), _p(x2, C.c_double), _p(y2, C.c_double), i0, i1)
+                rcs.append(L.or_calctransforms(C.c_void_p(obs.h), C.byref(Pk), _p(S, C.c_float), _p(s, C.c_double),
+                                               _p(obs.otype, C.c_short), C.c_int(jj), C.c_int(jj + 1),
+                                               _p(T, C.c_float), _p(w, C.c_float), _p(T64, C.c_double),
+                                               _p(w64, C.c_double), _p(nlobs, C.c_int), _p(dfs, C.c_float),
+                                               _p(srf, C.c_float), _p(pn, C.c_int), _p(pd, C.c_float),
+                                               _p(ps, C.c_float)))
+
+        ts = [threading.Thread(target=worker) for _ in range(max(1, threads))]
+        for t in ts:
+            t.start()
+        for t in ts:
+            t.join()
+        if any(rcs):
+            raise RuntimeError(f"LAPACK failure {[r for r in rcs if r]}")
+        return dict(T=T, w=w, T64=T64, w64=w64, nlobs=nlobs, dfs=dfs, srf=srf, pnlobs=pn, pdfs=pd, psrf=ps)
     if rows is None:
         rowlist = list(range(nj))
     elif isinstance(rows, tuple) and len(rows) == 2:

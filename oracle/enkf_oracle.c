@@ -517,10 +517,12 @@ int or_calctransforms(const or_obsset* obs, const or_calcparams* P, const float*
     int enkf = (P->mode == OR_MODE_ENKF || P->mode == OR_MODE_HYBRID);
     int jj, ii, e, o, ot, ret = 0;
 
+    int iend = (P->ii1 > 0 && P->ii1 < ni) ? P->ii1 : ni;
+
     for (jj = jj0; jj < jj1 && jj < nj; ++jj) {
         int j = jj * stride;
 
-        for (ii = 0; ii < ni; ++ii) {
+        for (ii = P->ii0 > 0 ? P->ii0 : 0; ii < iend; ++ii) {
             int i = ii * stride;
             size_t cell = (size_t) jj * ni + ii;
             double lon, lat;

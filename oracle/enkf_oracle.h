@@ -64,10 +64,11 @@ typedef struct {
     const double* y;            /* rectangular grid: y[mnj] */
     const double* x2d;          /* curvilinear: [mnj][mni] (or NULL) */
     const double* y2d;
+    int ii0, ii1;               /* strided columns ii0 <= ii < ii1 (ii1 <= 0: all) */
 } or_calcparams;
 
 /* das_calctransforms inner loop (transforms.c:1150-1360) over strided rows
- * jj in [jj0, jj1).  All output arrays are full-size (indexed by the strided
+ * jj in [jj0, jj1) (and the strided columns p->ii0 .. p->ii1 - 1 of each).  All output arrays are full-size (indexed by the strided
  * row): T float [nj][ni][m_dyn][m] (NULL for EnOI), w float [nj][ni][m],
  * T64/w64 the same in double before the float cast (NULL to skip), nlobs/dfs/
  * srf [nj][ni], pnlobs/pdfs/psrf [ntypes][nj][ni] (NULL to skip).  S is

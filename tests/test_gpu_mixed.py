@@ -134,21 +134,32 @@ def test_mixed_plain_grid_path(ctx):
 
 
 def test_bounded_wait_expires_and_context_recovers(ctx, gpu_lib):
-    """A wait limit of 1 ns on the context makes the mixed kernel's waits for
-    its tensor-core MMAs expire (every point here takes hundreds of
-    observations, so each point waits on MMAs it has just issued): the call
-    returns ENKFG_ETIMEOUT, no fault, and the next call on the same context,
-    with the default limit, gives the usual result."""
+    """The timeout path of the mixed kernel's bounded waits: with the drill
+    on, each CTA first waits on an mbarrier that nothing completes, with a
+    limit of 1 ms, so the wait runs out; the call returns ENKFG_ETIMEOUT (no
+    fault, no hang), and the next calls on the same context -- one with a
+    1 ns limit on the real MMA waits, then one with the default limit -- give
+    the usual results."""
     w = synth.make(3, scale=0.12, nobs=30000, nmem=96, with_fields=False)
     S, s = prepare(w)
     _, tabs = obsset(w)
     gpu_setup(ctx, w, S, s, tabs)
     ref = ctx.calctransforms(mode=0, scheme=1, path=1, precision=1, want64=True, want_diag=False)
-    ctx.set_wait_limit(1)
+    ctx.set_wait_limit(1_000_000)
+    ctx.set_wait_drill(True)
     try:
         with pytest.raises(gpu_lib.EnkfgError) as e:
             ctx.calctransforms(mode=0, scheme=1, path=1, precision=1, want64=True, want_diag=False)
         assert e.value.status == 4, e.value       # ENKFG_ETIMEOUT
+    finally:
+        ctx.set_wait_drill(False)
+    # a 1 ns bound on the real waits: they expire only if the MMAs outlast a
+    # tick of the global timer, so either outcome is allowed, but no other
+    ctx.set_wait_limit(1)
+    try:
+        ctx.calctransforms(mode=0, scheme=1, path=1, precision=1, want64=True, want_diag=False)
+    except gpu_lib.EnkfgError as e2:
+        assert e2.status == 4, e2
     finally:
         ctx.set_wait_limit(0)
     out = ctx.calctransforms(mode=0, scheme=1, path=1, precision=1, want64=True, want_diag=False)
