@@ -58,6 +58,131 @@ struct EmSlots {
 // 1a. FP32 Householder tridiagonalisation, one CTA per slot.  Also splits M
 //     into its double-float pair for the residual.
 // ---------------------------------------------------------------------------
+namespace em {
+
+// sum over the CTA of one value per thread (NT threads); red: NT/32 floats
+template <int NT>
+__device__ __forceinline__ float cta_sum(float v, float* red)
+{
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    __syncthreads();
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+    __syncthreads();
+    float s = 0.0f;
+#pragma unroll
+    for (int w = 0; w < NT / 32; ++w) s += red[w];
+    return s;
+}
+
+// Householder tridiagonalisation of the symmetric A (n x n, row stride lda,
+// both triangles valid) with the transformations accumulated, the steps of
+// tred2 (Wilkinson & Reinsch) without the row scaling (M = I + S'S is far
+// from FP32 overflow and underflow).  The dot products run warp-wide (lanes
+// over k, a shuffle reduction), one row or column per warp; the rank-2 and
+// rank-1 updates go row by row over the warps.  Lower-triangle storage:
+// A[j][k] with k <= j; the reflectors are kept in the rows and, scaled, in
+// the columns above the diagonal.  On return A holds Q, d the diagonal and e
+// the off-diagonal in QL form (e[i] couples i and i+1, e[n-1] = 0).
+template <int NT>
+__device__ void tred2_f32(float* A, int n, int lda, float* d, float* e, float* red)
+{
+    const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+    constexpr int NW = NT / 32;
+    for (int i = n - 1; i >= 1; --i) {
+        const int l = i - 1;
+        float* Ai = A + (size_t)i * lda;
+        float part = 0.0f;
+        for (int k = tid; k <= l; k += NT) part = fmaf(Ai[k], Ai[k], part);
+        float h = cta_sum<NT>(part, red);
+        if (l == 0 || h == 0.0f) {
+            if (tid == 0) {
+                e[i] = Ai[l];
+                d[i] = 0.0f;
+            }
+            __syncthreads();
+            continue;
+        }
+        const float f = Ai[l];
+        const float g = (f >= 0.0f) ? -sqrtf(h) : sqrtf(h);
+        h -= f * g;
+        const float ih = 1.0f / h;
+        __syncthreads();              // every thread has read Ai[l]
+        if (tid == 0) {
+            e[i] = g;
+            Ai[l] = f - g;
+            d[i] = h;
+        }
+        __syncthreads();
+        // p = A u / h into e[0..l] (u = row i), column i keeps u / h; the
+        // warp's share of sum_j p_j u_j along the way
+        float ffw = 0.0f;
+        for (int j = wid; j <= l; j += NW) {
+            const float* Aj = A + (size_t)j * lda;
+            float acc = 0.0f;
+            for (int k = lane; k <= l; k += 32) {
+                const float a = (k <= j) ? Aj[k] : A[(size_t)k * lda + j];
+                acc = fmaf(a, Ai[k], acc);
+            }
+            for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+            const float pj = acc * ih;
+            if (lane == 0) {
+                e[j] = pj;
+                A[(size_t)j * lda + i] = Ai[j] * ih;
+            }
+            ffw = fmaf(pj, Ai[j], ffw);
+        }
+        const float ff = cta_sum<NT>(lane == 0 ? ffw : 0.0f, red);
+        const float hh = ff / (h + h);
+        for (int j = tid; j <= l; j += NT) e[j] = e[j] - hh * Ai[j];   // q
+        __syncthreads();
+        // A[j][k] -= u_j q_k + q_j u_k  (k <= j <= l)
+        for (int j = wid; j <= l; j += NW) {
+            float* Aj = A + (size_t)j * lda;
+            const float uj = Ai[j], qj = e[j];
+            for (int k = lane; k <= j; k += 32) Aj[k] -= uj * e[k] + qj * Ai[k];
+        }
+        __syncthreads();
+    }
+    if (tid == 0) {
+        d[0] = 0.0f;
+        e[0] = 0.0f;
+    }
+    __syncthreads();
+    // accumulate Q = H_{n-1} ... H_1: step i applies reflector i to the
+    // leading i x i block (columns j < i: g_j = row i . column j)
+    for (int i = 0; i < n; ++i) {
+        const int l = i - 1;
+        float* Ai = A + (size_t)i * lda;
+        if (d[i] != 0.0f) {
+            for (int j = wid; j <= l; j += NW) {
+                float acc = 0.0f;
+                for (int k = lane; k <= l; k += 32) acc = fmaf(Ai[k], A[(size_t)k * lda + j], acc);
+                for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+                for (int k = lane; k <= l; k += 32) A[(size_t)k * lda + j] -= acc * A[(size_t)k * lda + i];
+            }
+            __syncthreads();
+        }
+        const float di = Ai[i];
+        __syncthreads();
+        if (tid == 0) {
+            d[i] = di;
+            Ai[i] = 1.0f;
+        }
+        for (int j = tid; j <= l; j += NT) {
+            A[(size_t)j * lda + i] = 0.0f;
+            Ai[j] = 0.0f;
+        }
+        __syncthreads();
+    }
+    if (tid == 0) {
+        for (int i = 1; i < n; ++i) e[i - 1] = e[i];
+        e[n - 1] = 0.0f;
+    }
+    __syncthreads();
+}
+
+}  // namespace em
+
 __global__ void __launch_bounds__(EM_TRED_NT) k_em_tred(CalcArgs a, EmSlots z)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -77,7 +202,7 @@ __global__ void __launch_bounds__(EM_TRED_NT) k_em_tred(CalcArgs a, EmSlots z)
         z.mhl[q0 + i] = make_float2(hi, (float)(v - (double)hi));
     }
     __syncthreads();
-    la::tred2<EM_TRED_NT>(A, m, lda, d, e, red);
+    em::tred2_f32<EM_TRED_NT>(A, m, lda, d, e, red);
     for (int i = tid; i < m * m; i += EM_TRED_NT) {
         const int r = i / m, c = i - r * m;
         z.q[q0 + i] = A[r * lda + c];
@@ -112,15 +237,22 @@ __global__ void __launch_bounds__(EM_QL_T) k_em_ql(int nslots, int m, const doub
 }
 
 // ---------------------------------------------------------------------------
-// 1c. The log replayed onto Q (rows in parallel); a point whose chain failed
-//     (log full, or no convergence within the chain) runs tql2 in the CTA.
+// 1c. The log replayed onto Q (rows in parallel, one thread each); a point
+//     whose chain failed (log full, or no convergence within the chain) runs
+//     tql2 in the CTA.  The log is staged through shared memory EM_RCH
+//     rotations at a time: every row walks the same sequence, so the
+//     control flow is uniform and each rotation is read from global memory
+//     once per point.
 // ---------------------------------------------------------------------------
+#define EM_RCH 1024
+
 __global__ void __launch_bounds__(EM_REPLAY_NT) k_em_replay(CalcArgs a, EmSlots z)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int m = a.m, lda = m + 1;
     const int tid = threadIdx.x, slot = blockIdx.x;
-    float* A = (float*)smem_raw;
+    float2* rbuf = (float2*)smem_raw;                 // [EM_RCH]
+    float* A = (float*)(rbuf + EM_RCH);
     float* d = A + (size_t)m * lda;
     float* e = d + m;
     float* cs = e + m;
@@ -139,9 +271,46 @@ __global__ void __launch_bounds__(EM_REPLAY_NT) k_em_replay(CalcArgs a, EmSlots 
     }
     __syncthreads();
     int rc = 0;
-    if (stt >= 0) la::ql_replay<EM_REPLAY_NT>(A, m, lda, z.rot + (size_t)slot * z.rcap, z.hdr + (size_t)slot * z.hcap,
-                                            stt);
-    else rc = la::tql2<EM_REPLAY_NT>(A, m, lda, d, e, cs, sn, ctl);
+    if (stt >= 0) {
+        const float2* rot = z.rot + (size_t)slot * z.rcap;
+        const int2* hdr = z.hdr + (size_t)slot * z.hcap;
+        float* Ak = A + (size_t)(tid < m ? tid : 0) * lda;
+        int h = 0, i = 0, r = 0;
+        bool inside = false;
+        float carry = 0.0f;
+        for (int c0 = 0; h < stt; c0 += EM_RCH) {
+            __syncthreads();
+            for (int q = tid; q < EM_RCH && c0 + q < z.rcap; q += EM_REPLAY_NT) rbuf[q] = rot[c0 + q];
+            __syncthreads();
+            while (h < stt) {
+                const int2 hd = hdr[h];
+                if (hd.x < hd.y) {       // an empty sweep
+                    ++h;
+                    continue;
+                }
+                if (!inside) {
+                    i = hd.x;
+                    if (tid < m) carry = Ak[i + 1];
+                    inside = true;
+                }
+                for (; i >= hd.y && r < c0 + EM_RCH; --i, ++r) {
+                    const float2 q = rbuf[r - c0];
+                    if (tid < m) {
+                        const float zi = Ak[i];
+                        Ak[i + 1] = q.y * zi + q.x * carry;
+                        carry = q.x * zi - q.y * carry;
+                    }
+                }
+                if (i >= hd.y) break;    // the chunk is used up inside the sweep
+                if (tid < m) Ak[hd.y] = carry;
+                inside = false;
+                ++h;
+            }
+        }
+        __syncthreads();
+    } else {
+        rc = la::tql2<EM_REPLAY_NT>(A, m, lda, d, e, cs, sn, ctl);
+    }
     if (rc != 0 && tid == 0) {
         const int pt = a.order ? a.order[slot] : a.item0 + slot;
         a.status[pt] = rc;
@@ -176,8 +345,9 @@ __device__ __forceinline__ void df_fma(float& sh, float& sl, float ah, float al,
 // C = op(X) op(Y) for MP x MP float matrices in shared memory (row stride
 // lda): thread (ty, tx) of the 16 x 16 grid owns rows ty + 16 r and columns
 // tx + 16 c; k runs over the first n indices (the rest are zero padding).
-// C may alias X or Y.
-template <int R, bool TX, bool TY>
+// SYM: the product is symmetric; only the blocks c >= r are formed and the
+// others mirrored.  C may alias X or Y.
+template <int R, bool TX, bool TY, bool SYM>
 __device__ __forceinline__ void mm(float* C, const float* X, const float* Y, int n, int lda)
 {
     const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
@@ -195,13 +365,18 @@ __device__ __forceinline__ void mm(float* C, const float* X, const float* Y, int
 #pragma unroll
         for (int r = 0; r < R; ++r)
 #pragma unroll
-            for (int c = 0; c < R; ++c) acc[r][c] = fmaf(xv[r], yv[c], acc[r][c]);
+            for (int c = 0; c < R; ++c)
+                if (!SYM || c >= r) acc[r][c] = fmaf(xv[r], yv[c], acc[r][c]);
     }
     __syncthreads();
 #pragma unroll
     for (int r = 0; r < R; ++r)
 #pragma unroll
-        for (int c = 0; c < R; ++c) C[(ty + 16 * r) * lda + tx + 16 * c] = acc[r][c];
+        for (int c = 0; c < R; ++c)
+            if (!SYM || c >= r) {
+                C[(ty + 16 * r) * lda + tx + 16 * c] = acc[r][c];
+                if (SYM && c > r) C[(tx + 16 * c) * lda + ty + 16 * r] = acc[r][c];
+            }
     __syncthreads();
 }
 
@@ -251,7 +426,7 @@ __global__ void __launch_bounds__(EM_NT, 1) k_em_refine(CalcArgs a, EmSlots z)
         B[r * LDA + c] = c < m ? Q[r * LDA + c] * rsqrtf(lam[c]) : 0.0f;
     }
     __syncthreads();
-    em::mm<R, false, true>(A, B, Q, m, LDA);
+    em::mm<R, false, true, true>(A, B, Q, m, LDA);
     for (int i = tid; i < MP * MP; i += EM_NT) {
         const int r = i / MP, c = i - r * MP;
         z.z0[z0 + i] = A[r * LDA + c];
@@ -311,32 +486,37 @@ __global__ void __launch_bounds__(EM_NT, 1) k_em_refine(CalcArgs a, EmSlots z)
 #pragma unroll
                 for (int r = 0; r < R; ++r)
 #pragma unroll
-                    for (int c = 0; c < R; ++c) em::df_fma(rh[r][c], rl[r][c], pv[c].x, pv[c].y, zv[r]);
+                    for (int c = 0; c < R; ++c)
+                        if (c >= r) em::df_fma(rh[r][c], rl[r][c], pv[c].x, pv[c].y, zv[r]);
             }
             __syncthreads();
         }
+        // R is symmetric: blocks c >= r formed, the others mirrored
 #pragma unroll
         for (int r = 0; r < R; ++r)
 #pragma unroll
-            for (int c = 0; c < R; ++c) {
-                const int i = ty + 16 * r, j = tx + 16 * c;
-                // (delta - hi) is exact near 1 (Sterbenz), then the low part
-                const float one = (i == j && i < m) ? 1.0f : 0.0f;
-                B[i * LDA + j] = (i < m && j < m) ? (one - rh[r][c]) - rl[r][c] : 0.0f;
-            }
+            for (int c = 0; c < R; ++c)
+                if (c >= r) {
+                    const int i = ty + 16 * r, j = tx + 16 * c;
+                    // (delta - hi) is exact near 1 (Sterbenz), then the low part
+                    const float one = (i == j && i < m) ? 1.0f : 0.0f;
+                    const float v = (i < m && j < m) ? (one - rh[r][c]) - rl[r][c] : 0.0f;
+                    B[i * LDA + j] = v;
+                    if (c > r) B[j * LDA + i] = v;
+                }
     }
     __syncthreads();
 
     // 4. D~ = Q' R Q, D~_ij /= (sigma_i + sigma_j), D = Q D~ Q'
-    em::mm<R, true, false>(A, Q, B, m, LDA);
-    em::mm<R, false, false>(B, A, Q, m, LDA);
+    em::mm<R, true, false, false>(A, Q, B, m, LDA);
+    em::mm<R, false, false, true>(B, A, Q, m, LDA);
     for (int i = tid; i < MP * MP; i += EM_NT) {
         const int r = i / MP, c = i - r * MP;
         B[r * LDA + c] = (r < m && c < m) ? B[r * LDA + c] / (sig[r] + sig[c]) : 0.0f;
     }
     __syncthreads();
-    em::mm<R, false, false>(A, Q, B, m, LDA);
-    em::mm<R, false, true>(B, A, Q, m, LDA);
+    em::mm<R, false, false, false>(A, Q, B, m, LDA);
+    em::mm<R, false, true, true>(B, A, Q, m, LDA);
 
     // 5. T = Z0 + D in FP64, relaxed and cast (transforms.c:1270-1296);
     //    tr(M^-1) = |T|_F^2 for the degrees of freedom
@@ -460,7 +640,7 @@ enkfg_status run_etkf_mixed(enkfg_ctx* ctx, const CalcArgs& a0, cudaStream_t st)
     const int lda = m + 1;
     const size_t tsmem = ((size_t)m * lda + 2 * (size_t)m + EM_TRED_NT / 32) * 4 + 16;
     const size_t qsmem = (size_t)2 * m * EM_QL_T * 4;
-    const size_t rsmem = ((size_t)m * lda + 4 * (size_t)m) * 4 + 16;
+    const size_t rsmem = (size_t)EM_RCH * 8 + ((size_t)m * lda + 4 * (size_t)m) * 4 + 16;
     CK(cudaFuncSetAttribute(k_em_tred, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tsmem));
     CK(cudaFuncSetAttribute(k_em_ql, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)qsmem));
     CK(cudaFuncSetAttribute(k_em_replay, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rsmem));
