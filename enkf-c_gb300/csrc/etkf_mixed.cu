@@ -77,12 +77,13 @@ __device__ __forceinline__ float cta_sum(float v, float* red)
 // Householder tridiagonalisation of the symmetric A (n x n, row stride lda,
 // both triangles valid) with the transformations accumulated, the steps of
 // tred2 (Wilkinson & Reinsch) without the row scaling (M = I + S'S is far
-// from FP32 overflow and underflow).  The dot products run warp-wide (lanes
-// over k, a shuffle reduction), one row or column per warp; the rank-2 and
-// rank-1 updates go row by row over the warps.  Lower-triangle storage:
-// A[j][k] with k <= j; the reflectors are kept in the rows and, scaled, in
-// the columns above the diagonal.  On return A holds Q, d the diagonal and e
-// the off-diagonal in QL form (e[i] couples i and i+1, e[n-1] = 0).
+// from FP32 overflow and underflow).  The matrix-vector products run one row
+// (or column) per thread, so that the n dependent chains overlap; the rank-2
+// update goes row by row over the warps (lanes over the row), with no index
+// arithmetic per element.  Lower-triangle storage: A[j][k] with k <= j; the
+// reflectors are kept in the rows and, scaled, in the columns above the
+// diagonal.  On return A holds Q, d the diagonal and e the off-diagonal in
+// QL form (e[i] couples i and i+1, e[n-1] = 0).
 template <int NT>
 __device__ void tred2_f32(float* A, int n, int lda, float* d, float* e, float* red)
 {
@@ -113,25 +114,28 @@ __device__ void tred2_f32(float* A, int n, int lda, float* d, float* e, float* r
             d[i] = h;
         }
         __syncthreads();
-        // p = A u / h into e[0..l] (u = row i), column i keeps u / h; the
-        // warp's share of sum_j p_j u_j along the way
-        float ffw = 0.0f;
-        for (int j = wid; j <= l; j += NW) {
+        // p = A u / h into e[0..l] (u = row i), column i keeps u / h
+        float ffp = 0.0f;
+        for (int j = tid; j <= l; j += NT) {
             const float* Aj = A + (size_t)j * lda;
-            float acc = 0.0f;
-            for (int k = lane; k <= l; k += 32) {
-                const float a = (k <= j) ? Aj[k] : A[(size_t)k * lda + j];
-                acc = fmaf(a, Ai[k], acc);
+            float acc0 = 0.0f, acc1 = 0.0f;
+            int k = 0;
+            for (; k + 1 <= j; k += 2) {
+                acc0 = fmaf(Aj[k], Ai[k], acc0);
+                acc1 = fmaf(Aj[k + 1], Ai[k + 1], acc1);
             }
-            for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-            const float pj = acc * ih;
-            if (lane == 0) {
-                e[j] = pj;
-                A[(size_t)j * lda + i] = Ai[j] * ih;
+            if (k <= j) acc0 = fmaf(Aj[k], Ai[k], acc0);
+            for (k = j + 1; k + 1 <= l; k += 2) {
+                acc0 = fmaf(A[(size_t)k * lda + j], Ai[k], acc0);
+                acc1 = fmaf(A[(size_t)(k + 1) * lda + j], Ai[k + 1], acc1);
             }
-            ffw = fmaf(pj, Ai[j], ffw);
+            if (k <= l) acc0 = fmaf(A[(size_t)k * lda + j], Ai[k], acc0);
+            const float pj = (acc0 + acc1) * ih;
+            e[j] = pj;
+            A[(size_t)j * lda + i] = Ai[j] * ih;
+            ffp = fmaf(pj, Ai[j], ffp);
         }
-        const float ff = cta_sum<NT>(lane == 0 ? ffw : 0.0f, red);
+        const float ff = cta_sum<NT>(ffp, red);
         const float hh = ff / (h + h);
         for (int j = tid; j <= l; j += NT) e[j] = e[j] - hh * Ai[j];   // q
         __syncthreads();
@@ -149,16 +153,21 @@ __device__ void tred2_f32(float* A, int n, int lda, float* d, float* e, float* r
     }
     __syncthreads();
     // accumulate Q = H_{n-1} ... H_1: step i applies reflector i to the
-    // leading i x i block (columns j < i: g_j = row i . column j)
+    // leading i x i block, one column per thread (g_j = row i . column j)
     for (int i = 0; i < n; ++i) {
         const int l = i - 1;
         float* Ai = A + (size_t)i * lda;
         if (d[i] != 0.0f) {
-            for (int j = wid; j <= l; j += NW) {
-                float acc = 0.0f;
-                for (int k = lane; k <= l; k += 32) acc = fmaf(Ai[k], A[(size_t)k * lda + j], acc);
-                for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-                for (int k = lane; k <= l; k += 32) A[(size_t)k * lda + j] -= acc * A[(size_t)k * lda + i];
+            for (int j = tid; j <= l; j += NT) {
+                float g0 = 0.0f, g1 = 0.0f;
+                int k = 0;
+                for (; k + 1 <= l; k += 2) {
+                    g0 = fmaf(Ai[k], A[(size_t)k * lda + j], g0);
+                    g1 = fmaf(Ai[k + 1], A[(size_t)(k + 1) * lda + j], g1);
+                }
+                if (k <= l) g0 = fmaf(Ai[k], A[(size_t)k * lda + j], g0);
+                const float g = g0 + g1;
+                for (k = 0; k <= l; ++k) A[(size_t)k * lda + j] -= g * A[(size_t)k * lda + i];
             }
             __syncthreads();
         }

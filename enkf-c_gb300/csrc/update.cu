@@ -447,6 +447,294 @@ __global__ void __launch_bounds__(UPD_NT) k_update_v2(UpdArgs a)
     }
 }
 
+// das_updatefields, version 3 (nmem > 64).  A CTA of 8 warps owns U3_NC = 8
+// consecutive cells of one model row (warp w: cell i0 + w) and up to U3_FG
+// field-layers.  The [nf][nmem][8] field block is staged with 32-byte row
+// pieces; each warp forms its cell's mask, missing-value test, mean and
+// anomalies (update.c:296-392).  The j-interpolated transforms of the
+// strided columns the 8 cells touch (Tjj, update.c:224-241) are streamed
+// through shared memory U3_KE members of the reduction at a time and shared
+// by all cells and field-layers: lane l of a warp owns output members l,
+// l + 32, ... (EPL of them), forms the i-interpolated X5 elements with the
+// reference's float operations (update.c:255-265) once per chunk, and
+// applies them to every field-layer's anomalies (register accumulators, 16-
+// byte broadcast loads of the anomalies).  The epilogue is version 2's: mean
+// update, hybrid rescaling, spread-capped inflation, increments, outputs back
+// into the staged block, then 32-byte row pieces out.
+#define U3_NC 8
+#define U3_KE 16
+#define U3_FG 10
+#define U3_TLD (U3_KE + 4)      // padded chunk row: 16-byte loads of 8 lanes hit distinct banks
+
+static inline size_t upd_v3_smem(int m, int md, int stride, int nf)
+{
+    const int M4 = (m + 3) & ~3, M16 = (m + 15) & ~15;
+    const int nsc = (U3_NC - 1 + stride - 1) / stride + 2;
+    return ((size_t)nf * m * U3_NC + (size_t)nf * U3_NC * M16 + (size_t)nsc * md * U3_TLD + (size_t)nsc * M4) *
+           sizeof(float);
+}
+
+template <bool F64, int EPL>
+__global__ void __launch_bounds__(UPD_NT) k_update_v3(UpdArgs a)
+{
+    extern __shared__ __align__(16) float usm[];
+    const int m = a.m, md = a.md, st = a.stride, nf = a.nfield;   // nf <= U3_FG
+    const int tid = threadIdx.x, lane = tid & 31, c = tid >> 5;
+    const int M4 = (m + 3) & ~3, M16 = (m + 15) & ~15;
+    const int jt = blockIdx.y, jg = a.j1 + jt;
+    const int jj = a.j1 / st + jt / st, stepj = jt % st;
+    const int jj2 = (jj < a.nj - 1) ? jj + 1 : jj;
+    const int i0 = blockIdx.x * U3_NC;
+    const int ncell = min(U3_NC, a.mni - i0);
+    const int iia = i0 / st, iib = (i0 + ncell - 1) / st;
+    const int nsc = iib - iia + 2;                 // strided columns, the last the i-neighbour
+    const int nb = (iib < a.ni - 1) ? iib + 1 : (a.periodic_i ? (iib + 1) % a.ni : iib);
+    const int nscap = (U3_NC - 1 + st - 1) / st + 2;   // strided columns of 8 cells, at most
+    float* raw = usm;                                          // [nf][m][U3_NC]
+    float* Am = raw + (size_t)nf * m * U3_NC;                  // [nf][U3_NC][M16] (zero past m)
+    float* Tc = Am + (size_t)nf * U3_NC * M16;                 // [nscap][md][U3_TLD]
+    float* Wc = Tc + (size_t)nscap * md * U3_TLD;              // [nscap][M4]
+    const float w2j = __fdiv_rn((float)stepj, (float)st), w1j = __fsub_rn(1.0f, w2j);
+    const bool jint = (st > 1 && stepj > 0);
+
+    // 1. the field block and the j-interpolated w of the strided columns
+    for (int idx = tid; idx < nf * m * U3_NC; idx += UPD_NT) {
+        const int cc = idx % U3_NC, fe = idx / U3_NC;
+        if (cc < ncell) {
+            const int f = fe / m, e = fe - f * m;
+            raw[idx] = a.fields[((size_t)f * m + e) * a.plane + (size_t)jt * a.mni + i0 + cc];
+        }
+    }
+    for (int idx = tid; idx < nsc * m; idx += UPD_NT) {
+        const int k = idx / m, e = idx - k * m;
+        const int col = (k < nsc - 1) ? iia + k : nb;
+        float v = __ldg(&a.w[((size_t)jj * a.ni + col) * m + e]);
+        if (jint) v = __fadd_rn(__fmul_rn(v, w1j), __fmul_rn(__ldg(&a.w[((size_t)jj2 * a.ni + col) * m + e]), w2j));
+        Wc[k * M4 + e] = v;
+    }
+    __syncthreads();
+
+    // 2. per warp (its cell): masks, missing values, mean, anomalies
+    const int i = i0 + c;
+    const bool live = c < ncell;
+    const int slot = live ? i / st - iia : 0, stepi = live ? i % st : 0;
+    const bool iint = (st > 1 && stepi > 0);
+    const float u2 = __fdiv_rn((float)stepi, (float)st), u1 = __fsub_rn(1.0f, u2);
+    const size_t ioff = (size_t)jt * a.mni + i;
+    unsigned active = 0;
+    Mean<F64> mean[U3_FG];
+    if (live) {
+        const int nl = a.numlevels[(size_t)jg * a.mni + i];
+        // (q unrolled: the means stay in registers)
+#pragma unroll
+        for (int q = 0; q < U3_FG; ++q) {
+            if (q >= nf) break;
+            float* v = raw + (size_t)q * m * U3_NC;
+            float* Aq = Am + ((size_t)q * U3_NC + c) * M16;
+            const int level = a.levels[q];
+            mean[q].zero();
+            const bool masked = (a.surfk == 0) ? (nl <= level) : (nl <= (a.issurfacevar ? 0 : a.surfk - level));
+            if (masked) {
+                for (int e = lane; e < m; e += 32) v[e * U3_NC + c] = 0.0f;
+                if (a.infl && lane == 0) a.infl[(size_t)q * a.plane + ioff] = 0.0f;
+                continue;
+            }
+            int first = m;
+            for (int e0 = 0; e0 < m && first == m; e0 += 32) {
+                const int e = e0 + lane;
+                bool bad = false;
+                if (e < m) {
+                    const float x = v[e * U3_NC + c];
+                    bad = !isfinite(x) || fabsf(x) > MAXOBSVAL_F;
+                }
+                const unsigned bal = __ballot_sync(0xffffffffu, bad);
+                if (bal) first = e0 + __ffs(bal) - 1;
+            }
+            if (a.infl && lane == 0) a.infl[(size_t)q * a.plane + ioff] = 0.0f;
+            if (first < md) {
+                for (int e = lane; e < m; e += 32) v[e * U3_NC + c] = 0.0f;
+                continue;
+            } else if (first < m) {
+                for (int e = md + lane; e < m; e += 32) v[e * U3_NC + c] = 0.0f;
+                if (md == 0) continue;
+            }
+            Acc<F64> sm;
+            for (int e = lane; e < md; e += 32) sm.add(v[e * U3_NC + c]);
+            sm.reduce();
+            mean[q].set(sm, md);
+            for (int e = lane; e < M16; e += 32) Aq[e] = (e < m) ? mean[q].sub(v[e * U3_NC + c]) : 0.0f;
+            active |= 1u << q;
+        }
+    }
+
+    // 3. A^a = A^f X5 over chunks of U3_KE members of the reduction
+    float acc[U3_FG][EPL];
+#pragma unroll
+    for (int q = 0; q < U3_FG; ++q)
+#pragma unroll
+        for (int k = 0; k < EPL; ++k) acc[q][k] = 0.0f;
+    for (int e0 = 0; e0 < m; e0 += U3_KE) {
+        const int ke_n = min(U3_KE, m - e0);
+        __syncthreads();   // the previous chunk is consumed (and the anomalies are written)
+        for (int idx = tid; idx < nsc * md * U3_KE; idx += UPD_NT) {
+            const int ke = idx % U3_KE, se = idx / U3_KE;
+            const int s = se / md, e1 = se - s * md;
+            float v = 0.0f;
+            if (ke < ke_n) {
+                const int col = (s < nsc - 1) ? iia + s : nb;
+                const size_t o = ((size_t)jj * a.ni + col) * md * m + (size_t)e1 * m + e0 + ke;
+                v = __ldg(&a.T[o]);
+                if (jint) {
+                    const float b = __ldg(&a.T[o + ((size_t)jj2 - jj) * a.ni * md * m]);
+                    v = __fadd_rn(__fmul_rn(v, w1j), __fmul_rn(b, w2j));
+                }
+            }
+            Tc[((size_t)s * md + e1) * U3_TLD + ke] = v;
+        }
+        __syncthreads();
+        if (active) {
+#pragma unroll
+            for (int ke = 0; ke < U3_KE; ke += 4) {
+                float4 t[EPL];
+#pragma unroll
+                for (int k = 0; k < EPL; ++k) {
+                    const int e1 = lane + 32 * k;
+                    t[k] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+                    if (e1 < md) {
+                        t[k] = *reinterpret_cast<const float4*>(&Tc[((size_t)slot * md + e1) * U3_TLD + ke]);
+                        if (iint) {
+                            const float4 tb =
+                                *reinterpret_cast<const float4*>(&Tc[((size_t)(slot + 1) * md + e1) * U3_TLD + ke]);
+                            t[k].x = __fadd_rn(__fmul_rn(t[k].x, u1), __fmul_rn(tb.x, u2));
+                            t[k].y = __fadd_rn(__fmul_rn(t[k].y, u1), __fmul_rn(tb.y, u2));
+                            t[k].z = __fadd_rn(__fmul_rn(t[k].z, u1), __fmul_rn(tb.z, u2));
+                            t[k].w = __fadd_rn(__fmul_rn(t[k].w, u1), __fmul_rn(tb.w, u2));
+                        }
+                    }
+                }
+#pragma unroll
+                for (int q = 0; q < U3_FG; ++q) {
+                    if (q < nf) {
+                        const float4 av =
+                            *reinterpret_cast<const float4*>(&Am[((size_t)q * U3_NC + c) * M16 + e0 + ke]);
+#pragma unroll
+                        for (int k = 0; k < EPL; ++k) {
+                            acc[q][k] = fmaf(t[k].x, av.x, acc[q][k]);
+                            acc[q][k] = fmaf(t[k].y, av.y, acc[q][k]);
+                            acc[q][k] = fmaf(t[k].z, av.z, acc[q][k]);
+                            acc[q][k] = fmaf(t[k].w, av.w, acc[q][k]);
+                        }
+                    }
+                }
+            }
+        }
+    }
+
+    // 4. per warp and field-layer: mean update, hybrid rescaling, inflation,
+    //    outputs into the staged block (update.c:393-516)
+    if (active) {
+        // (q unrolled: the accumulators stay in registers)
+#pragma unroll
+        for (int q = 0; q < U3_FG; ++q) {
+            if (q >= nf) break;
+            if (!((active >> q) & 1u)) continue;
+            float* v = raw + (size_t)q * m * U3_NC;
+            const float* Aq = Am + ((size_t)q * U3_NC + c) * M16;
+            float inflation = a.inflation0;
+            Acc<F64> sa;
+            for (int e = lane; e < m; e += 32) {
+                float t = Wc[slot * M4 + e];
+                if (iint) t = __fadd_rn(__fmul_rn(t, u1), __fmul_rn(Wc[(slot + 1) * M4 + e], u2));
+                sa.add_prod(Aq[e], t);
+            }
+            sa.reduce();
+            const Mean<F64> v1_a = mean[q].plus(sa);
+            float af[EPL], aa[EPL];
+#pragma unroll
+            for (int k = 0; k < EPL; ++k) {
+                const int e = lane + 32 * k;
+                af[k] = (e < m) ? Aq[e] : 0.0f;
+                aa[k] = acc[q][k];
+            }
+            if (a.mode == ENKFG_MODE_HYBRID) {
+                if constexpr (F64) {
+                    const double k_d = (md > 1) ? sqrt((double)(m - 1) / (double)(md - 1)) : 1.0;
+#pragma unroll
+                    for (int k = 0; k < EPL; ++k)
+                        if (lane + 32 * k < md) {
+                            aa[k] = (float)((double)aa[k] / k_d);
+                            af[k] = (float)((double)af[k] / k_d);
+                        }
+                } else {
+                    const float rk = a.inv_kd;
+#pragma unroll
+                    for (int k = 0; k < EPL; ++k)
+                        if (lane + 32 * k < md) {
+                            aa[k] = __fmul_rn(aa[k], rk);
+                            af[k] = __fmul_rn(af[k], rk);
+                        }
+                }
+            }
+            if (!isnan(a.inf_ratio)) {
+                Acc<F64> s2f, s2a;
+#pragma unroll
+                for (int k = 0; k < EPL; ++k)
+                    if (lane + 32 * k < md) {
+                        s2f.add_prod(af[k], af[k]);
+                        s2a.add_prod(aa[k], aa[k]);
+                    }
+                s2f.reduce();
+                s2a.reduce();
+                if constexpr (F64) {
+                    const double v2_f = s2f.value(), v2_a = s2a.value();
+                    if (v2_a > 0.0) {
+                        inflation = (float)(sqrt(v2_f / v2_a) * a.inf_ratio + 1.0 - a.inf_ratio);
+                        if (inflation >= a.inflation0) inflation = a.inflation0;
+                    }
+                } else {
+                    const float v2_f = s2f.hi + s2f.lo, v2_a = s2a.hi + s2a.lo;
+                    if (v2_a > 0.0f) {
+                        const float r = (float)a.inf_ratio;
+                        inflation = fmaf(sqrtf(__fdiv_rn(v2_f, v2_a)), r, 1.0f - r);
+                        if (inflation >= a.inflation0) inflation = a.inflation0;
+                    }
+                }
+            }
+            const bool inflate = __fsub_rn(inflation, 1.0f) > 1.0e-6f;
+            if (!inflate) inflation = 1.0f;
+#pragma unroll
+            for (int k = 0; k < EPL; ++k) {
+                const int e1 = lane + 32 * k;
+                if (e1 < md) {
+                    float va = inflate ? __fmul_rn(aa[k], inflation) : aa[k];
+                    va = v1_a.add(va);
+                    const float vf = mean[q].add(af[k]);
+                    float out;
+                    if (!a.output_increment) out = va;
+                    else if (!a.applylog) out = __fsub_rn(va, vf);
+                    else {
+                        const float avf = fabsf(vf);
+                        const bool normal = (avf >= 1.17549435e-38f) && (avf <= 3.40282347e+38f);
+                        const double ea = pow(10.0, (double)va), ef = pow(10.0, (double)vf);
+                        out = normal ? (float)(ea - ef) : 0.0f;
+                    }
+                    v[e1 * U3_NC + c] = out;
+                }
+            }
+            if (a.infl && lane == 0) a.infl[(size_t)q * a.plane + ioff] = inflation;
+        }
+    }
+    __syncthreads();
+    // 5. the block back out
+    for (int idx = tid; idx < nf * m * U3_NC; idx += UPD_NT) {
+        const int cc = idx % U3_NC, fe = idx / U3_NC;
+        if (cc < ncell) {
+            const int f = fe / m, e = fe - f * m;
+            a.fields[((size_t)f * m + e) * a.plane + (size_t)jt * a.mni + i0 + cc] = raw[idx];
+        }
+    }
+}
+
 // das_updatefields, thread-per-cell form for nmem <= 64 (MT = nmem rounded
 // up to a multiple of 8).  A CTA of 4 warps owns UPC_NC = 16 consecutive
 // cells of one model row: lane l of warp w takes cell i0 + (l & 15) and
@@ -924,6 +1212,42 @@ enkfg_status run_update(enkfg_ctx* ctx, const enkfg_update_params* p, const int*
     if (a.m > 32 * MAXE_PER_LANE || a.md > 32 * MAXE_PER_LANE) {
         set_err(ctx, "nmem = %d too large for the update kernel", a.m);
         return ENKFG_EUNSUPPORTED;
+    }
+    // version 3: 8 cells per CTA, the transforms streamed once per group of
+    // U3_FG field-layers
+    {
+        const int fg3 = nfield < U3_FG ? nfield : U3_FG;
+        const size_t smem3 = upd_v3_smem(a.m, a.md, a.stride, fg3);
+        if (smem3 <= 200 * 1024) {
+            const bool f64 = (p->precision == ENKFG_PREC_FP64);
+            const int epl = (a.md + 31) / 32;
+            auto launch3 = [&](auto kern) -> enkfg_status {
+                CK(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem3));
+                for (int g0 = 0; g0 < nfield; g0 += 448) {
+                    const int ng = nfield - g0 < 448 ? nfield - g0 : 448;
+                    if ((s = upload_levels(ctx, levels + g0, ng, d_levels, st))) return s;
+                    for (int f0 = g0; f0 < g0 + ng; f0 += fg3) {
+                        const int nf = g0 + ng - f0 < fg3 ? g0 + ng - f0 : fg3;
+                        a.levels = d_levels + (f0 - g0);
+                        a.nfield = nf;
+                        a.fields = d_fields + (size_t)f0 * a.m * a.plane;
+                        a.infl = d_infl ? d_infl + (size_t)f0 * a.plane : nullptr;
+                        dim3 g(div_up(a.mni, U3_NC), a.jsize);
+                        kern<<<g, UPD_NT, smem3, st>>>(a);
+                        CKL();
+                    }
+                }
+                cudaEventRecord(ctx->ev[5], st);
+                return ENKFG_OK;
+            };
+            switch (epl) {
+            case 1: return f64 ? launch3(k_update_v3<true, 1>) : launch3(k_update_v3<false, 1>);
+            case 2: return f64 ? launch3(k_update_v3<true, 2>) : launch3(k_update_v3<false, 2>);
+            case 3: return f64 ? launch3(k_update_v3<true, 3>) : launch3(k_update_v3<false, 3>);
+            case 4: return f64 ? launch3(k_update_v3<true, 4>) : launch3(k_update_v3<false, 4>);
+            default: return f64 ? launch3(k_update_v3<true, 5>) : launch3(k_update_v3<false, 5>);
+            }
+        }
     }
     // strided columns per CTA, field-layers per warp task and per launch: keep
     // two CTAs per SM (<= ~100 KB of shared memory each) when possible

@@ -180,6 +180,10 @@ UPDATE_CASES = [
     ("hybrid_s1_missing_static", 2, 20, 22, 16, 10, 1, 0, 0, -1, 0, 0, 0, 1.0, float("nan"), 0, 0),
     ("enoi_s3", 1, 31, 40, 14, 14, 3, 0, 0, -1, 0, 0, 0, 1.0, float("nan"), 0, 0),
     ("enoi_s2_tile_surfk", 1, 30, 27, 10, 10, 2, 1, 4, 21, 1, 3, 0, 1.0, float("nan"), 0, 0),
+    # ensembles above 64 members (the device's warp-per-cell kernel)
+    ("enkf_m80_s3_mask_ratio", 0, 13, 13, 80, 80, 3, 0, 0, -1, 1, 0, 0, 1.1, 0.5, 0, 0),
+    ("hybrid_m72_s2_periodic_tile", 2, 11, 13, 72, 48, 2, 1, 2, 9, 0, 0, 0, 1.03, 0.3, 0, 0),
+    ("enkf_m96_s1_increment_log", 0, 6, 7, 96, 96, 1, 0, 0, -1, 0, 2, 0, 1.0, float("nan"), 1, 1),
 ]
 
 
