@@ -379,6 +379,54 @@ def run_gpu(args, rank, world, local_rank):
                 "obs_member_values_per_s": w.nobs * m / ht, "bytes_per_pass": hb, "achieved_gbs": hb / ht / 1e9,
                 "peak_gbs": peaks["hbm_gbs"], "frac": hb / ht / 1e9 / peaks["hbm_gbs"]}
 
+    # the observation-impact adjoint on workload 4 (the grid and observations
+    # of workload 2, 64 members, J = sum over wet cells of (analysis mean -
+    # verifying field)^2): the forward transforms (batched mixed, as the
+    # cycle runs them), then the adjoint of the mean update and of the
+    # transforms -- the FP32 production form and the FP64 form
+    def measure_adjoint():
+        w4 = workload(4, args.scale)
+        c4 = enkfg.Enkfg(local_rank)
+        try:
+            nl4, lr4, lw4 = obs_tables(w4)
+            c4.set_obstypes(nl4, lr4, lw4, np.ones(w4.ntypes))
+            c4.set_obs(w4.lon, w4.lat, w4.otype, w4.status, w4.estd, w4.value)
+            c4.set_HE(w4.HE)
+            c4.calcinnandspread(want=False)
+            c4.standardise()
+            c4.set_grid(w4.x, w4.y, stride=w4.stride)
+            layer = w4.fields[0, 0]
+            wet = w4.numlevels > 0
+            g = np.where(wet, 2.0 * (layer.astype(np.float64).mean(axis=0) - w4.verify), 0.0)
+            res = {}
+            for k in range(2):
+                t0 = time.perf_counter()
+                out = c4.calctransforms(mode=w4.mode, scheme=w4.scheme, path=enkfg.PATH_BATCHED,
+                                        precision=enkfg.PREC_MIXED, want64=True, want_diag=False)
+                t1 = time.perf_counter()
+                wbar = c4.adjoint_mean(layer, g)
+                t2 = time.perf_counter()
+                g32 = c4.adjoint_transforms(wbar, mode=w4.mode, scheme=w4.scheme, precision=enkfg.PREC_MIXED)
+                t3 = time.perf_counter()
+                g64 = c4.adjoint_transforms(wbar, mode=w4.mode, scheme=w4.scheme, precision=enkfg.PREC_FP64)
+                t4 = time.perf_counter()
+                res = {"workload": workload_name(w4), "forward_ms": (t1 - t0) * 1e3, "adjoint_mean_ms": (t2 - t1) * 1e3,
+                       "adjoint_fp32_ms": (t3 - t2) * 1e3, "adjoint_fp64_ms": (t4 - t3) * 1e3,
+                       "fp32_vs_fp64_innov": float(np.linalg.norm(g32[0] - g64[0]) / np.linalg.norm(g64[0])),
+                       "fp32_vs_fp64_var": float(np.linalg.norm(g32[1] - g64[1]) / np.linalg.norm(g64[1])),
+                       "timing": "host wall clock around each call (host-buffer entry points, copies included), "
+                                 "second of two runs"}
+            return res
+        finally:
+            c4.close()
+
+    adjoint = None
+    if args.adjoint:
+        try:
+            adjoint = measure_adjoint()
+        except Exception as exc:   # report, do not hide: the cycle's numbers stand
+            adjoint = {"error": str(exc)[:300]}
+
     he_stage = None
     if args.he:
         try:
@@ -444,6 +492,7 @@ def run_gpu(args, rank, world, local_rank):
             "gpu_launches": int(launches),
             "plain_gpu_fp64": plain64,
             "he_stage": he_stage,
+            "adjoint": adjoint,
             "speedup_vs_plain_gpu_fp64": (value / plain64["value"]) if plain64 else None,
             "clocks": clk.summary(),
         }
@@ -581,6 +630,7 @@ def main():
     ap.add_argument("--graph", type=int, default=1, help="also time the cycle replayed from a CUDA graph")
     ap.add_argument("--compare-fp64", type=int, default=1, help="also time the plain GPU FP64 path")
     ap.add_argument("--he", type=int, default=1, help="also time the device forward operator (HE stage)")
+    ap.add_argument("--adjoint", type=int, default=1, help="also time the observation-impact adjoint (workload 4)")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))

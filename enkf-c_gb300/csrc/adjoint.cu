@@ -29,7 +29,12 @@
 //                  GC' vanish at x = 1, so obs entering or leaving the
 //                  neighbourhood contribute nothing).
 // Gradients with respect to estd^2 (the variance the obs file carries) are
-// dJ/dR_o * rfactor.  Everything runs in FP64.
+// dJ/dR_o * rfactor.  The kernel is a template on the arithmetic type F:
+// double (FP64 throughout: the form checked against finite differences) or
+// float (the production form, enkfg_calc_params.precision = mixed: the
+// recomputed S'S, eigendecomposition, Daleckii-Krein products and
+// per-observation passes in FP32; the taper, its derivative and the
+// gradient accumulators stay FP64).
 //
 // The mean-update part (update.c:405-410, x_a = x_f + A w_cell, w_cell the
 // stride-interpolated w) is reversed by k_adj_mean: wbar_i = sum over cells of
@@ -59,19 +64,20 @@ struct AdjArgs {
     double* drho;              // [1]
 };
 
+template <typename F>
 struct AdjProc {
     const AdjArgs& A;
     const PointScratch& s;
-    double* tile;              // [KC_MAX][MP] untapered S rows of the chunk
-    const double* lam;         // M^-1 wbar
-    const double* w;           // w
-    const double* P;           // Mbar + Mbar' (null: no T term)
+    F* tile;                   // [KC_MAX][MP] untapered S rows of the chunk
+    const F* lam;              // M^-1 wbar
+    const F* w;                // w
+    const F* P;                // Mbar + Mbar' (null: no T term)
     int lda;
     int mp;
     double qx, qy, qz;
     double rho_acc;
-    __device__ AdjProc(const AdjArgs& A_, const PointScratch& s_, double* tile_, const double* lam_,
-                       const double* w_, const double* P_, int lda_, int mp_, double qx_, double qy_, double qz_)
+    __device__ AdjProc(const AdjArgs& A_, const PointScratch& s_, F* tile_, const F* lam_, const F* w_, const F* P_,
+                       int lda_, int mp_, double qx_, double qy_, double qz_)
         : A(A_), s(s_), tile(tile_), lam(lam_), w(w_), P(P_), lda(lda_), mp(mp_), qx(qx_), qy(qy_), qz(qz_),
           rho_acc(0.0) {}
     __device__ void chunk(int nc, int t)
@@ -80,19 +86,19 @@ struct AdjProc {
         const int tid = threadIdx.x, m = a.m, lane = tid & 31, wid = tid >> 5;
         for (int i = tid; i < nc * mp; i += CALC_NT) {
             int o = i / mp, e = i - o * mp;
-            tile[i] = (e < m) ? (double)a.St[(size_t)s.lid[o] * a.mpad + e] : 0.0;
+            tile[i] = (e < m) ? (F)a.St[(size_t)s.lid[o] * a.mpad + e] : F(0);
         }
         __syncthreads();
         const TypeIndex& ti = a.types[t];
         // one warp per observation of the chunk
         for (int o = wid; o < nc; o += CALC_NT / 32) {
-            const double* u = tile + (size_t)o * mp;
-            double av = 0.0, cv = 0.0, qv = 0.0;
+            const F* u = tile + (size_t)o * mp;
+            F av = F(0), cv = F(0), qv = F(0);
             for (int e = lane; e < m; e += 32) {
                 av = fma(u[e], lam[e], av);
                 cv = fma(u[e], w[e], cv);
                 if (P != nullptr) {
-                    double pu = 0.0;
+                    F pu = F(0);
                     for (int k = 0; k < m; ++k) pu = fma(P[(size_t)e * lda + k], u[k], pu);
                     qv = fma(u[e], pu, qv);
                 }
@@ -106,9 +112,9 @@ struct AdjProc {
                 const int p = s.lid[o];
                 const double lc = s.llc[o];
                 const double su = a.ss[p];
-                const double dlc = 2.0 * lc * av * (su - cv) + lc * qv;
+                const double dlc = 2.0 * lc * (double)av * (su - (double)cv) + lc * (double)qv;
                 const int id = A.sid[p];
-                atomicAdd(&A.dinn[id], lc * lc * av / A.sig[p]);
+                atomicAdd(&A.dinn[id], lc * lc * (double)av / A.sig[p]);
                 atomicAdd(&A.dvar[id], -lc * dlc / (2.0 * A.R[p]));
                 // d lc / d rho
                 const double d2 = a.ndim == 2 ? exact::dist2(a.sx[p], a.sy[p], qx, qy)
@@ -127,22 +133,27 @@ struct AdjProc {
     __device__ void type_end(int) {}
 };
 
-template <int R>
+// products rounded to nearest in F: FP64 with the forward kernel's explicit
+// rounding, FP32 plainly
+__device__ __forceinline__ double adj_mul(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ float adj_mul(float a, float b) { return __fmul_rn(a, b); }
+
+template <int R, typename F>
 struct GramProcAdj {
-    // FP64 S'S and S's (same arithmetic as the FP64 forward kernel)
+    // S'S and S's in F (FP64: the same arithmetic as the FP64 forward kernel)
     const CalcArgs& a;
     const PointScratch& s;
-    double* tile;
-    double* sloc;
-    double acc[R][R];
-    double bacc;
-    __device__ GramProcAdj(const CalcArgs& a_, const PointScratch& s_, double* tile_, double* sloc_)
-        : a(a_), s(s_), tile(tile_), sloc(sloc_), bacc(0.0)
+    F* tile;
+    F* sloc;
+    F acc[R][R];
+    F bacc;
+    __device__ GramProcAdj(const CalcArgs& a_, const PointScratch& s_, F* tile_, F* sloc_)
+        : a(a_), s(s_), tile(tile_), sloc(sloc_), bacc(F(0))
     {
 #pragma unroll
         for (int i = 0; i < R; ++i)
 #pragma unroll
-            for (int j = 0; j < R; ++j) acc[i][j] = 0.0;
+            for (int j = 0; j < R; ++j) acc[i][j] = F(0);
     }
     __device__ void chunk(int nc, int)
     {
@@ -150,13 +161,13 @@ struct GramProcAdj {
         const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4, m = a.m;
         for (int i = tid; i < nc * MP; i += CALC_NT) {
             int o = i / MP, e = i - o * MP;
-            tile[i] = (e < m) ? __dmul_rn((double)a.St[(size_t)s.lid[o] * a.mpad + e], s.llc[o]) : 0.0;
+            tile[i] = (e < m) ? adj_mul((F)a.St[(size_t)s.lid[o] * a.mpad + e], (F)s.llc[o]) : F(0);
         }
-        if (tid < nc) sloc[tid] = __dmul_rn(a.ss[s.lid[tid]], s.llc[tid]);
+        if (tid < nc) sloc[tid] = adj_mul((F)a.ss[s.lid[tid]], (F)s.llc[tid]);
         __syncthreads();
         if (tx >= ty)
             for (int o = 0; o < nc; ++o) {
-                double av[R], bv[R];
+                F av[R], bv[R];
 #pragma unroll
                 for (int i = 0; i < R; ++i) av[i] = tile[o * MP + ty * R + i];
 #pragma unroll
@@ -173,28 +184,30 @@ struct GramProcAdj {
     __device__ void type_end(int) {}
 };
 
-template <int R>
+template <int R, typename F>
 __global__ void __launch_bounds__(CALC_NT) k_adjoint(AdjArgs A)
 {
     constexpr int MP = 16 * R, LDA = MP + 1;
+    constexpr size_t FS = sizeof(F);
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const CalcArgs& a = A.c;
     const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
     const int m = a.m, md = a.md;
     unsigned char* sp = smem_raw;
-    double* tile = (double*)sp;   sp += (size_t)KC_MAX * MP * 8;
     double* llc = (double*)sp;    sp += (size_t)LIST_EXTRA * 8;
-    double* sloc = (double*)sp;   sp += (size_t)KC_MAX * 8;
-    double* Z = (double*)sp;      sp += (size_t)MP * LDA * 8;     // M, then its eigenvectors
-    double* W = (double*)sp;      sp += (size_t)MP * LDA * 8;     // work (Z'GZ, then P)
-    double* b = (double*)sp;      sp += MP * 8;
-    double* d = (double*)sp;      sp += MP * 8;
-    double* e = (double*)sp;      sp += MP * 8;
-    double* cs = (double*)sp;     sp += MP * 8;
-    double* sn = (double*)sp;     sp += MP * 8;
-    double* w = (double*)sp;      sp += MP * 8;
-    double* lam = (double*)sp;    sp += MP * 8;
-    sp += MP * 8;                 // (spare row: keeps the layout of the shared-memory size formula)
+    F* tile = (F*)sp;             sp += (size_t)KC_MAX * MP * FS;
+    F* sloc = (F*)sp;             sp += (size_t)KC_MAX * FS;
+    F* Z = (F*)sp;                sp += (size_t)MP * LDA * FS;    // M, then its eigenvectors
+    F* W = (F*)sp;                sp += (size_t)MP * LDA * FS;    // work (Z'GZ, then P)
+    F* b = (F*)sp;                sp += MP * FS;
+    F* d = (F*)sp;                sp += MP * FS;
+    F* e = (F*)sp;                sp += MP * FS;
+    F* cs = (F*)sp;               sp += MP * FS;
+    F* sn = (F*)sp;               sp += MP * FS;
+    F* w = (F*)sp;                sp += MP * FS;
+    F* lam = (F*)sp;              sp += MP * FS;
+    F* fred = (F*)sp;             sp += MP * FS;                  // (CALC_NT / 32 <= MP) block sums in F
+    sp = (unsigned char*)(((uintptr_t)sp + 7) & ~(uintptr_t)7);
     double* tss = (double*)sp;    sp += ENKFG_MAXTYPES * 8;
     double* tpd = (double*)sp;    sp += ENKFG_MAXTYPES * 8;
     double* red = (double*)sp;    sp += (CALC_NT / 32) * 8;
@@ -217,7 +230,7 @@ __global__ void __launch_bounds__(CALC_NT) k_adjoint(AdjArgs A)
         if (nz == 0.0) return;
     }
     // 1. forward recomputation: M, b, eigendecomposition, w
-    GramProcAdj<R> gp(a, s, tile, sloc);
+    GramProcAdj<R, F> gp(a, s, tile, sloc);
     const int p = enumerate_obs<0>(a, a.kc, qx, qy, qz, s, gp, true);
     if (p == 0) return;
     if (tx >= ty)
@@ -233,26 +246,26 @@ __global__ void __launch_bounds__(CALC_NT) k_adjoint(AdjArgs A)
             }
     if (tid < m) b[tid] = gp.bacc;
     __syncthreads();
-    if (tid < m) Z[tid * LDA + tid] += 1.0;
+    if (tid < m) Z[tid * LDA + tid] += F(1);
     __syncthreads();
-    int rc = la::eig_sym<CALC_NT>(Z, m, LDA, d, e, cs, sn, ictl + 16, red);
+    int rc = la::eig_sym<CALC_NT>(Z, m, LDA, d, e, cs, sn, ictl + 16, fred);
     if (rc != 0) {
         if (tid == 0) a.status[pt] = rc;
         return;
     }
     // w = Z diag(1/l) Z' b ; lam = Z diag(1/l) Z' wbar
     if (tid < m) {
-        double cb = 0.0, cw = 0.0;
+        F cb = F(0), cw = F(0);
         for (int q = 0; q < m; ++q) {
             cb = fma(Z[q * LDA + tid], b[q], cb);
-            cw = fma(Z[q * LDA + tid], wb[q], cw);
+            cw = fma(Z[q * LDA + tid], (F)wb[q], cw);
         }
         cs[tid] = cb / d[tid];
         sn[tid] = cw / d[tid];
     }
     __syncthreads();
     if (tid < m) {
-        double x = 0.0, y = 0.0;
+        F x = F(0), y = F(0);
         for (int k = 0; k < m; ++k) {
             x = fma(Z[tid * LDA + k], cs[k], x);
             y = fma(Z[tid * LDA + k], sn[k], y);
@@ -262,16 +275,16 @@ __global__ void __launch_bounds__(CALC_NT) k_adjoint(AdjArgs A)
     }
     __syncthreads();
     // 2. T term (Daleckii-Krein): P = Mbar_T + Mbar_T', Mbar_T = Z (F o Z' G Z) Z'
-    const double* Pp = nullptr;
+    const F* Pp = nullptr;
     if (Tb != nullptr && a.mode != ENKFG_MODE_ENOI) {
         const bool etkf = (a.scheme == ENKFG_SCHEME_ETKF);
         // W = G Z, G = alpha Tbar on rows e1 < md (T[e1][e2] is column e1 of the
         // reference's T; f(M) is symmetric, so G can be taken row-wise)
         for (int idx = tid; idx < m * m; idx += CALC_NT) {
             int r = idx / m, c = idx - r * m;
-            double v = 0.0;
+            F v = F(0);
             if (r < md)
-                for (int k = 0; k < m; ++k) v = fma(a.alpha * Tb[(size_t)r * m + k], Z[k * LDA + c], v);
+                for (int k = 0; k < m; ++k) v = fma((F)(a.alpha * Tb[(size_t)r * m + k]), Z[k * LDA + c], v);
             W[r * LDA + c] = v;
         }
         __syncthreads();
@@ -284,21 +297,21 @@ __global__ void __launch_bounds__(CALC_NT) k_adjoint(AdjArgs A)
             const int nb = (m - c0 < KC_MAX) ? m - c0 : KC_MAX;
             for (int idx = tid; idx < m * nb; idx += CALC_NT) {
                 const int r = idx / nb, cc = idx - r * nb, c = c0 + cc;
-                double v = 0.0;
+                F v = F(0);
                 for (int k = 0; k < m; ++k) v = fma(Z[k * LDA + r], W[k * LDA + c], v);
                 // divided differences in closed form (no cancellation when
                 // l_i ~ l_j, exact limit f'(l) on the diagonal):
                 //   ETKF  f = l^-1/2:        F = -1 / (sqrt(li) sqrt(lj) (sqrt(li) + sqrt(lj)))
                 //   DEnKF f = (1 + 1/l) / 2: F = -1 / (2 li lj)
-                const double li = d[r], lj = d[c];
-                double F;
+                const F li = d[r], lj = d[c];
+                F dd;
                 if (etkf) {
-                    const double qi = sqrt(li), qj = sqrt(lj);
-                    F = -1.0 / (qi * qj * (qi + qj));
+                    const F qi = sqrt(li), qj = sqrt(lj);
+                    dd = F(-1) / (qi * qj * (qi + qj));
                 } else {
-                    F = -0.5 / (li * lj);
+                    dd = F(-0.5) / (li * lj);
                 }
-                tile[(size_t)cc * MP + r] = F * v;
+                tile[(size_t)cc * MP + r] = dd * v;
             }
             __syncthreads();
             for (int idx = tid; idx < m * nb; idx += CALC_NT) {
@@ -312,7 +325,7 @@ __global__ void __launch_bounds__(CALC_NT) k_adjoint(AdjArgs A)
             const int nb = (m - c0 < KC_MAX) ? m - c0 : KC_MAX;
             for (int idx = tid; idx < m * nb; idx += CALC_NT) {
                 const int r = idx / nb, cc = idx - r * nb, c = c0 + cc;
-                double v = 0.0;
+                F v = F(0);
                 for (int k = 0; k < m; ++k) v = fma(Z[r * LDA + k], W[k * LDA + c], v);
                 tile[(size_t)cc * MP + r] = v;
             }
@@ -328,7 +341,7 @@ __global__ void __launch_bounds__(CALC_NT) k_adjoint(AdjArgs A)
             const int nb = (m - r0 < KC_MAX) ? m - r0 : KC_MAX;
             for (int idx = tid; idx < nb * m; idx += CALC_NT) {
                 const int rr = idx / m, c = idx - rr * m, r = r0 + rr;
-                double v = 0.0;
+                F v = F(0);
                 for (int k = 0; k < m; ++k) v = fma(W[r * LDA + k], Z[c * LDA + k], v);
                 tile[(size_t)rr * MP + c] = v;
             }
@@ -343,7 +356,7 @@ __global__ void __launch_bounds__(CALC_NT) k_adjoint(AdjArgs A)
         for (int idx = tid; idx < m * m; idx += CALC_NT) {
             const int r = idx / m, c = idx - r * m;
             if (c < r) continue;
-            const double v = W[r * LDA + c] + W[c * LDA + r];
+            const F v = W[r * LDA + c] + W[c * LDA + r];
             W[r * LDA + c] = v;
             W[c * LDA + r] = v;
         }
@@ -352,7 +365,7 @@ __global__ void __launch_bounds__(CALC_NT) k_adjoint(AdjArgs A)
     }
     // 3. per-observation sensitivities (second pass over the local obs; the
     //    chunks are staged in the tile region, P stays in W)
-    AdjProc ap(A, s, tile, lam, w, Pp, LDA, MP, qx, qy, qz);
+    AdjProc<F> ap(A, s, tile, lam, w, Pp, LDA, MP, qx, qy, qz);
     enumerate_obs<0>(a, a.kc, qx, qy, qz, s, ap, false);
     double rs = la::block_sum<CALC_NT>(ap.rho_acc, red);
     if (tid == 0 && rs != 0.0) atomicAdd(A.drho, rs);
@@ -417,18 +430,20 @@ __global__ void k_adj_sorted(int nsorted, const int* __restrict__ sid, const flo
     R[p] = sg * sg;
 }
 
-template <int R>
+template <int R, typename F>
 static enkfg_status launch_adj(enkfg_ctx* ctx, AdjArgs& A, cudaStream_t st)
 {
     constexpr int MP = 16 * R, LDA = MP + 1;
-    size_t smem = (size_t)KC_MAX * MP * 8 + LIST_EXTRA * 8 + KC_MAX * 8 + 2 * (size_t)MP * LDA * 8 + 8 * MP * 8 +
-                  2 * ENKFG_MAXTYPES * 8 + (CALC_NT / 32) * 8 + LIST_EXTRA * 4 + ENKFG_MAXTYPES * 4 + 256;
+    constexpr size_t FS = sizeof(F);
+    size_t smem = LIST_EXTRA * 8 + (size_t)KC_MAX * MP * FS + KC_MAX * FS + 2 * (size_t)MP * LDA * FS +
+                  8 * MP * FS + 8 + 2 * ENKFG_MAXTYPES * 8 + (CALC_NT / 32) * 8 + LIST_EXTRA * 4 +
+                  ENKFG_MAXTYPES * 4 + 256;
     if (smem > 227 * 1024) {
         set_err(ctx, "adjoint: nmem = %d needs too much shared memory", A.c.m);
         return ENKFG_EUNSUPPORTED;
     }
-    CK(cudaFuncSetAttribute(k_adjoint<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    k_adjoint<R><<<A.c.npts, CALC_NT, smem, st>>>(A);
+    CK(cudaFuncSetAttribute(k_adjoint<R, F>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    k_adjoint<R, F><<<A.c.npts, CALC_NT, smem, st>>>(A);
     CKL();
     return ENKFG_OK;
 }
@@ -489,10 +504,11 @@ enkfg_status run_adjoint(enkfg_ctx* ctx, const enkfg_calc_params* p, const doubl
     A.dinn = d_dinn;
     A.dvar = d_dvar;
     A.drho = d_drho;
-    if (m <= 32) s = launch_adj<2>(ctx, A, st);
-    else if (m <= 48) s = launch_adj<3>(ctx, A, st);
-    else if (m <= 64) s = launch_adj<4>(ctx, A, st);
-    else s = launch_adj<6>(ctx, A, st);
+    const bool f32 = (p->precision == ENKFG_PREC_MIXED);
+    if (m <= 32) s = f32 ? launch_adj<2, float>(ctx, A, st) : launch_adj<2, double>(ctx, A, st);
+    else if (m <= 48) s = f32 ? launch_adj<3, float>(ctx, A, st) : launch_adj<3, double>(ctx, A, st);
+    else if (m <= 64) s = f32 ? launch_adj<4, float>(ctx, A, st) : launch_adj<4, double>(ctx, A, st);
+    else s = f32 ? launch_adj<6, float>(ctx, A, st) : launch_adj<6, double>(ctx, A, st);
     cudaError_t e = cudaStreamSynchronize(st);
     cudaFree(sig);
     cudaFree(R);

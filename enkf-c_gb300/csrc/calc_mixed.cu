@@ -425,8 +425,11 @@ struct GramProcTC {
         const int m = a.m;
         const float* cq = ms.qs + m;   // 1.5 2^23 q_r: (v + c) - c rounds v to a multiple of q_r
         double ssq = 0.0;
-        auto one = [&](int rg, int r) -> float {
-            const float v = __fmul_rn(rp[rg << 3], ck);
+        // the raw values are all loaded before any piece is stored (the
+        // tiles and the raw rows share shared memory, so a store would
+        // otherwise keep the next load behind it), then split
+        auto split = [&](int rg, int r, float raw_v) -> float {
+            const float v = __fmul_rn(raw_v, ck);
             if (TS) ssq += (double)v * (double)v;
             // hi = q rint(v / q): |v| <= 256 q < 2^22 q keeps v + c in the
             // binade of c, whose spacing is q (ties to even, as rint)
@@ -444,12 +447,19 @@ struct GramProcTC {
             return v;
         };
         if constexpr (FS) {
+            float rv[2 * HB];
+#pragma unroll
+            for (int i = 0; i < 2 * HB; ++i) {
+                const int rg = rg0 + i * rstep;
+                const int r = (rg << 3) + (lane >> 2);
+                rv[i] = (rg < nrg && r < m) ? rp[rg << 3] : 0.0f;
+            }
 #pragma unroll
             for (int i = 0; i < 2 * HB; ++i) {
                 const int rg = rg0 + i * rstep;
                 const int r = (rg << 3) + (lane >> 2);
                 if (rg < nrg && r < m) {
-                    const float v = one(rg, r);
+                    const float v = split(rg, r, rv[i]);
                     const float p = v * xk, pe = fmaf(v, xk, -p);
                     const float sm = fh[i] + p, bp = sm - fh[i];
                     fl[i] += ((fh[i] - (sm - bp)) + (p - bp)) + pe;
@@ -457,9 +467,23 @@ struct GramProcTC {
                 }
             }
         } else {
-            for (int rg = rg0; rg < nrg; rg += rstep) {
+            int rg = rg0;
+            for (; rg + 3 * rstep < nrg; rg += 4 * rstep) {
+                float rv[4];
+#pragma unroll
+                for (int u = 0; u < 4; ++u) {
+                    const int r = ((rg + u * rstep) << 3) + (lane >> 2);
+                    rv[u] = r < m ? rp[(rg + u * rstep) << 3] : 0.0f;
+                }
+#pragma unroll
+                for (int u = 0; u < 4; ++u) {
+                    const int r = ((rg + u * rstep) << 3) + (lane >> 2);
+                    if (r < m) split(rg + u * rstep, r, rv[u]);
+                }
+            }
+            for (; rg < nrg; rg += rstep) {
                 const int r = (rg << 3) + (lane >> 2);
-                if (r < m) one(rg, r);
+                if (r < m) split(rg, r, rp[rg << 3]);
             }
         }
         return ssq;

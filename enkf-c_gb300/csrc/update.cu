@@ -477,6 +477,7 @@ static inline size_t upd_v3_smem(int m, int md, int stride, int nf)
 template <bool F64, int EPL>
 __global__ void __launch_bounds__(UPD_NT) k_update_v3(UpdArgs a)
 {
+    static_assert(U3_KE == 16 && U3_NC == 8, "the staging loops index by shifts");
     extern __shared__ __align__(16) float usm[];
     const int m = a.m, md = a.md, st = a.stride, nf = a.nfield;   // nf <= U3_FG
     const int tid = threadIdx.x, lane = tid & 31, c = tid >> 5;
@@ -497,12 +498,14 @@ __global__ void __launch_bounds__(UPD_NT) k_update_v3(UpdArgs a)
     const float w2j = __fdiv_rn((float)stepj, (float)st), w1j = __fsub_rn(1.0f, w2j);
     const bool jint = (st > 1 && stepj > 0);
 
-    // 1. the field block and the j-interpolated w of the strided columns
-    for (int idx = tid; idx < nf * m * U3_NC; idx += UPD_NT) {
-        const int cc = idx % U3_NC, fe = idx / U3_NC;
-        if (cc < ncell) {
-            const int f = fe / m, e = fe - f * m;
-            raw[idx] = a.fields[((size_t)f * m + e) * a.plane + (size_t)jt * a.mni + i0 + cc];
+    // 1. the field block (member rows of 8 cells: 32-byte pieces) and the
+    //    j-interpolated w of the strided columns
+    for (int q = 0; q < nf; ++q) {
+        const float* src = a.fields + (size_t)q * m * a.plane + (size_t)jt * a.mni + i0;
+        float* dst = raw + (size_t)q * m * U3_NC;
+        for (int idx = tid; idx < m * U3_NC; idx += UPD_NT) {
+            const int e = idx >> 3, cc = idx & 7;
+            if (cc < ncell) dst[idx] = src[(size_t)e * a.plane + cc];
         }
     }
     for (int idx = tid; idx < nsc * m; idx += UPD_NT) {
@@ -576,20 +579,40 @@ __global__ void __launch_bounds__(UPD_NT) k_update_v3(UpdArgs a)
     for (int e0 = 0; e0 < m; e0 += U3_KE) {
         const int ke_n = min(U3_KE, m - e0);
         __syncthreads();   // the previous chunk is consumed (and the anomalies are written)
-        for (int idx = tid; idx < nsc * md * U3_KE; idx += UPD_NT) {
-            const int ke = idx % U3_KE, se = idx / U3_KE;
-            const int s = se / md, e1 = se - s * md;
-            float v = 0.0f;
-            if (ke < ke_n) {
-                const int col = (s < nsc - 1) ? iia + s : nb;
-                const size_t o = ((size_t)jj * a.ni + col) * md * m + (size_t)e1 * m + e0 + ke;
-                v = __ldg(&a.T[o]);
+        // rows (slot, e1) of U3_KE members: four lanes per row with 16-byte
+        // loads when the rows are 16-byte aligned (nmem a multiple of 4 and
+        // the chunk whole), else one lane per element
+        const size_t jstep = ((size_t)jj2 - jj) * a.ni * md * m;
+        if ((m & 3) == 0 && ke_n == U3_KE) {
+            for (int idx = tid; idx < nsc * md * 4; idx += UPD_NT) {
+                const int qd = idx & 3, se = idx >> 2;
+                const int sl = se / md, e1 = se - sl * md;
+                const int col = (sl < nsc - 1) ? iia + sl : nb;
+                const size_t o = ((size_t)jj * a.ni + col) * md * m + (size_t)e1 * m + e0 + 4 * qd;
+                float4 v = __ldg(reinterpret_cast<const float4*>(a.T + o));
                 if (jint) {
-                    const float b = __ldg(&a.T[o + ((size_t)jj2 - jj) * a.ni * md * m]);
-                    v = __fadd_rn(__fmul_rn(v, w1j), __fmul_rn(b, w2j));
+                    const float4 b = __ldg(reinterpret_cast<const float4*>(a.T + o + jstep));
+                    v.x = __fadd_rn(__fmul_rn(v.x, w1j), __fmul_rn(b.x, w2j));
+                    v.y = __fadd_rn(__fmul_rn(v.y, w1j), __fmul_rn(b.y, w2j));
+                    v.z = __fadd_rn(__fmul_rn(v.z, w1j), __fmul_rn(b.z, w2j));
+                    v.w = __fadd_rn(__fmul_rn(v.w, w1j), __fmul_rn(b.w, w2j));
+                }
+                *reinterpret_cast<float4*>(&Tc[((size_t)sl * md + e1) * U3_TLD + 4 * qd]) = v;
+            }
+        } else {
+            for (int sl = 0; sl < nsc; ++sl) {
+                const int col = (sl < nsc - 1) ? iia + sl : nb;
+                for (int idx = tid; idx < md * U3_KE; idx += UPD_NT) {
+                    const int e1 = idx >> 4, ke = idx & 15;
+                    float v = 0.0f;
+                    if (ke < ke_n) {
+                        const size_t o = ((size_t)jj * a.ni + col) * md * m + (size_t)e1 * m + e0 + ke;
+                        v = __ldg(&a.T[o]);
+                        if (jint) v = __fadd_rn(__fmul_rn(v, w1j), __fmul_rn(__ldg(&a.T[o + jstep]), w2j));
+                    }
+                    Tc[((size_t)sl * md + e1) * U3_TLD + ke] = v;
                 }
             }
-            Tc[((size_t)s * md + e1) * U3_TLD + ke] = v;
         }
         __syncthreads();
         if (active) {
@@ -726,11 +749,12 @@ __global__ void __launch_bounds__(UPD_NT) k_update_v3(UpdArgs a)
     }
     __syncthreads();
     // 5. the block back out
-    for (int idx = tid; idx < nf * m * U3_NC; idx += UPD_NT) {
-        const int cc = idx % U3_NC, fe = idx / U3_NC;
-        if (cc < ncell) {
-            const int f = fe / m, e = fe - f * m;
-            a.fields[((size_t)f * m + e) * a.plane + (size_t)jt * a.mni + i0 + cc] = raw[idx];
+    for (int q = 0; q < nf; ++q) {
+        float* dst = a.fields + (size_t)q * m * a.plane + (size_t)jt * a.mni + i0;
+        const float* src = raw + (size_t)q * m * U3_NC;
+        for (int idx = tid; idx < m * U3_NC; idx += UPD_NT) {
+            const int e = idx >> 3, cc = idx & 7;
+            if (cc < ncell) dst[(size_t)e * a.plane + cc] = src[idx];
         }
     }
 }

@@ -385,14 +385,16 @@ class Enkfg:
                                              _p(w, C.c_float)))
 
     # ---- adjoint (observation impact) -----------------------------------
-    def adjoint_transforms(self, wbar, Tbar=None, mode=MODE_ENKF, scheme=SCHEME_ETKF, alpha=1.0):
-        """dJ/d(innovation) [nobs], dJ/d(estd^2) [nobs], dJ/d(radius scale)."""
+    def adjoint_transforms(self, wbar, Tbar=None, mode=MODE_ENKF, scheme=SCHEME_ETKF, alpha=1.0,
+                           precision=PREC_FP64):
+        """dJ/d(innovation) [nobs], dJ/d(estd^2) [nobs], dJ/d(radius scale);
+        precision PREC_MIXED runs the FP32 (production) form."""
         wbar = np.ascontiguousarray(wbar, np.float64)
         Tbar = None if Tbar is None else np.ascontiguousarray(Tbar, np.float64)
         dinn = np.zeros(self.nobs)
         dvar = np.zeros(self.nobs)
         drad = np.zeros(1)
-        prm = CalcParams(mode, scheme, float(alpha), PATH_PLAIN, PREC_FP64, 0, 0)
+        prm = CalcParams(mode, scheme, float(alpha), PATH_PLAIN, precision, 0, 0)
         self._ck(self.L.enkfg_adjoint_transforms(self.h, C.byref(prm), _p(wbar, C.c_double), _p(Tbar, C.c_double),
                                                  _p(dinn, C.c_double), _p(dvar, C.c_double), _p(drad, C.c_double)))
         return dinn, dvar, float(drad[0])

@@ -273,7 +273,9 @@ ENKFG_API enkfg_status enkfg_rebuild_index(enkfg_ctx* ctx);
  * reference; it differentiates das_calctransforms, transforms.c:1150-1360).
  * Given wbar = dJ/dw [nj][ni][m] (and optionally Tbar = dJ/dT
  * [nj][ni][m_dyn][m], NULL if J does not depend on T) for the transforms of
- * the current inputs, computes, in FP64,
+ * the current inputs, computes, in FP64 (p->precision ENKFG_PREC_FP64) or
+ * in FP32 arithmetic with FP64 accumulators (ENKFG_PREC_MIXED, the
+ * production form),
  *   dJ_dinnovation [nobs]  dJ/d(y - Hx) per observation,
  *   dJ_dvariance   [nobs]  dJ/d(estd^2) per observation,
  *   dJ_dradius     [1]     dJ/d(rho), rho a common scale of all LOCRAD

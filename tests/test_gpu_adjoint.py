@@ -10,7 +10,7 @@ localisation radius.
 The GPU forward and the GPU adjoint are wrapped, for this test only, in a
 torch.autograd.Function (ObsImpact).  Checks, all in FP64:
   * central finite differences (step 1e-6) of the GPU forward for 200 random
-    innovations and for rho: relative error <= 1e-5 (normwise over the 200);
+    innovations and for rho: relative error <= 1e-6 (normwise over the 200);
   * an FP64 reference gradient -- torch autograd through an independent
     pure-torch forward of the same analysis -- for the innovations, the
     variances and rho: relative error <= 1e-6.
@@ -69,8 +69,8 @@ def record(name, summary):
 
 
 class Problem:
-    def __init__(self, ctx):
-        w = synth.make(4, scale=0.08, nobs=2500, nmem=32)
+    def __init__(self, ctx, nmem=64, scale=0.1, nobs=4000):
+        w = synth.make(4, scale=scale, nobs=nobs, nmem=nmem)
         w.locrad = 8.0
         self.w = w
         self.ctx = ctx
@@ -110,11 +110,11 @@ class Problem:
         r = np.where(self.wet, xa - self.verify, 0.0)
         return float((r * r).sum()), r
 
-    def adjoint(self, r, rho):
+    def adjoint(self, r, rho, precision=0):
         w, ctx = self.w, self.ctx
         g = 2.0 * r
         wbar = ctx.adjoint_mean(self.field, g.reshape(w.nj, w.ni))
-        dinn, dvar, drho = ctx.adjoint_transforms(wbar, mode=0, scheme=w.scheme)
+        dinn, dvar, drho = ctx.adjoint_transforms(wbar, mode=0, scheme=w.scheme, precision=precision)
         return dinn, dvar, drho
 
 
@@ -247,11 +247,27 @@ def test_adjoint_against_fd_and_reference(ctx):
     jrel = abs(float(J.detach()) - float(Jr.detach())) / abs(float(Jr.detach()))
     summary = dict(J=float(J.detach()), J_ref_rel=jrel, fd_innov=err_fd, fd_rho=err_rho_fd, ref_innov=err_ref_d,
                    ref_var=err_ref_R, ref_rho=err_ref_rho, n_fd=int(pick.size), nobs=int(w.nobs), nmem=m)
-    record("w_term_workload4_m32", summary)
+    record(f"w_term_workload4_m{m}", summary)
     assert jrel < 1e-9, summary
-    assert err_fd < 1e-5, summary
-    assert err_rho_fd < 1e-5, summary
+    assert err_fd < 1e-6, summary
+    assert err_rho_fd < 1e-6, summary
     assert err_ref_d < 1e-9 and err_ref_R < 1e-9 and err_ref_rho < 1e-9, summary
+
+
+def test_adjoint_fp32_production_against_fp64(ctx):
+    """The FP32 production adjoint (S'S, eigendecomposition, Daleckii-Krein
+    and per-observation passes in FP32, FP64 accumulators) against the FP64
+    adjoint on workload 4's shape with m = 64: normwise relative error of
+    each gradient (recorded; bound 1e-3)."""
+    prob = Problem(ctx)
+    J, r = prob.forward(prob.d0, prob.R0, 1.0)
+    g64 = prob.adjoint(r, 1.0, precision=0)
+    g32 = prob.adjoint(r, 1.0, precision=1)
+    rel = lambda a, b: float(np.linalg.norm(np.asarray(a) - np.asarray(b)) / np.linalg.norm(np.asarray(b)))
+    summary = dict(innov=rel(g32[0], g64[0]), var=rel(g32[1], g64[1]), rho=abs(g32[2] - g64[2]) / abs(g64[2]),
+                   nmem=prob.w.nmem, nobs=int(prob.w.nobs))
+    record(f"fp32_vs_fp64_workload4_m{prob.w.nmem}", summary)
+    assert summary["innov"] < 1e-3 and summary["var"] < 1e-3 and summary["rho"] < 1e-3, summary
 
 
 @pytest.mark.parametrize("scheme,nmem", [(1, 24), (0, 24), (1, 80)])
@@ -287,6 +303,31 @@ def test_adjoint_T_term_daleckii_krein(ctx, scheme, nmem):
     h = 1e-6
     fd = (J_of(1.0 + h) - J_of(1.0 - h)) / (2 * h)
 
+    # central differences in 50 innovations (J depends on them through w;
+    # the variances act through S, which is stored in float, so a 1e-6 step
+    # would measure S's rounding: they are checked against the reference)
+    def J_of_s(s_new):
+        ctx.set_obstypes(nl, lr, lw, np.ones(1))
+        ctx.set_obs(w.lon, w.lat, w.otype, w.status, w.estd, w.value)
+        ctx.set_S(S, s_new)
+        ctx.set_grid(w.x, w.y, stride=w.stride)
+        out = ctx.calctransforms(mode=0, scheme=scheme, alpha=alpha, want64=True, want_diag=False)
+        return float((Tbar * out["T64"]).sum() + (wbar * out["w64"]).sum())
+
+    R0v = w.estd.astype(np.float64) ** 2
+    sig0v = np.sqrt(R0v) * np.sqrt(m - 1.0)
+    big = np.nonzero(np.abs(dinn) > 1e-3 * np.abs(dinn).max())[0]
+    pick = np.random.default_rng(12).choice(big, size=min(50, big.size), replace=False)
+    fd_inn = np.zeros(pick.size)
+    for k, o in enumerate(pick):
+        sp = s.copy()
+        sp[o] += h / sig0v[o]
+        jp = J_of_s(sp)
+        sp[o] -= 2 * h / sig0v[o]
+        jm = J_of_s(sp)
+        fd_inn[k] = (jp - jm) / (2 * h)
+    err_fd_inn = float(np.linalg.norm(dinn[pick] - fd_inn) / np.linalg.norm(fd_inn))
+
     R0 = w.estd.astype(np.float64) ** 2
     sig0 = np.sqrt(R0) * np.sqrt(m - 1.0)
     d0 = s * sig0
@@ -300,11 +341,13 @@ def test_adjoint_T_term_daleckii_krein(ctx, scheme, nmem):
     Jr.backward()
     rel = lambda a, b: float(np.linalg.norm(a - b) / np.linalg.norm(b))
     summary = dict(J_ref_rel=abs(J0 - float(Jr)) / abs(float(Jr)), fd_rho=abs(drho - fd) / abs(fd),
+                   fd_innov=err_fd_inn, n_fd=int(pick.size),
                    ref_innov=rel(dinn, d2.grad.numpy()), ref_var=rel(dvar, R2.grad.numpy()),
                    ref_rho=abs(drho - float(rho2.grad)) / abs(float(rho2.grad)), nmem=m, nobs=int(w.nobs))
     record(f"T_term_{'etkf' if scheme == 1 else 'denkf'}_m{m}", summary)
     assert summary["J_ref_rel"] < 1e-9, summary
-    assert summary["fd_rho"] < 1e-5, summary
+    assert summary["fd_rho"] < 1e-6, summary
+    assert summary["fd_innov"] < 1e-6, summary
     # 1e-8: the Denman-Beavers reference itself is good to ~1e-10 when M's
     # eigenvalues cluster near 1 (m = 80 members over ~a dozen field modes)
     assert summary["ref_innov"] < 1e-8 and summary["ref_var"] < 1e-8 and summary["ref_rho"] < 1e-8, summary
