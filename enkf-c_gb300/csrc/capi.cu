@@ -72,6 +72,13 @@ ENKFG_API enkfg_status enkfg_set_wait_limit(enkfg_ctx* ctx, unsigned long long n
     return ENKFG_OK;
 }
 
+ENKFG_API enkfg_status enkfg_set_field_buffer_size(enkfg_ctx* ctx, int nfield)
+{
+    if (!ctx || nfield < 0) return ENKFG_EINVAL;
+    ctx->field_buffer = nfield;
+    return ENKFG_OK;
+}
+
 ENKFG_API enkfg_status enkfg_set_wait_drill(enkfg_ctx* ctx, int on)
 {
     if (!ctx) return ENKFG_EINVAL;
@@ -131,6 +138,10 @@ ENKFG_API void enkfg_destroy(enkfg_ctx* ctx)
     for (int k = 0; k < 10; ++k)
         if (ctx->ev[k]) cudaEventDestroy(ctx->ev[k]);
     for (int k = 0; k < ctx->nbev; ++k) cudaEventDestroy(ctx->bev[k]);
+    for (int k = 0; k < 2; ++k)
+        if (ctx->cstream[k]) cudaStreamDestroy(ctx->cstream[k]);
+    for (int k = 0; k < 9; ++k)
+        if (ctx->uev[k]) cudaEventDestroy(ctx->uev[k]);
     if (ctx->own_stream) ctx->stream = ctx->own_stream;
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
     free(ctx);
@@ -744,6 +755,15 @@ ENKFG_API enkfg_status enkfg_update_fields_dev(enkfg_ctx* ctx, const enkfg_updat
     return run_update(ctx, p, numlevels_dev, nfield, levels, fields_dev, infl_dev, pick(ctx, stream));
 }
 
+// The host-buffer update streams the field-layers through the device in
+// groups (the reference's FIELDBUFFERSIZE batches, update/update.c:1552-2132):
+// three device buffers in turn, the copy of group g + 1 in and of group g - 1
+// out running on the context's two copy streams while group g is updated.
+// A group holds whole multiples of the update kernel's field-layer pass
+// where it can (the transforms are staged once per pass) within about 3 GB.
+// With pinned host buffers the copies overlap the update; with pageable ones
+// they are staged by the driver and serialise.
+#define UPD_GROUP_BYTES ((size_t)3 << 30)
 ENKFG_API enkfg_status enkfg_update_fields(enkfg_ctx* ctx, const enkfg_update_params* p, const int* numlevels,
                                           int nfield, const int* levels, float* fields, float* infl)
 {
@@ -756,20 +776,56 @@ ENKFG_API enkfg_status enkfg_update_fields(enkfg_ctx* ctx, const enkfg_update_pa
     int j2 = p->j2 < 0 ? ctx->mnj - 1 : p->j2;
     size_t jsize = (size_t)(j2 - p->j1 + 1);
     size_t plane = jsize * ctx->mni;
-    size_t per = (size_t)(p->mode == ENKFG_MODE_ENOI ? p->nmem + 1 : p->nmem) * plane;
-    size_t nf = (size_t)nfield * per;
+    size_t per = (size_t)(p->mode == ENKFG_MODE_ENOI ? p->nmem + 1 : p->nmem) * plane;   // floats per field-layer
+    int G = (int)(UPD_GROUP_BYTES / (per * sizeof(float)));
+    if (G < 1) G = 1;
+    if (G >= 10) G -= G % 10;
+    if (ctx->field_buffer > 0) G = ctx->field_buffer;
+    if (G > nfield) G = nfield;
+    const int ngroups = (nfield + G - 1) / G;
+    const int nbuf = ngroups < 3 ? ngroups : 3;
     if ((s = ensure(ctx, &ctx->d_numlevels, &ctx->numlevels_cap, (size_t)ctx->mnj * ctx->mni))) return s;
-    if ((s = ensure(ctx, &ctx->d_fields, &ctx->fields_cap, nf))) return s;
-    if (infl && (s = ensure(ctx, &ctx->d_infl, &ctx->infl_cap, (size_t)nfield * plane))) return s;
-    CK(cudaMemcpyAsync(ctx->d_numlevels, numlevels, (size_t)ctx->mnj * ctx->mni * sizeof(int), cudaMemcpyHostToDevice, st));
-    CK(cudaMemcpyAsync(ctx->d_fields, fields, nf * sizeof(float), cudaMemcpyHostToDevice, st));
-    if ((s = run_update(ctx, p, ctx->d_numlevels, nfield, levels, ctx->d_fields, infl ? ctx->d_infl : nullptr, st)))
-        return s;
-    CK(cudaMemcpyAsync(fields, ctx->d_fields, nf * sizeof(float), cudaMemcpyDeviceToHost, st));
-    if (infl) CK(cudaMemcpyAsync(infl, ctx->d_infl, (size_t)nfield * plane * sizeof(float), cudaMemcpyDeviceToHost, st));
+    if ((s = ensure(ctx, &ctx->d_fields, &ctx->fields_cap, (size_t)nbuf * G * per))) return s;
+    if (infl && (s = ensure(ctx, &ctx->d_infl, &ctx->infl_cap, (size_t)nbuf * G * plane))) return s;
+    for (int k = 0; k < 2; ++k)
+        if (ctx->cstream[k] == nullptr) CK(cudaStreamCreateWithFlags(&ctx->cstream[k], cudaStreamNonBlocking));
+    for (int k = 0; k < 9; ++k)
+        if (ctx->uev[k] == nullptr) CK(cudaEventCreateWithFlags(&ctx->uev[k], cudaEventDisableTiming));
+    cudaStream_t cin = ctx->cstream[0], cout = ctx->cstream[1];
+    CK(cudaMemcpyAsync(ctx->d_numlevels, numlevels, (size_t)ctx->mnj * ctx->mni * sizeof(int), cudaMemcpyHostToDevice,
+                       st));
+    cudaEventRecord(ctx->ev[6], st);
+    for (int g = 0; g < ngroups; ++g) {
+        const int b = g % nbuf, f0 = g * G, nf = (nfield - f0 < G) ? nfield - f0 : G;
+        float* dbuf = ctx->d_fields + (size_t)b * G * per;
+        float* dinf = infl ? ctx->d_infl + (size_t)b * G * plane : nullptr;
+        cudaEvent_t in_done = ctx->uev[3 * b], upd_done = ctx->uev[3 * b + 1], out_done = ctx->uev[3 * b + 2];
+        // the buffer's previous group has left the device; the update before
+        // this call (stream order of st) has finished with the buffers
+        if (g >= nbuf) CK(cudaStreamWaitEvent(cin, out_done, 0));
+        else {
+            CK(cudaEventRecord(in_done, st));
+            CK(cudaStreamWaitEvent(cin, in_done, 0));
+        }
+        CK(cudaMemcpyAsync(dbuf, fields + (size_t)f0 * per, (size_t)nf * per * sizeof(float), cudaMemcpyHostToDevice,
+                           cin));
+        CK(cudaEventRecord(in_done, cin));
+        CK(cudaStreamWaitEvent(st, in_done, 0));
+        if ((s = run_update(ctx, p, ctx->d_numlevels, nf, levels + f0, dbuf, dinf, st))) return s;
+        CK(cudaEventRecord(upd_done, st));
+        CK(cudaStreamWaitEvent(cout, upd_done, 0));
+        CK(cudaMemcpyAsync(fields + (size_t)f0 * per, dbuf, (size_t)nf * per * sizeof(float), cudaMemcpyDeviceToHost,
+                           cout));
+        if (infl)
+            CK(cudaMemcpyAsync(infl + (size_t)f0 * plane, dinf, (size_t)nf * plane * sizeof(float),
+                               cudaMemcpyDeviceToHost, cout));
+        CK(cudaEventRecord(out_done, cout));
+    }
+    cudaEventRecord(ctx->ev[7], st);
+    CK(cudaStreamSynchronize(cout));
     CK(cudaStreamSynchronize(st));
     float ms = 0.0f;
-    cudaEventElapsedTime(&ms, ctx->ev[4], ctx->ev[5]);
+    cudaEventElapsedTime(&ms, ctx->ev[6], ctx->ev[7]);
     ctx->stage_ms[3] = ms;
     return ENKFG_OK;
 }

@@ -392,15 +392,16 @@ __device__ __forceinline__ void mm(float* C, const float* X, const float* Y, int
 }  // namespace em
 
 template <int R>
-__global__ void __launch_bounds__(EM_NT, 1) k_em_refine(CalcArgs a, EmSlots z)
+__global__ void __launch_bounds__(EM_NT, 2) k_em_refine(CalcArgs a, EmSlots z)
 {
     constexpr int MP = 16 * R, LDA = MP + 1;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int m = a.m, md = a.md;
     const int tid = threadIdx.x, slot = blockIdx.x, tx = tid & 15, ty = tid >> 4;
+    // two matrices: the products run in place (mm writes its result after
+    // every operand read), so that two CTAs fit on an SM
     float* Q = (float*)smem_raw;                     // [MP][LDA] eigenvectors (columns)
-    float* A = Q + MP * LDA;                         // [MP][LDA]
-    float* B = A + MP * LDA;                         // [MP][LDA]
+    float* B = Q + MP * LDA;                         // [MP][LDA] Z0, then R, D~, D
     float2* S = (float2*)(B + MP * LDA);             // [EM_KCH][MP] staged rows of P
     float* lam = (float*)(S + EM_KCH * MP);          // [MP] eigenvalues
     float* sig = lam + MP;                           // [MP] lambda^1/2
@@ -429,45 +430,50 @@ __global__ void __launch_bounds__(EM_NT, 1) k_em_refine(CalcArgs a, EmSlots z)
     }
     __syncthreads();
 
-    // 2. Z0 = Q diag(lambda^-1/2) Q'  (B = Q diag, A = B Q')
+    // 2. Z0 = Q diag(lambda^-1/2) Q'  (B = Q diag, then B Q' in place)
     for (int i = tid; i < MP * MP; i += EM_NT) {
         const int r = i / MP, c = i - r * MP;
         B[r * LDA + c] = c < m ? Q[r * LDA + c] * rsqrtf(lam[c]) : 0.0f;
     }
     __syncthreads();
-    em::mm<R, false, true, true>(A, B, Q, m, LDA);
+    em::mm<R, false, true, true>(B, B, Q, m, LDA);
     for (int i = tid; i < MP * MP; i += EM_NT) {
         const int r = i / MP, c = i - r * MP;
-        z.z0[z0 + i] = A[r * LDA + c];
+        z.z0[z0 + i] = B[r * LDA + c];
     }
 
-    // 3a. P = M Z0 (double-float; M as its hi/lo pair, rows from global)
-    {
-        float ph[R][R], pl[R][R];
+    // 3a. P = M Z0 (double-float; M as its hi/lo pair, rows from global),
+    //     in two halves of the column blocks (register pressure)
+    constexpr int RC = (R + 1) / 2;
+#pragma unroll
+    for (int cb = 0; cb < R; cb += RC) {
+        float ph[R][RC], pl[R][RC];
 #pragma unroll
         for (int r = 0; r < R; ++r)
 #pragma unroll
-            for (int c = 0; c < R; ++c) ph[r][c] = pl[r][c] = 0.0f;
+            for (int c = 0; c < RC; ++c) ph[r][c] = pl[r][c] = 0.0f;
         for (int k = 0; k < m; ++k) {
             float2 mv[R];
-            float zv[R];
+            float zv[RC];
 #pragma unroll
             for (int r = 0; r < R; ++r) {
                 const int i = ty + 16 * r;
                 mv[r] = i < m ? z.mhl[q0 + (size_t)i * m + k] : make_float2(0.0f, 0.0f);
             }
 #pragma unroll
-            for (int c = 0; c < R; ++c) zv[c] = A[k * LDA + tx + 16 * c];
+            for (int c = 0; c < RC; ++c) zv[c] = (cb + c < R) ? B[k * LDA + tx + 16 * (cb + c)] : 0.0f;
 #pragma unroll
             for (int r = 0; r < R; ++r)
 #pragma unroll
-                for (int c = 0; c < R; ++c) em::df_fma(ph[r][c], pl[r][c], mv[r].x, mv[r].y, zv[c]);
+                for (int c = 0; c < RC; ++c)
+                    if (cb + c < R) em::df_fma(ph[r][c], pl[r][c], mv[r].x, mv[r].y, zv[c]);
         }
 #pragma unroll
         for (int r = 0; r < R; ++r)
 #pragma unroll
-            for (int c = 0; c < R; ++c)
-                z.p[z0 + (size_t)(ty + 16 * r) * MP + tx + 16 * c] = make_float2(ph[r][c], pl[r][c]);
+            for (int c = 0; c < RC; ++c)
+                if (cb + c < R)
+                    z.p[z0 + (size_t)(ty + 16 * r) * MP + tx + 16 * (cb + c)] = make_float2(ph[r][c], pl[r][c]);
     }
     __syncthreads();   // P complete in global memory for the whole CTA
 
@@ -489,7 +495,7 @@ __global__ void __launch_bounds__(EM_NT, 1) k_em_refine(CalcArgs a, EmSlots z)
                 float zv[R];
                 float2 pv[R];
 #pragma unroll
-                for (int r = 0; r < R; ++r) zv[r] = A[(ty + 16 * r) * LDA + k0 + kk];
+                for (int r = 0; r < R; ++r) zv[r] = B[(ty + 16 * r) * LDA + k0 + kk];
 #pragma unroll
                 for (int c = 0; c < R; ++c) pv[c] = S[kk * MP + tx + 16 * c];
 #pragma unroll
@@ -500,6 +506,7 @@ __global__ void __launch_bounds__(EM_NT, 1) k_em_refine(CalcArgs a, EmSlots z)
             }
             __syncthreads();
         }
+        __syncthreads();   // every thread is done reading Z0 from B
         // R is symmetric: blocks c >= r formed, the others mirrored
 #pragma unroll
         for (int r = 0; r < R; ++r)
@@ -517,15 +524,15 @@ __global__ void __launch_bounds__(EM_NT, 1) k_em_refine(CalcArgs a, EmSlots z)
     __syncthreads();
 
     // 4. D~ = Q' R Q, D~_ij /= (sigma_i + sigma_j), D = Q D~ Q'
-    em::mm<R, true, false, false>(A, Q, B, m, LDA);
-    em::mm<R, false, false, true>(B, A, Q, m, LDA);
+    em::mm<R, true, false, false>(B, Q, B, m, LDA);
+    em::mm<R, false, false, true>(B, B, Q, m, LDA);
     for (int i = tid; i < MP * MP; i += EM_NT) {
         const int r = i / MP, c = i - r * MP;
         B[r * LDA + c] = (r < m && c < m) ? B[r * LDA + c] / (sig[r] + sig[c]) : 0.0f;
     }
     __syncthreads();
-    em::mm<R, false, false, false>(A, Q, B, m, LDA);
-    em::mm<R, false, true, true>(B, A, Q, m, LDA);
+    em::mm<R, false, false, false>(B, Q, B, m, LDA);
+    em::mm<R, false, true, true>(B, B, Q, m, LDA);
 
     // 5. T = Z0 + D in FP64, relaxed and cast (transforms.c:1270-1296);
     //    tr(M^-1) = |T|_F^2 for the degrees of freedom
@@ -586,7 +593,7 @@ template <int R>
 static size_t em_refine_smem()
 {
     constexpr int MP = 16 * R, LDA = MP + 1;
-    return (size_t)3 * MP * LDA * 4 + (size_t)EM_KCH * MP * 8 + (size_t)4 * MP * 4 + (size_t)3 * MP * 8 +
+    return (size_t)2 * MP * LDA * 4 + (size_t)EM_KCH * MP * 8 + (size_t)4 * MP * 4 + (size_t)3 * MP * 8 +
            (EM_NT / 32) * 8;
 }
 

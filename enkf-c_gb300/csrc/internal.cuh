@@ -50,6 +50,9 @@ struct enkfg_ctx {
     int device;
     cudaStream_t stream;        // stream all work goes to
     cudaStream_t own_stream;    // the context's own stream while a caller stream is bound
+    cudaStream_t cstream[2];    // host-buffer update: copies in, copies out (created on first use)
+    cudaEvent_t uev[9];         // host-buffer update: per buffer, copy-in / update / copy-out done
+    int field_buffer;           // host-buffer update: field-layers per group (0: automatic)
     char err[1024];
     long long launches;
     unsigned long long wait_ns; // bound on a device wait (enkfg_set_wait_limit)

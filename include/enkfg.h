@@ -241,8 +241,18 @@ typedef struct {
  * count.  infl (or NULL) receives [nfield][jsize][mni] inflation
  * (--write-inflation).  For ENKFG_MODE_ENOI the call is das_updatebg
  * (update.c:568-814) and fields are [nfield][nmem+1][jsize][mni] with the
- * background in slot nmem.  Uses the transforms resident in the context. */
+ * background in slot nmem.  Uses the transforms resident in the context.
+ * The field-layers stream through the device in groups (as the reference's
+ * FIELDBUFFERSIZE batches, update/update.c:1552-2132), three device buffers
+ * in turn: the copies in and out of neighbouring groups run on the
+ * context's copy streams while a group is updated, so with pinned host
+ * buffers the transfers overlap the update and the device holds three
+ * groups, not the whole ensemble. */
 ENKFG_API enkfg_status enkfg_update_fields(enkfg_ctx* ctx, const enkfg_update_params* p, const int* numlevels, int nfield, const int* levels, float* fields, float* infl);
+
+/* Field-layers per group of the host-buffer update (FIELDBUFFERSIZE,
+ * common/enkfprm.c:381-388); 0 (the default) picks groups of about 3 GB. */
+ENKFG_API enkfg_status enkfg_set_field_buffer_size(enkfg_ctx* ctx, int nfield);
 
 /* Device-resident form: fields/infl are device addresses. */
 ENKFG_API enkfg_status enkfg_update_fields_dev(enkfg_ctx* ctx, const enkfg_update_params* p, const int* numlevels_dev, int nfield, const int* levels, float* fields_dev, float* infl_dev, void* stream);

@@ -193,3 +193,26 @@ def test_update_against_reference_golden(ctx, precision):
         assert np.array_equal(got == 0.0, exp == 0.0), name
         tol = 1e-4 if alog else 2e-5
         assert close(got, exp) < tol, (name, close(got, exp))
+
+
+def test_update_streamed_groups_match_one_group(ctx):
+    """The host-buffer update in groups of 1 and 3 field-layers (three device
+    buffers in turn, copies overlapped on the copy streams) gives the same
+    fields as one group, and as the oracle (m = 96 and m = 24 kernels)."""
+    for nmem in (96, 24):
+        w = synth.make(3, scale=0.06, nobs=3000, nmem=nmem)
+        w.nlayers = 10
+        out = transforms(ctx, w)
+        fl = np.ascontiguousarray(w.fields.reshape(-1, *w.fields.shape[2:]))   # 20 field-layers
+        levels = np.tile(np.arange(w.fields.shape[1]), w.fields.shape[0])
+        ctx.set_field_buffer_size(0)
+        whole = ctx.updatefields(fl, w.numlevels, levels, inflation=1.03, inf_ratio=0.4)
+        for g in (1, 3):
+            ctx.set_field_buffer_size(g)
+            got = ctx.updatefields(fl, w.numlevels, levels, inflation=1.03, inf_ratio=0.4)
+            assert np.array_equal(got, whole), (nmem, g)
+        ctx.set_field_buffer_size(0)
+        ref = np.stack([oracle.updatefields(fl[f], out["T"], out["w"], w.numlevels, mode=0, nmem=w.nmem,
+                                            nmem_dynamic=w.nmem_dynamic, stride=w.stride, level=int(levels[f]),
+                                            inflation=1.03, inf_ratio=0.4) for f in range(fl.shape[0])])
+        assert close(whole, ref) < 2e-5
