@@ -299,7 +299,12 @@ struct MixedSync {
 // tapered innovation into every row it splits and keeps a double-float sum
 // per row (2 HB rows at most) in registers for the whole point; otherwise
 // S's is a separate pass over the staged rows by thread groups.
-template <int HB, bool FS, bool ST>
+// DF: compact form of the deferred solve -- one TMEM accumulator set (2N
+// columns) and the upper triangle of the double-float S'S packed in shared
+// memory, so that two CTAs fit on an SM; a window is drained at the end of
+// the round that closes it, after that round's MMAs, before the next round's
+// MMAs overwrite the set.
+template <int HB, bool FS, bool ST, bool DF>
 struct GramProcTC {
     const CalcArgs& a;
     const PointScratch& s;
@@ -346,50 +351,64 @@ struct GramProcTC {
         if (sync) __syncthreads();
     }
 
+    // element (r, c >= r) of the packed upper triangle (DF) is at pk(r) + c
+    __device__ __forceinline__ int pk(int r) const { return r * a.m - ((r * (r + 1)) >> 1); }
+
     // add accumulator set `set` to the shared double-float S'S (its MMAs
     // have completed); thread (warp w, lane l) owns row 32 (w % 4) + l and
-    // columns (w / 4) N/2 + [0, N/2)
+    // columns (w / 4) N/2 + [0, N/2).  The TMEM loads of two 8-column
+    // blocks (both accumulators) are issued before one wait.  DF: only c >=
+    // r, and blocks wholly below the diagonal are not loaded.
     __device__ __forceinline__ void read_set(int set)
     {
         const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
         if (*ms.err) return;
-        const int r = 32 * (wid & 3) + lane;
+        const int rq = 32 * (wid & 3), r = rq + lane;
         // stacked: lanes N..N+m-1 hold remainder products of row r - N
         const int lanes = ST ? ms.N + a.m : a.m;
-        if (32 * (wid & 3) < lanes) {
-            const int half = ms.N >> 1;
-            const int c0 = (wid >> 2) * half;
-            const uint32_t base = ms.taddr + ((uint32_t)(32 * (wid & 3)) << 16) + (uint32_t)(2 * set * ms.N + c0);
+        const int half = ms.N >> 1;
+        const int c0 = (wid >> 2) * half;
+        if (rq < lanes && !(DF && rq >= c0 + half)) {
+            const uint32_t base = ms.taddr + ((uint32_t)rq << 16) + (uint32_t)(2 * set * ms.N + c0);
             const bool direct = r < a.m;
             const bool offset = ST && r >= ms.N && r < ms.N + a.m;
-            float2* row = ms.Macc + (size_t)(direct ? r : 0) * ms.lda;
+            float2* row = ms.Macc + (direct ? (DF ? pk(r) : r * ms.lda) : 0);
             float* rrow = ST ? ms.Mrest + (size_t)(offset ? r - ms.N : 0) * ms.lda : nullptr;
+            constexpr int BB = 1;
 #pragma unroll
-            for (int b = 0; b < HB; ++b)
-                if (8 * b < half) {
-                    uint32_t vh[8], vr[8];
-                    tc::tmem_ld8_nowait(base + (uint32_t)(8 * b), vh);
-                    tc::tmem_ld8_nowait(base + (uint32_t)(ms.N + 8 * b), vr);
-                    tc::tmem_wait_ld();
-                    if (direct) {
+            for (int b0 = 0; b0 < HB; b0 += BB) {
+                if (8 * b0 >= half || (DF && c0 + 8 * (b0 + BB) <= rq)) continue;
+                uint32_t vh[BB][8], vr[BB][8];
 #pragma unroll
-                        for (int j = 0; j < 8; ++j) {
-                            const int c = c0 + 8 * b + j;
-                            if (c < a.m) {
-                                float2 acc = row[c];
-                                df_add(acc, __uint_as_float(vh[j]));
-                                acc.y += __uint_as_float(vr[j]);   // <= 2^-8 of hi*hi'
-                                row[c] = acc;
+                for (int u = 0; u < BB; ++u)
+                    if (b0 + u < HB && 8 * (b0 + u) < half) {
+                        tc::tmem_ld8_nowait(base + (uint32_t)(8 * (b0 + u)), vh[u]);
+                        tc::tmem_ld8_nowait(base + (uint32_t)(ms.N + 8 * (b0 + u)), vr[u]);
+                    }
+                tc::tmem_wait_ld();
+#pragma unroll
+                for (int u = 0; u < BB; ++u)
+                    if (b0 + u < HB && 8 * (b0 + u) < half) {
+                        if (direct) {
+#pragma unroll
+                            for (int j = 0; j < 8; ++j) {
+                                const int c = c0 + 8 * (b0 + u) + j;
+                                if (c < a.m && (!DF || c >= r)) {
+                                    float2 acc = row[c];
+                                    df_add(acc, __uint_as_float(vh[u][j]));
+                                    acc.y += __uint_as_float(vr[u][j]);   // <= 2^-8 of hi*hi'
+                                    row[c] = acc;
+                                }
+                            }
+                        } else if (offset) {
+#pragma unroll
+                            for (int j = 0; j < 8; ++j) {
+                                const int c = c0 + 8 * (b0 + u) + j;
+                                if (c < a.m) rrow[c] += __uint_as_float(vh[u][j]) + __uint_as_float(vr[u][j]);
                             }
                         }
-                    } else if (offset) {
-#pragma unroll
-                        for (int j = 0; j < 8; ++j) {
-                            const int c = c0 + 8 * b + j;
-                            if (c < a.m) rrow[c] += __uint_as_float(vh[j]) + __uint_as_float(vr[j]);
-                        }
                     }
-                }
+            }
         }
         tc::fence_before();
     }
@@ -401,11 +420,20 @@ struct GramProcTC {
     {
         const int tid = threadIdx.x, kc = ms.kc, m4 = a.mpad >> 2;
         float* dst = ms.rawb(rb);
+        // (row k, piece c) of element i = tid + j CALC_NT, stepped without a
+        // division per element
+        const int dk = CALC_NT / m4, dc = CALC_NT - dk * m4;
+        int k = tid / m4, c = tid - k * m4;
         for (int i = tid; i < kc * m4; i += CALC_NT) {
-            const int k = i / m4, c = i - k * m4;
             float* d = dst + k * ms.ldv + 4 * c;
             if (k < nc) tc::cp_async16(d, a.St + (size_t)lid[base + k] * a.mpad + 4 * c);
             else *reinterpret_cast<float4*>(d) = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            k += dk;
+            c += dc;
+            if (c >= m4) {
+                c -= m4;
+                ++k;
+            }
         }
         if (tid < kc) {
             double* d = ms.srawb(rb) + tid;
@@ -606,14 +634,16 @@ struct GramProcTC {
         }
         // 4. the window closed one round ago: its last commit is on the other
         //    buffer; drain it while this round's MMAs run
-        if (drain_set >= 0) {
+        if (!DF && drain_set >= 0) {
             wait_buf(drain_buf, false);
             read_set(drain_set);
             drain_set = -1;
         }
         // 5. close the current window when the next round might overflow it
+        //    (DF: drained at the end of this round)
         win_obs += nc;
-        if (win_obs + kc > MX_WIN) {
+        const bool close_now = DF && win_obs + kc > MX_WIN;
+        if (!DF && win_obs + kc > MX_WIN) {
             drain_set = win;
             drain_buf = buf;
             win ^= 1;
@@ -635,6 +665,12 @@ struct GramProcTC {
             }
             sy.completed(buf ^ 1);
             tc::fence_after();
+        }
+        if (close_now) {
+            // the single set: this round's MMAs, then the window into S'S
+            wait_buf(buf, false);
+            read_set(0);
+            win_obs = 0;
         }
         tc::cp_async_wait_all();
         __syncthreads();
@@ -888,7 +924,8 @@ static __host__ __device__ size_t mixed_list_bytes(int lseg)
     return a > b ? a : b;
 }
 
-static size_t mixed_smem_bytes(int m, int kc, int lseg, int st)
+// df: the compact deferred form (packed upper triangle, b only)
+static size_t mixed_smem_bytes(int m, int kc, int lseg, int st, int df)
 {
     int lda = (m % 2 == 0) ? m + 1 : m + 2;
     size_t s = 0;
@@ -898,9 +935,9 @@ static size_t mixed_smem_bytes(int m, int kc, int lseg, int st)
     s += (size_t)2 * kc * 8;                               // raw innovations, two buffers
     s += (size_t)2 * m * 4;                                // quantum q, rounding constant
     s += 16;                                               // alignment
-    s += (size_t)m * lda * 8;                              // Macc (also A)
+    s += df ? (size_t)m * (m + 1) / 2 * 8 : (size_t)m * lda * 8;   // Macc (also A)
     s += (size_t)2 * ((kc + 3) & ~3) * 4;                  // tapered innovations, taper of the round
-    s += (size_t)6 * (m + 1) * 8;                          // b d e cs sn v
+    s += (size_t)(df ? 1 : 6) * (m + 1) * 8;               // b d e cs sn v
     s += (size_t)ENKFG_MAXTYPES * 8 * 2;
     s += (size_t)(CALC_NT / 32) * 8;
     s += mixed_list_bytes(lseg);
@@ -911,7 +948,7 @@ static size_t mixed_smem_bytes(int m, int kc, int lseg, int st)
     return s;
 }
 
-template <int HB, bool FS, bool ST>
+template <int HB, bool FS, bool ST, bool DF>
 __global__ void __launch_bounds__(CALC_NT, 2) k_transforms_mixed(CalcArgs a, int kcm, int N, uint32_t tcols, int lseg)
 {
     extern __shared__ __align__(128) unsigned char smem_raw[];
@@ -925,16 +962,18 @@ __global__ void __launch_bounds__(CALC_NT, 2) k_transforms_mixed(CalcArgs a, int
     double* sraw0 = (double*)sp;      sp += (size_t)2 * kcm * 8;
     float* qs = (float*)sp;           sp += (size_t)2 * m * 4;
     sp = (unsigned char*)(((uintptr_t)sp + 15) & ~(uintptr_t)15);
-    double* Macc = (double*)sp;       sp += (size_t)m * lda * 8;
+    const int nmacc = DF ? m * (m + 1) / 2 : m * lda;      // DF: packed upper triangle
+    double* Macc = (double*)sp;       sp += (size_t)nmacc * 8;
     float* Mrest = (float*)sp;        sp += ST ? (size_t)m * lda * 4 : 0;
     float* sl = (float*)sp;           sp += (size_t)((kcm + 3) & ~3) * 4;
     float* lr = (float*)sp;           sp += (size_t)((kcm + 3) & ~3) * 4;
     double* b = (double*)sp;          sp += (m + 1) * 8;
-    double* d = (double*)sp;          sp += (m + 1) * 8;
-    double* e = (double*)sp;          sp += (m + 1) * 8;
-    double* cs = (double*)sp;         sp += (m + 1) * 8;
-    double* sn = (double*)sp;         sp += (m + 1) * 8;
-    double* v = (double*)sp;          sp += (m + 1) * 8;
+    // the in-kernel solve's vectors (not in the compact deferred form)
+    double* d = (double*)sp;          sp += DF ? 0 : (m + 1) * 8;
+    double* e = (double*)sp;          sp += DF ? 0 : (m + 1) * 8;
+    double* cs = (double*)sp;         sp += DF ? 0 : (m + 1) * 8;
+    double* sn = (double*)sp;         sp += DF ? 0 : (m + 1) * 8;
+    double* v = (double*)sp;          sp += DF ? 0 : (m + 1) * 8;
     double* tss = (double*)sp;        sp += ENKFG_MAXTYPES * 8;
     double* tpd = (double*)sp;        sp += ENKFG_MAXTYPES * 8;
     double* red = (double*)sp;        sp += (CALC_NT / 32) * 8;
@@ -1004,7 +1043,7 @@ __global__ void __launch_bounds__(CALC_NT, 2) k_transforms_mixed(CalcArgs a, int
             tpd[tid] = 0.0;
             tcount[tid] = 0;
         }
-        for (int i = tid; i < m * lda; i += CALC_NT) {
+        for (int i = tid; i < nmacc; i += CALC_NT) {
             Macc[i] = 0.0;   // also zero as float2
             if (ST) Mrest[i] = 0.0f;
         }
@@ -1017,7 +1056,7 @@ __global__ void __launch_bounds__(CALC_NT, 2) k_transforms_mixed(CalcArgs a, int
         if (ST)
             for (int i = tid; i < ms.piece; i += CALC_NT) ms.zblock()[i] = 0.0f;
         __syncthreads();
-        GramProcTC<HB, FS, ST> proc(a, s, ms, sy, rnd);
+        GramProcTC<HB, FS, ST, DF> proc(a, s, ms, sy, rnd);
         const int p = (a.sxf != nullptr && a.ndim == 2)
                           ? enumerate_obs_seg<2>(a, lseg, qx, qy, qz, slid, slcf, ictl + 8, nb0, ncum, tcount, proc)
                           : enumerate_obs_seg<1>(a, lseg, qx, qy, qz, slid, slcf, ictl + 8, nb0, ncum, tcount, proc);
@@ -1060,6 +1099,39 @@ __global__ void __launch_bounds__(CALC_NT, 2) k_transforms_mixed(CalcArgs a, int
                     (((double)proc.bl[0] + (double)proc.bl[1]) + ((double)proc.bl[2] + (double)proc.bl[3]));
             nparts = proc.sgroups;
         }
+        if constexpr (DF) {
+            // the batched solve's inputs straight from the packed S'S: M = I +
+            // S'S (upper triangle, FP64) into slot idx, S's, p and tr(S'S)
+            __syncthreads();
+            const size_t q0 = (size_t)idx * m * m;
+            if (tid < m) {
+                double acc = 0.0;
+                for (int g = 0; g < nparts; ++g) acc += bpart[g * m + tid];
+                a.eb[(size_t)idx * m + tid] = acc;
+            }
+            const float2* Mp = (const float2*)Macc;
+            const int lane = tid & 31;
+            for (int r = wid; r < m; r += CALC_NT / 32) {
+                const float2* row = Mp + proc.pk(r);
+                for (int c = r + lane; c < m; c += 32) {
+                    const float2 v2 = row[c];
+                    const double x = (double)v2.x + (double)v2.y;
+                    a.eq[q0 + (size_t)r * m + c] = c == r ? x + 1.0 : x;
+                }
+            }
+            double dg = 0.0;
+            if (tid < m) {
+                const float2 v2 = Mp[proc.pk(tid) + tid];
+                dg = (double)v2.x + (double)v2.y;
+            }
+            const double trss = la::block_sum<CALC_NT>(dg, red);
+            if (tid == 0) {
+                a.eaux[2 * (size_t)idx] = (double)p;
+                a.eaux[2 * (size_t)idx + 1] = trss;
+            }
+            __syncthreads();
+            continue;
+        }
         // double-float -> FP64 in place
         for (int i = tid; i < m * lda; i += CALC_NT) {
             float2 v2 = ((float2*)Macc)[i];
@@ -1086,17 +1158,17 @@ __global__ void __launch_bounds__(CALC_NT, 2) k_transforms_mixed(CalcArgs a, int
     if (wid == 0) tc::tmem_dealloc(*tslot, tcols);
 }
 
-template <int HB, bool FS, bool ST>
+template <int HB, bool FS, bool ST, bool DF>
 static enkfg_status launch_mixed_hb(enkfg_ctx* ctx, CalcArgs& a, int kcm, int N, uint32_t tcols, size_t smem,
                                     int lseg, cudaStream_t st)
 {
-    CK(cudaFuncSetAttribute(k_transforms_mixed<HB, FS, ST>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    CK(cudaFuncSetAttribute(k_transforms_mixed<HB, FS, ST, DF>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     // computed residency (the occupancy query reports one CTA per SM here)
     // and the carveout that holds it, the rest staying L1
     int per_sm = 0, carve = 100;
-    enkfg_status s = resident_ctas(ctx, (const void*)k_transforms_mixed<HB, FS, ST>, CALC_NT, smem, &per_sm, &carve);
+    enkfg_status s = resident_ctas(ctx, (const void*)k_transforms_mixed<HB, FS, ST, DF>, CALC_NT, smem, &per_sm, &carve);
     if (s) return s;
-    CK(cudaFuncSetAttribute(k_transforms_mixed<HB, FS, ST>, cudaFuncAttributePreferredSharedMemoryCarveout, carve));
+    CK(cudaFuncSetAttribute(k_transforms_mixed<HB, FS, ST, DF>, cudaFuncAttributePreferredSharedMemoryCarveout, carve));
     int grid = a.nitems;
     if (a.persistent) {
         int nsm = 0;
@@ -1107,7 +1179,7 @@ static enkfg_status launch_mixed_hb(enkfg_ctx* ctx, CalcArgs& a, int kcm, int N,
         if (grid > a.nitems) grid = a.nitems;
     }
     if (grid < 1) return ENKFG_OK;
-    k_transforms_mixed<HB, FS, ST><<<grid, CALC_NT, smem, st>>>(a, kcm, N, tcols, lseg);
+    k_transforms_mixed<HB, FS, ST, DF><<<grid, CALC_NT, smem, st>>>(a, kcm, N, tcols, lseg);
     CKL();
     return ENKFG_OK;
 }
@@ -1124,9 +1196,21 @@ enkfg_status launch_mixed(enkfg_ctx* ctx, CalcArgs& a, cudaStream_t st)
     int lseg = 1024;
     const size_t two = 113 * 1024, one = 227 * 1024;
     const int stk = N <= 64 ? 1 : 0;                     // stacked products
-    const size_t lim = mixed_smem_bytes(m, kcm, 256, stk) <= two ? two : one;
-    while (lseg > 256 && mixed_smem_bytes(m, kcm, lseg, stk) > lim) lseg >>= 1;
-    size_t smem = mixed_smem_bytes(m, kcm, lseg, stk);
+    const int hb = ((N >> 1) + 7) / 8;
+    if (a.defer && !stk && hb <= 6) {
+        // the compact deferred form: one TMEM set of 2N columns (at most
+        // 256) and the packed S'S, 16 observations a round -- two CTAs per
+        // SM, where that fits
+        int ls = 1024;
+        while (ls > 256 && mixed_smem_bytes(m, 16, ls, 0, 1) > two) ls >>= 1;
+        const size_t sm = mixed_smem_bytes(m, 16, ls, 0, 1);
+        uint32_t tc1 = 32;
+        while ((int)tc1 < 2 * N) tc1 <<= 1;
+        if (sm <= two && tc1 <= 256) return launch_mixed_hb<6, false, false, true>(ctx, a, 16, N, tc1, sm, ls, st);
+    }
+    const size_t lim = mixed_smem_bytes(m, kcm, 256, stk, 0) <= two ? two : one;
+    while (lseg > 256 && mixed_smem_bytes(m, kcm, lseg, stk, 0) > lim) lseg >>= 1;
+    size_t smem = mixed_smem_bytes(m, kcm, lseg, stk, 0);
     if (smem > 227 * 1024) {
         set_err(ctx, "mixed path: nmem = %d needs %zu bytes of shared memory", m, smem);
         return ENKFG_EUNSUPPORTED;
@@ -1136,12 +1220,11 @@ enkfg_status launch_mixed(enkfg_ctx* ctx, CalcArgs& a, cudaStream_t st)
         set_err(ctx, "mixed path: tile too small for the per-type pass");
         return ENKFG_EUNSUPPORTED;
     }
-    const int hb = ((N >> 1) + 7) / 8;
     // S's fused into the split up to 8 rows per thread (registers)
     // (N <= 64 is hb <= 4: fused S's and stacked products together)
-    if (hb <= 2) return launch_mixed_hb<2, true, true>(ctx, a, kcm, N, tcols, smem, lseg, st);
-    if (hb <= 3) return launch_mixed_hb<3, true, true>(ctx, a, kcm, N, tcols, smem, lseg, st);
-    if (hb <= 4) return launch_mixed_hb<4, true, true>(ctx, a, kcm, N, tcols, smem, lseg, st);
-    if (hb <= 6) return launch_mixed_hb<6, false, false>(ctx, a, kcm, N, tcols, smem, lseg, st);
-    return launch_mixed_hb<8, false, false>(ctx, a, kcm, N, tcols, smem, lseg, st);
+    if (hb <= 2) return launch_mixed_hb<2, true, true, false>(ctx, a, kcm, N, tcols, smem, lseg, st);
+    if (hb <= 3) return launch_mixed_hb<3, true, true, false>(ctx, a, kcm, N, tcols, smem, lseg, st);
+    if (hb <= 4) return launch_mixed_hb<4, true, true, false>(ctx, a, kcm, N, tcols, smem, lseg, st);
+    if (hb <= 6) return launch_mixed_hb<6, false, false, false>(ctx, a, kcm, N, tcols, smem, lseg, st);
+    return launch_mixed_hb<8, false, false, false>(ctx, a, kcm, N, tcols, smem, lseg, st);
 }
