@@ -236,8 +236,6 @@ struct MixedShared {
     float* Mrest;          // [m x lda] stacked form: the remainder products from the offset lanes
     int lda;
     int stacked;           // tile order [hi mid lo Z] [lo hi mid] (else [hi mid lo] x 2)
-    float* sl;             // [kc] tapered innovations of the round
-    float* lr;             // [kc] taper coefficients of the round (0 past its end)
     uint64_t* mbar;        // [2] one per operand buffer
     uint32_t taddr;
     int N;                 // MMA N (m rounded up to 16)
@@ -315,18 +313,24 @@ struct GramProcTC {
     int win_obs;       // observations in the current window
     int drain_set;     // closed window awaiting its drain (-1: none)
     int drain_buf;     // operand buffer whose commit closes it
-    int sgroups;       // S's thread groups: CALC_NT / (m rounded up to 32)
-    int s_g, s_r;      // this thread's group and member
-    float bh[4], bl[4]; // S's for member s_r, group s_g: four double-float partial sums
+    int sgroups;       // S's observation groups (warps 0 .. 6; the last warp issues the MMAs)
+    int s_g, s_q;      // this thread's group and quad of members (4 s_q .. 4 s_q + 3)
+    float bh[4], bl[4]; // S's of those four members over group s_g: double-float sums
+    // DF: the batch staged last round, whose MMAs are issued at the start of
+    // the next round (while that round is split), and whether the window
+    // closes with it
+    bool pend, drain_after;
+    int pend_buf, pend_nc;
     float fh[FS ? 2 * HB : 1], fl[FS ? 2 * HB : 1];   // fused S's: per row slot
     __device__ __forceinline__ GramProcTC(const CalcArgs& a_, const PointScratch& s_, MixedShared& ms_, MixedSync& sy_,
                                           uint32_t& rnd_)
-        : a(a_), s(s_), ms(ms_), sy(sy_), rnd(rnd_), win(0), win_obs(0), drain_set(-1), drain_buf(0)
+        : a(a_), s(s_), ms(ms_), sy(sy_), rnd(rnd_), win(0), win_obs(0), drain_set(-1), drain_buf(0), pend(false),
+          drain_after(false), pend_buf(0), pend_nc(0)
     {
-        const int mr = (a.m + 31) & ~31;
-        sgroups = CALC_NT / mr;
-        s_g = (int)threadIdx.x / mr;
-        s_r = (int)threadIdx.x - s_g * mr;
+        const int nq = (a.m + 3) >> 2;
+        sgroups = (CALC_NT - 32) / nq;
+        s_g = (int)threadIdx.x / nq;
+        s_q = (int)threadIdx.x - s_g * nq;
 #pragma unroll
         for (int i = 0; i < (FS ? 2 * HB : 1); ++i) fh[i] = fl[i] = 0.0f;
         for (int j = 0; j < 4; ++j) bh[j] = bl[j] = 0.0f;
@@ -517,6 +521,168 @@ struct GramProcTC {
         return ssq;
     }
 
+    // S's from the staged rows of raw buffer rb (compensated FP32, not
+    // fused): thread (group g, quad q) takes members 4q .. 4q + 3 (one
+    // 16-byte load a row) and observations g, g + G, ... < nc, with the
+    // taper and the tapered innovation formed as the fused split forms them
+    __device__ __forceinline__ void ss_pass(const float* lcf, int base, int nc, int rb)
+    {
+        if (FS || s_g >= sgroups) return;
+        const float* raw = ms.rawb(rb) + 4 * s_q;
+        const double* sr = ms.srawb(rb);
+        for (int k = s_g; k < nc; k += sgroups) {
+            const float4 rv = *reinterpret_cast<const float4*>(raw + k * ms.ldv);
+            const float c = lcf[base + k];
+            const float x = __fmul_rn((float)sr[k], c);
+            const float v[4] = { __fmul_rn(rv.x, c), __fmul_rn(rv.y, c), __fmul_rn(rv.z, c), __fmul_rn(rv.w, c) };
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                const float p = v[u] * x, pe = fmaf(v[u], x, -p);
+                const float sm = bh[u] + p, bp = sm - bh[u];
+                bl[u] += ((bh[u] - (sm - bp)) + (p - bp)) + pe;
+                bh[u] = sm;
+            }
+        }
+    }
+
+    // the MMAs of one staged batch (ng groups of 8 observations in operand
+    // buffer buf) into the current window's set, issued by one elected lane
+    // of the last warp: hi*hi' into the exact accumulator, the five other
+    // products (hi*mid', mid*hi', hi*lo', lo*hi', mid*mid') into the rest
+    // (stacked: four MMAs, see above).  A and B are the same tiles; A has
+    // 128 rows, of which rows >= N read the padding behind the tiles and land
+    // in accumulator rows that are never read.
+    __device__ __forceinline__ void issue_mmas(int buf, int ngroups)
+    {
+        if ((threadIdx.x >> 5) != CALC_NT / 32 - 1) return;
+        tc::fence_after();
+        float* tH = ms.tile(buf, 0);
+        float* tM = ms.tile(buf, 1);
+        float* tL = ms.tile(buf, 2);
+        const uint32_t sbo = (uint32_t)ms.kc * 32u, idesc = tc::idesc_tf32(MX_ROWS, ms.N);
+        const uint32_t dhh = ms.taddr + (uint32_t)(2 * win * ms.N), dr = dhh + (uint32_t)ms.N;
+        // a group of 8 observations is two 128-byte core matrices further
+        // on: 256 bytes, 16 in the descriptor's address field (addresses
+        // below 256 KB do not carry out of the field)
+        uint64_t dh = tc::desc_kmajor_noswizzle(tc::smem_u32(tH), 128u, sbo);
+        uint64_t dm = tc::desc_kmajor_noswizzle(tc::smem_u32(tM), 128u, sbo);
+        uint64_t dl = tc::desc_kmajor_noswizzle(tc::smem_u32(tL), 128u, sbo);
+        const uint32_t lead = tc::elect_lane();
+        if constexpr (ST) {
+            // A = [lo; Z] (buffer 0) or [Z; lo] (buffer 1) for lo*hi'
+            uint64_t dz = tc::desc_kmajor_noswizzle(tc::smem_u32(buf == 0 ? tL : ms.zblock()), 128u, sbo);
+            for (int g = 0; g < ngroups; ++g, dh += 16u, dm += 16u, dl += 16u, dz += 16u) {
+                const uint32_t fresh = (win_obs == 0 && g == 0) ? 0u : 1u;
+                tc::mma_tf32_lead(dhh, dh, dh, idesc, fresh, lead);   // [hi; mid] hi'
+                tc::mma_tf32_lead(dr, dh, dm, idesc, fresh, lead);    // [hi; mid] mid'
+                tc::mma_tf32_lead(dr, dh, dl, idesc, 1u, lead);       // [hi; mid] lo'
+                tc::mma_tf32_lead(dr, dz, dh, idesc, 1u, lead);       // lo hi'
+            }
+        } else {
+            for (int g = 0; g < ngroups; ++g, dh += 16u, dm += 16u, dl += 16u) {
+                const uint32_t fresh = (win_obs == 0 && g == 0) ? 0u : 1u;
+                tc::mma_tf32_lead(dhh, dh, dh, idesc, fresh, lead);
+                tc::mma_tf32_lead(dr, dh, dm, idesc, fresh, lead);
+                tc::mma_tf32_lead(dr, dm, dh, idesc, 1u, lead);
+                tc::mma_tf32_lead(dr, dh, dl, idesc, 1u, lead);
+                tc::mma_tf32_lead(dr, dl, dh, idesc, 1u, lead);
+                tc::mma_tf32_lead(dr, dm, dm, idesc, 1u, lead);
+            }
+        }
+        tc::commit_lead(ms.mbar + buf, lead);
+    }
+
+    // DF: issue the pending batch (every thread keeps the bookkeeping)
+    __device__ __forceinline__ void issue_pending()
+    {
+        issue_mmas(pend_buf, (pend_nc + 7) / 8);
+        sy.out |= 1u << pend_buf;
+        win_obs += pend_nc;
+        drain_after = win_obs + ms.kc > MX_WIN;
+        pend = false;
+    }
+
+    // DF round: the MMAs of the previous batch are issued first, so that
+    // they run while this batch is split and its S's formed; this batch's
+    // operand buffer is free once the MMAs of two batches ago are done.  A
+    // window closed by the batch just issued is drained at the end of the
+    // round (its MMAs have had the round to finish), before the next issue.
+    __device__ void round_df(const float* lcf, int base, int nc, int rb)
+    {
+        const int buf = (int)(rnd & 1u);
+        if (pend) issue_pending();
+        if (sy.outstanding(buf)) wait_buf(buf, false);
+        split_vec(buf, rb, lcf, base, nc);
+        ss_pass(lcf, base, nc, rb);
+        ++rnd;
+        pend = true;
+        pend_buf = buf;
+        pend_nc = nc;
+        if (drain_after) {
+            wait_buf(buf ^ 1, false);
+            read_set(0);
+            win_obs = 0;
+            drain_after = false;
+        }
+        tc::fence_async_smem();
+        tc::cp_async_wait_all();
+        __syncthreads();
+    }
+
+    // the hi / mid / lo pieces of a round without the fused S's: a thread
+    // takes (member r, K group kg) pairs -- four observations of one member
+    // -- and stores each piece as one 16-byte row of a core matrix, so that
+    // eight lanes fill one core matrix (128 contiguous bytes) and a warp's
+    // raw reads are consecutive members of one observation.  Rows >= m are
+    // not written (they only reach accumulator rows and columns that are
+    // never read); observations past nc have zero rows and zero taper.
+    __device__ __forceinline__ void split_vec(int buf, int rb, const float* lcf, int base, int nc)
+    {
+        const int m = a.m, nkg = ms.kc >> 2, rows = ((m + 7) >> 3) << 3;
+        const int npair = nkg * rows;
+        float* tH = ms.tile(buf, 0);
+        float* tM = ms.tile(buf, 1);
+        float* tL = ms.tile(buf, 2);
+        const float* raw = ms.rawb(rb);
+        const float* cq = ms.qs + m;
+        const int dk = CALC_NT / rows, dr = CALC_NT - dk * rows;
+        int kg = (int)threadIdx.x / rows, r = (int)threadIdx.x - kg * rows;
+        for (int i = threadIdx.x; i < npair; i += CALC_NT) {
+            if (r < m) {
+                const int k0 = kg << 2;
+                float v[4], c[4];
+#pragma unroll
+                for (int j = 0; j < 4; ++j) {
+                    v[j] = raw[(k0 + j) * ms.ldv + r];
+                    c[j] = k0 + j < nc ? lcf[base + k0 + j] : 0.0f;
+                }
+                const float cr = cq[r];
+                float h[4], md[4], lo[4];
+#pragma unroll
+                for (int j = 0; j < 4; ++j) {
+                    // as split_rows: hi = q rint(v / q) through the rounding
+                    // constant, mid and lo rounded to TF32 (to nearest, ties
+                    // away from zero)
+                    const float vv = __fmul_rn(v[j], c[j]);
+                    h[j] = __fsub_rn(__fadd_rn(vv, cr), cr);
+                    const float r1 = __fsub_rn(vv, h[j]);
+                    md[j] = tc::tf32_rna(r1);
+                    lo[j] = tc::tf32_rna(__fsub_rn(r1, md[j]));
+                }
+                const int off = ((((r >> 3) * nkg + kg) << 5)) + ((r & 7) << 2);
+                *reinterpret_cast<float4*>(tH + off) = make_float4(h[0], h[1], h[2], h[3]);
+                *reinterpret_cast<float4*>(tM + off) = make_float4(md[0], md[1], md[2], md[3]);
+                *reinterpret_cast<float4*>(tL + off) = make_float4(lo[0], lo[1], lo[2], lo[3]);
+            }
+            kg += dk;
+            r += dr;
+            if (r >= rows) {
+                r -= rows;
+                ++kg;
+            }
+        }
+    }
+
     // one round: nc (<= kc) observations at list positions [base, base + nc)
     // whose rows are in raw buffer rb
     __device__ void round(const float* lcf, int base, int nc, int t, int rb)
@@ -536,14 +702,7 @@ struct GramProcTC {
         float* tM = ms.tile(buf, 1);
         float* tL = ms.tile(buf, 2);
         const float* raw = ms.rawb(rb);
-        // 1. taper and tapered innovations of the round (zero past nc), for
-        //    the separate S's pass
-        if (!FS && tid < kc) {
-            const float c = tid < nc ? lcf[base + tid] : 0.0f;
-            ms.lr[tid] = c;
-            ms.sl[tid] = tid < nc ? (float)ms.srawb(rb)[tid] * c : 0.0f;
-        }
-        // tapered S: hi / mid / lo pieces into this round's operand tiles.
+        // 1. tapered S: hi / mid / lo pieces into this round's operand tiles.
         // One warp per core matrix (8 rows x 4 observations = 128 bytes):
         // lane -> row r&7 = lane>>2, observation k&3 = lane&3, so the piece
         // stores and the raw reads (row stride = 8 mod 32) are conflict-free;
@@ -561,89 +720,28 @@ struct GramProcTC {
             const float xk = (FS && k < nc) ? __fmul_rn((float)ms.srawb(rb)[k], ck) : 0.0f;
             const float* rp = raw + k * ms.ldv + (lane >> 2);
             if (tsum) ssq = split_rows<true>(tH, tM, tL, rp, ck, xk, nrg, nkg, kg, rg0, rstep, lane);
-            else split_rows<false>(tH, tM, tL, rp, ck, xk, nrg, nkg, kg, rg0, rstep, lane);
+            else if (FS) split_rows<false>(tH, tM, tL, rp, ck, xk, nrg, nkg, kg, rg0, rstep, lane);
+            else split_vec(buf, rb, lcf, base, nc);
         }
         tc::fence_async_smem();
         __syncthreads();
-        // 2. one thread issues the round's MMAs into the current window's
-        //    set: hi*hi' into the exact accumulator, the five other products
-        //    (hi*mid', mid*hi', hi*lo', lo*hi', mid*mid') into the rest.  A
-        //    and B are the same tiles; A has 128 rows, of which rows >= N
-        //    read the padding behind the tiles and land in accumulator rows
-        //    that are never read.
-        const int ngroups = (nc + 7) / 8;
-        // the last warp issues (one elected lane), so that the S's of the
-        // first warps runs at the same time
-        if ((tid >> 5) == CALC_NT / 32 - 1) {
-            tc::fence_after();
-            const uint32_t sbo = (uint32_t)kc * 32u, idesc = tc::idesc_tf32(MX_ROWS, ms.N);
-            const uint32_t dhh = ms.taddr + (uint32_t)(2 * win * ms.N), dr = dhh + (uint32_t)ms.N;
-            // a group of 8 observations is two 128-byte core matrices further
-            // on: 256 bytes, 16 in the descriptor's address field (addresses
-            // below 256 KB do not carry out of the field)
-            uint64_t dh = tc::desc_kmajor_noswizzle(tc::smem_u32(tH), 128u, sbo);
-            uint64_t dm = tc::desc_kmajor_noswizzle(tc::smem_u32(tM), 128u, sbo);
-            uint64_t dl = tc::desc_kmajor_noswizzle(tc::smem_u32(tL), 128u, sbo);
-            if constexpr (ST) {
-                // A = [lo; Z] (buffer 0) or [Z; lo] (buffer 1) for lo*hi'
-                uint64_t dz = tc::desc_kmajor_noswizzle(tc::smem_u32(buf == 0 ? tL : ms.zblock()), 128u, sbo);
-                const uint32_t lead = tc::elect_lane();
-                for (int g = 0; g < ngroups; ++g, dh += 16u, dm += 16u, dl += 16u, dz += 16u) {
-                    const uint32_t fresh = (win_obs == 0 && g == 0) ? 0u : 1u;
-                    tc::mma_tf32_lead(dhh, dh, dh, idesc, fresh, lead);   // [hi; mid] hi'
-                    tc::mma_tf32_lead(dr, dh, dm, idesc, fresh, lead);    // [hi; mid] mid'
-                    tc::mma_tf32_lead(dr, dh, dl, idesc, 1u, lead);       // [hi; mid] lo'
-                    tc::mma_tf32_lead(dr, dz, dh, idesc, 1u, lead);       // lo hi'
-                }
-                tc::commit_lead(ms.mbar + buf, lead);
-            } else {
-                const uint32_t lead = tc::elect_lane();
-                for (int g = 0; g < ngroups; ++g, dh += 16u, dm += 16u, dl += 16u) {
-                    const uint32_t fresh = (win_obs == 0 && g == 0) ? 0u : 1u;
-                    tc::mma_tf32_lead(dhh, dh, dh, idesc, fresh, lead);
-                    tc::mma_tf32_lead(dr, dh, dm, idesc, fresh, lead);
-                    tc::mma_tf32_lead(dr, dm, dh, idesc, 1u, lead);
-                    tc::mma_tf32_lead(dr, dh, dl, idesc, 1u, lead);
-                    tc::mma_tf32_lead(dr, dl, dh, idesc, 1u, lead);
-                    tc::mma_tf32_lead(dr, dm, dm, idesc, 1u, lead);
-                }
-                tc::commit_lead(ms.mbar + buf, lead);
-            }
-        }
+        // 2. the round's MMAs (the last warp, so that the S's of the first
+        //    warps runs at the same time)
+        issue_mmas(buf, (nc + 7) / 8);
         sy.out |= 1u << buf;
         ++rnd;
-        // 3. S's from the staged rows (compensated FP32): thread group g of
-        //    sgroups takes member r = tid - g mr and observations g, g + G,
-        //    ...; four independent double-float partial sums for ILP.  Raw
-        //    rows, lr and sl are zero past nc, so the tail adds nothing.
-        if (!FS && s_r < m && s_g < sgroups) {
-            const int G = sgroups;
-            for (int k0 = s_g; k0 < kc; k0 += 4 * G) {
-#pragma unroll
-                for (int j = 0; j < 4; ++j) {
-                    const int k = k0 + j * G;
-                    if (k >= kc) break;
-                    const float v = __fmul_rn(raw[k * ms.ldv + s_r], ms.lr[k]);
-                    const float x = ms.sl[k];
-                    const float p = v * x, pe = fmaf(v, x, -p);
-                    const float sm = bh[j] + p, bp = sm - bh[j];
-                    bl[j] += ((bh[j] - (sm - bp)) + (p - bp)) + pe;
-                    bh[j] = sm;
-                }
-            }
-        }
+        // 3. S's from the staged rows
+        ss_pass(lcf, base, nc, rb);
         // 4. the window closed one round ago: its last commit is on the other
         //    buffer; drain it while this round's MMAs run
-        if (!DF && drain_set >= 0) {
+        if (drain_set >= 0) {
             wait_buf(drain_buf, false);
             read_set(drain_set);
             drain_set = -1;
         }
         // 5. close the current window when the next round might overflow it
-        //    (DF: drained at the end of this round)
         win_obs += nc;
-        const bool close_now = DF && win_obs + kc > MX_WIN;
-        if (!DF && win_obs + kc > MX_WIN) {
+        if (win_obs + kc > MX_WIN) {
             drain_set = win;
             drain_buf = buf;
             win ^= 1;
@@ -665,12 +763,6 @@ struct GramProcTC {
             }
             sy.completed(buf ^ 1);
             tc::fence_after();
-        }
-        if (close_now) {
-            // the single set: this round's MMAs, then the window into S'S
-            wait_buf(buf, false);
-            read_set(0);
-            win_obs = 0;
         }
         tc::cp_async_wait_all();
         __syncthreads();
@@ -696,7 +788,8 @@ struct GramProcTC {
                 const int nn = n - base - kc;
                 stage_rows(lid, base + kc, nn < kc ? nn : kc, rb ^ 1);
             }
-            round(lcf, base, nc, t, rb);
+            if constexpr (DF) round_df(lcf, base, nc, rb);
+            else round(lcf, base, nc, t, rb);
             if (*ms.err) break;
         }
         tc::cp_async_wait_all();   // nothing in flight after an early exit
@@ -708,6 +801,9 @@ struct GramProcTC {
     // no MMA is in flight when TMEM is released)
     __device__ __forceinline__ void finish()
     {
+        if (DF && pend && !*ms.err) issue_pending();
+        pend = false;
+        drain_after = false;
         wait_buf(0);
         wait_buf(1);
         if (drain_set >= 0) read_set(drain_set);
@@ -936,7 +1032,6 @@ static size_t mixed_smem_bytes(int m, int kc, int lseg, int st, int df)
     s += (size_t)2 * m * 4;                                // quantum q, rounding constant
     s += 16;                                               // alignment
     s += df ? (size_t)m * (m + 1) / 2 * 8 : (size_t)m * lda * 8;   // Macc (also A)
-    s += (size_t)2 * ((kc + 3) & ~3) * 4;                  // tapered innovations, taper of the round
     s += (size_t)(df ? 1 : 6) * (m + 1) * 8;               // b d e cs sn v
     s += (size_t)ENKFG_MAXTYPES * 8 * 2;
     s += (size_t)(CALC_NT / 32) * 8;
@@ -965,8 +1060,6 @@ __global__ void __launch_bounds__(CALC_NT, 2) k_transforms_mixed(CalcArgs a, int
     const int nmacc = DF ? m * (m + 1) / 2 : m * lda;      // DF: packed upper triangle
     double* Macc = (double*)sp;       sp += (size_t)nmacc * 8;
     float* Mrest = (float*)sp;        sp += ST ? (size_t)m * lda * 4 : 0;
-    float* sl = (float*)sp;           sp += (size_t)((kcm + 3) & ~3) * 4;
-    float* lr = (float*)sp;           sp += (size_t)((kcm + 3) & ~3) * 4;
     double* b = (double*)sp;          sp += (m + 1) * 8;
     // the in-kernel solve's vectors (not in the compact deferred form)
     double* d = (double*)sp;          sp += DF ? 0 : (m + 1) * 8;
@@ -1012,7 +1105,7 @@ __global__ void __launch_bounds__(CALC_NT, 2) k_transforms_mixed(CalcArgs a, int
     __syncthreads();
     tc::fence_after();
     MixedShared ms{ tiles, (int)piece, raw0, kcm * ldv, sraw0, kcm, ldv, qs, (float2*)Macc, Mrest, lda, ST ? 1 : 0,
-                    sl, lr, mbar, *tslot, N, kcm, err };
+                    mbar, *tslot, N, kcm, err };
     MixedSync sy{ 0u, 0u };
     uint32_t rnd = 0;
 
@@ -1093,10 +1186,12 @@ __global__ void __launch_bounds__(CALC_NT, 2) k_transforms_mixed(CalcArgs a, int
             }
             nparts = nkg;
         } else {
-            if (proc.s_r < m && proc.s_g < proc.sgroups)
-                bpart[proc.s_g * m + proc.s_r] =
-                    (((double)proc.bh[0] + (double)proc.bh[1]) + ((double)proc.bh[2] + (double)proc.bh[3])) +
-                    (((double)proc.bl[0] + (double)proc.bl[1]) + ((double)proc.bl[2] + (double)proc.bl[3]));
+            if (proc.s_g < proc.sgroups)
+#pragma unroll
+                for (int u = 0; u < 4; ++u) {
+                    const int r = 4 * proc.s_q + u;
+                    if (r < m) bpart[proc.s_g * m + r] = (double)proc.bh[u] + (double)proc.bl[u];
+                }
             nparts = proc.sgroups;
         }
         if constexpr (DF) {
@@ -1130,28 +1225,28 @@ __global__ void __launch_bounds__(CALC_NT, 2) k_transforms_mixed(CalcArgs a, int
                 a.eaux[2 * (size_t)idx + 1] = trss;
             }
             __syncthreads();
-            continue;
-        }
-        // double-float -> FP64 in place
-        for (int i = tid; i < m * lda; i += CALC_NT) {
-            float2 v2 = ((float2*)Macc)[i];
-            Macc[i] = ST ? ((double)v2.x + (double)v2.y) + (double)Mrest[i] : (double)v2.x + (double)v2.y;
-        }
-        __syncthreads();
-        if (tid < m) {
-            double acc = 0.0;
-            for (int g = 0; g < nparts; ++g) acc += bpart[g * m + tid];
-            b[tid] = acc;
-        }
-        __syncthreads();
-        const double trss = la::block_sum<CALC_NT>(tid < m ? Macc[tid * lda + tid] : 0.0, red);
-        if (tid < m) Macc[tid * lda + tid] += 1.0;
-        __syncthreads();
-        // the per-type pass reuses the operand tiles as its FP64 chunk buffer
-        solve_point(a, pt, idx, p, ms.kc, qx, qy, qz, Macc, lda, b, trss, d, e, cs, sn, v, s, (double*)tiles, m);
-        if (a.want_diag && a.ntypes > 1) {
-            for (size_t i = tid; i < ntile; i += CALC_NT) tiles[i] = 0.0f;
+        } else {
+            // double-float -> FP64 in place
+            for (int i = tid; i < m * lda; i += CALC_NT) {
+                float2 v2 = ((float2*)Macc)[i];
+                Macc[i] = ST ? ((double)v2.x + (double)v2.y) + (double)Mrest[i] : (double)v2.x + (double)v2.y;
+            }
             __syncthreads();
+            if (tid < m) {
+                double acc = 0.0;
+                for (int g = 0; g < nparts; ++g) acc += bpart[g * m + tid];
+                b[tid] = acc;
+            }
+            __syncthreads();
+            const double trss = la::block_sum<CALC_NT>(tid < m ? Macc[tid * lda + tid] : 0.0, red);
+            if (tid < m) Macc[tid * lda + tid] += 1.0;
+            __syncthreads();
+            // the per-type pass reuses the operand tiles as its FP64 chunk buffer
+            solve_point(a, pt, idx, p, ms.kc, qx, qy, qz, Macc, lda, b, trss, d, e, cs, sn, v, s, (double*)tiles, m);
+            if (a.want_diag && a.ntypes > 1) {
+                for (size_t i = tid; i < ntile; i += CALC_NT) tiles[i] = 0.0f;
+                __syncthreads();
+            }
         }
     }
     __syncthreads();
