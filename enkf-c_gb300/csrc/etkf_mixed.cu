@@ -32,7 +32,6 @@
 // double-float product pair.
 #include "calc_common.cuh"
 
-#define EM_TRED_NT 128
 #define EM_QL_T 32
 #define EM_REPLAY_NT 128
 #define EM_NT 256
@@ -55,170 +54,237 @@ struct EmSlots {
 };
 
 // ---------------------------------------------------------------------------
-// 1a. FP32 Householder tridiagonalisation, one CTA per slot.  Also splits M
-//     into its double-float pair for the residual.
+// 1a. FP32 Householder tridiagonalisation, one CTA of 256 threads (a 16 x 16
+//     grid) per slot, the matrix in registers.  Also splits M into its
+//     double-float pair for the residual.
+//
+//     Reduction: thread (tx, ty) holds A[ty + 16 r][tx + 16 c] (both
+//     triangles) in a[r][c].  Step i (i = n-1 .. 1, l = i - 1), with the
+//     steps of tred2 (Wilkinson & Reinsch) without the row scaling:
+//       - the half-warp that owns row i has written u = A[i][0..l] (with
+//         u_l = f - g), h and g to shared memory at the end of step i + 1;
+//       - p = A u / h: partial sums over each thread's columns, summed
+//         across the half-warp by shuffles; f = p.u from per-half-warp
+//         partials;
+//       - A -= u q' + q u' (q = p - f / 2h u) on every element j, k <= l,
+//         in registers; u / h goes to column i of the shared array;
+//     two barriers a step.  Row i lives on in the shared array's lower
+//     triangle, u / h in its upper triangle, as tred2 keeps them in A.
+//     Accumulation: thread (tx, ty) holds Q[tx + 16 c][ty + 16 r], so that
+//     g = u' Q (a sum over rows) stays within a half-warp; no barriers.
 // ---------------------------------------------------------------------------
 namespace em {
 
-// sum over the CTA of one value per thread (NT threads); red: NT/32 floats
-template <int NT>
-__device__ __forceinline__ float cta_sum(float v, float* red)
+template <int R>
+struct TredSmem {
+    static constexpr int MP = 16 * R, LD = MP + 1;
+    // W [MP][LD]: u_i in row i below the diagonal, u_i / h_i in column i
+    // above it; P [MP]: p; hv, ev, dv [MP]: h (0: no reflector), e (tred2
+    // form), the diagonal; red [16]: f partials
+    static constexpr size_t bytes() { return ((size_t)MP * LD + 4 * MP + 16) * 4; }
+};
+
+// the lanes of this thread's half-warp
+__device__ __forceinline__ unsigned hw_mask() { return 0xFFFFu << (threadIdx.x & 16); }
+
+// half-warp all-reduce (the lanes of one half-warp hold one row's partials)
+__device__ __forceinline__ float hw_sum(float v)
 {
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-    __syncthreads();
-    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
-    __syncthreads();
-    float s = 0.0f;
-#pragma unroll
-    for (int w = 0; w < NT / 32; ++w) s += red[w];
-    return s;
+    const unsigned hm = hw_mask();
+    v += __shfl_xor_sync(hm, v, 1);
+    v += __shfl_xor_sync(hm, v, 2);
+    v += __shfl_xor_sync(hm, v, 4);
+    v += __shfl_xor_sync(hm, v, 8);
+    return v;
 }
 
-// Householder tridiagonalisation of the symmetric A (n x n, row stride lda,
-// both triangles valid) with the transformations accumulated, the steps of
-// tred2 (Wilkinson & Reinsch) without the row scaling (M = I + S'S is far
-// from FP32 overflow and underflow).  The matrix-vector products run one row
-// (or column) per thread, so that the n dependent chains overlap; the rank-2
-// update goes row by row over the warps (lanes over the row), with no index
-// arithmetic per element.  Lower-triangle storage: A[j][k] with k <= j; the
-// reflectors are kept in the rows and, scaled, in the columns above the
-// diagonal.  On return A holds Q, d the diagonal and e the off-diagonal in
-// QL form (e[i] couples i and i+1, e[n-1] = 0).
-template <int NT>
-__device__ void tred2_f32(float* A, int n, int lda, float* d, float* e, float* red)
+// the owner half-warp of row i (ty == i % 16) publishes u = A[i][0..l], the
+// reflector's h and g (or the skip: h = 0, e = A[i][l]) and the final
+// diagonal A[i][i]
+template <int R>
+__device__ __forceinline__ void tred_publish(const float (&a)[R][R], int i, int tx, int ty, float* W, float* hv,
+                                             float* ev, float* dv)
 {
-    const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
-    constexpr int NW = NT / 32;
-    for (int i = n - 1; i >= 1; --i) {
-        const int l = i - 1;
-        float* Ai = A + (size_t)i * lda;
-        float part = 0.0f;
-        for (int k = tid; k <= l; k += NT) part = fmaf(Ai[k], Ai[k], part);
-        float h = cta_sum<NT>(part, red);
-        if (l == 0 || h == 0.0f) {
-            if (tid == 0) {
-                e[i] = Ai[l];
-                d[i] = 0.0f;
-            }
-            __syncthreads();
-            continue;
-        }
-        const float f = Ai[l];
-        const float g = (f >= 0.0f) ? -sqrtf(h) : sqrtf(h);
-        h -= f * g;
-        const float ih = 1.0f / h;
-        __syncthreads();              // every thread has read Ai[l]
-        if (tid == 0) {
-            e[i] = g;
-            Ai[l] = f - g;
-            d[i] = h;
-        }
-        __syncthreads();
-        // p = A u / h into e[0..l] (u = row i), column i keeps u / h
-        float ffp = 0.0f;
-        for (int j = tid; j <= l; j += NT) {
-            const float* Aj = A + (size_t)j * lda;
-            float acc0 = 0.0f, acc1 = 0.0f;
-            int k = 0;
-            for (; k + 1 <= j; k += 2) {
-                acc0 = fmaf(Aj[k], Ai[k], acc0);
-                acc1 = fmaf(Aj[k + 1], Ai[k + 1], acc1);
-            }
-            if (k <= j) acc0 = fmaf(Aj[k], Ai[k], acc0);
-            for (k = j + 1; k + 1 <= l; k += 2) {
-                acc0 = fmaf(A[(size_t)k * lda + j], Ai[k], acc0);
-                acc1 = fmaf(A[(size_t)(k + 1) * lda + j], Ai[k + 1], acc1);
-            }
-            if (k <= l) acc0 = fmaf(A[(size_t)k * lda + j], Ai[k], acc0);
-            const float pj = (acc0 + acc1) * ih;
-            e[j] = pj;
-            A[(size_t)j * lda + i] = Ai[j] * ih;
-            ffp = fmaf(pj, Ai[j], ffp);
-        }
-        const float ff = cta_sum<NT>(ffp, red);
-        const float hh = ff / (h + h);
-        for (int j = tid; j <= l; j += NT) e[j] = e[j] - hh * Ai[j];   // q
-        __syncthreads();
-        // A[j][k] -= u_j q_k + q_j u_k  (k <= j <= l)
-        for (int j = wid; j <= l; j += NW) {
-            float* Aj = A + (size_t)j * lda;
-            const float uj = Ai[j], qj = e[j];
-            for (int k = lane; k <= j; k += 32) Aj[k] -= uj * e[k] + qj * Ai[k];
-        }
-        __syncthreads();
-    }
-    if (tid == 0) {
-        d[0] = 0.0f;
-        e[0] = 0.0f;
-    }
-    __syncthreads();
-    // accumulate Q = H_{n-1} ... H_1: step i applies reflector i to the
-    // leading i x i block, one column per thread (g_j = row i . column j)
-    for (int i = 0; i < n; ++i) {
-        const int l = i - 1;
-        float* Ai = A + (size_t)i * lda;
-        if (d[i] != 0.0f) {
-            for (int j = tid; j <= l; j += NT) {
-                float g0 = 0.0f, g1 = 0.0f;
-                int k = 0;
-                for (; k + 1 <= l; k += 2) {
-                    g0 = fmaf(Ai[k], A[(size_t)k * lda + j], g0);
-                    g1 = fmaf(Ai[k + 1], A[(size_t)(k + 1) * lda + j], g1);
+    constexpr int LD = 16 * R + 1;
+    if ((i & 15) != ty) return;
+    const int l = i - 1;
+    float hp = 0.0f, f = 0.0f, aii = 0.0f;
+#pragma unroll
+    for (int r = 0; r < R; ++r)
+        if (16 * r + ty == i) {
+#pragma unroll
+            for (int c = 0; c < R; ++c) {
+                const int k = tx + 16 * c;
+                const float v = a[r][c];
+                if (k <= l) {
+                    W[i * LD + k] = v;
+                    hp = fmaf(v, v, hp);
                 }
-                if (k <= l) g0 = fmaf(Ai[k], A[(size_t)k * lda + j], g0);
-                const float g = g0 + g1;
-                for (k = 0; k <= l; ++k) A[(size_t)k * lda + j] -= g * A[(size_t)k * lda + i];
+                if (k == l) f = v;
+                if (k == i) aii = v;
             }
-            __syncthreads();
         }
-        const float di = Ai[i];
-        __syncthreads();
-        if (tid == 0) {
-            d[i] = di;
-            Ai[i] = 1.0f;
+    const float h0 = hw_sum(hp);
+    const int lsrc = (threadIdx.x & 16) | (l & 15);   // lane of this half-warp holding column l
+    const int isrc = (threadIdx.x & 16) | (i & 15);
+    f = __shfl_sync(hw_mask(), f, lsrc);
+    aii = __shfl_sync(hw_mask(), aii, isrc);
+    if (tx == 0) {
+        dv[i] = aii;
+        if (l == 0 || h0 == 0.0f) {
+            hv[i] = 0.0f;
+            ev[i] = f;
+        } else {
+            const float g = (f >= 0.0f) ? -sqrtf(h0) : sqrtf(h0);
+            hv[i] = h0 - f * g;
+            ev[i] = g;
+            W[i * LD + l] = f - g;
         }
-        for (int j = tid; j <= l; j += NT) {
-            A[(size_t)j * lda + i] = 0.0f;
-            Ai[j] = 0.0f;
-        }
-        __syncthreads();
     }
-    if (tid == 0) {
-        for (int i = 1; i < n; ++i) e[i - 1] = e[i];
-        e[n - 1] = 0.0f;
-    }
-    __syncthreads();
 }
 
 }  // namespace em
 
-__global__ void __launch_bounds__(EM_TRED_NT) k_em_tred(CalcArgs a, EmSlots z)
+template <int R>
+__global__ void __launch_bounds__(256, 2) k_em_tred(CalcArgs a, EmSlots z)
 {
+    using TS = em::TredSmem<R>;
+    constexpr int MP = TS::MP, LD = TS::LD;
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    const int m = a.m, lda = m + 1;
-    const int tid = threadIdx.x, slot = blockIdx.x;
-    float* A = (float*)smem_raw;
-    float* d = A + (size_t)m * lda;
-    float* e = d + m;
-    float* red = e + m;
+    float* W = (float*)smem_raw;
+    float* P = W + MP * LD;
+    float* hv = P + MP;
+    float* ev = hv + MP;
+    float* dv = ev + MP;
+    float* red = dv + MP;
+    const int m = a.m, n = a.m;
+    const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4, slot = blockIdx.x;
     if (!(a.eaux[2 * (size_t)slot] > 0.0)) return;   // empty point
     const size_t q0 = (size_t)slot * m * m;
-    for (int i = tid; i < m * m; i += EM_TRED_NT) {
+    if (tid == 0) {
+        hv[0] = 0.0f;   // no reflector at index 0
+        ev[0] = 0.0f;
+    }
+    // M's double-float pair for the residual (both triangles)
+    for (int i = tid; i < m * m; i += 256) {
         const int r = i / m, c = i - r * m;
         const double v = (c >= r) ? a.eq[q0 + i] : a.eq[q0 + (size_t)c * m + r];
         const float hi = (float)v;
-        A[r * lda + c] = hi;
         z.mhl[q0 + i] = make_float2(hi, (float)(v - (double)hi));
     }
-    __syncthreads();
-    em::tred2_f32<EM_TRED_NT>(A, m, lda, d, e, red);
-    for (int i = tid; i < m * m; i += EM_TRED_NT) {
-        const int r = i / m, c = i - r * m;
-        z.q[q0 + i] = A[r * lda + c];
+    float a_[R][R];
+#pragma unroll
+    for (int r = 0; r < R; ++r)
+#pragma unroll
+        for (int c = 0; c < R; ++c) {
+            const int j = ty + 16 * r, k = tx + 16 * c;
+            a_[r][c] = (j < m && k < m) ? (float)(k >= j ? a.eq[q0 + (size_t)j * m + k] : a.eq[q0 + (size_t)k * m + j])
+                                        : 0.0f;
+        }
+    em::tred_publish<R>(a_, n - 1, tx, ty, W, hv, ev, dv);
+    for (int i = n - 1; i >= 1; --i) {
+        const int l = i - 1;
+        __syncthreads();   // row i, h, g published; the last step's P and red read
+        const float h = hv[i];
+        if (h != 0.0f) {
+            const float ih = 1.0f / h;
+            float uk[R], uj[R];
+#pragma unroll
+            for (int c = 0; c < R; ++c) {
+                const int k = tx + 16 * c;
+                uk[c] = k <= l ? W[i * LD + k] : 0.0f;
+            }
+#pragma unroll
+            for (int r = 0; r < R; ++r) {
+                const int j = ty + 16 * r;
+                uj[r] = j <= l ? W[i * LD + j] : 0.0f;
+            }
+            // p = A u / h, f = p.u
+            float fp = 0.0f;
+#pragma unroll
+            for (int r = 0; r < R; ++r) {
+                float s = 0.0f;
+#pragma unroll
+                for (int c = 0; c < R; ++c) s = fmaf(a_[r][c], uk[c], s);
+                s = em::hw_sum(s) * ih;
+                const int j = ty + 16 * r;
+                if (tx == 0 && j <= l) P[j] = s;
+                fp = fmaf(s, uj[r], fp);
+            }
+            if (tx == 0) red[ty] = fp;
+            // u / h into column i (tred2 keeps it for the accumulation)
+            if (tid <= l) W[tid * LD + i] = W[i * LD + tid] * ih;
+            __syncthreads();
+            float f = 0.0f;
+#pragma unroll
+            for (int t = 0; t < 16; ++t) f += red[t];
+            const float hh = f / (h + h);
+            float qk[R];
+#pragma unroll
+            for (int c = 0; c < R; ++c) {
+                const int k = tx + 16 * c;
+                qk[c] = k <= l ? P[k] - hh * uk[c] : 0.0f;
+            }
+#pragma unroll
+            for (int r = 0; r < R; ++r) {
+                const int j = ty + 16 * r;
+                const float qj = j <= l ? P[j] - hh * uj[r] : 0.0f;
+#pragma unroll
+                for (int c = 0; c < R; ++c) a_[r][c] -= uj[r] * qk[c] + qj * uk[c];
+            }
+        }
+        if (l >= 1) em::tred_publish<R>(a_, l, tx, ty, W, hv, ev, dv);
+        else if (ty == 0 && tx == 0) dv[0] = a_[0][0];
     }
-    for (int i = tid; i < m; i += EM_TRED_NT) {
-        z.d[(size_t)slot * m + i] = d[i];
-        z.e[(size_t)slot * m + i] = e[i];
+    __syncthreads();
+    // accumulation of Q = H_{n-1} ... H_1 (tred2's second loop)
+    float q_[R][R];   // q_[c][r] = Q[tx + 16 c][ty + 16 r]
+#pragma unroll
+    for (int c = 0; c < R; ++c)
+#pragma unroll
+        for (int r = 0; r < R; ++r) q_[c][r] = 0.0f;
+    for (int i = 0; i < n; ++i) {
+        const int l = i - 1;
+        if (hv[i] != 0.0f) {
+            float uk[R], vk[R];
+#pragma unroll
+            for (int c = 0; c < R; ++c) {
+                const int k = tx + 16 * c;
+                uk[c] = k <= l ? W[i * LD + k] : 0.0f;
+                vk[c] = k <= l ? W[k * LD + i] : 0.0f;
+            }
+#pragma unroll
+            for (int r = 0; r < R; ++r) {
+                float g = 0.0f;
+#pragma unroll
+                for (int c = 0; c < R; ++c) g = fmaf(uk[c], q_[c][r], g);
+                g = em::hw_sum(g);
+                const int j = ty + 16 * r;
+                if (j <= l)
+#pragma unroll
+                    for (int c = 0; c < R; ++c) q_[c][r] -= g * vk[c];
+            }
+        }
+#pragma unroll
+        for (int c = 0; c < R; ++c)
+#pragma unroll
+            for (int r = 0; r < R; ++r)
+                if (tx + 16 * c == i && ty + 16 * r == i) q_[c][r] = 1.0f;
+    }
+    __syncthreads();   // W free
+#pragma unroll
+    for (int c = 0; c < R; ++c)
+#pragma unroll
+        for (int r = 0; r < R; ++r) W[(tx + 16 * c) * LD + ty + 16 * r] = q_[c][r];
+    __syncthreads();
+    for (int i = tid; i < m * m; i += 256) {
+        const int r = i / m, c = i - r * m;
+        z.q[q0 + i] = W[r * LD + c];
+    }
+    // d and e in QL form (e[i] couples i and i + 1)
+    for (int i = tid; i < m; i += 256) {
+        z.d[(size_t)slot * m + i] = dv[i];
+        z.e[(size_t)slot * m + i] = i + 1 < m ? ev[i + 1] : 0.0f;
     }
 }
 
@@ -654,10 +720,10 @@ enkfg_status run_etkf_mixed(enkfg_ctx* ctx, const CalcArgs& a0, cudaStream_t st)
     z.hcap = hcap;
     z.mp = MP;
     const int lda = m + 1;
-    const size_t tsmem = ((size_t)m * lda + 2 * (size_t)m + EM_TRED_NT / 32) * 4 + 16;
+    const size_t tsmem = R == 2 ? em::TredSmem<2>::bytes() : R == 3 ? em::TredSmem<3>::bytes()
+                         : R == 4 ? em::TredSmem<4>::bytes() : em::TredSmem<6>::bytes();
     const size_t qsmem = (size_t)2 * m * EM_QL_T * 4;
     const size_t rsmem = (size_t)EM_RCH * 8 + ((size_t)m * lda + 4 * (size_t)m) * 4 + 16;
-    CK(cudaFuncSetAttribute(k_em_tred, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tsmem));
     CK(cudaFuncSetAttribute(k_em_ql, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)qsmem));
     CK(cudaFuncSetAttribute(k_em_replay, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rsmem));
     for (int i0 = 0; i0 < nitems; i0 += (int)B) {
@@ -678,7 +744,12 @@ enkfg_status run_etkf_mixed(enkfg_ctx* ctx, const CalcArgs& a0, cudaStream_t st)
         batch_mark(ctx, 0, st);
         if ((s = launch_mixed(ctx, b, st))) return s;
         batch_mark(ctx, 1, st);
-        k_em_tred<<<nb, EM_TRED_NT, tsmem, st>>>(b, z);
+        switch (R) {
+        case 2: k_em_tred<2><<<nb, 256, tsmem, st>>>(b, z); break;
+        case 3: k_em_tred<3><<<nb, 256, tsmem, st>>>(b, z); break;
+        case 4: k_em_tred<4><<<nb, 256, tsmem, st>>>(b, z); break;
+        default: k_em_tred<6><<<nb, 256, tsmem, st>>>(b, z); break;
+        }
         CKL();
         k_em_ql<<<div_up(nb, EM_QL_T), EM_QL_T, qsmem, st>>>(nb, m, ctx->d_eaux, z);
         CKL();
