@@ -737,6 +737,7 @@ enkfg_status run_transforms(enkfg_ctx* ctx, const enkfg_calc_params* p, cudaStre
     a.qscale = ctx->d_qscale;
     a.mpad = ctx->mpad;
     a.ss = ctx->d_ss;
+    a.ssf = ctx->d_ssf;
     a.qx = ctx->d_qx;
     a.qy = ctx->d_qy;
     a.qz = ctx->d_qz;

@@ -30,6 +30,7 @@ struct CalcArgs {
     const float* qscale;   // [2][ENKFG_MAXMEM] mixed path: per-member quantum q and 1/q
     int mpad;
     const double* ss;
+    const float* ssf;      // ss rounded to float (mixed path)
     const double* qx;
     const double* qy;
     const double* qz;

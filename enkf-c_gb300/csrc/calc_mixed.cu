@@ -208,6 +208,13 @@ __device__ __forceinline__ void cp_async8(void* dst, const void* src)
                  : "memory");
 }
 
+__device__ __forceinline__ void cp_async4(void* dst, const void* src)
+{
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(smem_u32(dst)),
+                 "l"((unsigned long long)__cvta_generic_to_global(src))
+                 : "memory");
+}
+
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
 
@@ -228,7 +235,7 @@ struct MixedShared {
     int piece;             // floats per piece tile
     float* raw;            // [buffer][kcm][ldv] untapered S rows of a round (cp.async)
     int rawsz;             // floats per raw buffer
-    double* sraw;          // [buffer][kcm] innovations of those observations (cp.async)
+    float* sraw;           // [buffer][kcm] innovations of those observations, float (cp.async)
     int kcm;
     int ldv;               // row stride of raw: >= mpad, = 8 mod 32 (conflict-free reads)
     const float* qs;       // [2][m]: quantum q_r and the rounding constant 1.5 2^23 q_r
@@ -248,7 +255,7 @@ struct MixedShared {
     }
     __device__ __forceinline__ float* zblock() const { return tiles + 3 * piece; }   // stacked: N zero rows
     __device__ __forceinline__ float* rawb(int rb) const { return raw + rb * rawsz; }
-    __device__ __forceinline__ double* srawb(int rb) const { return sraw + rb * kcm; }
+    __device__ __forceinline__ float* srawb(int rb) const { return sraw + rb * kcm; }
 };
 
 // error-free (TwoSum) accumulation of x into the double-float (a.x + a.y)
@@ -316,6 +323,11 @@ struct GramProcTC {
     int sgroups;       // S's observation groups (warps 0 .. 6; the last warp issues the MMAs)
     int s_g, s_q;      // this thread's group and quad of members (4 s_q .. 4 s_q + 3)
     float bh[4], bl[4]; // S's of those four members over group s_g: double-float sums
+    // S's fused into the vectorised split: one double-float sum per (member,
+    // K group) pair the thread splits (the pairs stay the thread's for the
+    // whole point)
+    static constexpr int NSLOT = FS ? 1 : (8 * 16 * HB + CALC_NT - 1) / CALC_NT;
+    float vh[NSLOT], vl[NSLOT];
     // DF: the batch staged last round, whose MMAs are issued at the start of
     // the next round (while that round is split), and whether the window
     // closes with it
@@ -334,6 +346,8 @@ struct GramProcTC {
 #pragma unroll
         for (int i = 0; i < (FS ? 2 * HB : 1); ++i) fh[i] = fl[i] = 0.0f;
         for (int j = 0; j < 4; ++j) bh[j] = bl[j] = 0.0f;
+#pragma unroll
+        for (int j = 0; j < NSLOT; ++j) vh[j] = vl[j] = 0.0f;
     }
 
     // bounded wait for the outstanding commit of operand buffer `buf`; on
@@ -440,9 +454,9 @@ struct GramProcTC {
             }
         }
         if (tid < kc) {
-            double* d = ms.srawb(rb) + tid;
-            if (tid < nc) tc::cp_async8(d, a.ss + lid[base + tid]);
-            else *d = 0.0;
+            float* d = ms.srawb(rb) + tid;
+            if (tid < nc) tc::cp_async4(d, a.ssf + lid[base + tid]);
+            else *d = 0.0f;
         }
         tc::cp_async_commit();
     }
@@ -529,11 +543,11 @@ struct GramProcTC {
     {
         if (FS || s_g >= sgroups) return;
         const float* raw = ms.rawb(rb) + 4 * s_q;
-        const double* sr = ms.srawb(rb);
+        const float* sr = ms.srawb(rb);
         for (int k = s_g; k < nc; k += sgroups) {
             const float4 rv = *reinterpret_cast<const float4*>(raw + k * ms.ldv);
             const float c = lcf[base + k];
-            const float x = __fmul_rn((float)sr[k], c);
+            const float x = __fmul_rn(sr[k], c);
             const float v[4] = { __fmul_rn(rv.x, c), __fmul_rn(rv.y, c), __fmul_rn(rv.z, c), __fmul_rn(rv.w, c) };
 #pragma unroll
             for (int u = 0; u < 4; ++u) {
@@ -612,8 +626,7 @@ struct GramProcTC {
         const int buf = (int)(rnd & 1u);
         if (pend) issue_pending();
         if (sy.outstanding(buf)) wait_buf(buf, false);
-        split_vec(buf, rb, lcf, base, nc);
-        ss_pass(lcf, base, nc, rb);
+        split_vec<true>(buf, rb, lcf, base, nc);
         ++rnd;
         pend = true;
         pend_buf = buf;
@@ -636,6 +649,9 @@ struct GramProcTC {
     // raw reads are consecutive members of one observation.  Rows >= m are
     // not written (they only reach accumulator rows and columns that are
     // never read); observations past nc have zero rows and zero taper.
+    // With SS, each pair's products with the observations' tapered
+    // innovations go into the pair's double-float S's sum (vh, vl).
+    template <bool SS>
     __device__ __forceinline__ void split_vec(int buf, int rb, const float* lcf, int base, int nc)
     {
         const int m = a.m, nkg = ms.kc >> 2, rows = ((m + 7) >> 3) << 3;
@@ -644,10 +660,13 @@ struct GramProcTC {
         float* tM = ms.tile(buf, 1);
         float* tL = ms.tile(buf, 2);
         const float* raw = ms.rawb(rb);
+        const float* sr = ms.srawb(rb);
         const float* cq = ms.qs + m;
         const int dk = CALC_NT / rows, dr = CALC_NT - dk * rows;
         int kg = (int)threadIdx.x / rows, r = (int)threadIdx.x - kg * rows;
-        for (int i = threadIdx.x; i < npair; i += CALC_NT) {
+#pragma unroll
+        for (int sl = 0; sl < NSLOT; ++sl) {
+            if ((int)threadIdx.x + sl * CALC_NT >= npair) break;
             if (r < m) {
                 const int k0 = kg << 2;
                 float v[4], c[4];
@@ -668,6 +687,14 @@ struct GramProcTC {
                     const float r1 = __fsub_rn(vv, h[j]);
                     md[j] = tc::tf32_rna(r1);
                     lo[j] = tc::tf32_rna(__fsub_rn(r1, md[j]));
+                    if constexpr (SS) {
+                        // TwoProd and TwoSum into the pair's sum
+                        const float x = __fmul_rn(sr[k0 + j], c[j]);
+                        const float pp = vv * x, pe = fmaf(vv, x, -pp);
+                        const float sm = vh[sl] + pp, bp = sm - vh[sl];
+                        vl[sl] += ((vh[sl] - (sm - bp)) + (pp - bp)) + pe;
+                        vh[sl] = sm;
+                    }
                 }
                 const int off = ((((r >> 3) * nkg + kg) << 5)) + ((r & 7) << 2);
                 *reinterpret_cast<float4*>(tH + off) = make_float4(h[0], h[1], h[2], h[3]);
@@ -717,11 +744,11 @@ struct GramProcTC {
             const int kg = wid & (nkg - 1), rg0 = wid / nkg, rstep = (CALC_NT / 32) / nkg;
             const int k = (kg << 2) + (lane & 3);
             const float ck = k < nc ? lcf[base + k] : 0.0f;
-            const float xk = (FS && k < nc) ? __fmul_rn((float)ms.srawb(rb)[k], ck) : 0.0f;
+            const float xk = (FS && k < nc) ? __fmul_rn(ms.srawb(rb)[k], ck) : 0.0f;
             const float* rp = raw + k * ms.ldv + (lane >> 2);
             if (tsum) ssq = split_rows<true>(tH, tM, tL, rp, ck, xk, nrg, nkg, kg, rg0, rstep, lane);
             else if (FS) split_rows<false>(tH, tM, tL, rp, ck, xk, nrg, nkg, kg, rg0, rstep, lane);
-            else split_vec(buf, rb, lcf, base, nc);
+            else split_vec<true>(buf, rb, lcf, base, nc);
         }
         tc::fence_async_smem();
         __syncthreads();
@@ -730,8 +757,8 @@ struct GramProcTC {
         issue_mmas(buf, (nc + 7) / 8);
         sy.out |= 1u << buf;
         ++rnd;
-        // 3. S's from the staged rows
-        ss_pass(lcf, base, nc, rb);
+        // 3. S's from the staged rows (fused into the split otherwise)
+        if (tsum) ss_pass(lcf, base, nc, rb);
         // 4. the window closed one round ago: its last commit is on the other
         //    buffer; drain it while this round's MMAs run
         if (drain_set >= 0) {
@@ -1028,7 +1055,7 @@ static size_t mixed_smem_bytes(int m, int kc, int lseg, int st, int df)
     s += mixed_tile_floats(m, kc, st) * 4;                 // operand tiles + padding
     if (st) s += (size_t)m * lda * 4;                      // Mrest
     s += (size_t)2 * kc * mixed_ldv(m) * 4;                // raw S rows, two buffers
-    s += (size_t)2 * kc * 8;                               // raw innovations, two buffers
+    s += (size_t)2 * kc * 4;                               // raw innovations, two buffers
     s += (size_t)2 * m * 4;                                // quantum q, rounding constant
     s += 16;                                               // alignment
     s += df ? (size_t)m * (m + 1) / 2 * 8 : (size_t)m * lda * 8;   // Macc (also A)
@@ -1054,7 +1081,7 @@ __global__ void __launch_bounds__(CALC_NT, 2) k_transforms_mixed(CalcArgs a, int
     float* tiles = (float*)sp;        sp += ntile * 4;
     const int ldv = mixed_ldv(m);
     float* raw0 = (float*)sp;         sp += (size_t)2 * kcm * ldv * 4;   // two buffers
-    double* sraw0 = (double*)sp;      sp += (size_t)2 * kcm * 8;
+    float* sraw0 = (float*)sp;        sp += (size_t)2 * kcm * 4;
     float* qs = (float*)sp;           sp += (size_t)2 * m * 4;
     sp = (unsigned char*)(((uintptr_t)sp + 15) & ~(uintptr_t)15);
     const int nmacc = DF ? m * (m + 1) / 2 : m * lda;      // DF: packed upper triangle
@@ -1185,7 +1212,7 @@ __global__ void __launch_bounds__(CALC_NT, 2) k_transforms_mixed(CalcArgs a, int
                 if ((lane & 3) == 0 && rg < nrg && r < m) bpart[kg * m + r] = d;
             }
             nparts = nkg;
-        } else {
+        } else if (a.want_diag && a.ntypes > 1) {
             if (proc.s_g < proc.sgroups)
 #pragma unroll
                 for (int u = 0; u < 4; ++u) {
@@ -1193,6 +1220,23 @@ __global__ void __launch_bounds__(CALC_NT, 2) k_transforms_mixed(CalcArgs a, int
                     if (r < m) bpart[proc.s_g * m + r] = (double)proc.bh[u] + (double)proc.bl[u];
                 }
             nparts = proc.sgroups;
+        } else {
+            // one partial per (K group, member): the pairs of split_vec
+            const int nkg = ms.kc >> 2, rows = ((m + 7) >> 3) << 3;
+            int kg = tid / rows, r = tid - kg * rows;
+            const int dk = CALC_NT / rows, dr = CALC_NT - dk * rows;
+#pragma unroll
+            for (int sl = 0; sl < proc.NSLOT; ++sl) {
+                if (tid + sl * CALC_NT < nkg * rows && r < m)
+                    bpart[kg * m + r] = (double)proc.vh[sl] + (double)proc.vl[sl];
+                kg += dk;
+                r += dr;
+                if (r >= rows) {
+                    r -= rows;
+                    ++kg;
+                }
+            }
+            nparts = nkg;
         }
         if constexpr (DF) {
             // the batched solve's inputs straight from the packed S'S: M = I +

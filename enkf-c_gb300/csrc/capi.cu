@@ -127,7 +127,7 @@ ENKFG_API void enkfg_destroy(enkfg_ctx* ctx)
                      ctx->d_emq, ctx->d_emmhl, ctx->d_emd, ctx->d_eme, ctx->d_emrot, ctx->d_emhdr, ctx->d_emnh,
                      ctx->d_emz0, ctx->d_emp,
                      ctx->d_S, ctx->d_s, ctx->d_std, ctx->d_types, ctx->d_bstart, ctx->d_bfill, ctx->d_key,
-                     ctx->d_sid, ctx->d_sx, ctx->d_sy, ctx->d_sz, ctx->d_sxf, ctx->d_syf, ctx->d_stype, ctx->d_St, ctx->d_ss, ctx->d_ox,
+                     ctx->d_sid, ctx->d_sx, ctx->d_sy, ctx->d_sz, ctx->d_sxf, ctx->d_syf, ctx->d_stype, ctx->d_St, ctx->d_ss, ctx->d_ssf, ctx->d_ox,
                      ctx->d_oy, ctx->d_oz, ctx->d_qx, ctx->d_qy, ctx->d_qz, ctx->d_T, ctx->d_w, ctx->d_T64,
                      ctx->d_w64, ctx->d_nlobs, ctx->d_dfs, ctx->d_srf, ctx->d_pnlobs, ctx->d_pdfs, ctx->d_psrf,
                      ctx->d_counts, ctx->d_order, ctx->d_qhead, ctx->d_status_pt, ctx->d_scratch,

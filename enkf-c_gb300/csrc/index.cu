@@ -240,7 +240,8 @@ __global__ void k_transpose_S(int nmem, int nobs, int mpad, const float* __restr
 }
 
 __global__ void k_gather_rows(int nsorted, int mpad, const int* __restrict__ sid, const float* __restrict__ src,
-                              const double* __restrict__ s, float* __restrict__ St, double* __restrict__ ss)
+                              const double* __restrict__ s, float* __restrict__ St, double* __restrict__ ss,
+                              float* __restrict__ ssf)
 {
     // one warp per sorted row, float4 copies
     int p = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -250,7 +251,10 @@ __global__ void k_gather_rows(int nsorted, int mpad, const int* __restrict__ sid
     const float4* a = (const float4*)(src + (size_t)o * mpad);
     float4* b = (float4*)(St + (size_t)p * mpad);
     for (int k = lane; k < mpad / 4; k += 32) b[k] = a[k];
-    if (lane == 0) ss[p] = s[o];
+    if (lane == 0) {
+        ss[p] = s[o];
+        ssf[p] = (float)s[o];
+    }
 }
 
 // Largest |St| per member over all sorted rows (float bits: non-negative
@@ -558,6 +562,7 @@ enkfg_status build_gather(enkfg_ctx* ctx, cudaStream_t st)
     enkfg_status s;
     if ((s = ensure(ctx, &ctx->d_St, &ctx->St_cap, ns * mpad))) return s;
     if ((s = ensure(ctx, &ctx->d_ss, &ctx->ss_cap, ns))) return s;
+    if ((s = ensure(ctx, &ctx->d_ssf, &ctx->ssf_cap, ns))) return s;
     if (nobs > 0 && ctx->nsorted > 0) {
         if ((s = ensure(ctx, &ctx->d_gtmp, &ctx->gtmp_cap, (size_t)nobs * mpad))) return s;
         dim3 g(div_up(nobs, 32), div_up(mpad, 32));
@@ -565,7 +570,7 @@ enkfg_status build_gather(enkfg_ctx* ctx, cudaStream_t st)
         CKL();
         k_gather_rows<<<div_up((long long)ctx->nsorted * 32, 256), 256, 0, st>>>(ctx->nsorted, mpad, ctx->d_sid,
                                                                                ctx->d_gtmp, ctx->d_s, ctx->d_St,
-                                                                               ctx->d_ss);
+                                                                               ctx->d_ss, ctx->d_ssf);
         CKL();
     }
     // the mixed path's per-member quantum

@@ -108,6 +108,7 @@ struct enkfg_ctx {
     int mpad;                   // member stride of d_St (multiple of 4)
     float* d_St;                // [nsorted][mpad] standardised S, sorted, member-contiguous
     double* d_ss;               // [nsorted] standardised innovation, sorted
+    float* d_ssf;               // [nsorted] the same rounded to float (mixed path)
     float* d_gtmp;              // [nobs][mpad] transpose scratch of the gather
     unsigned int* d_smax;       // [ENKFG_MAXMEM] max |St| per member (float bits), mixed-path quantum
     float* d_qscale;            // [2][ENKFG_MAXMEM] per-member quantum q and 1/q (powers of two)
@@ -115,7 +116,7 @@ struct enkfg_ctx {
     // device addresses when the sizes do not grow (CUDA graphs captured on
     // the cycle keep pointing at valid buffers)
     size_t bstart_cap, bfill_cap, key_cap, sid_cap, sx_cap, sy_cap, sz_cap, sxf_cap, syf_cap, stype_cap;
-    size_t St_cap, ss_cap, gtmp_cap;
+    size_t St_cap, ss_cap, ssf_cap, gtmp_cap;
     double* d_ox;               // [nobs] kd coordinates (original order)
     double* d_oy;
     double* d_oz;
