@@ -58,6 +58,7 @@ struct CalcArgs {
     double* ee;        // [slots][m] and off-diagonal (QL form)
     double* eb;        // [slots][m] S's
     double* eaux;      // [slots][2] local obs count p, tr(S'S)
+    float2* emhl;      // [slots][m][m] refined ETKF solve: M also as a float pair (hi + lo exact), upper triangle
 };
 
 __host__ __device__ static inline int count_bin(int p)
@@ -433,7 +434,14 @@ __device__ inline void solve_point(const CalcArgs& a, int pt, int slot, int p, i
         const size_t q0 = (size_t)slot * m * m;
         for (int i = tid; i < m * m; i += CALC_NT) {
             const int r = i / m, c = i - r * m;
-            if (c >= r) a.eq[q0 + i] = A[r * lda + c];
+            if (c >= r) {
+                const double x = A[r * lda + c];
+                a.eq[q0 + i] = x;
+                if (a.emhl) {
+                    const float hi = (float)x;
+                    a.emhl[q0 + i] = make_float2(hi, (float)(x - (double)hi));
+                }
+            }
         }
         if (tid < m) a.eb[(size_t)slot * m + tid] = b[tid];
         if (tid == 0) {

@@ -369,8 +369,22 @@ struct GramProcTC {
         if (sync) __syncthreads();
     }
 
-    // element (r, c >= r) of the packed upper triangle (DF) is at pk(r) + c
-    __device__ __forceinline__ int pk(int r) const { return r * a.m - ((r * (r + 1)) >> 1); }
+    // element (r, c >= r) of the upper triangle (DF) is at e0 + es c:
+    // rectangular packing in ceil(m/2) lines of L = m + 1 rounded up to
+    // even, line t holding row t and, reversed, row m - 1 - t.  A warp's
+    // 32 rows at one column then step by L - 1 (odd) float2 elements, so
+    // the drain's accesses do not share banks.
+    __device__ __forceinline__ void tri(int r, int& e0, int& es) const
+    {
+        const int m = a.m, L1 = ((m + 2) & ~1) - 1;
+        if (2 * r < m) {
+            e0 = r * L1;
+            es = 1;
+        } else {
+            e0 = (m - 1 - r) * L1 + 2 * m - 1;
+            es = -1;
+        }
+    }
 
     // add accumulator set `set` to the shared double-float S'S (its MMAs
     // have completed); thread (warp w, lane l) owns row 32 (w % 4) + l and
@@ -390,7 +404,9 @@ struct GramProcTC {
             const uint32_t base = ms.taddr + ((uint32_t)rq << 16) + (uint32_t)(2 * set * ms.N + c0);
             const bool direct = r < a.m;
             const bool offset = ST && r >= ms.N && r < ms.N + a.m;
-            float2* row = ms.Macc + (direct ? (DF ? pk(r) : r * ms.lda) : 0);
+            int e0 = 0, es = 1;
+            if (DF) tri(direct ? r : 0, e0, es);
+            else e0 = direct ? r * ms.lda : 0;
             float* rrow = ST ? ms.Mrest + (size_t)(offset ? r - ms.N : 0) * ms.lda : nullptr;
             constexpr int BB = 1;
 #pragma unroll
@@ -412,10 +428,11 @@ struct GramProcTC {
                             for (int j = 0; j < 8; ++j) {
                                 const int c = c0 + 8 * (b0 + u) + j;
                                 if (c < a.m && (!DF || c >= r)) {
-                                    float2 acc = row[c];
+                                    float2* el = ms.Macc + (e0 + es * c);
+                                    float2 acc = *el;
                                     df_add(acc, __uint_as_float(vh[u][j]));
                                     acc.y += __uint_as_float(vr[u][j]);   // <= 2^-8 of hi*hi'
-                                    row[c] = acc;
+                                    *el = acc;
                                 }
                             }
                         } else if (offset) {
@@ -1058,7 +1075,7 @@ static size_t mixed_smem_bytes(int m, int kc, int lseg, int st, int df)
     s += (size_t)2 * kc * 4;                               // raw innovations, two buffers
     s += (size_t)2 * m * 4;                                // quantum q, rounding constant
     s += 16;                                               // alignment
-    s += df ? (size_t)m * (m + 1) / 2 * 8 : (size_t)m * lda * 8;   // Macc (also A)
+    s += df ? (size_t)((m + 1) / 2) * ((m + 2) & ~1) * 8 : (size_t)m * lda * 8;   // Macc (also A)
     s += (size_t)(df ? 1 : 6) * (m + 1) * 8;               // b d e cs sn v
     s += (size_t)ENKFG_MAXTYPES * 8 * 2;
     s += (size_t)(CALC_NT / 32) * 8;
@@ -1084,7 +1101,7 @@ __global__ void __launch_bounds__(CALC_NT, 2) k_transforms_mixed(CalcArgs a, int
     float* sraw0 = (float*)sp;        sp += (size_t)2 * kcm * 4;
     float* qs = (float*)sp;           sp += (size_t)2 * m * 4;
     sp = (unsigned char*)(((uintptr_t)sp + 15) & ~(uintptr_t)15);
-    const int nmacc = DF ? m * (m + 1) / 2 : m * lda;      // DF: packed upper triangle
+    const int nmacc = DF ? ((m + 1) / 2) * ((m + 2) & ~1) : m * lda;   // DF: packed upper triangle
     double* Macc = (double*)sp;       sp += (size_t)nmacc * 8;
     float* Mrest = (float*)sp;        sp += ST ? (size_t)m * lda * 4 : 0;
     double* b = (double*)sp;          sp += (m + 1) * 8;
@@ -1251,16 +1268,32 @@ __global__ void __launch_bounds__(CALC_NT, 2) k_transforms_mixed(CalcArgs a, int
             const float2* Mp = (const float2*)Macc;
             const int lane = tid & 31;
             for (int r = wid; r < m; r += CALC_NT / 32) {
-                const float2* row = Mp + proc.pk(r);
+                int e0, es;
+                proc.tri(r, e0, es);
                 for (int c = r + lane; c < m; c += 32) {
-                    const float2 v2 = row[c];
+                    const float2 v2 = Mp[e0 + es * c];
                     const double x = (double)v2.x + (double)v2.y;
                     a.eq[q0 + (size_t)r * m + c] = c == r ? x + 1.0 : x;
+                    if (a.emhl) {
+                        // the same value as a float pair: Fast2Sum (|y| <=
+                        // |x|), through FP64 on the diagonal for the 1
+                        float2 o;
+                        if (c == r) {
+                            o.x = (float)(x + 1.0);
+                            o.y = (float)((x + 1.0) - (double)o.x);
+                        } else {
+                            o.x = v2.x + v2.y;
+                            o.y = (v2.x - o.x) + v2.y;
+                        }
+                        a.emhl[q0 + (size_t)r * m + c] = o;
+                    }
                 }
             }
             double dg = 0.0;
             if (tid < m) {
-                const float2 v2 = Mp[proc.pk(tid) + tid];
+                int e0, es;
+                proc.tri(tid, e0, es);
+                const float2 v2 = Mp[e0 + es * tid];
                 dg = (double)v2.x + (double)v2.y;
             }
             const double trss = la::block_sum<CALC_NT>(dg, red);

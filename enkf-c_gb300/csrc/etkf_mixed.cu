@@ -42,7 +42,8 @@
 // ---------------------------------------------------------------------------
 struct EmSlots {
     float* q;          // [slots][m][m]  Q of tred2, then the eigenvectors (columns)
-    float2* mhl;       // [slots][m][m]  M as a double-float pair (hi, lo), both triangles
+    float2* mhl;       // [slots][m][m]  M as a double-float pair (hi, lo): the upper triangle from the
+                       //                transform kernel, the lower one mirrored by k_em_replay
     float* d;          // [slots][m]     tridiagonal diagonal, then the eigenvalues
     float* e;          // [slots][m]     tridiagonal off-diagonal
     float2* rot;       // [slots][rcap]  QL rotation log
@@ -143,10 +144,118 @@ __device__ __forceinline__ void tred_publish(const float (&a)[R][R], int i, int 
     }
 }
 
+// one reduction step on the leading NB x NB blocks of 16 (NB = l / 16 + 1:
+// the blocks wholly past l hold no work), with its barrier between p and
+// the update
+template <int R, int NB>
+__device__ __forceinline__ void tred_step(float (&a)[R][R], int i, int l, float h, int tx, int ty, float* W,
+                                          float* P, float* red)
+{
+    constexpr int LD = 16 * R + 1;
+    const int tid = threadIdx.x;
+    const float ih = 1.0f / h;
+    float uk[NB], uj[NB];
+#pragma unroll
+    for (int c = 0; c < NB; ++c) {
+        const int k = tx + 16 * c;
+        uk[c] = k <= l ? W[i * LD + k] : 0.0f;
+    }
+#pragma unroll
+    for (int r = 0; r < NB; ++r) {
+        const int j = ty + 16 * r;
+        uj[r] = j <= l ? W[i * LD + j] : 0.0f;
+    }
+    // p = A u / h, f = p.u
+    float fp = 0.0f;
+#pragma unroll
+    for (int r = 0; r < NB; ++r) {
+        float sm = 0.0f;
+#pragma unroll
+        for (int c = 0; c < NB; ++c) sm = fmaf(a[r][c], uk[c], sm);
+        sm = hw_sum(sm) * ih;
+        const int j = ty + 16 * r;
+        if (tx == 0 && j <= l) P[j] = sm;
+        fp = fmaf(sm, uj[r], fp);
+    }
+    if (tx == 0) red[ty] = fp;
+    // u / h into column i (tred2 keeps it for the accumulation)
+    if (tid <= l) W[tid * LD + i] = W[i * LD + tid] * ih;
+    __syncthreads();
+    float fr[16];
+#pragma unroll
+    for (int t = 0; t < 16; ++t) fr[t] = red[t];
+#pragma unroll
+    for (int w = 8; w >= 1; w >>= 1)
+#pragma unroll
+        for (int t = 0; t < w; ++t) fr[t] += fr[t + w];
+    const float hh = fr[0] / (h + h);
+    float qk[NB];
+#pragma unroll
+    for (int c = 0; c < NB; ++c) {
+        const int k = tx + 16 * c;
+        qk[c] = k <= l ? P[k] - hh * uk[c] : 0.0f;
+    }
+#pragma unroll
+    for (int r = 0; r < NB; ++r) {
+        const int j = ty + 16 * r;
+        const float qj = j <= l ? P[j] - hh * uj[r] : 0.0f;
+#pragma unroll
+        for (int c = 0; c < NB; ++c) a[r][c] -= uj[r] * qk[c] + qj * uk[c];
+    }
+}
+
+template <int R, int NB>
+__device__ __forceinline__ void tred_step_nb(int nb, float (&a)[R][R], int i, int l, float h, int tx, int ty,
+                                             float* W, float* P, float* red)
+{
+    if constexpr (NB < R) {
+        if (nb == NB) tred_step<R, NB>(a, i, l, h, tx, ty, W, P, red);
+        else tred_step_nb<R, NB + 1>(nb, a, i, l, h, tx, ty, W, P, red);
+    } else {
+        tred_step<R, R>(a, i, l, h, tx, ty, W, P, red);
+    }
+}
+
+// one accumulation step on the leading NB x NB blocks
+template <int R, int NB>
+__device__ __forceinline__ void acc_step(float (&q)[R][R], int i, int l, int tx, int ty, const float* W)
+{
+    constexpr int LD = 16 * R + 1;
+    float uk[NB], vk[NB];
+#pragma unroll
+    for (int c = 0; c < NB; ++c) {
+        const int k = tx + 16 * c;
+        uk[c] = k <= l ? W[i * LD + k] : 0.0f;
+        vk[c] = k <= l ? W[k * LD + i] : 0.0f;
+    }
+#pragma unroll
+    for (int r = 0; r < NB; ++r) {
+        float g = 0.0f;
+#pragma unroll
+        for (int c = 0; c < NB; ++c) g = fmaf(uk[c], q[c][r], g);
+        g = hw_sum(g);
+        const int j = ty + 16 * r;
+        if (j <= l)
+#pragma unroll
+            for (int c = 0; c < NB; ++c) q[c][r] -= g * vk[c];
+    }
+}
+
+template <int R, int NB>
+__device__ __forceinline__ void acc_step_nb(int nb, float (&q)[R][R], int i, int l, int tx, int ty, const float* W)
+{
+    if constexpr (NB < R) {
+        if (nb == NB) acc_step<R, NB>(q, i, l, tx, ty, W);
+        else acc_step_nb<R, NB + 1>(nb, q, i, l, tx, ty, W);
+    } else {
+        acc_step<R, R>(q, i, l, tx, ty, W);
+    }
+}
+
 }  // namespace em
 
 template <int R>
-__global__ void __launch_bounds__(256, 2) k_em_tred(CalcArgs a, EmSlots z)
+__global__ void __launch_bounds__(256, 3) k_em_tred(CalcArgs a, EmSlots z)
 {
     using TS = em::TredSmem<R>;
     constexpr int MP = TS::MP, LD = TS::LD;
@@ -165,74 +274,22 @@ __global__ void __launch_bounds__(256, 2) k_em_tred(CalcArgs a, EmSlots z)
         hv[0] = 0.0f;   // no reflector at index 0
         ev[0] = 0.0f;
     }
-    // M's double-float pair for the residual (both triangles)
-    for (int i = tid; i < m * m; i += 256) {
-        const int r = i / m, c = i - r * m;
-        const double v = (c >= r) ? a.eq[q0 + i] : a.eq[q0 + (size_t)c * m + r];
-        const float hi = (float)v;
-        z.mhl[q0 + i] = make_float2(hi, (float)(v - (double)hi));
-    }
+    // M as the transform kernel left it (float pairs, upper triangle): the
+    // high parts, both triangles, into registers
     float a_[R][R];
 #pragma unroll
     for (int r = 0; r < R; ++r)
 #pragma unroll
         for (int c = 0; c < R; ++c) {
             const int j = ty + 16 * r, k = tx + 16 * c;
-            a_[r][c] = (j < m && k < m) ? (float)(k >= j ? a.eq[q0 + (size_t)j * m + k] : a.eq[q0 + (size_t)k * m + j])
-                                        : 0.0f;
+            a_[r][c] = (j < m && k < m) ? z.mhl[q0 + (size_t)(k >= j ? j * m + k : k * m + j)].x : 0.0f;
         }
     em::tred_publish<R>(a_, n - 1, tx, ty, W, hv, ev, dv);
     for (int i = n - 1; i >= 1; --i) {
         const int l = i - 1;
         __syncthreads();   // row i, h, g published; the last step's P and red read
         const float h = hv[i];
-        if (h != 0.0f) {
-            const float ih = 1.0f / h;
-            float uk[R], uj[R];
-#pragma unroll
-            for (int c = 0; c < R; ++c) {
-                const int k = tx + 16 * c;
-                uk[c] = k <= l ? W[i * LD + k] : 0.0f;
-            }
-#pragma unroll
-            for (int r = 0; r < R; ++r) {
-                const int j = ty + 16 * r;
-                uj[r] = j <= l ? W[i * LD + j] : 0.0f;
-            }
-            // p = A u / h, f = p.u
-            float fp = 0.0f;
-#pragma unroll
-            for (int r = 0; r < R; ++r) {
-                float s = 0.0f;
-#pragma unroll
-                for (int c = 0; c < R; ++c) s = fmaf(a_[r][c], uk[c], s);
-                s = em::hw_sum(s) * ih;
-                const int j = ty + 16 * r;
-                if (tx == 0 && j <= l) P[j] = s;
-                fp = fmaf(s, uj[r], fp);
-            }
-            if (tx == 0) red[ty] = fp;
-            // u / h into column i (tred2 keeps it for the accumulation)
-            if (tid <= l) W[tid * LD + i] = W[i * LD + tid] * ih;
-            __syncthreads();
-            float f = 0.0f;
-#pragma unroll
-            for (int t = 0; t < 16; ++t) f += red[t];
-            const float hh = f / (h + h);
-            float qk[R];
-#pragma unroll
-            for (int c = 0; c < R; ++c) {
-                const int k = tx + 16 * c;
-                qk[c] = k <= l ? P[k] - hh * uk[c] : 0.0f;
-            }
-#pragma unroll
-            for (int r = 0; r < R; ++r) {
-                const int j = ty + 16 * r;
-                const float qj = j <= l ? P[j] - hh * uj[r] : 0.0f;
-#pragma unroll
-                for (int c = 0; c < R; ++c) a_[r][c] -= uj[r] * qk[c] + qj * uk[c];
-            }
-        }
+        if (h != 0.0f) em::tred_step_nb<R, 1>((l >> 4) + 1, a_, i, l, h, tx, ty, W, P, red);
         if (l >= 1) em::tred_publish<R>(a_, l, tx, ty, W, hv, ev, dv);
         else if (ty == 0 && tx == 0) dv[0] = a_[0][0];
     }
@@ -245,26 +302,7 @@ __global__ void __launch_bounds__(256, 2) k_em_tred(CalcArgs a, EmSlots z)
         for (int r = 0; r < R; ++r) q_[c][r] = 0.0f;
     for (int i = 0; i < n; ++i) {
         const int l = i - 1;
-        if (hv[i] != 0.0f) {
-            float uk[R], vk[R];
-#pragma unroll
-            for (int c = 0; c < R; ++c) {
-                const int k = tx + 16 * c;
-                uk[c] = k <= l ? W[i * LD + k] : 0.0f;
-                vk[c] = k <= l ? W[k * LD + i] : 0.0f;
-            }
-#pragma unroll
-            for (int r = 0; r < R; ++r) {
-                float g = 0.0f;
-#pragma unroll
-                for (int c = 0; c < R; ++c) g = fmaf(uk[c], q_[c][r], g);
-                g = em::hw_sum(g);
-                const int j = ty + 16 * r;
-                if (j <= l)
-#pragma unroll
-                    for (int c = 0; c < R; ++c) q_[c][r] -= g * vk[c];
-            }
-        }
+        if (hv[i] != 0.0f) em::acc_step_nb<R, 1>((l >> 4) + 1, q_, i, l, tx, ty, W);
 #pragma unroll
         for (int c = 0; c < R; ++c)
 #pragma unroll
@@ -338,6 +376,8 @@ __global__ void __launch_bounds__(EM_REPLAY_NT) k_em_replay(CalcArgs a, EmSlots 
     for (int i = tid; i < m * m; i += EM_REPLAY_NT) {
         const int r = i / m, c = i - r * m;
         A[r * lda + c] = z.q[q0 + i];
+        // the lower triangle of M's float pairs, for the residual's rows
+        if (c < r) z.mhl[q0 + i] = z.mhl[q0 + (size_t)c * m + r];
     }
     const int stt = z.nh[slot];
     for (int i = tid; i < m; i += EM_REPLAY_NT) {
@@ -740,6 +780,7 @@ enkfg_status run_etkf_mixed(enkfg_ctx* ctx, const CalcArgs& a0, cudaStream_t st)
         b.eq = ctx->d_eq;
         b.eb = ctx->d_eb;
         b.eaux = ctx->d_eaux;
+        b.emhl = z.mhl;
         if (b.persistent) CK(cudaMemsetAsync(ctx->d_qhead, 0, sizeof(int), st));
         batch_mark(ctx, 0, st);
         if ((s = launch_mixed(ctx, b, st))) return s;
