@@ -756,14 +756,18 @@ ENKFG_API enkfg_status enkfg_update_fields_dev(enkfg_ctx* ctx, const enkfg_updat
 }
 
 // The host-buffer update streams the field-layers through the device in
-// groups (the reference's FIELDBUFFERSIZE batches, update/update.c:1552-2132):
-// three device buffers in turn, the copy of group g + 1 in and of group g - 1
-// out running on the context's two copy streams while group g is updated.
-// A group holds whole multiples of the update kernel's field-layer pass
-// where it can (the transforms are staged once per pass) within about 3 GB.
-// With pinned host buffers the copies overlap the update; with pageable ones
-// they are staged by the driver and serialise.
+// units (the reference's FIELDBUFFERSIZE batches, update/update.c:1552-2132):
+// a unit is a group of field-layers -- whole multiples of the update
+// kernel's ten-layer pass where it can, within about 3 GB -- cut into blocks
+// of model rows of about UPD_UNIT_BYTES (a multiple of the stride, so that a
+// block starts on a strided row and its rows interpolate X5 exactly as in
+// one call).  Three device buffers in turn: the copy of unit u + 1 in and of
+// unit u - 1 out run on the context's two copy streams (one 2-D copy each,
+// the unit's rows of every member plane) while unit u is updated.  With
+// pinned host buffers the copies overlap the update; with pageable ones they
+// are staged by the driver and serialise.
 #define UPD_GROUP_BYTES ((size_t)3 << 30)
+#define UPD_UNIT_BYTES ((size_t)512 << 20)
 ENKFG_API enkfg_status enkfg_update_fields(enkfg_ctx* ctx, const enkfg_update_params* p, const int* numlevels,
                                           int nfield, const int* levels, float* fields, float* infl)
 {
@@ -774,19 +778,30 @@ ENKFG_API enkfg_status enkfg_update_fields(enkfg_ctx* ctx, const enkfg_update_pa
     SETDEV();
     cudaStream_t st = ctx->stream;
     int j2 = p->j2 < 0 ? ctx->mnj - 1 : p->j2;
-    size_t jsize = (size_t)(j2 - p->j1 + 1);
-    size_t plane = jsize * ctx->mni;
-    size_t per = (size_t)(p->mode == ENKFG_MODE_ENOI ? p->nmem + 1 : p->nmem) * plane;   // floats per field-layer
+    const int jsize = j2 - p->j1 + 1;
+    const size_t mni = (size_t)ctx->mni;
+    const size_t plane = (size_t)jsize * mni;
+    const int mp = p->mode == ENKFG_MODE_ENOI ? p->nmem + 1 : p->nmem;   // member planes a field-layer
+    const size_t per = (size_t)mp * plane;                                // floats per field-layer
     int G = (int)(UPD_GROUP_BYTES / (per * sizeof(float)));
     if (G < 1) G = 1;
     if (G >= 10) G -= G % 10;
     if (ctx->field_buffer > 0) G = ctx->field_buffer;
     if (G > nfield) G = nfield;
     const int ngroups = (nfield + G - 1) / G;
-    const int nbuf = ngroups < 3 ? ngroups : 3;
+    // rows per unit
+    const int stp = ctx->stride > 0 ? ctx->stride : 1;
+    int R = (int)(UPD_UNIT_BYTES / ((size_t)G * mp * mni * sizeof(float)));
+    R -= R % stp;
+    if (R < stp) R = stp;
+    if (R > jsize) R = jsize;
+    const int nrb = (jsize + R - 1) / R;
+    const int nunits = ngroups * nrb;
+    const int nbuf = nunits < 3 ? nunits : 3;
+    const size_t ufl = (size_t)G * mp * R * mni, uinf = (size_t)G * R * mni;   // floats a buffer
     if ((s = ensure(ctx, &ctx->d_numlevels, &ctx->numlevels_cap, (size_t)ctx->mnj * ctx->mni))) return s;
-    if ((s = ensure(ctx, &ctx->d_fields, &ctx->fields_cap, (size_t)nbuf * G * per))) return s;
-    if (infl && (s = ensure(ctx, &ctx->d_infl, &ctx->infl_cap, (size_t)nbuf * G * plane))) return s;
+    if ((s = ensure(ctx, &ctx->d_fields, &ctx->fields_cap, (size_t)nbuf * ufl))) return s;
+    if (infl && (s = ensure(ctx, &ctx->d_infl, &ctx->infl_cap, (size_t)nbuf * uinf))) return s;
     for (int k = 0; k < 2; ++k)
         if (ctx->cstream[k] == nullptr) CK(cudaStreamCreateWithFlags(&ctx->cstream[k], cudaStreamNonBlocking));
     for (int k = 0; k < 9; ++k)
@@ -795,30 +810,37 @@ ENKFG_API enkfg_status enkfg_update_fields(enkfg_ctx* ctx, const enkfg_update_pa
     CK(cudaMemcpyAsync(ctx->d_numlevels, numlevels, (size_t)ctx->mnj * ctx->mni * sizeof(int), cudaMemcpyHostToDevice,
                        st));
     cudaEventRecord(ctx->ev[6], st);
-    for (int g = 0; g < ngroups; ++g) {
-        const int b = g % nbuf, f0 = g * G, nf = (nfield - f0 < G) ? nfield - f0 : G;
-        float* dbuf = ctx->d_fields + (size_t)b * G * per;
-        float* dinf = infl ? ctx->d_infl + (size_t)b * G * plane : nullptr;
+    for (int u = 0; u < nunits; ++u) {
+        const int g = u / nrb, rb = u - g * nrb;
+        const int b = u % nbuf, f0 = g * G, nf = (nfield - f0 < G) ? nfield - f0 : G;
+        const int r0 = rb * R, rr = (jsize - r0 < R) ? jsize - r0 : R;
+        const size_t wbytes = (size_t)rr * mni * sizeof(float);            // one member plane's rows
+        float* dbuf = ctx->d_fields + (size_t)b * ufl;
+        float* dinf = infl ? ctx->d_infl + (size_t)b * uinf : nullptr;
+        float* hsrc = fields + (size_t)f0 * per + (size_t)r0 * mni;
         cudaEvent_t in_done = ctx->uev[3 * b], upd_done = ctx->uev[3 * b + 1], out_done = ctx->uev[3 * b + 2];
-        // the buffer's previous group has left the device; the update before
+        // the buffer's previous unit has left the device; the update before
         // this call (stream order of st) has finished with the buffers
-        if (g >= nbuf) CK(cudaStreamWaitEvent(cin, out_done, 0));
+        if (u >= nbuf) CK(cudaStreamWaitEvent(cin, out_done, 0));
         else {
             CK(cudaEventRecord(in_done, st));
             CK(cudaStreamWaitEvent(cin, in_done, 0));
         }
-        CK(cudaMemcpyAsync(dbuf, fields + (size_t)f0 * per, (size_t)nf * per * sizeof(float), cudaMemcpyHostToDevice,
-                           cin));
+        CK(cudaMemcpy2DAsync(dbuf, wbytes, hsrc, plane * sizeof(float), wbytes, (size_t)nf * mp,
+                             cudaMemcpyHostToDevice, cin));
         CK(cudaEventRecord(in_done, cin));
         CK(cudaStreamWaitEvent(st, in_done, 0));
-        if ((s = run_update(ctx, p, ctx->d_numlevels, nf, levels + f0, dbuf, dinf, st))) return s;
+        enkfg_update_params pu = *p;
+        pu.j1 = p->j1 + r0;
+        pu.j2 = pu.j1 + rr - 1;
+        if ((s = run_update(ctx, &pu, ctx->d_numlevels, nf, levels + f0, dbuf, dinf, st))) return s;
         CK(cudaEventRecord(upd_done, st));
         CK(cudaStreamWaitEvent(cout, upd_done, 0));
-        CK(cudaMemcpyAsync(fields + (size_t)f0 * per, dbuf, (size_t)nf * per * sizeof(float), cudaMemcpyDeviceToHost,
-                           cout));
+        CK(cudaMemcpy2DAsync(hsrc, plane * sizeof(float), dbuf, wbytes, wbytes, (size_t)nf * mp,
+                             cudaMemcpyDeviceToHost, cout));
         if (infl)
-            CK(cudaMemcpyAsync(infl + (size_t)f0 * plane, dinf, (size_t)nf * plane * sizeof(float),
-                               cudaMemcpyDeviceToHost, cout));
+            CK(cudaMemcpy2DAsync(infl + (size_t)f0 * plane + (size_t)r0 * mni, plane * sizeof(float), dinf, wbytes,
+                                 wbytes, (size_t)nf, cudaMemcpyDeviceToHost, cout));
         CK(cudaEventRecord(out_done, cout));
     }
     cudaEventRecord(ctx->ev[7], st);

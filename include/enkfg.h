@@ -243,11 +243,13 @@ typedef struct {
  * (update.c:568-814) and fields are [nfield][nmem+1][jsize][mni] with the
  * background in slot nmem.  Uses the transforms resident in the context.
  * The field-layers stream through the device in groups (as the reference's
- * FIELDBUFFERSIZE batches, update/update.c:1552-2132), three device buffers
- * in turn: the copies in and out of neighbouring groups run on the
- * context's copy streams while a group is updated, so with pinned host
+ * FIELDBUFFERSIZE batches, update/update.c:1552-2132), each group in blocks
+ * of model rows (about 512 MB, a multiple of the stride), three device
+ * buffers in turn: the copies in and out of neighbouring blocks run on the
+ * context's copy streams while a block is updated, so with pinned host
  * buffers the transfers overlap the update and the device holds three
- * groups, not the whole ensemble. */
+ * blocks, not the whole ensemble.  The result does not depend on the
+ * grouping. */
 ENKFG_API enkfg_status enkfg_update_fields(enkfg_ctx* ctx, const enkfg_update_params* p, const int* numlevels, int nfield, const int* levels, float* fields, float* infl);
 
 /* Field-layers per group of the host-buffer update (FIELDBUFFERSIZE,
