@@ -213,17 +213,22 @@ __global__ void k_queue_rank(int n, const int* __restrict__ counts, int* __restr
     }
 }
 
-// blkcnt [nblk][NBINS] -> exclusive offsets of (block, bin) in bin-major order
-__global__ void k_queue_offsets(int nblk, int* blkcnt)
+// blkcnt [nblk][NBINS] -> exclusive offsets of (block, bin): segments of
+// bps blocks in turn, bin-major within a segment, so that the queue holds
+// each segment's points (sorted by bin) in the segment's own range
+__global__ void k_queue_offsets(int nblk, int bps, int* blkcnt)
 {
     if (threadIdx.x != 0 || blockIdx.x != 0) return;
     int acc = 0;
-    for (int b = 0; b < NBINS; ++b)
-        for (int k = 0; k < nblk; ++k) {
-            int v = blkcnt[k * NBINS + b];
-            blkcnt[k * NBINS + b] = acc;
-            acc += v;
-        }
+    for (int k0 = 0; k0 < nblk; k0 += bps) {
+        const int k1 = (k0 + bps < nblk) ? k0 + bps : nblk;
+        for (int b = 0; b < NBINS; ++b)
+            for (int k = k0; k < k1; ++k) {
+                int v = blkcnt[k * NBINS + b];
+                blkcnt[k * NBINS + b] = acc;
+                acc += v;
+            }
+    }
 }
 
 __global__ void k_queue_scatter(int n, const int* __restrict__ counts, const int* __restrict__ rank,
@@ -235,7 +240,8 @@ __global__ void k_queue_scatter(int n, const int* __restrict__ counts, const int
     order[blkoff[blockIdx.x * NBINS + b] + rank[i]] = i;
 }
 
-enkfg_status build_queue(enkfg_ctx* ctx, int npts, cudaStream_t st)
+// seg: points per segment (a multiple of QS_T; 0: one segment)
+enkfg_status build_queue(enkfg_ctx* ctx, int npts, int seg, cudaStream_t st)
 {
     enkfg_status s;
     const int nblk = div_up(npts, QS_T);
@@ -246,7 +252,7 @@ enkfg_status build_queue(enkfg_ctx* ctx, int npts, cudaStream_t st)
     int* blk = rank + npts;
     k_queue_rank<<<nblk, QS_T, 0, st>>>(npts, ctx->d_counts, rank, blk);
     CKL();
-    k_queue_offsets<<<1, 32, 0, st>>>(nblk, blk);
+    k_queue_offsets<<<1, 32, 0, st>>>(nblk, seg > 0 ? seg / QS_T : nblk, blk);
     CKL();
     k_queue_scatter<<<nblk, QS_T, 0, st>>>(npts, ctx->d_counts, rank, blk, ctx->d_order);
     CKL();
@@ -351,6 +357,7 @@ static enkfg_status autotune(enkfg_ctx* ctx, CalcArgs a, int precision, cudaStre
     for (int b = 0; b < NBINS; ++b) table[b] = precision == ENKFG_PREC_MIXED ? 32 : (b < 4 ? 8 : b < 6 ? 16 : b < 9 ? 32 : 64);
     int* kct = ctx->d_qhead + 2 + NBINS;
     enkfg_status s = ENKFG_OK;
+    bool done[NBINS] = {};   // the queue repeats the bins once per segment: tune each once
     int pos = 0;
     while (pos < npts && s == ENKFG_OK) {
         const int bin = count_bin(counts[order[pos]]);
@@ -359,7 +366,8 @@ static enkfg_status autotune(enkfg_ctx* ctx, CalcArgs a, int precision, cudaStre
         const int len = end - pos;
         const int take = len < TUNE_SAMPLE ? len : TUNE_SAMPLE;
         const int first = pos + (len - take) / 2;
-        if (take >= 64 && bin >= 2) {
+        if (take >= 64 && bin >= 2 && !done[bin]) {
+            done[bin] = true;
             float best = 1e30f;
             for (int k = 0; k < ncand; ++k) {
                 int tab[NBINS];
@@ -532,14 +540,49 @@ void batch_mark(enkfg_ctx* ctx, int k, cudaStream_t st)
     cudaEventRecord(ctx->bev[idx], st);
 }
 
+size_t batch_points(size_t per_slot, size_t budget, int nitems)
+{
+    size_t B = budget / per_slot;
+    if (B < 256) B = 256;
+    if (B >= 1024) B -= B % 1024;
+    if (B > (size_t)nitems) B = (size_t)nitems;
+    return B;
+}
+
+// slot bytes of the batched FP64 inverse and eigensolver
+static size_t inv_slot_bytes(int m) { return (size_t)m * m * 8 + (size_t)m * 8 + 16; }
+static size_t etkf_slot_bytes(int m)
+{
+    const size_t rcap = (size_t)m * m + 64 * (size_t)m, hcap = 8 * (size_t)m;
+    return (size_t)m * m * 8 + (size_t)5 * m * 8 + 16 + rcap * 16 + hcap * 8 + 4;
+}
+
+void batch_out(enkfg_ctx* ctx, int i0, int nb, cudaStream_t st)
+{
+    if (ctx->out_seg <= 0) return;
+    cudaStream_t cout = ctx->cstream[1];
+    const size_t m = ctx->nmem, md = ctx->nmem_dyn;
+    cudaEventRecord(ctx->out_ev, st);
+    cudaStreamWaitEvent(cout, ctx->out_ev, 0);
+    if (ctx->out_T)
+        cudaMemcpyAsync(ctx->out_T + (size_t)i0 * md * m, ctx->d_T + (size_t)i0 * md * m, (size_t)nb * md * m * 4,
+                        cudaMemcpyDeviceToHost, cout);
+    if (ctx->out_w)
+        cudaMemcpyAsync(ctx->out_w + (size_t)i0 * m, ctx->d_w + (size_t)i0 * m, (size_t)nb * m * 4,
+                        cudaMemcpyDeviceToHost, cout);
+    if (ctx->out_T64)
+        cudaMemcpyAsync(ctx->out_T64 + (size_t)i0 * md * m, ctx->d_T64 + (size_t)i0 * md * m,
+                        (size_t)nb * md * m * 8, cudaMemcpyDeviceToHost, cout);
+    if (ctx->out_w64)
+        cudaMemcpyAsync(ctx->out_w64 + (size_t)i0 * m, ctx->d_w64 + (size_t)i0 * m, (size_t)nb * m * 8,
+                        cudaMemcpyDeviceToHost, cout);
+}
+
 static enkfg_status run_inv_batched(enkfg_ctx* ctx, const CalcArgs& a0, int precision, cudaStream_t st)
 {
     enkfg_status s;
     const int m = a0.m, nitems = a0.nitems;
-    const size_t per = (size_t)m * m * 8 + (size_t)m * 8 + 16;
-    size_t B = ((size_t)2 << 30) / per;      // about 2 GB of scratch per batch
-    if (B < 256) B = 256;
-    if (B > (size_t)nitems) B = (size_t)nitems;
+    const size_t B = batch_points(inv_slot_bytes(m), (size_t)2 << 30, nitems);   // about 2 GB a batch
     if ((s = ensure(ctx, &ctx->d_eq, &ctx->eq_cap, B * m * m))) return s;
     if ((s = ensure(ctx, &ctx->d_eb, &ctx->eb_cap, B * m))) return s;
     if ((s = ensure(ctx, &ctx->d_eaux, &ctx->eaux_cap, B * 2))) return s;
@@ -571,6 +614,7 @@ static enkfg_status run_inv_batched(enkfg_ctx* ctx, const CalcArgs& a0, int prec
         k_inv_finish<<<nb, INV_NT, ismem, st>>>(b);
         CKL();
         batch_mark(ctx, 2, st);
+        batch_out(ctx, i0, nb, st);
     }
     return ENKFG_OK;
 }
@@ -618,10 +662,7 @@ static enkfg_status run_etkf_batched(enkfg_ctx* ctx, const CalcArgs& a0, int pre
     const int m = a0.m, nitems = a0.nitems;
     const int rcap = m * m + 64 * m;         // QL typically needs about 0.75 m^2 rotations
     const int hcap = 8 * m;
-    const size_t per = (size_t)m * m * 8 + (size_t)5 * m * 8 + 16 + (size_t)rcap * 16 + (size_t)hcap * 8 + 4;
-    size_t B = ((size_t)2 << 30) / per;      // about 2 GB of scratch per batch
-    if (B < 256) B = 256;
-    if (B > (size_t)nitems) B = (size_t)nitems;
+    const size_t B = batch_points(etkf_slot_bytes(m), (size_t)2 << 30, nitems);   // about 2 GB a batch
     if ((s = ensure(ctx, &ctx->d_eq, &ctx->eq_cap, B * m * m))) return s;
     if ((s = ensure(ctx, &ctx->d_ed, &ctx->ed_cap, B * m))) return s;
     if ((s = ensure(ctx, &ctx->d_ee, &ctx->ee_cap, B * m))) return s;
@@ -669,6 +710,7 @@ static enkfg_status run_etkf_batched(enkfg_ctx* ctx, const CalcArgs& a0, int pre
         k_eig_finish<<<nb, CALC_NT, fsmem, st>>>(b, ctx->d_eval, ctx->d_erot, rcap, ctx->d_ehdr, hcap, ctx->d_enh);
         CKL();
         batch_mark(ctx, 2, st);
+        batch_out(ctx, i0, nb, st);
     }
     return ENKFG_OK;
 }
@@ -756,7 +798,27 @@ enkfg_status run_transforms(enkfg_ctx* ctx, const enkfg_calc_params* p, cudaStre
     if (p->path == ENKFG_PATH_BATCHED) {
         // size-sorted queue (by candidate count)
         if ((s = count_candidates(ctx, ctx->d_counts, st))) return s;
-        if ((s = build_queue(ctx, npts, st))) return s;
+        // the queue sorted within segments of one solve batch, so that a
+        // batch covers a contiguous range of points and its outputs can
+        // leave while the next batch runs
+        int seg = 0;
+        {
+            const bool etkf_ = (p->mode != ENKFG_MODE_ENOI && p->scheme == ENKFG_SCHEME_ETKF);
+            const bool defer_ = !(p->want_diag && ctx->ntypes > 1);
+            if (defer_) {
+                size_t B;
+                if (etkf_ && p->precision == ENKFG_PREC_MIXED && etkf_mixed_supported(m))
+                    B = batch_points(etkf_mixed_slot_bytes(m), (size_t)8 << 30, npts);
+                else if (etkf_)
+                    B = batch_points(etkf_slot_bytes(m), (size_t)2 << 30, npts);
+                else
+                    B = batch_points(inv_slot_bytes(m), (size_t)2 << 30, npts);
+                if (B % QS_T == 0 && B < (size_t)npts) seg = (int)B;
+                else if (B >= (size_t)npts) seg = npts;   // one batch
+            }
+        }
+        if ((s = build_queue(ctx, npts, seg % QS_T == 0 ? seg : 0, st))) return s;
+        if (ctx->out_seg && seg == 0) ctx->out_seg = 0;   // batches mix regions: copy at the end
         a.persistent = 1;
         a.order = ctx->d_order;
         a.qhead = ctx->d_qhead;
@@ -787,6 +849,7 @@ enkfg_status run_transforms(enkfg_ctx* ctx, const enkfg_calc_params* p, cudaStre
     // pass, so they keep the in-kernel one)
     const bool etkf = (p->mode != ENKFG_MODE_ENOI && p->scheme == ENKFG_SCHEME_ETKF);
     const bool defer = !(a.want_diag && a.ntypes > 1);
+    if (!defer) ctx->out_seg = 0;   // one launch: the host call copies at the end
     ctx->nbatch = 0;
     if (defer && etkf && p->precision == ENKFG_PREC_MIXED && etkf_mixed_supported(m)) {
         if ((s = run_etkf_mixed(ctx, a, st))) return s;

@@ -142,6 +142,7 @@ ENKFG_API void enkfg_destroy(enkfg_ctx* ctx)
         if (ctx->cstream[k]) cudaStreamDestroy(ctx->cstream[k]);
     for (int k = 0; k < 9; ++k)
         if (ctx->uev[k]) cudaEventDestroy(ctx->uev[k]);
+    if (ctx->out_ev) cudaEventDestroy(ctx->out_ev);
     if (ctx->own_stream) ctx->stream = ctx->own_stream;
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
     free(ctx);
@@ -680,13 +681,38 @@ ENKFG_API enkfg_status enkfg_calc_transforms(enkfg_ctx* ctx, const enkfg_calc_pa
     enkfg_calc_params q = *p;
     if (diag && diag->nlobs) q.want_diag = 1;
     ctx->want64 = (T64 != nullptr || w64 != nullptr);
-    if ((s = run_transforms(ctx, &q, st))) return s;
+    // T and w leave batch by batch on the output copy stream while the next
+    // batch runs, where the batches cover contiguous ranges of points
+    if (ctx->cstream[1] == nullptr) CK(cudaStreamCreateWithFlags(&ctx->cstream[1], cudaStreamNonBlocking));
+    if (ctx->out_ev == nullptr) CK(cudaEventCreateWithFlags(&ctx->out_ev, cudaEventDisableTiming));
+    struct OutGuard {
+        enkfg_ctx* c;
+        ~OutGuard()
+        {
+            c->out_T = c->out_w = nullptr;
+            c->out_T64 = c->out_w64 = nullptr;
+            c->out_seg = 0;
+        }
+    } guard{ ctx };
+    ctx->out_T = enkf ? T : nullptr;
+    ctx->out_w = w;
+    ctx->out_T64 = enkf ? T64 : nullptr;
+    ctx->out_w64 = w64;
+    ctx->out_seg = 1;
+    s = run_transforms(ctx, &q, st);
+    const bool per_batch = ctx->out_seg > 0;
+    ctx->out_seg = 0;
+    cudaStreamSynchronize(ctx->cstream[1]);   // no copy in flight past this call
+    if (s) return s;
     if ((s = finish_calc(ctx, st))) return s;
     size_t npts = (size_t)ctx->nj * ctx->ni, m = ctx->nmem, md = ctx->nmem_dyn;
-    if (enkf) CK(cudaMemcpyAsync(T, ctx->d_T, npts * md * m * sizeof(float), cudaMemcpyDeviceToHost, st));
-    CK(cudaMemcpyAsync(w, ctx->d_w, npts * m * sizeof(float), cudaMemcpyDeviceToHost, st));
-    if (enkf && T64) CK(cudaMemcpyAsync(T64, ctx->d_T64, npts * md * m * sizeof(double), cudaMemcpyDeviceToHost, st));
-    if (w64) CK(cudaMemcpyAsync(w64, ctx->d_w64, npts * m * sizeof(double), cudaMemcpyDeviceToHost, st));
+    if (!per_batch) {
+        if (enkf) CK(cudaMemcpyAsync(T, ctx->d_T, npts * md * m * sizeof(float), cudaMemcpyDeviceToHost, st));
+        CK(cudaMemcpyAsync(w, ctx->d_w, npts * m * sizeof(float), cudaMemcpyDeviceToHost, st));
+        if (enkf && T64)
+            CK(cudaMemcpyAsync(T64, ctx->d_T64, npts * md * m * sizeof(double), cudaMemcpyDeviceToHost, st));
+        if (w64) CK(cudaMemcpyAsync(w64, ctx->d_w64, npts * m * sizeof(double), cudaMemcpyDeviceToHost, st));
+    }
     if (diag && q.want_diag) {
         size_t pn = npts * ctx->ntypes;
         if (diag->nlobs) CK(cudaMemcpyAsync(diag->nlobs, ctx->d_nlobs, npts * sizeof(int), cudaMemcpyDeviceToHost, st));

@@ -695,6 +695,19 @@ __global__ void __launch_bounds__(EM_NT, 2) k_em_refine(CalcArgs a, EmSlots z)
 
 bool etkf_mixed_supported(int m) { return m >= 2 && m <= 96; }
 
+// bytes of one batch slot of the refined solve
+size_t etkf_mixed_slot_bytes(int m)
+{
+    int R = (m + 15) / 16;
+    if (R < 2) R = 2;
+    if (R == 5) R = 6;
+    const size_t MP = 16 * (size_t)R, rcap = (size_t)m * m + 64 * (size_t)m, hcap = 8 * (size_t)m;
+    return (size_t)m * m * 8 + (size_t)3 * m * 8 + 16     // M, S's, aux (FP64 slots)
+           + (size_t)m * m * 12 + (size_t)2 * m * 4        // Q, M hi/lo, d, e
+           + rcap * 8 + hcap * 8 + 4                       // rotation log
+           + MP * MP * 12;                                 // Z0, P
+}
+
 template <int R>
 static size_t em_refine_smem()
 {
@@ -727,13 +740,7 @@ enkfg_status run_etkf_mixed(enkfg_ctx* ctx, const CalcArgs& a0, cudaStream_t st)
     const int MP = 16 * R;
     const int rcap = m * m + 64 * m;         // QL typically needs about 0.75 m^2 rotations
     const int hcap = 8 * m;
-    const size_t per = (size_t)m * m * 8 + (size_t)3 * m * 8 + 16     // M, S's, aux (FP64 slots)
-                       + (size_t)m * m * 12 + (size_t)2 * m * 4           // Q, M hi/lo, d, e
-                       + (size_t)rcap * 8 + (size_t)hcap * 8 + 4          // rotation log
-                       + (size_t)MP * MP * 12;                            // Z0, P
-    size_t B = ((size_t)8 << 30) / per;      // about 8 GB of scratch per batch
-    if (B < 256) B = 256;
-    if (B > (size_t)nitems) B = (size_t)nitems;
+    const size_t B = batch_points(etkf_mixed_slot_bytes(m), (size_t)8 << 30, nitems);   // about 8 GB a batch
     if ((s = ensure(ctx, &ctx->d_eq, &ctx->eq_cap, B * m * m))) return s;
     if ((s = ensure(ctx, &ctx->d_eb, &ctx->eb_cap, B * m))) return s;
     if ((s = ensure(ctx, &ctx->d_eaux, &ctx->eaux_cap, B * 2))) return s;
@@ -807,6 +814,7 @@ enkfg_status run_etkf_mixed(enkfg_ctx* ctx, const CalcArgs& a0, cudaStream_t st)
         }
         if (s) return s;
         batch_mark(ctx, 2, st);
+        batch_out(ctx, i0, nb, st);
     }
     return ENKFG_OK;
 }

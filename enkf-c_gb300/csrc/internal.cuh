@@ -109,6 +109,14 @@ struct enkfg_ctx {
     float* d_St;                // [nsorted][mpad] standardised S, sorted, member-contiguous
     double* d_ss;               // [nsorted] standardised innovation, sorted
     float* d_ssf;               // [nsorted] the same rounded to float (mixed path)
+    // host outputs of the transform call being run, copied out batch by
+    // batch when the queue segments match the batches (out_seg > 0)
+    float* out_T;
+    float* out_w;
+    double* out_T64;
+    double* out_w64;
+    int out_seg;
+    cudaEvent_t out_ev;
     float* d_gtmp;              // [nobs][mpad] transpose scratch of the gather
     unsigned int* d_smax;       // [ENKFG_MAXMEM] max |St| per member (float bits), mixed-path quantum
     float* d_qscale;            // [2][ENKFG_MAXMEM] per-member quantum q and 1/q (powers of two)
@@ -281,6 +289,14 @@ enkfg_status run_transforms(enkfg_ctx* ctx, const enkfg_calc_params* p, cudaStre
 // per-batch timing (calc.cu): k = 0 before a batch's transform kernel, 1
 // after it, 2 after the batch's solve kernels
 void batch_mark(enkfg_ctx* ctx, int k, cudaStream_t st);
+// points per batch of a batched solve: budget / per-slot bytes, at least
+// 256, a multiple of 1024 from 1024 on, at most nitems
+size_t batch_points(size_t per_slot, size_t budget, int nitems);
+size_t etkf_mixed_slot_bytes(int m);
+// after the last kernel of the batch of queue items [i0, i0 + nb): the
+// host outputs of those points (a contiguous range when the queue is
+// sorted within batch-sized segments) start to copy out
+void batch_out(enkfg_ctx* ctx, int i0, int nb, cudaStream_t st);
 // the transform stage's FP32 eigendecomposition + refined solve for ETKF on
 // the mixed path (etkf_mixed.cu); false if nmem is beyond its register tiles
 bool etkf_mixed_supported(int m);
