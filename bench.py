@@ -42,14 +42,19 @@ import numpy as np  # noqa: E402
 
 METRIC = "local analyses/s (calc + update cycle)"
 
-# DRAM bytes per local analysis from one ncu capture of the current version
-# of a kernel on workload 2 at half edge length (15,000 analyses):
-# k_update_cells 462.6 MB (dram__bytes.sum.per_second x duration).  Traffic
-# grows with the analyses (and, for the update, with the cells they cover),
-# so a full launch scales by the analyses.  A kernel without a capture of
-# its current version reports no traffic.
+# DRAM bytes per local analysis from ncu captures of the current version of
+# a kernel:
+#   k_update_cells, workload 2 at half edge length (15,000 analyses):
+#     462.6 MB (dram__bytes.sum.per_second x duration);
+#   k_transforms_mixed, workload 3 at full size, three launches of one solve
+#     batch (19,456 analyses each): 820.2 MB read + 1,450.1 MB written on
+#     average (dram__bytes_read.sum, dram__bytes_write.sum).
+# Traffic grows with the analyses (and, for the update, with the cells they
+# cover), so a full launch scales by the analyses.  A kernel without a
+# capture of its current version reports no traffic.
 TRAFFIC_PER_ANALYSIS = {
     (2, "k_update_cells"): 462.6e6 / 15000,
+    (3, "k_transforms_mixed"): (820.2e6 + 1450.1e6) / 19456,
 }
 UNIT = "analyses/s"
 
@@ -307,8 +312,8 @@ def run_gpu(args, rank, world, local_rank):
     # observations: 4 MMAs of 128 x N x 8 in the stacked form, N <= 64,
     # else 6).  Update kernel: fields read + written and X5 read once, over
     # its CUDA-event time, against the measured HBM copy bandwidth.
-    # traffic: DRAM bytes (read + write) per analysis from one ncu capture of
-    # each kernel on workload 2 at half edge length, scaled to the launch.
+    # traffic: DRAM bytes (read + write) per analysis from an ncu capture of
+    # the kernel (TRAFFIC_PER_ANALYSIS), scaled to the launch's analyses.
     peaks, peak_src = load_peaks()
     calc_t = statistics.median(calc_ms) / 1e3
     upd_t = statistics.median(upd_ms) / 1e3
@@ -338,8 +343,9 @@ def run_gpu(args, rank, world, local_rank):
     roof["kernel_ms"] = kern_t * 1e3
     roof["solve_kernels_ms"] = statistics.median(fin_ms)
     roof["flops_per_launch"] = flops
-    upa = TRAFFIC_PER_ANALYSIS.get((w.cfg, "k_update_cells")) if m <= 64 else None
-    uroof = {"kernel": "k_update_cells" if m <= 64 else "k_update_v2", "bound": "hbm",
+    ukname = "k_update_cells" if m <= 64 else "k_update_v3"
+    upa = TRAFFIC_PER_ANALYSIS.get((w.cfg, ukname))
+    uroof = {"kernel": ukname, "bound": "hbm",
              "traffic": upa * w.nanalyses if upa else None,
              "achieved": ub / ukern_t / 1e9, "peak": peaks["hbm_gbs"], "unit": "GB/s",
              "frac": ub / ukern_t / 1e9 / peaks["hbm_gbs"], "bytes_per_launch": ub, "kernel_ms": ukern_t * 1e3,
