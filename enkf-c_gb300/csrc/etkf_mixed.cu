@@ -33,7 +33,6 @@
 #include "calc_common.cuh"
 
 #define EM_QL_T 32
-#define EM_REPLAY_NT 128
 #define EM_NT 256
 #define EM_KCH 16      // rows of the global operand staged per step
 
@@ -359,7 +358,9 @@ __global__ void __launch_bounds__(EM_QL_T) k_em_ql(int nslots, int m, const doub
 // ---------------------------------------------------------------------------
 #define EM_RCH 1024
 
-__global__ void __launch_bounds__(EM_REPLAY_NT) k_em_replay(CalcArgs a, EmSlots z)
+// NT = m rounded up to 32: a thread per row of Q and no idle warp
+template <int NT>
+__global__ void __launch_bounds__(NT) k_em_replay(CalcArgs a, EmSlots z)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int m = a.m, lda = m + 1;
@@ -373,14 +374,14 @@ __global__ void __launch_bounds__(EM_REPLAY_NT) k_em_replay(CalcArgs a, EmSlots 
     int* ctl = (int*)(sn + m);
     if (!(a.eaux[2 * (size_t)slot] > 0.0)) return;
     const size_t q0 = (size_t)slot * m * m;
-    for (int i = tid; i < m * m; i += EM_REPLAY_NT) {
+    for (int i = tid; i < m * m; i += NT) {
         const int r = i / m, c = i - r * m;
         A[r * lda + c] = z.q[q0 + i];
         // the lower triangle of M's float pairs, for the residual's rows
         if (c < r) z.mhl[q0 + i] = z.mhl[q0 + (size_t)c * m + r];
     }
     const int stt = z.nh[slot];
-    for (int i = tid; i < m; i += EM_REPLAY_NT) {
+    for (int i = tid; i < m; i += NT) {
         d[i] = z.d[(size_t)slot * m + i];
         e[i] = z.e[(size_t)slot * m + i];
     }
@@ -395,7 +396,7 @@ __global__ void __launch_bounds__(EM_REPLAY_NT) k_em_replay(CalcArgs a, EmSlots 
         float carry = 0.0f;
         for (int c0 = 0; h < stt; c0 += EM_RCH) {
             __syncthreads();
-            for (int q = tid; q < EM_RCH && c0 + q < z.rcap; q += EM_REPLAY_NT) rbuf[q] = rot[c0 + q];
+            for (int q = tid; q < EM_RCH && c0 + q < z.rcap; q += NT) rbuf[q] = rot[c0 + q];
             __syncthreads();
             while (h < stt) {
                 const int2 hd = hdr[h];
@@ -408,14 +409,22 @@ __global__ void __launch_bounds__(EM_REPLAY_NT) k_em_replay(CalcArgs a, EmSlots 
                     if (tid < m) carry = Ak[i + 1];
                     inside = true;
                 }
-                for (; i >= hd.y && r < c0 + EM_RCH; --i, ++r) {
-                    const float2 q = rbuf[r - c0];
-                    if (tid < m) {
-                        const float zi = Ak[i];
-                        Ak[i + 1] = q.y * zi + q.x * carry;
+                // the rotations of this sweep that are in the chunk (i runs
+                // down to hd.y), with the bounds taken out of the loop
+                const int nit = (i - hd.y + 1 < c0 + EM_RCH - r) ? i - hd.y + 1 : c0 + EM_RCH - r;
+                if (tid < m) {
+                    const float2* qp = rbuf + (r - c0);
+                    float* ap = Ak + i;
+#pragma unroll 4
+                    for (int t = 0; t < nit; ++t) {
+                        const float2 q = qp[t];
+                        const float zi = ap[-t];
+                        ap[1 - t] = q.y * zi + q.x * carry;
                         carry = q.x * zi - q.y * carry;
                     }
                 }
+                i -= nit;
+                r += nit;
                 if (i >= hd.y) break;    // the chunk is used up inside the sweep
                 if (tid < m) Ak[hd.y] = carry;
                 inside = false;
@@ -424,18 +433,18 @@ __global__ void __launch_bounds__(EM_REPLAY_NT) k_em_replay(CalcArgs a, EmSlots 
         }
         __syncthreads();
     } else {
-        rc = la::tql2<EM_REPLAY_NT>(A, m, lda, d, e, cs, sn, ctl);
+        rc = la::tql2<NT>(A, m, lda, d, e, cs, sn, ctl);
     }
     if (rc != 0 && tid == 0) {
         const int pt = a.order ? a.order[slot] : a.item0 + slot;
         a.status[pt] = rc;
     }
-    for (int i = tid; i < m * m; i += EM_REPLAY_NT) {
+    for (int i = tid; i < m * m; i += NT) {
         const int r = i / m, c = i - r * m;
         z.q[q0 + i] = A[r * lda + c];
     }
     if (stt < 0)
-        for (int i = tid; i < m; i += EM_REPLAY_NT) z.d[(size_t)slot * m + i] = d[i];
+        for (int i = tid; i < m; i += NT) z.d[(size_t)slot * m + i] = d[i];
 }
 
 // ---------------------------------------------------------------------------
@@ -772,7 +781,12 @@ enkfg_status run_etkf_mixed(enkfg_ctx* ctx, const CalcArgs& a0, cudaStream_t st)
     const size_t qsmem = (size_t)2 * m * EM_QL_T * 4;
     const size_t rsmem = (size_t)EM_RCH * 8 + ((size_t)m * lda + 4 * (size_t)m) * 4 + 16;
     CK(cudaFuncSetAttribute(k_em_ql, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)qsmem));
-    CK(cudaFuncSetAttribute(k_em_replay, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rsmem));
+    const int rnt = (m + 31) / 32 * 32;   // k_em_replay: a thread per row
+    switch (rnt) {
+    case 32: CK(cudaFuncSetAttribute(k_em_replay<32>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rsmem)); break;
+    case 64: CK(cudaFuncSetAttribute(k_em_replay<64>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rsmem)); break;
+    default: CK(cudaFuncSetAttribute(k_em_replay<96>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rsmem)); break;
+    }
     for (int i0 = 0; i0 < nitems; i0 += (int)B) {
         const int nb = (nitems - i0 < (int)B) ? nitems - i0 : (int)B;
         CalcArgs b = a0;
@@ -801,7 +815,11 @@ enkfg_status run_etkf_mixed(enkfg_ctx* ctx, const CalcArgs& a0, cudaStream_t st)
         CKL();
         k_em_ql<<<div_up(nb, EM_QL_T), EM_QL_T, qsmem, st>>>(nb, m, ctx->d_eaux, z);
         CKL();
-        k_em_replay<<<nb, EM_REPLAY_NT, rsmem, st>>>(b, z);
+        switch (rnt) {
+        case 32: k_em_replay<32><<<nb, 32, rsmem, st>>>(b, z); break;
+        case 64: k_em_replay<64><<<nb, 64, rsmem, st>>>(b, z); break;
+        default: k_em_replay<96><<<nb, 96, rsmem, st>>>(b, z); break;
+        }
         CKL();
         switch (R) {
         case 2: s = em_launch_refine<2>(ctx, b, z, nb, st); break;
