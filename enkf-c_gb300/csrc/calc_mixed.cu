@@ -424,10 +424,21 @@ struct GramProcTC {
         const uint32_t dhh = ms.taddr + (uint32_t)(2 * win * ms.N), dr = dhh + (uint32_t)ms.N;
         // a group of 8 observations is two 128-byte core matrices further
         // on: 256 bytes, 16 in the descriptor's address field (addresses
-        // below 256 KB do not carry out of the field)
-        uint64_t dh = tc::desc_kmajor_noswizzle(tc::smem_u32(tH), 128u, sbo);
-        uint64_t dm = tc::desc_kmajor_noswizzle(tc::smem_u32(tM), 128u, sbo);
-        uint64_t dl = tc::desc_kmajor_noswizzle(tc::smem_u32(tL), 128u, sbo);
+        // below 256 KB do not carry out of the field); DF: 64-byte swizzled
+        // rows of 16 observations, a group of 8 is 32 bytes (2) along the row
+        uint64_t dh, dm, dl;
+        uint32_t kstep;
+        if constexpr (DF) {
+            dh = tc::desc_kmajor_sw64(tc::smem_u32(tH), 512u);
+            dm = tc::desc_kmajor_sw64(tc::smem_u32(tM), 512u);
+            dl = tc::desc_kmajor_sw64(tc::smem_u32(tL), 512u);
+            kstep = 2u;
+        } else {
+            dh = tc::desc_kmajor_noswizzle(tc::smem_u32(tH), 128u, sbo);
+            dm = tc::desc_kmajor_noswizzle(tc::smem_u32(tM), 128u, sbo);
+            dl = tc::desc_kmajor_noswizzle(tc::smem_u32(tL), 128u, sbo);
+            kstep = 16u;
+        }
         const uint32_t lead = tc::elect_lane();
         if constexpr (ST) {
             // A = [lo; Z] (buffer 0) or [Z; lo] (buffer 1) for lo*hi'
@@ -440,7 +451,7 @@ struct GramProcTC {
                 tc::mma_tf32_lead(dr, dz, dh, idesc, 1u, lead);       // lo hi'
             }
         } else {
-            for (int g = 0; g < ngroups; ++g, dh += 16u, dm += 16u, dl += 16u) {
+            for (int g = 0; g < ngroups; ++g, dh += kstep, dm += kstep, dl += kstep) {
                 const uint32_t fresh = (win_obs == 0 && g == 0) ? 0u : 1u;
                 tc::mma_tf32_lead(dhh, dh, dh, idesc, fresh, lead);
                 tc::mma_tf32_lead(dr, dh, dm, idesc, fresh, lead);
@@ -543,7 +554,9 @@ struct GramProcTC {
                         vh[sl] = sm;
                     }
                 }
-                const int off = ((((r >> 3) * nkg + kg) << 5)) + ((r & 7) << 2);
+                // DF: 64-byte rows (kc = 16), chunk kg at kg ^ ((r >> 1) & 3)
+                const int off = DF ? (((r >> 3) << 7) + ((r & 7) << 4) + ((kg ^ ((r >> 1) & 3)) << 2))
+                                   : ((((r >> 3) * nkg + kg) << 5)) + ((r & 7) << 2);
                 *reinterpret_cast<float4*>(tH + off) = make_float4(h[0], h[1], h[2], h[3]);
                 *reinterpret_cast<float4*>(tM + off) = make_float4(md[0], md[1], md[2], md[3]);
                 *reinterpret_cast<float4*>(tL + off) = make_float4(lo[0], lo[1], lo[2], lo[3]);
@@ -900,6 +913,7 @@ static size_t mixed_smem_bytes(int m, int kc, int lseg, int st, int df)
     int lda = (m % 2 == 0) ? m + 1 : m + 2;
     size_t s = 0;
     s += mixed_tile_floats(m, kc, st) * 4;                 // operand tiles + padding
+    if (df) s += 1024;                                     // the swizzled tiles on a 1 KB boundary
     if (st) s += (size_t)m * lda * 4;                      // Mrest
     s += (size_t)2 * kc * mixed_ldv(m) * 4;                // raw S rows, two buffers
     s += (size_t)2 * kc * 4;                               // raw innovations, two buffers
@@ -924,7 +938,8 @@ __global__ void __launch_bounds__(CALC_NT, 2) k_transforms_mixed(CalcArgs a, int
     const int tid = threadIdx.x, wid = tid >> 5;
     const int m = a.m, lda = (m % 2 == 0) ? m + 1 : m + 2;   // odd stride: fewer bank conflicts
     const size_t ntile = mixed_tile_floats(m, kcm, ST);     // operand pieces + padding for A's rows
-    unsigned char* sp = smem_raw;
+    // DF: the swizzled tiles start on a 1 KB boundary of the shared window
+    unsigned char* sp = smem_raw + (DF ? (1024u - (tc::smem_u32(smem_raw) & 1023u)) & 1023u : 0u);
     float* tiles = (float*)sp;        sp += ntile * 4;
     const int ldv = mixed_ldv(m);
     float* raw0 = (float*)sp;         sp += (size_t)2 * kcm * ldv * 4;   // two buffers
@@ -1001,7 +1016,7 @@ __global__ void __launch_bounds__(CALC_NT, 2) k_transforms_mixed(CalcArgs a, int
         // observations per round: 8, 16 or 32 (a power of two), per count
         // bin when tuned
         ms.kc = kcm;
-        if (a.kc_table != nullptr && a.counts != nullptr) {
+        if (!DF && a.kc_table != nullptr && a.counts != nullptr) {   // DF: the swizzled rows are 16 wide
             const int k = a.kc_table[count_bin(a.counts[pt])];
             ms.kc = k >= kcm ? kcm : k >= 16 ? 16 : 8;
         }

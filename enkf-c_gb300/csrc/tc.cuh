@@ -29,6 +29,21 @@ __device__ __forceinline__ uint64_t desc_kmajor_noswizzle(uint32_t saddr, uint32
     return d;
 }
 
+// K-major operand with 64-byte swizzling: rows of 64 bytes (16 TF32 of K),
+// eight-row groups of 512 bytes sbo apart, the 16-byte chunk c of row r
+// stored at chunk c ^ ((r >> 1) & 3) (the tile based on a 512-byte
+// boundary); the leading byte offset is unused for this layout (1)
+__device__ __forceinline__ uint64_t desc_kmajor_sw64(uint32_t saddr, uint32_t sbo)
+{
+    uint64_t d = 0;
+    d |= (uint64_t)((saddr >> 4) & 0x3FFFu);
+    d |= (uint64_t)1 << 16;
+    d |= (uint64_t)((sbo >> 4) & 0x3FFFu) << 32;
+    d |= (uint64_t)1 << 46;     // descriptor version for tcgen05
+    d |= (uint64_t)4 << 61;     // swizzling mode: 64 bytes
+    return d;
+}
+
 // instruction descriptor: kind::tf32, D = F32, A = B = TF32, K-major, M x N
 __host__ __device__ __forceinline__ uint32_t idesc_tf32(int M, int N)
 {
