@@ -29,12 +29,20 @@
 //
 // The double-float S'S is then converted to FP64 and goes through the same
 // FP64 solve as the plain path (Householder + QL for ETKF, the symmetric
-// sweep inverse for DEnKF/EnOI).
+// sweep inverse for DEnKF/EnOI), or, deferred, is handed to the batched
+// solves through a slot in global memory.
+//
+// The compact deferred form (DF, 64 < m <= 96) differs so that two CTAs fit
+// on an SM: rounds of 16 observations; one TMEM accumulator set, a window
+// drained at the end of the round that closes it; the S'S upper triangle in
+// rectangular packing; each round's MMAs issued at the start of the next
+// round, while that round is split; S's fused into the split (split_vec).
 //
 // Shared-memory operand layout (canonical K-major, no swizzle): core matrices
 // of 8 rows x 16 bytes (4 TF32) stored as 128 contiguous bytes; core matrix
 // (row group g, K group q) at (g * kc/4 + q) * 128 bytes.  Descriptor:
-// leading (K) byte offset 128, stride (row-group) byte offset kc*32.
+// leading (K) byte offset 128, stride (row-group) byte offset kc*32.  DF:
+// 64-byte swizzled rows of the round's 16 observations (tc.cuh).
 //
 // Every wait on an MMA mbarrier is bounded; on expiry the CTA records an
 // error status for the point, stops, releases its TMEM and returns.
@@ -484,7 +492,7 @@ struct GramProcTC {
         const int buf = (int)(rnd & 1u);
         if (pend) issue_pending();
         if (sy.outstanding(buf)) wait_buf(buf, false);
-        split_vec<true>(buf, rb, lcf, base, nc);
+        split_vec(buf, rb, lcf, base, nc);
         ++rnd;
         pend = true;
         pend_buf = buf;
@@ -507,9 +515,8 @@ struct GramProcTC {
     // raw reads are consecutive members of one observation.  Rows >= m are
     // not written (they only reach accumulator rows and columns that are
     // never read); observations past nc have zero rows and zero taper.
-    // With SS, each pair's products with the observations' tapered
-    // innovations go into the pair's double-float S's sum (vh, vl).
-    template <bool SS>
+    // Each pair's products with the observations' tapered innovations go
+    // into the pair's double-float S's sum (vh, vl).
     __device__ __forceinline__ void split_vec(int buf, int rb, const float* lcf, int base, int nc)
     {
         const int m = a.m, nkg = ms.kc >> 2, rows = ((m + 7) >> 3) << 3;
@@ -545,7 +552,7 @@ struct GramProcTC {
                     const float r1 = __fsub_rn(vv, h[j]);
                     md[j] = tc::tf32_rna(r1);
                     lo[j] = tc::tf32_rna(__fsub_rn(r1, md[j]));
-                    if constexpr (SS) {
+                    {
                         // TwoProd and TwoSum into the pair's sum
                         const float x = __fmul_rn(sr[k0 + j], c[j]);
                         const float pp = vv * x, pe = fmaf(vv, x, -pp);
@@ -608,7 +615,7 @@ struct GramProcTC {
             const float* rp = raw + k * ms.ldv + (lane >> 2);
             if (tsum) ssq = split_rows<true>(tH, tM, tL, rp, ck, xk, nrg, nkg, kg, rg0, rstep, lane);
             else if (FS) split_rows<false>(tH, tM, tL, rp, ck, xk, nrg, nkg, kg, rg0, rstep, lane);
-            else split_vec<true>(buf, rb, lcf, base, nc);
+            else split_vec(buf, rb, lcf, base, nc);
         }
         tc::fence_async_smem();
         __syncthreads();
