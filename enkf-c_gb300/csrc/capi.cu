@@ -79,6 +79,13 @@ ENKFG_API enkfg_status enkfg_set_field_buffer_size(enkfg_ctx* ctx, int nfield)
     return ENKFG_OK;
 }
 
+ENKFG_API enkfg_status enkfg_set_field_block_rows(enkfg_ctx* ctx, int rows)
+{
+    if (!ctx || rows < 0) return ENKFG_EINVAL;
+    ctx->field_rows = rows;
+    return ENKFG_OK;
+}
+
 ENKFG_API enkfg_status enkfg_set_wait_drill(enkfg_ctx* ctx, int on)
 {
     if (!ctx) return ENKFG_EINVAL;
@@ -818,6 +825,7 @@ ENKFG_API enkfg_status enkfg_update_fields(enkfg_ctx* ctx, const enkfg_update_pa
     // rows per unit
     const int stp = ctx->stride > 0 ? ctx->stride : 1;
     int R = (int)(UPD_UNIT_BYTES / ((size_t)G * mp * mni * sizeof(float)));
+    if (ctx->field_rows > 0) R = (ctx->field_rows + stp - 1) / stp * stp;
     R -= R % stp;
     if (R < stp) R = stp;
     if (R > jsize) R = jsize;

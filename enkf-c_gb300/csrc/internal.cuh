@@ -53,6 +53,7 @@ struct enkfg_ctx {
     cudaStream_t cstream[2];    // host-buffer update: copies in, copies out (created on first use)
     cudaEvent_t uev[9];         // host-buffer update: per buffer, copy-in / update / copy-out done
     int field_buffer;           // host-buffer update: field-layers per group (0: automatic)
+    int field_rows;             // host-buffer update: model rows per block (0: automatic)
     char err[1024];
     long long launches;
     unsigned long long wait_ns; // bound on a device wait (enkfg_set_wait_limit)

@@ -256,6 +256,12 @@ ENKFG_API enkfg_status enkfg_update_fields(enkfg_ctx* ctx, const enkfg_update_pa
  * common/enkfprm.c:381-388); 0 (the default) picks groups of about 3 GB. */
 ENKFG_API enkfg_status enkfg_set_field_buffer_size(enkfg_ctx* ctx, int nfield);
 
+/* Model rows per block of the host-buffer update, rounded up to a multiple
+ * of the stride; 0 (the default) picks blocks of about 512 MB.  No
+ * counterpart in the reference (it reads whole fields); the result does
+ * not depend on it. */
+ENKFG_API enkfg_status enkfg_set_field_block_rows(enkfg_ctx* ctx, int rows);
+
 /* Device-resident form: fields/infl are device addresses. */
 ENKFG_API enkfg_status enkfg_update_fields_dev(enkfg_ctx* ctx, const enkfg_update_params* p, const int* numlevels_dev, int nfield, const int* levels, float* fields_dev, float* infl_dev, void* stream);
 

@@ -197,8 +197,9 @@ def test_update_against_reference_golden(ctx, precision):
 
 def test_update_streamed_groups_match_one_group(ctx):
     """The host-buffer update in groups of 1 and 3 field-layers (three device
-    buffers in turn, copies overlapped on the copy streams) gives the same
-    fields as one group, and as the oracle (m = 96 and m = 24 kernels)."""
+    buffers in turn, copies overlapped on the copy streams), and in blocks of
+    model rows, gives the same fields (and inflation) as one group, and as
+    the oracle (m = 96 and m = 24 kernels)."""
     for nmem in (96, 24):
         w = synth.make(3, scale=0.06, nobs=3000, nmem=nmem)
         w.nlayers = 10
@@ -212,6 +213,20 @@ def test_update_streamed_groups_match_one_group(ctx):
             got = ctx.updatefields(fl, w.numlevels, levels, inflation=1.03, inf_ratio=0.4)
             assert np.array_equal(got, whole), (nmem, g)
         ctx.set_field_buffer_size(0)
+        # blocks of model rows (a multiple of the stride, the last one
+        # shorter), with the inflation output
+        whole_f, whole_i = ctx.updatefields(fl, w.numlevels, levels, inflation=1.03, inf_ratio=0.4, want_infl=True)
+        for g, rows in ((1, 1), (3, 5), (20, 7)):
+            ctx.set_field_buffer_size(g)
+            ctx.set_field_block_rows(rows)
+            try:
+                got_f, got_i = ctx.updatefields(fl, w.numlevels, levels, inflation=1.03, inf_ratio=0.4,
+                                                want_infl=True)
+            finally:
+                ctx.set_field_buffer_size(0)
+                ctx.set_field_block_rows(0)
+            assert np.array_equal(got_f, whole_f), (nmem, g, rows)
+            assert np.array_equal(got_i, whole_i), (nmem, g, rows)
         ref = np.stack([oracle.updatefields(fl[f], out["T"], out["w"], w.numlevels, mode=0, nmem=w.nmem,
                                             nmem_dynamic=w.nmem_dynamic, stride=w.stride, level=int(levels[f]),
                                             inflation=1.03, inf_ratio=0.4) for f in range(fl.shape[0])])
