@@ -540,9 +540,9 @@ void batch_mark(enkfg_ctx* ctx, int k, cudaStream_t st)
     cudaEventRecord(ctx->bev[idx], st);
 }
 
-size_t batch_points(size_t per_slot, size_t budget, int nitems)
+size_t batch_points(const enkfg_ctx* ctx, size_t per_slot, size_t budget, int nitems)
 {
-    size_t B = budget / per_slot;
+    size_t B = ctx->solve_batch > 0 ? (size_t)ctx->solve_batch : budget / per_slot;
     if (B < 256) B = 256;
     if (B >= 1024) B -= B % 1024;
     if (B > (size_t)nitems) B = (size_t)nitems;
@@ -582,7 +582,7 @@ static enkfg_status run_inv_batched(enkfg_ctx* ctx, const CalcArgs& a0, int prec
 {
     enkfg_status s;
     const int m = a0.m, nitems = a0.nitems;
-    const size_t B = batch_points(inv_slot_bytes(m), (size_t)2 << 30, nitems);   // about 2 GB a batch
+    const size_t B = batch_points(ctx, inv_slot_bytes(m), (size_t)2 << 30, nitems);   // about 2 GB a batch
     if ((s = ensure(ctx, &ctx->d_eq, &ctx->eq_cap, B * m * m))) return s;
     if ((s = ensure(ctx, &ctx->d_eb, &ctx->eb_cap, B * m))) return s;
     if ((s = ensure(ctx, &ctx->d_eaux, &ctx->eaux_cap, B * 2))) return s;
@@ -662,7 +662,7 @@ static enkfg_status run_etkf_batched(enkfg_ctx* ctx, const CalcArgs& a0, int pre
     const int m = a0.m, nitems = a0.nitems;
     const int rcap = m * m + 64 * m;         // QL typically needs about 0.75 m^2 rotations
     const int hcap = 8 * m;
-    const size_t B = batch_points(etkf_slot_bytes(m), (size_t)2 << 30, nitems);   // about 2 GB a batch
+    const size_t B = batch_points(ctx, etkf_slot_bytes(m), (size_t)2 << 30, nitems);   // about 2 GB a batch
     if ((s = ensure(ctx, &ctx->d_eq, &ctx->eq_cap, B * m * m))) return s;
     if ((s = ensure(ctx, &ctx->d_ed, &ctx->ed_cap, B * m))) return s;
     if ((s = ensure(ctx, &ctx->d_ee, &ctx->ee_cap, B * m))) return s;
@@ -808,11 +808,11 @@ enkfg_status run_transforms(enkfg_ctx* ctx, const enkfg_calc_params* p, cudaStre
             if (defer_) {
                 size_t B;
                 if (etkf_ && p->precision == ENKFG_PREC_MIXED && etkf_mixed_supported(m))
-                    B = batch_points(etkf_mixed_slot_bytes(m), (size_t)8 << 30, npts);
+                    B = batch_points(ctx, etkf_mixed_slot_bytes(m), (size_t)8 << 30, npts);
                 else if (etkf_)
-                    B = batch_points(etkf_slot_bytes(m), (size_t)2 << 30, npts);
+                    B = batch_points(ctx, etkf_slot_bytes(m), (size_t)2 << 30, npts);
                 else
-                    B = batch_points(inv_slot_bytes(m), (size_t)2 << 30, npts);
+                    B = batch_points(ctx, inv_slot_bytes(m), (size_t)2 << 30, npts);
                 if (B % QS_T == 0 && B < (size_t)npts) seg = (int)B;
                 else if (B >= (size_t)npts) seg = npts;   // one batch
             }

@@ -153,7 +153,7 @@ struct GramProcTC {
     const PointScratch& s;
     MixedShared& ms;
     MixedSync& sy;
-    uint32_t& rnd;     // rounds issued by this CTA (all points): operand buffer = rnd & 1
+    uint32_t& rnd;     // rounds of this point so far: operand buffer = rnd & 1
     int win;           // current window's accumulator set
     int win_obs;       // observations in the current window
     int drain_set;     // closed window awaiting its drain (-1: none)
@@ -1045,6 +1045,12 @@ __global__ void __launch_bounds__(CALC_NT, 2) k_transforms_mixed(CalcArgs a, int
         if (ST)
             for (int i = tid; i < ms.piece; i += CALC_NT) ms.zblock()[i] = 0.0f;
         __syncthreads();
+        // every point starts on operand buffer 0 (the previous point's MMAs
+        // are all complete: finish() waited for both buffers), so that which
+        // buffer a round uses -- and, in the stacked form, which accumulator
+        // rows take lo*hi' -- does not depend on the points the CTA did
+        // before, and the result of a point does not depend on the queue
+        rnd = 0;
         GramProcTC<HB, FS, ST, DF> proc(a, s, ms, sy, rnd);
         const int p = (a.sxf != nullptr && a.ndim == 2)
                           ? enumerate_obs_seg<2>(a, lseg, qx, qy, qz, slid, slcf, ictl + 8, nb0, ncum, tcount, proc)

@@ -79,6 +79,13 @@ ENKFG_API enkfg_status enkfg_set_field_buffer_size(enkfg_ctx* ctx, int nfield)
     return ENKFG_OK;
 }
 
+ENKFG_API enkfg_status enkfg_set_solve_batch(enkfg_ctx* ctx, int points)
+{
+    if (!ctx || points < 0) return ENKFG_EINVAL;
+    ctx->solve_batch = points;
+    return ENKFG_OK;
+}
+
 ENKFG_API enkfg_status enkfg_set_field_block_rows(enkfg_ctx* ctx, int rows)
 {
     if (!ctx || rows < 0) return ENKFG_EINVAL;

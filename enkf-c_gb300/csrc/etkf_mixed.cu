@@ -749,7 +749,7 @@ enkfg_status run_etkf_mixed(enkfg_ctx* ctx, const CalcArgs& a0, cudaStream_t st)
     const int MP = 16 * R;
     const int rcap = m * m + 64 * m;         // QL typically needs about 0.75 m^2 rotations
     const int hcap = 8 * m;
-    const size_t B = batch_points(etkf_mixed_slot_bytes(m), (size_t)8 << 30, nitems);   // about 8 GB a batch
+    const size_t B = batch_points(ctx, etkf_mixed_slot_bytes(m), (size_t)8 << 30, nitems);   // about 8 GB a batch
     if ((s = ensure(ctx, &ctx->d_eq, &ctx->eq_cap, B * m * m))) return s;
     if ((s = ensure(ctx, &ctx->d_eb, &ctx->eb_cap, B * m))) return s;
     if ((s = ensure(ctx, &ctx->d_eaux, &ctx->eaux_cap, B * 2))) return s;

@@ -54,6 +54,7 @@ struct enkfg_ctx {
     cudaEvent_t uev[9];         // host-buffer update: per buffer, copy-in / update / copy-out done
     int field_buffer;           // host-buffer update: field-layers per group (0: automatic)
     int field_rows;             // host-buffer update: model rows per block (0: automatic)
+    int solve_batch;            // batched solves: points per batch (0: automatic)
     char err[1024];
     long long launches;
     unsigned long long wait_ns; // bound on a device wait (enkfg_set_wait_limit)
@@ -290,9 +291,10 @@ enkfg_status run_transforms(enkfg_ctx* ctx, const enkfg_calc_params* p, cudaStre
 // per-batch timing (calc.cu): k = 0 before a batch's transform kernel, 1
 // after it, 2 after the batch's solve kernels
 void batch_mark(enkfg_ctx* ctx, int k, cudaStream_t st);
-// points per batch of a batched solve: budget / per-slot bytes, at least
-// 256, a multiple of 1024 from 1024 on, at most nitems
-size_t batch_points(size_t per_slot, size_t budget, int nitems);
+// points per batch of a batched solve: budget / per-slot bytes (or the
+// context's setting, enkfg_set_solve_batch), at least 256, a multiple of
+// 1024 from 1024 on, at most nitems
+size_t batch_points(const enkfg_ctx* ctx, size_t per_slot, size_t budget, int nitems);
 size_t etkf_mixed_slot_bytes(int m);
 // after the last kernel of the batch of queue items [i0, i0 + nb): the
 // host outputs of those points (a contiguous range when the queue is

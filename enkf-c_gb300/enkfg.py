@@ -38,7 +38,7 @@ STATUS = {0: "OK", 1: "EINVAL", 2: "ECUDA", 3: "ENOMEM", 4: "ETIMEOUT", 5: "ENUM
           7: "ESTATE", 8: "EUNSUPPORTED"}
 
 # every symbol include/enkfg.h declares
-EXPORTS = ["enkfg_create", "enkfg_destroy", "enkfg_set_wait_limit", "enkfg_set_wait_drill", "enkfg_set_field_buffer_size", "enkfg_set_field_block_rows", "enkfg_last_error", "enkfg_status_string", "enkfg_version",
+EXPORTS = ["enkfg_create", "enkfg_destroy", "enkfg_set_wait_limit", "enkfg_set_wait_drill", "enkfg_set_field_buffer_size", "enkfg_set_field_block_rows", "enkfg_set_solve_batch", "enkfg_last_error", "enkfg_status_string", "enkfg_version",
            "enkfg_set_obstypes", "enkfg_set_obs", "enkfg_set_HE", "enkfg_calc_innovations", "enkfg_standardise",
            "enkfg_set_S", "enkfg_get_S", "enkfg_set_grid", "enkfg_transform_dims", "enkfg_local_obs",
            "enkfg_calc_transforms", "enkfg_calc_transforms_dev", "enkfg_transforms_dev_ptr",
@@ -156,6 +156,10 @@ class Enkfg:
     def set_field_buffer_size(self, nfield: int = 0):
         """Field-layers per group of the host-buffer update (0: about 3 GB)."""
         self._ck(self.L.enkfg_set_field_buffer_size(self.h, C.c_int(int(nfield))))
+
+    def set_solve_batch(self, points: int = 0):
+        """Local analyses per batch of the batched solves (0: automatic)."""
+        self._ck(self.L.enkfg_set_solve_batch(self.h, C.c_int(int(points))))
 
     def set_field_block_rows(self, rows: int = 0):
         """Model rows per block of the host-buffer update (0: about 512 MB)."""

@@ -256,6 +256,15 @@ ENKFG_API enkfg_status enkfg_update_fields(enkfg_ctx* ctx, const enkfg_update_pa
  * common/enkfprm.c:381-388); 0 (the default) picks groups of about 3 GB. */
 ENKFG_API enkfg_status enkfg_set_field_buffer_size(enkfg_ctx* ctx, int nfield);
 
+/* Local analyses per batch of the batched solves (the transform kernel
+ * hands each batch's points to the solve kernels through a scratch slot of
+ * each point; the host outputs of enkfg_calc_transforms leave batch by
+ * batch).  0 (the default) sizes batches by their scratch: about 8 GB for
+ * the refined ETKF solve, 2 GB for the FP64 ones.  Taken to at least 256
+ * and, from 1024 on, to a multiple of 1024.  No counterpart in the
+ * reference; the result does not depend on it. */
+ENKFG_API enkfg_status enkfg_set_solve_batch(enkfg_ctx* ctx, int points);
+
 /* Model rows per block of the host-buffer update, rounded up to a multiple
  * of the stride; 0 (the default) picks blocks of about 512 MB.  No
  * counterpart in the reference (it reads whole fields); the result does

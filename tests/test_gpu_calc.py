@@ -222,3 +222,32 @@ def test_errors_are_status_codes(ctx, gpu_lib):
         c2.calctransforms()
     assert e.value.status == 7
     c2.close()
+
+
+# (precision, mode, scheme, workload, members): the three batched solves --
+# the refined mixed ETKF solve, the FP64 eigensolver and the FP64 inverse
+SPLIT_CASES = [(1, 0, 1, 3, 96), (0, 0, 1, 3, 48), (0, 0, 0, 2, 48), (1, 0, 0, 2, 48)]
+
+
+@pytest.mark.parametrize("case", SPLIT_CASES, ids=["mixed_etkf_m96", "fp64_etkf_m48", "fp64_denkf_m48",
+                                                   "mixed_denkf_m48"])
+def test_transforms_in_several_solve_batches(ctx, case):
+    """The batched path in batches of 1,024 and 2,048 points (the queue is
+    then sorted within each batch, and the host outputs leave batch by
+    batch) gives the same T and w, bit for bit, as one batch."""
+    prec, mode, scheme, cfg, m = case
+    w = synth.make(cfg, scale=0.15 if cfg == 3 else 0.35, nmem=m, with_fields=False)
+    S, s = prepare(w)
+    _, tabs = obsset(w)
+    gpu_setup(ctx, w, S, s, tabs)
+    npts = w.nj_s * w.ni_s
+    assert npts > 4096
+    one = ctx.calctransforms(mode=mode, scheme=scheme, path=1, precision=prec, want_diag=False)
+    for b in (1024, 2048):
+        ctx.set_solve_batch(b)
+        try:
+            got = ctx.calctransforms(mode=mode, scheme=scheme, path=1, precision=prec, want_diag=False)
+        finally:
+            ctx.set_solve_batch(0)
+        assert np.array_equal(got["w"], one["w"]), (case, b)
+        assert np.array_equal(got["T"], one["T"]), (case, b)
