@@ -20,7 +20,7 @@
 //      D = Q D~ Q' (FP32: D is of the size of R);
 //   5. T = Z0 + D (summed in FP64), relaxed and cast as the reference does;
 //   6. w by iterative refinement: w += Q diag(1/lambda) Q' r with the
-//      residual r = S's - M w in FP64, three times.
+//      residual r = S's - M w in FP64, EM_W_STEPS times.
 //
 // The FP32 decomposition is backward stable with an error of order u32
 // lambda_max (about 1e-4 at lambda_max ~ 1e3), which is the error of Z0; one
@@ -35,6 +35,10 @@
 #define EM_QL_T 32
 #define EM_NT 256
 #define EM_KCH 16      // rows of the global operand staged per step
+// iterative-refinement steps of w: each multiplies the relative error by
+// about u32 lambda_max(M), so two leave about (6e-8 lambda_max)^2 -- below
+// 4e-7 up to lambda_max = 1e4, under the errors of the FP32 taper and S
+#define EM_W_STEPS 2
 
 // ---------------------------------------------------------------------------
 // per-slot scratch of the refined solve (float unless noted)
@@ -109,21 +113,35 @@ __device__ __forceinline__ void tred_publish(const float (&a)[R][R], int i, int 
     if ((i & 15) != ty) return;
     const int l = i - 1;
     float hp = 0.0f, f = 0.0f, aii = 0.0f;
+    // the row's register block (a branch on i / 16, not R predicated copies)
+    float rv[R];
+    switch (i >> 4) {
+#define EM_ROW_CASE(X)                                                          \
+    case X:                                                                     \
+        _Pragma("unroll") for (int c = 0; c < R; ++c) rv[c] = a[(X) < R ? (X) : 0][c]; \
+        break;
+        EM_ROW_CASE(0)
+        EM_ROW_CASE(1)
+        EM_ROW_CASE(2)
+        EM_ROW_CASE(3)
+        EM_ROW_CASE(4)
+        EM_ROW_CASE(5)
+#undef EM_ROW_CASE
+    default:
 #pragma unroll
-    for (int r = 0; r < R; ++r)
-        if (16 * r + ty == i) {
+        for (int c = 0; c < R; ++c) rv[c] = 0.0f;
+    }
 #pragma unroll
-            for (int c = 0; c < R; ++c) {
-                const int k = tx + 16 * c;
-                const float v = a[r][c];
-                if (k <= l) {
-                    W[i * LD + k] = v;
-                    hp = fmaf(v, v, hp);
-                }
-                if (k == l) f = v;
-                if (k == i) aii = v;
-            }
+    for (int c = 0; c < R; ++c) {
+        const int k = tx + 16 * c;
+        const float v = rv[c];
+        if (k <= l) {
+            W[i * LD + k] = v;
+            hp = fmaf(v, v, hp);
         }
+        if (k == l) f = v;
+        if (k == i) aii = v;
+    }
     const float h0 = hw_sum(hp);
     const int lsrc = (threadIdx.x & 16) | (l & 15);   // lane of this half-warp holding column l
     const int isrc = (threadIdx.x & 16) | (i & 15);
@@ -180,14 +198,8 @@ __device__ __forceinline__ void tred_step(float (&a)[R][R], int i, int l, float 
     // u / h into column i (tred2 keeps it for the accumulation)
     if (tid <= l) W[tid * LD + i] = W[i * LD + tid] * ih;
     __syncthreads();
-    float fr[16];
-#pragma unroll
-    for (int t = 0; t < 16; ++t) fr[t] = red[t];
-#pragma unroll
-    for (int w = 8; w >= 1; w >>= 1)
-#pragma unroll
-        for (int t = 0; t < w; ++t) fr[t] += fr[t + w];
-    const float hh = fr[0] / (h + h);
+    // f: the 16 half-warp partials, one a lane, summed across each half-warp
+    const float hh = hw_sum(red[tx]) / (h + h);
     float qk[NB];
 #pragma unroll
     for (int c = 0; c < NB; ++c) {
@@ -672,7 +684,7 @@ __global__ void __launch_bounds__(EM_NT, 2) k_em_refine(CalcArgs a, EmSlots z)
         rv[i] = bv[i];
     }
     __syncthreads();
-    for (int it = 0; it < 3; ++it) {
+    for (int it = 0; it < EM_W_STEPS; ++it) {
         if (tid < m) {
             float t = 0.0f;
             for (int k = 0; k < m; ++k) t = fmaf(Q[k * LDA + tid], (float)rv[k], t);
