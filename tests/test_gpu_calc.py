@@ -213,6 +213,38 @@ def test_empty_and_edge_points(ctx):
     assert per_point_rel(out["T64"], ref["T64"]) < 1e-10
 
 
+@pytest.mark.parametrize("mode,scheme,prec", [(0, 1, 0), (0, 0, 0), (0, 1, 1)])
+def test_transforms_at_point_logs(ctx, mode, scheme, prec):
+    """Transforms at point-log positions (the recipe of a 1 x n curvilinear
+    "grid" of log points, as das_calcpointlogtransforms needs them at
+    arbitrary positions), plain and batched paths: local counts bit-exact,
+    T and w against the oracle at the same positions.  One log point lies
+    outside the observed region (T = I, w = 0)."""
+    w = synth.make(1, scale=0.5, with_fields=False)
+    S, s = prepare(w)
+    obs, tabs = obsset(w)
+    rng = np.random.default_rng(11)
+    n = 37
+    px = rng.uniform(w.x.min(), w.x.max(), n)
+    py = rng.uniform(w.y.min(), w.y.max(), n)
+    px[5], py[5] = w.x.max() + 10 * w.locrad, w.y.max() + 10 * w.locrad
+    x2d, y2d = px[None, :], py[None, :]
+    ref = oracle.calctransforms(obs, mode=mode, scheme=scheme, nmem=w.nmem, nmem_dynamic=w.nmem, alpha=1.0,
+                                stride=1, x=px, y=py, S=S, s=s, want64=True, x2d=x2d, y2d=y2d)
+    gpu_setup(ctx, w, S, s, tabs)
+    ctx.set_grid(x2d=x2d, y2d=y2d, stride=1)
+    assert (ctx.nj, ctx.ni) == (1, n)
+    assert ref["nlobs"][0, 5] == 0 and (ref["nlobs"] > 0).sum() == n - 1
+    tol = 1e-10 if prec == 0 else 1e-5     # the FP64 and the mixed-precision contracts
+    for path in ((0, 1) if prec == 0 else (1,)):
+        out = ctx.calctransforms(mode=mode, scheme=scheme, alpha=1.0, path=path, precision=prec, want64=True)
+        assert np.array_equal(out["nlobs"], ref["nlobs"])
+        assert per_point_rel(out["T64"], ref["T64"]) < tol, path
+        assert per_point_rel(out["w64"], ref["w64"]) < tol, path
+        assert np.array_equal(out["T"][0, 5], np.eye(w.nmem, dtype=np.float32))
+        assert np.all(out["w"][0, 5] == 0)
+
+
 def test_errors_are_status_codes(ctx, gpu_lib):
     with pytest.raises(gpu_lib.EnkfgError) as e:
         ctx.set_obstypes(np.array([0], np.int32), np.zeros(8))
