@@ -231,7 +231,7 @@ __global__ void __launch_bounds__(CALC_NT) k_adjoint(AdjArgs A)
     }
     // 1. forward recomputation: M, b, eigendecomposition, w
     GramProcAdj<R, F> gp(a, s, tile, sloc);
-    const int p = enumerate_obs<0>(a, a.kc, qx, qy, qz, s, gp, true);
+    const int p = enumerate_obs<0>(a, pt, a.kc, qx, qy, qz, s, gp, true);
     if (p == 0) return;
     if (tx >= ty)
 #pragma unroll
@@ -366,7 +366,7 @@ __global__ void __launch_bounds__(CALC_NT) k_adjoint(AdjArgs A)
     // 3. per-observation sensitivities (second pass over the local obs; the
     //    chunks are staged in the tile region, P stays in W)
     AdjProc<F> ap(A, s, tile, lam, w, Pp, LDA, MP, qx, qy, qz);
-    enumerate_obs<0>(a, a.kc, qx, qy, qz, s, ap, false);
+    enumerate_obs<0>(a, pt, a.kc, qx, qy, qz, s, ap, false);
     double rs = la::block_sum<CALC_NT>(ap.rho_acc, red);
     if (tid == 0 && rs != 0.0) atomicAdd(A.drho, rs);
 }
@@ -457,7 +457,7 @@ enkfg_status run_adjoint(enkfg_ctx* ctx, const enkfg_calc_params* p, const doubl
         set_err(ctx, "the adjoint supports nmem <= 96 (got %d)", m);
         return ENKFG_EUNSUPPORTED;
     }
-    if (!ctx->index_valid && (s = build_index(ctx, st))) return s;
+    if ((s = prepare_search(ctx, st))) return s;
     if (!ctx->gather_valid && (s = build_gather(ctx, st))) return s;
     const int npts = ctx->nj * ctx->ni;
     if ((s = ensure(ctx, &ctx->d_status_pt, &ctx->status_cap, (size_t)npts))) return s;
@@ -495,6 +495,8 @@ enkfg_status run_adjoint(enkfg_ctx* ctx, const enkfg_calc_params* p, const doubl
     a.qx = ctx->d_qx;
     a.qy = ctx->d_qy;
     a.qz = ctx->d_qz;
+    a.sid = ctx->d_sid;
+    a.cut = any_nlobsmax(ctx) ? ctx->d_cut : nullptr;
     a.status = ctx->d_status_pt;
     A.wbar = d_wbar;
     A.Tbar = d_Tbar;

@@ -153,7 +153,7 @@ __global__ void __launch_bounds__(CALC_NT) k_transforms(CalcArgs a)
         }
         __syncthreads();
         GramProc64<R> proc(a, s, tile, sloc);
-        const int p = enumerate_obs<0>(a, kc, qx, qy, qz, s, proc, true);
+        const int p = enumerate_obs<0>(a, pt, kc, qx, qy, qz, s, proc, true);
         if (p == 0) {
             store_empty(a, pt);
             if (a.defer && tid == 0) a.eaux[2 * (size_t)idx] = 0.0;
@@ -730,7 +730,7 @@ enkfg_status run_transforms(enkfg_ctx* ctx, const enkfg_calc_params* p, cudaStre
         return ENKFG_EUNSUPPORTED;
     }
     cudaEventRecord(ctx->ev[0], st);
-    if (!ctx->index_valid && (s = build_index(ctx, st))) return s;
+    if ((s = prepare_search(ctx, st))) return s;
     if (!ctx->gather_valid && (s = build_gather(ctx, st))) return s;
     cudaEventRecord(ctx->ev[1], st);
 
@@ -783,6 +783,8 @@ enkfg_status run_transforms(enkfg_ctx* ctx, const enkfg_calc_params* p, cudaStre
     a.qx = ctx->d_qx;
     a.qy = ctx->d_qy;
     a.qz = ctx->d_qz;
+    a.sid = ctx->d_sid;
+    a.cut = any_nlobsmax(ctx) ? ctx->d_cut : nullptr;
     a.T = enkf ? ctx->d_T : nullptr;
     a.w = ctx->d_w;
     a.T64 = (enkf && w64) ? ctx->d_T64 : nullptr;

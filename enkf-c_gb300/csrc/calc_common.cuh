@@ -34,6 +34,8 @@ struct CalcArgs {
     const double* qx;
     const double* qy;
     const double* qz;
+    const int* sid;        // observation id at each sorted position
+    const CutKey* cut;     // [ntypes][npts] NLOBSMAX cuts (null: no type has a limit)
     const int* order;
     int* qhead;
     const int* counts;
@@ -140,12 +142,28 @@ static __device__ __noinline__ bool exact_in2(double ox, double oy, double qx, d
     return exact::dist2(ox, oy, qx, qy) <= r2;
 }
 
+// The NLOBSMAX cut of a candidate the FP32 pre-test accepted: its exact FP64
+// squared distance against the point's cut key *ck (not inlined, as
+// exact_in2; the key is loaded here, so that the search loop keeps nothing
+// of it live).
+static __device__ __noinline__ bool exact_cut2(double ox, double oy, double qx, double qy, int id,
+                                               const CutKey* ck)
+{
+    return cut_keeps(exact::dist2(ox, oy, qx, qy), id, *ck);
+}
+
+// The same for a candidate whose exact squared distance d2 is at hand.
+static __device__ __noinline__ bool keeps_cut(double d2, int id, const CutKey* ck)
+{
+    return cut_keeps(d2, id, *ck);
+}
+
 // SEARCH: 0 exact FP64 distance and FP64 taper (bit-exact coefficients);
 // 1 FP64 distance, FP32 taper; 2 FP32 distance with the exact FP64 test only
 // inside the undecided band, FP32 taper from the double-float distance (2-D).
 template <int SEARCH, class Proc>
-__device__ int enumerate_obs(const CalcArgs& a, int kc, double qx, double qy, double qz, const PointScratch& s,
-                             Proc& proc, bool count_types)
+__device__ int enumerate_obs(const CalcArgs& a, int pt, int kc, double qx, double qy, double qz,
+                             const PointScratch& s, Proc& proc, bool count_types)
 {
     constexpr bool FAST = SEARCH > 0;
     float* llcf = reinterpret_cast<float*>(s.llc);
@@ -156,6 +174,7 @@ __device__ int enumerate_obs(const CalcArgs& a, int kc, double qx, double qy, do
         const TypeIndex& ti = a.types[t];
         int tcnt = 0;
         if (ti.pos_end > ti.pos_begin) {
+            const bool cut_on = a.cut != nullptr && ti.nlobsmax > 0;
             long long bk[27];
             int nb = calc_neighbours(ti, a.ndim, qx, qy, qz, bk);
             // FP32 pre-test (SEARCH 2): the query split into hi + lo floats;
@@ -181,11 +200,14 @@ __device__ int enumerate_obs(const CalcArgs& a, int kc, double qx, double qy, do
                         }
                         if (__any_sync(0xffffffffu, band))
                             if (band) in = exact_in2(a.sx[p], a.sy[p], qx, qy, ti.rmax2);
+                        if (cut_on && in)
+                            in = exact_cut2(a.sx[p], a.sy[p], qx, qy, a.sid[p], a.cut + (size_t)t * a.npts + pt);
                     } else {
                         if (p < b1) {
                             d2 = a.ndim == 2 ? exact::dist2(a.sx[p], a.sy[p], qx, qy)
                                              : exact::dist3(a.sx[p], a.sy[p], a.sz[p], qx, qy, qz);
                             in = d2 <= ti.rmax2;
+                            if (cut_on && in) in = keeps_cut(d2, a.sid[p], a.cut + (size_t)t * a.npts + pt);
                         }
                     }
                     unsigned bal = __ballot_sync(0xffffffffu, in);
@@ -477,7 +499,7 @@ __device__ inline void solve_point(const CalcArgs& a, int pt, int slot, int p, i
         } else {
             __syncthreads();
             QuadProc qp(a, s, tile, tld, Q, gq, lda);
-            enumerate_obs<0>(a, kc, qx, qy, qz, s, qp, false);
+            enumerate_obs<0>(a, pt, kc, qx, qy, qz, s, qp, false);
             if (tid < a.ntypes) {
                 int t = tid;
                 size_t k = (size_t)t * a.npts + pt;

@@ -770,8 +770,8 @@ __device__ __forceinline__ void neighbour_ranges(const CalcArgs& a, const TypeIn
 // with an exact FP64 test in the band (2-D); SEARCH 1: exact FP64 distances.
 // Returns the number of local observations.
 template <int SEARCH, class Proc>
-__device__ int enumerate_obs_seg(const CalcArgs& a, int lseg, double qx, double qy, double qz, int* lid, float* lcf,
-                                 int* wsum, long long* sb0, int* scum, int* tcount, Proc& proc)
+__device__ int enumerate_obs_seg(const CalcArgs& a, int pt, int lseg, double qx, double qy, double qz, int* lid,
+                                 float* lcf, int* wsum, long long* sb0, int* scum, int* tcount, Proc& proc)
 {
     const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
     int total = 0;
@@ -780,6 +780,8 @@ __device__ int enumerate_obs_seg(const CalcArgs& a, int lseg, double qx, double 
         int n = 0;   // list entries (the same in every thread)
         int tcnt = 0;
         if (ti.pos_end > ti.pos_begin) {
+            // NLOBSMAX: the point's cut for this type applies
+            const bool cut_on = a.cut != nullptr && ti.nlobsmax > 0;
             if (wid == 0) neighbour_ranges(a, ti, qx, qy, qz, sb0, scum);
             __syncthreads();
             const int nb = scum[28], ncand = scum[nb];
@@ -833,10 +835,13 @@ __device__ int enumerate_obs_seg(const CalcArgs& a, int lseg, double qx, double 
                     }
                     if (__any_sync(0xffffffffu, band))
                         if (band) in = exact_in2(a.sx[p], a.sy[p], qx, qy, ti.rmax2);
+                    if (cut_on && in)
+                        in = exact_cut2(a.sx[p], a.sy[p], qx, qy, a.sid[p], a.cut + (size_t)t * a.npts + pt);
                 } else {
                     if (p >= 0) {
                         d2 = a.ndim == 2 ? exact::dist2(x, y, qx, qy) : exact::dist3(x, y, z, qx, qy, qz);
                         in = d2 <= ti.rmax2;
+                        if (cut_on && in) in = keeps_cut(d2, a.sid[p], a.cut + (size_t)t * a.npts + pt);
                     }
                 }
                 const unsigned bal = __ballot_sync(0xffffffffu, in);
@@ -1053,8 +1058,10 @@ __global__ void __launch_bounds__(CALC_NT, 2) k_transforms_mixed(CalcArgs a, int
         rnd = 0;
         GramProcTC<HB, FS, ST, DF> proc(a, s, ms, sy, rnd);
         const int p = (a.sxf != nullptr && a.ndim == 2)
-                          ? enumerate_obs_seg<2>(a, lseg, qx, qy, qz, slid, slcf, ictl + 8, nb0, ncum, tcount, proc)
-                          : enumerate_obs_seg<1>(a, lseg, qx, qy, qz, slid, slcf, ictl + 8, nb0, ncum, tcount, proc);
+                          ? enumerate_obs_seg<2>(a, pt, lseg, qx, qy, qz, slid, slcf, ictl + 8, nb0, ncum, tcount,
+                                                 proc)
+                          : enumerate_obs_seg<1>(a, pt, lseg, qx, qy, qz, slid, slcf, ictl + 8, nb0, ncum, tcount,
+                                                 proc);
         proc.finish();
         __syncthreads();
         if (*err) {

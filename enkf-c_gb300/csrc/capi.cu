@@ -146,7 +146,7 @@ ENKFG_API void enkfg_destroy(enkfg_ctx* ctx)
                      ctx->d_w64, ctx->d_nlobs, ctx->d_dfs, ctx->d_srf, ctx->d_pnlobs, ctx->d_pdfs, ctx->d_psrf,
                      ctx->d_counts, ctx->d_order, ctx->d_qhead, ctx->d_status_pt, ctx->d_scratch,
                      ctx->d_numlevels, ctx->d_fields, ctx->d_infl, ctx->d_fi, ctx->d_fj, ctx->d_fk, ctx->d_Hx,
-                     ctx->d_hflag, ctx->d_hids, ctx->d_hsrc, ctx->d_hlev, ctx->d_hoff };
+                     ctx->d_hflag, ctx->d_hids, ctx->d_hsrc, ctx->d_hlev, ctx->d_hoff, ctx->d_cut };
     for (size_t k = 0; k < sizeof(ptrs) / sizeof(ptrs[0]); ++k)
         if (ptrs[k]) cudaFree(ptrs[k]);
     for (int k = 0; k < 10; ++k)
@@ -349,6 +349,9 @@ ENKFG_API enkfg_status enkfg_set_obstypes(enkfg_ctx* ctx, int ntypes, const int*
         ctx->rfactor[t] = rfactor ? rfactor[t] : 1.0;
     }
     if (ctx->types_set && (ctx->ntypes != ntypes || ctx->geographic != (geographic ? 1 : 0))) ctx->obs_set = false;
+    // a new type table: no NLOBSMAX limits, every type visible
+    memset(ctx->nlobsmax, 0, sizeof(ctx->nlobsmax));
+    memset(ctx->hidden, 0, sizeof(ctx->hidden));
     ctx->ntypes = ntypes;
     ctx->geographic = geographic ? 1 : 0;
     ctx->types_set = true;
@@ -361,6 +364,37 @@ ENKFG_API enkfg_status enkfg_set_obstypes(enkfg_ctx* ctx, int ntypes, const int*
         for (int t = 0; t < ntypes; ++t) sr[t] = sqrt(ctx->rfactor[t]);
         SETDEV();
         CK(cudaMemcpy(ctx->d_rfac_sqrt, sr, ntypes * sizeof(double), cudaMemcpyHostToDevice));
+    }
+    return ENKFG_OK;
+}
+
+ENKFG_API enkfg_status enkfg_set_obstype_nlobsmax(enkfg_ctx* ctx, int ntypes, const int* nlobsmax)
+{
+    if (!ctx) return ENKFG_EINVAL;
+    NEED(ctx->types_set, ENKFG_ESTATE, "enkfg_set_obstypes must come first");
+    NEED(ntypes == ctx->ntypes, ENKFG_EINVAL, "ntypes = %d, the context has %d types", ntypes, ctx->ntypes);
+    for (int t = 0; t < ENKFG_MAXTYPES; ++t)
+        ctx->nlobsmax[t] = (nlobsmax != nullptr && t < ntypes && nlobsmax[t] > 0) ? nlobsmax[t] : 0;
+    ctx->cut_valid = false;
+    if (ctx->index_valid) {
+        SETDEV();
+        enkfg_status s = upload_types(ctx, ctx->stream);
+        if (s) return s;
+    }
+    return ENKFG_OK;
+}
+
+ENKFG_API enkfg_status enkfg_set_obstype_visible(enkfg_ctx* ctx, int ntypes, const int* visible)
+{
+    if (!ctx) return ENKFG_EINVAL;
+    NEED(ctx->types_set, ENKFG_ESTATE, "enkfg_set_obstypes must come first");
+    NEED(ntypes == ctx->ntypes, ENKFG_EINVAL, "ntypes = %d, the context has %d types", ntypes, ctx->ntypes);
+    for (int t = 0; t < ENKFG_MAXTYPES; ++t) ctx->hidden[t] = (visible != nullptr && t < ntypes && !visible[t]) ? 1 : 0;
+    ctx->cut_valid = false;
+    if (ctx->index_valid) {
+        SETDEV();
+        enkfg_status s = upload_types(ctx, ctx->stream);
+        if (s) return s;
     }
     return ENKFG_OK;
 }
@@ -558,6 +592,7 @@ ENKFG_API enkfg_status enkfg_set_grid(enkfg_ctx* ctx, const enkfg_grid* g)
     if (s) return s;
     ctx->grid_set = true;
     ctx->t_valid = false;
+    ctx->cut_valid = false;
     return ENKFG_OK;
 }
 
@@ -579,7 +614,7 @@ ENKFG_API enkfg_status enkfg_local_obs(enkfg_ctx* ctx, int* counts, long long* o
     SETDEV();
     enkfg_status s;
     cudaStream_t st = ctx->stream;
-    if (!ctx->index_valid && (s = build_index(ctx, st))) return s;
+    if ((s = prepare_search(ctx, st))) return s;
     int npts = ctx->nj * ctx->ni;
     if ((s = ensure(ctx, &ctx->d_counts, &ctx->counts_cap, (size_t)npts))) return s;
     if ((s = count_local(ctx, ctx->d_counts, nullptr, st))) return s;

@@ -440,6 +440,7 @@ enkfg_status build_index(enkfg_ctx* ctx, cudaStream_t st)
             // relative leaves a margin of about 8x
             ti.rmax2_lo = (float)(ti.rmax2 * (1.0 - 2e-6));
             ti.rmax2_hi = (float)(ti.rmax2 * (1.0 + 2e-6));
+            ti.nlobsmax = ctx->nlobsmax[t];
             bool empty = (h[t * 6] == ~0ull);
             double lo[3] = { 0, 0, 0 }, hi[3] = { 0, 0, 0 };
             if (!empty)
@@ -547,9 +548,23 @@ enkfg_status build_index(enkfg_ctx* ctx, cudaStream_t st)
         ctx->h_types[t].pos_begin = (int)r[0];
         ctx->h_types[t].pos_end = (int)r[1];
     }
-    CK(cudaMemcpyAsync(ctx->d_types, ctx->h_types, sizeof(TypeIndex) * ntypes, cudaMemcpyHostToDevice, st));
+    if ((s = upload_types(ctx, st))) return s;
     ctx->index_valid = true;
     ctx->gather_valid = false;
+    ctx->cut_valid = false;
+    return ENKFG_OK;
+}
+
+enkfg_status upload_types(enkfg_ctx* ctx, cudaStream_t st)
+{
+    // observations.c:1877-1892: a type whose domains do not include the
+    // grid's is skipped by obs_findlocal; here its position range is empty
+    for (int t = 0; t < ctx->ntypes; ++t) {
+        ctx->h_types_up[t] = ctx->h_types[t];
+        ctx->h_types_up[t].nlobsmax = ctx->nlobsmax[t];
+        if (ctx->hidden[t]) ctx->h_types_up[t].pos_end = ctx->h_types_up[t].pos_begin;
+    }
+    CK(cudaMemcpyAsync(ctx->d_types, ctx->h_types_up, sizeof(TypeIndex) * ctx->ntypes, cudaMemcpyHostToDevice, st));
     return ENKFG_OK;
 }
 
@@ -629,7 +644,8 @@ __global__ void k_count_local(int npts, int ntypes, int ndim, const TypeIndex* _
                               const long long* __restrict__ bstart, const double* __restrict__ sx,
                               const double* __restrict__ sy, const double* __restrict__ sz,
                               const double* __restrict__ qx, const double* __restrict__ qy,
-                              const double* __restrict__ qz, int* __restrict__ counts, int* __restrict__ pcounts)
+                              const double* __restrict__ qz, const int* __restrict__ sid,
+                              const CutKey* __restrict__ cut, int* __restrict__ counts, int* __restrict__ pcounts)
 {
     int pt = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     int lane = threadIdx.x & 31;
@@ -640,6 +656,9 @@ __global__ void k_count_local(int npts, int ntypes, int ndim, const TypeIndex* _
         const TypeIndex& ti = types[t];
         int nt = 0;
         if (ti.pos_end > ti.pos_begin) {
+            const bool cut_on = cut != nullptr && ti.nlobsmax > 0;
+            CutKey ck{};
+            if (cut_on) ck = cut[(size_t)t * npts + pt];
             long long bk[27];
             int nb = neighbour_buckets(ti, ndim, x, y, z, bk);
             for (int k = 0; k < nb; ++k) {
@@ -651,6 +670,7 @@ __global__ void k_count_local(int npts, int ntypes, int ndim, const TypeIndex* _
                         double d2 = ndim == 2 ? exact::dist2(sx[p], sy[p], x, y)
                                               : exact::dist3(sx[p], sy[p], sz[p], x, y, z);
                         in = d2 <= ti.rmax2;
+                        if (cut_on && in) in = cut_keeps(d2, sid[p], ck);
                     }
                     nt += __popc(__ballot_sync(0xffffffffu, in));
                 }
@@ -702,7 +722,7 @@ enkfg_status count_local(enkfg_ctx* ctx, int* d_counts, int* d_pcounts, cudaStre
     int ndim = ctx->geographic ? 3 : 2;
     k_count_local<<<div_up((long long)npts * 32, 256), 256, 0, st>>>(
         npts, ctx->ntypes, ndim, ctx->d_types, ctx->d_bstart, ctx->d_sx, ctx->d_sy, ctx->d_sz, ctx->d_qx, ctx->d_qy,
-        ctx->d_qz, d_counts, d_pcounts);
+        ctx->d_qz, ctx->d_sid, any_nlobsmax(ctx) ? ctx->d_cut : nullptr, d_counts, d_pcounts);
     CKL();
     return ENKFG_OK;
 }
@@ -719,6 +739,7 @@ __global__ void __launch_bounds__(LIST_T) k_list_local(int npts, int ntypes, int
                                                        const double* __restrict__ sz, const int* __restrict__ sid,
                                                        const double* __restrict__ qx, const double* __restrict__ qy,
                                                        const double* __restrict__ qz,
+                                                       const CutKey* __restrict__ cut,
                                                        const long long* __restrict__ offsets, int* __restrict__ ids,
                                                        double* __restrict__ coeffs, int* __restrict__ err)
 {
@@ -736,6 +757,9 @@ __global__ void __launch_bounds__(LIST_T) k_list_local(int npts, int ntypes, int
     for (int t = 0; t < ntypes; ++t) {
         const TypeIndex& ti = types[t];
         if (ti.pos_end <= ti.pos_begin) continue;
+        const bool cut_on = cut != nullptr && ti.nlobsmax > 0;
+        CutKey ck{};
+        if (cut_on) ck = cut[(size_t)t * npts + pt];
         long long bk[27];
         int nb = neighbour_buckets(ti, ndim, x, y, z, bk);
         for (int k = 0; k < nb; ++k) {
@@ -747,6 +771,7 @@ __global__ void __launch_bounds__(LIST_T) k_list_local(int npts, int ntypes, int
                 if (p < b1) {
                     d2 = ndim == 2 ? exact::dist2(sx[p], sy[p], x, y) : exact::dist3(sx[p], sy[p], sz[p], x, y, z);
                     in = d2 <= ti.rmax2;
+                    if (cut_on && in) in = cut_keeps(d2, sid[p], ck);
                 }
                 unsigned bal = __ballot_sync(0xffffffffu, in);
                 if (lane == 0) wsum[wid] = __popc(bal);
@@ -811,7 +836,8 @@ enkfg_status list_local(enkfg_ctx* ctx, const long long* d_offsets, int* d_ids, 
     CK(cudaMemsetAsync(ctx->d_qhead, 0, 2 * sizeof(int), st));
     k_list_local<<<npts, LIST_T, smem, st>>>(npts, ctx->ntypes, ndim, ctx->d_types, ctx->d_bstart, ctx->d_sx,
                                              ctx->d_sy, ctx->d_sz, ctx->d_sid, ctx->d_qx, ctx->d_qy, ctx->d_qz,
-                                             d_offsets, d_ids, d_coeffs, ctx->d_qhead + 1);
+                                             any_nlobsmax(ctx) ? ctx->d_cut : nullptr, d_offsets, d_ids, d_coeffs,
+                                             ctx->d_qhead + 1);
     CKL();
     int over = 0;
     CK(cudaMemcpyAsync(&over, ctx->d_qhead + 1, sizeof(int), cudaMemcpyDeviceToHost, st));
@@ -820,5 +846,205 @@ enkfg_status list_local(enkfg_ctx* ctx, const long long* d_offsets, int* d_ids, 
         set_err(ctx, "a point has %d local observations, above the list capacity %d", over, LIST_CAP);
         return ENKFG_ECAPACITY;
     }
+    return ENKFG_OK;
+}
+
+// ---------------------------------------------------------------------------
+// NLOBSMAX cuts (observations.c:1899-1901, kdtree.c:558-574: with a limit the
+// range results of a type are sorted by squared distance and the first
+// nlobsmax kept).  One CTA per point: for each type with a limit, the
+// nlobsmax-th smallest key (d2, id) among the observations in range, by a
+// radix select (8-bit digits) over the 64 bits of the FP64 squared distance
+// (non-negative, so its bit pattern orders as the value) and then, among the
+// observations at that distance, over the 32 bits of the id.  Keys are staged
+// in shared memory when they fit (CUT_CAP); otherwise every pass runs the
+// search again.  Equal distances are ordered by id.
+// ---------------------------------------------------------------------------
+#define CUT_T 256
+#define CUT_CAP 8192
+
+struct CutSmem {
+    unsigned long long kd[CUT_CAP];   // FP64 bits of d2
+    int kid[CUT_CAP];                 // observation id
+    int hist[256];
+    int wsum[CUT_T / 32];
+    int n;                            // keys of the type in range
+    int rank;                         // rank still to find (1-based)
+    int sel;                          // selected digit
+    int tie;                          // keys in the selected digit
+};
+
+__global__ void __launch_bounds__(CUT_T) k_cut_local(int npts, int ntypes, int ndim,
+                                                     const TypeIndex* __restrict__ types,
+                                                     const long long* __restrict__ bstart,
+                                                     const double* __restrict__ sx, const double* __restrict__ sy,
+                                                     const double* __restrict__ sz, const int* __restrict__ sid,
+                                                     const double* __restrict__ qx, const double* __restrict__ qy,
+                                                     const double* __restrict__ qz, CutKey* __restrict__ cut)
+{
+    extern __shared__ unsigned char smem_raw[];
+    CutSmem& sm = *reinterpret_cast<CutSmem*>(smem_raw);
+    const int pt = blockIdx.x, tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+    if (pt >= npts) return;
+    const double x = qx[pt], y = qy[pt], z = ndim == 3 ? qz[pt] : 0.0;
+    for (int t = 0; t < ntypes; ++t) {
+        const TypeIndex& ti = types[t];
+        CutKey res;
+        res.d2 = __longlong_as_double(0x7ff0000000000000ll);   // +inf: keep all
+        res.id = 0x7fffffff;
+        res.pad = 0;
+        if (ti.nlobsmax <= 0 || ti.pos_end <= ti.pos_begin) {
+            if (tid == 0) cut[(size_t)t * npts + pt] = res;
+            continue;
+        }
+        long long bk[27];
+        const int nb = neighbour_buckets(ti, ndim, x, y, z, bk);
+        // every observation of the type in range, as (d2 bits, id), in
+        // passes over the candidates (staged: from shared memory)
+        auto search = [&](auto&& f) {
+            for (int k = 0; k < nb; ++k) {
+                const long long b0 = bstart[bk[k]], b1 = bstart[bk[k] + 1];
+                for (long long p = b0 + tid; p < b1; p += CUT_T) {
+                    const double d2 = ndim == 2 ? exact::dist2(sx[p], sy[p], x, y)
+                                                : exact::dist3(sx[p], sy[p], sz[p], x, y, z);
+                    if (d2 <= ti.rmax2) f((unsigned long long)__double_as_longlong(d2), sid[p]);
+                }
+            }
+        };
+        // count and stage
+        if (tid == 0) sm.n = 0;
+        __syncthreads();
+        for (int k = 0; k < nb; ++k) {
+            const long long b0 = bstart[bk[k]], b1 = bstart[bk[k] + 1];
+            for (long long base = b0; base < b1; base += CUT_T) {
+                const long long p = base + tid;
+                bool in = false;
+                double d2 = 0.0;
+                if (p < b1) {
+                    d2 = ndim == 2 ? exact::dist2(sx[p], sy[p], x, y) : exact::dist3(sx[p], sy[p], sz[p], x, y, z);
+                    in = d2 <= ti.rmax2;
+                }
+                const unsigned bal = __ballot_sync(0xffffffffu, in);
+                if (lane == 0) sm.wsum[wid] = __popc(bal);
+                __syncthreads();
+                int before = 0, tot = 0;
+                for (int w = 0; w < CUT_T / 32; ++w) {
+                    before += (w < wid) ? sm.wsum[w] : 0;
+                    tot += sm.wsum[w];
+                }
+                const int pos = sm.n + before + __popc(bal & ((1u << lane) - 1));
+                if (in && pos < CUT_CAP) {
+                    sm.kd[pos] = (unsigned long long)__double_as_longlong(d2);
+                    sm.kid[pos] = sid[p];
+                }
+                __syncthreads();
+                if (tid == 0) sm.n += tot;
+                __syncthreads();
+            }
+        }
+        const int n = sm.n;
+        if (n <= ti.nlobsmax) {
+            if (tid == 0) cut[(size_t)t * npts + pt] = res;
+            __syncthreads();
+            continue;
+        }
+        const bool staged = n <= CUT_CAP;
+        auto each_key = [&](auto&& f) {
+            if (staged) {
+                for (int i = tid; i < n; i += CUT_T) f(sm.kd[i], sm.kid[i]);
+            } else {
+                search(f);
+            }
+        };
+        // warp 0 finds the digit holding the rank-th key and updates the rank
+        auto pick = [&]() {
+            if (wid == 0) {
+                int c[8], s = 0;
+#pragma unroll
+                for (int i = 0; i < 8; ++i) {
+                    c[i] = sm.hist[lane * 8 + i];
+                    s += c[i];
+                }
+                int incl = s;
+#pragma unroll
+                for (int o = 1; o < 32; o <<= 1) {
+                    const int v = __shfl_up_sync(0xffffffffu, incl, o);
+                    if (lane >= o) incl += v;
+                }
+                const int r = sm.rank;
+                const unsigned hit = __ballot_sync(0xffffffffu, incl >= r);
+                const int L = __ffs(hit) - 1;   // the rank is at most the count: some lane hits
+                if (lane == L) {
+                    int cum = incl - s;
+                    for (int i = 0; i < 8; ++i) {
+                        if (cum + c[i] >= r) {
+                            sm.sel = lane * 8 + i;
+                            sm.tie = c[i];
+                            sm.rank = r - cum;
+                            break;
+                        }
+                        cum += c[i];
+                    }
+                }
+            }
+            __syncthreads();
+        };
+        if (tid == 0) sm.rank = ti.nlobsmax;
+        unsigned long long dpre = 0;
+        for (int shift = 56; shift >= 0; shift -= 8) {
+            sm.hist[tid] = 0;
+            __syncthreads();
+            const unsigned long long hmask = shift == 56 ? 0ull : (~0ull << (shift + 8));
+            each_key([&](unsigned long long kd, int) {
+                if ((kd & hmask) == dpre) atomicAdd(&sm.hist[(int)((kd >> shift) & 255ull)], 1);
+            });
+            __syncthreads();
+            pick();
+            dpre |= (unsigned long long)sm.sel << shift;
+        }
+        res.d2 = __longlong_as_double((long long)dpre);
+        if (sm.rank < sm.tie) {
+            // among the keys at distance d2, the rank-th smallest id
+            unsigned ipre = 0;
+            for (int shift = 24; shift >= 0; shift -= 8) {
+                sm.hist[tid] = 0;
+                __syncthreads();
+                const unsigned imask = shift == 24 ? 0u : (~0u << (shift + 8));
+                each_key([&](unsigned long long kd, int id) {
+                    if (kd == dpre && ((unsigned)id & imask) == ipre)
+                        atomicAdd(&sm.hist[(int)(((unsigned)id >> shift) & 255u)], 1);
+                });
+                __syncthreads();
+                pick();
+                ipre |= (unsigned)sm.sel << shift;
+            }
+            res.id = (int)ipre;
+        }
+        if (tid == 0) cut[(size_t)t * npts + pt] = res;
+        __syncthreads();
+    }
+}
+
+bool any_nlobsmax(const enkfg_ctx* ctx)
+{
+    for (int t = 0; t < ctx->ntypes; ++t)
+        if (ctx->nlobsmax[t] > 0 && !ctx->hidden[t]) return true;
+    return false;
+}
+
+enkfg_status prepare_search(enkfg_ctx* ctx, cudaStream_t st)
+{
+    enkfg_status s;
+    if (!ctx->index_valid && (s = build_index(ctx, st))) return s;
+    if (!any_nlobsmax(ctx) || ctx->cut_valid) return ENKFG_OK;
+    const int npts = ctx->nj * ctx->ni, ndim = ctx->geographic ? 3 : 2;
+    if ((s = ensure(ctx, &ctx->d_cut, &ctx->cut_cap, (size_t)ctx->ntypes * npts))) return s;
+    const size_t smem = sizeof(CutSmem);
+    CK(cudaFuncSetAttribute(k_cut_local, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    k_cut_local<<<npts, CUT_T, smem, st>>>(npts, ctx->ntypes, ndim, ctx->d_types, ctx->d_bstart, ctx->d_sx,
+                                           ctx->d_sy, ctx->d_sz, ctx->d_sid, ctx->d_qx, ctx->d_qy, ctx->d_qz,
+                                           ctx->d_cut);
+    CKL();
+    ctx->cut_valid = true;
     return ENKFG_OK;
 }

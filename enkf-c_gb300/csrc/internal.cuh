@@ -44,7 +44,25 @@ struct TypeIndex {
     float r2_fl[ENKFG_MAXLOCRAD];
     float locweight_f[ENKFG_MAXLOCRAD];
     float rmax2_lo, rmax2_hi;
+    // NLOBSMAX of the type (0: no limit): a point keeps its nlobsmax nearest
+    // observations of the type, those at or before the point's cut key
+    int nlobsmax;
 };
+
+// Cut of a point's local observations of one type under NLOBSMAX: an
+// observation in range is kept when (d2, id) <= (d2, id) of the cut in
+// lexicographic order, d2 the exact FP64 squared distance the search
+// computes and id the observation's index.  {+inf, INT_MAX}: no cut.
+struct CutKey {
+    double d2;
+    int id;
+    int pad;
+};
+
+__host__ __device__ __forceinline__ bool cut_keeps(double d2, int id, const CutKey& c)
+{
+    return d2 < c.d2 || (d2 == c.d2 && id <= c.id);
+}
 
 struct enkfg_ctx {
     int device;
@@ -69,6 +87,8 @@ struct enkfg_ctx {
     double locrad[ENKFG_MAXTYPES][ENKFG_MAXLOCRAD];
     double locweight[ENKFG_MAXTYPES][ENKFG_MAXLOCRAD];
     double rfactor[ENKFG_MAXTYPES];
+    int nlobsmax[ENKFG_MAXTYPES];   // enkfg_set_obstype_nlobsmax (0: no limit)
+    int hidden[ENKFG_MAXTYPES];     // enkfg_set_obstype_visible (1: hidden from the search)
     bool types_set;
 
     // observations (original order)
@@ -95,6 +115,7 @@ struct enkfg_ctx {
     bool gather_valid;
     int nsorted;                // obs with status OK
     TypeIndex h_types[ENKFG_MAXTYPES];
+    TypeIndex h_types_up[ENKFG_MAXTYPES];   // the copy uploaded (hidden types emptied)
     TypeIndex* d_types;
     long long nbuckets;
     long long* d_bstart;        // [nbuckets + 1]
@@ -127,6 +148,11 @@ struct enkfg_ctx {
     // the cycle keep pointing at valid buffers)
     size_t bstart_cap, bfill_cap, key_cap, sid_cap, sx_cap, sy_cap, sz_cap, sxf_cap, syf_cap, stype_cap;
     size_t St_cap, ss_cap, ssf_cap, gtmp_cap;
+    // NLOBSMAX cuts of the current grid: [ntypes][nj*ni] (valid while
+    // cut_valid; computed only when a type has a limit)
+    CutKey* d_cut;
+    size_t cut_cap;
+    bool cut_valid;
     double* d_ox;               // [nobs] kd coordinates (original order)
     double* d_oy;
     double* d_oz;
@@ -283,6 +309,14 @@ enkfg_status scan_counts(enkfg_ctx* ctx, const int* d_in, long long* d_out, long
 
 // stages implemented in the .cu files
 enkfg_status build_index(enkfg_ctx* ctx, cudaStream_t st);
+// the index (built if stale) and, when a type has an NLOBSMAX, the cuts of
+// the current grid's points: what every local search needs first
+enkfg_status prepare_search(enkfg_ctx* ctx, cudaStream_t st);
+// device copy of the type table: types hidden by enkfg_set_obstype_visible
+// get an empty position range, so that no search visits them
+enkfg_status upload_types(enkfg_ctx* ctx, cudaStream_t st);
+// true when some type has an NLOBSMAX (the cut table is in use)
+bool any_nlobsmax(const enkfg_ctx* ctx);
 enkfg_status build_gather(enkfg_ctx* ctx, cudaStream_t st);
 enkfg_status count_local(enkfg_ctx* ctx, int* d_counts, int* d_pcounts, cudaStream_t st);
 enkfg_status count_candidates(enkfg_ctx* ctx, int* d_counts, cudaStream_t st);

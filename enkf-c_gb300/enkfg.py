@@ -39,7 +39,7 @@ STATUS = {0: "OK", 1: "EINVAL", 2: "ECUDA", 3: "ENOMEM", 4: "ETIMEOUT", 5: "ENUM
 
 # every symbol include/enkfg.h declares
 EXPORTS = ["enkfg_create", "enkfg_destroy", "enkfg_set_wait_limit", "enkfg_set_wait_drill", "enkfg_set_field_buffer_size", "enkfg_set_field_block_rows", "enkfg_set_solve_batch", "enkfg_last_error", "enkfg_status_string", "enkfg_version",
-           "enkfg_set_obstypes", "enkfg_set_obs", "enkfg_set_HE", "enkfg_calc_innovations", "enkfg_standardise",
+           "enkfg_set_obstypes", "enkfg_set_obstype_nlobsmax", "enkfg_set_obstype_visible", "enkfg_set_obs", "enkfg_set_HE", "enkfg_calc_innovations", "enkfg_standardise",
            "enkfg_set_S", "enkfg_get_S", "enkfg_set_grid", "enkfg_transform_dims", "enkfg_local_obs",
            "enkfg_calc_transforms", "enkfg_calc_transforms_dev", "enkfg_transforms_dev_ptr",
            "enkfg_set_transforms", "enkfg_update_fields", "enkfg_update_fields_dev", "enkfg_set_hybrid_ensemble",
@@ -190,6 +190,17 @@ class Enkfg:
         self._keep_types = (nlocrad, lr, lw, rf)
         self._ck(self.L.enkfg_set_obstypes(self.h, C.c_int(self.ntypes), _p(nlocrad, C.c_int), _p(lr, C.c_double),
                                            _p(lw, C.c_double), _p(rf, C.c_double), C.c_int(int(geographic))))
+
+    def set_obstype_nlobsmax(self, nlobsmax=None):
+        """NLOBSMAX per type (<= 0: no limit); None clears every limit."""
+        nl = None if nlobsmax is None else np.ascontiguousarray(nlobsmax, np.int32)
+        self._ck(self.L.enkfg_set_obstype_nlobsmax(self.h, C.c_int(self.ntypes), _p(nl, C.c_int)))
+
+    def set_obstype_visible(self, visible=None):
+        """Per type, 0 hides it from the local search (obs-type domains);
+        None shows every type."""
+        v = None if visible is None else np.ascontiguousarray(visible, np.int32)
+        self._ck(self.L.enkfg_set_obstype_visible(self.h, C.c_int(self.ntypes), _p(v, C.c_int)))
 
     def set_obs(self, lon, lat, otype, status, estd=None, value=None):
         lon = np.ascontiguousarray(lon, np.float32)

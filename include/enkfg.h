@@ -87,6 +87,25 @@ ENKFG_API int enkfg_version(void);
  * distances on the sphere (ll2xyz, utils.c:1449). */
 ENKFG_API enkfg_status enkfg_set_obstypes(enkfg_ctx* ctx, int ntypes, const int* nlocrad, const double* locrad, const double* locweight, const double* rfactor, int geographic);
 
+/* NLOBSMAX per observation type (obstype NLOBSMAX, obstypes.c:432 and 547;
+ * applied in obs_findlocal, observations.c:1899-1901, with the distance sort
+ * of kd_findnodeswithinrange, kdtree.c:558-574): a point keeps, of each type
+ * t with nlobsmax[t] > 0, the nlobsmax[t] observations nearest to it (exact
+ * FP64 squared distance; equal distances in order of observation index).
+ * nlobsmax[t] <= 0: no limit (the default).  nlobsmax NULL clears every
+ * limit.  Applies to enkfg_local_obs, the transforms and the adjoint;
+ * enkfg_set_obstypes clears the limits. */
+ENKFG_API enkfg_status enkfg_set_obstype_nlobsmax(enkfg_ctx* ctx, int ntypes, const int* nlobsmax);
+
+/* Which observation types the current grid sees (obstype DOMAINS against the
+ * grid's domain name: observations.c:1877-1892, where a type whose domain
+ * list does not hold the grid's domain is skipped by obs_findlocal).  The
+ * caller compares the names; visible[t] = 0 hides type t from the local
+ * search (enkfg_local_obs, the transforms, the adjoint) until it is set
+ * again.  visible NULL shows every type (the default, and the state after
+ * enkfg_set_obstypes). */
+ENKFG_API enkfg_status enkfg_set_obstype_visible(enkfg_ctx* ctx, int ntypes, const int* visible);
+
 /* Observations (observation fields used on the path, observations.h:47-100):
  * float lon/lat, type, status (0 = STATUS_OK), float estd and value. */
 ENKFG_API enkfg_status enkfg_set_obs(enkfg_ctx* ctx, int nobs, const float* lon, const float* lat, const short* type, const short* status, const float* estd, const float* value);

@@ -11,6 +11,11 @@ GPU library without needing the reference at test time:
                   own order, for trees built as obs_createkdtrees does
                   (sequential insertion by obs index), several query points,
                   two observation types.
+  nlobsmax.npz    kd_findnodeswithinrange with ordered = 1 (the distance
+                  sort obs_findlocal asks for when NLOBSMAX is set), in the
+                  order the reference returns, for two observation types
+                  whose observations come partly in groups at one position
+                  (profiles: equal distances), at grid and off-grid queries.
   transforms.npz  das_calctransforms on a sample of workload-1 points: local
                   obs from the reference kd-tree, taper and gather as
                   transforms.c:1250-1258 (restated here), numerics from the
@@ -85,6 +90,46 @@ def kdtree():
             out[f"t{t}_q{k}_d2"] = d2
     np.savez_compressed(os.path.join(HERE, "kdtree.npz"), **out)
     print("kdtree:", w.nobs, "obs,", len(qs), "queries")
+
+
+def nlobsmax_obs(seed=5):
+    """Observations of two types on a 60 x 40 domain; a third of each type in
+    groups of 2-6 at one position (equal distances to any query)."""
+    rng = np.random.default_rng(seed)
+    lon, lat, ot = [], [], []
+    for t, n in ((0, 900), (1, 500)):
+        k = 0
+        while k < n:
+            x, y = rng.uniform(0, 60), rng.uniform(0, 40)
+            g = int(rng.integers(2, 7)) if rng.uniform() < 0.33 else 1
+            g = min(g, n - k)
+            lon += [x] * g
+            lat += [y] * g
+            ot += [t] * g
+            k += g
+    perm = rng.permutation(len(lon))     # types and groups interleaved in id order
+    lon = np.asarray(lon, np.float32)[perm]
+    lat = np.asarray(lat, np.float32)[perm]
+    ot = np.asarray(ot, np.int16)[perm]
+    qs = np.stack([rng.uniform(0, 59, 30), rng.uniform(0, 39, 30)], 1)
+    qs[:10] = np.floor(qs[:10])
+    return lon, lat, ot, qs
+
+
+def nlobsmax():
+    lon, lat, ot, qs = nlobsmax_obs()
+    coords = np.stack([lon.astype(np.float64), lat.astype(np.float64)], 1)
+    r = np.array([8.0, 11.0])
+    out = dict(lon=lon, lat=lat, otype=ot, q=qs, r=r)
+    for t in range(2):
+        ids = np.nonzero(ot == t)[0]
+        tree = oracle.RefKdTree(coords[ids])
+        for k, q in enumerate(qs):
+            d, d2 = tree.range(q, r[t], ordered=True)
+            out[f"t{t}_q{k}_ids"] = ids[d].astype(np.int32)
+            out[f"t{t}_q{k}_d2"] = d2
+    np.savez_compressed(os.path.join(HERE, "nlobsmax.npz"), **out)
+    print("nlobsmax:", lon.size, "obs,", len(qs), "queries")
 
 
 def transforms():
@@ -245,7 +290,7 @@ if __name__ == "__main__":
     oracle.build()
     if oracle.reflib() is None or oracle.reflib_utils() is None or oracle.reflib_update() is None:
         sys.exit("the reference libraries under oracle/_ref could not be built")
-    which = sys.argv[1:] or ["numerics", "kdtree", "transforms", "model2obs", "update"]
+    which = sys.argv[1:] or ["numerics", "kdtree", "nlobsmax", "transforms", "model2obs", "update"]
     for name in which:
-        {"numerics": numerics, "kdtree": kdtree, "transforms": transforms, "model2obs": model2obs,
-         "update": update}[name]()
+        {"numerics": numerics, "kdtree": kdtree, "nlobsmax": nlobsmax, "transforms": transforms,
+         "model2obs": model2obs, "update": update}[name]()

@@ -62,6 +62,24 @@ def test_kdtree_against_reference_golden():
         assert np.array_equal(lc, ref_lc)
 
 
+@pytest.mark.parametrize("nmax", [(1, 1), (7, 3), (25, 40), (60, 1000)])
+def test_nlobsmax_against_reference_golden(nmax):
+    """NLOBSMAX: per type, the first nlobsmax of the reference's distance-sorted
+    range results (kd_findnodeswithinrange, ordered = 1), in that order."""
+    g = np.load(os.path.join(GOLD, "nlobsmax.npz"))
+    nl, lr, lw = oracle.locrad_table(2, [[float(r)] for r in g["r"]])
+    n = g["lon"].size
+    obs = oracle.ObsSet(g["lon"], g["lat"], g["otype"], np.zeros(n, np.int16), 2, nl, lr, lw, nlobsmax=np.array(nmax))
+    cut = 0
+    for k, q in enumerate(g["q"]):
+        ids, _ = obs.findlocal(q[0], q[1])
+        ref = [g[f"t{t}_q{k}_ids"][:nmax[t]] for t in range(2)]
+        assert np.array_equal(ids, np.concatenate(ref)), k
+        cut += sum(g[f"t{t}_q{k}_ids"].size > nmax[t] for t in range(2))
+    if nmax[1] < 1000:
+        assert cut > 0
+
+
 def test_transforms_against_reference_golden():
     g = np.load(os.path.join(GOLD, "transforms.npz"))
     nl, lr, lw = oracle.locrad_table(1, float(g["locrad"]))
