@@ -174,7 +174,10 @@ __device__ int enumerate_obs(const CalcArgs& a, int pt, int kc, double qx, doubl
         const TypeIndex& ti = a.types[t];
         int tcnt = 0;
         if (ti.pos_end > ti.pos_begin) {
-            const bool cut_on = a.cut != nullptr && ti.nlobsmax > 0;
+            // NLOBSMAX: the point's cut for this type applies (a point with
+            // no more observations in range than the limit has none)
+            bool cut_on = false;
+            if (a.cut != nullptr && ti.nlobsmax > 0) cut_on = a.cut[(size_t)t * a.npts + pt].d2 <= ti.rmax2;
             long long bk[27];
             int nb = calc_neighbours(ti, a.ndim, qx, qy, qz, bk);
             // FP32 pre-test (SEARCH 2): the query split into hi + lo floats;

@@ -780,8 +780,10 @@ __device__ int enumerate_obs_seg(const CalcArgs& a, int pt, int lseg, double qx,
         int n = 0;   // list entries (the same in every thread)
         int tcnt = 0;
         if (ti.pos_end > ti.pos_begin) {
-            // NLOBSMAX: the point's cut for this type applies
-            const bool cut_on = a.cut != nullptr && ti.nlobsmax > 0;
+            // NLOBSMAX: the point's cut for this type applies (a point with
+            // no more observations in range than the limit has none)
+            bool cut_on = false;
+            if (a.cut != nullptr && ti.nlobsmax > 0) cut_on = a.cut[(size_t)t * a.npts + pt].d2 <= ti.rmax2;
             if (wid == 0) neighbour_ranges(a, ti, qx, qy, qz, sb0, scum);
             __syncthreads();
             const int nb = scum[28], ncand = scum[nb];
