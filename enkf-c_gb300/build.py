@@ -20,6 +20,7 @@ SOURCES = ["capi.cu", "prep.cu", "index.cu", "calc.cu", "calc_mixed.cu", "etkf_m
            "noalloc.cu", "model2obs.cu", "ncio.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-fvisibility=hidden",
+         "-Xcompiler", "-ffp-contract=off",
          "--expt-relaxed-constexpr", "-I" + os.path.join(ROOT, "include")]
 
 

@@ -146,7 +146,7 @@ ENKFG_API void enkfg_destroy(enkfg_ctx* ctx)
                      ctx->d_w64, ctx->d_nlobs, ctx->d_dfs, ctx->d_srf, ctx->d_pnlobs, ctx->d_pdfs, ctx->d_psrf,
                      ctx->d_counts, ctx->d_order, ctx->d_qhead, ctx->d_status_pt, ctx->d_scratch,
                      ctx->d_numlevels, ctx->d_fields, ctx->d_infl, ctx->d_fi, ctx->d_fj, ctx->d_fk, ctx->d_Hx,
-                     ctx->d_hflag, ctx->d_hids, ctx->d_hsrc, ctx->d_hlev, ctx->d_hoff, ctx->d_cut };
+                     ctx->d_hflag, ctx->d_hids, ctx->d_hsrc, ctx->d_hlev, ctx->d_hoff, ctx->d_cut, ctx->d_noise };
     for (size_t k = 0; k < sizeof(ptrs) / sizeof(ptrs[0]); ++k)
         if (ptrs[k]) cudaFree(ptrs[k]);
     for (int k = 0; k < 10; ++k)
@@ -818,6 +818,67 @@ static enkfg_status check_update(enkfg_ctx* ctx, const enkfg_update_params* p, i
     return ENKFG_OK;
 }
 
+// The noise given by enkfg_set_field_noise is for this call: it must match
+// its field-layers and ensemble (and is used up by it).
+static enkfg_status take_noise(enkfg_ctx* ctx, const enkfg_update_params* p, int nfield, bool* on)
+{
+    *on = ctx->noise_nfield > 0;
+    if (!*on) return ENKFG_OK;
+    const int nf = ctx->noise_nfield, nm = ctx->noise_nmem;
+    ctx->noise_nfield = 0;
+    NEED(p->mode != ENKFG_MODE_ENOI, ENKFG_EINVAL, "RANDOMISE noise is not applied by the EnOI update");
+    NEED(nf == nfield && nm == p->nmem, ENKFG_EINVAL, "noise given for %d field-layers of %d members, update of %d of %d",
+         nf, nm, nfield, p->nmem);
+    return ENKFG_OK;
+}
+
+ENKFG_API enkfg_status enkfg_set_field_noise(enkfg_ctx* ctx, int nfield, int nmem, const double* deflation,
+                                             const double* sigma, const double* random)
+{
+    if (!ctx) return ENKFG_EINVAL;
+    ctx->noise_nfield = 0;
+    if (nfield == 0 || deflation == nullptr) return ENKFG_OK;
+    NEED(nfield > 0 && nmem >= 1 && sigma && random, ENKFG_EINVAL, "bad noise arguments");
+    // addnoise (update/update.c:46-87): the mean of the member normals is
+    // removed; mult = (float)(sqrt(1 - deflation^2) * sigma); each member's
+    // term mult * r_e in double
+    const size_t n = (size_t)nfield * (nmem + 1);
+    double* h = (double*)malloc(n * sizeof(double));
+    NEED(h, ENKFG_ENOMEM, "host allocation failed");
+    for (int f = 0; f < nfield; ++f) {
+        const double d = deflation[f];
+        double* term = h + nfield + (size_t)f * nmem;
+        h[f] = d;
+        if (isnan(d)) {
+            for (int e = 0; e < nmem; ++e) term[e] = 0.0;
+            continue;
+        }
+        if (!isfinite(d) || !isfinite(sigma[f])) {
+            free(h);
+            set_err(ctx, "field-layer %d: deflation %g, sigma %g", f, d, sigma[f]);
+            return ENKFG_EINVAL;
+        }
+        const double* r = random + (size_t)f * nmem;
+        double sum = 0.0;
+        for (int e = 0; e < nmem; ++e) sum += r[e];
+        sum /= (double)nmem;
+        const double dd = d * d;
+        const float mult = (float)(sqrt(1.0 - dd) * sigma[f]);
+        for (int e = 0; e < nmem; ++e) term[e] = (double)mult * (r[e] - sum);
+    }
+    SETDEV();
+    enkfg_status s = ensure(ctx, &ctx->d_noise, &ctx->noise_cap, n);
+    if (!s) {
+        cudaError_t e = cudaMemcpy(ctx->d_noise, h, n * sizeof(double), cudaMemcpyHostToDevice);
+        if (e != cudaSuccess) s = cuda_fail(ctx, e, "noise upload", __LINE__);
+    }
+    free(h);
+    if (s) return s;
+    ctx->noise_nfield = nfield;
+    ctx->noise_nmem = nmem;
+    return ENKFG_OK;
+}
+
 ENKFG_API enkfg_status enkfg_update_fields_dev(enkfg_ctx* ctx, const enkfg_update_params* p, const int* numlevels_dev,
                                                int nfield, const int* levels, float* fields_dev, float* infl_dev,
                                                void* stream)
@@ -825,9 +886,17 @@ ENKFG_API enkfg_status enkfg_update_fields_dev(enkfg_ctx* ctx, const enkfg_updat
     if (!ctx) return ENKFG_EINVAL;
     enkfg_status s = check_update(ctx, p, nfield, levels);
     if (s) return s;
+    bool noise;
+    if ((s = take_noise(ctx, p, nfield, &noise))) return s;
     NEED(numlevels_dev && fields_dev, ENKFG_EINVAL, "device buffers are required");
     SETDEV();
-    return run_update(ctx, p, numlevels_dev, nfield, levels, fields_dev, infl_dev, pick(ctx, stream));
+    cudaStream_t st = pick(ctx, stream);
+    if ((s = run_update(ctx, p, numlevels_dev, nfield, levels, fields_dev, infl_dev, st))) return s;
+    if (noise) {
+        const int j2 = p->j2 < 0 ? ctx->mnj - 1 : p->j2;
+        s = run_noise(ctx, fields_dev, 0, nfield, p->nmem, (long long)(j2 - p->j1 + 1) * ctx->mni, st);
+    }
+    return s;
 }
 
 // The host-buffer update streams the field-layers through the device in
@@ -849,6 +918,8 @@ ENKFG_API enkfg_status enkfg_update_fields(enkfg_ctx* ctx, const enkfg_update_pa
     if (!ctx) return ENKFG_EINVAL;
     enkfg_status s = check_update(ctx, p, nfield, levels);
     if (s) return s;
+    bool noise;
+    if ((s = take_noise(ctx, p, nfield, &noise))) return s;
     NEED(numlevels && fields, ENKFG_EINVAL, "numlevels and fields are required");
     SETDEV();
     cudaStream_t st = ctx->stream;
@@ -910,6 +981,7 @@ ENKFG_API enkfg_status enkfg_update_fields(enkfg_ctx* ctx, const enkfg_update_pa
         pu.j1 = p->j1 + r0;
         pu.j2 = pu.j1 + rr - 1;
         if ((s = run_update(ctx, &pu, ctx->d_numlevels, nf, levels + f0, dbuf, dinf, st))) return s;
+        if (noise && (s = run_noise(ctx, dbuf, f0, nf, p->nmem, (long long)rr * mni, st))) return s;
         CK(cudaEventRecord(upd_done, st));
         CK(cudaStreamWaitEvent(cout, upd_done, 0));
         CK(cudaMemcpy2DAsync(hsrc, plane * sizeof(float), dbuf, wbytes, wbytes, (size_t)nf * mp,

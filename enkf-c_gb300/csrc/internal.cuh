@@ -234,6 +234,13 @@ struct enkfg_ctx {
     float* d_infl;
     size_t infl_cap;
 
+    // RANDOMISE of the next update call (enkfg_set_field_noise): d_noise
+    // holds [noise_nfield] deflations, then [noise_nfield][noise_nmem]
+    // member terms; noise_nfield = 0: none
+    int noise_nfield, noise_nmem;
+    double* d_noise;
+    size_t noise_cap;
+
     // forward-operator (HE) stage
     double* d_fi;               // [nobs] observation.fij[0]
     double* d_fj;               // [nobs] observation.fij[1]
@@ -348,6 +355,9 @@ enkfg_status resident_ctas(enkfg_ctx* ctx, const void* fn, int nt, size_t dsmem,
 enkfg_status run_update(enkfg_ctx* ctx, const enkfg_update_params* p, const int* d_numlevels, int nfield,
                         const int* levels, float* d_fields, float* d_infl, cudaStream_t st);
 enkfg_status run_innovations(enkfg_ctx* ctx, cudaStream_t st);
+// RANDOMISE on nf field-layers (layers f0.. of the set the noise was given
+// for) at d_v: [nf][nmem] planes of ncell floats
+enkfg_status run_noise(enkfg_ctx* ctx, float* d_v, int f0, int nf, int nmem, long long ncell, cudaStream_t st);
 // (re)allocate S, s and std_f for nmem members of the current observations
 extern "C" enkfg_status alloc_S(enkfg_ctx* ctx, int nmem, int nmem_dynamic);
 enkfg_status run_standardise(enkfg_ctx* ctx, cudaStream_t st);

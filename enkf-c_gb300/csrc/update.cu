@@ -1323,3 +1323,40 @@ enkfg_status run_update(enkfg_ctx* ctx, const enkfg_update_params* p, const int*
     cudaEventRecord(ctx->ev[5], st);
     return ENKFG_OK;
 }
+
+// ---------------------------------------------------------------------------
+// RANDOMISE (addnoise, update/update.c:46-87, applied after the update of a
+// set of fields, :552-563): every cell of member e of a field-layer with a
+// finite deflation becomes v * (float)deflation + mult * r_e, where the
+// member's term mult * r_e (mult = (float)(sqrt(1 - deflation^2) * sigma), r
+// the host's normals less their member mean) is a double formed on the host
+// (enkfg_set_field_noise).  The precisions are the reference's: the float
+// product, then the double sum rounded to float.  One plane (member of a
+// field-layer) per blockIdx.y; planes are [layer][member], ncell floats each.
+// ---------------------------------------------------------------------------
+__global__ void k_add_noise(float* __restrict__ v, int nplanes, int nmem, long long ncell,
+                            const double* __restrict__ defl, const double* __restrict__ term)
+{
+    for (int pl = blockIdx.y; pl < nplanes; pl += gridDim.y) {
+        const double d = defl[pl / nmem];
+        if (d != d) continue;   // NaN deflation: the layer takes no noise
+        const float fd = (float)d;
+        const double t = term[pl];
+        float* vp = v + (size_t)pl * ncell;
+        for (long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x; c < ncell;
+             c += (long long)gridDim.x * blockDim.x)
+            vp[c] = __double2float_rn(__dadd_rn((double)__fmul_rn(vp[c], fd), t));
+    }
+}
+
+enkfg_status run_noise(enkfg_ctx* ctx, float* d_v, int f0, int nf, int nmem, long long ncell, cudaStream_t st)
+{
+    if (nf <= 0 || ncell <= 0) return ENKFG_OK;
+    const int nplanes = nf * nmem;
+    const int gx = ncell >= 256 * 64 ? 64 : div_up(ncell, 256);
+    dim3 g(gx, nplanes < 65535 ? nplanes : 65535);
+    k_add_noise<<<g, 256, 0, st>>>(d_v, nplanes, nmem, ncell, ctx->d_noise + f0,
+                                   ctx->d_noise + ctx->noise_nfield + (size_t)f0 * nmem);
+    CKL();
+    return ENKFG_OK;
+}

@@ -42,7 +42,7 @@ EXPORTS = ["enkfg_create", "enkfg_destroy", "enkfg_set_wait_limit", "enkfg_set_w
            "enkfg_set_obstypes", "enkfg_set_obstype_nlobsmax", "enkfg_set_obstype_visible", "enkfg_set_obs", "enkfg_set_HE", "enkfg_calc_innovations", "enkfg_standardise",
            "enkfg_set_S", "enkfg_get_S", "enkfg_set_grid", "enkfg_transform_dims", "enkfg_local_obs",
            "enkfg_calc_transforms", "enkfg_calc_transforms_dev", "enkfg_transforms_dev_ptr",
-           "enkfg_set_transforms", "enkfg_update_fields", "enkfg_update_fields_dev", "enkfg_set_hybrid_ensemble",
+           "enkfg_set_transforms", "enkfg_update_fields", "enkfg_update_fields_dev", "enkfg_set_field_noise", "enkfg_set_hybrid_ensemble",
            "enkfg_set_hybrid_ensemble_dev", "enkfg_kernel_launches", "enkfg_stage_times", "enkfg_kernel_times", "enkfg_set_stream",
            "enkfg_set_HE_dev", "enkfg_rebuild_index", "enkfg_local_offsets_noalloc", "enkfg_autotune_table",
            "enkfg_autotune_reset", "enkfg_adjoint_transforms", "enkfg_adjoint_mean", "enkfg_set_obs_positions",
@@ -457,6 +457,20 @@ class Enkfg:
         self._ck(self.L.enkfg_update_fields(self.h, C.byref(prm), _p(nl, C.c_int), C.c_int(nfield), _p(lv, C.c_int),
                                             _p(f, C.c_float), _p(infl, C.c_float)))
         return (f, infl) if want_infl else f
+
+    def set_field_noise(self, deflation=None, sigma=None, random=None):
+        """RANDOMISE for the next update call: deflation, sigma [nfield]
+        (NaN deflation: no noise for that field-layer), random [nfield][nmem]
+        standard normals.  No arguments: none."""
+        if deflation is None:
+            self._ck(self.L.enkfg_set_field_noise(self.h, C.c_int(0), C.c_int(0), None, None, None))
+            return
+        d = np.ascontiguousarray(deflation, np.float64)
+        sg = np.ascontiguousarray(sigma, np.float64)
+        r = np.ascontiguousarray(random, np.float64)
+        nfield, nmem = r.shape
+        self._ck(self.L.enkfg_set_field_noise(self.h, C.c_int(nfield), C.c_int(nmem), _p(d, C.c_double),
+                                              _p(sg, C.c_double), _p(r, C.c_double)))
 
     def updatebg(self, fields, numlevels, levels, **kw):
         kw["mode"] = MODE_ENOI

@@ -290,6 +290,21 @@ ENKFG_API enkfg_status enkfg_set_solve_batch(enkfg_ctx* ctx, int points);
  * not depend on it. */
 ENKFG_API enkfg_status enkfg_set_field_block_rows(enkfg_ctx* ctx, int rows);
 
+/* RANDOMISE ("propagate") for the next enkfg_update_fields or
+ * enkfg_update_fields_dev call (addnoise, update/update.c:46-87, which
+ * das_updatefields applies to each of its fields after the update,
+ * :552-563): field-layer f with a non-NaN deflation[f] (DEFLATION of its
+ * model variable) becomes, in every cell of member e,
+ *     v * (float)deflation + mult * (random[f][e] - mean_e random[f][e]),
+ *     mult = (float)(sqrt(1 - deflation^2) * sigma[f])   (SIGMA),
+ * in the reference's precisions.  random [nfield][nmem] are the standard
+ * normals the host draws for the field (get_normalpair, utils.c:1477-1484,
+ * in the reference's order: (nmem + 1) / 2 pairs, the first nmem used).
+ * The noise covers the rows the update call covers (its j1..j2 tile).
+ * nfield and nmem must be the next call's; ENOI updates take no noise.
+ * nfield 0 or deflation NULL: none.  The next update call uses it up. */
+ENKFG_API enkfg_status enkfg_set_field_noise(enkfg_ctx* ctx, int nfield, int nmem, const double* deflation, const double* sigma, const double* random);
+
 /* Device-resident form: fields/infl are device addresses. */
 ENKFG_API enkfg_status enkfg_update_fields_dev(enkfg_ctx* ctx, const enkfg_update_params* p, const int* numlevels_dev, int nfield, const int* levels, float* fields_dev, float* infl_dev, void* stream);
 

@@ -431,6 +431,17 @@ def sethybridensemble(v, nmem_d, gamma):
     return v, vmean
 
 
+def addnoise(v, deflation, sigma, random):
+    """addnoise (update/update.c:46-87) on v [nmem][...] (copied): returns
+    the randomised field.  random: at least nmem standard normals."""
+    v = np.ascontiguousarray(v, np.float32).copy()
+    m = v.shape[0]
+    r = np.ascontiguousarray(random, np.float64)
+    lib().or_addnoise(C.c_int(m), C.c_long(v.size // m), C.c_double(deflation), C.c_double(sigma), _p(r, C.c_double),
+                      _p(v, C.c_float))
+    return v
+
+
 # ---------------------------------------------------------------------------
 # forward operator (calc/model2obs.c) and the end of das_getHE (calc/ensobs.c)
 # ---------------------------------------------------------------------------
@@ -581,6 +592,9 @@ def reflib_update():
             L.ref_update_layer.argtypes = [C.c_int] * 12 + [C.c_float, C.c_double, C.c_int, C.c_int] + \
                 [C.c_void_p] * 4
             L.ref_sethybridensemble.argtypes = [C.c_int, C.c_int, C.c_double, C.c_int, C.c_void_p]
+            L.ref_set_noise.argtypes = [C.c_double, C.c_double]
+            L.ref_srand48.argtypes = [C.c_long]
+            L.ref_normalpair.argtypes = [C.c_void_p]
             _refup = L
     return _refup
 
@@ -609,6 +623,30 @@ def ref_update_layer(v, T, w, numlevels, *, mode, nmem, nmem_dynamic, stride, pe
                        float(inf_ratio), int(output_increment), int(applylog),
                        None if Tc is None else Tc.ctypes.data, wc.ctypes.data, nl.ctypes.data, v.ctypes.data)
     return v
+
+
+def ref_update_layer_noise(v, T, w, numlevels, *, deflation, sigma, seed, **kw):
+    """ref_update_layer with RANDOMISE: the reference's das_updatefields ends
+    with its addnoise, whose normals come from drand48 seeded with `seed`.
+    Returns (updated field, the normals addnoise drew: (nmem + 1) // 2 pairs
+    flattened)."""
+    L = reflib_update()
+    if L is None:
+        raise RuntimeError("reference update library not built")
+    nmem = int(kw["nmem"])
+    L.ref_set_noise(float(deflation), float(sigma))
+    try:
+        L.ref_srand48(int(seed))
+        out = ref_update_layer(v, T, w, numlevels, **kw)
+    finally:
+        L.ref_set_noise(float("nan"), float("nan"))
+    L.ref_srand48(int(seed))
+    r = np.zeros((nmem + 1) // 2 * 2)
+    for e in range((nmem + 1) // 2):
+        pair = np.zeros(2)
+        L.ref_normalpair(pair.ctypes.data)
+        r[2 * e:2 * e + 2] = pair
+    return out, r
 
 
 def ref_sethybridensemble(v, nmem_d, gamma):

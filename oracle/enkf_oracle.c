@@ -1224,6 +1224,32 @@ int or_updatebg(const or_updateparams* P, const float* w, const int* numlevels, 
     return 0;
 }
 
+/* addnoise (update.c:46-87): the member normals less their mean, then
+ * v * (float) deflation + mult * r_e with mult a float; the float product
+ * is widened to double for the sum, which is rounded back to float. */
+void or_addnoise(int nmem, long ncell, double deflation, double sigma, const double* random, float* v)
+{
+    double* r = malloc(nmem * sizeof(double));
+    double sum = 0.0;
+    float mult;
+    int e;
+    long i;
+
+    for (e = 0; e < nmem; ++e)
+        sum += random[e];
+    sum /= (double) nmem;
+    for (e = 0; e < nmem; ++e)
+        r[e] = random[e] - sum;
+    mult = (float) (sqrt(1.0 - deflation * deflation) * sigma);
+    for (e = 0; e < nmem; ++e) {
+        float* vv = v + (size_t) e * ncell;
+
+        for (i = 0; i < ncell; ++i)
+            vv[i] = vv[i] * (float) deflation + mult * r[e];
+    }
+    free(r);
+}
+
 /* das_sethybridensemble (dasystem.c:775-819) */
 void or_sethybridensemble(int nmem, int nmem_d, int nmem_s, double gamma, int nij, float* v, double* vmean)
 {

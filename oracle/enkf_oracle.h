@@ -141,6 +141,11 @@ int or_updatebg(const or_updateparams* p, const float* w, const int* numlevels, 
  * receives the double dynamic mean [nij]. */
 void or_sethybridensemble(int nmem, int nmem_d, int nmem_s, double gamma, int nij, float* v, double* vmean);
 
+/* addnoise (update.c:46-87) on one field of nmem members of ncell cells,
+ * v [nmem][ncell] in place; random holds at least nmem standard normals
+ * (copied: the member mean is removed from the copy). */
+void or_addnoise(int nmem, long ncell, double deflation, double sigma, const double* random, float* v);
+
 #ifdef __cplusplus
 }
 #endif

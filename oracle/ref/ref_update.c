@@ -11,7 +11,9 @@
  * included here and the entry points below call them directly.  What they
  * reach outside update.c is supplied in memory:
  *   - the model: one variable on one grid (its log flag, inflation,
- *     inflation ratio; deflation NaN, so addnoise is not called);
+ *     inflation ratio, and its deflation and sigma: NaN unless
+ *     ref_set_noise gave them, in which case das_updatefields ends with
+ *     addnoise, drawing its normals with get_normalpair from utils.c);
  *   - the grid: size, stride, surface layer id, periodic flag, numlevels;
  *   - the transforms file (transforms.nc, read through ncw_*): T
  *     [nj][ni][m_dyn][m] and w [nj][ni][m] arrays and the stride attribute.
@@ -73,18 +75,20 @@ void model_getvarinflation(model* m, int varid, float* inflation, double* inf_ra
     *inf_ratio = ((orref_model*) m)->inf_ratio;
 }
 
+static double orref_deflation = NAN, orref_sigma = NAN;
+
 double model_getvardeflation(model* m, int varid)
 {
     (void) m;
     (void) varid;
-    return NAN;
+    return orref_deflation;
 }
 
 double model_getvarsigma(model* m, int varid)
 {
     (void) m;
     (void) varid;
-    return NAN;
+    return orref_sigma;
 }
 
 void model_getvargridsize(model* m, int vid, int* ni, int* nj, int* nk)
@@ -328,6 +332,25 @@ int ref_update_layer(int mode, int nmem, int nmem_dynamic, int stride, int perio
     orref_free3(rows, nrows);
     free(g.numlevels);
     return 0;
+}
+
+/* DEFLATION and SIGMA of the variable of the next ref_update_layer (NaN
+ * deflation: no RANDOMISE); the generator state of drand48, which
+ * get_normalpair (common/utils.c:1477-1484) draws from; and one pair. */
+void ref_set_noise(double deflation, double sigma)
+{
+    orref_deflation = deflation;
+    orref_sigma = sigma;
+}
+
+void ref_srand48(long seed)
+{
+    srand48(seed);
+}
+
+void ref_normalpair(double* x)
+{
+    get_normalpair(x);
 }
 
 /* das_sethybridensemble on v [nmem + 2][nij] (rows nmem, nmem + 1 hold the

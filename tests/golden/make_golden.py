@@ -35,6 +35,11 @@ GPU library without needing the reference at test time:
                   (j1..j2), land and level masks with surfk 0 and > 0,
                   missing values in dynamic and static members, spread-capped
                   inflation, increments, log10 fields, hybrid and EnOI.
+  addnoise.npz    das_updatefields with RANDOMISE (deflation and sigma of the
+                  variable set, so update.c ends with its addnoise), the
+                  normals drawn by the reference's get_normalpair from a
+                  seeded drand48 stored as inputs: ENKF and hybrid, odd and
+                  even ensembles, strides 1-3, increments, log10 fields.
 
 Usage:  python tests/golden/make_golden.py [fixture ...]   (default: all)
 """
@@ -286,11 +291,55 @@ def update():
     print("update:", len(UPDATE_CASES), "cases")
 
 
+# (name, mode, mnj, mni, m, md, stride, periodic, inc, alog, deflation, sigma, seed)
+NOISE_CASES = [
+    ("enkf_m10_s1", 0, 14, 17, 10, 10, 1, 0, 0, 0, 0.9, 0.4, 11),
+    ("enkf_m11_s2_periodic", 0, 15, 16, 11, 11, 2, 1, 0, 0, 0.6, 1.5, 12),
+    ("hybrid_m12_s3", 2, 16, 19, 12, 8, 3, 0, 0, 0, 0.95, 0.2, 13),
+    ("enkf_m10_increment", 0, 12, 13, 10, 10, 2, 0, 1, 0, 0.8, 0.3, 14),
+    ("enkf_m24_log", 0, 13, 15, 24, 24, 1, 0, 0, 1, 0.7, 0.1, 15),
+]
+
+
+def addnoise():
+    rng = np.random.default_rng(20261)
+    out = {"names": np.array([c[0] for c in NOISE_CASES])}
+    for k, (name, mode, mnj, mni, m, md, stride, per, inc, alog, defl, sigma, seed) in enumerate(NOISE_CASES):
+        nj = (mnj - 1) // stride + 1
+        ni = (mni - 1) // stride + 1
+        T = (np.eye(m, dtype=np.float64)[None, None, :md, :] +
+             0.15 * rng.standard_normal((nj, ni, md, m))).astype(np.float32)
+        w = (0.08 * rng.standard_normal((nj, ni, m))).astype(np.float32)
+        numlevels = np.full((mnj, mni), 4, np.int32)
+        numlevels[rng.random((mnj, mni)) < 0.2] = 0
+        v = (15.0 + rng.standard_normal((m, mnj, mni))).astype(np.float32)
+        if alog:
+            v = np.log10(np.abs(v) + 1.0).astype(np.float32)
+        if mode == 2:
+            v = oracle.ref_sethybridensemble(v.reshape(m, -1), md, 0.5)[0].reshape(m, mnj, mni).copy()
+        res, r = oracle.ref_update_layer_noise(v, T, w, numlevels, deflation=defl, sigma=sigma, seed=seed, mode=mode,
+                                               nmem=m, nmem_dynamic=md, stride=stride, periodic_i=per,
+                                               output_increment=inc, applylog=alog)
+        plain = oracle.ref_update_layer(v, T, w, numlevels, mode=mode, nmem=m, nmem_dynamic=md, stride=stride,
+                                        periodic_i=per, output_increment=inc, applylog=alog)
+        out[f"n{k}_prm"] = np.array([mode, mnj, mni, m, md, stride, per, inc, alog], np.int32)
+        out[f"n{k}_noise"] = np.array([defl, sigma])
+        out[f"n{k}_random"] = r
+        out[f"n{k}_T"] = T
+        out[f"n{k}_w"] = w
+        out[f"n{k}_numlevels"] = numlevels
+        out[f"n{k}_v"] = v
+        out[f"n{k}_plain"] = plain
+        out[f"n{k}_out"] = res
+    np.savez_compressed(os.path.join(HERE, "addnoise.npz"), **out)
+    print("addnoise:", len(NOISE_CASES), "cases")
+
+
 if __name__ == "__main__":
     oracle.build()
     if oracle.reflib() is None or oracle.reflib_utils() is None or oracle.reflib_update() is None:
         sys.exit("the reference libraries under oracle/_ref could not be built")
-    which = sys.argv[1:] or ["numerics", "kdtree", "nlobsmax", "transforms", "model2obs", "update"]
+    which = sys.argv[1:] or ["numerics", "kdtree", "nlobsmax", "transforms", "model2obs", "update", "addnoise"]
     for name in which:
         {"numerics": numerics, "kdtree": kdtree, "nlobsmax": nlobsmax, "transforms": transforms,
-         "model2obs": model2obs, "update": update}[name]()
+         "model2obs": model2obs, "update": update, "addnoise": addnoise}[name]()

@@ -231,3 +231,80 @@ def test_update_streamed_groups_match_one_group(ctx):
                                             nmem_dynamic=w.nmem_dynamic, stride=w.stride, level=int(levels[f]),
                                             inflation=1.03, inf_ratio=0.4) for f in range(fl.shape[0])])
         assert close(whole, ref) < 2e-5
+
+
+def test_randomise_against_reference_golden(ctx):
+    """RANDOMISE (addnoise, update/update.c:46-87) after the update, against
+    the reference's own das_updatefields with DEFLATION and SIGMA set
+    (tests/golden/addnoise.npz: the normals its get_normalpair drew are
+    inputs): the field within the update tolerance of the reference's, and
+    the noise itself bit for bit (the randomised device field equals the
+    oracle's addnoise of the device's plain update).  Host-buffer and
+    device-buffer calls."""
+    import os
+    import torch
+    g = np.load(os.path.join(os.path.dirname(__file__), "golden", "addnoise.npz"))
+    nl1, lr1, lw1 = oracle.locrad_table(1, 5.0)
+    dev = torch.device("cuda", 0)
+    for k, name in enumerate(g["names"]):
+        mode, mnj, mni, m, md, stride, per, inc, alog = [int(x) for x in g[f"n{k}_prm"]]
+        defl, sigma = [float(x) for x in g[f"n{k}_noise"]]
+        r = g[f"n{k}_random"][:m]
+        ctx.set_obstypes(nl1, lr1, lw1, np.ones(1))
+        ctx.set_obs(np.array([1.0], np.float32), np.array([1.0], np.float32), np.zeros(1, np.int16),
+                    np.zeros(1, np.int16), np.ones(1, np.float32), np.zeros(1, np.float32))
+        ctx.set_grid(np.arange(mni, dtype=np.float64), np.arange(mnj, dtype=np.float64), stride=stride,
+                     periodic_i=bool(per))
+        ctx.set_transforms(g[f"n{k}_T"], g[f"n{k}_w"], mode=mode, nmem=m, nmem_dynamic=md)
+        kw = dict(mode=mode, nmem=m, nmem_dynamic=md, output_increment=inc, applylog=alog)
+        v = g[f"n{k}_v"][None]
+        plain = ctx.updatefields(v, g[f"n{k}_numlevels"], [0], **kw)[0]
+        ctx.set_field_noise([defl], [sigma], r[None])
+        got = ctx.updatefields(v, g[f"n{k}_numlevels"], [0], **kw)[0]
+        assert np.array_equal(got, oracle.addnoise(plain, defl, sigma, r), equal_nan=True), name
+        assert close(got, g[f"n{k}_out"]) < (1e-4 if alog else 2e-5), name
+        # device buffers
+        fd = torch.from_numpy(np.ascontiguousarray(v)).to(dev)
+        nd = torch.from_numpy(g[f"n{k}_numlevels"]).to(dev)
+        ctx.set_field_noise([defl], [sigma], r[None])
+        ctx.updatefields_dev(fd.data_ptr(), nd.data_ptr(), 1, [0], **kw)
+        torch.cuda.synchronize()
+        assert np.array_equal(fd.cpu().numpy()[0], got, equal_nan=True), name
+        # the noise is used up: the next update has none
+        assert np.array_equal(ctx.updatefields(v, g[f"n{k}_numlevels"], [0], **kw)[0], plain, equal_nan=True)
+
+
+def test_randomise_streamed_layers_and_blocks(ctx, gpu_lib):
+    """Several field-layers, one without noise (NaN deflation), through the
+    host-buffer pipeline in groups and row blocks: each layer is the oracle's
+    addnoise of the plain device update with that layer's normals; a noise
+    set for another layer count is refused."""
+    w = synth.make(3, scale=0.06, nobs=3000, nmem=24)
+    w.nlayers = 3
+    transforms(ctx, w)
+    fl = np.ascontiguousarray(w.fields.reshape(-1, *w.fields.shape[2:]))[:5]
+    levels = [0, 1, 2, 0, 1]
+    kw = dict(mode=0, nmem=w.nmem, nmem_dynamic=w.nmem, inflation=1.05)
+    plain = ctx.updatefields(fl, w.numlevels, levels, **kw)
+    rng = np.random.default_rng(4)
+    defl = np.array([0.9, np.nan, 0.5, 0.99, 0.7])
+    sigma = np.array([0.3, 0.3, 2.0, 0.05, 1.0])
+    r = rng.standard_normal((5, w.nmem))
+    want = plain.copy()
+    for f in range(5):
+        if not np.isnan(defl[f]):
+            want[f] = oracle.addnoise(plain[f], defl[f], sigma[f], r[f])
+    for g_, rows in ((1, 0), (2, 5), (5, 3)):
+        ctx.set_field_buffer_size(g_)
+        ctx.set_field_block_rows(rows)
+        try:
+            ctx.set_field_noise(defl, sigma, r)
+            got = ctx.updatefields(fl, w.numlevels, levels, **kw)
+        finally:
+            ctx.set_field_buffer_size(0)
+            ctx.set_field_block_rows(0)
+        assert np.array_equal(got, want, equal_nan=True), (g_, rows)
+    ctx.set_field_noise(defl[:4], sigma[:4], r[:4])
+    with pytest.raises(gpu_lib.EnkfgError) as e:
+        ctx.updatefields(fl, w.numlevels, levels, **kw)
+    assert e.value.status == 1

@@ -80,6 +80,19 @@ def test_nlobsmax_against_reference_golden(nmax):
         assert cut > 0
 
 
+def test_addnoise_against_reference_golden():
+    """RANDOMISE: the oracle's addnoise of the reference's plain update equals
+    the reference's randomised update bit for bit (tests/golden/addnoise.npz,
+    from update.c with DEFLATION and SIGMA set)."""
+    g = np.load(os.path.join(GOLD, "addnoise.npz"))
+    for k, name in enumerate(g["names"]):
+        m = int(g[f"n{k}_prm"][3])
+        defl, sigma = [float(x) for x in g[f"n{k}_noise"]]
+        got = oracle.addnoise(g[f"n{k}_plain"], defl, sigma, g[f"n{k}_random"][:m])
+        assert np.array_equal(got, g[f"n{k}_out"], equal_nan=True), name
+        assert not np.array_equal(got, g[f"n{k}_plain"]), name
+
+
 def test_transforms_against_reference_golden():
     g = np.load(os.path.join(GOLD, "transforms.npz"))
     nl, lr, lw = oracle.locrad_table(1, float(g["locrad"]))
