@@ -874,7 +874,7 @@ ENKFG_API enkfg_status enkfg_set_field_noise(enkfg_ctx* ctx, int nfield, int nme
     }
     free(h);
     if (s) return s;
-    ctx->noise_nfield = nfield;
+    ctx->noise_nfield = ctx->noise_nlayer = nfield;
     ctx->noise_nmem = nmem;
     return ENKFG_OK;
 }

@@ -235,9 +235,10 @@ struct enkfg_ctx {
     size_t infl_cap;
 
     // RANDOMISE of the next update call (enkfg_set_field_noise): d_noise
-    // holds [noise_nfield] deflations, then [noise_nfield][noise_nmem]
-    // member terms; noise_nfield = 0: none
-    int noise_nfield, noise_nmem;
+    // holds [noise_nlayer] deflations, then [noise_nlayer][noise_nmem]
+    // member terms; noise_nfield = noise_nlayer until an update call takes
+    // the noise (0: none pending)
+    int noise_nfield, noise_nmem, noise_nlayer;
     double* d_noise;
     size_t noise_cap;
 

@@ -1356,7 +1356,7 @@ enkfg_status run_noise(enkfg_ctx* ctx, float* d_v, int f0, int nf, int nmem, lon
     const int gx = ncell >= 256 * 64 ? 64 : div_up(ncell, 256);
     dim3 g(gx, nplanes < 65535 ? nplanes : 65535);
     k_add_noise<<<g, 256, 0, st>>>(d_v, nplanes, nmem, ncell, ctx->d_noise + f0,
-                                   ctx->d_noise + ctx->noise_nfield + (size_t)f0 * nmem);
+                                   ctx->d_noise + ctx->noise_nlayer + (size_t)f0 * nmem);
     CKL();
     return ENKFG_OK;
 }
