@@ -116,18 +116,16 @@ struct AdjProc {
                 const int id = A.sid[p];
                 atomicAdd(&A.dinn[id], lc * lc * (double)av / A.sig[p]);
                 atomicAdd(&A.dvar[id], -lc * dlc / (2.0 * A.R[p]));
-                // d lc / d rho (a point without coordinates has lc = 1)
-                if (!isnan(qx + qy)) {
-                    const double d2 = a.ndim == 2 ? exact::dist2(a.sx[p], a.sy[p], qx, qy)
-                                                  : exact::dist3(a.sx[p], a.sy[p], a.sz[p], qx, qy, qz);
-                    const double dist = sqrt(d2);
-                    double dl = 0.0;
-                    for (int k = 0; k < ti.nlocrad; ++k) {
-                        const double x = dist / ti.locrad[k];
-                        dl -= ti.locweight[k] * x * gc_deriv(x);
-                    }
-                    rho_acc += dlc * dl;
+                // d lc / d rho
+                const double d2 = a.ndim == 2 ? exact::dist2(a.sx[p], a.sy[p], qx, qy)
+                                              : exact::dist3(a.sx[p], a.sy[p], a.sz[p], qx, qy, qz);
+                const double dist = sqrt(d2);
+                double dl = 0.0;
+                for (int k = 0; k < ti.nlocrad; ++k) {
+                    const double x = dist / ti.locrad[k];
+                    dl -= ti.locweight[k] * x * gc_deriv(x);
                 }
+                rho_acc += dlc * dl;
             }
         }
         __syncthreads();

@@ -170,9 +170,6 @@ __device__ int enumerate_obs(const CalcArgs& a, int pt, int kc, double qx, doubl
     const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
     int* wsum = s.ictl + 8;
     int total = 0;
-    // a point without coordinates (a grid of type NONE) takes every
-    // observation with coefficient 1 (obs_getglobal, observations.c:1773-1817)
-    const bool glob = isnan(qx + qy);
     for (int t = 0; t < a.ntypes; ++t) {
         const TypeIndex& ti = a.types[t];
         int tcnt = 0;
@@ -182,7 +179,7 @@ __device__ int enumerate_obs(const CalcArgs& a, int pt, int kc, double qx, doubl
             bool cut_on = false;
             if (a.cut != nullptr && ti.nlobsmax > 0) cut_on = a.cut[(size_t)t * a.npts + pt].d2 <= ti.rmax2;
             long long bk[27];
-            const int nb = glob ? 1 : calc_neighbours(ti, a.ndim, qx, qy, qz, bk);
+            int nb = calc_neighbours(ti, a.ndim, qx, qy, qz, bk);
             // FP32 pre-test (SEARCH 2): the query split into hi + lo floats;
             // candidates inside the band [rmax2_lo, rmax2_hi] take the exact
             // FP64 test, which keeps the neighbour sets bit-exact
@@ -191,8 +188,7 @@ __device__ int enumerate_obs(const CalcArgs& a, int pt, int kc, double qx, doubl
             if (tid == 0) s.ictl[0] = 0;
             __syncthreads();
             for (int k = 0; k < nb; ++k) {
-                const long long b0 = glob ? ti.pos_begin : a.bstart[bk[k]];
-                const long long b1 = glob ? ti.pos_end : a.bstart[bk[k] + 1];
+                long long b0 = a.bstart[bk[k]], b1 = a.bstart[bk[k] + 1];
                 for (long long base = b0; base < b1; base += CALC_NT) {
                     long long p = base + tid;
                     bool in = false;
@@ -217,7 +213,6 @@ __device__ int enumerate_obs(const CalcArgs& a, int pt, int kc, double qx, doubl
                             if (cut_on && in) in = keeps_cut(d2, a.sid[p], a.cut + (size_t)t * a.npts + pt);
                         }
                     }
-                    if (glob) in = p < b1;
                     unsigned bal = __ballot_sync(0xffffffffu, in);
                     if (lane == 0) wsum[wid] = __popc(bal);
                     __syncthreads();
@@ -232,10 +227,7 @@ __device__ int enumerate_obs(const CalcArgs& a, int pt, int kc, double qx, doubl
                     if (in) {
                         int pos = n0 + before + __popc(bal & ((1u << lane) - 1));
                         s.lid[pos] = (int)p;
-                        if (glob) {
-                            if constexpr (FAST) llcf[pos] = 1.0f;
-                            else s.llc[pos] = 1.0;
-                        } else if constexpr (SEARCH == 2)
+                        if constexpr (SEARCH == 2)
                             llcf[pos] = exact::calclcoeff_df(ti, d2f, d2l);
                         else if constexpr (SEARCH == 1)
                             llcf[pos] = exact::calclcoeff_f(ti.nlocrad, ti.locrad, ti.locweight, d2);

@@ -718,16 +718,6 @@ __device__ __forceinline__ void neighbour_ranges(const CalcArgs& a, const TypeIn
                                                  double qz, long long* sb0, int* scum)
 {
     const int lane = threadIdx.x & 31, ndim = a.ndim;
-    if (isnan(qx + qy)) {
-        // no coordinates (a grid of type NONE): the type's whole range
-        if (lane == 0) {
-            sb0[0] = t.pos_begin;
-            scum[0] = 0;
-            scum[1] = t.pos_end - t.pos_begin;
-            scum[28] = 1;
-        }
-        return;
-    }
     const double fx = floor((qx - t.x0) * t.inv_cell), fy = floor((qy - t.y0) * t.inv_cell);
     const double fz = ndim == 3 ? floor((qz - t.z0) * t.inv_cell) : 0.0;
     bool inside = fx >= -1.0 && fx <= (double)t.ncx && fy >= -1.0 && fy <= (double)t.ncy;
@@ -785,9 +775,6 @@ __device__ int enumerate_obs_seg(const CalcArgs& a, int pt, int lseg, double qx,
 {
     const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
     int total = 0;
-    // a point without coordinates (a grid of type NONE) takes every
-    // observation with coefficient 1 (obs_getglobal, observations.c:1773-1817)
-    const bool glob = isnan(qx + qy);
     for (int t = 0; t < a.ntypes; ++t) {
         const TypeIndex& ti = a.types[t];
         int n = 0;   // list entries (the same in every thread)
@@ -859,7 +846,6 @@ __device__ int enumerate_obs_seg(const CalcArgs& a, int pt, int lseg, double qx,
                         if (cut_on && in) in = keeps_cut(d2, a.sid[p], a.cut + (size_t)t * a.npts + pt);
                     }
                 }
-                if (glob) in = p >= 0;
                 const unsigned bal = __ballot_sync(0xffffffffu, in);
                 if (lane == 0) wsum[wid] = __popc(bal);
                 __syncthreads();
@@ -873,9 +859,7 @@ __device__ int enumerate_obs_seg(const CalcArgs& a, int pt, int lseg, double qx,
                 if (in) {
                     const int pos = n + before + __popc(bal & ((1u << lane) - 1));
                     lid[pos] = (int)p;
-                    if (glob)
-                        lcf[pos] = 1.0f;
-                    else if constexpr (SEARCH == 2)
+                    if constexpr (SEARCH == 2)
                         lcf[pos] = exact::calclcoeff_df(ti, d2f, d2l);
                     else
                         lcf[pos] = exact::calclcoeff_f(ti.nlocrad, ti.locrad, ti.locweight, d2);

@@ -651,15 +651,11 @@ __global__ void k_count_local(int npts, int ntypes, int ndim, const TypeIndex* _
     int lane = threadIdx.x & 31;
     if (pt >= npts) return;
     double x = qx[pt], y = qy[pt], z = ndim == 3 ? qz[pt] : 0.0;
-    // no coordinates (a grid of type NONE): every observation (obs_getglobal)
-    const bool glob = isnan(x + y);
     int total = 0;
     for (int t = 0; t < ntypes; ++t) {
         const TypeIndex& ti = types[t];
         int nt = 0;
-        if (glob) {
-            nt = ti.pos_end - ti.pos_begin;
-        } else if (ti.pos_end > ti.pos_begin) {
+        if (ti.pos_end > ti.pos_begin) {
             const bool cut_on = cut != nullptr && ti.nlobsmax > 0;
             CutKey ck{};
             if (cut_on) ck = cut[(size_t)t * npts + pt];
@@ -703,10 +699,6 @@ __global__ void k_count_candidates(int npts, int ntypes, int ndim, const TypeInd
     for (int t = 0; t < ntypes; ++t) {
         const TypeIndex& ti = types[t];
         if (ti.pos_end <= ti.pos_begin) continue;
-        if (isnan(x + y)) {   // no coordinates: every observation
-            total += ti.pos_end - ti.pos_begin;
-            continue;
-        }
         long long bk[27];
         const int nb = neighbour_buckets(ti, ndim, x, y, z, bk);
         for (int k = 0; k < nb; ++k) total += bstart[bk[k] + 1] - bstart[bk[k]];
@@ -762,8 +754,6 @@ __global__ void __launch_bounds__(LIST_T) k_list_local(int npts, int ntypes, int
     int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     if (threadIdx.x == 0) n_sh = 0;
     __syncthreads();
-    // no coordinates (a grid of type NONE): every observation, coefficient 1
-    const bool glob = isnan(x + y);
     for (int t = 0; t < ntypes; ++t) {
         const TypeIndex& ti = types[t];
         if (ti.pos_end <= ti.pos_begin) continue;
@@ -771,17 +761,14 @@ __global__ void __launch_bounds__(LIST_T) k_list_local(int npts, int ntypes, int
         CutKey ck{};
         if (cut_on) ck = cut[(size_t)t * npts + pt];
         long long bk[27];
-        const int nb = glob ? 1 : neighbour_buckets(ti, ndim, x, y, z, bk);
+        int nb = neighbour_buckets(ti, ndim, x, y, z, bk);
         for (int k = 0; k < nb; ++k) {
-            const long long b0 = glob ? ti.pos_begin : bstart[bk[k]];
-            const long long b1 = glob ? ti.pos_end : bstart[bk[k] + 1];
+            long long b0 = bstart[bk[k]], b1 = bstart[bk[k] + 1];
             for (long long base = b0; base < b1; base += LIST_T) {
                 long long p = base + threadIdx.x;
                 bool in = false;
                 double d2 = 0.0;
-                if (p < b1 && glob) {
-                    in = true;
-                } else if (p < b1) {
+                if (p < b1) {
                     d2 = ndim == 2 ? exact::dist2(sx[p], sy[p], x, y) : exact::dist3(sx[p], sy[p], sz[p], x, y, z);
                     in = d2 <= ti.rmax2;
                     if (cut_on && in) in = cut_keeps(d2, sid[p], ck);
@@ -797,7 +784,7 @@ __global__ void __launch_bounds__(LIST_T) k_list_local(int npts, int ntypes, int
                 int pos = n_sh + before + __popc(bal & ((1u << lane) - 1));
                 if (in && pos < LIST_CAP) {
                     kid[pos] = sid[p];
-                    kc[pos] = glob ? 1.0 : exact::calclcoeff(ti.nlocrad, ti.locrad, ti.locweight, __dsqrt_rn(d2));
+                    kc[pos] = exact::calclcoeff(ti.nlocrad, ti.locrad, ti.locweight, __dsqrt_rn(d2));
                 }
                 __syncthreads();
                 if (threadIdx.x == 0) n_sh += tot;
@@ -906,9 +893,7 @@ __global__ void __launch_bounds__(CUT_T) k_cut_local(int npts, int ntypes, int n
         res.d2 = __longlong_as_double(0x7ff0000000000000ll);   // +inf: keep all
         res.id = 0x7fffffff;
         res.pad = 0;
-        if (ti.nlobsmax <= 0 || ti.pos_end <= ti.pos_begin || isnan(x + y)) {
-            // (a point without coordinates takes every observation: no limit,
-            // as obs_getglobal applies none)
+        if (ti.nlobsmax <= 0 || ti.pos_end <= ti.pos_begin) {
             if (tid == 0) cut[(size_t)t * npts + pt] = res;
             continue;
         }

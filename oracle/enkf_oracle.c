@@ -315,8 +315,7 @@ double or_calclcoeff(int nlocrad, const double* locrad, const double* locweight,
 }
 
 /* obs_findlocal (observations.c:1837-1927); domains are not modelled (every
- * type is visible from the single grid; a hidden type is modelled by its
- * observations' status). */
+ * type is visible from the single grid). */
 int or_findlocal(const or_obsset* o, double lon, double lat, int* ids, double* lcoeffs, int cap)
 {
     double q[3];
@@ -325,24 +324,6 @@ int or_findlocal(const or_obsset* o, double lon, double lat, int* ids, double* l
     size_t* stack = NULL;
     int t, n = 0, overflow = 0;
 
-    if (isnan(lon + lat)) {
-        /* obs_getglobal (observations.c:1773-1817): a point without
-         * coordinates (grid type NONE) takes every observation of every
-         * type, in the type's id order, with coefficient 1 */
-        for (t = 0; t < o->ntypes; ++t) {
-            int i;
-
-            for (i = 0; i < o->nobs_t[t]; ++i) {
-                if (n < cap) {
-                    ids[n] = o->obsids[t][i];
-                    lcoeffs[n] = 1.0;
-                } else
-                    overflow = 1;
-                n++;
-            }
-        }
-        return overflow ? -n : n;
-    }
     if (o->geographic) {
         double ll[2] = { lon, lat };
 

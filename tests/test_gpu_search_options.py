@@ -181,61 +181,3 @@ def test_obstype_domains_hide_a_type(octx, prec):
     out = ctx.calctransforms(mode=0, scheme=1, path=1, precision=prec, want64=True, want_diag=False)
     assert per_point_rel(out["T64"], ref_all["T64"]) < tol
     assert per_point_rel(out["w64"], ref_all["w64"]) < tol
-
-
-@pytest.mark.parametrize("prec", [0, 1])
-def test_points_without_coordinates(octx, prec):
-    """Points of a grid of type NONE (no coordinates: NaN) take every
-    observation of every visible type with coefficient 1 (obs_getglobal,
-    observations.c:1773-1817), beside ordinary points; NLOBSMAX does not apply
-    to them; a hidden type stays out."""
-    ctx = octx
-    rng = np.random.default_rng(21)
-    n, m = 900, 24
-    lon = rng.uniform(0, 40, n).astype(np.float32)
-    lat = rng.uniform(0, 30, n).astype(np.float32)
-    otype = (rng.uniform(size=n) < 0.4).astype(np.int16)
-    status = np.zeros(n, np.int16)
-    status[::23] = 1
-    HE = (15.0 + rng.standard_normal((m, n))).astype(np.float32)
-    value = (15.0 + rng.standard_normal(n)).astype(np.float32)
-    estd = rng.uniform(0.3, 0.8, n).astype(np.float32)
-    S, s_f, _ = oracle.calcinnandspread(HE, value, status)
-    S, s = oracle.standardise(S, s_f, estd, otype, np.ones(2))
-    nl, lr, lw = oracle.locrad_table(2, [[6.0], [9.0]])
-    px = rng.uniform(0, 40, 12)
-    py = rng.uniform(0, 30, 12)
-    px[[2, 7]] = np.nan
-    py[[2, 7, 9]] = np.nan
-    x2d, y2d = px[None, :], py[None, :]
-    ctx.set_obstypes(nl, lr, lw, np.ones(2))
-    ctx.set_obs(lon, lat, otype, status, estd, value)
-    ctx.set_S(S, s, m)
-    ctx.set_grid(x2d=x2d, y2d=y2d, stride=1)
-    tol = 1e-10 if prec == 0 else 1e-5
-    for hidden in (None, 1):
-        st = status.copy()
-        if hidden is not None:
-            st[otype == hidden] = 1
-            ctx.set_obstype_visible(np.array([1, 0]))
-        for nmax in (None, (5, 5)):
-            ctx.set_obstype_nlobsmax(None if nmax is None else np.array(nmax))
-            obs = oracle.ObsSet(lon, lat, otype, st, 2, nl, lr, lw,
-                                nlobsmax=None if nmax is None else np.array(nmax))
-            ref = oracle.calctransforms(obs, mode=0, scheme=1, nmem=m, nmem_dynamic=m, alpha=1.0, stride=1, x=px,
-                                        y=py, S=S, s=s, want64=True, x2d=x2d, y2d=y2d)
-            nan_pts = [2, 7, 9]
-            assert all(ref["nlobs"][0, k] == (st == 0).sum() for k in nan_pts)
-            counts, offsets, ids, coeffs = ctx.findlocal(lists=True)
-            for k in range(12):
-                rid, rlc = obs.findlocal(px[k], py[k])
-                order = np.argsort(rid, kind="stable")
-                assert np.array_equal(ids[offsets[k]:offsets[k + 1]], rid[order]), (hidden, nmax, k)
-                assert np.array_equal(coeffs[offsets[k]:offsets[k + 1]], rlc[order]), (hidden, nmax, k)
-            for path in ((0, 1) if prec == 0 else (1,)):
-                out = ctx.calctransforms(mode=0, scheme=1, alpha=1.0, path=path, precision=prec, want64=True,
-                                         want_diag=(path == 0))
-                if path == 0:
-                    assert np.array_equal(out["nlobs"], ref["nlobs"])
-                assert per_point_rel(out["T64"], ref["T64"]) < tol, (hidden, nmax, path)
-                assert per_point_rel(out["w64"], ref["w64"]) < tol, (hidden, nmax, path)

@@ -80,26 +80,6 @@ def test_nlobsmax_against_reference_golden(nmax):
         assert cut > 0
 
 
-def test_findlocal_without_coordinates_takes_everything():
-    """obs_getglobal (observations.c:1773-1817): a point whose coordinates are
-    NaN (grid type NONE) takes every observation with status OK, type by
-    type in id order, coefficient 1, whatever NLOBSMAX says."""
-    rng = np.random.default_rng(3)
-    n = 300
-    lon = rng.uniform(0, 10, n).astype(np.float32)
-    lat = rng.uniform(0, 10, n).astype(np.float32)
-    ot = (rng.uniform(size=n) < 0.5).astype(np.int16)
-    st = np.zeros(n, np.int16)
-    st[::7] = 1
-    nl, lr, lw = oracle.locrad_table(2, [[2.0], [3.0]])
-    for nmax in (None, np.array([3, 3])):
-        obs = oracle.ObsSet(lon, lat, ot, st, 2, nl, lr, lw, nlobsmax=nmax)
-        ids, lc = obs.findlocal(float("nan"), 5.0)
-        want = np.concatenate([np.nonzero((ot == t) & (st == 0))[0] for t in range(2)])
-        assert np.array_equal(ids, want)
-        assert np.all(lc == 1.0)
-
-
 def test_addnoise_against_reference_golden():
     """RANDOMISE: the oracle's addnoise of the reference's plain update equals
     the reference's randomised update bit for bit (tests/golden/addnoise.npz,
