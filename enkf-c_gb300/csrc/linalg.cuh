@@ -172,6 +172,12 @@ __device__ int tql2(F* A, int n, int lda, F* d, F* e, F* cs, F* sn, int* ctl)
     if (tid == 0) ctl[3] = 0;
     __syncthreads();
     for (int l = 0; l < n; ++l) {
+        // the step that ends a sweep leaves the loop below before its
+        // closing barrier: every thread must have read that step's control
+        // words before thread 0 writes the next sweep's, or a late thread
+        // would take the new words for the old sweep and fall out of step
+        // with the block's barriers
+        __syncthreads();
         int iter = 0;
         for (;;) {
             if (tid == 0) {
@@ -251,7 +257,9 @@ __device__ int tql2(F* A, int n, int lda, F* d, F* e, F* cs, F* sn, int* ctl)
             __syncthreads();
         }
     }
-    return ctl[3];
+    const int rc = ctl[3];
+    __syncthreads();   // every thread has its status before the caller reuses ctl
+    return rc;
 }
 
 // A: n x n, row stride lda, symmetric (both triangles valid on entry).

@@ -50,6 +50,9 @@ def test_status_strings_and_errors_without_device(lib):
     # calls on a NULL context fail cleanly
     assert lib.enkfg_standardise(None) == 1
     assert lib.enkfg_set_grid(None, None) == 1
+    assert lib.enkfg_set_obstype_nlobsmax(None, 1, None) == 1
+    assert lib.enkfg_set_obstype_visible(None, 1, None) == 1
+    assert lib.enkfg_set_field_noise(None, 0, 0, None, None, None) == 1
 
 
 def test_plain_c_client(tmp_path):
