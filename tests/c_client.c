@@ -48,10 +48,16 @@ int main(int argc, char** argv)
     st = enkfg_nc_inq_var(argv[1], "nope", NULL, NULL, NULL, NULL);
     CHECK(st == ENKFG_EINVAL && strstr(enkfg_nc_last_error(), "nope") != NULL, "missing variable is an error");
 
+    /* the per-type search options and RANDOMISE: a NULL context is refused */
+    CHECK(enkfg_set_obstype_nlobsmax(NULL, 1, NULL) == ENKFG_EINVAL, "nlobsmax without a context");
+    CHECK(enkfg_set_obstype_visible(NULL, 1, NULL) == ENKFG_EINVAL, "visibility without a context");
+    CHECK(enkfg_set_field_noise(NULL, 0, 0, NULL, NULL, NULL) == ENKFG_EINVAL, "noise without a context");
+
     /* a context: ENKFG_OK on a GPU machine, an error status (not an abort) without one */
     st = enkfg_create(0, &ctx);
     if (st == ENKFG_OK) {
         CHECK(enkfg_set_obs(ctx, 1, NULL, NULL, NULL, NULL, NULL, NULL) == ENKFG_ESTATE, "call order is checked");
+        CHECK(enkfg_set_obstype_nlobsmax(ctx, 1, NULL) == ENKFG_ESTATE, "nlobsmax needs the obs types");
         enkfg_destroy(ctx);
     } else {
         CHECK(ctx == NULL || st != ENKFG_OK, "failed creation");
