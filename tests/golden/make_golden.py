@@ -15,7 +15,9 @@ GPU library without needing the reference at test time:
                   sort obs_findlocal asks for when NLOBSMAX is set), in the
                   order the reference returns, for two observation types
                   whose observations come partly in groups at one position
-                  (profiles: equal distances), at grid and off-grid queries.
+                  (profiles: equal distances), at grid and off-grid queries;
+                  in 2-D and on the sphere (3-D trees of the reference's
+                  ll2xyz coordinates).
   transforms.npz  das_calctransforms on a sample of workload-1 points: local
                   obs from the reference kd-tree, taper and gather as
                   transforms.c:1250-1258 (restated here), numerics from the
@@ -121,6 +123,19 @@ def nlobsmax_obs(seed=5):
     return lon, lat, ot, qs
 
 
+def ref_xyz(lon, lat):
+    """ll2xyz of the reference's own utils.c for each (lon, lat)."""
+    import ctypes as C
+    R = oracle.reflib_utils()
+    out = np.zeros((len(lon), 3))
+    for i, (x, y) in enumerate(zip(lon, lat)):
+        ll = (C.c_double * 2)(float(x), float(y))
+        v = (C.c_double * 3)()
+        R.ll2xyz(ll, v)
+        out[i] = list(v)
+    return out
+
+
 def nlobsmax():
     lon, lat, ot, qs = nlobsmax_obs()
     coords = np.stack([lon.astype(np.float64), lat.astype(np.float64)], 1)
@@ -133,8 +148,24 @@ def nlobsmax():
             d, d2 = tree.range(q, r[t], ordered=True)
             out[f"t{t}_q{k}_ids"] = ids[d].astype(np.int32)
             out[f"t{t}_q{k}_d2"] = d2
+    # the same layout as degrees on the sphere (GEOGRAPHIC 1): 3-D trees of
+    # the reference's ll2xyz coordinates, radii in km
+    glon = (150.0 + 0.5 * lon).astype(np.float32)
+    glat = (-10.0 + 0.5 * lat).astype(np.float32)
+    gq = np.stack([150.0 + 0.5 * qs[:, 0], -10.0 + 0.5 * qs[:, 1]], 1)
+    gr = np.array([450.0, 600.0])
+    out.update(g_lon=glon, g_lat=glat, g_q=gq, g_r=gr)
+    gxyz = ref_xyz(glon.astype(np.float64), glat.astype(np.float64))
+    qxyz = ref_xyz(gq[:, 0], gq[:, 1])
+    for t in range(2):
+        ids = np.nonzero(ot == t)[0]
+        tree = oracle.RefKdTree(gxyz[ids])
+        for k in range(len(gq)):
+            d, d2 = tree.range(qxyz[k], gr[t], ordered=True)
+            out[f"g_t{t}_q{k}_ids"] = ids[d].astype(np.int32)
+            out[f"g_t{t}_q{k}_d2"] = d2
     np.savez_compressed(os.path.join(HERE, "nlobsmax.npz"), **out)
-    print("nlobsmax:", lon.size, "obs,", len(qs), "queries")
+    print("nlobsmax:", lon.size, "obs,", len(qs), "queries (2-D and on the sphere)")
 
 
 def transforms():

@@ -80,6 +80,22 @@ def test_nlobsmax_against_reference_golden(nmax):
         assert cut > 0
 
 
+@pytest.mark.parametrize("nmax", [(1, 1), (7, 3), (25, 40)])
+def test_nlobsmax_on_the_sphere_against_reference_golden(nmax):
+    """NLOBSMAX with GEOGRAPHIC 1: the oracle's 3-D search against the
+    reference's distance-sorted kd search on the reference's own ll2xyz
+    coordinates (radii in km)."""
+    g = np.load(os.path.join(GOLD, "nlobsmax.npz"))
+    nl, lr, lw = oracle.locrad_table(2, [[float(r)] for r in g["g_r"]])
+    n = g["g_lon"].size
+    obs = oracle.ObsSet(g["g_lon"], g["g_lat"], g["otype"], np.zeros(n, np.int16), 2, nl, lr, lw,
+                        nlobsmax=np.array(nmax), geographic=True)
+    for k, q in enumerate(g["g_q"]):
+        ids, _ = obs.findlocal(q[0], q[1])
+        ref = [g[f"g_t{t}_q{k}_ids"][:nmax[t]] for t in range(2)]
+        assert np.array_equal(ids, np.concatenate(ref)), k
+
+
 def test_addnoise_against_reference_golden():
     """RANDOMISE: the oracle's addnoise of the reference's plain update equals
     the reference's randomised update bit for bit (tests/golden/addnoise.npz,
