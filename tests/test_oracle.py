@@ -311,6 +311,40 @@ def test_finish_HE_semantics():
     assert nbad == 0 and st2[5] == 0
 
 
+@pytest.mark.skipif(oracle.reflib() is None, reason="reference library not built here")
+def test_traceprod_equals_reference_build():
+    """The diagnostics' traceprod (calc/calcs.c:41-97): the oracle's, on
+    contiguous blocks, equals the reference's compiled one bit for bit in the
+    compact form (dfs, srf) and in the row-pointer form the per-type pdfs and
+    psrf use (transforms.c:1330-1335), for the operand orders those use."""
+    import ctypes as C
+    L, R = oracle.lib(), oracle.reflib()
+    L.or_traceprod.restype = C.c_double
+    L.or_traceprod.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p]
+    R.traceprod.restype = C.c_double
+    R.traceprod.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_int]
+    rng = np.random.default_rng(12)
+    for (p, m) in [(7, 24), (60, 24), (300, 48), (5, 96)]:
+        G = rng.standard_normal((p, m))        # G[o][e]
+        S = rng.standard_normal((m, p))        # S[e][o]
+        # dfs = traceprod(0, 0, p, m, G, S), srf: traceprod(0, 1, m, p, S, S)
+        for ta, tb, mm, nn, A, B in ((0, 0, p, m, G, S), (0, 1, m, p, S, S)):
+            want = L.or_traceprod(ta, tb, mm, nn, A.ctypes.data, B.ctypes.data)
+            ra, rb = oracle._rows(A, C.c_double), oracle._rows(B, C.c_double)
+            assert R.traceprod(ta, tb, mm, nn, ra, rb, 1) == want
+        # a type's sub-block in the row-pointer form: rows of G from o0,
+        # member rows of S from column o0 (a wider matrix underneath)
+        o0, q = p // 3, max(1, p // 2)
+        Gw, Sw = rng.standard_normal((p + 4, m)), rng.standard_normal((m, p + 9))
+        pG = Gw[o0:o0 + q]
+        pS = Sw[:, o0:o0 + q]
+        gr = (C.c_void_p * q)(*[Gw.ctypes.data + (o0 + i) * Gw.strides[0] for i in range(q)])
+        sr = (C.c_void_p * m)(*[Sw.ctypes.data + e * Sw.strides[0] + o0 * 8 for e in range(m)])
+        cG, cS = np.ascontiguousarray(pG), np.ascontiguousarray(pS)
+        assert R.traceprod(0, 0, q, m, gr, sr, 0) == L.or_traceprod(0, 0, q, m, cG.ctypes.data, cS.ctypes.data)
+        assert R.traceprod(0, 1, m, q, sr, sr, 0) == L.or_traceprod(0, 1, m, q, cS.ctypes.data, cS.ctypes.data)
+
+
 @pytest.mark.skipif(oracle.reflib_utils() is None, reason="reference library not built here")
 def test_ll2xyz_equals_reference_build():
     import ctypes as C
