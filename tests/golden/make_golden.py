@@ -23,6 +23,11 @@ GPU library without needing the reference at test time:
                   transforms.c:1250-1258 (restated here), numerics from the
                   reference's calcs.c: double T and w before the float cast.
                   The inputs (obs, S, s) are stored alongside.
+  transforms_multitype.npz
+                  the same for a two-type workload with rejected
+                  observations (ENKF DEnKF and ETKF, EnOI; alpha 0.7), with
+                  the diagnostics dfs, srf and per-type pdfs, psrf through
+                  the reference's traceprod.
   model2obs.npz   interpolate2d_structured / interpolate3d_structured
                   (common/utils.c, from oracle/_ref/libenkf_ref_utils.so) on
                   seeded fields, wet-level counts, OFFSET data and positions
@@ -208,6 +213,98 @@ def transforms():
     print("transforms:", pts.size, "points, mean p", nl.mean())
 
 
+def ref_traceprod(ta, tb, m, n, A, B, compact=True):
+    """traceprod of the reference's calcs.c; A and B row-major blocks, or
+    (compact False) lists of row addresses."""
+    import ctypes as C
+    R = oracle.reflib()
+    R.traceprod.restype = C.c_double
+    R.traceprod.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_int]
+    ra = oracle._rows(A, C.c_double) if compact else A
+    rb = oracle._rows(B, C.c_double) if compact else B
+    return R.traceprod(ta, tb, m, n, ra, rb, 1 if compact else 0)
+
+
+def transforms_multitype():
+    """das_calctransforms on a sample of points of a two-type workload with
+    rejected observations, with the diagnostics of transforms.c:1298-1345:
+    local obs from the reference kd-trees (type by type, tree order), the
+    reference's taper_gc, calcs.c for w, T and G, relaxation alpha = 0.7,
+    then dfs/srf and per-type pdfs/psrf through the reference's traceprod
+    (the per-type ones in its row-pointer form), with the float stores of
+    the reference's diagnostic arrays."""
+    import ctypes as C
+    w = synth.make(2, scale=0.1, nobs=6000, with_fields=False, nmem=20)
+    st = w.status.copy()
+    st[::17] = 1
+    S, s_f, _ = oracle.calcinnandspread(w.HE, w.value, st)
+    S, s = oracle.standardise(S, s_f, w.estd, w.otype, np.ones(w.ntypes))
+    m, alpha = w.nmem, 0.7
+    radius = np.array([6.0, 9.0])
+    coords = np.stack([w.lon.astype(np.float64), w.lat.astype(np.float64)], 1)
+    trees, tids = [], []
+    for t in range(w.ntypes):
+        ids = np.nonzero((w.otype == t) & (st == 0))[0]
+        tids.append(ids)
+        trees.append(oracle.RefKdTree(coords[ids]))
+    rng = np.random.default_rng(13)
+    npts = w.nanalyses
+    pts = np.sort(rng.choice(npts, 120, replace=False))
+    out = dict(lon=w.lon, lat=w.lat, otype=w.otype, status=st, S=S, s=s, x=w.x, y=w.y, radius=radius,
+               stride=np.array(w.stride), pts=pts, alpha=np.array(alpha))
+    for mode, scheme, name in ((0, 0, "denkf"), (0, 1, "etkf"), (1, 0, "enoi")):
+        T64 = np.zeros((pts.size, m, m))
+        w64 = np.zeros((pts.size, m))
+        diag = np.zeros((pts.size, 3))              # nlobs, dfs, srf (the stored floats)
+        pdiag = np.zeros((pts.size, w.ntypes, 3))   # pnlobs, pdfs, psrf
+        for k, pt in enumerate(pts):
+            jj, ii = divmod(int(pt), w.ni_s)
+            q = np.array([w.x[ii * w.stride], w.y[jj * w.stride]])
+            lobs, lc, lt = [], [], []
+            for t in range(w.ntypes):
+                d, d2 = trees[t].range(q, radius[t])
+                lobs += list(tids[t][d])
+                lc += [oracle.ref_taper_gc(np.sqrt(v) / radius[t]) for v in d2]
+                lt += [t] * d.size
+            p = len(lobs)
+            if p == 0:
+                T64[k] = np.eye(m)
+                continue
+            lobs, lc = np.array(lobs), np.array(lc)
+            Sloc = np.ascontiguousarray(S[:, lobs].astype(np.float64) * lc[None, :])
+            sloc = s[lobs] * lc
+            ww, T, G = oracle.ref_calc_wT(mode, scheme, m, m, sloc, Sloc)
+            if mode != 1:
+                for e1 in range(m):
+                    T[e1, e1] -= 1.0
+                    T[e1, :] *= alpha
+                    T[e1, e1] += 1.0
+                T64[k] = T
+            w64[k] = ww
+            G = np.ascontiguousarray(G)
+            dfs = np.float32(ref_traceprod(0, 0, p, m, G, Sloc))
+            srf = np.float32(np.sqrt(ref_traceprod(0, 1, m, p, Sloc, Sloc) / float(dfs)) - 1.0)
+            diag[k] = [p, dfs, srf]
+            lt = np.array(lt)
+            for t in range(w.ntypes):
+                sel = np.nonzero(lt == t)[0]
+                if sel.size == 0:
+                    continue
+                o0, pq = int(sel[0]), sel.size
+                gr = (C.c_void_p * pq)(*[G.ctypes.data + (o0 + i) * G.strides[0] for i in range(pq)])
+                sr = (C.c_void_p * m)(*[Sloc.ctypes.data + e * Sloc.strides[0] + o0 * 8 for e in range(m)])
+                pdfs = np.float32(ref_traceprod(0, 0, pq, m, gr, sr, compact=False))
+                psrf = np.float32(np.sqrt(ref_traceprod(0, 1, m, pq, sr, sr, compact=False) / float(pdfs)) - 1.0) \
+                    if float(pdfs) > 1.0e-6 else np.float32(0.0)
+                pdiag[k, t] = [pq, pdfs, psrf]
+        out[f"{name}_T64"] = T64
+        out[f"{name}_w64"] = w64
+        out[f"{name}_diag"] = diag
+        out[f"{name}_pdiag"] = pdiag
+    np.savez_compressed(os.path.join(HERE, "transforms_multitype.npz"), **out)
+    print("transforms_multitype:", pts.size, "points")
+
+
 def model2obs():
     rng = np.random.default_rng(20250)
     ni, nj, nk, m, n = 23, 17, 5, 3, 600
@@ -370,7 +467,9 @@ if __name__ == "__main__":
     oracle.build()
     if oracle.reflib() is None or oracle.reflib_utils() is None or oracle.reflib_update() is None:
         sys.exit("the reference libraries under oracle/_ref could not be built")
-    which = sys.argv[1:] or ["numerics", "kdtree", "nlobsmax", "transforms", "model2obs", "update", "addnoise"]
+    which = sys.argv[1:] or ["numerics", "kdtree", "nlobsmax", "transforms", "transforms_multitype", "model2obs",
+                             "update", "addnoise"]
     for name in which:
         {"numerics": numerics, "kdtree": kdtree, "nlobsmax": nlobsmax, "transforms": transforms,
-         "model2obs": model2obs, "update": update, "addnoise": addnoise}[name]()
+         "transforms_multitype": transforms_multitype, "model2obs": model2obs, "update": update,
+         "addnoise": addnoise}[name]()

@@ -96,6 +96,46 @@ def test_nlobsmax_on_the_sphere_against_reference_golden(nmax):
         assert np.array_equal(ids, np.concatenate(ref)), k
 
 
+@pytest.mark.parametrize("case", [(0, 0, "denkf"), (0, 1, "etkf"), (1, 0, "enoi")])
+def test_transforms_multitype_against_reference_golden(case):
+    """Two observation types, rejected observations, alpha 0.7: T and w
+    within 1e-12 of the reference's own search, taper and calcs.c, and the
+    stored diagnostics (nlobs, dfs, srf and per type pnlobs, pdfs, psrf)
+    equal to the reference's float values within one float ulp
+    (tests/golden/transforms_multitype.npz)."""
+    mode, scheme, name = case
+    g = np.load(os.path.join(GOLD, "transforms_multitype.npz"))
+    nl, lr, lw = oracle.locrad_table(2, [[float(r)] for r in g["radius"]])
+    obs = oracle.ObsSet(g["lon"], g["lat"], g["otype"], g["status"], 2, nl, lr, lw)
+    m = g["S"].shape[0]
+    out = oracle.calctransforms(obs, mode=mode, scheme=scheme, nmem=m, nmem_dynamic=m, alpha=float(g["alpha"]),
+                                stride=int(g["stride"]), x=g["x"], y=g["y"], S=g["S"], s=g["s"], want64=True,
+                                threads=8)
+    ni = out["w"].shape[1]
+    T64, w64 = g[f"{name}_T64"], g[f"{name}_w64"]
+    diag, pdiag = g[f"{name}_diag"], g[f"{name}_pdiag"]
+
+    def ulps(a, b):
+        a, b = np.float32(a), np.float32(b)
+        return abs(float(a) - float(b)) / float(np.spacing(max(abs(a), abs(b), np.float32(1e-30))))
+
+    for k, pt in enumerate(g["pts"]):
+        jj, ii = divmod(int(pt), ni)
+        if mode != 1:
+            assert rel(out["T64"][jj, ii], T64[k]) < 1e-12, (name, k)
+        if np.abs(w64[k]).max() > 0:
+            assert rel(out["w64"][jj, ii], w64[k]) < 1e-12, (name, k)
+        assert out["nlobs"][jj, ii] == diag[k, 0], (name, k)
+        if diag[k, 0] > 0:
+            assert ulps(out["dfs"][jj, ii], diag[k, 1]) <= 1, (name, k)
+            assert ulps(out["srf"][jj, ii], diag[k, 2]) <= 1, (name, k)
+        for t in range(2):
+            assert out["pnlobs"][t, jj, ii] == pdiag[k, t, 0], (name, k, t)
+            if pdiag[k, t, 0] > 0:
+                assert ulps(out["pdfs"][t, jj, ii], pdiag[k, t, 1]) <= 1, (name, k, t)
+                assert ulps(out["psrf"][t, jj, ii], pdiag[k, t, 2]) <= 1, (name, k, t)
+
+
 def test_addnoise_against_reference_golden():
     """RANDOMISE: the oracle's addnoise of the reference's plain update equals
     the reference's randomised update bit for bit (tests/golden/addnoise.npz,
