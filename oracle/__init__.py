@@ -577,6 +577,54 @@ def finish_HE(HE, status, *, mode, nmem_dynamic, gamma=0.0, Hx=None, skip_bad=Fa
 # (common/dasystem.c), compiled unmodified (oracle/ref/ref_update.c)
 # ---------------------------------------------------------------------------
 
+REFLIB_ENSOBS = os.path.join(HERE, "_ref", "libenkf_ref_ensobs.so")
+_refeo = None
+
+
+def reflib_ensobs():
+    """libenkf_ref_ensobs.so (the reference's calc/ensobs.c), or None where
+    it is not built."""
+    global _refeo
+    with _lock:
+        if _refeo is None and os.path.exists(REFLIB_ENSOBS):
+            L = C.CDLL(REFLIB_ENSOBS)
+            L.ref_calcinnandspread.argtypes = [C.c_int, C.c_int] + [C.c_void_p] * 5
+            L.ref_standardise.argtypes = [C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int,
+                                          C.c_void_p]
+            _refeo = L
+    return _refeo
+
+
+def ref_calcinnandspread(HE, value, status):
+    """das_calcinnandspread of the reference itself: (S = HA, s_f, std_f)."""
+    L = reflib_ensobs()
+    if L is None:
+        raise RuntimeError("reference ensobs library not built")
+    S = np.ascontiguousarray(HE, np.float32).copy()
+    m, n = S.shape
+    v = np.ascontiguousarray(value, np.float32)
+    st = np.ascontiguousarray(status, np.int16)
+    s_f = np.zeros(n)
+    std_f = np.zeros(n)
+    L.ref_calcinnandspread(m, n, S.ctypes.data, v.ctypes.data, st.ctypes.data, s_f.ctypes.data, std_f.ctypes.data)
+    return S, s_f, std_f
+
+
+def ref_standardise(S, s_f, estd, otype, rfactor):
+    """das_standardise of the reference itself: (S, s) standardised."""
+    L = reflib_ensobs()
+    if L is None:
+        raise RuntimeError("reference ensobs library not built")
+    S = np.ascontiguousarray(S, np.float32).copy()
+    s = np.ascontiguousarray(s_f, np.float64).copy()
+    m, n = S.shape
+    e = np.ascontiguousarray(estd, np.float32)
+    t = np.ascontiguousarray(otype, np.int16)
+    rf = np.ascontiguousarray(rfactor, np.float64)
+    L.ref_standardise(m, n, S.ctypes.data, s.ctypes.data, e.ctypes.data, t.ctypes.data, rf.size, rf.ctypes.data)
+    return S, s
+
+
 REFLIB_UPDATE = os.path.join(HERE, "_ref", "libenkf_ref_update.so")
 _refup = None
 

@@ -1,7 +1,8 @@
 /*
  * netcdf.h stand-in for compiling the reference's common/utils.c (which
  * includes common/ncw.h) into oracle/_ref/libenkf_ref_utils.so, and
- * update/update.c + common/dasystem.c into libenkf_ref_update.so.  TEST
+ * update/update.c + common/dasystem.c into libenkf_ref_update.so, and
+ * calc/ensobs.c into libenkf_ref_ensobs.so.  TEST
  * INFRASTRUCTURE ONLY.  Declares the handful of names the headers and
  * these files mention; nothing of NetCDF is called by the functions the
  * tests use (interpolation, taper, field update, hybrid ensemble).
@@ -30,4 +31,10 @@ typedef int nc_type;
 #define NC_DOUBLE 6
 #define NC_CHUNKED 0
 #define NC_CONTIGUOUS 1
+#define NC_NOFILL 0x100
+#define NC_UINT 9
+#define NC_INT64 10
+#define NC_UINT64 11
+#define NC_UBYTE 7
+#define NC_USHORT 8
 #endif

@@ -385,6 +385,35 @@ def test_traceprod_equals_reference_build():
         assert R.traceprod(0, 1, m, q, sr, sr, 0) == L.or_traceprod(0, 1, m, q, cS.ctypes.data, cS.ctypes.data)
 
 
+@pytest.mark.skipif(oracle.reflib_ensobs() is None, reason="reference library not built here")
+@pytest.mark.parametrize("m,n", [(24, 3000), (96, 5000), (7, 40)])
+def test_innovations_and_standardise_equal_reference_build(m, n):
+    """das_calcinnandspread and das_standardise (calc/ensobs.c:541-690,
+    849-898, compiled unmodified): the oracle's S, s_f, std_f and the
+    standardised S and s equal the reference's bit for bit, with rejected
+    observations (their s_f and std_f stay the ensemble mean and the sum of
+    squares, as the reference leaves them) and three types of different
+    rfactor."""
+    rng = np.random.default_rng(m + n)
+    HE = (15.0 + rng.standard_normal((m, n)) * rng.uniform(0.1, 3.0, n)).astype(np.float32)
+    value = (15.0 + rng.standard_normal(n)).astype(np.float32)
+    status = np.zeros(n, np.int16)
+    status[rng.uniform(size=n) < 0.1] = 1
+    status[rng.uniform(size=n) < 0.02] = 2
+    S0, s0, d0 = oracle.calcinnandspread(HE, value, status)
+    S1, s1, d1 = oracle.ref_calcinnandspread(HE, value, status)
+    assert np.array_equal(S0, S1)
+    assert np.array_equal(s0, s1)
+    assert np.array_equal(d0, d1)
+    estd = rng.uniform(0.2, 0.9, n).astype(np.float32)
+    otype = rng.integers(0, 3, n).astype(np.int16)
+    rfactor = np.array([1.0, 2.5, 0.7])
+    Sa, sa = oracle.standardise(S0, s0, estd, otype, rfactor)
+    Sb, sb = oracle.ref_standardise(S1, s1, estd, otype, rfactor)
+    assert np.array_equal(Sa, Sb)
+    assert np.array_equal(sa, sb)
+
+
 @pytest.mark.skipif(oracle.reflib_utils() is None, reason="reference library not built here")
 def test_ll2xyz_equals_reference_build():
     import ctypes as C
