@@ -625,6 +625,61 @@ def ref_standardise(S, s_f, estd, otype, rfactor):
     return S, s
 
 
+REFLIB_OBS = os.path.join(HERE, "_ref", "libenkf_ref_obs.so")
+_refob = None
+
+
+def reflib_obs():
+    """libenkf_ref_obs.so (the reference's obs_findlocal), or None where it
+    is not built."""
+    global _refob
+    with _lock:
+        if _refob is None and os.path.exists(REFLIB_OBS):
+            L = C.CDLL(REFLIB_OBS)
+            L.ref_findlocal.restype = C.c_longlong
+            L.ref_findlocal.argtypes = [C.c_int] + [C.c_void_p] * 4 + [C.c_int, C.c_int] + [C.c_void_p] * 5 + \
+                [C.c_int, C.c_int] + [C.c_void_p] * 5 + [C.c_longlong]
+            _refob = L
+    return _refob
+
+
+def ref_findlocal(lon, lat, otype, status, ntypes, nlocrad, locrad, locweight, qlon, qlat, nlobsmax=None,
+                  visible=None, geographic=False):
+    """obs_findlocal of the reference itself at each query (NaN: a point
+    without coordinates): a list of (ids, taper coefficients) in the
+    reference's order.  locrad, locweight: [ntypes][MAXLOCRAD]."""
+    L = reflib_obs()
+    if L is None:
+        raise RuntimeError("reference observations library not built")
+    lon = np.ascontiguousarray(lon, np.float32)
+    lat = np.ascontiguousarray(lat, np.float32)
+    ot = np.ascontiguousarray(otype, np.int16)
+    st = np.ascontiguousarray(status, np.int16)
+    nl = np.ascontiguousarray(nlocrad, np.int32)
+    lr = np.ascontiguousarray(locrad, np.float64).reshape(ntypes, -1)
+    lw = np.ascontiguousarray(locweight, np.float64).reshape(ntypes, -1)
+    nm = None if nlobsmax is None else np.ascontiguousarray(nlobsmax, np.int32)
+    vis = None if visible is None else np.ascontiguousarray(visible, np.int32)
+    qx = np.ascontiguousarray(qlon, np.float64)
+    qy = np.ascontiguousarray(qlat, np.float64)
+    nq = qx.size
+    cap = max(1, lon.size) * nq
+    counts = np.zeros(nq, np.int32)
+    ids = np.zeros(cap, np.int32)
+    lc = np.zeros(cap)
+    tot = L.ref_findlocal(lon.size, lon.ctypes.data, lat.ctypes.data, ot.ctypes.data, st.ctypes.data, ntypes,
+                          lr.shape[1], nl.ctypes.data, lr.ctypes.data, lw.ctypes.data,
+                          None if nm is None else nm.ctypes.data, None if vis is None else vis.ctypes.data,
+                          int(geographic), nq, qx.ctypes.data, qy.ctypes.data, counts.ctypes.data, ids.ctypes.data,
+                          lc.ctypes.data, cap)
+    assert tot >= 0
+    out, k0 = [], 0
+    for c in counts:
+        out.append((ids[k0:k0 + c].copy(), lc[k0:k0 + c].copy()))
+        k0 += c
+    return out
+
+
 REFLIB_UPDATE = os.path.join(HERE, "_ref", "libenkf_ref_update.so")
 _refup = None
 

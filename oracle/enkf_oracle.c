@@ -324,6 +324,24 @@ int or_findlocal(const or_obsset* o, double lon, double lat, int* ids, double* l
     size_t* stack = NULL;
     int t, n = 0, overflow = 0;
 
+    if (isnan(lon + lat)) {
+        /* obs_getglobal (observations.c:1773-1817): a point without
+         * coordinates (grid type NONE) takes every observation with status
+         * OK, type by type in id order, coefficient 1, no NLOBSMAX */
+        for (t = 0; t < o->ntypes; ++t) {
+            int i;
+
+            for (i = 0; i < o->nobs_t[t]; ++i) {
+                if (n < cap) {
+                    ids[n] = o->obsids[t][i];
+                    lcoeffs[n] = 1.0;
+                } else
+                    overflow = 1;
+                n++;
+            }
+        }
+        return overflow ? -n : n;
+    }
     if (o->geographic) {
         double ll[2] = { lon, lat };
 

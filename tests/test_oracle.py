@@ -385,6 +385,53 @@ def test_traceprod_equals_reference_build():
         assert R.traceprod(0, 1, m, q, sr, sr, 0) == L.or_traceprod(0, 1, m, q, cS.ctypes.data, cS.ctypes.data)
 
 
+@pytest.mark.skipif(oracle.reflib_obs() is None, reason="reference library not built here")
+@pytest.mark.parametrize("geographic", [False, True])
+@pytest.mark.parametrize("nlobsmax", [None, (9, 4, 30)])
+@pytest.mark.parametrize("hidden", [None, 1])
+def test_findlocal_equals_reference_build(geographic, nlobsmax, hidden):
+    """obs_findlocal (common/observations.c:1837-1927 with obstypes.c and
+    kdtree.c, compiled unmodified): ids and taper coefficients, in the
+    reference's order, equal the oracle's at every query -- three types, one
+    with two radii and weights, rejected observations, a quarter of the
+    observations in groups at one position, NLOBSMAX, a type hidden by its
+    domains (the oracle: its observations rejected) and queries without
+    coordinates (obs_getglobal)."""
+    rng = np.random.default_rng(31 + 2 * int(geographic) + (4 if nlobsmax else 0) + (8 if hidden else 0))
+    n = 2500
+    lon = rng.uniform(0, 50, n)
+    lat = rng.uniform(0, 40, n)
+    for i in rng.choice(np.arange(1, n), n // 4, replace=False):
+        j = rng.integers(0, i)
+        lon[i], lat[i] = lon[j], lat[j]
+    otype = rng.integers(0, 3, n).astype(np.int16)
+    status = np.zeros(n, np.int16)
+    status[::11] = 1
+    radii = [[4.0, 2.0], [6.0], [3.0]]
+    if geographic:
+        lon, lat = 140.0 + 0.4 * lon, -20.0 + 0.4 * lat
+        radii = [[180.0, 90.0], [260.0], [130.0]]
+    lon, lat = lon.astype(np.float32), lat.astype(np.float32)
+    nl, lr, lw = oracle.locrad_table(3, radii, [[0.7, 0.3], [1.0], [1.0]])
+    qx = rng.uniform(float(lon.min()), float(lon.max()), 40)
+    qy = rng.uniform(float(lat.min()), float(lat.max()), 40)
+    qx[:6] = np.floor(qx[:6])
+    qx[7], qy[19] = np.nan, np.nan
+    visible = None if hidden is None else np.array([1 if t != hidden else 0 for t in range(3)])
+    ref = oracle.ref_findlocal(lon, lat, otype, status, 3, nl, lr, lw, qx, qy, nlobsmax=nlobsmax, visible=visible,
+                               geographic=geographic)
+    st = status.copy()
+    if hidden is not None:
+        st[otype == hidden] = 1
+    obs = oracle.ObsSet(lon, lat, otype, st, 3, nl, lr, lw, nlobsmax=None if nlobsmax is None else np.array(nlobsmax),
+                        geographic=geographic)
+    for k in range(qx.size):
+        ids, lc = obs.findlocal(qx[k], qy[k])
+        assert np.array_equal(ids, ref[k][0]), k
+        assert np.array_equal(lc, ref[k][1]), k
+    assert ref[7][0].size == (st == 0).sum() and np.all(ref[7][1] == 1.0)
+
+
 @pytest.mark.skipif(oracle.reflib_ensobs() is None, reason="reference library not built here")
 @pytest.mark.parametrize("m,n", [(24, 3000), (96, 5000), (7, 40)])
 def test_innovations_and_standardise_equal_reference_build(m, n):
