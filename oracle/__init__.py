@@ -167,6 +167,8 @@ class ObsSet:
                                  _p(self.nlocrad, C.c_int), _p(self.locrad, C.c_double),
                                  _p(self.locweight, C.c_double), _p(nlm, C.c_int), C.c_int(int(geographic)))
         self.nobs = self.lon.size
+        self.geographic = bool(geographic)
+        self.nlobsmax = nlm
 
     def __del__(self):
         try:
@@ -678,6 +680,69 @@ def ref_findlocal(lon, lat, otype, status, ntypes, nlocrad, locrad, locweight, q
         out.append((ids[k0:k0 + c].copy(), lc[k0:k0 + c].copy()))
         k0 += c
     return out
+
+
+REFLIB_TRANSFORMS = os.path.join(HERE, "_ref", "libenkf_ref_transforms.so")
+_reftr = None
+
+
+def reflib_transforms():
+    """libenkf_ref_transforms.so (the reference's das_calctransforms), or
+    None where it is not built."""
+    global _reftr
+    with _lock:
+        if _reftr is None and os.path.exists(REFLIB_TRANSFORMS):
+            L = C.CDLL(REFLIB_TRANSFORMS)
+            if L.or_blas_load(blas_path().encode()) != 0:
+                return None
+            L.ref_calctransforms.argtypes = [C.c_int, C.c_int, C.c_double, C.c_int, C.c_int, C.c_int] + \
+                [C.c_void_p] * 6 + [C.c_int, C.c_int] + [C.c_void_p] * 5 + [C.c_int, C.c_int, C.c_int] + \
+                [C.c_void_p] * 2 + [C.c_int] + [C.c_void_p] * 8
+            _reftr = L
+    return _reftr
+
+
+def ref_calctransforms(obs, *, mode, scheme, nmem, nmem_dynamic, alpha, stride, x, y, S, s, nlobsmax=None,
+                       visible=None):
+    """das_calctransforms of the reference itself on the rectangular grid
+    (x, y) for the observation set `obs` (an ObsSet: positions, types,
+    statuses, radii, weights, geographic flag), with S and s standardised.
+    Returns the float outputs as the reference writes them: T (ENKF and
+    HYBRID), w, nlobs, dfs, srf, pnlobs, pdfs, psrf."""
+    L = reflib_transforms()
+    if L is None:
+        raise RuntimeError("reference transforms library not built")
+    x = np.ascontiguousarray(x, np.float64)
+    y = np.ascontiguousarray(y, np.float64)
+    mni, mnj = x.size, y.size
+    nj, ni = (mnj - 1) // stride + 1, (mni - 1) // stride + 1
+    m, md, nt = nmem, nmem_dynamic, obs.ntypes
+    S = np.ascontiguousarray(S, np.float32).copy()
+    s = np.ascontiguousarray(s, np.float64).copy()
+    T = np.zeros((nj, ni, md, m), np.float32)
+    w = np.zeros((nj, ni, m), np.float32)
+    nlobs = np.zeros((nj, ni), np.int32)
+    dfs = np.zeros((nj, ni), np.float32)
+    srf = np.zeros((nj, ni), np.float32)
+    pn = np.zeros((nt, nj, ni), np.int32)
+    pd = np.zeros((nt, nj, ni), np.float32)
+    ps = np.zeros((nt, nj, ni), np.float32)
+    lr = np.ascontiguousarray(obs.locrad, np.float64).reshape(nt, -1)
+    lw = np.ascontiguousarray(obs.locweight, np.float64).reshape(nt, -1)
+    if nlobsmax is None:
+        nlobsmax = obs.nlobsmax
+    nm = None if nlobsmax is None else np.ascontiguousarray(nlobsmax, np.int32)
+    vis = None if visible is None else np.ascontiguousarray(visible, np.int32)
+    # this library's mode codes (0 ENKF, 1 ENOI, 2 HYBRID) and scheme codes
+    # (0 DEnKF, 1 ETKF) -> the reference's (common/global.h:64-72)
+    L.ref_calctransforms(int(mode) + 1, int(scheme) + 1, float(alpha), m, md, obs.nobs, obs.lon.ctypes.data,
+                         obs.lat.ctypes.data, obs.otype.ctypes.data, obs.status.ctypes.data, S.ctypes.data,
+                         s.ctypes.data, nt, lr.shape[1], obs.nlocrad.ctypes.data, lr.ctypes.data, lw.ctypes.data,
+                         None if nm is None else nm.ctypes.data, None if vis is None else vis.ctypes.data,
+                         int(obs.geographic), mni, mnj, x.ctypes.data, y.ctypes.data, int(stride), T.ctypes.data,
+                         w.ctypes.data, nlobs.ctypes.data, dfs.ctypes.data, srf.ctypes.data, pn.ctypes.data,
+                         pd.ctypes.data, ps.ctypes.data)
+    return dict(T=T if mode != 1 else None, w=w, nlobs=nlobs, dfs=dfs, srf=srf, pnlobs=pn, pdfs=pd, psrf=ps)
 
 
 REFLIB_UPDATE = os.path.join(HERE, "_ref", "libenkf_ref_update.so")

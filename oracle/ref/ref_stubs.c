@@ -7,8 +7,8 @@
  *
  * Provides the few utilities those two files link against (enkf_quit,
  * alloc2d, cast2d, seed_rand48: reference common/utils.c) written here from
- * their documented behaviour, the LAPACK wrappers named by shim.h, and flat
- * entry points convenient for ctypes.
+ * their documented behaviour, and flat entry points convenient for ctypes
+ * (the LAPACK wrappers named by shim.h are in ref_blas.c).
  */
 #define _GNU_SOURCE
 #include <stdarg.h>
@@ -53,45 +53,6 @@ void* cast2d(void* p, size_t nj, size_t ni, size_t unitsize)
     return pp;
 }
 
-int orref_dgemm_(char* ta, char* tb, int* m, int* n, int* k, double* a, double* A, int* lda, double* B, int* ldb, double* b, double* C, int* ldc)
-{
-    or_dgemm(*ta, *tb, *m, *n, *k, *a, A, *lda, B, *ldb, *b, C, *ldc);
-    return 0;
-}
-
-int orref_dgemv_(char* t, int* m, int* n, double* a, double* A, int* lda, double* x, int* incx, double* b, double* y, int* incy)
-{
-    (void) incx;
-    (void) incy;
-    or_dgemv(*t, *m, *n, *a, A, *lda, x, *b, y);
-    return 0;
-}
-
-int orref_sgemv_(char* t, int* m, int* n, float* a, float* A, int* lda, float* x, int* incx, float* b, float* y, int* incy)
-{
-    (void) incx;
-    (void) incy;
-    or_sgemv(*t, *m, *n, *a, A, *lda, x, *b, y);
-    return 0;
-}
-
-int orref_dpotrf_(char* uplo, int* n, double* A, int* lda, int* info)
-{
-    *info = or_dpotrf(*uplo, *n, A, *lda);
-    return 0;
-}
-
-int orref_dpotri_(char* uplo, int* n, double* A, int* lda, int* info)
-{
-    *info = or_dpotri(*uplo, *n, A, *lda);
-    return 0;
-}
-
-int orref_dgesvd_(char* ju, char* jv, int* m, int* n, double* A, int* lda, double* S, double* U, int* ldu, double* VT, int* ldvt, double* work, int* lwork, int* info)
-{
-    *info = or_dgesvd(*ju, *jv, *m, *n, A, *lda, S, U, *ldu, VT, *ldvt, work, *lwork);
-    return 0;
-}
 
 /* --- the reference API (calc/calcs.h, common/kdtree.h) ------------------- */
 void calc_G(int m, int p, double** Min, double** S, double** G);

@@ -28,6 +28,11 @@ GPU library without needing the reference at test time:
                   observations (ENKF DEnKF and ETKF, EnOI; alpha 0.7), with
                   the diagnostics dfs, srf and per-type pdfs, psrf through
                   the reference's traceprod.
+  calctransforms.npz
+                  das_calctransforms itself (calc/transforms.c and the
+                  files it calls, compiled unmodified, the grid and the
+                  output files in memory): the float T, w and diagnostics of
+                  a two-type workload at stride 3, ETKF (alpha 0.7) and DEnKF.
   model2obs.npz   interpolate2d_structured / interpolate3d_structured
                   (common/utils.c, from oracle/_ref/libenkf_ref_utils.so) on
                   seeded fields, wet-level counts, OFFSET data and positions
@@ -305,6 +310,31 @@ def transforms_multitype():
     print("transforms_multitype:", pts.size, "points")
 
 
+def calctransforms():
+    """das_calctransforms of the reference itself (calc/transforms.c with
+    calcs.c, observations.c, obstypes.c, kdtree.c, compiled unmodified; grid
+    and output files in memory) on a two-type workload with rejected
+    observations at stride 3: the float T, w and diagnostics it writes, for
+    ETKF with alpha 0.7 and for DEnKF.  S and s are stored standardised."""
+    w = synth.make(2, scale=0.1, nobs=6000, with_fields=False, nmem=20)
+    st = w.status.copy()
+    st[::23] = 1
+    S, s_f, _ = oracle.calcinnandspread(w.HE, w.value, st)
+    S, s = oracle.standardise(S, s_f, w.estd, w.otype, np.ones(w.ntypes))
+    nl, lr, lw = oracle.locrad_table(w.ntypes, 12.0)
+    obs = oracle.ObsSet(w.lon, w.lat, w.otype, st, w.ntypes, nl, lr, lw)
+    out = dict(lon=w.lon, lat=w.lat, otype=w.otype, status=st, S=S, s=s, x=w.x, y=w.y, locrad=np.array(12.0),
+               stride=np.array(w.stride), nmem=np.array(w.nmem))
+    for mode, scheme, alpha, name in ((0, 1, 0.7, "etkf"), (0, 0, 1.0, "denkf")):
+        r = oracle.ref_calctransforms(obs, mode=mode, scheme=scheme, nmem=w.nmem, nmem_dynamic=w.nmem, alpha=alpha,
+                                      stride=w.stride, x=w.x, y=w.y, S=S, s=s)
+        out[f"{name}_alpha"] = np.array(alpha)
+        for k in ("T", "w", "nlobs", "dfs", "srf", "pnlobs", "pdfs", "psrf"):
+            out[f"{name}_{k}"] = r[k]
+    np.savez_compressed(os.path.join(HERE, "calctransforms.npz"), **out)
+    print("calctransforms:", w.nj_s * w.ni_s, "points")
+
+
 def model2obs():
     rng = np.random.default_rng(20250)
     ni, nj, nk, m, n = 23, 17, 5, 3, 600
@@ -465,11 +495,12 @@ def addnoise():
 
 if __name__ == "__main__":
     oracle.build()
-    if oracle.reflib() is None or oracle.reflib_utils() is None or oracle.reflib_update() is None:
+    if (oracle.reflib() is None or oracle.reflib_utils() is None or oracle.reflib_update() is None
+            or oracle.reflib_transforms() is None):
         sys.exit("the reference libraries under oracle/_ref could not be built")
-    which = sys.argv[1:] or ["numerics", "kdtree", "nlobsmax", "transforms", "transforms_multitype", "model2obs",
-                             "update", "addnoise"]
+    which = sys.argv[1:] or ["numerics", "kdtree", "nlobsmax", "transforms", "transforms_multitype", "calctransforms",
+                             "model2obs", "update", "addnoise"]
     for name in which:
         {"numerics": numerics, "kdtree": kdtree, "nlobsmax": nlobsmax, "transforms": transforms,
-         "transforms_multitype": transforms_multitype, "model2obs": model2obs, "update": update,
-         "addnoise": addnoise}[name]()
+         "transforms_multitype": transforms_multitype, "calctransforms": calctransforms, "model2obs": model2obs,
+         "update": update, "addnoise": addnoise}[name]()

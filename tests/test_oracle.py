@@ -385,6 +385,86 @@ def test_traceprod_equals_reference_build():
         assert R.traceprod(0, 1, m, q, sr, sr, 0) == L.or_traceprod(0, 1, m, q, cS.ctypes.data, cS.ctypes.data)
 
 
+@pytest.mark.parametrize("name,mode,scheme", [("etkf", 0, 1), ("denkf", 0, 0)])
+def test_calctransforms_against_reference_golden(name, mode, scheme):
+    """The oracle's transform stage against the float outputs of the
+    reference's own das_calctransforms (tests/golden/calctransforms.npz),
+    bit for bit."""
+    g = np.load(os.path.join(GOLD, "calctransforms.npz"))
+    nt = int(g["otype"].max()) + 1
+    nl, lr, lw = oracle.locrad_table(nt, float(g["locrad"]))
+    obs = oracle.ObsSet(g["lon"], g["lat"], g["otype"], g["status"], nt, nl, lr, lw)
+    m = int(g["nmem"])
+    out = oracle.calctransforms(obs, mode=mode, scheme=scheme, nmem=m, nmem_dynamic=m, alpha=float(g[f"{name}_alpha"]),
+                                stride=int(g["stride"]), x=g["x"], y=g["y"], S=g["S"], s=g["s"], threads=8)
+    for k in ("T", "w", "nlobs", "dfs", "srf", "pnlobs", "pdfs", "psrf"):
+        assert np.array_equal(out[k], g[f"{name}_{k}"]), (name, k)
+
+
+# (name, workload, scale, nmem, nmem_dynamic, mode, scheme, alpha, options)
+TRANSFORM_CASES = [
+    ("w1_etkf", 1, 1.0, 24, 24, 0, 1, 1.0, {}),
+    ("w1_denkf_alpha", 1, 0.5, 24, 24, 0, 0, 0.7, {}),
+    ("w2_denkf_stride3", 2, 0.1, 20, 20, 0, 0, 1.0, {}),
+    ("w2_etkf_alpha", 2, 0.1, 20, 20, 0, 1, 0.7, {}),
+    ("w2_enoi", 2, 0.1, 20, 20, 1, 0, 1.0, {}),
+    ("w2_hybrid_etkf", 2, 0.1, 24, 16, 2, 1, 0.8, {}),
+    ("w2_etkf_nlobsmax_hidden", 2, 0.1, 20, 20, 0, 1, 1.0, dict(nlobsmax=(25, 10), visible=(1, 0))),
+    ("w2_denkf_geographic", 2, 0.1, 20, 20, 0, 0, 1.0, dict(geographic=True)),
+]
+
+
+@pytest.mark.skipif(oracle.reflib_transforms() is None, reason="reference library not built here")
+@pytest.mark.parametrize("case", TRANSFORM_CASES, ids=[c[0] for c in TRANSFORM_CASES])
+def test_calctransforms_equals_reference_build(case):
+    """das_calctransforms (calc/transforms.c:991-1637, compiled unmodified
+    with calcs.c, observations.c, obstypes.c and kdtree.c; the model grid and
+    the output files in memory): the oracle's T, w and diagnostics -- nlobs,
+    dfs, srf and per type pnlobs, pdfs, psrf, as the reference writes them in
+    float -- equal the reference's bit for bit over the whole strided grid:
+    ETKF, DEnKF, EnOI and hybrid, relaxation, one and two observation types
+    with rejected observations and points without local observations,
+    NLOBSMAX with a type hidden by its domains, and GEOGRAPHIC 1."""
+    import synth
+    from helpers import prepare
+    name, cfg, scale, m, md, mode, scheme, alpha, opt = case
+    kw = dict(nobs=6000) if cfg == 2 else {}
+    w = synth.make(cfg, scale=scale, nmem=m, with_fields=False, **kw)
+    w.nmem_dynamic = md
+    st = w.status.copy()
+    st[::23] = 1
+    w.status = st
+    x, y, radius = w.x, w.y, (12.0 if cfg == 2 else w.locrad)
+    geo = opt.get("geographic", False)
+    if geo:
+        sx, sy = 60.0 / (w.x.size - 1), 60.0 / (w.y.size - 1)
+        w.lon = (100.0 + w.lon * sx).astype(np.float32)
+        w.lat = (-30.0 + w.lat * sy).astype(np.float32)
+        x, y, radius = 100.0 + w.x * sx, -30.0 + w.y * sy, 400.0
+    S, s = prepare(w)
+    nl, lr, lw = oracle.locrad_table(w.ntypes, radius)
+    vis = opt.get("visible")
+    st_o = st.copy()
+    if vis is not None:
+        for t, v in enumerate(vis):
+            if not v:
+                st_o[w.otype == t] = 1
+    nm = opt.get("nlobsmax")
+    obs_o = oracle.ObsSet(w.lon, w.lat, w.otype, st_o, w.ntypes, nl, lr, lw,
+                          nlobsmax=None if nm is None else np.array(nm), geographic=geo)
+    obs_r = oracle.ObsSet(w.lon, w.lat, w.otype, st, w.ntypes, nl, lr, lw,
+                          nlobsmax=None if nm is None else np.array(nm), geographic=geo)
+    out = oracle.calctransforms(obs_o, mode=mode, scheme=scheme, nmem=m, nmem_dynamic=md, alpha=alpha,
+                                stride=w.stride, x=x, y=y, S=S, s=s, threads=8)
+    ref = oracle.ref_calctransforms(obs_r, mode=mode, scheme=scheme, nmem=m, nmem_dynamic=md, alpha=alpha,
+                                    stride=w.stride, x=x, y=y, S=S, s=s, visible=vis)
+    assert (ref["nlobs"] == 0).any() or cfg == 1
+    for k in ("T", "w", "nlobs", "dfs", "srf", "pnlobs", "pdfs", "psrf"):
+        if ref[k] is None:
+            continue
+        assert np.array_equal(out[k], ref[k]), (name, k)
+
+
 @pytest.mark.skipif(oracle.reflib_obs() is None, reason="reference library not built here")
 @pytest.mark.parametrize("geographic", [False, True])
 @pytest.mark.parametrize("nlobsmax", [None, (9, 4, 30)])
