@@ -745,6 +745,47 @@ def ref_calctransforms(obs, *, mode, scheme, nmem, nmem_dynamic, alpha, stride, 
     return dict(T=T if mode != 1 else None, w=w, nlobs=nlobs, dfs=dfs, srf=srf, pnlobs=pn, pdfs=pd, psrf=ps)
 
 
+REFLIB_MODEL2OBS = os.path.join(HERE, "_ref", "libenkf_ref_model2obs.so")
+_refmo = None
+
+
+def reflib_model2obs():
+    """libenkf_ref_model2obs.so (the reference's H_surf_standard and
+    H_subsurf_standard), or None where it is not built."""
+    global _refmo
+    with _lock:
+        if _refmo is None and os.path.exists(REFLIB_MODEL2OBS):
+            L = C.CDLL(REFLIB_MODEL2OBS)
+            L.ref_H.argtypes = [C.c_int] * 6 + [C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_int, C.c_int] + \
+                [C.c_void_p] * 4 + [C.c_int, C.c_void_p]
+            _refmo = L
+    return _refmo
+
+
+def ref_H(field3, numlevels, ids, fi, fj, fk=None, *, three_d, ksurf, periodic_i=0, offset=None, offset_kind=0,
+          skip_bad=True):
+    """H_surf_standard (three_d False: layer ksurf of field3) or
+    H_subsurf_standard of the reference itself for one member; field3 is
+    [nk][nj][ni].  Returns dst [nobs] (NaN where not computed)."""
+    L = reflib_model2obs()
+    if L is None:
+        raise RuntimeError("reference model2obs library not built")
+    f = np.ascontiguousarray(field3, np.float32)
+    nk, nj, ni = f.shape
+    nl = np.ascontiguousarray(numlevels, np.int32).copy()
+    ids = np.ascontiguousarray(ids, np.int32)
+    fi = np.ascontiguousarray(fi, np.float64)
+    fj = np.ascontiguousarray(fj, np.float64)
+    fkk = np.ascontiguousarray(fk if fk is not None else np.zeros(fi.size), np.float32)
+    off = None if offset is None else np.ascontiguousarray(offset, np.float32)
+    dst = np.zeros(fi.size, np.float32)
+    L.ref_H(int(three_d), ni, nj, nk, int(ksurf), int(periodic_i), nl.ctypes.data,
+            None if off is None else off.ctypes.data, int(offset_kind) if off is not None else 0, f.ctypes.data,
+            fi.size, ids.size, ids.ctypes.data, fi.ctypes.data, fj.ctypes.data, fkk.ctypes.data, int(skip_bad),
+            dst.ctypes.data)
+    return dst
+
+
 REFLIB_UPDATE = os.path.join(HERE, "_ref", "libenkf_ref_update.so")
 _refup = None
 

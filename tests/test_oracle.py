@@ -512,6 +512,47 @@ def test_findlocal_equals_reference_build(geographic, nlobsmax, hidden):
     assert ref[7][0].size == (st == 0).sum() and np.all(ref[7][1] == 1.0)
 
 
+@pytest.mark.skipif(oracle.reflib_model2obs() is None, reason="reference library not built here")
+@pytest.mark.parametrize("three_d", [False, True])
+def test_forward_operators_equal_reference_build(three_d):
+    """H_surf_standard and H_subsurf_standard (calc/model2obs.c, compiled
+    unmodified; the model variable, grid and observations in memory): the
+    oracle's HE equals the reference's bit for bit -- both surface-layer
+    conventions, periodic i, OFFSET data of every shape the function takes,
+    positions on grid lines, and bad forecasts (NaN under
+    --skip-bad-forecast-obs)."""
+    rng = np.random.default_rng(5 + int(three_d))
+    ni, nj, nk = 23, 17, 5
+    nl = rng.integers(0, nk + 1, (nj, ni)).astype(np.int32)
+    nl[rng.random((nj, ni)) < 0.5] = nk
+    f3 = rng.normal(10.0, 2.0, (nk, nj, ni)).astype(np.float32)
+    f3[0, 3, 4] = np.nan
+    f3[nk - 1, 5, 6] = 2.0e6
+    n = 400
+    fi = rng.uniform(0, ni - 1, n)
+    fj = rng.uniform(0, nj - 1, n)
+    fk = rng.uniform(0, nk - 1, n).astype(np.float32)
+    fi[:20] = np.floor(fi[:20])
+    fj[20:40] = np.floor(fj[20:40])
+    fi[40:44], fj[40:44] = [3.5, 4.0, 6.2, 5.5], [2.5, 3.0, 4.7, 5.0]
+    ids = np.arange(n, dtype=np.int32)
+    kinds = [0, 1, 2, 3] if three_d else [0, 2]
+    for ksurf in (0, nk - 1):
+        for per in (0, 1):
+            for ok in kinds:
+                off = None
+                if ok:
+                    shape = {1: (nk,), 2: (nj, ni), 3: (nk, nj, ni)}[ok]
+                    off = rng.normal(0.0, 1.0, shape).astype(np.float32)
+                ref = oracle.ref_H(f3, nl, ids, fi, fj, fk, three_d=three_d, ksurf=ksurf, periodic_i=per, offset=off,
+                                   offset_kind=ok)
+                HE = np.full((1, n), np.nan, np.float32)
+                rc = oracle.map_obs(HE, 0, f3 if three_d else f3[ksurf], nl, ids, fi, fj, fk, three_d=three_d,
+                                    ktop=ksurf, periodic_i=per, offset=off, offset_kind=ok, skip_bad=True)
+                assert rc == 0
+                assert np.array_equal(HE[0], ref, equal_nan=True), (ksurf, per, ok)
+
+
 @pytest.mark.skipif(oracle.reflib_ensobs() is None, reason="reference library not built here")
 @pytest.mark.parametrize("m,n", [(24, 3000), (96, 5000), (7, 40)])
 def test_innovations_and_standardise_equal_reference_build(m, n):
