@@ -786,6 +786,50 @@ def ref_H(field3, numlevels, ids, fi, fj, fk=None, *, three_d, ksurf, periodic_i
     return dst
 
 
+REFLIB_GETHE = os.path.join(HERE, "_ref", "libenkf_ref_gethe.so")
+_refge = None
+
+
+def reflib_gethe():
+    """libenkf_ref_gethe.so (the reference's das_getHE), or None where it is
+    not built."""
+    global _refge
+    with _lock:
+        if _refge is None and os.path.exists(REFLIB_GETHE):
+            L = C.CDLL(REFLIB_GETHE)
+            L.ref_getHE.argtypes = [C.c_int, C.c_int, C.c_int, C.c_double, C.c_int] + [C.c_int] * 5 + \
+                [C.c_void_p, C.c_void_p, C.c_int] + [C.c_void_p] * 5 + [C.c_int, C.c_void_p, C.c_void_p]
+            _refge = L
+    return _refge
+
+
+def ref_getHE(members, numlevels, otype, status, fi, fj, fk, issurface, *, mode, nmem_dynamic, gamma=0.0, ksurf=0,
+              periodic_i=0, skip_bad=True):
+    """das_getHE of the reference itself: members [nmem (+1: the EnOI
+    background)][nk][nj][ni] of one variable; observation types with
+    issurface[t] (H_surf_standard, else H_subsurf_standard).  mode: this
+    library's codes (0 ENKF, 1 ENOI, 2 HYBRID).  Returns (HE [rows][nobs],
+    statuses)."""
+    L = reflib_gethe()
+    if L is None:
+        raise RuntimeError("reference das_getHE library not built")
+    f = np.ascontiguousarray(members, np.float32)
+    rows, nk, nj, ni = f.shape
+    nmem = rows - 1 if mode == 1 else rows
+    nl = np.ascontiguousarray(numlevels, np.int32).copy()
+    ot = np.ascontiguousarray(otype, np.int16)
+    st = np.ascontiguousarray(status, np.int16).copy()
+    fi = np.ascontiguousarray(fi, np.float64)
+    fj = np.ascontiguousarray(fj, np.float64)
+    fk = np.ascontiguousarray(fk, np.float32)
+    iss = np.ascontiguousarray(issurface, np.int32)
+    HE = np.zeros((rows, ot.size), np.float32)
+    L.ref_getHE(int(mode) + 1, nmem, int(nmem_dynamic), float(gamma), int(skip_bad), ni, nj, nk, int(ksurf),
+                int(periodic_i), nl.ctypes.data, f.ctypes.data, ot.size, ot.ctypes.data, st.ctypes.data,
+                fi.ctypes.data, fj.ctypes.data, fk.ctypes.data, iss.size, iss.ctypes.data, HE.ctypes.data)
+    return HE, st
+
+
 REFLIB_UPDATE = os.path.join(HERE, "_ref", "libenkf_ref_update.so")
 _refup = None
 

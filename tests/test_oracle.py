@@ -553,6 +553,49 @@ def test_forward_operators_equal_reference_build(three_d):
                 assert np.array_equal(HE[0], ref, equal_nan=True), (ksurf, per, ok)
 
 
+@pytest.mark.skipif(oracle.reflib_gethe() is None, reason="reference library not built here")
+@pytest.mark.parametrize("mode,m,md,gamma", [(0, 6, 6, 0.0), (1, 6, 6, 0.0), (2, 8, 5, 0.5)])
+def test_he_stage_equals_reference_build(mode, m, md, gamma):
+    """das_getHE (calc/ensobs.c:46-490 with calc/model2obs.c, calc/allhs.c and
+    the observation module, compiled unmodified; members, grid and
+    observations in memory): the oracle's per-type forward operators for
+    every member (and the EnOI background) followed by its restatement of
+    the end of das_getHE give the reference's HE and statuses bit for bit --
+    ENKF, EnOI and hybrid, a surface and a subsurface type, both
+    surface-layer conventions, rejected observations and a bad forecast
+    under --skip-bad-forecast-obs."""
+    rng = np.random.default_rng(17 + mode)
+    ni, nj, nk = 23, 17, 5
+    nl = rng.integers(0, nk + 1, (nj, ni)).astype(np.int32)
+    nl[rng.random((nj, ni)) < 0.5] = nk
+    n = 300
+    fi = rng.uniform(0, ni - 1, n)
+    fj = rng.uniform(0, nj - 1, n)
+    fk = rng.uniform(0, nk - 1, n).astype(np.float32)
+    otype = rng.integers(0, 2, n).astype(np.int16)
+    status = np.zeros(n, np.int16)
+    status[::13] = 1
+    issurface = np.array([1, 0])
+    rows = m + 1 if mode == 1 else m
+    mem = rng.normal(10.0, 2.0, (rows, nk, nj, ni)).astype(np.float32)
+    mem[2, 0, 4, 5] = np.nan
+    for ksurf in (0, nk - 1):
+        HEr, st_r = oracle.ref_getHE(mem, nl, otype, status, fi, fj, fk, issurface, mode=mode, nmem_dynamic=md,
+                                     gamma=gamma, ksurf=ksurf)
+        HE = np.full((rows, n), np.nan, np.float32)
+        for e in range(rows):
+            for t in range(2):
+                ids = np.nonzero((otype == t) & (status == 0))[0].astype(np.int32)
+                three = not issurface[t]
+                assert oracle.map_obs(HE, e, mem[e] if three else mem[e][ksurf], nl, ids, fi, fj, fk, three_d=three,
+                                      ktop=ksurf, skip_bad=True) == 0
+        S, st, nbad = oracle.finish_HE(HE[:m], status, mode=mode, nmem_dynamic=md, gamma=gamma,
+                                       Hx=HE[m] if mode == 1 else None, skip_bad=True)
+        assert np.array_equal(S, HEr[:m], equal_nan=True), ksurf
+        assert np.array_equal(st, st_r), ksurf
+        assert nbad == (st_r == 10).sum() > 0
+
+
 @pytest.mark.skipif(oracle.reflib_ensobs() is None, reason="reference library not built here")
 @pytest.mark.parametrize("m,n", [(24, 3000), (96, 5000), (7, 40)])
 def test_innovations_and_standardise_equal_reference_build(m, n):
