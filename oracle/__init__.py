@@ -695,6 +695,8 @@ def reflib_transforms():
             L = C.CDLL(REFLIB_TRANSFORMS)
             if L.or_blas_load(blas_path().encode()) != 0:
                 return None
+            L.ref_calcpointlogtransforms.argtypes = [C.c_int, C.c_int, C.c_double, C.c_int, C.c_int, C.c_int] + \
+                [C.c_void_p] * 6 + [C.c_int, C.c_int] + [C.c_void_p] * 4 + [C.c_int, C.c_int] + [C.c_void_p] * 4
             L.ref_calctransforms.argtypes = [C.c_int, C.c_int, C.c_double, C.c_int, C.c_int, C.c_int] + \
                 [C.c_void_p] * 6 + [C.c_int, C.c_int] + [C.c_void_p] * 5 + [C.c_int, C.c_int, C.c_int] + \
                 [C.c_void_p] * 2 + [C.c_int] + [C.c_void_p] * 8
@@ -828,6 +830,32 @@ def ref_getHE(members, numlevels, otype, status, fi, fj, fk, issurface, *, mode,
                 int(periodic_i), nl.ctypes.data, f.ctypes.data, ot.size, ot.ctypes.data, st.ctypes.data,
                 fi.ctypes.data, fj.ctypes.data, fk.ctypes.data, iss.size, iss.ctypes.data, HE.ctypes.data)
     return HE, st
+
+
+def ref_calcpointlogtransforms(obs, *, mode, scheme, nmem, nmem_dynamic, alpha, plon, plat, S, s):
+    """das_calcpointlogtransforms of the reference itself at the log points
+    (plon, plat): the double T [npl][nmem][nmem] (ENKF, HYBRID; None for
+    EnOI) and w [npl][nmem] it hands to the point-log writer."""
+    L = reflib_transforms()
+    if L is None:
+        raise RuntimeError("reference transforms library not built")
+    m, nt = nmem, obs.ntypes
+    px = np.ascontiguousarray(plon, np.float64)
+    py = np.ascontiguousarray(plat, np.float64)
+    S = np.ascontiguousarray(S, np.float32).copy()
+    s = np.ascontiguousarray(s, np.float64).copy()
+    T = np.zeros((px.size, m, m)) if mode != 1 else None
+    w = np.zeros((px.size, m))
+    lr = np.ascontiguousarray(obs.locrad, np.float64).reshape(nt, -1)
+    lw = np.ascontiguousarray(obs.locweight, np.float64).reshape(nt, -1)
+    nm = obs.nlobsmax
+    L.ref_calcpointlogtransforms(int(mode) + 1, int(scheme) + 1, float(alpha), m, int(nmem_dynamic), obs.nobs,
+                                 obs.lon.ctypes.data, obs.lat.ctypes.data, obs.otype.ctypes.data,
+                                 obs.status.ctypes.data, S.ctypes.data, s.ctypes.data, nt, lr.shape[1],
+                                 obs.nlocrad.ctypes.data, lr.ctypes.data, lw.ctypes.data,
+                                 None if nm is None else nm.ctypes.data, int(obs.geographic), px.size,
+                                 px.ctypes.data, py.ctypes.data, None if T is None else T.ctypes.data, w.ctypes.data)
+    return T, w
 
 
 REFLIB_UPDATE = os.path.join(HERE, "_ref", "libenkf_ref_update.so")

@@ -25,6 +25,7 @@
 #include "utils.h"
 #include "observations.h"
 #include "dasystem.h"
+#include "pointlog.h"
 
 observations* orref_obs_build(int nobs, const float* lon, const float* lat, const short* type, const short* status,
                               const float* value, const float* estd, int ntypes, int maxlocrad, const int* nlocrad,
@@ -34,6 +35,8 @@ void orref_obs_free(observations* obs);
 void orref_tio_set(int mni, int mnj, const double* x, const double* y, int stride, int geographic, int nj, int ni,
                    int md, int m, int ntypes, float* T, float* w, int* nlobs, float* dfs, float* srf, int* pnlobs,
                    float* pdfs, float* psrf);
+
+void orref_plog_set(int nmem, double* T, double* w);
 
 /* das_standardise (calc/ensobs.c:849-898) is pinned separately; the data
  * come in standardised */
@@ -85,6 +88,59 @@ int ref_calctransforms(int mode, int scheme, double alpha, int nmem, int nmem_dy
     das.m = (model*) &das;      /* any non-NULL handle: the model stand-ins ignore it */
     enkf_verbose = 0;
     das_calctransforms(&das);
+    free(rows);
+    orref_obs_free(obs);
+    return 0;
+}
+
+/*
+ * das_calcpointlogtransforms (calc/transforms.c:1646-1773) at npl log points
+ * (plon, plat) on the one model grid (geographic as given): the double T
+ * [npl][nmem][nmem] (ENKF and HYBRID) and w [npl][nmem] it hands to the
+ * point-log writer, after the relaxation and before any float cast.
+ */
+int ref_calcpointlogtransforms(int mode, int scheme, double alpha, int nmem, int nmem_dynamic, int nobs,
+                               const float* lon, const float* lat, const short* type, const short* status, float* S,
+                               double* s, int ntypes, int maxlocrad, const int* nlocrad, const double* locrad,
+                               const double* locweight, const int* nlobsmax, int geographic, int npl,
+                               const double* plon, const double* plat, double* T, double* w)
+{
+    dasystem das;
+    observations* obs = orref_obs_build(nobs, lon, lat, type, status, NULL, NULL, ntypes, maxlocrad, nlocrad, locrad,
+                                        locweight, nlobsmax, NULL, geographic, NULL);
+    float** rows = malloc((nmem > 0 ? nmem : 1) * sizeof(float*));
+    pointlog* plogs = calloc(npl > 0 ? npl : 1, sizeof(pointlog));
+    static const double x0 = 0.0;
+    int e, k;
+
+    orref_tio_set(1, 1, &x0, &x0, 1, geographic, 1, 1, nmem_dynamic, nmem, ntypes, NULL, NULL, NULL, NULL, NULL,
+                  NULL, NULL, NULL);
+    orref_plog_set(nmem, T, w);
+    for (k = 0; k < npl; ++k) {
+        plogs[k].id = k;
+        plogs[k].lon = plon[k];
+        plogs[k].lat = plat[k];
+        plogs[k].gridid = -1;
+    }
+    for (e = 0; e < nmem; ++e)
+        rows[e] = S + (size_t) e * nobs;
+    memset(&das, 0, sizeof(das));
+    das.mode = mode;
+    das.scheme = scheme;
+    das.alpha = alpha;
+    das.nmem = nmem;
+    das.nmem_dynamic = nmem_dynamic;
+    das.nmem_static = nmem - nmem_dynamic;
+    das.obs = obs;
+    das.S = rows;
+    das.s_f = s;
+    das.s_mode = S_MODE_S_f;
+    das.m = (model*) &das;
+    das.nplog = npl;
+    das.plogs = plogs;
+    enkf_verbose = 0;
+    das_calcpointlogtransforms(&das);
+    free(plogs);
     free(rows);
     orref_obs_free(obs);
     return 0;

@@ -9,7 +9,8 @@
  * distribution of all iterations to this one process, and the NetCDF
  * wrappers of the transforms and diagnostics files, whose variable writes
  * are copied into the arrays ref_calctransforms was given; and
- * kd_printinfo, a print.  Everything else
+ * kd_printinfo, a print; and the point-log writer, whose transforms are
+ * copied into the arrays ref_calcpointlogtransforms was given.  Everything else
  * the compiled files name (file input of observations and obstypes, point
  * logs) aborts if reached.
  */
@@ -207,11 +208,46 @@ void ncw_put_var_float(int ncid, int varid, const float v[])
         unreachable("ncw_put_var_float");
 }
 
+/* ---- the point-log writer: the transforms land in the caller's arrays ---- */
+static struct {
+    int nmem;
+    double* T;                  /* [nplog][nmem][nmem] or NULL */
+    double* w;                  /* [nplog][nmem] */
+} plo;
+
+void orref_plog_set(int nmem, double* T, double* w)
+{
+    plo.nmem = nmem;
+    plo.T = T;
+    plo.w = w;
+}
+
+void das_createplog(void* das, int plogid, int ploc, int* lobs, double* lcoeffs)
+{
+    (void) das;
+    (void) plogid;
+    (void) ploc;
+    (void) lobs;
+    (void) lcoeffs;
+}
+
+void das_writeplogtransform(void* das, int plogid, int gid, int ploc, double* s, double* S, double* w, double* T)
+{
+    const size_t m = (size_t) plo.nmem;
+
+    (void) das;
+    (void) gid;
+    (void) ploc;
+    (void) s;
+    (void) S;
+    memcpy(plo.w + (size_t) plogid * m, w, m * sizeof(double));
+    if (T != NULL && plo.T != NULL)
+        memcpy(plo.T + (size_t) plogid * m * m, T, m * m * sizeof(double));
+}
+
 /* ---- not reached by das_calctransforms ---- */
 #define UNREACHABLE(name) void name(void) { unreachable(#name); }
 
-UNREACHABLE(das_createplog)
-UNREACHABLE(das_writeplogtransform)
 UNREACHABLE(ncw_att_exists)
 UNREACHABLE(model_adddata)
 UNREACHABLE(model_getdomainid)

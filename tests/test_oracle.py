@@ -465,6 +465,34 @@ def test_calctransforms_equals_reference_build(case):
         assert np.array_equal(out[k], ref[k]), (name, k)
 
 
+@pytest.mark.skipif(oracle.reflib_transforms() is None, reason="reference library not built here")
+@pytest.mark.parametrize("mode,scheme", [(0, 1), (0, 0), (1, 0)])
+def test_pointlog_transforms_equal_reference_build(mode, scheme):
+    """das_calcpointlogtransforms (calc/transforms.c:1646-1773, compiled
+    unmodified; the point-log writer's arrays captured): the oracle at the
+    log points, taken as a 1 x n curvilinear grid -- the recipe the library
+    documents for point logs -- gives the reference's double T and w bit for
+    bit, including a log point with no local observation."""
+    import synth
+    from helpers import prepare, obsset
+    w = synth.make(1, scale=0.5, with_fields=False)
+    S, s = prepare(w)
+    obs, _ = obsset(w)
+    rng = np.random.default_rng(11)
+    n = 37
+    px = rng.uniform(w.x.min(), w.x.max(), n)
+    py = rng.uniform(w.y.min(), w.y.max(), n)
+    px[5], py[5] = w.x.max() + 10 * w.locrad, w.y.max() + 10 * w.locrad
+    Tr, wr = oracle.ref_calcpointlogtransforms(obs, mode=mode, scheme=scheme, nmem=w.nmem, nmem_dynamic=w.nmem,
+                                               alpha=0.7, plon=px, plat=py, S=S, s=s)
+    out = oracle.calctransforms(obs, mode=mode, scheme=scheme, nmem=w.nmem, nmem_dynamic=w.nmem, alpha=0.7, stride=1,
+                                x=px, y=py, S=S, s=s, want64=True, x2d=px[None, :], y2d=py[None, :])
+    assert np.array_equal(out["w64"][0], wr)
+    if mode != 1:
+        assert np.array_equal(out["T64"][0], Tr)
+    assert np.all(wr[5] == 0.0)
+
+
 @pytest.mark.skipif(oracle.reflib_obs() is None, reason="reference library not built here")
 @pytest.mark.parametrize("geographic", [False, True])
 @pytest.mark.parametrize("nlobsmax", [None, (9, 4, 30)])
