@@ -853,9 +853,11 @@ ENKFG_API enkfg_status enkfg_set_field_noise(enkfg_ctx* ctx, int nfield, int nme
             for (int e = 0; e < nmem; ++e) term[e] = 0.0;
             continue;
         }
-        if (!isfinite(d) || !isfinite(sigma[f])) {
+        // the reference's model parameters allow a deflation in [0, 1]
+        // (common/model.c:253-256)
+        if (!(d >= 0.0 && d <= 1.0) || !isfinite(sigma[f])) {
             free(h);
-            set_err(ctx, "field-layer %d: deflation %g, sigma %g", f, d, sigma[f]);
+            set_err(ctx, "field-layer %d: deflation %g (must be in [0, 1]), sigma %g", f, d, sigma[f]);
             return ENKFG_EINVAL;
         }
         const double* r = random + (size_t)f * nmem;

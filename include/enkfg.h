@@ -301,6 +301,8 @@ ENKFG_API enkfg_status enkfg_set_field_block_rows(enkfg_ctx* ctx, int rows);
  * normals the host draws for the field (get_normalpair, utils.c:1477-1484,
  * in the reference's order: (nmem + 1) / 2 pairs, the first nmem used).
  * The noise covers the rows the update call covers (its j1..j2 tile).
+ * A deflation outside [0, 1] or a non-finite sigma is refused (the
+ * reference's model parameter check, common/model.c:253-256).
  * nfield and nmem must be the next call's; ENOI updates take no noise.
  * nfield 0 or deflation NULL: none.  The next update call uses it up. */
 ENKFG_API enkfg_status enkfg_set_field_noise(enkfg_ctx* ctx, int nfield, int nmem, const double* deflation, const double* sigma, const double* random);
