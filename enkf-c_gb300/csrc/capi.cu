@@ -573,6 +573,21 @@ ENKFG_API enkfg_status enkfg_set_grid(enkfg_ctx* ctx, const enkfg_grid* g)
     NEED(g->mni >= 1 && g->mnj >= 1 && g->stride >= 1, ENKFG_EINVAL, "bad grid %d x %d stride %d", g->mni, g->mnj,
          g->stride);
     NEED((g->x && g->y) || (g->x2d && g->y2d), ENKFG_EINVAL, "grid coordinates are required");
+    // a point without coordinates (a grid of type NONE) takes every
+    // observation in the reference (obs_getglobal, observations.c:
+    // 1773-1817); the device search does not do that, so such grids are
+    // refused rather than given T = I
+    {
+        const int nj = (g->mnj - 1) / g->stride + 1, ni = (g->mni - 1) / g->stride + 1;
+        for (int j = 0; j < nj; ++j)
+            for (int i = 0; i < ni; ++i) {
+                const size_t jj = (size_t)j * g->stride, ii = (size_t)i * g->stride;
+                const double x = g->x2d ? g->x2d[jj * g->mni + ii] : g->x[ii];
+                const double y = g->x2d ? g->y2d[jj * g->mni + ii] : g->y[jj];
+                NEED(!isnan(x + y), ENKFG_EUNSUPPORTED,
+                     "grid point (%zu, %zu) has no coordinates (a grid of type NONE is not supported)", ii, jj);
+            }
+    }
     SETDEV();
     ctx->mni = g->mni;
     ctx->mnj = g->mnj;

@@ -183,7 +183,9 @@ ENKFG_API enkfg_status enkfg_get_S(enkfg_ctx* ctx, float* S, double* s);
 /* Model grid of the analysed variables (rectangular: x[mni], y[mnj];
  * curvilinear: x2d/y2d [mnj][mni], x/y NULL) with the transform stride and
  * the periodic-i flag (grid_getstride, grid_isperiodic_i; hgrid_ij2xy,
- * hgrid.c:457-472). */
+ * hgrid.c:457-472).  A strided point without coordinates (NaN: a grid of
+ * type NONE, where obs_findlocal takes every observation) is refused with
+ * ENKFG_EUNSUPPORTED. */
 typedef struct {
     int mni, mnj;
     const double* x;

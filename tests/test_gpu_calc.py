@@ -253,6 +253,12 @@ def test_errors_are_status_codes(ctx, gpu_lib):
     with pytest.raises(gpu_lib.EnkfgError) as e:
         c2.calctransforms()
     assert e.value.status == 7
+    # a strided point without coordinates (a grid of type NONE) is refused
+    nl, lr, lw = oracle.locrad_table(1, 5.0)
+    c2.set_obstypes(nl, lr, lw, np.ones(1))
+    with pytest.raises(gpu_lib.EnkfgError) as e:
+        c2.set_grid(x2d=np.array([[0.0, np.nan]]), y2d=np.array([[0.0, 1.0]]), stride=1)
+    assert e.value.status == 8
     c2.close()
 
 
