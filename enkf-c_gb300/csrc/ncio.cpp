@@ -849,10 +849,9 @@ static enkfg_status impl_write_transforms(const char* path, int nj, int ni, int 
         return fail(ENKFG_EINVAL, "bad transforms dimensions %d x %d, m_dyn %d, m %d", nj, ni, nmem_dynamic, nmem);
     NcFile nc = transforms_file(nj, ni, nmem_dynamic, nmem, T != nullptr, stride, grid_name);
     std::vector<FixedVar> data;
-    if (T)
-        data = { { T }, { w } };
-    else
-        data = { { w } };
+    data.reserve(2);
+    if (T) data.push_back(FixedVar{ T });
+    data.push_back(FixedVar{ w });
     return write_fixed(path, nc, data);
 }
 
